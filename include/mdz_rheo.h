@@ -1,0 +1,217 @@
+/*
+ * mdz_rheo.h -- C ABI of the GB300 local-rheology library (libmdz_rheo_gb300.so).
+ *
+ * The library evaluates MDOODZ7.0's per-node local rheology update on one
+ * GPU (sm_103a).  Every entry point takes plain pointers and sizes; no
+ * MDOODZ struct crosses this boundary, so the header is usable from C, C++,
+ * Python (ctypes) or any FFI.  The MDOODZ-side drop-in (the functions with the
+ * reference's own signatures, which unpack `grid`/`mat_prop`/`params`/`scale`
+ * into the structs below) lives in mdoodz7.0_gb300/host/mdz_rheo_mdoodz.c.
+ *
+ * Reference interfaces replaced (paths inside the MDOODZ7.0 tree):
+ *   mdz_rheo_sweep          <- NonNewtonianViscosityGrid
+ *                              MDLIB/mdoodz-private.h:423, def MDLIB/RheologyDensity.c:1131
+ *   mdz_rheo_sweep_aniso    <- NonNewtonianViscosityGridAniso
+ *                              MDLIB/mdoodz-private.h:437, def MDLIB/AnisotropyRoutines.c:885
+ *   mdz_rheo_points         <- ViscosityConcise / ViscosityConciseAniso called per point
+ *                              MDLIB/mdoodz-private.h:634-635 (callers: FD_Jacobian.c:66-67,
+ *                              RheologyDensity.c:2194 GenerateDeformationMaps)
+ *   (vertex fields T_s,P_s,d0_s,phi0_s)  <- InterpCentroidsToVerticesDouble
+ *                              MDLIB/GridRoutines.c:108, fused into the sweep
+ *
+ * All arithmetic is IEEE binary64.  Unless a call says otherwise it is
+ * synchronous (returns after the results are in the caller's buffers), like
+ * the reference.
+ */
+#ifndef MDZ_RHEO_H
+#define MDZ_RHEO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDZ_RHEO_ABI_VERSION 1
+#define MDZ_MAX_PHASES 20 /* mat_prop arrays are sized [20] (MDLIB/include/mdoodz.h:152-240) */
+
+/* ---- status codes ------------------------------------------------------
+ * The reference prints a message and calls exit(); the library returns one of
+ * these instead.  The drop-in maps them back to the reference's exit codes. */
+#define MDZ_OK                0
+#define MDZ_EINVAL           -1  /* bad argument / size */
+#define MDZ_ECUDA            -2  /* CUDA runtime error */
+#define MDZ_EUNSUPPORTED     -3  /* flag combination outside the implemented path */
+#define MDZ_ENOMEM           -4
+#define MDZ_ENOTREADY        -5  /* e.g. warm start requested without weights */
+#define MDZ_EVE_ITER        -10  /* VE local iterations failed  (RheologyDensity.c:175-177, exit 0) */
+#define MDZ_EGSE_ITER       -11  /* GSE local iteration failed / non-finite (:312-315, :366-368, exit 346) */
+#define MDZ_ESINGULAR       -12  /* singular 3x3 plastic Jacobian (:839-841, exit 1) */
+#define MDZ_EEMPTY_CELL     -13  /* cell went empty (:1274-1277, exit 345) */
+#define MDZ_ENONFINITE      -14  /* Inf/NaN harmonic viscosity (:1280-1301, exit 1) */
+#define MDZ_EWDISS          -15  /* negative dissipation (:1045-1050, exit 1) */
+#define MDZ_EGRAIN_ZERO     -16  /* grain-size dependent creep with d=0 (:507-510, exit 1) */
+#define MDZ_ELINESEARCH     -17  /* tensile line search alpha<0.01 (:868-872, exit 0) */
+#define MDZ_EANISO_NAN      -18  /* aniso VE residual NaN (AnisotropyRoutines.c:543, exit 1) */
+#define MDZ_EANISO_ITER     -19  /* aniso VE iterations failed (AnisotropyRoutines.c:580-583, exit 0) */
+
+/* memory space of the field pointers handed to a sweep */
+#define MDZ_MEM_HOST   0  /* host memory: the library copies in and out (drop-in mode) */
+#define MDZ_MEM_DEVICE 1  /* device memory of the context's GPU: no copies */
+
+/* sweep flags */
+#define MDZ_SWEEP_ASYNC      0x1  /* MDZ_MEM_DEVICE only: return after enqueue; call mdz_rheo_sync */
+#define MDZ_SWEEP_WARMSTART  0x2  /* start each local Newton from the learned guess (needs weights) */
+#define MDZ_SWEEP_ITERS      0x4  /* record per-(node,phase) local iteration counts (mdz_rheo_get_iterations) */
+
+/* ---- per-phase material table -----------------------------------------
+ * The subset of `mat_prop` (MDLIB/include/mdoodz.h:152-240) that the local
+ * update reads, with the same names and units (already scaled).            */
+typedef struct mdz_materials {
+  int    Nb_phases;
+  double R;                              /* gas constant, scaled */
+  /* mechanism switches */
+  int    cstv[MDZ_MAX_PHASES], pwlv[MDZ_MAX_PHASES], linv[MDZ_MAX_PHASES], gbsv[MDZ_MAX_PHASES],
+         expv[MDZ_MAX_PHASES], gs[MDZ_MAX_PHASES], kin[MDZ_MAX_PHASES], plast[MDZ_MAX_PHASES],
+         density_model[MDZ_MAX_PHASES], phase_mix[MDZ_MAX_PHASES], phase_two[MDZ_MAX_PHASES],
+         reac_soft[MDZ_MAX_PHASES], reac_phase[MDZ_MAX_PHASES], melt[MDZ_MAX_PHASES];
+  /* general */
+  double eta0[MDZ_MAX_PHASES], rho[MDZ_MAX_PHASES], drho[MDZ_MAX_PHASES], alp[MDZ_MAX_PHASES],
+         bet[MDZ_MAX_PHASES], T0[MDZ_MAX_PHASES], P0[MDZ_MAX_PHASES], Slim[MDZ_MAX_PHASES],
+         eta_vp[MDZ_MAX_PHASES], n_vp[MDZ_MAX_PHASES], T_st[MDZ_MAX_PHASES], gs_ref[MDZ_MAX_PHASES];
+  /* dislocation (power law) */
+  double Qpwl[MDZ_MAX_PHASES], Vpwl[MDZ_MAX_PHASES], npwl[MDZ_MAX_PHASES], mpwl[MDZ_MAX_PHASES],
+         rpwl[MDZ_MAX_PHASES], Apwl[MDZ_MAX_PHASES], fpwl[MDZ_MAX_PHASES], apwl[MDZ_MAX_PHASES],
+         Fpwl[MDZ_MAX_PHASES], pref_pwl[MDZ_MAX_PHASES];
+  /* diffusion (linear) */
+  double Qlin[MDZ_MAX_PHASES], Vlin[MDZ_MAX_PHASES], nlin[MDZ_MAX_PHASES], mlin[MDZ_MAX_PHASES],
+         rlin[MDZ_MAX_PHASES], Alin[MDZ_MAX_PHASES], flin[MDZ_MAX_PHASES], alin[MDZ_MAX_PHASES],
+         Flin[MDZ_MAX_PHASES];
+  /* grain-boundary sliding */
+  double Qgbs[MDZ_MAX_PHASES], Vgbs[MDZ_MAX_PHASES], ngbs[MDZ_MAX_PHASES], mgbs[MDZ_MAX_PHASES],
+         rgbs[MDZ_MAX_PHASES], Agbs[MDZ_MAX_PHASES], fgbs[MDZ_MAX_PHASES], agbs[MDZ_MAX_PHASES],
+         Fgbs[MDZ_MAX_PHASES];
+  /* Peierls (exponential) */
+  double Qexp[MDZ_MAX_PHASES], Sexp[MDZ_MAX_PHASES], Eexp[MDZ_MAX_PHASES], Gexp[MDZ_MAX_PHASES],
+         nexp[MDZ_MAX_PHASES];
+  /* paleowattmeter grain-size evolution */
+  double Kpzm[MDZ_MAX_PHASES], Qpzm[MDZ_MAX_PHASES], Gpzm[MDZ_MAX_PHASES], Lpzm[MDZ_MAX_PHASES],
+         cpzm[MDZ_MAX_PHASES], ppzm[MDZ_MAX_PHASES];
+} mdz_materials;
+
+/* ---- model switches and scaling ---------------------------------------
+ * The `params` (MDLIB/include/mdoodz.h:49-139) and `scale` (:142-144)
+ * fields the local update reads.                                           */
+typedef struct mdz_model {
+  int    Nx, Nz;              /* vertices; centroids are (Nx-1) x (Nz-1) */
+  int    Nb_phases;
+  int    step, elastic, eta_average, periodic_x, density_variations, tensile_line_search;
+  int    melting, chemical_production, diffuse_X, diffuse_avg;
+  double dt, min_eta, max_eta, eta_tol;
+  double scale_eta, scale_L, scale_T, scale_S, scale_E;
+} mdz_model;
+
+/* ---- grid fields -------------------------------------------------------
+ * Row-major flat arrays exactly as in `grid` (MDLIB/mdoodz-private.h:75-147):
+ * centroid c0 = k + l*Ncx, vertex c1 = k + l*Nx.  Phase fields are arrays of
+ * Nb_phases pointers (the `double**` layout of phase_perc_n etc.).
+ * Fields the chosen sweep does not use may be NULL (e.g. the anisotropy
+ * inputs for mdz_rheo_sweep, rho_n when density_variations==0).            */
+typedef struct mdz_grid_fields {
+  /* centroid inputs, (Nx-1)*(Nz-1) each */
+  const double *mu_n, *T, *p_in, *d0_n, *phi0_n, *X0_n, *exxd, *ezzd, *exz_n, *sxxd0, *szzd0,
+               *sxz0_n, *strain_n, *dil_n, *fric_n, *C_n, *p0_n, *T0_n, *bet_n, *div_u;
+  const double *const *phase_perc_n;
+  const signed char   *BCp_type;
+  /* vertex inputs, Nx*Nz each */
+  const double *mu_s, *X0_s, *exxd_s, *ezzd_s, *exz, *sxxd0_s, *szzd0_s, *sxz0, *strain_s,
+               *dil_s, *fric_s, *C_s, *p0_s, *bet_s, *div_u_s;
+  const double *const *phase_perc_s;
+  const signed char   *BCg_type;
+  /* anisotropy inputs (mdz_rheo_sweep_aniso only) */
+  const double *d1_n, *d2_n, *angle_n, *aniso_factor_n, *d1_s, *d2_s, *angle_s, *aniso_factor_s;
+  /* vertex fields interpolated from centroids (written by the sweep) */
+  double *T_s, *P_s, *d0_s, *phi0_s;
+  /* centroid outputs */
+  double *eta_n, *eta_phys_n, *VE_n, *sxxd, *szzd, *sxz_n, *eII_el, *eII_pl, *eII_pwl, *eII_exp,
+         *eII_lin, *eII_gbs, *eII_cst, *d_n, *p_corr, *div_u_el, *div_u_pl, *div_u_r, *Wtot,
+         *Wel, *Wdiss, *X_n, *OverS_n, *rho_n;
+  double *const *phase_eta_n;
+  /* vertex outputs */
+  double *sxxd_s, *szzd_s, *sxz, *eta_phys_s, *eta_s, *X_s, *VE_s;
+  double *const *phase_eta_s;
+} mdz_grid_fields;
+
+/* ---- sweep statistics ----------------------------------------------- */
+typedef struct mdz_sweep_stats {
+  uint64_t phase_calls;      /* (node, active phase) local solves */
+  uint64_t newton_iters;     /* sum of VE local iterations over all phase calls */
+  uint32_t max_newton_iters; /* max VE local iterations of one phase call */
+  uint64_t plastic_calls;    /* phase calls that yielded (is_pl) */
+  int32_t  status;           /* MDZ_OK or the first error code met */
+  int64_t  error_node;       /* node of that error: centroid c0, or Nc + c1 for a vertex; -1 if none */
+  double   elapsed_ms;       /* device time of the sweep kernels (CUDA events) */
+} mdz_sweep_stats;
+
+/* ---- point batches (ViscosityConcise / ViscosityConciseAniso per point) -- */
+typedef struct mdz_point_inputs {
+  const int32_t *phase;
+  const double  *G, *T, *P, *d, *phi, *X0, *Exx, *Ezz, *Exz, *Txx0, *Tzz0, *Txz0, *strain_acc,
+                *dil, *fric, *C, *P0, *T0, *beta, *div;
+  const double  *lxlz, *lx2, *angle, *ani_fac; /* anisotropic points only */
+  int post_process, centroid, final_update;
+} mdz_point_inputs;
+
+typedef struct mdz_point_outputs {
+  double *eta;  /* return value of ViscosityConcise (eta_phys) */
+  double *Txx, *Tzz, *Txz, *etaVE, *VEcoeff, *Eii_el, *Eii_pl, *Eii_pwl, *Eii_exp, *Eii_lin,
+         *Eii_gbs, *Eii_cst, *d1, *X1, *OverS, *Pcorr, *rho, *div_el, *div_pl, *div_r, *Wtot,
+         *Wel, *Wdiss;
+  int32_t *iters;   /* VE local iterations (may be NULL) */
+  int32_t *status;  /* per point MDZ_OK / error code (may be NULL) */
+} mdz_point_outputs;
+
+typedef struct mdz_rheo_ctx mdz_rheo_ctx;
+
+/* ---- context -------------------------------------------------------- */
+int         mdz_rheo_version(void);
+/* sizeof() of mdz_materials, mdz_model, mdz_grid_fields, mdz_sweep_stats,
+ * mdz_point_inputs, mdz_point_outputs as compiled into the library (out[0..5];
+ * out[6..7] are 0), so FFI bindings can check their struct layouts. */
+void        mdz_rheo_abi_sizes(size_t out[8]);
+const char *mdz_rheo_status_string(int status);
+/* Create a context on CUDA device `device`: one stream, device mirrors for
+ * host-memory sweeps (grown on demand, kept until destroy). */
+int mdz_rheo_create(int device, mdz_rheo_ctx **out);
+int mdz_rheo_destroy(mdz_rheo_ctx *ctx);
+/* Run the context's work on an external CUDA stream (cudaStream_t passed as
+ * void*); NULL restores the context's own stream. */
+int mdz_rheo_set_stream(mdz_rheo_ctx *ctx, void *stream);
+/* Wait for an MDZ_SWEEP_ASYNC sweep and fetch its statistics. */
+int mdz_rheo_sync(mdz_rheo_ctx *ctx, mdz_sweep_stats *stats);
+
+/* ---- the hot path --------------------------------------------------- */
+/* NonNewtonianViscosityGrid: vertex interpolation of T, p_in, d0, phi0, then
+ * every centroid and vertex: per active phase local solve, phase averaging,
+ * final stress.  `mem` is MDZ_MEM_HOST or MDZ_MEM_DEVICE; `stats` may be NULL. */
+int mdz_rheo_sweep(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                   const mdz_grid_fields *f, int final_update, int mem, int flags,
+                   mdz_sweep_stats *stats);
+/* NonNewtonianViscosityGridAniso, same conventions. */
+int mdz_rheo_sweep_aniso(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                         const mdz_grid_fields *f, int final_update, int mem, int flags,
+                         mdz_sweep_stats *stats);
+/* ViscosityConcise (aniso=0) or ViscosityConciseAniso (aniso=1) on n points. */
+int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                    const mdz_point_inputs *in, mdz_point_outputs *out, int64_t n, int aniso,
+                    int mem);
+/* Per-(phase, node) VE local iteration counts of the last sweep run with
+ * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
+ * inactive.  Host buffers. */
+int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDZ_RHEO_H */

@@ -1,0 +1,300 @@
+"""Python binding of the GB300 local-rheology library (include/mdz_rheo.h).
+
+This is the host-side mirror of MDOODZ7.0's interface for the local rheology
+update: `sweep` plays NonNewtonianViscosityGrid (MDLIB/RheologyDensity.c:1131),
+`sweep_aniso` NonNewtonianViscosityGridAniso (MDLIB/AnisotropyRoutines.c:885)
+and `points` ViscosityConcise / ViscosityConciseAniso per point
+(MDLIB/RheologyDensity.c:385, MDLIB/AnisotropyRoutines.c:282).  Field names
+are the reference's `grid` member names (MDLIB/mdoodz-private.h:75-147).
+
+Everything goes through the C ABI with ctypes; buffers are numpy arrays
+(host memory) or torch CUDA tensors (device memory).  There is no CPU
+fallback: if the CUDA library is missing, loading fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "libmdz_rheo_gb300.so")
+
+MAX_PHASES = 20
+
+# ---- status codes (include/mdz_rheo.h) ----------------------------------
+MDZ_OK = 0
+MDZ_EINVAL = -1
+MDZ_ECUDA = -2
+MDZ_EUNSUPPORTED = -3
+MDZ_ENOMEM = -4
+MDZ_ENOTREADY = -5
+MDZ_EVE_ITER = -10
+MDZ_EGSE_ITER = -11
+MDZ_ESINGULAR = -12
+MDZ_EEMPTY_CELL = -13
+MDZ_ENONFINITE = -14
+MDZ_EWDISS = -15
+MDZ_EGRAIN_ZERO = -16
+MDZ_ELINESEARCH = -17
+MDZ_EANISO_NAN = -18
+MDZ_EANISO_ITER = -19
+
+MEM_HOST = 0
+MEM_DEVICE = 1
+SWEEP_ASYNC = 0x1
+SWEEP_WARMSTART = 0x2
+SWEEP_ITERS = 0x4
+
+# ---- struct layouts (must follow include/mdz_rheo.h field by field) -------
+MAT_INT = ["cstv", "pwlv", "linv", "gbsv", "expv", "gs", "kin", "plast", "density_model",
+           "phase_mix", "phase_two", "reac_soft", "reac_phase", "melt"]
+MAT_DBL = ["eta0", "rho", "drho", "alp", "bet", "T0", "P0", "Slim", "eta_vp", "n_vp", "T_st", "gs_ref",
+           "Qpwl", "Vpwl", "npwl", "mpwl", "rpwl", "Apwl", "fpwl", "apwl", "Fpwl", "pref_pwl",
+           "Qlin", "Vlin", "nlin", "mlin", "rlin", "Alin", "flin", "alin", "Flin",
+           "Qgbs", "Vgbs", "ngbs", "mgbs", "rgbs", "Agbs", "fgbs", "agbs", "Fgbs",
+           "Qexp", "Sexp", "Eexp", "Gexp", "nexp",
+           "Kpzm", "Qpzm", "Gpzm", "Lpzm", "cpzm", "ppzm"]
+
+
+class Materials(C.Structure):
+    _fields_ = ([("Nb_phases", C.c_int), ("R", C.c_double)]
+                + [(n, C.c_int * MAX_PHASES) for n in MAT_INT]
+                + [(n, C.c_double * MAX_PHASES) for n in MAT_DBL])
+
+
+MODEL_INT = ["Nx", "Nz", "Nb_phases", "step", "elastic", "eta_average", "periodic_x",
+             "density_variations", "tensile_line_search", "melting", "chemical_production",
+             "diffuse_X", "diffuse_avg"]
+MODEL_DBL = ["dt", "min_eta", "max_eta", "eta_tol", "scale_eta", "scale_L", "scale_T", "scale_S",
+             "scale_E"]
+
+
+class Model(C.Structure):
+    _fields_ = [(n, C.c_int) for n in MODEL_INT] + [(n, C.c_double) for n in MODEL_DBL]
+
+
+CEN_IN = ["mu_n", "T", "p_in", "d0_n", "phi0_n", "X0_n", "exxd", "ezzd", "exz_n", "sxxd0", "szzd0",
+          "sxz0_n", "strain_n", "dil_n", "fric_n", "C_n", "p0_n", "T0_n", "bet_n", "div_u"]
+VER_IN = ["mu_s", "X0_s", "exxd_s", "ezzd_s", "exz", "sxxd0_s", "szzd0_s", "sxz0", "strain_s",
+          "dil_s", "fric_s", "C_s", "p0_s", "bet_s", "div_u_s"]
+ANI_IN_N = ["d1_n", "d2_n", "angle_n", "aniso_factor_n"]
+ANI_IN_S = ["d1_s", "d2_s", "angle_s", "aniso_factor_s"]
+VER_INTERP = ["T_s", "P_s", "d0_s", "phi0_s"]
+CEN_OUT = ["eta_n", "eta_phys_n", "VE_n", "sxxd", "szzd", "sxz_n", "eII_el", "eII_pl", "eII_pwl",
+           "eII_exp", "eII_lin", "eII_gbs", "eII_cst", "d_n", "p_corr", "div_u_el", "div_u_pl",
+           "div_u_r", "Wtot", "Wel", "Wdiss", "X_n", "OverS_n", "rho_n"]
+VER_OUT = ["sxxd_s", "szzd_s", "sxz", "eta_phys_s", "eta_s", "X_s", "VE_s"]
+
+_P = C.c_void_p
+_PP = C.POINTER(C.c_void_p)
+
+
+class GridFields(C.Structure):
+    _fields_ = ([(n, _P) for n in CEN_IN] + [("phase_perc_n", _PP), ("BCp_type", _P)]
+                + [(n, _P) for n in VER_IN] + [("phase_perc_s", _PP), ("BCg_type", _P)]
+                + [(n, _P) for n in ANI_IN_N + ANI_IN_S] + [(n, _P) for n in VER_INTERP]
+                + [(n, _P) for n in CEN_OUT] + [("phase_eta_n", _PP)]
+                + [(n, _P) for n in VER_OUT] + [("phase_eta_s", _PP)])
+
+
+class SweepStats(C.Structure):
+    _fields_ = [("phase_calls", C.c_uint64), ("newton_iters", C.c_uint64),
+                ("max_newton_iters", C.c_uint32), ("plastic_calls", C.c_uint64),
+                ("status", C.c_int32), ("error_node", C.c_int64), ("elapsed_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+PT_IN = ["G", "T", "P", "d", "phi", "X0", "Exx", "Ezz", "Exz", "Txx0", "Tzz0", "Txz0", "strain_acc",
+         "dil", "fric", "C", "P0", "T0", "beta", "div"]
+PT_ANI = ["lxlz", "lx2", "angle", "ani_fac"]
+PT_OUT = ["eta", "Txx", "Tzz", "Txz", "etaVE", "VEcoeff", "Eii_el", "Eii_pl", "Eii_pwl", "Eii_exp",
+          "Eii_lin", "Eii_gbs", "Eii_cst", "d1", "X1", "OverS", "Pcorr", "rho", "div_el", "div_pl",
+          "div_r", "Wtot", "Wel", "Wdiss"]
+
+
+class PointInputs(C.Structure):
+    _fields_ = ([("phase", _P)] + [(n, _P) for n in PT_IN] + [(n, _P) for n in PT_ANI]
+                + [("post_process", C.c_int), ("centroid", C.c_int), ("final_update", C.c_int)])
+
+
+class PointOutputs(C.Structure):
+    _fields_ = [(n, _P) for n in PT_OUT] + [("iters", _P), ("status", _P)]
+
+
+# ---- buffer helpers ---------------------------------------------------------
+def _ptr(a) -> Optional[int]:
+    """Address of a numpy array or torch tensor (None stays NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"], "arrays must be contiguous"
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def _ptr_array(lst):
+    if lst is None:
+        return None
+    arr = (C.c_void_p * max(1, len(lst)))(*[_ptr(a) for a in lst])
+    return arr
+
+
+class FieldSet:
+    """A dict of grid arrays plus the mdz_grid_fields struct that points at them.
+
+    `arrays` maps reference field names to arrays; `phase_perc_n`,
+    `phase_perc_s`, `phase_eta_n`, `phase_eta_s` map to lists (one array per
+    phase).  Missing names become NULL.
+    """
+
+    def __init__(self, arrays: Dict[str, object]):
+        self.arrays = arrays
+        self._keep = []
+        s = GridFields()
+        for name, _ in GridFields._fields_:
+            v = arrays.get(name)
+            if name.startswith("phase_"):
+                pa = _ptr_array(v)
+                self._keep.append(pa)
+                setattr(s, name, C.cast(pa, _PP) if pa is not None else None)
+            else:
+                setattr(s, name, _ptr(v))
+        self.struct = s
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+
+def make_points(inputs: Dict[str, object], outputs: Dict[str, object], post_process=1, centroid=1,
+                final_update=0):
+    pi = PointInputs()
+    for name, _ in PointInputs._fields_:
+        if name in ("post_process", "centroid", "final_update"):
+            continue
+        setattr(pi, name, _ptr(inputs.get(name)))
+    pi.post_process, pi.centroid, pi.final_update = post_process, centroid, final_update
+    po = PointOutputs()
+    for name, _ in PointOutputs._fields_:
+        setattr(po, name, _ptr(outputs.get(name)))
+    return pi, po
+
+
+# ---- library ----------------------------------------------------------------
+class RheoError(RuntimeError):
+    def __init__(self, code, where=""):
+        self.code = code
+        super().__init__(f"{where}: {status_string(code)} ({code})")
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libmdz_rheo_gb300.so.  Raises if it was not built: there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"GB300 rheology library not built: {path} (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    lib.mdz_rheo_version.restype = C.c_int
+    lib.mdz_rheo_status_string.restype = C.c_char_p
+    lib.mdz_rheo_status_string.argtypes = [C.c_int]
+    lib.mdz_rheo_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    lib.mdz_rheo_destroy.argtypes = [C.c_void_p]
+    lib.mdz_rheo_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mdz_rheo_sync.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
+    for fn in (lib.mdz_rheo_sweep, lib.mdz_rheo_sweep_aniso):
+        fn.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
+                       C.c_int, C.c_int, C.c_int, C.POINTER(SweepStats)]
+    lib.mdz_rheo_points.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials),
+                                    C.POINTER(PointInputs), C.POINTER(PointOutputs), C.c_int64,
+                                    C.c_int, C.c_int]
+    lib.mdz_rheo_get_iterations.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.mdz_rheo_abi_sizes.argtypes = [C.POINTER(C.c_size_t)]
+    _lib = lib
+    return lib
+
+
+def status_string(code: int) -> str:
+    try:
+        return load_library().mdz_rheo_status_string(code).decode()
+    except Exception:  # library absent: still give a readable message
+        return f"status {code}"
+
+
+def abi_sizes():
+    """sizeof() of the C structs as compiled into the library, for ABI checks."""
+    lib = load_library()
+    out = (C.c_size_t * 8)()
+    lib.mdz_rheo_abi_sizes(out)
+    return list(out)
+
+
+def python_struct_sizes():
+    return [C.sizeof(Materials), C.sizeof(Model), C.sizeof(GridFields), C.sizeof(SweepStats),
+            C.sizeof(PointInputs), C.sizeof(PointOutputs)]
+
+
+class Context:
+    """One mdz_rheo_ctx: a CUDA stream plus device mirrors for host-memory sweeps."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        rc = self.lib.mdz_rheo_create(device, C.byref(h))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.mdz_rheo_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: Optional[int]):
+        rc = self.lib.mdz_rheo_set_stream(self.handle, stream_ptr)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_set_stream")
+
+    def _sweep(self, fn, model, mat, fields, final_update, mem, flags, check):
+        st = SweepStats()
+        rc = fn(self.handle, C.byref(model), C.byref(mat), C.byref(fields.struct), final_update, mem,
+                flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, fn.__name__)
+        return rc, st
+
+    def sweep(self, model, mat, fields, final_update=0, mem=MEM_HOST, flags=0, check=True):
+        """NonNewtonianViscosityGrid on `fields` (a FieldSet).  Returns (status, SweepStats)."""
+        return self._sweep(self.lib.mdz_rheo_sweep, model, mat, fields, final_update, mem, flags, check)
+
+    def sweep_aniso(self, model, mat, fields, final_update=0, mem=MEM_HOST, flags=0, check=True):
+        """NonNewtonianViscosityGridAniso on `fields`.  Returns (status, SweepStats)."""
+        return self._sweep(self.lib.mdz_rheo_sweep_aniso, model, mat, fields, final_update, mem,
+                           flags, check)
+
+    def sync(self):
+        st = SweepStats()
+        rc = self.lib.mdz_rheo_sync(self.handle, C.byref(st))
+        return rc, st
+
+    def points(self, model, mat, pin, pout, n, aniso=0, mem=MEM_HOST):
+        return self.lib.mdz_rheo_points(self.handle, C.byref(model), C.byref(mat), C.byref(pin),
+                                        C.byref(pout), n, aniso, mem)
+
+    def get_iterations(self, out_n: np.ndarray, out_s: np.ndarray):
+        rc = self.lib.mdz_rheo_get_iterations(self.handle, _ptr(out_n), _ptr(out_s))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_get_iterations")

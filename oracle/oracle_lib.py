@@ -1,0 +1,113 @@
+"""ctypes loader for the CPU oracle.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py, as the checker.  Two libraries can be loaded:
+
+  * build/librheo_oracle.so -- the C restatement (rheo_oracle.c), built on any
+    host by `make -C oracle`;
+  * _ref/libmdz_ref.so      -- MDOODZ7.0's own sources plus ref_harness.c,
+    built by `make -C oracle ref` where the reference tree is present.
+
+Both take the same plain-pointer structs as the GPU library (include/mdz_rheo.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(REPO, "mdoodz7.0_gb300"))
+import mdz_rheo as R  # noqa: E402
+
+ORACLE_SO = os.path.join(HERE, "build", "librheo_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libmdz_ref.so")
+REF_TREE = os.environ.get("MDZ_REFERENCE_TREE", "/root/reference")
+
+
+def build(ref: bool = False, quiet: bool = True):
+    """Build the restatement (and, when asked and the reference tree exists, _ref)."""
+    targets = ["all"]
+    if ref and os.path.isdir(os.path.join(REF_TREE, "MDLIB")):
+        targets.append("ref")
+    out = subprocess.run(["make", "-C", HERE, f"REF={REF_TREE}", "-j8"] + targets,
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def _bind(lib, prefix):
+    for name in ("sweep", "sweep_aniso"):
+        fn = getattr(lib, f"{prefix}_{name}", None)
+        if fn is None:
+            continue
+        if prefix == "orc":
+            fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields), C.c_int,
+                           C.c_void_p, C.c_void_p, C.POINTER(R.SweepStats)]
+        fn.restype = C.c_int
+    pts = getattr(lib, f"{prefix}_points")
+    pts.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.PointInputs),
+                    C.POINTER(R.PointOutputs), C.c_int64, C.c_int]
+    pts.restype = C.c_int
+    return lib
+
+
+_orc = None
+_ref = None
+
+
+def oracle():
+    global _orc
+    if _orc is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        lib = C.CDLL(ORACLE_SO)
+        _bind(lib, "orc")
+        lib.orc_interp_c2v.argtypes = [C.POINTER(R.Model), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.orc_num_threads.restype = C.c_int
+        _orc = lib
+    return _orc
+
+
+def reference():
+    """The reference's own code, or None where it was not built."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            return None
+        lib = C.CDLL(REF_SO)
+        lib.ref_sweep.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields),
+                                  C.c_int, C.c_int]
+        lib.ref_sweep.restype = C.c_int
+        _bind(lib, "ref")
+        _ref = lib
+    return _ref
+
+
+def orc_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False, iters_n=None, iters_s=None):
+    lib = oracle()
+    st = R.SweepStats()
+    fn = lib.orc_sweep_aniso if aniso else lib.orc_sweep
+    rc = fn(C.byref(model), C.byref(mat), C.byref(fs.struct), final_update,
+            None if iters_n is None else iters_n.ctypes.data,
+            None if iters_s is None else iters_s.ctypes.data, C.byref(st))
+    return rc, st
+
+
+def ref_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False):
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    return lib.ref_sweep(C.byref(model), C.byref(mat), C.byref(fs.struct), final_update, int(aniso))
+
+
+def orc_points(model, mat, pin, pout, n, aniso=0):
+    return oracle().orc_points(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso)
+
+
+def ref_points(model, mat, pin, pout, n, aniso=0):
+    return reference().ref_points(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso)

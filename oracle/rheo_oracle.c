@@ -1,0 +1,1036 @@
+/*
+ * rheo_oracle.c -- CPU restatement of MDOODZ7.0's local rheology update.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product).  See
+ * rheo_oracle.h.  Every block cites the reference lines it restates; the
+ * floating-point expressions keep the reference's evaluation order so that,
+ * compiled with -ffp-contract=off, results are bit-identical to the reference
+ * built from its own sources on x86-64.  Dead computations of the reference
+ * (values that never reach an output) are left out and noted.
+ */
+#include "rheo_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ZEROC 273.15 /* MDLIB/include/mdoodz.h:4 */
+#define ORC_MIN(a, b) ((a) <= (b) ? (a) : (b)) /* MINV, MDLIB/mdoodz-private.h:11 */
+#define ORC_MAX(a, b) ((a) >= (b) ? (a) : (b)) /* MAXV, MDLIB/mdoodz-private.h:12 */
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* one point: scalar inputs and outputs                                      */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int    phase;
+  double G, T, P, d, phi, X0, Exx, Ezz, Exz, Txx0, Tzz0, Txz0, dil, fric, C, P0, T0, beta;
+  double lxlz, lx2, angle, ani_fac; /* aniso only */
+  int    post_process, centroid, final_update;
+} orc_pt;
+
+typedef struct {
+  double eta, Txx, Tzz, Txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_exp, Eii_lin, Eii_gbs,
+         Eii_cst, d1, X1, OverS, Pcorr, rho, div_el, div_pl, div_r, Wtot, Wel, Wdiss;
+  int    iters, is_pl, status;
+} orc_res;
+
+static void set_status(int *st, int code) {
+  if (*st == MDZ_OK) *st = code;
+}
+
+/* ------------------------------------------------------------------------ */
+/* local visco-elastic solves: LocalIterationParams (RheologyDensity.h:17-48) */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int    elastic, peierls, dislocation, diffusion, constant, gbs;
+  double Eii, eta_el, eta_cst, C_pwl, n_pwl, C_gbs, n_gbs, C_lin, n_lin, m_lin, C_exp, ST, n_exp;
+  double d, eta_up, eta_lo, Ag, gam, lam, cg, pg;
+} orc_ve;
+
+typedef struct {
+  double eta, Tii, d1, e_cst, e_pwl, e_gbs, e_exp, e_lin;
+  int    iters, status;
+} orc_ve_out;
+
+/* LocalIterationViscoElastic, RheologyDensity.c:152-197 */
+static void orc_ve_newton(const orc_ve *q, orc_ve_out *o) {
+  const int    nitmax = 20;
+  const double tol    = 1.0e-11;
+  double eta = o->eta, Tii = o->Tii;
+  double e_cst = 0., e_pwl = 0., e_gbs = 0., e_exp = 0., e_lin = 0.;
+  int    it, iters = nitmax;
+  for (it = 0; it < nitmax; it++) {
+    Tii = 2.0 * eta * q->Eii;
+    if (q->constant) e_cst = Tii / 2.0 / q->eta_cst;
+    if (q->dislocation) e_pwl = q->C_pwl * pow(Tii, q->n_pwl);
+    if (q->gbs) e_gbs = q->C_gbs * pow(Tii, q->n_gbs);
+    if (q->peierls) e_exp = q->C_exp * pow(Tii, q->ST + q->n_exp);
+    if (q->diffusion) e_lin = q->C_lin * pow(Tii, q->n_lin) * pow(q->d, -q->m_lin);
+    const double e_vis = e_pwl + e_exp + e_lin + e_gbs + e_cst;
+    const double r     = q->Eii - q->elastic * Tii / (2.0 * q->eta_el) - e_vis;
+    const double res   = fabs(r / q->Eii);
+    if (res < tol / 100) {
+      iters = it + 1;
+      break;
+    } else if (it == nitmax - 1 && res > tol) { /* reference: exit(0) */
+      set_status(&o->status, MDZ_EVE_ITER);
+      break;
+    }
+    double dfdeta = 0.0;
+    if (q->elastic) dfdeta += -q->Eii / q->eta_el;
+    if (q->peierls) dfdeta += -(e_exp) * (q->ST + q->n_exp) / eta;
+    if (q->diffusion) dfdeta += -(e_lin) * q->n_lin / eta;
+    if (q->dislocation) dfdeta += -(e_pwl) * q->n_pwl / eta;
+    if (q->constant) dfdeta += -q->Eii / q->eta_cst;
+    eta -= r / dfdeta;
+  }
+  o->eta = eta; o->Tii = Tii; o->iters = iters;
+  o->e_cst = e_cst; o->e_exp = e_exp; o->e_gbs = e_gbs; o->e_pwl = e_pwl; o->e_lin = e_lin;
+}
+
+/* LocalIterationViscoElasticGrainSize, RheologyDensity.c:203-379.  The two
+ * bracket-end evaluations at :221-243 only feed the unused r_eta_lo/r_eta_up
+ * and are overwritten inside the loop, so they are not restated. */
+static void orc_ve_gse(const orc_ve *q, orc_ve_out *o) {
+  const int    nitmax = 50, bisection_steps = 20;
+  const double tol    = 1.0e-11;
+  double d_ve = o->d1, eta = o->eta, Tii = o->Tii;
+  const double p = q->pg, Eii = q->Eii, n_pwl = q->n_pwl, Ag = q->Ag;
+  const double Bg    = q->lam / (q->cg * q->gam);
+  const double C_pwl = q->C_pwl;
+  double eta_up = q->eta_up, eta_lo = q->eta_lo;
+  double e_cst = 0., e_pwl = 0., e_gbs = 0., e_exp = 0., e_lin = 0.;
+  int    it, iters = nitmax;
+  for (it = 0; it < nitmax; it++) {
+    if (it < bisection_steps) eta = sqrt(eta_up * eta_lo);
+    Tii = 2.0 * eta * q->Eii;
+    if (q->constant) e_cst = Tii / 2.0 / q->eta_cst;
+    if (q->dislocation) e_pwl = q->C_pwl * pow(Tii, q->n_pwl);
+    d_ve = pow(2 * Bg * q->Eii * e_pwl * eta * p / q->Ag, (-1.0 / (p + 1)));
+    if (q->gbs) e_gbs = q->C_gbs * pow(Tii, q->n_gbs);
+    if (q->peierls) e_exp = q->C_exp * pow(Tii, q->ST + q->n_exp);
+    if (q->diffusion) e_lin = q->C_lin * pow(Tii, q->n_lin) * pow(d_ve, -q->m_lin);
+    const double e_vis = e_pwl + e_exp + e_lin + e_gbs + e_cst;
+    const double r     = q->Eii - q->elastic * Tii / (2.0 * q->eta_el) - e_vis;
+    const double res   = fabs(r / q->Eii);
+    if (res < tol / 100) { iters = it + 1; break; }
+    if (it == bisection_steps - 1 && res < tol) { iters = it + 1; break; }
+    if (it < bisection_steps) {
+      if (r > 0.0) eta_up = eta;
+      else         eta_lo = eta;
+    } else {
+      const double dddeta = -1.0 / 2.0 * Ag * d_ve * pow(2 * Eii * eta, -n_pwl) *
+                            (2 * Bg * C_pwl * Eii * n_pwl * p * pow(2 * Eii * eta, n_pwl) / Ag +
+                             2 * Bg * C_pwl * Eii * p * pow(2 * Eii * eta, n_pwl) / Ag) /
+                            (Bg * C_pwl * Eii * eta * p * (p + 1));
+      double dfdeta = 0.0;
+      if (q->elastic) dfdeta += -q->Eii / q->eta_el;
+      if (q->constant) dfdeta += -q->Eii / q->eta_cst;
+      if (q->peierls) dfdeta += -(e_exp) * (q->ST + q->n_exp) / eta;
+      if (q->diffusion) dfdeta += -(e_lin) * q->n_lin / eta;
+      if (q->dislocation) dfdeta += -(e_pwl) * q->n_pwl / eta;
+      dfdeta += q->m_lin * e_lin * dddeta / d_ve;
+      eta -= r / dfdeta;
+    }
+    if (it == nitmax - 1 && res > tol) { /* reference: exit(346) */
+      set_status(&o->status, MDZ_EGSE_ITER);
+      break;
+    }
+  }
+  if (isnan(eta) || isinf(eta)) set_status(&o->status, MDZ_EGSE_ITER);
+  o->eta = eta; o->d1 = d_ve; o->Tii = Tii; o->iters = iters;
+  o->e_cst = e_cst; o->e_exp = e_exp; o->e_gbs = e_gbs; o->e_pwl = e_pwl; o->e_lin = e_lin;
+}
+
+/* solve_local_3x3, RheologyDensity.c:1082-1125 */
+static int orc_solve3(double J11, double J12, double J13, double J21, double J22, double J23,
+                      double J31, double J32, double J33, double R1, double R2, double R3,
+                      double *dT, double *dP, double *dl) {
+  const double det = J11 * (J22 * J33 - J23 * J32) - J12 * (J21 * J33 - J23 * J31) +
+                     J13 * (J21 * J32 - J22 * J31);
+  if (fabs(det) < 1e-30) return 0;
+  const double inv = 1.0 / det;
+  *dT = -inv * ((J22 * J33 - J23 * J32) * R1 + (J13 * J32 - J12 * J33) * R2 +
+                (J12 * J23 - J13 * J22) * R3);
+  *dP = -inv * ((J23 * J31 - J21 * J33) * R1 + (J11 * J33 - J13 * J31) * R2 +
+                (J13 * J21 - J11 * J23) * R3);
+  *dl = -inv * ((J21 * J32 - J22 * J31) * R1 + (J12 * J31 - J11 * J32) * R2 +
+                (J11 * J22 - J12 * J21) * R3);
+  return 1;
+}
+
+/* EvaluateDensity, RheologyDensity.c:1761-1831 (models 0, 1, 3, 5; 2 and 4
+ * need phase-diagram tables and are rejected before the sweep when their
+ * value is used). */
+static double orc_density(const mdz_model *m, const mdz_materials *mt, int p, double T, double P,
+                          double X, double phi) {
+  double rho = 0.0;
+  const int dm = mt->density_model[p];
+  if (dm == 0) rho = mt->rho[p];
+  if (dm == 1) {
+    rho = (1.0 - mt->alp[p] * (T - mt->T0[p])) * (1.0 + mt->bet[p] * (P - mt->P0[p]));
+    rho = ((1.0 - X) * mt->rho[p] + X * (mt->rho[p] + mt->drho[p])) * rho;
+  }
+  if (dm == 3 && m->density_variations == 0) rho = mt->rho[p] * exp(mt->bet[p] * P - mt->alp[p] * T);
+  if (dm == 3 && m->density_variations == 1) {
+    const double rho_ref = (1.0 - X) * mt->rho[p] + X * mt->rho[mt->reac_phase[p]];
+    rho = rho_ref * exp(mt->bet[p] * P - mt->alp[p] * T);
+  }
+  if (dm == 5) {
+    const double rs = mt->rho[p] * exp(mt->bet[p] * P - mt->alp[p] * T);
+    const double rl = (mt->rho[p] + mt->drho[p]) * exp(mt->bet[p] * P - mt->alp[p] * T);
+    rho = (1 - phi) * rs + phi * rl;
+  }
+  return rho;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ViscosityConcise, RheologyDensity.c:385-1080                              */
+/* ------------------------------------------------------------------------ */
+static void orc_viscosity_concise(const mdz_model *m, const mdz_materials *mt, const orc_pt *in,
+                                  orc_res *o) {
+  const int phase = in->phase;
+  const int nitmax = 20;
+  double G = in->G, T = in->T, P = in->P, d = in->d, dil = in->dil, C = in->C;
+  const double phi = in->phi, X0 = in->X0, Exx = in->Exx, Ezz = in->Ezz, Exz = in->Exz;
+  const double Txx0 = in->Txx0, Tzz0 = in->Tzz0, Txz0 = in->Txz0, fric = in->fric;
+  const double R = mt->R, min_eta = m->min_eta, max_eta = m->max_eta;
+  const double TmaxPeierls = (1200.0 + ZEROC) / m->scale_T; /* :390 */
+  const double dt = (m->step == 0) ? 1e100 : m->dt;      /* :392-394 */
+  const double tol = m->eta_tol;
+  int    plastic = 0, constant = 0, dislocation = 0, peierls = 0, diffusion = 0, gbs = 0;
+  int    elastic = m->elastic, gs = 0, is_pl = 0;
+  double K = 1.0 / in->beta;
+  const double Tiimin = 1e5 / m->scale_S;                  /* :427 */
+  const double n_pwl = mt->npwl[phase], n_lin = mt->nlin[phase], m_lin = mt->mlin[phase];
+  const double n_gbs = mt->ngbs[phase], n_exp = mt->nexp[phase];
+  const double eta_vp0 = mt->eta_vp[phase], n_vp = mt->n_vp[phase];
+  double eta_vp = mt->eta_vp[phase];
+  int    constant_mix = mt->phase_mix[phase];
+  if (m->diffuse_X == 0) constant_mix = 0;                 /* :440 */
+
+  memset(o, 0, sizeof(*o));                                /* :451-455 */
+  /* invariants, :461-464 */
+  const double Eyy = -(Exx + Ezz);
+  double Eii = sqrt(1.0 / 2.0 * (Exx * Exx + Ezz * Ezz + Eyy * Eyy) + Exz * Exz);
+  if (Eii * m->scale_E < 1e-30) Eii = 1e-30 / m->scale_E;
+  o->Pcorr = P;                                            /* :467 */
+  /* mechanism switches, :471-483 */
+  if (mt->cstv[phase] != 0) constant = 1;
+  if (mt->pwlv[phase] != 0) dislocation = 1;
+  if (mt->expv[phase] != 0 && T < TmaxPeierls) peierls = 1;
+  if (mt->linv[phase] != 0) diffusion = 1;
+  if (mt->gbsv[phase] != 0) gbs = 1;
+  if (mt->gs[phase] != 0) gs = 1;
+  if (mt->plast[phase] == 1) plastic = 1;
+  if (mt->plast[phase] == 2) plastic = 2;
+  if (m->step == 0) { elastic = 0; plastic = 0; }
+  o->d1 = mt->gs_ref[phase];                               /* :486 */
+  if (elastic == 0) { G = 1e1; dil = 0.0; K = 1e10; }      /* :493 */
+  if (T < ZEROC / m->scale_T) T = ZEROC / m->scale_T;      /* :496 */
+
+  /* Arrhenius pre-factors, :501-523 */
+  double B_pwl = 0.0, C_pwl = 0.0, B_lin = 0.0, C_lin = 0.0, B_gbs = 0.0, B_exp = 0.0, C_exp = 0.0;
+  double ST = 0.0;
+  if (dislocation == 1) {
+    B_pwl = mt->pref_pwl[phase] * mt->Fpwl[phase] * pow(mt->Apwl[phase], -1.0 / n_pwl) *
+            exp((mt->Qpwl[phase] + P * mt->Vpwl[phase]) / R / n_pwl / T) *
+            pow(d, mt->mpwl[phase] / n_pwl) * pow(mt->fpwl[phase], -mt->rpwl[phase] / n_pwl) *
+            exp(-mt->apwl[phase] * phi / n_pwl);
+    C_pwl = pow(2.0 * B_pwl, -n_pwl);
+  }
+  if (diffusion == 1) {
+    if (m_lin > 0.0 && d < 1e-13 / m->scale_L) set_status(&o->status, MDZ_EGRAIN_ZERO);
+    B_lin = mt->Flin[phase] * pow(mt->Alin[phase], -1.0 / n_lin) *
+            exp((mt->Qlin[phase] + P * mt->Vlin[phase]) / R / n_lin / T) *
+            pow(mt->flin[phase], -mt->rlin[phase] / n_lin) * exp(-mt->alin[phase] * phi / n_lin);
+    C_lin = pow(2.0 * B_lin, -n_lin);
+  }
+  if (gbs == 1) {
+    B_gbs = mt->Fgbs[phase] * pow(mt->Agbs[phase], -1.0 / n_gbs) *
+            exp((mt->Qgbs[phase] + P * mt->Vgbs[phase]) / R / n_gbs / T) *
+            pow(d, mt->mgbs[phase] / n_gbs) * pow(mt->fgbs[phase], -mt->rgbs[phase] / n_gbs) *
+            exp(-mt->agbs[phase] * phi / n_gbs);
+  }
+  if (peierls == 1) {
+    const double Ea = mt->Qexp[phase], gamma = mt->Gexp[phase];
+    ST = Ea / R / T * 2.0 * gamma * (1 - gamma);
+    const double Arr = exp(-Ea / R / T * pow(1.0 - gamma, 2.0));
+    const double F_exp = pow(pow(2.0, 1.0 - ST - n_exp) / pow(sqrt(3.0), ST + n_exp + 1.0),
+                             1.0 / (ST + n_exp));
+    B_exp = F_exp * (pow(gamma * mt->Sexp[phase], ST / (ST + n_exp)) /
+                     pow(mt->Eexp[phase] * Arr, 1.0 / (ST + n_exp)));
+    C_exp = pow(2.0 * B_exp, -(ST + n_exp));
+  }
+  const double cos_fric = cos(fric), sin_fric = sin(fric), sin_dil = sin(dil);
+  double Tyield = 0.0;
+  if (plastic == 1) {                                      /* :530-539 */
+    Tyield = C * cos_fric + P * sin_fric;
+    if (mt->Slim[phase] < Tyield) { C = mt->Slim[phase]; Tyield = mt->Slim[phase]; }
+  }
+  o->X1 = X0;                                              /* :545, :554 */
+
+  /* isolated viscosities, :559-592 */
+  const double eta_el = G * dt;
+  double eta_cst = 0.0, eta_pwl = 0.0, eta_lin = 0.0, eta_gbs = 0.0, eta_exp = 0.0, Ag = 0.0;
+  if (constant == 1) eta_cst = mt->eta0[phase];
+  if (constant_mix == 1) {
+    const double e1 = mt->eta0[phase], e2 = mt->eta0[mt->phase_two[phase]];
+    if (m->diffuse_avg == 0) eta_cst = X0 * e1 + (1 - X0) * e2;
+    if (m->diffuse_avg == 1) eta_cst = pow(X0 / e1 + (1 - X0) / e2, -1.0);
+    if (m->diffuse_avg == 2) eta_cst = exp(X0 * log(e1) + (1 - X0) * log(e2));
+  }
+  if (dislocation == 1) eta_pwl = B_pwl * pow(Eii, 1.0 / n_pwl - 1.0);
+  double Tii = 0.0;
+  if (gs == 1) {                                           /* :567-576 */
+    Ag = mt->Kpzm[phase] * exp(-mt->Qpzm[phase] / R / T);
+    const double gam = mt->Gpzm[phase], lam = mt->Lpzm[phase], cg = mt->cpzm[phase], pg = mt->ppzm[phase];
+    Tii = 2. * eta_el * Eii;
+    o->Eii_pwl = Tii / 2.0 / eta_pwl;
+    d = exp(log(Ag * gam / (lam * (1.0 / cg) * Tii * (o->Eii_pwl) * pg)) / (1.0 + pg));
+  }
+  if (diffusion == 1) eta_lin = B_lin * pow(Eii, 1.0 / n_lin - 1.0) * pow(d, m_lin / n_lin);
+  if (gbs == 1) eta_gbs = B_gbs * pow(Eii, 1.0 / n_gbs - 1.0);
+  if (peierls == 1) eta_exp = B_exp * pow(Eii, 1.0 / (ST + n_exp) - 1.0);
+  o->Eii_pl = 0.0;
+  double eta_up = 1.0e100 / m->scale_eta, eta_lo = -1.0e100 / m->scale_eta;
+  if (constant == 1)    { eta_up = ORC_MIN(eta_up, eta_cst); eta_lo = ORC_MAX(eta_lo, eta_cst); }
+  if (dislocation == 1) { eta_up = ORC_MIN(eta_up, eta_pwl); eta_lo = ORC_MAX(eta_lo, eta_pwl); }
+  if (elastic == 1)     { eta_up = ORC_MIN(eta_up, eta_el);  eta_lo = ORC_MAX(eta_lo, eta_el);  }
+  if (peierls == 1)     { eta_up = ORC_MIN(eta_up, eta_exp); eta_lo = ORC_MAX(eta_lo, eta_exp); }
+  if (diffusion == 1)   { eta_up = ORC_MIN(eta_up, eta_lin); eta_lo = ORC_MAX(eta_lo, eta_lin); }
+  if (gbs == 1)         { eta_up = ORC_MIN(eta_up, eta_gbs); eta_lo = ORC_MAX(eta_lo, eta_gbs); }
+
+  /* initial guess and local solve, :597-647 (the d_it of :610 is unused) */
+  double eta_ve = eta_up;
+  Tii = 2.0 * eta_ve * Eii;
+  if (gs == 1) o->d1 = d;
+  orc_ve q = {0};
+  q.elastic = elastic; q.peierls = peierls; q.dislocation = dislocation; q.diffusion = diffusion;
+  q.constant = constant; q.gbs = gbs; q.Eii = Eii; q.eta_el = eta_el; q.eta_cst = eta_cst;
+  q.C_pwl = C_pwl; q.n_pwl = n_pwl; q.C_gbs = 0.0; /* C_gbs is never set, :616-642 */
+  q.n_gbs = n_gbs; q.C_lin = C_lin; q.n_lin = n_lin; q.m_lin = m_lin; q.C_exp = C_exp; q.ST = ST;
+  q.n_exp = n_exp; q.d = d; q.eta_up = eta_up; q.eta_lo = eta_lo; q.Ag = Ag;
+  q.gam = mt->Gpzm[phase]; q.lam = mt->Lpzm[phase]; q.cg = mt->cpzm[phase]; q.pg = mt->ppzm[phase];
+  orc_ve_out vo = {0};
+  vo.eta = eta_ve; vo.Tii = Tii; vo.d1 = o->d1; vo.status = MDZ_OK;
+  if (gs) orc_ve_gse(&q, &vo);
+  else    orc_ve_newton(&q, &vo);
+  set_status(&o->status, vo.status);
+  eta_ve = vo.eta; Tii = vo.Tii; o->iters = vo.iters;
+  if (gs) o->d1 = vo.d1;
+  o->Eii_cst = vo.e_cst; o->Eii_exp = vo.e_exp; o->Eii_gbs = vo.e_gbs; o->Eii_pwl = vo.e_pwl;
+  o->Eii_lin = vo.e_lin;
+
+  /* plastic corrections */
+  double gdot = 0.0, divp = 0.0, Pc = P, eta_vep = 0.0, lam_dot = 0.0, A_tau = 1.0, A_P = 0.0;
+  if (plastic == 1) {                                      /* :655-707 */
+    double F_trial = Tii - Tyield;
+    if (F_trial > 1e-17) {
+      double Tiic = 0.0, res_pl;
+      is_pl   = 1;
+      eta_vp  = eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
+      gdot    = F_trial / (eta_ve + eta_vp + K * dt * sin_fric * sin_dil);
+      A_P     = -sin_dil;
+      const double F_trial0 = F_trial;
+      for (int it = 0; it < nitmax; it++) {
+        A_P     = -sin_dil;
+        divp    = -gdot * A_P;
+        Pc      = P + K * dt * divp;
+        eta_vp  = eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+        Tyield  = Tyield + gdot * eta_vp;
+        Tiic    = Tii - eta_ve * gdot;
+        F_trial = Tiic - Tyield;
+        res_pl  = fabs(F_trial);
+        if (res_pl < tol || res_pl / F_trial0 < tol) break;
+        const double dFdgdot = -eta_ve - eta_vp / n_vp - K * dt * sin_fric * sin_dil;
+        gdot -= F_trial / dFdgdot;
+      }
+      if (Tiic < 0.0) {                                    /* :697-704 */
+        F_trial = Tii - Tiimin;
+        gdot    = F_trial / (eta_ve);
+        Tiic    = Tiimin;
+        Pc      = P;
+      }
+      o->Pcorr = Pc;
+      eta_vep  = Tiic / (2.0 * Eii);
+      Tii      = Tiic;
+    }
+  }
+  if (plastic == 2) {                                      /* :710-930 */
+    const double k = sin_fric, kq = sin_dil, c = C * cos_fric;
+    const double a = sqrt(1.0 + k * k), b = sqrt(1.0 + kq * kq);
+    const double T_st = mt->T_st[phase];
+    const double py = (T_st + c / a) / (1.0 - k / a);
+    const double Ry = py - T_st;
+    const double pd = py - Ry * k / a;
+    const double tau_d = k * pd + c;
+    const double pq = pd + kq * tau_d;
+    double R_haty = sqrt(Tii * Tii + (P - py) * (P - py));
+    double R_hatq;
+    int on_yield = (Tii * (py - pd)) >= (tau_d * (py - P)), on_flow;
+    double F_trial = on_yield ? Tii - k * P - c : a * (R_haty - Ry);
+    divp = 0.0;
+    if (F_trial > 1e-17) {
+      const double atol = 1e-10, rtol = 1e-8;
+      double Tiic = Tii, R0n = 2.0 * atol, Rn;
+      double A_tau_2 = 0, A_P_2 = 0, A_tau_P = 0, A_P_tau = 0, dFdT, dFdP;
+      is_pl = 1; Pc = P; lam_dot = 0.0;
+      for (int it = 0; it < nitmax; it++) {
+        if (Tiic < 0.0) Tiic = 0.0;
+        on_yield = (Tiic * (py - pd)) >= (tau_d * (py - Pc));
+        on_flow  = (Tiic * (pq - pd)) >= (tau_d * (pq - Pc));
+        eta_vp   = eta_vp0;
+        R_haty   = sqrt(Tiic * Tiic + (Pc - py) * (Pc - py));
+        R_hatq   = sqrt(Tiic * Tiic + (Pc - pq) * (Pc - pq));
+        if (on_yield) { F_trial = Tiic - k * Pc - c; dFdT = 1.0; dFdP = -k; }
+        else { F_trial = a * (R_haty - Ry); dFdT = a * Tiic / R_haty; dFdP = a * (Pc - py) / R_haty; }
+        if (on_flow) { A_tau = 0.5; A_P = kq; A_tau_2 = 0.0; A_P_2 = 0.0; A_tau_P = 0.0; A_P_tau = 0.0; }
+        else {
+          A_tau   = b * Tiic / (2.0 * R_hatq);
+          A_P     = -b * (Pc - pq) / R_hatq;
+          A_tau_2 = b * (R_hatq * R_hatq - Tiic * Tiic) / (2.0 * R_hatq * R_hatq * R_hatq);
+          A_P_2   = -b * (R_hatq * R_hatq - (Pc - pq) * (Pc - pq)) / (R_hatq * R_hatq * R_hatq);
+          A_tau_P = -b * Tiic * (Pc - pq) / (2.0 * R_hatq * R_hatq * R_hatq);
+          A_P_tau = b * Tiic * (Pc - pq) / (R_hatq * R_hatq * R_hatq);
+        }
+        double R1 = (Tii - Tiic) / (2.0 * eta_ve) - lam_dot * A_tau;
+        double R2 = (Pc - P) / (K * dt) - lam_dot * A_P;
+        double R3 = F_trial - lam_dot * eta_vp;
+        Rn = sqrt(R1 * R1 + R2 * R2 + R3 * R3);
+        if (Rn < atol || Rn / R0n < rtol) break;
+        R0n = Rn;
+        const double J11 = -1.0 / 2.0 / eta_ve - lam_dot * A_tau_2, J12 = -lam_dot * A_tau_P, J13 = -A_tau;
+        const double J21 = -lam_dot * A_P_tau, J22 = 1.0 / K / dt - lam_dot * A_P_2, J23 = -A_P;
+        const double J31 = dFdT, J32 = dFdP, J33 = -eta_vp;
+        double dT, dP, dl;
+        if (!orc_solve3(J11, J12, J13, J21, J22, J23, J31, J32, J33, R1, R2, R3, &dT, &dP, &dl)) {
+          set_status(&o->status, MDZ_ESINGULAR);           /* reference: exit(1) */
+          break;
+        }
+        double alpha = 1.0;
+        if (m->tensile_line_search == 1) {                 /* :845-887 */
+          const double c_ls = 1e-4, R0ls = 0.5 * (R1 * R1 + R2 * R2 + R3 * R3);
+          int failed = 0;
+          for (int ls = 0; ls < 100; ls++) {
+            const double Tl = Tiic + dT * alpha, Pl = Pc + dP * alpha;
+            on_yield = (Tl * (py - pd) >= tau_d * (py - Pl));
+            on_flow  = (Tl * (pq - pd) >= tau_d * (pq - Pl));
+            eta_vp   = eta_vp0;
+            R_haty   = sqrt(Tl * Tl + (Pl - py) * (Pl - py));
+            R_hatq   = sqrt(Tl * Tl + (Pl - pq) * (Pl - pq));
+            const double Fl = on_yield ? Tl - k * Pl - c : a * (R_haty - Ry);
+            if (on_flow) { A_tau = 0.5; A_P = kq; }
+            else { A_tau = b * Tl / (2.0 * R_hatq); A_P = -b * (Pl - pq) / R_hatq; }
+            R1 = (Tii - Tl) / (2.0 * eta_ve) - lam_dot * A_tau;
+            R2 = (Pl - P) / (K * dt) - lam_dot * A_P;
+            R3 = Fl - lam_dot * eta_vp;
+            const double Rls = 0.5 * (R1 * R1 + R2 * R2 + R3 * R3);
+            if (Rls < R0ls - 2.0 * c_ls * alpha * Rls && ls > 0) break;
+            alpha *= 0.5;
+            if (alpha < 1e-2) { failed = 1; break; }
+          }
+          if (failed) { set_status(&o->status, MDZ_ELINESEARCH); break; } /* reference: exit(0) */
+        }
+        Tiic += alpha * dT;
+        Pc += alpha * dP;
+        lam_dot += alpha * dl;
+      }
+      o->Pcorr = Pc;
+      eta_vep  = Tiic / (2.0 * Eii);
+      Tii      = Tiic;
+      divp     = lam_dot * A_P;
+    }
+  }
+
+  /* density, :934-960 (kinetics only alters rho when density_variations==0,
+   * where the grid never reads it) */
+  if (in->centroid > 0) {
+    const double Pd = (in->final_update == 1) ? Pc : P;
+    o->rho = orc_density(m, mt, phase, T, Pd, X0, phi);
+  }
+
+  double eta_pl = 0.0;
+  if (is_pl == 0) { o->etaVE = eta_ve; o->div_pl = 0.0; }
+  else if (plastic == 1) { o->etaVE = eta_vep; o->div_pl = divp; eta_pl = Tii / gdot; }
+  else if (plastic == 2) { o->etaVE = eta_vep; o->div_pl = divp; eta_pl = Tii / (2.0 * lam_dot * A_tau); }
+  o->is_pl = is_pl;
+  o->Txx = 2.0 * (o->etaVE) * Exx;                         /* :981-983 */
+  o->Tzz = 2.0 * (o->etaVE) * Ezz;
+  o->Txz = 2.0 * (o->etaVE) * Exz;
+
+  double eta = 0.0;
+  if (in->post_process == 1) {                             /* :986-1053 */
+    if (dislocation == 1) eta_pwl = B_pwl * pow(o->Eii_pwl, 1.0 / n_pwl - 1.0);
+    if (diffusion == 1) eta_lin = B_lin * pow(o->Eii_lin, 1.0 / n_lin - 1.0) * pow(o->d1, m_lin / n_lin);
+    if (peierls == 1) eta_exp = B_exp * pow(o->Eii_exp, 1.0 / (ST + n_exp) - 1.0);
+    if (elastic) {
+      const double Tyy = -(o->Txx + o->Tzz), Tyy0 = -(Txx0 + Tzz0);
+      const double Exx_el = (o->Txx - Txx0) / 2 / eta_el, Ezz_el = (o->Tzz - Tzz0) / 2 / eta_el;
+      const double Eyy_el = (Tyy - Tyy0) / 2 / eta_el, Exz_el = (o->Txz - Txz0) / 2 / eta_el;
+      o->Eii_el = sqrt(0.5 * (Exx_el * Exx_el + Ezz_el * Ezz_el + Eyy_el * Eyy_el) + Exz_el * Exz_el);
+    }
+    if (is_pl && plastic == 1) o->Eii_pl = gdot / 2.0;
+    else if (is_pl && plastic == 2) o->Eii_pl = lam_dot * A_tau;
+    else o->Eii_pl = 0.0;
+    o->div_pl = divp;
+    o->div_el = -(Pc - in->P0) / (K * dt);
+    o->div_r  = 0.0;
+    double inv = 0.0;
+    if (peierls == 1) inv += (1.0 / eta_exp);
+    if (dislocation == 1) inv += (1.0 / eta_pwl);
+    if (diffusion == 1) inv += (1.0 / eta_lin);
+    if (constant == 1) inv += (1.0 / eta_cst);
+    if (is_pl == 1) inv += (1.0 / eta_pl);
+    eta = 1.0 / (inv);
+    if (plastic == 1) o->OverS = eta_vp * gdot;
+    if (plastic == 2) o->OverS = eta_vp * lam_dot * A_tau;
+    if (in->centroid == 1) {
+      o->Wtot  = Tii * Tii / eta_ve;
+      o->Wel   = Tii * Tii / eta_el;
+      o->Wdiss = Tii * Tii / eta;
+      if (o->Wdiss < 0.0) set_status(&o->status, MDZ_EWDISS); /* reference: exit(1) */
+    }
+  }
+  /* limiters, :1058-1073 */
+  if (o->etaVE > max_eta) o->etaVE = max_eta;
+  if (o->etaVE < min_eta) o->etaVE = min_eta;
+  if (eta > max_eta) eta = max_eta;
+  if (eta < min_eta) eta = min_eta;
+  o->eta = eta;
+}
+
+/* ------------------------------------------------------------------------ */
+/* ViscosityConciseAniso, AnisotropyRoutines.c:282-727                        */
+/* ------------------------------------------------------------------------ */
+static void orc_viscosity_concise_aniso(const mdz_model *m, const mdz_materials *mt,
+                                        const orc_pt *in, orc_res *o) {
+  const int    phase = in->phase;
+  const double tol = 1e-11, R = mt->R, dt = m->dt, min_eta = m->min_eta, max_eta = m->max_eta;
+  const int    nitmax = 50;
+  const double TmaxPeierls = (1200.0 + ZEROC) / m->scale_T;
+  double G = in->G, T = in->T, P = in->P, dil = in->dil, Coh = in->C;
+  const double fric = in->fric, phi = in->phi, lxlz = in->lxlz, lx2 = in->lx2, ani_fac = in->ani_fac;
+  int    plastic = 0, constant = 0, dislocation = 0, peierls = 0, diffusion = 0;
+  int    elastic = m->elastic, is_pl = 0;
+  double eta_el = 1e20, eta_cst = 0.0;
+  const double n_pwl = mt->npwl[phase], n_lin = mt->nlin[phase], m_lin = mt->mlin[phase];
+  const double n_exp = mt->nexp[phase];
+
+  memset(o, 0, sizeof(*o));                                /* :310-318 */
+  o->Pcorr = P;
+  o->d1    = in->d;
+  if (mt->cstv[phase] != 0) constant = 1;                  /* :322-326 */
+  if (mt->pwlv[phase] != 0) dislocation = 1;
+  if (mt->expv[phase] != 0 && T < TmaxPeierls) peierls = 1;
+  if (mt->linv[phase] != 0) diffusion = 1;
+  if (mt->plast[phase] != 0) plastic = 1;
+  if (m->step == 0) elastic = 0;
+  if (elastic == 0) { G = 1e1; dil = 0.0; }
+  if (T < ZEROC / m->scale_T) T = ZEROC / m->scale_T;
+
+  double B_pwl = 0.0, C_pwl = 0.0, B_lin = 0.0, C_lin = 0.0, B_exp = 0.0, C_exp = 0.0, ST = 0.0;
+  if (dislocation == 1) {                                  /* :334-337 */
+    B_pwl = mt->pref_pwl[phase] * mt->Fpwl[phase] * pow(mt->Apwl[phase], -1.0 / n_pwl) *
+            exp((mt->Qpwl[phase] + P * mt->Vpwl[phase]) / R / n_pwl / T) *
+            pow(in->d, mt->mpwl[phase] / n_pwl) * pow(mt->fpwl[phase], -mt->rpwl[phase] / n_pwl) *
+            exp(-mt->apwl[phase] * phi / n_pwl);
+    C_pwl = pow(2.0 * B_pwl, -n_pwl);
+  }
+  if (diffusion == 1) {                                    /* :342-349 */
+    if (m_lin > 0.0 && o->d1 < 1e-13 / m->scale_L) set_status(&o->status, MDZ_EGRAIN_ZERO);
+    B_lin = mt->Flin[phase] * pow(mt->Alin[phase], -1.0 / n_lin) *
+            exp((mt->Qlin[phase] + P * mt->Vlin[phase]) / R / n_lin / T) *
+            pow(mt->flin[phase], -mt->rlin[phase] / n_lin) * exp(-mt->alin[phase] * phi / n_lin);
+    C_lin = pow(2.0 * B_lin, -n_lin);
+  }
+  if (peierls == 1) {                                      /* :355-362 */
+    const double Ea = mt->Qexp[phase], gamma = mt->Gexp[phase];
+    ST = Ea / R / T * 2.0 * gamma * (1 - gamma);
+    const double Arr = exp(-Ea / R / T * pow(1.0 - gamma, 2.0));
+    const double F_exp = pow(pow(2.0, 1.0 - ST - n_exp) / pow(sqrt(3.0), ST + n_exp + 1.0),
+                             1.0 / (ST + n_exp));
+    B_exp = F_exp * (pow(gamma * mt->Sexp[phase], ST / (ST + n_exp)) /
+                     pow(mt->Eexp[phase] * Arr, 1.0 / (ST + n_exp)));
+    C_exp = pow(2.0 * B_exp, -(ST + n_exp));
+  }
+  double Tyield = 0.0;
+  const double K = 1.0 / in->beta;
+  if (plastic == 1) {                                      /* :370-377 */
+    Tyield = Coh * cos(fric) + P * sin(fric);
+    if (mt->Slim[phase] < Tyield) { Coh = mt->Slim[phase]; Tyield = mt->Slim[phase]; }
+  }
+  /* rotate the strain rate, :379-383 */
+  const double nz2 = 1.0 - lx2;
+  const double Er_xx = lx2 * in->Exx + nz2 * in->Ezz + 2. * lxlz * in->Exz;
+  const double Er_zz = nz2 * in->Exx + lx2 * in->Ezz - 2. * lxlz * in->Exz;
+  const double Er_xz = -lxlz * in->Exx + lxlz * in->Ezz + (lx2 - nz2) * in->Exz;
+  const double Er_yy = -Er_xx - Er_zz;
+  /* I2, :263-265 */
+  const double Eii = sqrt(0.5 * (pow(Er_xx, 2) + pow(Er_zz, 2) + pow(Er_yy, 2)) + pow(Er_xz, 2));
+  double eta_pwl = 0.0, eta_lin = 0.0, eta_exp = 0.0;
+  if (constant) eta_cst = mt->eta0[phase];                 /* :390-397 */
+  if (dislocation) eta_pwl = B_pwl * pow(Eii, (1 - n_pwl) / n_pwl);
+  if (elastic) eta_el = G * dt;
+  if (diffusion == 1) eta_lin = B_lin * pow(Eii, 1.0 / n_lin - 1.0) * pow(o->d1, m_lin / n_lin);
+  if (peierls == 1) eta_exp = B_exp * pow(Eii, 1.0 / (ST + n_exp) - 1.0);
+  double eta_up = 1.0e100 / m->scale_eta, eta_lo = -1.0e100 / m->scale_eta; /* :409-415 */
+  if (constant)    { eta_up = ORC_MIN(eta_up, eta_cst); eta_lo = ORC_MAX(eta_lo, eta_cst); }
+  if (dislocation) { eta_up = ORC_MIN(eta_up, eta_pwl); eta_lo = ORC_MAX(eta_lo, eta_pwl); }
+  if (elastic)     { eta_up = ORC_MIN(eta_up, eta_el);  eta_lo = ORC_MAX(eta_lo, eta_el);  }
+  if (peierls)     { eta_up = ORC_MIN(eta_up, eta_exp); eta_lo = ORC_MAX(eta_lo, eta_exp); }
+  if (diffusion)   { eta_up = ORC_MIN(eta_up, eta_lin); eta_lo = ORC_MAX(eta_lo, eta_lin); }
+  double eta_ve = eta_up, Tii = 0.0;
+
+  if (mt->gs[phase] != 0) {                                /* :429-473 */
+    orc_ve q = {0};
+    q.Ag = mt->Kpzm[phase] * exp(-mt->Qpzm[phase] / (R * T));
+    q.gam = mt->Gpzm[phase]; q.lam = mt->Lpzm[phase]; q.cg = mt->cpzm[phase]; q.pg = mt->ppzm[phase];
+    q.Eii = Eii; q.C_pwl = C_pwl; q.n_pwl = n_pwl; q.C_lin = C_lin; q.n_lin = n_lin; q.m_lin = m_lin;
+    q.ST = ST; q.n_exp = n_exp; q.elastic = elastic; q.eta_el = eta_el; q.peierls = peierls;
+    q.C_exp = C_exp; q.dislocation = dislocation; q.diffusion = diffusion; q.constant = constant;
+    q.eta_cst = eta_cst; q.gbs = 0; q.C_gbs = 0.0; q.n_gbs = 1.0; q.d = o->d1;
+    q.eta_up = eta_up; q.eta_lo = eta_lo;
+    orc_ve_out vo = {0};
+    vo.eta = eta_ve; vo.Tii = Tii; vo.d1 = o->d1; vo.status = MDZ_OK;
+    orc_ve_gse(&q, &vo);
+    set_status(&o->status, vo.status);
+    eta_ve = vo.eta; Tii = vo.Tii; o->d1 = vo.d1; o->iters = vo.iters;
+    o->Eii_cst = vo.e_cst; o->Eii_lin = vo.e_lin; o->Eii_gbs = vo.e_gbs; o->Eii_pwl = vo.e_pwl;
+    o->Eii_exp = vo.e_exp;
+  } else {                                                 /* :474-585 */
+    double r = 0.0, eta_bi_lo = min_eta * 1.0e-3, eta_bi_hi = 10.0 * ORC_MAX(eta_lo, max_eta);
+    const double d = o->d1;
+    for (int bit = 0; bit < 10; bit++) {
+      eta_ve = sqrt(eta_bi_lo * eta_bi_hi);
+      Tii = 2.0 * eta_ve * Eii;
+      if (constant) o->Eii_cst = Tii / 2.0 / eta_cst;
+      if (dislocation) o->Eii_pwl = C_pwl * pow(Tii, n_pwl);
+      if (peierls) o->Eii_exp = C_exp * pow(Tii, ST + n_exp);
+      if (diffusion) o->Eii_lin = C_lin * pow(Tii, n_lin) * pow(d, -m_lin);
+      const double Eii_vis = o->Eii_pwl + o->Eii_cst + o->Eii_exp + o->Eii_lin;
+      const double r_bi = Eii - elastic * Tii / 2 / eta_el - Eii_vis;
+      if (r_bi > 0.0) eta_bi_lo = eta_ve;
+      else eta_bi_hi = eta_ve;
+      if (fabs(r_bi / Eii) < tol / 100) break;
+    }
+    eta_ve = sqrt(eta_bi_lo * eta_bi_hi);
+    o->iters = nitmax;
+    for (int it = 0; it < nitmax; it++) {
+      Tii = 2.0 * eta_ve * Eii;
+      if (constant) o->Eii_cst = Tii / 2.0 / eta_cst;
+      if (dislocation) o->Eii_pwl = C_pwl * pow(Tii, n_pwl);
+      if (peierls) o->Eii_exp = C_exp * pow(Tii, ST + n_exp);
+      if (diffusion) o->Eii_lin = C_lin * pow(Tii, n_lin) * pow(d, -m_lin);
+      const double Eii_vis = o->Eii_pwl + o->Eii_cst + o->Eii_exp + o->Eii_lin;
+      r = Eii - elastic * Tii / 2 / eta_el - Eii_vis;
+      if (isnan(r)) { set_status(&o->status, MDZ_EANISO_NAN); o->iters = it + 1; break; }
+      double drdeta = 0.0;
+      if (elastic) drdeta += -elastic * Eii / eta_el;
+      if (dislocation) drdeta += -o->Eii_pwl * n_pwl / eta_ve;
+      if (constant) drdeta += -constant * Eii / eta_cst;
+      if (peierls) drdeta += -(o->Eii_exp) * (ST + n_exp) / eta_ve;
+      if (diffusion) drdeta += -(o->Eii_lin) * n_lin / eta_ve;
+      eta_ve -= r / drdeta;
+      if (eta_ve <= 0.0) eta_ve = min_eta;
+      if (fabs(r / Eii) < tol / 100) { o->iters = it + 1; break; }
+      if (it == nitmax - 1 && fabs(r / Eii) < 10.0 * tol) break;
+      if (it == nitmax - 1 && (fabs(r / Eii) > tol)) { set_status(&o->status, MDZ_EANISO_ITER); break; }
+    }
+  }
+  if (eta_ve < min_eta) eta_ve = min_eta;                  /* :589-603 */
+  if (eta_ve > max_eta) eta_ve = max_eta;
+  double Tr_xx = 2.0 * eta_ve * Er_xx, Tr_zz = 2.0 * eta_ve * Er_zz;
+  double Tr_xz = 2.0 * eta_ve * Er_xz / ani_fac;
+  double eta_vep = eta_ve;
+  const double eta_vp = mt->eta_vp[phase], eta_vp0 = mt->eta_vp[phase];
+  const double Ft = Tii - Tyield;
+  double gdot = 0.0, Pc = P;
+  if (Ft > 1e-17 && plastic == 1) {                        /* :625-648 */
+    is_pl = 1;
+    gdot = Ft / (eta_ve + eta_vp0 + K * dt * sin(dil) * sin(fric));
+    const double Tiic = Tii - gdot * eta_ve;
+    Pc = P + K * dt * sin(dil) * gdot;
+    eta_vep = Tiic / 2.0 / Eii;
+    Tr_xx = 2.0 * (eta_vep) * Er_xx;
+    Tr_zz = 2.0 * (eta_vep) * Er_zz;
+    Tr_xz = 2.0 * (eta_vep) * Er_xz / ani_fac;
+    o->div_pl = gdot * sin(dil);
+    o->Eii_pl = gdot / 2.0;
+    Tii = Tiic;
+  }
+  o->Txx = lx2 * Tr_xx + nz2 * Tr_zz - 2. * lxlz * Tr_xz; /* :650-652 */
+  o->Tzz = nz2 * Tr_xx + lx2 * Tr_zz + 2. * lxlz * Tr_xz;
+  o->Txz = lxlz * Tr_xx - lxlz * Tr_zz + (lx2 - nz2) * Tr_xz;
+  o->Pcorr = Pc;
+  if (eta_vep < min_eta) eta_vep = min_eta;                /* :664-677 */
+  if (eta_vep > max_eta) eta_vep = max_eta;
+  o->etaVE = eta_vep;
+  o->is_pl = is_pl;
+  double eta = eta_vep;
+  const double eta_pl = Tii / gdot, divp = gdot * sin(dil);
+  if (in->post_process == 1) {                             /* :681-714 */
+    if (dislocation == 1) eta_pwl = B_pwl * pow(o->Eii_pwl, 1.0 / n_pwl - 1.0);
+    if (diffusion == 1) eta_lin = B_lin * pow(o->Eii_lin, 1.0 / n_lin - 1.0) * pow(o->d1, m_lin / n_lin);
+    if (peierls == 1) eta_exp = B_exp * pow(o->Eii_exp, 1.0 / (ST + n_exp) - 1.0);
+    if (elastic) o->Eii_el = Tii * Tii / (4 * eta_el * eta_el);
+    if (is_pl) o->Eii_pl = gdot / 2.0;
+    o->div_pl = divp;
+    o->div_el = -(Pc - in->P0) / (K * dt);
+    double inv = 0.0;
+    if (diffusion == 1) inv += (1.0 / eta_lin);
+    if (peierls == 1) inv += (1.0 / eta_exp);
+    if (dislocation == 1) inv += (1.0 / eta_pwl);
+    if (constant == 1) inv += (1.0 / eta_cst);
+    if (is_pl == 1) inv += (1.0 / eta_pl);
+    eta = 1.0 / (inv);
+    o->OverS = eta_vp * gdot;
+    if (in->centroid == 1) {
+      o->Wtot  = Tii * Tii / eta_ve;
+      o->Wel   = Tii * Tii / eta_el;
+      o->Wdiss = Tii * Tii / eta;
+    }
+  }
+  if (eta > max_eta) eta = max_eta;                        /* :720-721 */
+  if (eta < min_eta) eta = min_eta;
+  o->eta = eta;
+}
+
+/* EffectiveStrainRate, RheologyDensity.c:116-146 */
+static void orc_effective_strain_rate(double *Exx, double *Ezz, double *Exz, double exx, double ezz,
+                                      double exz, double Txx, double Tzz, double Txz, double d1,
+                                      double d2, double ani, double eta_e, int elastic) {
+  if (!elastic) { *Exx = exx; *Ezz = ezz; *Exz = exz; return; }
+  const double Da11 = 2.0 - 2.0 * ani * d1, Da12 = 2.0 * ani * d1, Da13 = -2.0 * ani * d2;
+  const double Da22 = 2.0 - 2.0 * ani * d1, Da23 = 2.0 * ani * d2;
+  const double Da33 = 1.0 + 2.0 * ani * (d1 - 0.5);
+  const double a11 = Da33 * Da22 - pow(Da23, 2), a12 = Da13 * Da23 - Da33 * Da12;
+  const double a13 = Da12 * Da23 - Da13 * Da22, a22 = Da33 * Da11 - pow(Da13, 2);
+  const double a23 = Da12 * Da13 - Da11 * Da23, a33 = Da11 * Da22 - pow(Da12, 2);
+  const double det = (Da11 * a11) + (Da12 * a12) + (Da13 * a13);
+  const double i11 = a11 / det, i12 = a12 / det, i13 = a13 / det, i22 = a22 / det, i23 = a23 / det,
+               i33 = a33 / det;
+  *Exx = exx + (i11 * Txx + i12 * Tzz + i13 * Txz) / eta_e;
+  *Ezz = ezz + (i12 * Txx + i22 * Tzz + i23 * Txz) / eta_e;
+  *Exz = exz + (i13 * Txx + i23 * Tzz + i33 * Txz) / eta_e / 2.0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* InterpCentroidsToVerticesDouble, GridRoutines.c:108-210.  The reference   */
+/* builds a ghost-ringed copy of the centroid field; vertex (k,l) reads ring  */
+/* cells (k..k+1, l..l+1), each of which maps to one centroid.                */
+/* ------------------------------------------------------------------------ */
+static int orc_ring_to_centroid(int i, int j, int Ncx, int Ncz, int per) {
+  int cj = j - 1, ci;
+  if (cj < 0) cj = 0;
+  if (cj > Ncz - 1) cj = Ncz - 1;
+  if (per == 1) ci = (i == 0) ? Ncx - 1 : (i == Ncx + 1) ? 0 : i - 1;
+  else { ci = i - 1; if (ci < 0) ci = 0; if (ci > Ncx - 1) ci = Ncx - 1; }
+  return ci + cj * Ncx;
+}
+
+static double orc_interp_vertex(const double *cen, const signed char *BCp, const signed char *BCg,
+                                int k, int l, int Nx, int Nz, int per) {
+  const int Ncx = Nx - 1, Ncz = Nz - 1, c1 = k + l * Nx;
+  if (BCg[c1] == 30) return 0.0;
+  const int sw = orc_ring_to_centroid(k, l, Ncx, Ncz, per), se = orc_ring_to_centroid(k + 1, l, Ncx, Ncz, per);
+  const int nw = orc_ring_to_centroid(k, l + 1, Ncx, Ncz, per), ne = orc_ring_to_centroid(k + 1, l + 1, Ncx, Ncz, per);
+  const int inSW = !(BCp[sw] == 30 || BCp[sw] == 31), inSE = !(BCp[se] == 30 || BCp[se] == 31);
+  const int inNW = !(BCp[nw] == 30 || BCp[nw] == 31), inNE = !(BCp[ne] == 30 || BCp[ne] == 31);
+  return 0.25 * (inSW * cen[sw] + inSE * cen[se] + inNW * cen[nw] + inNE * cen[ne]);
+}
+
+void orc_interp_c2v(const mdz_model *m, const double *cen, const signed char *BCp,
+                    const signed char *BCg, double *vert) {
+  const int Nx = m->Nx, Nz = m->Nz;
+#pragma omp parallel for
+  for (int c1 = 0; c1 < Nx * Nz; c1++)
+    vert[c1] = orc_interp_vertex(cen, BCp, BCg, c1 % Nx, c1 / Nx, Nx, Nz, m->periodic_x);
+}
+
+/* ------------------------------------------------------------------------ */
+/* sweeps                                                                     */
+/* ------------------------------------------------------------------------ */
+static int orc_check_supported(const mdz_model *m, const mdz_materials *mt) {
+  if (m->Nx < 2 || m->Nz < 2 || m->Nb_phases < 1 || m->Nb_phases > MDZ_MAX_PHASES) return MDZ_EINVAL;
+  if (m->melting || m->chemical_production) return MDZ_EUNSUPPORTED;
+  for (int p = 0; p < m->Nb_phases; p++) {
+    const int dm = mt->density_model[p];
+    if (m->density_variations == 1 && (dm == 2 || dm == 4)) return MDZ_EUNSUPPORTED;
+  }
+  return MDZ_OK;
+}
+
+typedef struct {
+  uint64_t calls, iters, plastic;
+  uint32_t maxit;
+  int      status;
+  int64_t  node;
+} orc_acc;
+
+static void acc_error(orc_acc *a, int status, int64_t node) {
+  if (status == MDZ_OK) return;
+#pragma omp critical(orc_err)
+  {
+    if (a->status == MDZ_OK || node < a->node) { a->status = status; a->node = node; }
+  }
+}
+
+static void fill_stats(mdz_sweep_stats *s, const orc_acc *a) {
+  if (!s) return;
+  s->phase_calls = a->calls; s->newton_iters = a->iters; s->max_newton_iters = a->maxit;
+  s->plastic_calls = a->plastic; s->status = a->status; s->error_node = a->status ? a->node : -1;
+  s->elapsed_ms = 0.0;
+}
+
+/* NonNewtonianViscosityGrid(Aniso): RheologyDensity.c:1131-1426,
+ * AnisotropyRoutines.c:885-1217.  kp/lp/kn/ln are the identity maps built by
+ * GridIndices (GridRoutines.c:543-585), so the loop index is the node. */
+static int orc_sweep_impl(const mdz_model *m, const mdz_materials *mt, const mdz_grid_fields *f,
+                          int final_update, int32_t *iters_n, int32_t *iters_s,
+                          mdz_sweep_stats *stats, int aniso) {
+  int st = orc_check_supported(m, mt);
+  if (st != MDZ_OK) return st;
+  const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1, Nc = Ncx * Ncz, Nv = Nx * Nz;
+  const int np = m->Nb_phases, avg = m->eta_average;
+  const double el = (m->elastic == 1) ? 1.0 : 0.0;
+  orc_acc acc = {0, 0, 0, 0, MDZ_OK, -1};
+  uint64_t calls = 0, iters = 0, plastic = 0;
+  uint32_t maxit = 0;
+
+  /* :1150-1153 / :903-906 */
+  orc_interp_c2v(m, f->T, f->BCp_type, f->BCg_type, f->T_s);
+  orc_interp_c2v(m, f->p_in, f->BCp_type, f->BCg_type, f->P_s);
+  orc_interp_c2v(m, f->d0_n, f->BCp_type, f->BCg_type, f->d0_s);
+  orc_interp_c2v(m, f->phi0_n, f->BCp_type, f->BCg_type, f->phi0_s);
+
+#pragma omp parallel for reduction(+ : calls, iters, plastic) reduction(max : maxit)
+  for (int c0 = 0; c0 < Nc; c0++) {
+    double *outs[23] = {f->eta_n, f->eta_phys_n, f->VE_n, f->sxxd, f->szzd, f->sxz_n, f->eII_el,
+                        f->eII_pl, f->eII_pwl, f->eII_exp, f->eII_lin, f->eII_gbs, f->eII_cst,
+                        f->d_n, f->p_corr, f->div_u_el, f->div_u_pl, f->div_u_r, f->Wtot, f->Wel,
+                        f->Wdiss, f->X_n, f->OverS_n};
+    for (int i = 0; i < 23; i++) outs[i][c0] = 0.0;
+    if (m->density_variations == 1) f->rho_n[c0] = 0.0;
+    if (iters_n) for (int p = 0; p < np; p++) iters_n[(int64_t)p * Nc + c0] = 0;
+    if (f->BCp_type[c0] == 30 || f->BCp_type[c0] == 31) continue;
+    const double eta_e = (m->elastic == 1) ? m->dt * f->mu_n[c0] : 1.0;
+    double Exx, Ezz, Exz, d1 = 0, d2 = 0;
+    orc_pt pt;
+    memset(&pt, 0, sizeof(pt));
+    if (!aniso) {
+      Exx = f->exxd[c0] + el * f->sxxd0[c0] / eta_e / 2.0;
+      Ezz = f->ezzd[c0] + el * f->szzd0[c0] / eta_e / 2.0;
+      Exz = f->exz_n[c0] + el * f->sxz0_n[c0] / eta_e / 2.0;
+    } else {
+      d1 = f->d1_n[c0]; d2 = f->d2_n[c0];
+      const double angle = f->angle_n[c0], lay = angle - M_PI / 2.0;
+      pt.lxlz = cos(lay) * sin(lay); pt.lx2 = cos(lay) * cos(lay); pt.angle = angle;
+      pt.ani_fac = f->aniso_factor_n[c0];
+      const double aniS_e = 1.0 - 1.0 / f->aniso_factor_n[c0];
+      orc_effective_strain_rate(&Exx, &Ezz, &Exz, f->exxd[c0], f->ezzd[c0], f->exz_n[c0], f->sxxd0[c0],
+                                f->szzd0[c0], f->sxz0_n[c0], d1, d2, aniS_e, eta_e, m->elastic);
+    }
+    pt.G = f->mu_n[c0]; pt.T = f->T[c0]; pt.P = f->p_in[c0]; pt.d = f->d0_n[c0];
+    pt.phi = f->phi0_n[c0]; pt.X0 = f->X0_n[c0]; pt.Exx = Exx; pt.Ezz = Ezz; pt.Exz = Exz;
+    pt.Txx0 = f->sxxd0[c0]; pt.Tzz0 = f->szzd0[c0]; pt.Txz0 = f->sxz0_n[c0]; pt.dil = f->dil_n[c0];
+    pt.fric = f->fric_n[c0]; pt.C = f->C_n[c0]; pt.P0 = f->p0_n[c0]; pt.T0 = f->T0_n[c0];
+    pt.beta = f->bet_n[c0]; pt.post_process = 1; pt.centroid = 1; pt.final_update = final_update;
+    for (int p = 0; p < np; p++) {
+      const double perc = f->phase_perc_n[p][c0];
+      if (!(fabs(perc) > 1e-13)) continue;                 /* :1210-1212 */
+      orc_res r;
+      pt.phase = p;
+      if (aniso) orc_viscosity_concise_aniso(m, mt, &pt, &r);
+      else       orc_viscosity_concise(m, mt, &pt, &r);
+      acc_error(&acc, r.status, c0);
+      calls++; iters += (uint64_t)r.iters; plastic += (uint64_t)r.is_pl;
+      if ((uint32_t)r.iters > maxit) maxit = (uint32_t)r.iters;
+      if (iters_n) iters_n[(int64_t)p * Nc + c0] = r.iters;
+      f->phase_eta_n[p][c0] = r.etaVE;
+      switch (avg) {
+        case 0: f->eta_n[c0] += perc * r.etaVE; f->eta_phys_n[c0] += perc * r.eta; break;
+        case 1: f->eta_n[c0] += perc * 1.0 / r.etaVE; f->eta_phys_n[c0] += perc * 1.0 / r.eta; break;
+        case 2: f->eta_n[c0] += perc * log(r.etaVE); f->eta_phys_n[c0] += perc * log(r.eta); break;
+      }
+      if (aniso) f->VE_n[c0] += perc * r.etaVE / eta_e;
+      else       f->VE_n[c0] += perc * r.VEcoeff;
+      f->eII_el[c0] += perc * r.Eii_el;
+      f->eII_pl[c0] += perc * r.Eii_pl;
+      f->eII_pwl[c0] += perc * r.Eii_pwl;
+      f->eII_exp[c0] += perc * r.Eii_exp;
+      f->eII_lin[c0] += perc * r.Eii_lin;
+      f->eII_gbs[c0] += perc * r.Eii_gbs;
+      f->eII_cst[c0] += perc * r.Eii_cst;
+      f->d_n[c0] += perc * 1.0 / r.d1;
+      f->Wtot[c0] += perc * r.Wtot;
+      f->Wdiss[c0] += perc * r.Wdiss;
+      f->Wel[c0] += perc * r.Wel;
+      f->p_corr[c0] += perc * r.Pcorr;
+      f->div_u_el[c0] += perc * r.div_el;
+      f->div_u_pl[c0] += perc * r.div_pl;
+      f->div_u_r[c0] += perc * r.div_r;
+      f->X_n[c0] += perc * r.X1;
+      f->OverS_n[c0] += perc * r.OverS;
+      if (m->density_variations == 1) f->rho_n[c0] += perc * (aniso ? 0.0 : r.rho);
+    }
+    f->d_n[c0] = 1.0 / f->d_n[c0];
+    if (!aniso && (isinf(f->d_n[c0]) || isnan(f->d_n[c0]))) acc_error(&acc, MDZ_EEMPTY_CELL, c0);
+    if (avg == 1) {
+      f->eta_n[c0] = 1.0 / f->eta_n[c0];
+      f->eta_phys_n[c0] = 1.0 / f->eta_phys_n[c0];
+      if (isinf(f->eta_phys_n[c0]) || isnan(f->eta_phys_n[c0])) acc_error(&acc, MDZ_ENONFINITE, c0);
+    }
+    if (avg == 2) {
+      f->eta_n[c0] = exp(f->eta_n[c0]);
+      f->eta_phys_n[c0] = exp(f->eta_phys_n[c0]);
+    }
+    if (!aniso) {                                          /* :1311-1313 */
+      f->sxxd[c0] = 2.0 * f->eta_n[c0] * Exx;
+      f->szzd[c0] = 2.0 * f->eta_n[c0] * Ezz;
+      f->sxz_n[c0] = 2.0 * f->eta_n[c0] * Exz;
+    } else {                                               /* AnisotropyRoutines.c:1079-1086 */
+      const double a = 1.0 - 1.0 / f->aniso_factor_n[c0];
+      const double Dxx = Exx * (1.0 - a * d1) + Ezz * a * d1 - 2.0 * Exz * a * d2;
+      const double Dzz = Ezz * (1.0 - a * d1) + Exx * a * d1 + 2.0 * Exz * a * d2;
+      const double Dxz = -Exx * a * d2 + Ezz * a * d2 + 2 * Exz * (a * (d1 - 0.5) + 0.5);
+      f->sxxd[c0] = 2.0 * f->eta_n[c0] * Dxx;
+      f->szzd[c0] = 2.0 * f->eta_n[c0] * Dzz;
+      f->sxz_n[c0] = 2.0 * f->eta_n[c0] * Dxz;
+    }
+  }
+
+#pragma omp parallel for reduction(+ : calls, iters, plastic) reduction(max : maxit)
+  for (int c1 = 0; c1 < Nv; c1++) {
+    f->sxxd_s[c1] = 0.0; f->szzd_s[c1] = 0.0; f->sxz[c1] = 0.0;
+    f->eta_phys_s[c1] = 0.0; f->eta_s[c1] = 0.0; f->X_s[c1] = 0.0;
+    if (aniso && f->VE_s) f->VE_s[c1] = 0.0;
+    if (iters_s) for (int p = 0; p < np; p++) iters_s[(int64_t)p * Nv + c1] = 0;
+    if (f->BCg_type[c1] == 30) continue;
+    const double eta_e = (m->elastic == 1) ? m->dt * f->mu_s[c1] : 1.0;
+    double Exx, Ezz, Exz, d1 = 0, d2 = 0;
+    orc_pt pt;
+    memset(&pt, 0, sizeof(pt));
+    if (!aniso) {
+      Exx = f->exxd_s[c1] + el * f->sxxd0_s[c1] / eta_e / 2.0;
+      Ezz = f->ezzd_s[c1] + el * f->szzd0_s[c1] / eta_e / 2.0;
+      Exz = f->exz[c1] + el * f->sxz0[c1] / eta_e / 2.0;
+    } else {
+      d1 = f->d1_s[c1]; d2 = f->d2_s[c1];
+      const double angle = f->angle_s[c1], lay = angle - M_PI / 2.0;
+      pt.lxlz = cos(lay) * sin(lay); pt.lx2 = cos(lay) * cos(lay); pt.angle = angle;
+      pt.ani_fac = f->aniso_factor_s[c1];
+      const double aniS_e = 1.0 - 1.0 / f->aniso_factor_s[c1];
+      orc_effective_strain_rate(&Exx, &Ezz, &Exz, f->exxd_s[c1], f->ezzd_s[c1], f->exz[c1],
+                                f->sxxd0_s[c1], f->szzd0_s[c1], f->sxz0[c1], d1, d2, aniS_e, eta_e,
+                                m->elastic);
+    }
+    pt.G = f->mu_s[c1]; pt.T = f->T_s[c1]; pt.P = f->P_s[c1]; pt.d = f->d0_s[c1];
+    pt.phi = f->phi0_s[c1]; pt.X0 = f->X0_s[c1]; pt.Exx = Exx; pt.Ezz = Ezz; pt.Exz = Exz;
+    pt.Txx0 = f->sxxd0_s[c1]; pt.Tzz0 = f->szzd0_s[c1]; pt.Txz0 = f->sxz0[c1]; pt.dil = f->dil_s[c1];
+    pt.fric = f->fric_s[c1]; pt.C = f->C_s[c1]; pt.P0 = f->p0_s[c1]; pt.T0 = 0.0;
+    pt.beta = f->bet_s[c1]; pt.post_process = 1; pt.centroid = 0; pt.final_update = final_update;
+    for (int p = 0; p < np; p++) {
+      const double perc = f->phase_perc_s[p][c1];
+      if (!(fabs(perc) > 1e-13)) continue;
+      orc_res r;
+      pt.phase = p;
+      if (aniso) orc_viscosity_concise_aniso(m, mt, &pt, &r);
+      else       orc_viscosity_concise(m, mt, &pt, &r);
+      acc_error(&acc, r.status, (int64_t)Nc + c1);
+      calls++; iters += (uint64_t)r.iters; plastic += (uint64_t)r.is_pl;
+      if ((uint32_t)r.iters > maxit) maxit = (uint32_t)r.iters;
+      if (iters_s) iters_s[(int64_t)p * Nv + c1] = r.iters;
+      f->phase_eta_s[p][c1] = r.etaVE;
+      switch (avg) {
+        case 0: f->eta_s[c1] += perc * r.etaVE; f->eta_phys_s[c1] += perc * r.eta; break;
+        case 1: f->eta_s[c1] += perc * 1.0 / r.etaVE; f->eta_phys_s[c1] += perc * 1.0 / r.eta; break;
+        case 2: f->eta_s[c1] += perc * log(r.etaVE); f->eta_phys_s[c1] += perc * log(r.eta); break;
+      }
+      if (aniso && f->VE_s) f->VE_s[c1] += perc * r.etaVE / eta_e;
+      f->X_s[c1] += perc * r.X1;
+    }
+    if (avg == 1) {
+      f->eta_s[c1] = 1.0 / f->eta_s[c1];
+      f->eta_phys_s[c1] = 1.0 / f->eta_phys_s[c1];
+      if (isinf(f->eta_phys_s[c1]) || isnan(f->eta_phys_s[c1])) acc_error(&acc, MDZ_ENONFINITE, (int64_t)Nc + c1);
+    }
+    if (avg == 2) {
+      f->eta_s[c1] = exp(f->eta_s[c1]);
+      f->eta_phys_s[c1] = exp(f->eta_phys_s[c1]);
+    }
+    if (!aniso) {
+      f->sxxd_s[c1] = 2.0 * f->eta_s[c1] * Exx;
+      f->szzd_s[c1] = 2.0 * f->eta_s[c1] * Ezz;
+      f->sxz[c1] = 2.0 * f->eta_s[c1] * Exz;
+    } else {
+      const double a = 1.0 - 1.0 / f->aniso_factor_s[c1];
+      const double Dxx = Exx * (1.0 - a * d1) + Ezz * a * d1 - 2.0 * Exz * a * d2;
+      const double Dzz = Ezz * (1.0 - a * d1) + Exx * a * d1 + 2.0 * Exz * a * d2;
+      const double Dxz = -Exx * a * d2 + Ezz * a * d2 + 2 * Exz * (a * (d1 - 0.5) + 0.5);
+      f->sxxd_s[c1] = 2.0 * f->eta_s[c1] * Dxx;
+      f->szzd_s[c1] = 2.0 * f->eta_s[c1] * Dzz;
+      f->sxz[c1] = 2.0 * f->eta_s[c1] * Dxz;
+    }
+  }
+  acc.calls = calls; acc.iters = iters; acc.plastic = plastic; acc.maxit = maxit;
+  fill_stats(stats, &acc);
+  return acc.status;
+}
+
+int orc_sweep(const mdz_model *m, const mdz_materials *mt, const mdz_grid_fields *f, int fu,
+              int32_t *in_, int32_t *is_, mdz_sweep_stats *s) {
+  return orc_sweep_impl(m, mt, f, fu, in_, is_, s, 0);
+}
+
+int orc_sweep_aniso(const mdz_model *m, const mdz_materials *mt, const mdz_grid_fields *f, int fu,
+                    int32_t *in_, int32_t *is_, mdz_sweep_stats *s) {
+  return orc_sweep_impl(m, mt, f, fu, in_, is_, s, 1);
+}
+
+int orc_points(const mdz_model *m, const mdz_materials *mt, const mdz_point_inputs *in,
+               mdz_point_outputs *out, int64_t n, int aniso) {
+  int status = MDZ_OK;
+#pragma omp parallel for
+  for (int64_t i = 0; i < n; i++) {
+    orc_pt pt;
+    memset(&pt, 0, sizeof(pt));
+    pt.phase = in->phase[i]; pt.G = in->G[i]; pt.T = in->T[i]; pt.P = in->P[i]; pt.d = in->d[i];
+    pt.phi = in->phi[i]; pt.X0 = in->X0[i]; pt.Exx = in->Exx[i]; pt.Ezz = in->Ezz[i];
+    pt.Exz = in->Exz[i]; pt.Txx0 = in->Txx0[i]; pt.Tzz0 = in->Tzz0[i]; pt.Txz0 = in->Txz0[i];
+    pt.dil = in->dil[i]; pt.fric = in->fric[i]; pt.C = in->C[i]; pt.P0 = in->P0[i];
+    pt.T0 = in->T0[i]; pt.beta = in->beta[i];
+    if (aniso) { pt.lxlz = in->lxlz[i]; pt.lx2 = in->lx2[i]; pt.angle = in->angle[i]; pt.ani_fac = in->ani_fac[i]; }
+    pt.post_process = in->post_process; pt.centroid = in->centroid; pt.final_update = in->final_update;
+    orc_res r;
+    if (aniso) orc_viscosity_concise_aniso(m, mt, &pt, &r);
+    else       orc_viscosity_concise(m, mt, &pt, &r);
+    double *dst[24] = {out->eta, out->Txx, out->Tzz, out->Txz, out->etaVE, out->VEcoeff, out->Eii_el,
+                       out->Eii_pl, out->Eii_pwl, out->Eii_exp, out->Eii_lin, out->Eii_gbs,
+                       out->Eii_cst, out->d1, out->X1, out->OverS, out->Pcorr, out->rho,
+                       out->div_el, out->div_pl, out->div_r, out->Wtot, out->Wel, out->Wdiss};
+    const double src[24] = {r.eta, r.Txx, r.Tzz, r.Txz, r.etaVE, r.VEcoeff, r.Eii_el, r.Eii_pl,
+                            r.Eii_pwl, r.Eii_exp, r.Eii_lin, r.Eii_gbs, r.Eii_cst, r.d1, r.X1,
+                            r.OverS, r.Pcorr, r.rho, r.div_el, r.div_pl, r.div_r, r.Wtot, r.Wel,
+                            r.Wdiss};
+    for (int j = 0; j < 24; j++) if (dst[j]) dst[j][i] = src[j];
+    if (out->iters) out->iters[i] = r.iters;
+    if (out->status) out->status[i] = r.status;
+    if (r.status != MDZ_OK) {
+#pragma omp critical(orc_pts)
+      if (status == MDZ_OK) status = r.status;
+    }
+  }
+  return status;
+}
