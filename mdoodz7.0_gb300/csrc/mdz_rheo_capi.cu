@@ -1,0 +1,514 @@
+// mdz_rheo_capi.cu -- the C ABI of include/mdz_rheo.h.
+//
+// A context owns one CUDA stream, a device statistics block and, for host-memory
+// sweeps, device mirrors of the grid fields (grown on demand, kept until destroy).
+// Per-phase material constants are folded here, once per call, into the PhaseConst
+// table the kernels read from their constant parameter bank.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "rheo_kernels.cuh"
+
+using namespace mdz;
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+struct mdz_rheo_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DevStats *d_stats = nullptr, *h_stats = nullptr;
+  std::vector<DevBuf> bufs;
+  int32_t *d_iters_n = nullptr, *d_iters_s = nullptr;
+  size_t cap_iters_n = 0, cap_iters_s = 0;
+  long long last_Nc = 0, last_Nv = 0;
+  int last_np = 0, have_iters = 0, pending = 0;
+  int block = 128, grid_cap = 0;
+};
+
+namespace {
+
+#define CK(x)                                                                 \
+  do {                                                                        \
+    cudaError_t e_ = (x);                                                     \
+    if (e_ != cudaSuccess) {                                                  \
+      fprintf(stderr, "mdz_rheo: %s failed: %s\n", #x, cudaGetErrorString(e_)); \
+      return MDZ_ECUDA;                                                       \
+    }                                                                         \
+  } while (0)
+
+int ensure(DevBuf &b, size_t bytes) {
+  if (b.cap >= bytes) return MDZ_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  if (cudaMalloc(&b.p, bytes) != cudaSuccess) return MDZ_ENOMEM;
+  b.cap = bytes;
+  return MDZ_OK;
+}
+
+// PhaseConst from one column of mat_prop (flow-law conventions of
+// MDLIB/RheologyDensity.c:501-539 folded into logs; see rheo_device.cuh).
+void fold_phase(const mdz_materials *m, const mdz_model *md, int p, PhaseConst &c) {
+  memset(&c, 0, sizeof(c));
+  int fl = 0;
+  if (m->cstv[p] != 0) fl |= F_CST;
+  if (m->pwlv[p] != 0) fl |= F_PWL;
+  if (m->expv[p] != 0) fl |= F_EXPV;
+  if (m->linv[p] != 0) fl |= F_LIN;
+  if (m->gbsv[p] != 0) fl |= F_GBS;
+  if (m->gs[p] != 0) fl |= F_GS;
+  if (m->plast[p] == 1) fl |= F_PL1;
+  if (m->plast[p] == 2) fl |= F_PL2;
+  if (m->plast[p] != 0) fl |= F_PLANY;
+  if (m->phase_mix[p] == 1 && md->diffuse_X != 0) fl |= F_CMIX;
+  if (m->nlin[p] == 1.0) fl |= F_LIN1;
+  if (m->mpwl[p] != 0.0) fl |= F_PWL_M;
+  if (m->apwl[p] != 0.0) fl |= F_PWL_A;
+  if (m->alin[p] != 0.0) fl |= F_LIN_A;
+  if (1.0 / m->n_vp[p] - 1.0 == 0.0) fl |= F_VP1;
+  c.flags = fl;
+  c.density_model = m->density_model[p];
+  c.phase_two = m->phase_two[p];
+  c.reac_phase = m->reac_phase[p];
+  const double R = m->R;
+  // dislocation: B = pref F A^(-1/n) exp((Q+PV)/(R n T)) d^(m/n) f^(-r/n) exp(-a phi/n)
+  {
+    const double n = m->npwl[p];
+    c.pwl_n = n;
+    c.pwl_lnK = log(m->pref_pwl[p]) + log(m->Fpwl[p]) - log(m->Apwl[p]) / n;
+    if (m->rpwl[p] != 0.0) c.pwl_lnK += -(m->rpwl[p] / n) * log(m->fpwl[p]);
+    c.pwl_Q = m->Qpwl[p]; c.pwl_V = m->Vpwl[p]; c.pwl_invRn = 1.0 / (R * n);
+    c.pwl_mn = m->mpwl[p] / n; c.pwl_an = m->apwl[p] / n;
+    c.pwl_A = m->Apwl[p]; c.pwl_pref = m->pref_pwl[p]; c.pwl_F = m->Fpwl[p]; c.pwl_m = m->mpwl[p];
+    c.pwl_r = m->rpwl[p]; c.pwl_f = m->fpwl[p]; c.pwl_a = m->apwl[p];
+  }
+  // diffusion: B = F A^(-1/n) exp((Q+PV)/(R n T)) f^(-r/n) exp(-a phi/n)
+  {
+    const double n = m->nlin[p];
+    c.lin_n = n;
+    c.lin_lnK = log(m->Flin[p]) - log(m->Alin[p]) / n;
+    if (m->rlin[p] != 0.0) c.lin_lnK += -(m->rlin[p] / n) * log(m->flin[p]);
+    c.lin_Q = m->Qlin[p]; c.lin_V = m->Vlin[p]; c.lin_invRn = 1.0 / (R * n);
+    c.lin_m = m->mlin[p]; c.lin_mn = m->mlin[p] / n; c.lin_an = m->alin[p] / n;
+    c.lin_A = m->Alin[p]; c.lin_F = m->Flin[p]; c.lin_r = m->rlin[p]; c.lin_f = m->flin[p]; c.lin_a = m->alin[p];
+  }
+  // grain-boundary sliding
+  {
+    const double n = m->ngbs[p];
+    c.gbs_n = n;
+    c.gbs_lnK = log(m->Fgbs[p]) - log(m->Agbs[p]) / n;
+    if (m->rgbs[p] != 0.0) c.gbs_lnK += -(m->rgbs[p] / n) * log(m->fgbs[p]);
+    c.gbs_Q = m->Qgbs[p]; c.gbs_V = m->Vgbs[p]; c.gbs_invRn = 1.0 / (R * n);
+    c.gbs_m = m->mgbs[p]; c.gbs_mn = m->mgbs[p] / n; c.gbs_an = m->agbs[p] / n;
+    c.gbs_A = m->Agbs[p]; c.gbs_F = m->Fgbs[p]; c.gbs_r = m->rgbs[p]; c.gbs_f = m->fgbs[p]; c.gbs_a = m->agbs[p];
+  }
+  // Peierls
+  {
+    const double g = m->Gexp[p];
+    c.exp_Ea = m->Qexp[p]; c.exp_EaR = m->Qexp[p] / R; c.exp_g2 = 2.0 * g * (1 - g);
+    c.exp_om2 = (1.0 - g) * (1.0 - g); c.exp_n = m->nexp[p]; c.exp_lngS = log(g * m->Sexp[p]);
+    c.exp_lnE = log(m->Eexp[p]); c.exp_gamma = g; c.exp_S = m->Sexp[p]; c.exp_E = m->Eexp[p];
+  }
+  c.eta0 = m->eta0[p];
+  const int p2 = m->phase_two[p];
+  c.eta0_two = (p2 >= 0 && p2 < MDZ_MAX_PHASES) ? m->eta0[p2] : m->eta0[p];
+  c.Slim = m->Slim[p]; c.eta_vp = m->eta_vp[p]; c.n_vp = m->n_vp[p]; c.T_st = m->T_st[p];
+  c.gs_ref = m->gs_ref[p]; c.ln_gs_ref = log(m->gs_ref[p]);
+  c.Kpzm = m->Kpzm[p]; c.Qpzm = m->Qpzm[p]; c.Gpzm = m->Gpzm[p]; c.Lpzm = m->Lpzm[p];
+  c.cpzm = m->cpzm[p]; c.ppzm = m->ppzm[p];
+  c.rho = m->rho[p]; c.drho = m->drho[p]; c.alp = m->alp[p]; c.bet = m->bet[p]; c.T0 = m->T0[p]; c.P0 = m->P0[p];
+  const int rp = m->reac_phase[p];
+  c.rho_reac = (rp >= 0 && rp < MDZ_MAX_PHASES) ? m->rho[rp] : m->rho[p];
+}
+
+int fold_model(const mdz_model *md, const mdz_materials *m, ModelConst &M) {
+  memset(&M, 0, sizeof(M));
+  if (md->Nb_phases < 1 || md->Nb_phases > MDZ_MAX_PHASES) return MDZ_EINVAL;
+  if (md->melting || md->chemical_production) return MDZ_EUNSUPPORTED;
+  M.np = md->Nb_phases;
+  M.elastic = md->elastic; M.step = md->step; M.eta_average = md->eta_average;
+  M.periodic_x = md->periodic_x; M.density_variations = md->density_variations;
+  M.tensile_line_search = md->tensile_line_search; M.diffuse_avg = md->diffuse_avg;
+  M.Nx = md->Nx; M.Nz = md->Nz; M.Ncx = md->Nx - 1; M.Ncz = md->Nz - 1;
+  M.Nc = (long long)M.Ncx * M.Ncz; M.Nv = (long long)M.Nx * M.Nz;
+  M.dt_model = md->dt;
+  M.dt = (md->step == 0) ? 1e100 : md->dt;  // RheologyDensity.c:392-394
+  M.min_eta = md->min_eta; M.max_eta = md->max_eta; M.eta_tol = md->eta_tol; M.R = m->R;
+  M.scale_eta = md->scale_eta; M.scale_L = md->scale_L; M.scale_T = md->scale_T; M.scale_S = md->scale_S;
+  M.scale_E = md->scale_E;
+  M.TmaxPeierls = (1200.0 + kZeroC) / md->scale_T;
+  M.Tmin = kZeroC / md->scale_T;
+  M.Tiimin = 1e5 / md->scale_S;
+  M.Eii_floor = 1e-30 / md->scale_E;
+  M.eta_up0 = 1.0e100 / md->scale_eta;
+  M.eta_lo0 = -1.0e100 / md->scale_eta;
+  M.d_min = 1e-13 / md->scale_L;
+  for (int p = 0; p < M.np; p++) {
+    const int dm = m->density_model[p];
+    if (md->density_variations == 1 && (dm == 2 || dm == 4)) return MDZ_EUNSUPPORTED;
+  }
+  return MDZ_OK;
+}
+
+bool need_lnd(const mdz_materials *m, int np) {
+  for (int p = 0; p < np; p++) {
+    if (m->pwlv[p] && m->mpwl[p] != 0.0) return true;
+    if (m->linv[p] && m->mlin[p] != 0.0) return true;
+    if (m->gbsv[p] && m->mgbs[p] != 0.0) return true;
+  }
+  return false;
+}
+
+int stats_from_device(mdz_rheo_ctx *ctx, mdz_sweep_stats *st, float ms) {
+  const DevStats &h = *ctx->h_stats;
+  int status = MDZ_OK;
+  long long node = -1;
+  if (h.err_key != ~0ull) {
+    status = -(int)(h.err_key & 0xff);
+    node = (long long)(h.err_key >> 8);
+  }
+  if (st) {
+    st->phase_calls = h.calls; st->newton_iters = h.iters; st->max_newton_iters = h.maxit;
+    st->plastic_calls = h.plastic; st->status = status; st->error_node = node; st->elapsed_ms = ms;
+  }
+  return status;
+}
+
+int reset_stats(mdz_rheo_ctx *ctx) {
+  DevStats init;
+  memset(&init, 0, sizeof(init));
+  init.err_key = ~0ull;
+  *ctx->h_stats = init;
+  CK(cudaMemcpyAsync(ctx->d_stats, ctx->h_stats, sizeof(DevStats), cudaMemcpyHostToDevice, ctx->stream));
+  return MDZ_OK;
+}
+
+int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
+  CK(cudaMemcpyAsync(ctx->h_stats, ctx->d_stats, sizeof(DevStats), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  return stats_from_device(ctx, st, ms);
+}
+
+// slot numbering of the host-mode mirrors
+enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
+       S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
+       S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_COUNT };
+
+struct Mirror {
+  mdz_rheo_ctx *ctx;
+  int err = MDZ_OK;
+  // upload (if host) a read-only array of n elements of `es` bytes into slot s
+  template <class T>
+  T *in(const T *h, int slot, size_t n, bool host) {
+    if (!h || err) return const_cast<T *>(h);
+    if (!host) return const_cast<T *>(h);
+    if ((err = ensure(ctx->bufs[slot], n * sizeof(T))) != MDZ_OK) return nullptr;
+    if (cudaMemcpyAsync(ctx->bufs[slot].p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+      err = MDZ_ECUDA;
+    return (T *)ctx->bufs[slot].p;
+  }
+  template <class T>
+  T *out(T *h, int slot, size_t n, bool host) {
+    if (!h || err) return h;
+    if (!host) return h;
+    if ((err = ensure(ctx->bufs[slot], n * sizeof(T))) != MDZ_OK) return nullptr;
+    return (T *)ctx->bufs[slot].p;
+  }
+  template <class T>
+  void back(T *h, int slot, size_t n, bool host) {
+    if (!h || err || !host) return;
+    if (cudaMemcpyAsync(h, ctx->bufs[slot].p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess)
+      err = MDZ_ECUDA;
+  }
+};
+
+int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat, const mdz_grid_fields *f,
+               int final_update, int mem, int flags, mdz_sweep_stats *st, bool aniso) {
+  if (!ctx || !md || !mat || !f) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (flags & MDZ_SWEEP_WARMSTART) return MDZ_ENOTREADY;
+  if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  static thread_local SweepArgs A;  // large: keep off the stack
+  memset(&A, 0, sizeof(A));
+  int rc = fold_model(md, mat, A.M);
+  if (rc != MDZ_OK) return rc;
+  for (int p = 0; p < A.M.np; p++) fold_phase(mat, md, p, A.ph[p]);
+  A.final_update = final_update;
+  A.need_lnd = need_lnd(mat, A.M.np);
+  const size_t Nc = (size_t)A.M.Nc, Nv = (size_t)A.M.Nv;
+  const int np = A.M.np;
+  const bool host = (mem == MDZ_MEM_HOST);
+  // required inputs
+  const double *cin[CI_COUNT] = {f->mu_n, f->T, f->p_in, f->d0_n, f->phi0_n, f->X0_n, f->exxd, f->ezzd, f->exz_n,
+                                 f->sxxd0, f->szzd0, f->sxz0_n, f->fric_n, f->C_n, f->dil_n, f->p0_n, f->T0_n,
+                                 f->bet_n, f->d1_n, f->d2_n, f->angle_n, f->aniso_factor_n};
+  const double *vin[VI_COUNT] = {f->mu_s, f->X0_s, f->exxd_s, f->ezzd_s, f->exz, f->sxxd0_s, f->szzd0_s, f->sxz0,
+                                 f->fric_s, f->C_s, f->dil_s, f->p0_s, f->bet_s, f->d1_s, f->d2_s, f->angle_s,
+                                 f->aniso_factor_s};
+  const int nci = aniso ? CI_COUNT : CI_d1, nvi = aniso ? VI_COUNT : VI_d1;
+  for (int i = 0; i < nci; i++) if (!cin[i]) return MDZ_EINVAL;
+  for (int i = 0; i < nvi; i++) if (!vin[i]) return MDZ_EINVAL;
+  if (!f->phase_perc_n || !f->phase_perc_s || !f->phase_eta_n || !f->phase_eta_s || !f->BCp_type || !f->BCg_type)
+    return MDZ_EINVAL;
+  double *cout[CO_COUNT] = {f->eta_n, f->eta_phys_n, f->VE_n, f->sxxd, f->szzd, f->sxz_n, f->eII_el, f->eII_pl,
+                            f->eII_pwl, f->eII_exp, f->eII_lin, f->eII_gbs, f->eII_cst, f->d_n, f->p_corr,
+                            f->div_u_el, f->div_u_pl, f->div_u_r, f->Wtot, f->Wel, f->Wdiss, f->X_n, f->OverS_n,
+                            md->density_variations == 1 ? f->rho_n : nullptr};
+  for (int i = 0; i < CO_rho; i++) if (!cout[i]) return MDZ_EINVAL;
+  if (md->density_variations == 1 && !f->rho_n) return MDZ_EINVAL;
+  double *vout[VO_COUNT] = {f->sxxd_s, f->szzd_s, f->sxz, f->eta_phys_s, f->eta_s, f->X_s,
+                            aniso ? f->VE_s : nullptr, f->T_s, f->P_s, f->d0_s, f->phi0_s};
+  for (int i = 0; i < VO_COUNT; i++) if (i != VO_VE && !vout[i]) return MDZ_EINVAL;
+  if (aniso && !f->VE_s) return MDZ_EINVAL;
+
+  Mirror mi{ctx};
+  for (int i = 0; i < nci; i++) A.ci[i] = mi.in(cin[i], S_CI + i, Nc, host);
+  for (int i = 0; i < nvi; i++) A.vi[i] = mi.in(vin[i], S_VI + i, Nv, host);
+  for (int p = 0; p < np; p++) {
+    A.perc_n[p] = mi.in(f->phase_perc_n[p], S_PN + p, Nc, host);
+    A.perc_s[p] = mi.in(f->phase_perc_s[p], S_PS + p, Nv, host);
+    // phase_eta of inactive phases keeps its previous value, as in the reference
+    A.peta_n[p] = (double *)mi.in((const double *)f->phase_eta_n[p], S_EN + p, Nc, host);
+    A.peta_s[p] = (double *)mi.in((const double *)f->phase_eta_s[p], S_ES + p, Nv, host);
+  }
+  A.bcp = mi.in(f->BCp_type, S_BCP, Nc, host);
+  A.bcg = mi.in(f->BCg_type, S_BCG, Nv, host);
+  for (int i = 0; i < CO_COUNT; i++) A.co[i] = mi.out(cout[i], S_CO + i, Nc, host);
+  for (int i = 0; i < VO_COUNT; i++) A.vo[i] = mi.out(vout[i], S_VO + i, Nv, host);
+  if (mi.err) return mi.err;
+  if (flags & MDZ_SWEEP_ITERS) {
+    const size_t bn = Nc * np * sizeof(int32_t), bs = Nv * np * sizeof(int32_t);
+    if (ctx->cap_iters_n < bn) {
+      cudaFree(ctx->d_iters_n);
+      ctx->d_iters_n = nullptr; ctx->cap_iters_n = 0;
+      CK(cudaMalloc(&ctx->d_iters_n, bn));
+      ctx->cap_iters_n = bn;
+    }
+    if (ctx->cap_iters_s < bs) {
+      cudaFree(ctx->d_iters_s);
+      ctx->d_iters_s = nullptr; ctx->cap_iters_s = 0;
+      CK(cudaMalloc(&ctx->d_iters_s, bs));
+      ctx->cap_iters_s = bs;
+    }
+    A.iters_n = ctx->d_iters_n; A.iters_s = ctx->d_iters_s;
+    ctx->have_iters = 1;
+    ctx->last_Nc = A.M.Nc; ctx->last_Nv = A.M.Nv; ctx->last_np = np;
+  }
+  A.stats = ctx->d_stats;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_sweep(A, aniso, ctx->stream, ctx->block, ctx->grid_cap));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  for (int i = 0; i < CO_COUNT; i++) mi.back(cout[i], S_CO + i, Nc, host);
+  for (int i = 0; i < VO_COUNT; i++) mi.back(vout[i], S_VO + i, Nv, host);
+  for (int p = 0; p < np; p++) {
+    mi.back(f->phase_eta_n[p], S_EN + p, Nc, host);
+    mi.back(f->phase_eta_s[p], S_ES + p, Nv, host);
+  }
+  if (mi.err) return mi.err;
+  if (flags & MDZ_SWEEP_ASYNC) {
+    ctx->pending = 1;
+    return MDZ_OK;
+  }
+  return finish(ctx, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdz_rheo_version(void) { return MDZ_RHEO_ABI_VERSION; }
+
+void mdz_rheo_abi_sizes(size_t out[8]) {
+  out[0] = sizeof(mdz_materials); out[1] = sizeof(mdz_model); out[2] = sizeof(mdz_grid_fields);
+  out[3] = sizeof(mdz_sweep_stats); out[4] = sizeof(mdz_point_inputs); out[5] = sizeof(mdz_point_outputs);
+  out[6] = 0; out[7] = 0;
+}
+
+const char *mdz_rheo_status_string(int s) {
+  switch (s) {
+    case MDZ_OK: return "ok";
+    case MDZ_EINVAL: return "invalid argument";
+    case MDZ_ECUDA: return "CUDA error";
+    case MDZ_EUNSUPPORTED: return "unsupported option (melting, chemical production, tabulated density)";
+    case MDZ_ENOMEM: return "out of device memory";
+    case MDZ_ENOTREADY: return "not ready (warm start without weights?)";
+    case MDZ_EVE_ITER: return "Visco-Elastic iterations failed!";
+    case MDZ_EGSE_ITER: return "GSE local iter failed to converge";
+    case MDZ_ESINGULAR: return "Singular Jacobian in Newton local solve";
+    case MDZ_EEMPTY_CELL: return "Cell went empty";
+    case MDZ_ENONFINITE: return "Inf/NaN viscosity";
+    case MDZ_EWDISS: return "negative dissipation";
+    case MDZ_EGRAIN_ZERO: return "grain size dependent viscosity with zero grain size";
+    case MDZ_ELINESEARCH: return "tensile plasticity line search failed (alpha < 0.01)";
+    case MDZ_EANISO_NAN: return "anisotropic VE residual is NaN";
+    case MDZ_EANISO_ITER: return "anisotropic Visco-Elastic iterations failed";
+    default: return "unknown status";
+  }
+}
+
+int mdz_rheo_create(int device, mdz_rheo_ctx **out) {
+  if (!out) return MDZ_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  CK(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return MDZ_EINVAL;
+  CK(cudaSetDevice(device));
+  mdz_rheo_ctx *c = new mdz_rheo_ctx();
+  c->device = device;
+  c->bufs.resize(S_COUNT);
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      cudaMalloc(&c->d_stats, sizeof(DevStats)) != cudaSuccess ||
+      cudaMallocHost(&c->h_stats, sizeof(DevStats)) != cudaSuccess) {
+    mdz_rheo_destroy(c);
+    return MDZ_ECUDA;
+  }
+  c->stream = c->own;
+  *out = c;
+  return MDZ_OK;
+}
+
+int mdz_rheo_destroy(mdz_rheo_ctx *c) {
+  if (!c) return MDZ_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto &b : c->bufs) if (b.p) cudaFree(b.p);
+  if (c->d_iters_n) cudaFree(c->d_iters_n);
+  if (c->d_iters_s) cudaFree(c->d_iters_s);
+  if (c->d_stats) cudaFree(c->d_stats);
+  if (c->h_stats) cudaFreeHost(c->h_stats);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return MDZ_OK;
+}
+
+int mdz_rheo_set_stream(mdz_rheo_ctx *c, void *stream) {
+  if (!c) return MDZ_EINVAL;
+  c->stream = stream ? (cudaStream_t)stream : c->own;
+  return MDZ_OK;
+}
+
+int mdz_rheo_sync(mdz_rheo_ctx *c, mdz_sweep_stats *st) {
+  if (!c) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  c->pending = 0;
+  return finish(c, st);
+}
+
+int mdz_rheo_sweep(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m, const mdz_grid_fields *f,
+                   int final_update, int mem, int flags, mdz_sweep_stats *st) {
+  return sweep_impl(c, md, m, f, final_update, mem, flags, st, false);
+}
+
+int mdz_rheo_sweep_aniso(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m, const mdz_grid_fields *f,
+                         int final_update, int mem, int flags, mdz_sweep_stats *st) {
+  return sweep_impl(c, md, m, f, final_update, mem, flags, st, true);
+}
+
+int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m, const mdz_point_inputs *in,
+                    mdz_point_outputs *out, int64_t n, int aniso, int mem) {
+  if (!c || !md || !m || !in || !out || n < 0) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  static thread_local PointArgs A;
+  memset(&A, 0, sizeof(A));
+  int rc = fold_model(md, m, A.M);
+  if (rc != MDZ_OK) return rc;
+  for (int p = 0; p < A.M.np; p++) fold_phase(m, md, p, A.ph[p]);
+  A.n = n;
+  A.aniso = aniso;
+  A.stats = c->d_stats;
+  if (n == 0) return MDZ_OK;
+  const bool host = (mem == MDZ_MEM_HOST);
+  std::vector<void *> tmp;
+  auto up = [&](const void *h, size_t bytes) -> void * {
+    if (!h) return nullptr;
+    if (!host) return const_cast<void *>(h);
+    void *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+    tmp.push_back(d);
+    cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream);
+    return d;
+  };
+  const size_t nb = (size_t)n * sizeof(double);
+  A.in = *in;
+  A.in.phase = (const int32_t *)up(in->phase, (size_t)n * sizeof(int32_t));
+  const double **pin[] = {&A.in.G, &A.in.T, &A.in.P, &A.in.d, &A.in.phi, &A.in.X0, &A.in.Exx, &A.in.Ezz,
+                          &A.in.Exz, &A.in.Txx0, &A.in.Tzz0, &A.in.Txz0, &A.in.strain_acc, &A.in.dil,
+                          &A.in.fric, &A.in.C, &A.in.P0, &A.in.T0, &A.in.beta, &A.in.div,
+                          &A.in.lxlz, &A.in.lx2, &A.in.angle, &A.in.ani_fac};
+  for (auto pp : pin) *pp = (const double *)up(*pp, nb);
+  // every input the kernel reads must be present
+  const void *req[] = {A.in.phase, A.in.G, A.in.T, A.in.P, A.in.d, A.in.phi, A.in.X0, A.in.Exx, A.in.Ezz,
+                       A.in.Exz, A.in.Txx0, A.in.Tzz0, A.in.Txz0, A.in.dil, A.in.fric, A.in.C, A.in.P0,
+                       A.in.T0, A.in.beta};
+  bool ok = true;
+  for (auto r : req) ok = ok && r;
+  if (aniso) ok = ok && A.in.lxlz && A.in.lx2 && A.in.ani_fac;
+  A.out = *out;
+  double **pout[] = {&A.out.eta, &A.out.Txx, &A.out.Tzz, &A.out.Txz, &A.out.etaVE, &A.out.VEcoeff,
+                     &A.out.Eii_el, &A.out.Eii_pl, &A.out.Eii_pwl, &A.out.Eii_exp, &A.out.Eii_lin,
+                     &A.out.Eii_gbs, &A.out.Eii_cst, &A.out.d1, &A.out.X1, &A.out.OverS, &A.out.Pcorr,
+                     &A.out.rho, &A.out.div_el, &A.out.div_pl, &A.out.div_r, &A.out.Wtot, &A.out.Wel,
+                     &A.out.Wdiss};
+  std::vector<std::pair<void *, void *>> backs;  // (host, device)
+  auto dn = [&](void *h, size_t bytes) -> void * {
+    if (!h) return nullptr;
+    if (!host) return h;
+    void *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+    tmp.push_back(d);
+    backs.push_back({h, d});
+    return d;
+  };
+  for (auto pp : pout) *pp = (double *)dn(*pp, nb);
+  A.out.iters = (int32_t *)dn(out->iters, (size_t)n * sizeof(int32_t));
+  A.out.status = (int32_t *)dn(out->status, (size_t)n * sizeof(int32_t));
+  if (ok) {
+    for (int p = 0; p < n && host; p++) {
+      if (in->phase[p] < 0 || in->phase[p] >= A.M.np) { ok = false; break; }
+    }
+  }
+  if (!ok) {
+    for (auto d : tmp) cudaFree(d);
+    return MDZ_EINVAL;
+  }
+  if ((rc = reset_stats(c)) != MDZ_OK) return rc;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(launch_points(A, c->stream));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  for (auto &b : backs) {
+    size_t bytes = (b.first == (void *)out->iters || b.first == (void *)out->status) ? (size_t)n * sizeof(int32_t) : nb;
+    cudaMemcpyAsync(b.first, b.second, bytes, cudaMemcpyDeviceToHost, c->stream);
+  }
+  rc = finish(c, nullptr);
+  for (auto d : tmp) cudaFree(d);
+  return rc;
+}
+
+int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {
+  if (!c || !c->have_iters) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (out_n) CK(cudaMemcpy(out_n, c->d_iters_n, (size_t)c->last_Nc * c->last_np * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (out_s) CK(cudaMemcpy(out_s, c->d_iters_s, (size_t)c->last_Nv * c->last_np * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return MDZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,821 @@
+// rheo_device.cuh -- device-side local rheology update (FP64) for sm_103a.
+//
+// One call of `point_iso` is one ViscosityConcise (MDLIB/RheologyDensity.c:385-1080);
+// `point_aniso` is ViscosityConciseAniso (MDLIB/AnisotropyRoutines.c:282-727).
+//
+// Design for GB300, where the FP64 pipe is the bound:
+//  * per-phase constants (pre-factors, 1/(R n), logs of A, F, f, ...) are folded on the
+//    host once per sweep (PhaseConst);
+//  * Arrhenius and Peierls pre-factors are formed in log space, so each creep
+//    mechanism costs one exp for its isolated viscosity instead of the reference's
+//    five to seven pow/exp calls, and C = (2B)^-n never leaves log space;
+//  * each Newton step evaluates log(Tii) once and one exp per non-linear mechanism
+//    (Newtonian laws are a multiply);
+//  * post-processing uses eta_k = Tii / (2 Eii_k), which is the reference's
+//    B_k * pow(Eii_k, 1/n_k - 1) rewritten with Eii_k = C_k Tii^n_k.
+// These are exact identities of the reference's formulas; results differ from the
+// reference only by rounding (about 1e-14 relative, checked by the parity tests).
+// The Newton iteration itself (start point, update, stopping test, iteration cap)
+// is the reference's, so iteration counts agree except where rounding moves a
+// residual across the stopping threshold.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mdz_rheo.h"
+
+namespace mdz {
+
+constexpr double kZeroC = 273.15;                 // MDLIB/include/mdoodz.h:4
+constexpr double kLn2 = 0.69314718055994530942;
+
+// mechanism / option bits of PhaseConst::flags
+enum : int {
+  F_CST = 1 << 0,   // cstv != 0
+  F_PWL = 1 << 1,   // pwlv != 0
+  F_EXPV = 1 << 2,  // expv != 0 (Peierls, still gated by T < TmaxPeierls)
+  F_LIN = 1 << 3,   // linv != 0
+  F_GBS = 1 << 4,   // gbsv != 0
+  F_GS = 1 << 5,    // gs != 0 (paleowattmeter grain size)
+  F_PL1 = 1 << 6,   // plast == 1
+  F_PL2 = 1 << 7,   // plast == 2
+  F_PLANY = 1 << 8, // plast != 0 (anisotropic path)
+  F_CMIX = 1 << 9,  // phase_mix with diffuse_X
+  F_LIN1 = 1 << 10, // nlin == 1: Newtonian diffusion creep (multiply, no exp)
+  F_PWL_M = 1 << 11,// mpwl != 0
+  F_PWL_A = 1 << 12,// apwl != 0
+  F_LIN_A = 1 << 13,// alin != 0
+  F_VP1 = 1 << 14,  // n_vp == 1 (pow(x, 1/n_vp - 1) == 1)
+};
+
+// Per-phase constants folded on the host (mdz_rheo_capi.cpp: fold_phase).
+struct PhaseConst {
+  int flags, density_model, phase_two, reac_phase;
+  // dislocation: ln B = lnK + (Q + P V) invRn / T + mn ln d - an phi
+  double pwl_n, pwl_lnK, pwl_Q, pwl_V, pwl_invRn, pwl_mn, pwl_an;
+  // raw reference values (faithful paths: grain-size evolution, anisotropy)
+  double pwl_A, pwl_pref, pwl_F, pwl_m, pwl_r, pwl_f, pwl_a;
+  // diffusion
+  double lin_n, lin_lnK, lin_Q, lin_V, lin_invRn, lin_m, lin_mn, lin_an;
+  double lin_A, lin_F, lin_r, lin_f, lin_a;
+  // grain-boundary sliding (bracket only: C_gbs is never set by the reference)
+  double gbs_n, gbs_lnK, gbs_Q, gbs_V, gbs_invRn, gbs_mn, gbs_an;
+  double gbs_A, gbs_F, gbs_m, gbs_r, gbs_f, gbs_a;
+  // Peierls: ST = EaR g2 / T, ln Arr = -EaR om2 / T
+  double exp_EaR, exp_g2, exp_om2, exp_n, exp_lngS, exp_lnE, exp_gamma, exp_S, exp_E, exp_Ea;
+  // constant viscosity
+  double eta0, eta0_two;
+  // plasticity
+  double Slim, eta_vp, n_vp, T_st;
+  // grain size / wattmeter
+  double gs_ref, ln_gs_ref, Kpzm, Qpzm, Gpzm, Lpzm, cpzm, ppzm;
+  // density
+  double rho, drho, alp, bet, T0, P0, rho_reac;
+};
+
+struct ModelConst {
+  int np, elastic, step, eta_average, periodic_x, density_variations, tensile_line_search;
+  int diffuse_avg, Nx, Nz, Ncx, Ncz;
+  long long Nc, Nv;
+  double dt, dt_model, min_eta, max_eta, eta_tol, R;
+  double scale_eta, scale_L, scale_T, scale_S, scale_E;
+  double TmaxPeierls, Tmin, Tiimin, Eii_floor, eta_up0, eta_lo0, d_min;
+};
+
+// Per-node values shared by all phases of one node.
+struct NodeIn {
+  double Exx, Ezz, Exz, Txx0, Tzz0, Txz0;
+  double G, T, P, d, phi, X0, dil, fric, C, P0, T0, beta;
+  double lxlz, lx2, ani_fac;  // anisotropic nodes
+  int centroid, final_update, post_process;
+};
+
+struct NodeCtx {
+  double Eii, lnEii, T, Traw, invT, lnd, K, G, dil, eta_el, sin_fric, cos_fric, sin_dil;
+  int elastic, plastic_on;  // plastic_on = (step != 0)
+};
+
+struct PointOut {
+  double eta, Txx, Tzz, Txz, etaVE, Eii_el, Eii_pl, Eii_pwl, Eii_exp, Eii_lin, Eii_gbs, Eii_cst, d1,
+      X1, OverS, Pcorr, rho, div_el, div_pl, Wtot, Wel, Wdiss;
+  int iters, is_pl, status;
+};
+
+__device__ __forceinline__ void set_status(int &st, int code) {
+  if (st == MDZ_OK) st = code;
+}
+
+// ---------------------------------------------------------------------------------------
+// node set-up: invariants and switches shared by the phases (RheologyDensity.c:461-496)
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn &in, bool need_lnd,
+                                               NodeCtx &c) {
+  const double Eyy = -(in.Exx + in.Ezz);
+  double Eii = sqrt(0.5 * (in.Exx * in.Exx + in.Ezz * in.Ezz + Eyy * Eyy) + in.Exz * in.Exz);
+  if (Eii * M.scale_E < 1e-30) Eii = M.Eii_floor;
+  c.Eii = Eii;
+  c.lnEii = log(Eii);
+  c.elastic = (M.step == 0) ? 0 : M.elastic;
+  c.plastic_on = (M.step != 0);
+  c.Traw = in.T;
+  c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
+  c.invT = 1.0 / c.T;
+  c.K = 1.0 / in.beta;
+  c.G = in.G;
+  c.dil = in.dil;
+  if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; c.K = 1e10; }
+  c.eta_el = c.G * M.dt;
+  c.lnd = need_lnd ? log(in.d) : 0.0;
+  sincos(in.fric, &c.sin_fric, &c.cos_fric);
+  c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
+}
+
+// EvaluateDensity, RheologyDensity.c:1761-1831 (models 0, 1, 3, 5)
+__device__ __forceinline__ double density(const ModelConst &M, const PhaseConst &ph, double T, double P,
+                                          double X, double phi) {
+  double rho = 0.0;
+  const int dm = ph.density_model;
+  if (dm == 0) rho = ph.rho;
+  if (dm == 1) {
+    rho = (1.0 - ph.alp * (T - ph.T0)) * (1.0 + ph.bet * (P - ph.P0));
+    rho = ((1.0 - X) * ph.rho + X * (ph.rho + ph.drho)) * rho;
+  }
+  if (dm == 3 && M.density_variations == 0) rho = ph.rho * exp(ph.bet * P - ph.alp * T);
+  if (dm == 3 && M.density_variations == 1)
+    rho = ((1.0 - X) * ph.rho + X * ph.rho_reac) * exp(ph.bet * P - ph.alp * T);
+  if (dm == 5) {
+    const double e = exp(ph.bet * P - ph.alp * T);
+    rho = (1 - phi) * (ph.rho * e) + phi * ((ph.rho + ph.drho) * e);
+  }
+  return rho;
+}
+
+// Local VE solve coefficients of one (node, phase): Eii_k = exp(lnC_k + n_k ln Tii).
+struct VeCoef {
+  double Eii, inv2eta_el, half_inv_cst, dfd_const;  // dfd_const = -el Eii/eta_el - Eii/eta_cst
+  double lnC_pwl, n_pwl, lnC_exp, n_exp, lnC_lin, C_lin1, n_lin;
+  int mech;  // F_CST | F_PWL | F_EXPV (active Peierls) | F_LIN | F_LIN1 | F_GBS
+  int elastic;
+};
+
+// LocalIterationViscoElastic, RheologyDensity.c:152-197, in log form.
+struct VeState {
+  double eta, Tii, e_cst, e_pwl, e_exp, e_lin;
+  int iters, status;
+};
+
+__device__ __forceinline__ void ve_eval(const VeCoef &q, double eta, VeState &s, double &r, double &dfdeta) {
+  const double Tii = 2.0 * eta * q.Eii;
+  double e_cst = 0.0, e_pwl = 0.0, e_exp = 0.0, e_lin = 0.0;
+  if (Tii > 0.0) {
+    const double lnT = (q.mech & (F_PWL | F_EXPV | F_LIN)) ? log(Tii) : 0.0;
+    if (q.mech & F_PWL) e_pwl = exp(fma(q.n_pwl, lnT, q.lnC_pwl));
+    if (q.mech & F_EXPV) e_exp = exp(fma(q.n_exp, lnT, q.lnC_exp));
+    if (q.mech & F_LIN) e_lin = (q.mech & F_LIN1) ? q.C_lin1 * Tii : exp(fma(q.n_lin, lnT, q.lnC_lin));
+  } else {  // outside the log domain: the reference's pow on a non-positive base
+    if (q.mech & F_PWL) e_pwl = exp(q.lnC_pwl) * pow(Tii, q.n_pwl);
+    if (q.mech & F_EXPV) e_exp = exp(q.lnC_exp) * pow(Tii, q.n_exp);
+    if (q.mech & F_LIN) e_lin = ((q.mech & F_LIN1) ? q.C_lin1 : exp(q.lnC_lin)) * pow(Tii, q.n_lin);
+  }
+  if (q.mech & F_CST) e_cst = Tii * q.half_inv_cst;
+  const double e_vis = e_pwl + e_exp + e_lin + e_cst;
+  r = q.Eii - q.elastic * Tii * q.inv2eta_el - e_vis;
+  dfdeta = q.dfd_const - (e_exp * q.n_exp + e_lin * q.n_lin + e_pwl * q.n_pwl) / eta;
+  s.Tii = Tii; s.e_cst = e_cst; s.e_pwl = e_pwl; s.e_exp = e_exp; s.e_lin = e_lin;
+}
+
+__device__ __forceinline__ void ve_newton(const VeCoef &q, VeState &s) {
+  const int nitmax = 20;
+  const double tol = 1.0e-11;
+  double eta = s.eta;
+  s.iters = nitmax;
+  for (int it = 0; it < nitmax; it++) {
+    double r, dfdeta;
+    ve_eval(q, eta, s, r, dfdeta);
+    const double res = fabs(r / q.Eii);
+    if (res < tol / 100) { s.iters = it + 1; break; }
+    if (it == nitmax - 1 && res > tol) { set_status(s.status, MDZ_EVE_ITER); break; }
+    eta -= r / dfdeta;
+  }
+  s.eta = eta;
+}
+
+// LocalIterationViscoElasticGrainSize, RheologyDensity.c:203-379 (faithful pow form;
+// the bracket-end evaluations at :221-243 never reach an output and are skipped).
+struct GseIn {
+  double Eii, eta_el, eta_cst, C_pwl, n_pwl, C_lin, n_lin, m_lin, C_exp, ST, n_exp, eta_up, eta_lo, Ag,
+      gam, lam, cg, pg;
+  int elastic, constant, dislocation, peierls, diffusion;
+};
+
+__device__ inline void ve_gse(const GseIn &q, double &eta_io, double &Tii_o, double &d_io, double &e_cst,
+                              double &e_pwl, double &e_exp, double &e_lin, int &iters, int &status) {
+  const int nitmax = 50, bisection_steps = 20;
+  const double tol = 1.0e-11;
+  double d_ve = d_io, eta = eta_io, Tii = Tii_o;
+  const double p = q.pg, Eii = q.Eii, n_pwl = q.n_pwl, Ag = q.Ag;
+  const double Bg = q.lam / (q.cg * q.gam);
+  const double C_pwl = q.C_pwl;
+  double eta_up = q.eta_up, eta_lo = q.eta_lo;
+  e_cst = e_pwl = e_exp = e_lin = 0.0;
+  iters = nitmax;
+  for (int it = 0; it < nitmax; it++) {
+    if (it < bisection_steps) eta = sqrt(eta_up * eta_lo);
+    Tii = 2.0 * eta * Eii;
+    if (q.constant) e_cst = Tii / 2.0 / q.eta_cst;
+    if (q.dislocation) e_pwl = C_pwl * pow(Tii, n_pwl);
+    d_ve = pow(2 * Bg * Eii * e_pwl * eta * p / Ag, (-1.0 / (p + 1)));
+    if (q.peierls) e_exp = q.C_exp * pow(Tii, q.ST + q.n_exp);
+    if (q.diffusion) e_lin = q.C_lin * pow(Tii, q.n_lin) * pow(d_ve, -q.m_lin);
+    const double e_vis = e_pwl + e_exp + e_lin + e_cst;
+    const double r = Eii - q.elastic * Tii / (2.0 * q.eta_el) - e_vis;
+    const double res = fabs(r / Eii);
+    if (res < tol / 100) { iters = it + 1; break; }
+    if (it == bisection_steps - 1 && res < tol) { iters = it + 1; break; }
+    if (it < bisection_steps) {
+      if (r > 0.0) eta_up = eta;
+      else eta_lo = eta;
+    } else {
+      const double pw = pow(2 * Eii * eta, n_pwl);
+      const double dddeta = -1.0 / 2.0 * Ag * d_ve * pow(2 * Eii * eta, -n_pwl) *
+                            (2 * Bg * C_pwl * Eii * n_pwl * p * pw / Ag + 2 * Bg * C_pwl * Eii * p * pw / Ag) /
+                            (Bg * C_pwl * Eii * eta * p * (p + 1));
+      double dfdeta = 0.0;
+      if (q.elastic) dfdeta += -Eii / q.eta_el;
+      if (q.constant) dfdeta += -Eii / q.eta_cst;
+      if (q.peierls) dfdeta += -(e_exp) * (q.ST + q.n_exp) / eta;
+      if (q.diffusion) dfdeta += -(e_lin) * q.n_lin / eta;
+      if (q.dislocation) dfdeta += -(e_pwl) * n_pwl / eta;
+      dfdeta += q.m_lin * e_lin * dddeta / d_ve;
+      eta -= r / dfdeta;
+    }
+    if (it == nitmax - 1 && res > tol) { set_status(status, MDZ_EGSE_ITER); break; }
+  }
+  if (isnan(eta) || isinf(eta)) set_status(status, MDZ_EGSE_ITER);
+  eta_io = eta; Tii_o = Tii; d_io = d_ve;
+}
+
+// solve_local_3x3, RheologyDensity.c:1082-1125
+__device__ __forceinline__ bool solve3(double J11, double J12, double J13, double J21, double J22, double J23,
+                                       double J31, double J32, double J33, double R1, double R2, double R3,
+                                       double &dT, double &dP, double &dl) {
+  const double det = J11 * (J22 * J33 - J23 * J32) - J12 * (J21 * J33 - J23 * J31) + J13 * (J21 * J32 - J22 * J31);
+  if (fabs(det) < 1e-30) return false;
+  const double inv = 1.0 / det;
+  dT = -inv * ((J22 * J33 - J23 * J32) * R1 + (J13 * J32 - J12 * J33) * R2 + (J12 * J23 - J13 * J22) * R3);
+  dP = -inv * ((J23 * J31 - J21 * J33) * R1 + (J11 * J33 - J13 * J31) * R2 + (J13 * J21 - J11 * J23) * R3);
+  dl = -inv * ((J21 * J32 - J22 * J31) * R1 + (J12 * J31 - J11 * J32) * R2 + (J11 * J22 - J12 * J21) * R3);
+  return true;
+}
+
+// Combined mode-I/mode-II return of Popov et al. 2025 (RheologyDensity.c:710-930).
+// Returns is_pl and updates Tii, Pc, lam_dot, A_tau, A_P, eta_vp.
+__device__ inline int plastic_popov(const ModelConst &M, const PhaseConst &ph, double Tii_in, double P, double C,
+                                    double cos_fric, double sin_fric, double sin_dil, double eta_ve, double K,
+                                    double &Tii, double &Pc, double &lam_dot, double &A_tau, double &A_P,
+                                    double &eta_vp, int &status) {
+  const int nitmax = 20;
+  const double k = sin_fric, kq = sin_dil, c = C * cos_fric, dt = M.dt;
+  const double a = sqrt(1.0 + k * k), b = sqrt(1.0 + kq * kq);
+  const double py = (ph.T_st + c / a) / (1.0 - k / a);
+  const double Ry = py - ph.T_st;
+  const double pd = py - Ry * k / a;
+  const double tau_d = k * pd + c;
+  const double pq = pd + kq * tau_d;
+  double R_haty = sqrt(Tii_in * Tii_in + (P - py) * (P - py)), R_hatq;
+  int on_yield = (Tii_in * (py - pd)) >= (tau_d * (py - P)), on_flow;
+  double F = on_yield ? Tii_in - k * P - c : a * (R_haty - Ry);
+  Tii = Tii_in;
+  if (!(F > 1e-17)) return 0;
+  const double atol = 1e-10, rtol = 1e-8;
+  const double eta_vp0 = ph.eta_vp;
+  double Tiic = Tii_in, R0n = 2.0 * atol;
+  double A_tau_2 = 0, A_P_2 = 0, A_tau_P = 0, A_P_tau = 0, dFdT, dFdP;
+  Pc = P; lam_dot = 0.0;
+  for (int it = 0; it < nitmax; it++) {
+    if (Tiic < 0.0) Tiic = 0.0;
+    on_yield = (Tiic * (py - pd)) >= (tau_d * (py - Pc));
+    on_flow = (Tiic * (pq - pd)) >= (tau_d * (pq - Pc));
+    eta_vp = eta_vp0;
+    R_haty = sqrt(Tiic * Tiic + (Pc - py) * (Pc - py));
+    R_hatq = sqrt(Tiic * Tiic + (Pc - pq) * (Pc - pq));
+    if (on_yield) { F = Tiic - k * Pc - c; dFdT = 1.0; dFdP = -k; }
+    else { F = a * (R_haty - Ry); dFdT = a * Tiic / R_haty; dFdP = a * (Pc - py) / R_haty; }
+    if (on_flow) { A_tau = 0.5; A_P = kq; A_tau_2 = 0.0; A_P_2 = 0.0; A_tau_P = 0.0; A_P_tau = 0.0; }
+    else {
+      const double R3h = R_hatq * R_hatq * R_hatq;
+      A_tau = b * Tiic / (2.0 * R_hatq);
+      A_P = -b * (Pc - pq) / R_hatq;
+      A_tau_2 = b * (R_hatq * R_hatq - Tiic * Tiic) / (2.0 * R3h);
+      A_P_2 = -b * (R_hatq * R_hatq - (Pc - pq) * (Pc - pq)) / R3h;
+      A_tau_P = -b * Tiic * (Pc - pq) / (2.0 * R3h);
+      A_P_tau = b * Tiic * (Pc - pq) / R3h;
+    }
+    double R1 = (Tii_in - Tiic) / (2.0 * eta_ve) - lam_dot * A_tau;
+    double R2 = (Pc - P) / (K * dt) - lam_dot * A_P;
+    double R3 = F - lam_dot * eta_vp;
+    const double Rn = sqrt(R1 * R1 + R2 * R2 + R3 * R3);
+    if (Rn < atol || Rn / R0n < rtol) break;
+    R0n = Rn;
+    double dT, dP, dl;
+    if (!solve3(-1.0 / 2.0 / eta_ve - lam_dot * A_tau_2, -lam_dot * A_tau_P, -A_tau, -lam_dot * A_P_tau,
+                1.0 / K / dt - lam_dot * A_P_2, -A_P, dFdT, dFdP, -eta_vp, R1, R2, R3, dT, dP, dl)) {
+      set_status(status, MDZ_ESINGULAR);
+      break;
+    }
+    double alpha = 1.0;
+    if (M.tensile_line_search == 1) {  // :845-887
+      const double c_ls = 1e-4, R0ls = 0.5 * (R1 * R1 + R2 * R2 + R3 * R3);
+      bool failed = false;
+      for (int ls = 0; ls < 100; ls++) {
+        const double Tl = Tiic + dT * alpha, Pl = Pc + dP * alpha;
+        on_yield = (Tl * (py - pd) >= tau_d * (py - Pl));
+        on_flow = (Tl * (pq - pd) >= tau_d * (pq - Pl));
+        eta_vp = eta_vp0;
+        R_haty = sqrt(Tl * Tl + (Pl - py) * (Pl - py));
+        R_hatq = sqrt(Tl * Tl + (Pl - pq) * (Pl - pq));
+        const double Fl = on_yield ? Tl - k * Pl - c : a * (R_haty - Ry);
+        if (on_flow) { A_tau = 0.5; A_P = kq; }
+        else { A_tau = b * Tl / (2.0 * R_hatq); A_P = -b * (Pl - pq) / R_hatq; }
+        R1 = (Tii_in - Tl) / (2.0 * eta_ve) - lam_dot * A_tau;
+        R2 = (Pl - P) / (K * dt) - lam_dot * A_P;
+        R3 = Fl - lam_dot * eta_vp;
+        const double Rls = 0.5 * (R1 * R1 + R2 * R2 + R3 * R3);
+        if (Rls < R0ls - 2.0 * c_ls * alpha * Rls && ls > 0) break;
+        alpha *= 0.5;
+        if (alpha < 1e-2) { failed = true; break; }
+      }
+      if (failed) { set_status(status, MDZ_ELINESEARCH); break; }
+    }
+    Tiic += alpha * dT;
+    Pc += alpha * dP;
+    lam_dot += alpha * dl;
+  }
+  Tii = Tiic;
+  return 1;
+}
+
+// ---------------------------------------------------------------------------------------
+// ViscosityConcise (RheologyDensity.c:385-1080) for phase `ph` at a node prepared by
+// node_setup_iso.  `warm_eta` > 0 replaces the initial guess eta_up (learned warm start).
+// ---------------------------------------------------------------------------------------
+__device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                 double warm_eta, PointOut &o) {
+  const int fl = ph.flags;
+  const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
+  const int gbs = (fl & F_GBS) != 0, gs = (fl & F_GS) != 0;
+  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
+  const int elastic = c.elastic;
+  const double T = c.T, P = in.P, Eii = c.Eii, lnEii = c.lnEii, eta_el = c.eta_el, K = c.K, dt = M.dt;
+  o.status = MDZ_OK;
+  o.Pcorr = P;
+  o.X1 = in.X0;
+  o.Eii_gbs = 0.0;
+  o.OverS = 0.0;
+  o.Wtot = o.Wel = o.Wdiss = 0.0;
+  o.Eii_el = 0.0;
+  o.rho = 0.0;
+  double d = in.d, lnd = c.lnd;
+  o.d1 = ph.gs_ref;
+
+  // Arrhenius pre-factors in log space (RheologyDensity.c:501-523)
+  double lnB_pwl = 0.0, lnB_lin = 0.0, lnB_exp = 0.0, ST = 0.0, nE = 0.0;
+  if (dislocation) {
+    lnB_pwl = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
+    if (fl & F_PWL_M) lnB_pwl += ph.pwl_mn * lnd;
+    if (fl & F_PWL_A) lnB_pwl -= ph.pwl_an * in.phi;
+  }
+  if (diffusion) {
+    if (ph.lin_m > 0.0 && d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
+    lnB_lin = ph.lin_lnK + (ph.lin_Q + P * ph.lin_V) * ph.lin_invRn * c.invT;
+    if (fl & F_LIN_A) lnB_lin -= ph.lin_an * in.phi;
+  }
+  if (peierls) {
+    ST = ph.exp_EaR * c.invT * ph.exp_g2;
+    nE = ST + ph.exp_n;
+    const double inv_nE = 1.0 / nE;
+    const double lnArr = -ph.exp_EaR * c.invT * ph.exp_om2;
+    const double lnF = ((1.0 - nE) * kLn2 - (nE + 1.0) * (0.5 * 1.09861228866810969140)) * inv_nE;
+    lnB_exp = lnF + (ST * ph.exp_lngS - ph.exp_lnE - lnArr) * inv_nE;
+  }
+  // Tyield with the von Mises cut-off (:530-539)
+  double Tyield = 0.0, C = in.C;
+  if (plastic == 1) {
+    Tyield = C * c.cos_fric + P * c.sin_fric;
+    if (ph.Slim < Tyield) { C = ph.Slim; Tyield = ph.Slim; }
+  }
+
+  // isolated viscosities and the bracket (:559-592)
+  double eta_cst = 0.0, eta_pwl = 0.0, eta_lin = 0.0, eta_gbs = 0.0, eta_exp = 0.0, Ag = 0.0;
+  if (constant) eta_cst = ph.eta0;
+  if (fl & F_CMIX) {
+    const double X0 = in.X0, e1 = ph.eta0, e2 = ph.eta0_two;
+    if (M.diffuse_avg == 0) eta_cst = X0 * e1 + (1 - X0) * e2;
+    if (M.diffuse_avg == 1) eta_cst = pow(X0 / e1 + (1 - X0) / e2, -1.0);
+    if (M.diffuse_avg == 2) eta_cst = exp(X0 * log(e1) + (1 - X0) * log(e2));
+  }
+  if (dislocation) eta_pwl = exp(fma(1.0 / ph.pwl_n - 1.0, lnEii, lnB_pwl));
+  if (gs) {  // wattmeter grain size (:567-576)
+    Ag = ph.Kpzm * exp(-ph.Qpzm / M.R / T);
+    const double Tii0 = 2. * eta_el * Eii;
+    const double epwl0 = Tii0 / 2.0 / eta_pwl;
+    d = exp(log(Ag * ph.Gpzm / (ph.Lpzm * (1.0 / ph.cpzm) * Tii0 * epwl0 * ph.ppzm)) / (1.0 + ph.ppzm));
+    lnd = log(d);
+  }
+  if (diffusion) eta_lin = exp(fma(1.0 / ph.lin_n - 1.0, lnEii, lnB_lin + (ph.lin_m != 0.0 ? ph.lin_mn * lnd : 0.0)));
+  if (gbs) {
+    double lnB_gbs = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * in.phi;
+    if (ph.gbs_m != 0.0) lnB_gbs += ph.gbs_mn * lnd;
+    eta_gbs = exp(fma(1.0 / ph.gbs_n - 1.0, lnEii, lnB_gbs));
+  }
+  if (peierls) eta_exp = exp(fma(1.0 / nE - 1.0, lnEii, lnB_exp));
+  double eta_up = M.eta_up0, eta_lo = M.eta_lo0;
+  if (constant) { eta_up = fmin(eta_up, eta_cst); eta_lo = fmax(eta_lo, eta_cst); }
+  if (dislocation) { eta_up = fmin(eta_up, eta_pwl); eta_lo = fmax(eta_lo, eta_pwl); }
+  if (elastic == 1) { eta_up = fmin(eta_up, eta_el); eta_lo = fmax(eta_lo, eta_el); }
+  if (peierls) { eta_up = fmin(eta_up, eta_exp); eta_lo = fmax(eta_lo, eta_exp); }
+  if (diffusion) { eta_up = fmin(eta_up, eta_lin); eta_lo = fmax(eta_lo, eta_lin); }
+  if (gbs) { eta_up = fmin(eta_up, eta_gbs); eta_lo = fmax(eta_lo, eta_gbs); }
+  if (gs) o.d1 = d;
+
+  // local visco-elastic solve (:597-647)
+  const double lnC_pwl = -ph.pwl_n * (kLn2 + lnB_pwl);
+  const double lnC_lin = -ph.lin_n * (kLn2 + lnB_lin);
+  const double lnC_exp = -nE * (kLn2 + lnB_exp);
+  double eta_ve, Tii, e_cst, e_pwl, e_exp, e_lin;
+  if (!gs) {
+    VeCoef q;
+    q.Eii = Eii;
+    q.elastic = elastic;
+    q.inv2eta_el = 1.0 / (2.0 * eta_el);
+    q.half_inv_cst = constant ? 0.5 / eta_cst : 0.0;
+    q.dfd_const = (elastic ? -Eii / eta_el : 0.0) + (constant ? -Eii / eta_cst : 0.0);
+    q.mech = (constant ? F_CST : 0) | (dislocation ? F_PWL : 0) | (peierls ? F_EXPV : 0) |
+             (diffusion ? (F_LIN | ((fl & F_LIN1) ? F_LIN1 : 0)) : 0);
+    q.lnC_pwl = lnC_pwl; q.n_pwl = dislocation ? ph.pwl_n : 0.0;
+    q.lnC_exp = lnC_exp; q.n_exp = peierls ? nE : 0.0;
+    q.lnC_lin = diffusion ? lnC_lin - (ph.lin_m != 0.0 ? ph.lin_m * lnd : 0.0) : 0.0;
+    q.C_lin1 = (diffusion && (fl & F_LIN1)) ? exp(q.lnC_lin) : 0.0;
+    q.n_lin = diffusion ? ph.lin_n : 0.0;
+    VeState s;
+    s.eta = (warm_eta > 0.0) ? warm_eta : eta_up;
+    s.status = MDZ_OK;
+    ve_newton(q, s);
+    set_status(o.status, s.status);
+    eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
+    o.iters = s.iters;
+  } else {
+    GseIn g;
+    g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst; g.C_pwl = exp(lnC_pwl); g.n_pwl = ph.pwl_n;
+    g.C_lin = exp(lnC_lin); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m; g.C_exp = exp(lnC_exp); g.ST = ST;
+    g.n_exp = ph.exp_n; g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = Ag; g.gam = ph.Gpzm; g.lam = ph.Lpzm;
+    g.cg = ph.cpzm; g.pg = ph.ppzm; g.elastic = elastic; g.constant = constant; g.dislocation = dislocation;
+    g.peierls = peierls; g.diffusion = diffusion;
+    eta_ve = eta_up;
+    Tii = 2.0 * eta_ve * Eii;
+    double dd = o.d1;
+    int st = MDZ_OK;
+    ve_gse(g, eta_ve, Tii, dd, e_cst, e_pwl, e_exp, e_lin, o.iters, st);
+    set_status(o.status, st);
+    o.d1 = dd;
+  }
+  const double Tii_ve = Tii;
+
+  // plastic corrections (:655-930)
+  int is_pl = 0;
+  double gdot = 0.0, divp = 0.0, Pc = P, eta_vep = 0.0, lam_dot = 0.0, A_tau = 1.0, eta_vp = ph.eta_vp;
+  if (plastic == 1) {
+    double F = Tii - Tyield;
+    if (F > 1e-17) {
+      const double tol = M.eta_tol, eta_vp0 = ph.eta_vp, n_vp = ph.n_vp;
+      const bool vp1 = (fl & F_VP1) != 0;
+      const double ksd = K * dt * c.sin_fric * c.sin_dil;
+      double Tiic = 0.0;
+      is_pl = 1;
+      eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
+      gdot = F / (eta_ve + eta_vp + ksd);
+      const double F0 = F;
+      for (int it = 0; it < 20; it++) {
+        divp = gdot * c.sin_dil;
+        Pc = P + K * dt * divp;
+        eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+        Tyield = Tyield + gdot * eta_vp;
+        Tiic = Tii - eta_ve * gdot;
+        F = Tiic - Tyield;
+        const double res = fabs(F);
+        if (res < tol || res / F0 < tol) break;
+        gdot -= F / (-eta_ve - eta_vp / n_vp - ksd);
+      }
+      if (Tiic < 0.0) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }
+      o.Pcorr = Pc;
+      eta_vep = Tiic / (2.0 * Eii);
+      Tii = Tiic;
+    }
+  }
+  double A_P = 0.0;
+  if (plastic == 2) {
+    int st = MDZ_OK;
+    double Tn = Tii;
+    is_pl = plastic_popov(M, ph, Tii, P, C, c.cos_fric, c.sin_fric, c.sin_dil, eta_ve, K, Tn, Pc, lam_dot, A_tau,
+                          A_P, eta_vp, st);
+    set_status(o.status, st);
+    if (is_pl) {
+      o.Pcorr = Pc;
+      eta_vep = Tn / (2.0 * Eii);
+      Tii = Tn;
+      divp = lam_dot * A_P;
+    }
+  }
+
+  // density on centroids (:934-960)
+  if (in.centroid > 0) o.rho = density(M, ph, T, (in.final_update == 1) ? Pc : P, in.X0, in.phi);
+
+  double eta_pl = 0.0;
+  if (is_pl == 0) o.etaVE = eta_ve;
+  else if (plastic == 1) { o.etaVE = eta_vep; eta_pl = Tii / gdot; }
+  else { o.etaVE = eta_vep; eta_pl = Tii / (2.0 * lam_dot * A_tau); }
+  o.is_pl = is_pl;
+  o.Txx = 2.0 * o.etaVE * in.Exx;
+  o.Tzz = 2.0 * o.etaVE * in.Ezz;
+  o.Txz = 2.0 * o.etaVE * in.Exz;
+  o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
+
+  double eta = 0.0;
+  if (in.post_process == 1) {  // :986-1053
+    double inv = 0.0;
+    const double half_T = 0.5 * Tii_ve;
+    if (peierls) inv += e_exp / half_T;           // 1/eta_exp, eta_exp = Tii/(2 Eii_exp)
+    if (dislocation) inv += e_pwl / half_T;
+    if (diffusion) {
+      // eta_lin = B pow(Eii_lin, 1/n-1) pow(d1, m/n) = Tii/(2 Eii_lin) (d1/d)^(m/n)
+      double inv_lin = e_lin / half_T;
+      if (ph.lin_m != 0.0 && !gs) inv_lin *= exp(ph.lin_mn * (lnd - ph.ln_gs_ref));
+      inv += inv_lin;
+    }
+    if (constant) inv += (1.0 / eta_cst);
+    if (is_pl == 1) inv += (1.0 / eta_pl);
+    eta = 1.0 / inv;
+    if (elastic) {
+      const double h = 0.5 / eta_el;
+      const double Tyy = -(o.Txx + o.Tzz), Tyy0 = -(in.Txx0 + in.Tzz0);
+      const double ex = (o.Txx - in.Txx0) * h, ez = (o.Tzz - in.Tzz0) * h;
+      const double ey = (Tyy - Tyy0) * h, exz = (o.Txz - in.Txz0) * h;
+      o.Eii_el = sqrt(0.5 * (ex * ex + ez * ez + ey * ey) + exz * exz);
+    }
+    o.Eii_pl = (is_pl && plastic == 1) ? gdot / 2.0 : ((is_pl && plastic == 2) ? lam_dot * A_tau : 0.0);
+    o.div_pl = divp;
+    o.div_el = -(Pc - in.P0) / (K * dt);
+    if (plastic == 1) o.OverS = eta_vp * gdot;
+    if (plastic == 2) o.OverS = eta_vp * lam_dot * A_tau;
+    if (in.centroid == 1) {
+      const double T2 = Tii * Tii;
+      o.Wtot = T2 / eta_ve;
+      o.Wel = T2 / eta_el;
+      o.Wdiss = T2 / eta;
+      if (o.Wdiss < 0.0) set_status(o.status, MDZ_EWDISS);
+    }
+  } else {
+    o.Eii_pl = 0.0;
+    o.div_pl = (is_pl ? divp : 0.0);
+    o.div_el = 0.0;
+  }
+  // limiters (:1058-1073)
+  if (o.etaVE > M.max_eta) o.etaVE = M.max_eta;
+  if (o.etaVE < M.min_eta) o.etaVE = M.min_eta;
+  if (eta > M.max_eta) eta = M.max_eta;
+  if (eta < M.min_eta) eta = M.min_eta;
+  o.eta = eta;
+}
+
+
+// ---------------------------------------------------------------------------------------
+// ViscosityConciseAniso (AnisotropyRoutines.c:282-727).  The node context carries the
+// rotated-frame invariant; Er_* are the rotated strain-rate components.
+// ---------------------------------------------------------------------------------------
+struct AnisoNode {
+  double Er_xx, Er_zz, Er_xz, lxlz, lx2;
+};
+
+__device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c,
+                                                 AnisoNode &a) {
+  const double lx2 = in.lx2, lxlz = in.lxlz, nz2 = 1.0 - lx2;  // :379-383
+  a.lx2 = lx2; a.lxlz = lxlz;
+  a.Er_xx = lx2 * in.Exx + nz2 * in.Ezz + 2. * lxlz * in.Exz;
+  a.Er_zz = nz2 * in.Exx + lx2 * in.Ezz - 2. * lxlz * in.Exz;
+  a.Er_xz = -lxlz * in.Exx + lxlz * in.Ezz + (lx2 - nz2) * in.Exz;
+  const double Er_yy = -a.Er_xx - a.Er_zz;
+  c.Eii = sqrt(0.5 * (a.Er_xx * a.Er_xx + a.Er_zz * a.Er_zz + Er_yy * Er_yy) + a.Er_xz * a.Er_xz);
+  c.lnEii = log(c.Eii);
+  c.elastic = (M.step == 0) ? 0 : M.elastic;
+  c.plastic_on = 1;
+  c.Traw = in.T;
+  c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
+  c.invT = 1.0 / c.T;
+  c.K = 1.0 / in.beta;
+  c.G = in.G;
+  c.dil = in.dil;
+  if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; }
+  c.eta_el = c.elastic ? c.G * M.dt_model : 1e20;
+  c.lnd = need_lnd ? log(in.d) : 0.0;
+  sincos(in.fric, &c.sin_fric, &c.cos_fric);
+  c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
+}
+
+__device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                   const AnisoNode &an, double warm_eta, PointOut &o) {
+  const int fl = ph.flags;
+  const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
+  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int plastic = (fl & F_PLANY) != 0;
+  const int elastic = c.elastic;
+  const double T = c.T, P = in.P, Eii = c.Eii, lnEii = c.lnEii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
+  const double tol = 1e-11, min_eta = M.min_eta, max_eta = M.max_eta;
+  o.status = MDZ_OK;
+  o.Pcorr = P;
+  o.X1 = 0.0; o.rho = 0.0; o.Eii_gbs = 0.0; o.Eii_el = 0.0; o.Eii_pl = 0.0; o.div_pl = 0.0; o.div_el = 0.0;
+  o.OverS = 0.0; o.Wtot = o.Wel = o.Wdiss = 0.0;
+  o.d1 = in.d;
+  const double lnd = c.lnd;
+
+  double lnB_pwl = 0.0, lnB_lin = 0.0, lnB_exp = 0.0, ST = 0.0, nE = 0.0;
+  if (dislocation) {  // :334-337
+    lnB_pwl = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
+    if (fl & F_PWL_M) lnB_pwl += ph.pwl_mn * lnd;
+    if (fl & F_PWL_A) lnB_pwl -= ph.pwl_an * in.phi;
+  }
+  if (diffusion) {  // :342-349
+    if (ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
+    lnB_lin = ph.lin_lnK + (ph.lin_Q + P * ph.lin_V) * ph.lin_invRn * c.invT;
+    if (fl & F_LIN_A) lnB_lin -= ph.lin_an * in.phi;
+  }
+  if (peierls) {  // :355-362
+    ST = ph.exp_EaR * c.invT * ph.exp_g2;
+    nE = ST + ph.exp_n;
+    const double inv_nE = 1.0 / nE;
+    const double lnArr = -ph.exp_EaR * c.invT * ph.exp_om2;
+    const double lnF = ((1.0 - nE) * kLn2 - (nE + 1.0) * (0.5 * 1.09861228866810969140)) * inv_nE;
+    lnB_exp = lnF + (ST * ph.exp_lngS - ph.exp_lnE - lnArr) * inv_nE;
+  }
+  double Tyield = 0.0, Coh = in.C;
+  if (plastic) {  // :370-377
+    Tyield = Coh * c.cos_fric + P * c.sin_fric;
+    if (ph.Slim < Tyield) { Coh = ph.Slim; Tyield = ph.Slim; }
+  }
+  double eta_cst = 0.0, eta_pwl = 0.0, eta_lin = 0.0, eta_exp = 0.0;  // :390-397
+  if (constant) eta_cst = ph.eta0;
+  if (dislocation) eta_pwl = exp(fma(1.0 / ph.pwl_n - 1.0, lnEii, lnB_pwl));
+  if (diffusion) eta_lin = exp(fma(1.0 / ph.lin_n - 1.0, lnEii, lnB_lin + (ph.lin_m != 0.0 ? ph.lin_mn * lnd : 0.0)));
+  if (peierls) eta_exp = exp(fma(1.0 / nE - 1.0, lnEii, lnB_exp));
+  double eta_up = M.eta_up0, eta_lo = M.eta_lo0;  // :409-415
+  if (constant) { eta_up = fmin(eta_up, eta_cst); eta_lo = fmax(eta_lo, eta_cst); }
+  if (dislocation) { eta_up = fmin(eta_up, eta_pwl); eta_lo = fmax(eta_lo, eta_pwl); }
+  if (elastic) { eta_up = fmin(eta_up, eta_el); eta_lo = fmax(eta_lo, eta_el); }
+  if (peierls) { eta_up = fmin(eta_up, eta_exp); eta_lo = fmax(eta_lo, eta_exp); }
+  if (diffusion) { eta_up = fmin(eta_up, eta_lin); eta_lo = fmax(eta_lo, eta_lin); }
+
+  const double lnC_pwl = -ph.pwl_n * (kLn2 + lnB_pwl);
+  const double lnC_lin = -ph.lin_n * (kLn2 + lnB_lin);
+  const double lnC_exp = -nE * (kLn2 + lnB_exp);
+  double eta_ve = eta_up, Tii = 0.0, e_cst = 0.0, e_pwl = 0.0, e_exp = 0.0, e_lin = 0.0;
+  if (fl & F_GS) {  // :429-473
+    GseIn g;
+    g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst; g.C_pwl = exp(lnC_pwl); g.n_pwl = ph.pwl_n;
+    g.C_lin = exp(lnC_lin); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m; g.C_exp = exp(lnC_exp); g.ST = ST;
+    g.n_exp = ph.exp_n; g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = ph.Kpzm * exp(-ph.Qpzm / (M.R * T));
+    g.gam = ph.Gpzm; g.lam = ph.Lpzm; g.cg = ph.cpzm; g.pg = ph.ppzm; g.elastic = elastic; g.constant = constant;
+    g.dislocation = dislocation; g.peierls = peierls; g.diffusion = diffusion;
+    double dd = in.d;
+    int st = MDZ_OK;
+    ve_gse(g, eta_ve, Tii, dd, e_cst, e_pwl, e_exp, e_lin, o.iters, st);
+    set_status(o.status, st);
+    o.d1 = dd;
+  } else {  // :474-585: 10 log-bisection steps, then Newton <= 50
+    VeCoef q;
+    q.Eii = Eii;
+    q.elastic = elastic;
+    q.inv2eta_el = 1.0 / (2.0 * eta_el);
+    q.half_inv_cst = constant ? 0.5 / eta_cst : 0.0;
+    q.dfd_const = (elastic ? -Eii / eta_el : 0.0) + (constant ? -Eii / eta_cst : 0.0);
+    q.mech = (constant ? F_CST : 0) | (dislocation ? F_PWL : 0) | (peierls ? F_EXPV : 0) |
+             (diffusion ? (F_LIN | ((fl & F_LIN1) ? F_LIN1 : 0)) : 0);
+    q.lnC_pwl = lnC_pwl; q.n_pwl = dislocation ? ph.pwl_n : 0.0;
+    q.lnC_exp = lnC_exp; q.n_exp = peierls ? nE : 0.0;
+    q.lnC_lin = diffusion ? lnC_lin - (ph.lin_m != 0.0 ? ph.lin_m * lnd : 0.0) : 0.0;
+    q.C_lin1 = (diffusion && (fl & F_LIN1)) ? exp(q.lnC_lin) : 0.0;
+    q.n_lin = diffusion ? ph.lin_n : 0.0;
+    VeState s;
+    s.status = MDZ_OK;
+    double r, dr;
+    if (warm_eta > 0.0) {
+      eta_ve = warm_eta;
+    } else {
+      double lo = min_eta * 1.0e-3, hi = 10.0 * fmax(eta_lo, max_eta);
+      for (int bit = 0; bit < 10; bit++) {
+        eta_ve = sqrt(lo * hi);
+        ve_eval(q, eta_ve, s, r, dr);
+        if (r > 0.0) lo = eta_ve;
+        else hi = eta_ve;
+        if (fabs(r / Eii) < tol / 100) break;
+      }
+      eta_ve = sqrt(lo * hi);
+    }
+    o.iters = 50;
+    for (int it = 0; it < 50; it++) {
+      ve_eval(q, eta_ve, s, r, dr);
+      if (isnan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
+      eta_ve -= r / dr;
+      if (eta_ve <= 0.0) eta_ve = min_eta;
+      const double res = fabs(r / Eii);
+      if (res < tol / 100) { o.iters = it + 1; break; }
+      if (it == 49 && res < 10.0 * tol) break;
+      if (it == 49 && res > tol) { set_status(o.status, MDZ_EANISO_ITER); break; }
+    }
+    Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
+  }
+  if (eta_ve < min_eta) eta_ve = min_eta;  // :589-603
+  if (eta_ve > max_eta) eta_ve = max_eta;
+  const double Tii_ve = Tii;
+  double Tr_xx = 2.0 * eta_ve * an.Er_xx, Tr_zz = 2.0 * eta_ve * an.Er_zz, Tr_xz = 2.0 * eta_ve * an.Er_xz / in.ani_fac;
+  double eta_vep = eta_ve, gdot = 0.0, Pc = P;
+  const double Ft = Tii - Tyield;
+  int is_pl = 0;
+  if (Ft > 1e-17 && plastic) {  // :625-648
+    is_pl = 1;
+    gdot = Ft / (eta_ve + ph.eta_vp + K * dt * c.sin_dil * c.sin_fric);
+    const double Tiic = Tii - gdot * eta_ve;
+    Pc = P + K * dt * c.sin_dil * gdot;
+    eta_vep = Tiic / 2.0 / Eii;
+    Tr_xx = 2.0 * eta_vep * an.Er_xx;
+    Tr_zz = 2.0 * eta_vep * an.Er_zz;
+    Tr_xz = 2.0 * eta_vep * an.Er_xz / in.ani_fac;
+    o.div_pl = gdot * c.sin_dil;
+    o.Eii_pl = gdot / 2.0;
+    Tii = Tiic;
+  }
+  const double lx2 = an.lx2, lxlz = an.lxlz, nz2 = 1.0 - lx2;  // :650-652
+  o.Txx = lx2 * Tr_xx + nz2 * Tr_zz - 2. * lxlz * Tr_xz;
+  o.Tzz = nz2 * Tr_xx + lx2 * Tr_zz + 2. * lxlz * Tr_xz;
+  o.Txz = lxlz * Tr_xx - lxlz * Tr_zz + (lx2 - nz2) * Tr_xz;
+  o.Pcorr = Pc;
+  if (eta_vep < min_eta) eta_vep = min_eta;
+  if (eta_vep > max_eta) eta_vep = max_eta;
+  o.etaVE = eta_vep;
+  o.is_pl = is_pl;
+  o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
+  double eta = eta_vep;
+  if (in.post_process == 1) {  // :681-714
+    const double half_T = 0.5 * Tii_ve;
+    double inv = 0.0;
+    if (diffusion) inv += e_lin / half_T;
+    if (peierls) inv += e_exp / half_T;
+    if (dislocation) inv += e_pwl / half_T;
+    if (constant) inv += 1.0 / eta_cst;
+    if (is_pl) inv += gdot / Tii;
+    eta = 1.0 / inv;
+    if (elastic) o.Eii_el = Tii * Tii / (4 * eta_el * eta_el);
+    if (is_pl) o.Eii_pl = gdot / 2.0;
+    o.div_pl = gdot * c.sin_dil;
+    o.div_el = -(Pc - in.P0) / (K * dt);
+    o.OverS = ph.eta_vp * gdot;
+    if (in.centroid == 1) {
+      const double T2 = Tii * Tii;
+      o.Wtot = T2 / eta_ve;
+      o.Wel = T2 / eta_el;
+      o.Wdiss = T2 / eta;
+    }
+  }
+  if (eta > max_eta) eta = max_eta;  // :720-721
+  if (eta < min_eta) eta = min_eta;
+  o.eta = eta;
+}
+
+// EffectiveStrainRate, RheologyDensity.c:116-146
+__device__ __forceinline__ void effective_strain_rate(double &Exx, double &Ezz, double &Exz, double exx, double ezz,
+                                                      double exz, double Txx, double Tzz, double Txz, double d1,
+                                                      double d2, double ani, double eta_e, int elastic) {
+  if (!elastic) { Exx = exx; Ezz = ezz; Exz = exz; return; }
+  const double Da11 = 2.0 - 2.0 * ani * d1, Da12 = 2.0 * ani * d1, Da13 = -2.0 * ani * d2;
+  const double Da22 = 2.0 - 2.0 * ani * d1, Da23 = 2.0 * ani * d2, Da33 = 1.0 + 2.0 * ani * (d1 - 0.5);
+  const double a11 = Da33 * Da22 - Da23 * Da23, a12 = Da13 * Da23 - Da33 * Da12, a13 = Da12 * Da23 - Da13 * Da22;
+  const double a22 = Da33 * Da11 - Da13 * Da13, a23 = Da12 * Da13 - Da11 * Da23, a33 = Da11 * Da22 - Da12 * Da12;
+  const double idet = 1.0 / ((Da11 * a11) + (Da12 * a12) + (Da13 * a13));
+  const double ie = 1.0 / eta_e;
+  Exx = exx + (a11 * Txx + a12 * Tzz + a13 * Txz) * idet * ie;
+  Ezz = ezz + (a12 * Txx + a22 * Tzz + a23 * Txz) * idet * ie;
+  Exz = exz + (a13 * Txx + a23 * Tzz + a33 * Txz) * idet * ie * 0.5;
+}
+
+// InterpCentroidsToVerticesDouble (GridRoutines.c:108-210): vertex (k,l) averages ring
+// cells (k..k+1, l..l+1) of the ghost-ringed centroid field; each ring cell is one
+// centroid (zero-flux edges, optional x-periodicity).  Air cells (30/31) count as 0.
+__device__ __forceinline__ int ring_to_centroid(int i, int j, int Ncx, int Ncz, int per) {
+  int cj = j - 1;
+  cj = cj < 0 ? 0 : (cj > Ncz - 1 ? Ncz - 1 : cj);
+  int ci;
+  if (per == 1) ci = (i == 0) ? Ncx - 1 : ((i == Ncx + 1) ? 0 : i - 1);
+  else { ci = i - 1; ci = ci < 0 ? 0 : (ci > Ncx - 1 ? Ncx - 1 : ci); }
+  return ci + cj * Ncx;
+}
+
+}  // namespace mdz

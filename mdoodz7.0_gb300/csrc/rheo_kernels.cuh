@@ -1,0 +1,59 @@
+// rheo_kernels.cuh -- launch-side declarations shared by the kernels and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "rheo_device.cuh"
+
+namespace mdz {
+
+// Centroid input fields (grid member names, MDLIB/mdoodz-private.h:75-147)
+enum CenIn { CI_mu, CI_T, CI_p_in, CI_d0, CI_phi0, CI_X0, CI_exxd, CI_ezzd, CI_exz, CI_sxxd0, CI_szzd0, CI_sxz0,
+             CI_fric, CI_C, CI_dil, CI_p0, CI_T0, CI_bet, CI_d1, CI_d2, CI_angle, CI_anif, CI_COUNT };
+enum VerIn { VI_mu, VI_X0, VI_exxd, VI_ezzd, VI_exz, VI_sxxd0, VI_szzd0, VI_sxz0, VI_fric, VI_C, VI_dil, VI_p0,
+             VI_bet, VI_d1, VI_d2, VI_angle, VI_anif, VI_COUNT };
+enum CenOut { CO_eta, CO_eta_phys, CO_VE, CO_sxxd, CO_szzd, CO_sxz, CO_eII_el, CO_eII_pl, CO_eII_pwl, CO_eII_exp,
+              CO_eII_lin, CO_eII_gbs, CO_eII_cst, CO_d, CO_p_corr, CO_div_el, CO_div_pl, CO_div_r, CO_Wtot,
+              CO_Wel, CO_Wdiss, CO_X, CO_OverS, CO_rho, CO_COUNT };
+enum VerOut { VO_sxxd, VO_szzd, VO_sxz, VO_eta_phys, VO_eta, VO_X, VO_VE, VO_T, VO_P, VO_d0, VO_phi0, VO_COUNT };
+
+// Device statistics block (one per context)
+struct DevStats {
+  unsigned long long err_key;  // (node << 8) | -status of the lowest failing node; ~0 if none
+  unsigned long long calls, iters, plastic;
+  unsigned int maxit;
+};
+
+struct SweepArgs {
+  ModelConst M;
+  PhaseConst ph[MDZ_MAX_PHASES];
+  const double *ci[CI_COUNT];
+  const double *vi[VI_COUNT];
+  double *co[CO_COUNT];
+  double *vo[VO_COUNT];
+  const double *perc_n[MDZ_MAX_PHASES];
+  const double *perc_s[MDZ_MAX_PHASES];
+  double *peta_n[MDZ_MAX_PHASES];
+  double *peta_s[MDZ_MAX_PHASES];
+  const signed char *bcp;
+  const signed char *bcg;
+  int32_t *iters_n, *iters_s;  // optional [p*N + node]
+  DevStats *stats;
+  int final_update, need_lnd;
+};
+
+struct PointArgs {
+  ModelConst M;
+  PhaseConst ph[MDZ_MAX_PHASES];
+  mdz_point_inputs in;
+  mdz_point_outputs out;
+  long long n;
+  int aniso;
+  DevStats *stats;
+};
+
+cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap);
+cudaError_t launch_points(const PointArgs &a, cudaStream_t s);
+void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block);
+
+}  // namespace mdz

@@ -1,0 +1,152 @@
+"""GPU parity: the CUDA sweep (through the C ABI) against the CPU oracle.
+
+The oracle is the C restatement of MDOODZ7.0's NonNewtonianViscosityGrid /
+ViscosityConcise (oracle/rheo_oracle.c), itself bit-identical to the
+reference built from its own sources (tests/test_oracle_vs_reference.py) and
+to the committed golden fixtures (tests/test_golden.py).
+"""
+import numpy as np
+import pytest
+
+import mdz_rheo as R
+import mdz_workloads as W
+import oracle_lib as O
+from common import RTOL, clone, field, rel_err, worst
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = R.Context(0)
+    yield c
+    c.close()
+
+
+def run_pair(ctx, w, aniso=False, final_update=0, flags=0):
+    g, c = clone(w.arrays), clone(w.arrays)
+    fn = ctx.sweep_aniso if aniso else ctx.sweep
+    rc, st = fn(w.model, w.mat, R.FieldSet(g), final_update=final_update, flags=flags, check=False)
+    rc2, st2 = O.orc_sweep(w.model, w.mat, R.FieldSet(c), final_update=final_update, aniso=aniso)
+    return rc, st, g, rc2, st2, c
+
+
+def check_close(g, c, label):
+    errs = worst(g, c)
+    bad = {k: v for k, v in errs.items() if v > RTOL}
+    print(label, "max scaled error", max(errs.values()), {k: f"{v:.1e}" for k, v in errs.items() if v > 1e-15})
+    assert not bad, f"{label}: fields above {RTOL}: {bad}"
+
+
+CASES = {
+    "plain_small_201": lambda: W.plain_small(seed=0),
+    "plain_large_129": lambda: W.plain_large(seed=1, ncx=129),
+    "plain_large_typical_scale": lambda: W.plain_large(seed=2, ncx=64, ncz=48, sc=W.TYPICAL),
+    "plain_large_harmonic": lambda: W.plain_large(seed=3, ncx=64, eta_average=1),
+    "plain_large_geometric": lambda: W.plain_large(seed=4, ncx=50, ncz=70, eta_average=2),
+    "plain_small_rect": lambda: W.plain_small(seed=5, ncx=37, ncz=81),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_sweep_matches_oracle(ctx, name):
+    w = CASES[name]()
+    rc, st, g, rc2, st2, c = run_pair(ctx, w)
+    assert rc == rc2 == R.MDZ_OK
+    assert st.phase_calls == st2.phase_calls
+    check_close(g, c, name)
+    # plastic flags may only flip where rounding moves Tii across the yield stress
+    assert abs(int(st.plastic_calls) - int(st2.plastic_calls)) <= max(1, st2.plastic_calls // 10000)
+
+
+def test_sweep_final_update_and_periodic(ctx):
+    w = W.plain_large(seed=7, ncx=40, ncz=33)
+    w.model.periodic_x = 1
+    rc, st, g, rc2, st2, c = run_pair(ctx, w, final_update=1)
+    assert rc == rc2 == R.MDZ_OK
+    check_close(g, c, "periodic+final_update")
+
+
+def test_sweep_air_cells(ctx):
+    w = W.plain_large(seed=10, ncx=40)
+    nx = w.model.Nx
+    w.arrays["BCp_type"][-200:] = 30
+    w.arrays["BCp_type"][-240:-200] = 31
+    w.arrays["BCg_type"][-nx * 6:] = 30
+    rc, st, g, rc2, st2, c = run_pair(ctx, w)
+    assert rc == rc2 == R.MDZ_OK
+    check_close(g, c, "air")
+    assert np.all(g["eta_n"][-200:] == 0.0) and np.all(g["T_s"][-nx * 6:] == 0.0)
+
+
+def test_inactive_phase_keeps_previous_phase_eta(ctx):
+    w = W.plain_small(seed=12, ncx=30)
+    w.arrays["phase_perc_n"][1][:50] = 0.0
+    w.arrays["phase_perc_n"][0][:50] = 1.0
+    w.arrays["phase_eta_n"][1][:] = 123.0
+    rc, st, g, rc2, st2, c = run_pair(ctx, w)
+    assert rc == rc2 == R.MDZ_OK
+    assert np.all(g["phase_eta_n"][1][:50] == 123.0)
+    check_close(g, c, "inactive")
+
+
+def test_iteration_counts_match(ctx):
+    w = W.plain_large(seed=13, ncx=96)
+    np_ = w.mat.Nb_phases
+    g = clone(w.arrays)
+    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(g), flags=R.SWEEP_ITERS)
+    itg_n = np.zeros(np_ * w.Nc, np.int32)
+    itg_s = np.zeros(np_ * w.Nv, np.int32)
+    ctx.get_iterations(itg_n, itg_s)
+    itc_n = np.zeros_like(itg_n)
+    itc_s = np.zeros_like(itg_s)
+    O.orc_sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), iters_n=itc_n, iters_s=itc_s)
+    a = np.concatenate([itg_n, itg_s])
+    b = np.concatenate([itc_n, itc_s])
+    same = np.mean(a == b)
+    print("iteration counts identical for", same, "of (node, phase) pairs; max |diff|", np.max(np.abs(a - b)))
+    assert same > 0.995
+    assert np.max(np.abs(a - b)) <= 1
+    assert st.newton_iters == a.sum()
+
+
+def test_device_memory_matches_host_memory(ctx):
+    torch = pytest.importorskip("torch")
+    w = W.plain_large(seed=14, ncx=64)
+    h = clone(w.arrays)
+    ctx.sweep(w.model, w.mat, R.FieldSet(h))
+    d = {}
+    for k, v in w.arrays.items():
+        if isinstance(v, list):
+            d[k] = [torch.from_numpy(x.copy()).cuda() for x in v]
+        else:
+            d[k] = torch.from_numpy(v.copy()).cuda()
+    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(d), mem=R.MEM_DEVICE)
+    torch.cuda.synchronize()
+    for k in ("eta_n", "sxxd", "eta_s", "sxz", "T_s", "eII_pl", "Wdiss"):
+        assert np.array_equal(d[k].cpu().numpy(), h[k]), k
+    for p in range(w.mat.Nb_phases):
+        assert np.array_equal(d["phase_eta_n"][p].cpu().numpy(), h["phase_eta_n"][p])
+
+
+def test_error_status_grain_size_zero(ctx):
+    w = W.plain_large(seed=15, ncx=32)
+    w.arrays["d0_n"][77] = 0.0  # diffusion creep with m>0 at d=0: reference exit(1)
+    rc, st, g, rc2, st2, c = run_pair(ctx, w)
+    assert rc2 == R.MDZ_EGRAIN_ZERO
+    assert rc == rc2 and st.error_node == st2.error_node
+
+
+def test_aniso_sweep_matches_oracle(ctx):
+    w = W.aniso(seed=4, ncx=96)
+    rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True)
+    assert rc == rc2 == R.MDZ_OK
+    check_close(g, c, "aniso")
+
+
+def test_aniso_typical_scale_harmonic(ctx):
+    w = W.aniso(seed=5, ncx=48, ncz=40, sc=W.TYPICAL)
+    w.model.eta_average = 1
+    rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True)
+    assert rc == rc2 == R.MDZ_OK
+    check_close(g, c, "aniso-typical-harmonic")
