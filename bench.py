@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 local rheology update (MDOODZ7.0 NonNewtonianViscosityGrid).
+
+Metric: rheology point-updates/s on 1 GB300 (plain FP64; the learned warm start is
+reported beside it when trained weights are available).  A point-update is one
+centroid or vertex fully processed by the sweep: every active phase's local solve,
+phase averaging and the final stress.  One step = one sweep over the 2049 x 2049-cell,
+5-phase grid (4,198,401 centroids + 4,202,500 vertices), synthetic seeded inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is timed with CUDA events on the launching stream with inputs resident in
+HBM (3.3 GB of fields, larger than the 129 MB L2, so no flush between steps);
+`e2e` is the same sweep through the C ABI with pinned host buffers, host<->device
+copies inside the timed region.  Under torchrun each rank sweeps its own grid
+(independent instances, weak scaling; the path has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "mdoodz7.0_gb300"))
+
+METRIC = "rheology point-updates/s on 1 GB300: plain FP64 vs NN warm-start at tol 1e-11"
+UNIT = "point-updates/s"
+
+# FP64 work of the sweep kernel per point-update on this workload, in flops
+# (DFMA = 2, DADD/DMUL = 1), from ncu's thread-level FP64 instruction counters of one
+# k_sweep launch on the same field distributions (profiles/k_sweep_plain_large.md).
+# None until that capture exists; then `roofline.achieved` is this x nodes / launch time.
+FP64_FLOPS_PER_POINT = None
+# DRAM bytes (read + write) per point-update of k_sweep, from the same capture.
+DRAM_BYTES_PER_POINT = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=2049, help="cells per side")
+    ap.add_argument("--phases", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def algorithmic_bytes(w):
+    """Compulsory HBM bytes of one sweep: every input field read once, every output
+    written once (field counts of NonNewtonianViscosityGrid, RheologyDensity.c:1131-1426)."""
+    np_ = w.mat.Nb_phases
+    nc, nv = w.Nc, w.Nv
+    cen = 8 * (18 + np_ + np_) + 1 + 8 * 23          # inputs, phase fractions, phase_eta, BC flag, outputs
+    ver = 8 * (13 + np_ + np_) + 1 + 8 * 6 + 8 * 4   # + the four interpolated fields written
+    return nc * cen + nv * ver
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def cpu_baseline(W, O, sample_cells=1025, reps=1):
+    """The oracle (C restatement of the reference, OpenMP, all host cores) on a bounded
+    sample of the same workload distribution."""
+    import mdz_rheo as R
+    ws = W.plain_large(seed=101, ncx=sample_cells)
+    O.orc_sweep(ws.model, ws.mat, R.FieldSet(ws.arrays))  # warm-up (page faults, thread pool)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        O.orc_sweep(ws.model, ws.mat, R.FieldSet(ws.arrays))
+    dt = (time.perf_counter() - t0) / reps
+    lib = O.reference()
+    kind = "port"
+    return {"value": ws.nodes / dt, "unit": UNIT, "cores": O.oracle().orc_num_threads(), "kind": kind,
+            "sample": f"{sample_cells}x{sample_cells}-cell grid of the same 5-phase workload "
+                      f"({ws.nodes} nodes), {reps} sweep(s), {dt:.2f} s each"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation of the path on the host cores.
+    The MDOODZ7.0 sources are compiled by oracle/Makefile where the tree exists (this
+    build host); elsewhere the C restatement of the same code (bit-identical, pinned by
+    the tests) stands in."""
+    ws_, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import mdz_rheo as R
+    import mdz_workloads as W
+    import oracle_lib as O
+    O.build(ref=True)
+    sample = 1025
+    w = W.plain_large(seed=101, ncx=sample, nphases=args.phases)
+    ref = O.reference()
+    kind = "reference" if ref is not None else "port"
+
+    def step():
+        fs = R.FieldSet(w.arrays)
+        if ref is not None:
+            O.ref_sweep(w.model, w.mat, fs)
+        else:
+            O.orc_sweep(w.model, w.mat, fs)
+
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    value = w.nodes / (ms * 1e-3)
+    cores = O.oracle().orc_num_threads()
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plain_large {args.size}x{args.size} cells, {args.phases} phases; "
+                                   f"each step a {sample}x{sample}-cell sample of it",
+                       "nodes_per_step": w.nodes},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{sample}x{sample}-cell grid, {w.nodes} nodes per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    import mdz_rheo as R
+    import mdz_workloads as W
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+
+    w = W.plain_large(seed=1 + rank, ncx=args.size, nphases=args.phases)
+    d = {k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
+         for k, v in w.arrays.items()}
+    fs = R.FieldSet(d)
+    ctx = R.Context(dev)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- device-resident timed region ----
+    for _ in range(args.warmup):
+        ctx.sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE)
+    kernel_ms, iters, calls, launches = [], 0, 0, 0
+    barrier()
+    with ClockSampler(dev) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            rc, st = ctx.sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE)
+            kernel_ms.append(st.elapsed_ms)
+            iters += st.newton_iters
+            calls += st.phase_calls
+            launches += st.kernel_launches
+        e1.record(stream)
+        barrier()
+    total_ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = ws * w.nodes / (ms_step * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        h = {k: ([torch.from_numpy(x).pin_memory() for x in v] if isinstance(v, list)
+                 else torch.from_numpy(v).pin_memory()) for k, v in w.arrays.items()}
+        fh = R.FieldSet(h)
+        for _ in range(max(1, args.warmup)):
+            ctx.sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
+        barrier()
+        e0.record(stream)
+        bi = bo = 0
+        for _ in range(args.steps):
+            rc, st = ctx.sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
+            bi, bo = st.h2d_bytes, st.d2h_bytes
+        e1.record(stream)
+        barrier()
+        e2e_ms = e0.elapsed_time(e1) / args.steps
+        if ws > 1:
+            t = torch.tensor([e2e_ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": ws * w.nodes / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo)}
+        del h, fh
+
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (k_sweep) ----
+    launch_ms = statistics.mean(kernel_ms)
+    peak_fp64 = R.measure_fp64_peak(dev)
+    if FP64_FLOPS_PER_POINT is not None:
+        achieved = FP64_FLOPS_PER_POINT * w.nodes / (launch_ms * 1e-3) / 1e12
+        roof = {"bound": "fp64", "achieved": achieved, "peak": peak_fp64, "unit": "TFLOP/s",
+                "frac": achieved / peak_fp64, "peak_source": "measured (DFMA probe, mdz_rheo_measure_fp64_peak)",
+                "traffic": (DRAM_BYTES_PER_POINT * w.nodes) if DRAM_BYTES_PER_POINT else None}
+    else:
+        roof = {"bound": "fp64", "achieved": None, "peak": peak_fp64, "unit": "TFLOP/s", "frac": None,
+                "peak_source": "measured (DFMA probe)", "traffic": None}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+        hbm = peaks.get("hbm_gbs")
+    except Exception:
+        hbm = None
+    bytes_alg = algorithmic_bytes(w)
+    roof["hbm_achieved_gbs"] = bytes_alg / (launch_ms * 1e-3) / 1e9
+    roof["hbm_frac"] = (roof["hbm_achieved_gbs"] / hbm) if hbm else None
+    roof["algorithmic_bytes_per_launch"] = bytes_alg
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        try:
+            import oracle_lib as O
+            O.build(ref=False)
+            cpu = cpu_baseline(W, O)
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plain_large: {args.size}x{args.size} cells, {args.phases} phases "
+                                   "(dislocation, diffusion, Peierls, softened Drucker-Prager), FP64, "
+                                   "plain Newton from the reference's start point",
+                       "nodes_per_gpu": w.nodes, "phase_calls_per_step": calls // args.steps,
+                       "mean_newton_iters": iters / max(calls, 1),
+                       "l2": "inputs larger than L2 (3.3 GB of fields), no flush",
+                       "parallelism": f"{ws} independent grid(s), one per GPU"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": launches, "kernel_ms_per_launch": launch_ms}
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -152,6 +152,9 @@ typedef struct mdz_sweep_stats {
   int32_t  status;           /* MDZ_OK or the first error code met */
   int64_t  error_node;       /* node of that error: centroid c0, or Nc + c1 for a vertex; -1 if none */
   double   elapsed_ms;       /* device time of the sweep kernels (CUDA events) */
+  uint64_t h2d_bytes;        /* bytes copied host->device by this call (MDZ_MEM_HOST) */
+  uint64_t d2h_bytes;        /* bytes copied device->host by this call (MDZ_MEM_HOST) */
+  uint32_t kernel_launches;  /* kernels this call launched */
 } mdz_sweep_stats;
 
 /* ---- point batches (ViscosityConcise / ViscosityConciseAniso per point) -- */
@@ -210,6 +213,12 @@ int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materia
  * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
  * inactive.  Host buffers. */
 int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);
+
+/* ---- measurement helper ----------------------------------------------- */
+/* Measured FP64 FMA throughput of `device` in TFLOP/s (a full-occupancy DFMA
+ * loop timed with CUDA events).  The roofline of this FP64-bound path is
+ * reported against it.  No reference counterpart. */
+int mdz_rheo_measure_fp64_peak(int device, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -31,6 +31,8 @@ struct mdz_rheo_ctx {
   size_t cap_iters_n = 0, cap_iters_s = 0;
   long long last_Nc = 0, last_Nv = 0;
   int last_np = 0, have_iters = 0, pending = 0;
+  unsigned long long h2d = 0, d2h = 0;
+  unsigned launches = 0;
   int block = 128, grid_cap = 0;
 };
 
@@ -71,6 +73,7 @@ void fold_phase(const mdz_materials *m, const mdz_model *md, int p, PhaseConst &
   if (m->plast[p] != 0) fl |= F_PLANY;
   if (m->phase_mix[p] == 1 && md->diffuse_X != 0) fl |= F_CMIX;
   if (m->nlin[p] == 1.0) fl |= F_LIN1;
+  if (m->npwl[p] == 1.0) fl |= F_PWL1;
   if (m->mpwl[p] != 0.0) fl |= F_PWL_M;
   if (m->apwl[p] != 0.0) fl |= F_PWL_A;
   if (m->alin[p] != 0.0) fl |= F_LIN_A;
@@ -83,46 +86,44 @@ void fold_phase(const mdz_materials *m, const mdz_model *md, int p, PhaseConst &
   // dislocation: B = pref F A^(-1/n) exp((Q+PV)/(R n T)) d^(m/n) f^(-r/n) exp(-a phi/n)
   {
     const double n = m->npwl[p];
-    c.pwl_n = n;
+    c.pwl_n = n; c.pwl_invn = 1.0 / n;
     c.pwl_lnK = log(m->pref_pwl[p]) + log(m->Fpwl[p]) - log(m->Apwl[p]) / n;
     if (m->rpwl[p] != 0.0) c.pwl_lnK += -(m->rpwl[p] / n) * log(m->fpwl[p]);
     c.pwl_Q = m->Qpwl[p]; c.pwl_V = m->Vpwl[p]; c.pwl_invRn = 1.0 / (R * n);
     c.pwl_mn = m->mpwl[p] / n; c.pwl_an = m->apwl[p] / n;
-    c.pwl_A = m->Apwl[p]; c.pwl_pref = m->pref_pwl[p]; c.pwl_F = m->Fpwl[p]; c.pwl_m = m->mpwl[p];
-    c.pwl_r = m->rpwl[p]; c.pwl_f = m->fpwl[p]; c.pwl_a = m->apwl[p];
   }
   // diffusion: B = F A^(-1/n) exp((Q+PV)/(R n T)) f^(-r/n) exp(-a phi/n)
   {
     const double n = m->nlin[p];
-    c.lin_n = n;
+    c.lin_n = n; c.lin_invn = 1.0 / n;
     c.lin_lnK = log(m->Flin[p]) - log(m->Alin[p]) / n;
     if (m->rlin[p] != 0.0) c.lin_lnK += -(m->rlin[p] / n) * log(m->flin[p]);
     c.lin_Q = m->Qlin[p]; c.lin_V = m->Vlin[p]; c.lin_invRn = 1.0 / (R * n);
     c.lin_m = m->mlin[p]; c.lin_mn = m->mlin[p] / n; c.lin_an = m->alin[p] / n;
-    c.lin_A = m->Alin[p]; c.lin_F = m->Flin[p]; c.lin_r = m->rlin[p]; c.lin_f = m->flin[p]; c.lin_a = m->alin[p];
   }
-  // grain-boundary sliding
+  // grain-boundary sliding (bracket only)
   {
     const double n = m->ngbs[p];
-    c.gbs_n = n;
+    c.gbs_n = n; c.gbs_invn = 1.0 / n;
     c.gbs_lnK = log(m->Fgbs[p]) - log(m->Agbs[p]) / n;
     if (m->rgbs[p] != 0.0) c.gbs_lnK += -(m->rgbs[p] / n) * log(m->fgbs[p]);
     c.gbs_Q = m->Qgbs[p]; c.gbs_V = m->Vgbs[p]; c.gbs_invRn = 1.0 / (R * n);
     c.gbs_m = m->mgbs[p]; c.gbs_mn = m->mgbs[p] / n; c.gbs_an = m->agbs[p] / n;
-    c.gbs_A = m->Agbs[p]; c.gbs_F = m->Fgbs[p]; c.gbs_r = m->rgbs[p]; c.gbs_f = m->fgbs[p]; c.gbs_a = m->agbs[p];
   }
-  // Peierls
+  // Peierls (RheologyDensity.c:518-523): with nE = ST + n,
+  //   C Tii^nE = (sqrt3/2) E Arr (gamma S)^n (sqrt3 Tii / (gamma S))^nE
   {
-    const double g = m->Gexp[p];
-    c.exp_Ea = m->Qexp[p]; c.exp_EaR = m->Qexp[p] / R; c.exp_g2 = 2.0 * g * (1 - g);
-    c.exp_om2 = (1.0 - g) * (1.0 - g); c.exp_n = m->nexp[p]; c.exp_lngS = log(g * m->Sexp[p]);
-    c.exp_lnE = log(m->Eexp[p]); c.exp_gamma = g; c.exp_S = m->Sexp[p]; c.exp_E = m->Eexp[p];
+    const double g = m->Gexp[p], gS = g * m->Sexp[p];
+    c.exp_EaR = m->Qexp[p] / R; c.exp_g2 = 2.0 * g * (1 - g); c.exp_om2 = (1.0 - g) * (1.0 - g);
+    c.exp_n = m->nexp[p];
+    c.exp_lnA0 = kLnSqrt3 - kLn2 + log(m->Eexp[p]) + (m->nexp[p] != 0.0 ? m->nexp[p] * log(gS) : 0.0);
+    c.exp_s3gS = kSqrt3 / gS;
   }
   c.eta0 = m->eta0[p];
   const int p2 = m->phase_two[p];
   c.eta0_two = (p2 >= 0 && p2 < MDZ_MAX_PHASES) ? m->eta0[p2] : m->eta0[p];
   c.Slim = m->Slim[p]; c.eta_vp = m->eta_vp[p]; c.n_vp = m->n_vp[p]; c.T_st = m->T_st[p];
-  c.gs_ref = m->gs_ref[p]; c.ln_gs_ref = log(m->gs_ref[p]);
+  c.gs_ref = m->gs_ref[p]; c.inv_gs_ref = 1.0 / m->gs_ref[p]; c.ln_gs_ref = log(m->gs_ref[p]);
   c.Kpzm = m->Kpzm[p]; c.Qpzm = m->Qpzm[p]; c.Gpzm = m->Gpzm[p]; c.Lpzm = m->Lpzm[p];
   c.cpzm = m->cpzm[p]; c.ppzm = m->ppzm[p];
   c.rho = m->rho[p]; c.drho = m->drho[p]; c.alp = m->alp[p]; c.bet = m->bet[p]; c.T0 = m->T0[p]; c.P0 = m->P0[p];
@@ -179,6 +180,7 @@ int stats_from_device(mdz_rheo_ctx *ctx, mdz_sweep_stats *st, float ms) {
   if (st) {
     st->phase_calls = h.calls; st->newton_iters = h.iters; st->max_newton_iters = h.maxit;
     st->plastic_calls = h.plastic; st->status = status; st->error_node = node; st->elapsed_ms = ms;
+    st->h2d_bytes = ctx->h2d; st->d2h_bytes = ctx->d2h; st->kernel_launches = ctx->launches;
   }
   return status;
 }
@@ -216,6 +218,7 @@ struct Mirror {
     if ((err = ensure(ctx->bufs[slot], n * sizeof(T))) != MDZ_OK) return nullptr;
     if (cudaMemcpyAsync(ctx->bufs[slot].p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
       err = MDZ_ECUDA;
+    ctx->h2d += n * sizeof(T);
     return (T *)ctx->bufs[slot].p;
   }
   template <class T>
@@ -230,6 +233,7 @@ struct Mirror {
     if (!h || err || !host) return;
     if (cudaMemcpyAsync(h, ctx->bufs[slot].p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess)
       err = MDZ_ECUDA;
+    ctx->d2h += n * sizeof(T);
   }
 };
 
@@ -274,6 +278,8 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   for (int i = 0; i < VO_COUNT; i++) if (i != VO_VE && !vout[i]) return MDZ_EINVAL;
   if (aniso && !f->VE_s) return MDZ_EINVAL;
 
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
   Mirror mi{ctx};
   for (int i = 0; i < nci; i++) A.ci[i] = mi.in(cin[i], S_CI + i, Nc, host);
   for (int i = 0; i < nvi; i++) A.vi[i] = mi.in(vin[i], S_VI + i, Nv, host);
@@ -311,6 +317,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   CK(launch_sweep(A, aniso, ctx->stream, ctx->block, ctx->grid_cap));
+  ctx->launches += 1;
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   for (int i = 0; i < CO_COUNT; i++) mi.back(cout[i], S_CO + i, Nc, host);
   for (int i = 0; i < VO_COUNT; i++) mi.back(vout[i], S_VO + i, Nv, host);
@@ -490,6 +497,8 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
     return MDZ_EINVAL;
   }
   if ((rc = reset_stats(c)) != MDZ_OK) return rc;
+  c->h2d = c->d2h = 0;
+  c->launches = 1;
   CK(cudaEventRecord(c->ev0, c->stream));
   CK(launch_points(A, c->stream));
   CK(cudaEventRecord(c->ev1, c->stream));

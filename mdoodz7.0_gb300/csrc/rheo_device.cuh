@@ -3,21 +3,25 @@
 // One call of `point_iso` is one ViscosityConcise (MDLIB/RheologyDensity.c:385-1080);
 // `point_aniso` is ViscosityConciseAniso (MDLIB/AnisotropyRoutines.c:282-727).
 //
-// Design for GB300, where the FP64 pipe is the bound:
-//  * per-phase constants (pre-factors, 1/(R n), logs of A, F, f, ...) are folded on the
-//    host once per sweep (PhaseConst);
-//  * Arrhenius and Peierls pre-factors are formed in log space, so each creep
-//    mechanism costs one exp for its isolated viscosity instead of the reference's
-//    five to seven pow/exp calls, and C = (2B)^-n never leaves log space;
-//  * each Newton step evaluates log(Tii) once and one exp per non-linear mechanism
-//    (Newtonian laws are a multiply);
-//  * post-processing uses eta_k = Tii / (2 Eii_k), which is the reference's
-//    B_k * pow(Eii_k, 1/n_k - 1) rewritten with Eii_k = C_k Tii^n_k.
-// These are exact identities of the reference's formulas; results differ from the
-// reference only by rounding (about 1e-14 relative, checked by the parity tests).
-// The Newton iteration itself (start point, update, stopping test, iteration cap)
-// is the reference's, so iteration counts agree except where rounding moves a
-// residual across the stopping threshold.
+// GB300 issues FP64 at 1/64 of its FP32 rate, and this path is bound by the FP64 pipe,
+// so the formulation minimises FP64 instructions while keeping every quantity
+// well conditioned:
+//  * per-phase constants (log pre-factors, 1/(R n), 1/n, ...) are folded on the host;
+//  * each creep law k is carried as the reciprocal of its isolated viscosity at the
+//    node's strain rate, 1/eta_k, formed as a product of well-conditioned factors
+//    (one exp); its strain rate at trial viscosity eta is then
+//        Eii_k(eta) = Eii (eta / eta_k)^n_k,
+//    the reference's C_k Tii^n_k with Tii = 2 eta Eii rewritten.  The Peierls law is
+//    used in the equivalent physical form A (sqrt(3) Tii / (gamma sigma_P))^(ST+n);
+//  * a Newton step takes one log, of eta / eta_p for the softest non-linear law p;
+//    the other laws are offset from it by log(eta_p / eta_k) <= 0, fixed per call, so
+//    no large logarithms cancel;
+//  * post-processing uses eta_k = Tii / (2 Eii_k), the reference's
+//    B_k pow(Eii_k, 1/n_k - 1) rewritten with the same identity.
+// These are identities of the reference's formulas: results differ only by rounding
+// (a few 1e-14 relative, checked by the parity tests).  The Newton iteration itself
+// (start point, update, stopping test, cap) is the reference's, so iteration counts
+// agree except where rounding moves a residual across the stopping threshold.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -28,6 +32,8 @@ namespace mdz {
 
 constexpr double kZeroC = 273.15;                 // MDLIB/include/mdoodz.h:4
 constexpr double kLn2 = 0.69314718055994530942;
+constexpr double kLnSqrt3 = 0.54930614433405484570;  // log(sqrt(3))
+constexpr double kSqrt3 = 1.73205080756887729353;
 
 // mechanism / option bits of PhaseConst::flags
 enum : int {
@@ -41,34 +47,31 @@ enum : int {
   F_PL2 = 1 << 7,   // plast == 2
   F_PLANY = 1 << 8, // plast != 0 (anisotropic path)
   F_CMIX = 1 << 9,  // phase_mix with diffuse_X
-  F_LIN1 = 1 << 10, // nlin == 1: Newtonian diffusion creep (multiply, no exp)
+  F_LIN1 = 1 << 10, // nlin == 1: Newtonian diffusion creep (linear in eta)
   F_PWL_M = 1 << 11,// mpwl != 0
   F_PWL_A = 1 << 12,// apwl != 0
   F_LIN_A = 1 << 13,// alin != 0
   F_VP1 = 1 << 14,  // n_vp == 1 (pow(x, 1/n_vp - 1) == 1)
+  F_PWL1 = 1 << 15, // npwl == 1
 };
 
-// Per-phase constants folded on the host (mdz_rheo_capi.cpp: fold_phase).
+// Per-phase constants folded on the host (mdz_rheo_capi.cu: fold_phase).
 struct PhaseConst {
   int flags, density_model, phase_two, reac_phase;
   // dislocation: ln B = lnK + (Q + P V) invRn / T + mn ln d - an phi
-  double pwl_n, pwl_lnK, pwl_Q, pwl_V, pwl_invRn, pwl_mn, pwl_an;
-  // raw reference values (faithful paths: grain-size evolution, anisotropy)
-  double pwl_A, pwl_pref, pwl_F, pwl_m, pwl_r, pwl_f, pwl_a;
-  // diffusion
-  double lin_n, lin_lnK, lin_Q, lin_V, lin_invRn, lin_m, lin_mn, lin_an;
-  double lin_A, lin_F, lin_r, lin_f, lin_a;
+  double pwl_n, pwl_invn, pwl_lnK, pwl_Q, pwl_V, pwl_invRn, pwl_mn, pwl_an;
+  // diffusion: ln B = lnK + (Q + P V) invRn / T - an phi; eta also carries d^(m/n)
+  double lin_n, lin_invn, lin_lnK, lin_Q, lin_V, lin_invRn, lin_m, lin_mn, lin_an;
   // grain-boundary sliding (bracket only: C_gbs is never set by the reference)
-  double gbs_n, gbs_lnK, gbs_Q, gbs_V, gbs_invRn, gbs_mn, gbs_an;
-  double gbs_A, gbs_F, gbs_m, gbs_r, gbs_f, gbs_a;
-  // Peierls: ST = EaR g2 / T, ln Arr = -EaR om2 / T
-  double exp_EaR, exp_g2, exp_om2, exp_n, exp_lngS, exp_lnE, exp_gamma, exp_S, exp_E, exp_Ea;
+  double gbs_n, gbs_invn, gbs_lnK, gbs_Q, gbs_V, gbs_invRn, gbs_m, gbs_mn, gbs_an;
+  // Peierls: ST = EaR g2 / T; Eii_exp = exp(lnA0 - EaR om2 / T) (s3gS Tii)^(ST+n)
+  double exp_EaR, exp_g2, exp_om2, exp_n, exp_lnA0, exp_s3gS;
   // constant viscosity
   double eta0, eta0_two;
   // plasticity
   double Slim, eta_vp, n_vp, T_st;
   // grain size / wattmeter
-  double gs_ref, ln_gs_ref, Kpzm, Qpzm, Gpzm, Lpzm, cpzm, ppzm;
+  double gs_ref, inv_gs_ref, ln_gs_ref, Kpzm, Qpzm, Gpzm, Lpzm, cpzm, ppzm;
   // density
   double rho, drho, alp, bet, T0, P0, rho_reac;
 };
@@ -87,16 +90,17 @@ struct NodeIn {
   double Exx, Ezz, Exz, Txx0, Tzz0, Txz0;
   double G, T, P, d, phi, X0, dil, fric, C, P0, T0, beta;
   double lxlz, lx2, ani_fac;  // anisotropic nodes
-  int centroid, final_update, post_process;
+  int centroid, final_update, post_process, want_rho;
 };
 
 struct NodeCtx {
-  double Eii, lnEii, T, Traw, invT, lnd, K, G, dil, eta_el, sin_fric, cos_fric, sin_dil;
+  double Eii, lnEii, T, Traw, invT, lnd, K, G, dil, eta_el, inv_eta_el, sin_fric, cos_fric, sin_dil;
+  double inv2Eii, inv_Kdt, inv_d;
   int elastic, plastic_on;  // plastic_on = (step != 0)
 };
 
 struct PointOut {
-  double eta, Txx, Tzz, Txz, etaVE, Eii_el, Eii_pl, Eii_pwl, Eii_exp, Eii_lin, Eii_gbs, Eii_cst, d1,
+  double eta, Txx, Tzz, Txz, etaVE, Eii_el, Eii_pl, Eii_pwl, Eii_exp, Eii_lin, Eii_gbs, Eii_cst, d1, inv_d1,
       X1, OverS, Pcorr, rho, div_el, div_pl, Wtot, Wel, Wdiss;
   int iters, is_pl, status;
 };
@@ -108,26 +112,34 @@ __device__ __forceinline__ void set_status(int &st, int code) {
 // ---------------------------------------------------------------------------------------
 // node set-up: invariants and switches shared by the phases (RheologyDensity.c:461-496)
 // ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c) {
+  c.lnEii = log(c.Eii);
+  c.inv2Eii = 0.5 / c.Eii;
+  c.Traw = in.T;
+  c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
+  c.invT = 1.0 / c.T;
+  c.lnd = need_lnd ? log(in.d) : 0.0;
+  c.inv_d = 0.0;
+  sincos(in.fric, &c.sin_fric, &c.cos_fric);
+  c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
+}
+
 __device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn &in, bool need_lnd,
                                                NodeCtx &c) {
   const double Eyy = -(in.Exx + in.Ezz);
   double Eii = sqrt(0.5 * (in.Exx * in.Exx + in.Ezz * in.Ezz + Eyy * Eyy) + in.Exz * in.Exz);
   if (Eii * M.scale_E < 1e-30) Eii = M.Eii_floor;
   c.Eii = Eii;
-  c.lnEii = log(Eii);
   c.elastic = (M.step == 0) ? 0 : M.elastic;
   c.plastic_on = (M.step != 0);
-  c.Traw = in.T;
-  c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
-  c.invT = 1.0 / c.T;
   c.K = 1.0 / in.beta;
   c.G = in.G;
   c.dil = in.dil;
   if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; c.K = 1e10; }
   c.eta_el = c.G * M.dt;
-  c.lnd = need_lnd ? log(in.d) : 0.0;
-  sincos(in.fric, &c.sin_fric, &c.cos_fric);
-  c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
+  c.inv_eta_el = 1.0 / c.eta_el;
+  c.inv_Kdt = 1.0 / (c.K * M.dt);
+  node_common(M, in, need_lnd, c);
 }
 
 // EvaluateDensity, RheologyDensity.c:1761-1831 (models 0, 1, 3, 5)
@@ -150,58 +162,154 @@ __device__ __forceinline__ double density(const ModelConst &M, const PhaseConst 
   return rho;
 }
 
-// Local VE solve coefficients of one (node, phase): Eii_k = exp(lnC_k + n_k ln Tii).
-struct VeCoef {
-  double Eii, inv2eta_el, half_inv_cst, dfd_const;  // dfd_const = -el Eii/eta_el - Eii/eta_cst
-  double lnC_pwl, n_pwl, lnC_exp, n_exp, lnC_lin, C_lin1, n_lin;
-  int mech;  // F_CST | F_PWL | F_EXPV (active Peierls) | F_LIN | F_LIN1 | F_GBS
-  int elastic;
+// ---------------------------------------------------------------------------------------
+// Creep laws of one (node, phase).  ln B and the isolated-viscosity reciprocals 1/eta_k
+// (RheologyDensity.c:501-523, 559-592), the forms documented at the top of the file.
+// ---------------------------------------------------------------------------------------
+enum { K_PWL = 0, K_EXP = 1, K_LIN = 2, K_COUNT = 3 };
+
+struct Laws {
+  int mech;            // F_CST | F_PWL | F_EXPV (active) | F_LIN | F_GBS
+  double inv[K_COUNT]; // 1/eta_k at the node's Eii (0 where inactive)
+  double n[K_COUNT];   // exponents n_pwl, ST + n_exp, n_lin
+  double lnB_pwl, lnB_lin, lnA_exp, ST, inv_gbs;
 };
 
-// LocalIterationViscoElastic, RheologyDensity.c:152-197, in log form.
+__device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst &ph, const NodeCtx &c, double P,
+                                           double phi, double lnd, int peierls, Laws &L) {
+  const int fl = ph.flags;
+  L.mech = (fl & (F_CST | F_PWL | F_LIN | F_GBS)) | (peierls ? F_EXPV : 0);
+  L.inv[0] = L.inv[1] = L.inv[2] = 0.0;
+  L.n[0] = ph.pwl_n; L.n[1] = 0.0; L.n[2] = ph.lin_n;
+  L.lnB_pwl = L.lnB_lin = L.lnA_exp = L.ST = L.inv_gbs = 0.0;
+  const double Eii = c.Eii, lnEii = c.lnEii;
+  if (fl & F_PWL) {
+    // B = pref F A^(-1/n) exp((Q+PV)/(RnT)) d^(m/n) f^(-r/n) exp(-a phi/n);
+    // 1/eta_pwl = Eii^(1-1/n) / B = Eii exp(-lnB - lnEii/n)
+    double lnB = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
+    if (fl & F_PWL_M) lnB += ph.pwl_mn * lnd;
+    if (fl & F_PWL_A) lnB -= ph.pwl_an * phi;
+    L.lnB_pwl = lnB;
+    L.inv[K_PWL] = Eii * exp(-fma(lnEii, ph.pwl_invn, lnB));
+  }
+  if (fl & F_LIN) {
+    // 1/eta_lin = Eii^(1-1/n) / (B d^(m/n))
+    double lnB = ph.lin_lnK + (ph.lin_Q + P * ph.lin_V) * ph.lin_invRn * c.invT;
+    if (fl & F_LIN_A) lnB -= ph.lin_an * phi;
+    L.lnB_lin = lnB;
+    const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, lnB) : lnB;
+    L.inv[K_LIN] = Eii * exp(-fma(lnEii, ph.lin_invn, lnBd));
+  }
+  if (peierls) {
+    // Eii_exp(Tii) = A (sqrt3 Tii / (gamma S))^nE, A = (sqrt3/2) E Arr (gamma S)^n;
+    // isolated: Tii* = (gamma S / sqrt3) (Eii/A)^(1/nE), 1/eta_exp = 2 Eii / Tii*
+    L.ST = ph.exp_EaR * c.invT * ph.exp_g2;
+    const double nE = L.ST + ph.exp_n;
+    L.n[K_EXP] = nE;
+    L.lnA_exp = ph.exp_lnA0 - ph.exp_EaR * ph.exp_om2 * c.invT;
+    L.inv[K_EXP] = 2.0 * Eii * ph.exp_s3gS * exp(-(lnEii - L.lnA_exp) / nE);
+  }
+  if (fl & F_GBS) {
+    double lnB = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * phi;
+    if (ph.gbs_m != 0.0) lnB += ph.gbs_mn * lnd;
+    L.inv_gbs = Eii * exp(-fma(lnEii, ph.gbs_invn, lnB));
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Local VE residual  r(eta) = Eii - el Tii/(2 eta_el) - sum_k Eii_k(eta),  Tii = 2 eta Eii
+// (LocalIterationViscoElastic, RheologyDensity.c:152-197).  Linear terms (elasticity,
+// constant viscosity, Newtonian laws) are eta * a_k; non-linear ones
+// Eii exp(n_k (log(eta inv_p) + c_k)).
+// ---------------------------------------------------------------------------------------
+struct VeCoef {
+  double Eii, thr_conv, thr_fail;  // Eii * tol/100, Eii * tol
+  double A;                        // sum of the linear coefficients (el, cst, Newtonian laws)
+  double a_cst, a_lin1, a_pwl1;    // e_cst = eta a_cst, e_lin = eta a_lin1 (n_lin==1), e_pwl = eta a_pwl1 (n_pwl==1)
+  double inv_p;                    // 1/eta of the primary (softest) non-linear law
+  double n[K_COUNT], nc[K_COUNT];  // exponent and n_k * log(eta_p / eta_k) per non-linear law
+  int nl;                          // bit k: law k is non-linear and active
+};
+
 struct VeState {
   double eta, Tii, e_cst, e_pwl, e_exp, e_lin;
   int iters, status;
 };
 
-__device__ __forceinline__ void ve_eval(const VeCoef &q, double eta, VeState &s, double &r, double &dfdeta) {
-  const double Tii = 2.0 * eta * q.Eii;
-  double e_cst = 0.0, e_pwl = 0.0, e_exp = 0.0, e_lin = 0.0;
-  if (Tii > 0.0) {
-    const double lnT = (q.mech & (F_PWL | F_EXPV | F_LIN)) ? log(Tii) : 0.0;
-    if (q.mech & F_PWL) e_pwl = exp(fma(q.n_pwl, lnT, q.lnC_pwl));
-    if (q.mech & F_EXPV) e_exp = exp(fma(q.n_exp, lnT, q.lnC_exp));
-    if (q.mech & F_LIN) e_lin = (q.mech & F_LIN1) ? q.C_lin1 * Tii : exp(fma(q.n_lin, lnT, q.lnC_lin));
-  } else {  // outside the log domain: the reference's pow on a non-positive base
-    if (q.mech & F_PWL) e_pwl = exp(q.lnC_pwl) * pow(Tii, q.n_pwl);
-    if (q.mech & F_EXPV) e_exp = exp(q.lnC_exp) * pow(Tii, q.n_exp);
-    if (q.mech & F_LIN) e_lin = ((q.mech & F_LIN1) ? q.C_lin1 : exp(q.lnC_lin)) * pow(Tii, q.n_lin);
+__device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double eta_cst, VeCoef &q) {
+  const double Eii = c.Eii;
+  const double tol = 1.0e-11;  // hard-coded in LocalIterationViscoElastic (:154)
+  q.Eii = Eii;
+  q.thr_conv = Eii * (tol / 100);
+  q.thr_fail = Eii * tol;
+  q.a_cst = (L.mech & F_CST) ? Eii / eta_cst : 0.0;
+  q.A = (c.elastic ? Eii * c.inv_eta_el : 0.0) + q.a_cst;
+  q.a_lin1 = q.a_pwl1 = 0.0;
+  q.nl = 0;
+  double inv_p = 0.0;
+  int p = -1;
+#pragma unroll
+  for (int k = 0; k < K_COUNT; k++) {
+    const int bit = (k == K_PWL) ? F_PWL : ((k == K_EXP) ? F_EXPV : F_LIN);
+    q.n[k] = L.n[k];
+    q.nc[k] = 0.0;
+    if (!(L.mech & bit)) continue;
+    if (k != K_EXP && L.n[k] == 1.0) {  // Newtonian law: Eii eta / eta_k
+      const double a = Eii * L.inv[k];
+      if (k == K_LIN) q.a_lin1 = a;
+      else q.a_pwl1 = a;
+      q.A += a;
+    } else {
+      q.nl |= 1 << k;
+      if (L.inv[k] > inv_p) { inv_p = L.inv[k]; p = k; }
+    }
   }
-  if (q.mech & F_CST) e_cst = Tii * q.half_inv_cst;
-  const double e_vis = e_pwl + e_exp + e_lin + e_cst;
-  r = q.Eii - q.elastic * Tii * q.inv2eta_el - e_vis;
-  dfdeta = q.dfd_const - (e_exp * q.n_exp + e_lin * q.n_lin + e_pwl * q.n_pwl) / eta;
-  s.Tii = Tii; s.e_cst = e_cst; s.e_pwl = e_pwl; s.e_exp = e_exp; s.e_lin = e_lin;
+  if (!(inv_p > 0.0)) q.nl = 0;  // every non-linear law underflowed: they carry no strain rate
+  q.inv_p = inv_p;
+  if (q.nl) {
+    const double r_p = 1.0 / inv_p;
+#pragma unroll
+    for (int k = 0; k < K_COUNT; k++)
+      if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * log(L.inv[k] * r_p);
+  }
 }
 
+__device__ __forceinline__ void ve_eval(const VeCoef &q, double eta, VeState &s, double &r, double &S) {
+  double e[K_COUNT] = {0.0, 0.0, 0.0};
+  S = 0.0;
+  if (q.nl) {
+    const double lx = log(eta * q.inv_p);
+#pragma unroll
+    for (int k = 0; k < K_COUNT; k++)
+      if (q.nl >> k & 1) {
+        e[k] = q.Eii * exp(fma(q.n[k], lx, q.nc[k]));
+        S = fma(q.n[k], e[k], S);
+      }
+  }
+  s.e_cst = eta * q.a_cst;
+  s.e_pwl = (q.nl >> K_PWL & 1) ? e[K_PWL] : eta * q.a_pwl1;
+  s.e_lin = (q.nl >> K_LIN & 1) ? e[K_LIN] : eta * q.a_lin1;
+  s.e_exp = e[K_EXP];
+  s.Tii = 2.0 * eta * q.Eii;
+  r = q.Eii - eta * q.A - (e[K_PWL] + e[K_EXP] + e[K_LIN]);
+}
+
+// Newton from s.eta: eta <- eta - r / r'(eta),  r' = -A - S/eta  (LocalIterationViscoElastic)
 __device__ __forceinline__ void ve_newton(const VeCoef &q, VeState &s) {
   const int nitmax = 20;
-  const double tol = 1.0e-11;
   double eta = s.eta;
   s.iters = nitmax;
   for (int it = 0; it < nitmax; it++) {
-    double r, dfdeta;
-    ve_eval(q, eta, s, r, dfdeta);
-    const double res = fabs(r / q.Eii);
-    if (res < tol / 100) { s.iters = it + 1; break; }
-    if (it == nitmax - 1 && res > tol) { set_status(s.status, MDZ_EVE_ITER); break; }
-    eta -= r / dfdeta;
+    double r, S;
+    ve_eval(q, eta, s, r, S);
+    const double ar = fabs(r);
+    if (ar < q.thr_conv) { s.iters = it + 1; break; }
+    if (it == nitmax - 1 && ar > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
+    eta += r * eta / fma(q.A, eta, S);
   }
   s.eta = eta;
 }
 
-// LocalIterationViscoElasticGrainSize, RheologyDensity.c:203-379 (faithful pow form;
-// the bracket-end evaluations at :221-243 never reach an output and are skipped).
 struct GseIn {
   double Eii, eta_el, eta_cst, C_pwl, n_pwl, C_lin, n_lin, m_lin, C_exp, ST, n_exp, eta_up, eta_lo, Ag,
       gam, lam, cg, pg;
@@ -355,6 +463,7 @@ __device__ inline int plastic_popov(const ModelConst &M, const PhaseConst &ph, d
   return 1;
 }
 
+
 // ---------------------------------------------------------------------------------------
 // ViscosityConcise (RheologyDensity.c:385-1080) for phase `ph` at a node prepared by
 // node_setup_iso.  `warm_eta` > 0 replaces the initial guess eta_up (learned warm start).
@@ -367,97 +476,57 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
   const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
   const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
   const int elastic = c.elastic;
-  const double T = c.T, P = in.P, Eii = c.Eii, lnEii = c.lnEii, eta_el = c.eta_el, K = c.K, dt = M.dt;
+  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt;
   o.status = MDZ_OK;
   o.Pcorr = P;
   o.X1 = in.X0;
-  o.Eii_gbs = 0.0;
+  o.Eii_gbs = 0.0;  // C_gbs is never set by the reference (:616-642)
   o.OverS = 0.0;
   o.Wtot = o.Wel = o.Wdiss = 0.0;
   o.Eii_el = 0.0;
   o.rho = 0.0;
-  double d = in.d, lnd = c.lnd;
   o.d1 = ph.gs_ref;
+  o.inv_d1 = ph.inv_gs_ref;
+  if (diffusion && ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
 
-  // Arrhenius pre-factors in log space (RheologyDensity.c:501-523)
-  double lnB_pwl = 0.0, lnB_lin = 0.0, lnB_exp = 0.0, ST = 0.0, nE = 0.0;
-  if (dislocation) {
-    lnB_pwl = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
-    if (fl & F_PWL_M) lnB_pwl += ph.pwl_mn * lnd;
-    if (fl & F_PWL_A) lnB_pwl -= ph.pwl_an * in.phi;
-  }
-  if (diffusion) {
-    if (ph.lin_m > 0.0 && d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
-    lnB_lin = ph.lin_lnK + (ph.lin_Q + P * ph.lin_V) * ph.lin_invRn * c.invT;
-    if (fl & F_LIN_A) lnB_lin -= ph.lin_an * in.phi;
-  }
-  if (peierls) {
-    ST = ph.exp_EaR * c.invT * ph.exp_g2;
-    nE = ST + ph.exp_n;
-    const double inv_nE = 1.0 / nE;
-    const double lnArr = -ph.exp_EaR * c.invT * ph.exp_om2;
-    const double lnF = ((1.0 - nE) * kLn2 - (nE + 1.0) * (0.5 * 1.09861228866810969140)) * inv_nE;
-    lnB_exp = lnF + (ST * ph.exp_lngS - ph.exp_lnE - lnArr) * inv_nE;
-  }
-  // Tyield with the von Mises cut-off (:530-539)
+  Laws L;
+  creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
   double Tyield = 0.0, C = in.C;
-  if (plastic == 1) {
+  if (plastic == 1) {  // :530-539
     Tyield = C * c.cos_fric + P * c.sin_fric;
     if (ph.Slim < Tyield) { C = ph.Slim; Tyield = ph.Slim; }
   }
-
-  // isolated viscosities and the bracket (:559-592)
-  double eta_cst = 0.0, eta_pwl = 0.0, eta_lin = 0.0, eta_gbs = 0.0, eta_exp = 0.0, Ag = 0.0;
+  double eta_cst = 0.0, Ag = 0.0, lnd = c.lnd;
   if (constant) eta_cst = ph.eta0;
-  if (fl & F_CMIX) {
+  if (fl & F_CMIX) {  // :563-565
     const double X0 = in.X0, e1 = ph.eta0, e2 = ph.eta0_two;
     if (M.diffuse_avg == 0) eta_cst = X0 * e1 + (1 - X0) * e2;
     if (M.diffuse_avg == 1) eta_cst = pow(X0 / e1 + (1 - X0) / e2, -1.0);
     if (M.diffuse_avg == 2) eta_cst = exp(X0 * log(e1) + (1 - X0) * log(e2));
   }
-  if (dislocation) eta_pwl = exp(fma(1.0 / ph.pwl_n - 1.0, lnEii, lnB_pwl));
-  if (gs) {  // wattmeter grain size (:567-576)
+  if (gs) {  // wattmeter grain size before eta_lin (:567-576)
     Ag = ph.Kpzm * exp(-ph.Qpzm / M.R / T);
     const double Tii0 = 2. * eta_el * Eii;
-    const double epwl0 = Tii0 / 2.0 / eta_pwl;
-    d = exp(log(Ag * ph.Gpzm / (ph.Lpzm * (1.0 / ph.cpzm) * Tii0 * epwl0 * ph.ppzm)) / (1.0 + ph.ppzm));
+    const double epwl0 = Tii0 / 2.0 * L.inv[K_PWL];
+    const double d = exp(log(Ag * ph.Gpzm / (ph.Lpzm * (1.0 / ph.cpzm) * Tii0 * epwl0 * ph.ppzm)) / (1.0 + ph.ppzm));
+    o.d1 = d;
     lnd = log(d);
+    if (diffusion) {
+      const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, L.lnB_lin) : L.lnB_lin;
+      L.inv[K_LIN] = Eii * exp(-fma(c.lnEii, ph.lin_invn, lnBd));
+    }
   }
-  if (diffusion) eta_lin = exp(fma(1.0 / ph.lin_n - 1.0, lnEii, lnB_lin + (ph.lin_m != 0.0 ? ph.lin_mn * lnd : 0.0)));
-  if (gbs) {
-    double lnB_gbs = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * in.phi;
-    if (ph.gbs_m != 0.0) lnB_gbs += ph.gbs_mn * lnd;
-    eta_gbs = exp(fma(1.0 / ph.gbs_n - 1.0, lnEii, lnB_gbs));
-  }
-  if (peierls) eta_exp = exp(fma(1.0 / nE - 1.0, lnEii, lnB_exp));
-  double eta_up = M.eta_up0, eta_lo = M.eta_lo0;
-  if (constant) { eta_up = fmin(eta_up, eta_cst); eta_lo = fmax(eta_lo, eta_cst); }
-  if (dislocation) { eta_up = fmin(eta_up, eta_pwl); eta_lo = fmax(eta_lo, eta_pwl); }
-  if (elastic == 1) { eta_up = fmin(eta_up, eta_el); eta_lo = fmax(eta_lo, eta_el); }
-  if (peierls) { eta_up = fmin(eta_up, eta_exp); eta_lo = fmax(eta_lo, eta_exp); }
-  if (diffusion) { eta_up = fmin(eta_up, eta_lin); eta_lo = fmax(eta_lo, eta_lin); }
-  if (gbs) { eta_up = fmin(eta_up, eta_gbs); eta_lo = fmax(eta_lo, eta_gbs); }
-  if (gs) o.d1 = d;
+  // bracket (:582-592): the smallest isolated viscosity is 1 / the largest reciprocal
+  const double inv_max = fmax(fmax(L.inv[K_PWL], L.inv[K_EXP]), fmax(L.inv[K_LIN], L.inv_gbs));
+  double eta_up = M.eta_up0;
+  if (constant) eta_up = fmin(eta_up, eta_cst);
+  if (inv_max > 0.0) eta_up = fmin(eta_up, 1.0 / inv_max);
+  if (elastic == 1) eta_up = fmin(eta_up, eta_el);
 
-  // local visco-elastic solve (:597-647)
-  const double lnC_pwl = -ph.pwl_n * (kLn2 + lnB_pwl);
-  const double lnC_lin = -ph.lin_n * (kLn2 + lnB_lin);
-  const double lnC_exp = -nE * (kLn2 + lnB_exp);
   double eta_ve, Tii, e_cst, e_pwl, e_exp, e_lin;
-  if (!gs) {
+  if (!gs) {  // LocalIterationViscoElastic (:646)
     VeCoef q;
-    q.Eii = Eii;
-    q.elastic = elastic;
-    q.inv2eta_el = 1.0 / (2.0 * eta_el);
-    q.half_inv_cst = constant ? 0.5 / eta_cst : 0.0;
-    q.dfd_const = (elastic ? -Eii / eta_el : 0.0) + (constant ? -Eii / eta_cst : 0.0);
-    q.mech = (constant ? F_CST : 0) | (dislocation ? F_PWL : 0) | (peierls ? F_EXPV : 0) |
-             (diffusion ? (F_LIN | ((fl & F_LIN1) ? F_LIN1 : 0)) : 0);
-    q.lnC_pwl = lnC_pwl; q.n_pwl = dislocation ? ph.pwl_n : 0.0;
-    q.lnC_exp = lnC_exp; q.n_exp = peierls ? nE : 0.0;
-    q.lnC_lin = diffusion ? lnC_lin - (ph.lin_m != 0.0 ? ph.lin_m * lnd : 0.0) : 0.0;
-    q.C_lin1 = (diffusion && (fl & F_LIN1)) ? exp(q.lnC_lin) : 0.0;
-    q.n_lin = diffusion ? ph.lin_n : 0.0;
+    ve_coef(L, c, eta_cst, q);
     VeState s;
     s.eta = (warm_eta > 0.0) ? warm_eta : eta_up;
     s.status = MDZ_OK;
@@ -465,11 +534,20 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
     set_status(o.status, s.status);
     eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
     o.iters = s.iters;
-  } else {
+  } else {  // LocalIterationViscoElasticGrainSize (:644)
+    double eta_lo = M.eta_lo0;
+    if (constant) eta_lo = fmax(eta_lo, eta_cst);
+    if (dislocation) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_PWL]);
+    if (elastic == 1) eta_lo = fmax(eta_lo, eta_el);
+    if (peierls) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_EXP]);
+    if (diffusion) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_LIN]);
+    if (gbs) eta_lo = fmax(eta_lo, 1.0 / L.inv_gbs);
     GseIn g;
-    g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst; g.C_pwl = exp(lnC_pwl); g.n_pwl = ph.pwl_n;
-    g.C_lin = exp(lnC_lin); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m; g.C_exp = exp(lnC_exp); g.ST = ST;
-    g.n_exp = ph.exp_n; g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = Ag; g.gam = ph.Gpzm; g.lam = ph.Lpzm;
+    g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst;
+    g.C_pwl = exp(-ph.pwl_n * (kLn2 + L.lnB_pwl)); g.n_pwl = ph.pwl_n;
+    g.C_lin = exp(-ph.lin_n * (kLn2 + L.lnB_lin)); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m;
+    g.C_exp = exp(fma(L.n[K_EXP], log(ph.exp_s3gS), L.lnA_exp)); g.ST = L.ST; g.n_exp = ph.exp_n;
+    g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = Ag; g.gam = ph.Gpzm; g.lam = ph.Lpzm;
     g.cg = ph.cpzm; g.pg = ph.ppzm; g.elastic = elastic; g.constant = constant; g.dislocation = dislocation;
     g.peierls = peierls; g.diffusion = diffusion;
     eta_ve = eta_up;
@@ -479,6 +557,7 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
     ve_gse(g, eta_ve, Tii, dd, e_cst, e_pwl, e_exp, e_lin, o.iters, st);
     set_status(o.status, st);
     o.d1 = dd;
+    o.inv_d1 = 1.0 / dd;
   }
   const double Tii_ve = Tii;
 
@@ -504,12 +583,12 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
         Tiic = Tii - eta_ve * gdot;
         F = Tiic - Tyield;
         const double res = fabs(F);
-        if (res < tol || res / F0 < tol) break;
+        if (res < tol || res < tol * F0) break;
         gdot -= F / (-eta_ve - eta_vp / n_vp - ksd);
       }
-      if (Tiic < 0.0) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }
+      if (Tiic < 0.0) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }  // :697-704
       o.Pcorr = Pc;
-      eta_vep = Tiic / (2.0 * Eii);
+      eta_vep = Tiic * c.inv2Eii;
       Tii = Tiic;
     }
   }
@@ -522,19 +601,19 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
     set_status(o.status, st);
     if (is_pl) {
       o.Pcorr = Pc;
-      eta_vep = Tn / (2.0 * Eii);
+      eta_vep = Tn * c.inv2Eii;
       Tii = Tn;
       divp = lam_dot * A_P;
     }
   }
 
-  // density on centroids (:934-960)
-  if (in.centroid > 0) o.rho = density(M, ph, T, (in.final_update == 1) ? Pc : P, in.X0, in.phi);
+  // density on centroids (:934-960); only density_variations==1 lets it reach the grid
+  if (in.centroid > 0 && in.want_rho) o.rho = density(M, ph, T, (in.final_update == 1) ? Pc : P, in.X0, in.phi);
 
-  double eta_pl = 0.0;
+  double inv_eta_pl = 0.0;
   if (is_pl == 0) o.etaVE = eta_ve;
-  else if (plastic == 1) { o.etaVE = eta_vep; eta_pl = Tii / gdot; }
-  else { o.etaVE = eta_vep; eta_pl = Tii / (2.0 * lam_dot * A_tau); }
+  else if (plastic == 1) { o.etaVE = eta_vep; inv_eta_pl = gdot / Tii; }
+  else { o.etaVE = eta_vep; inv_eta_pl = 2.0 * lam_dot * A_tau / Tii; }
   o.is_pl = is_pl;
   o.Txx = 2.0 * o.etaVE * in.Exx;
   o.Tzz = 2.0 * o.etaVE * in.Ezz;
@@ -543,21 +622,21 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
 
   double eta = 0.0;
   if (in.post_process == 1) {  // :986-1053
+    const double inv_half_T = 2.0 / Tii_ve;  // 1/eta_k = 2 Eii_k / Tii
     double inv = 0.0;
-    const double half_T = 0.5 * Tii_ve;
-    if (peierls) inv += e_exp / half_T;           // 1/eta_exp, eta_exp = Tii/(2 Eii_exp)
-    if (dislocation) inv += e_pwl / half_T;
+    if (peierls) inv += e_exp * inv_half_T;
+    if (dislocation) inv += e_pwl * inv_half_T;
     if (diffusion) {
-      // eta_lin = B pow(Eii_lin, 1/n-1) pow(d1, m/n) = Tii/(2 Eii_lin) (d1/d)^(m/n)
-      double inv_lin = e_lin / half_T;
+      // eta_lin = B pow(Eii_lin, 1/n-1) pow(d1, m/n) = Tii/(2 Eii_lin) (d1/d)^(m/n), d1 = gs_ref
+      double inv_lin = e_lin * inv_half_T;
       if (ph.lin_m != 0.0 && !gs) inv_lin *= exp(ph.lin_mn * (lnd - ph.ln_gs_ref));
       inv += inv_lin;
     }
     if (constant) inv += (1.0 / eta_cst);
-    if (is_pl == 1) inv += (1.0 / eta_pl);
+    if (is_pl == 1) inv += inv_eta_pl;
     eta = 1.0 / inv;
     if (elastic) {
-      const double h = 0.5 / eta_el;
+      const double h = 0.5 * c.inv_eta_el;
       const double Tyy = -(o.Txx + o.Tzz), Tyy0 = -(in.Txx0 + in.Tzz0);
       const double ex = (o.Txx - in.Txx0) * h, ez = (o.Tzz - in.Tzz0) * h;
       const double ey = (Tyy - Tyy0) * h, exz = (o.Txz - in.Txz0) * h;
@@ -565,14 +644,14 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
     }
     o.Eii_pl = (is_pl && plastic == 1) ? gdot / 2.0 : ((is_pl && plastic == 2) ? lam_dot * A_tau : 0.0);
     o.div_pl = divp;
-    o.div_el = -(Pc - in.P0) / (K * dt);
+    o.div_el = -(Pc - in.P0) * c.inv_Kdt;
     if (plastic == 1) o.OverS = eta_vp * gdot;
     if (plastic == 2) o.OverS = eta_vp * lam_dot * A_tau;
     if (in.centroid == 1) {
       const double T2 = Tii * Tii;
       o.Wtot = T2 / eta_ve;
-      o.Wel = T2 / eta_el;
-      o.Wdiss = T2 / eta;
+      o.Wel = T2 * c.inv_eta_el;
+      o.Wdiss = T2 * inv;
       if (o.Wdiss < 0.0) set_status(o.status, MDZ_EWDISS);
     }
   } else {
@@ -587,7 +666,6 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
   if (eta < M.min_eta) eta = M.min_eta;
   o.eta = eta;
 }
-
 
 // ---------------------------------------------------------------------------------------
 // ViscosityConciseAniso (AnisotropyRoutines.c:282-727).  The node context carries the
@@ -606,20 +684,17 @@ __device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const Node
   a.Er_xz = -lxlz * in.Exx + lxlz * in.Ezz + (lx2 - nz2) * in.Exz;
   const double Er_yy = -a.Er_xx - a.Er_zz;
   c.Eii = sqrt(0.5 * (a.Er_xx * a.Er_xx + a.Er_zz * a.Er_zz + Er_yy * Er_yy) + a.Er_xz * a.Er_xz);
-  c.lnEii = log(c.Eii);
   c.elastic = (M.step == 0) ? 0 : M.elastic;
   c.plastic_on = 1;
-  c.Traw = in.T;
-  c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
-  c.invT = 1.0 / c.T;
   c.K = 1.0 / in.beta;
   c.G = in.G;
   c.dil = in.dil;
   if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; }
   c.eta_el = c.elastic ? c.G * M.dt_model : 1e20;
-  c.lnd = need_lnd ? log(in.d) : 0.0;
-  sincos(in.fric, &c.sin_fric, &c.cos_fric);
-  c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
+  c.inv_eta_el = 1.0 / c.eta_el;
+  c.inv_Kdt = 1.0 / (c.K * M.dt_model);
+  node_common(M, in, need_lnd, c);
+  c.inv_d = 1.0 / in.d;
 }
 
 __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
@@ -629,60 +704,44 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
   const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
   const int plastic = (fl & F_PLANY) != 0;
   const int elastic = c.elastic;
-  const double T = c.T, P = in.P, Eii = c.Eii, lnEii = c.lnEii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
-  const double tol = 1e-11, min_eta = M.min_eta, max_eta = M.max_eta;
+  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
+  const double min_eta = M.min_eta, max_eta = M.max_eta;
   o.status = MDZ_OK;
   o.Pcorr = P;
   o.X1 = 0.0; o.rho = 0.0; o.Eii_gbs = 0.0; o.Eii_el = 0.0; o.Eii_pl = 0.0; o.div_pl = 0.0; o.div_el = 0.0;
   o.OverS = 0.0; o.Wtot = o.Wel = o.Wdiss = 0.0;
   o.d1 = in.d;
-  const double lnd = c.lnd;
+  o.inv_d1 = c.inv_d;
+  if (diffusion && ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
 
-  double lnB_pwl = 0.0, lnB_lin = 0.0, lnB_exp = 0.0, ST = 0.0, nE = 0.0;
-  if (dislocation) {  // :334-337
-    lnB_pwl = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
-    if (fl & F_PWL_M) lnB_pwl += ph.pwl_mn * lnd;
-    if (fl & F_PWL_A) lnB_pwl -= ph.pwl_an * in.phi;
-  }
-  if (diffusion) {  // :342-349
-    if (ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
-    lnB_lin = ph.lin_lnK + (ph.lin_Q + P * ph.lin_V) * ph.lin_invRn * c.invT;
-    if (fl & F_LIN_A) lnB_lin -= ph.lin_an * in.phi;
-  }
-  if (peierls) {  // :355-362
-    ST = ph.exp_EaR * c.invT * ph.exp_g2;
-    nE = ST + ph.exp_n;
-    const double inv_nE = 1.0 / nE;
-    const double lnArr = -ph.exp_EaR * c.invT * ph.exp_om2;
-    const double lnF = ((1.0 - nE) * kLn2 - (nE + 1.0) * (0.5 * 1.09861228866810969140)) * inv_nE;
-    lnB_exp = lnF + (ST * ph.exp_lngS - ph.exp_lnE - lnArr) * inv_nE;
-  }
+  Laws L;
+  creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
+  L.mech &= ~F_GBS;  // the anisotropic path has no grain-boundary sliding
+  L.inv_gbs = 0.0;
   double Tyield = 0.0, Coh = in.C;
   if (plastic) {  // :370-377
     Tyield = Coh * c.cos_fric + P * c.sin_fric;
     if (ph.Slim < Tyield) { Coh = ph.Slim; Tyield = ph.Slim; }
   }
-  double eta_cst = 0.0, eta_pwl = 0.0, eta_lin = 0.0, eta_exp = 0.0;  // :390-397
-  if (constant) eta_cst = ph.eta0;
-  if (dislocation) eta_pwl = exp(fma(1.0 / ph.pwl_n - 1.0, lnEii, lnB_pwl));
-  if (diffusion) eta_lin = exp(fma(1.0 / ph.lin_n - 1.0, lnEii, lnB_lin + (ph.lin_m != 0.0 ? ph.lin_mn * lnd : 0.0)));
-  if (peierls) eta_exp = exp(fma(1.0 / nE - 1.0, lnEii, lnB_exp));
-  double eta_up = M.eta_up0, eta_lo = M.eta_lo0;  // :409-415
+  const double eta_cst = constant ? ph.eta0 : 0.0;
+  // bracket (:409-415)
+  const double inv_max = fmax(fmax(L.inv[K_PWL], L.inv[K_EXP]), L.inv[K_LIN]);
+  double eta_up = M.eta_up0, eta_lo = M.eta_lo0;
   if (constant) { eta_up = fmin(eta_up, eta_cst); eta_lo = fmax(eta_lo, eta_cst); }
-  if (dislocation) { eta_up = fmin(eta_up, eta_pwl); eta_lo = fmax(eta_lo, eta_pwl); }
+  if (inv_max > 0.0) eta_up = fmin(eta_up, 1.0 / inv_max);
   if (elastic) { eta_up = fmin(eta_up, eta_el); eta_lo = fmax(eta_lo, eta_el); }
-  if (peierls) { eta_up = fmin(eta_up, eta_exp); eta_lo = fmax(eta_lo, eta_exp); }
-  if (diffusion) { eta_up = fmin(eta_up, eta_lin); eta_lo = fmax(eta_lo, eta_lin); }
+  if (dislocation) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_PWL]);
+  if (peierls) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_EXP]);
+  if (diffusion) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_LIN]);
 
-  const double lnC_pwl = -ph.pwl_n * (kLn2 + lnB_pwl);
-  const double lnC_lin = -ph.lin_n * (kLn2 + lnB_lin);
-  const double lnC_exp = -nE * (kLn2 + lnB_exp);
   double eta_ve = eta_up, Tii = 0.0, e_cst = 0.0, e_pwl = 0.0, e_exp = 0.0, e_lin = 0.0;
   if (fl & F_GS) {  // :429-473
     GseIn g;
-    g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst; g.C_pwl = exp(lnC_pwl); g.n_pwl = ph.pwl_n;
-    g.C_lin = exp(lnC_lin); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m; g.C_exp = exp(lnC_exp); g.ST = ST;
-    g.n_exp = ph.exp_n; g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = ph.Kpzm * exp(-ph.Qpzm / (M.R * T));
+    g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst;
+    g.C_pwl = exp(-ph.pwl_n * (kLn2 + L.lnB_pwl)); g.n_pwl = ph.pwl_n;
+    g.C_lin = exp(-ph.lin_n * (kLn2 + L.lnB_lin)); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m;
+    g.C_exp = exp(fma(L.n[K_EXP], log(ph.exp_s3gS), L.lnA_exp)); g.ST = L.ST; g.n_exp = ph.exp_n;
+    g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = ph.Kpzm * exp(-ph.Qpzm / (M.R * T));
     g.gam = ph.Gpzm; g.lam = ph.Lpzm; g.cg = ph.cpzm; g.pg = ph.ppzm; g.elastic = elastic; g.constant = constant;
     g.dislocation = dislocation; g.peierls = peierls; g.diffusion = diffusion;
     double dd = in.d;
@@ -690,46 +749,37 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
     ve_gse(g, eta_ve, Tii, dd, e_cst, e_pwl, e_exp, e_lin, o.iters, st);
     set_status(o.status, st);
     o.d1 = dd;
-  } else {  // :474-585: 10 log-bisection steps, then Newton <= 50
+    o.inv_d1 = 1.0 / dd;
+  } else {  // :474-585: 10 log-space bisection steps on [min_eta 1e-3, 10 max(eta_lo, max_eta)], then Newton
+    const double tol = 1e-11;
     VeCoef q;
-    q.Eii = Eii;
-    q.elastic = elastic;
-    q.inv2eta_el = 1.0 / (2.0 * eta_el);
-    q.half_inv_cst = constant ? 0.5 / eta_cst : 0.0;
-    q.dfd_const = (elastic ? -Eii / eta_el : 0.0) + (constant ? -Eii / eta_cst : 0.0);
-    q.mech = (constant ? F_CST : 0) | (dislocation ? F_PWL : 0) | (peierls ? F_EXPV : 0) |
-             (diffusion ? (F_LIN | ((fl & F_LIN1) ? F_LIN1 : 0)) : 0);
-    q.lnC_pwl = lnC_pwl; q.n_pwl = dislocation ? ph.pwl_n : 0.0;
-    q.lnC_exp = lnC_exp; q.n_exp = peierls ? nE : 0.0;
-    q.lnC_lin = diffusion ? lnC_lin - (ph.lin_m != 0.0 ? ph.lin_m * lnd : 0.0) : 0.0;
-    q.C_lin1 = (diffusion && (fl & F_LIN1)) ? exp(q.lnC_lin) : 0.0;
-    q.n_lin = diffusion ? ph.lin_n : 0.0;
+    ve_coef(L, c, eta_cst, q);
     VeState s;
     s.status = MDZ_OK;
-    double r, dr;
+    double r, S;
     if (warm_eta > 0.0) {
       eta_ve = warm_eta;
     } else {
       double lo = min_eta * 1.0e-3, hi = 10.0 * fmax(eta_lo, max_eta);
       for (int bit = 0; bit < 10; bit++) {
         eta_ve = sqrt(lo * hi);
-        ve_eval(q, eta_ve, s, r, dr);
+        ve_eval(q, eta_ve, s, r, S);
         if (r > 0.0) lo = eta_ve;
         else hi = eta_ve;
-        if (fabs(r / Eii) < tol / 100) break;
+        if (fabs(r) < q.thr_conv) break;
       }
       eta_ve = sqrt(lo * hi);
     }
     o.iters = 50;
     for (int it = 0; it < 50; it++) {
-      ve_eval(q, eta_ve, s, r, dr);
+      ve_eval(q, eta_ve, s, r, S);
       if (isnan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
-      eta_ve -= r / dr;
+      eta_ve += r * eta_ve / fma(q.A, eta_ve, S);
       if (eta_ve <= 0.0) eta_ve = min_eta;
-      const double res = fabs(r / Eii);
-      if (res < tol / 100) { o.iters = it + 1; break; }
-      if (it == 49 && res < 10.0 * tol) break;
-      if (it == 49 && res > tol) { set_status(o.status, MDZ_EANISO_ITER); break; }
+      const double ar = fabs(r);
+      if (ar < q.thr_conv) { o.iters = it + 1; break; }
+      if (it == 49 && ar < 10.0 * tol * Eii) break;
+      if (it == 49 && ar > q.thr_fail) { set_status(o.status, MDZ_EANISO_ITER); break; }
     }
     Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
   }
@@ -745,7 +795,7 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
     gdot = Ft / (eta_ve + ph.eta_vp + K * dt * c.sin_dil * c.sin_fric);
     const double Tiic = Tii - gdot * eta_ve;
     Pc = P + K * dt * c.sin_dil * gdot;
-    eta_vep = Tiic / 2.0 / Eii;
+    eta_vep = Tiic * c.inv2Eii;
     Tr_xx = 2.0 * eta_vep * an.Er_xx;
     Tr_zz = 2.0 * eta_vep * an.Er_zz;
     Tr_xz = 2.0 * eta_vep * an.Er_xz / in.ani_fac;
@@ -764,25 +814,25 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
   o.is_pl = is_pl;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
   double eta = eta_vep;
-  if (in.post_process == 1) {  // :681-714
-    const double half_T = 0.5 * Tii_ve;
+  if (in.post_process == 1) {  // :681-714 (eta_lin uses *d, the same d as the Newton: no correction)
+    const double inv_half_T = 2.0 / Tii_ve;
     double inv = 0.0;
-    if (diffusion) inv += e_lin / half_T;
-    if (peierls) inv += e_exp / half_T;
-    if (dislocation) inv += e_pwl / half_T;
+    if (diffusion) inv += e_lin * inv_half_T;
+    if (peierls) inv += e_exp * inv_half_T;
+    if (dislocation) inv += e_pwl * inv_half_T;
     if (constant) inv += 1.0 / eta_cst;
     if (is_pl) inv += gdot / Tii;
     eta = 1.0 / inv;
-    if (elastic) o.Eii_el = Tii * Tii / (4 * eta_el * eta_el);
+    if (elastic) o.Eii_el = Tii * Tii * (0.25 * c.inv_eta_el * c.inv_eta_el);
     if (is_pl) o.Eii_pl = gdot / 2.0;
     o.div_pl = gdot * c.sin_dil;
-    o.div_el = -(Pc - in.P0) / (K * dt);
+    o.div_el = -(Pc - in.P0) * c.inv_Kdt;
     o.OverS = ph.eta_vp * gdot;
     if (in.centroid == 1) {
       const double T2 = Tii * Tii;
       o.Wtot = T2 / eta_ve;
-      o.Wel = T2 / eta_el;
-      o.Wdiss = T2 / eta;
+      o.Wel = T2 * c.inv_eta_el;
+      o.Wdiss = T2 * inv;
     }
   }
   if (eta > max_eta) eta = max_eta;  // :720-721

@@ -38,14 +38,16 @@ __device__ __forceinline__ void do_centroid(const SweepArgs &A, long long c0, Ac
     NodeIn in;
     const double mu = A.ci[CI_mu][c0];
     const double eta_e = (M.elastic == 1) ? M.dt_model * mu : 1.0;
+    const double inv_eta_e = ANISO ? 1.0 / eta_e : 0.0;
     const double el = (M.elastic == 1) ? 1.0 : 0.0;
     const double exxd = A.ci[CI_exxd][c0], ezzd = A.ci[CI_ezzd][c0], exz = A.ci[CI_exz][c0];
     in.Txx0 = A.ci[CI_sxxd0][c0]; in.Tzz0 = A.ci[CI_szzd0][c0]; in.Txz0 = A.ci[CI_sxz0][c0];
     double d1 = 0.0, d2 = 0.0, anif = 1.0;
     if (!ANISO) {
-      in.Exx = exxd + el * in.Txx0 / eta_e / 2.0;
-      in.Ezz = ezzd + el * in.Tzz0 / eta_e / 2.0;
-      in.Exz = exz + el * in.Txz0 / eta_e / 2.0;
+      const double h = el * 0.5 / eta_e;  // el / eta_e / 2
+      in.Exx = exxd + in.Txx0 * h;
+      in.Ezz = ezzd + in.Tzz0 * h;
+      in.Exz = exz + in.Txz0 * h;
     } else {
       d1 = A.ci[CI_d1][c0]; d2 = A.ci[CI_d2][c0]; anif = A.ci[CI_anif][c0];
       double sn, cs;
@@ -59,6 +61,7 @@ __device__ __forceinline__ void do_centroid(const SweepArgs &A, long long c0, Ac
     in.fric = A.ci[CI_fric][c0]; in.C = A.ci[CI_C][c0]; in.P0 = A.ci[CI_p0][c0]; in.T0 = A.ci[CI_T0][c0];
     in.beta = A.ci[CI_bet][c0];
     in.centroid = 1; in.final_update = A.final_update; in.post_process = 1;
+    in.want_rho = (M.density_variations == 1);
     NodeCtx ctx;
     AnisoNode an;
     if (ANISO) node_setup_aniso(M, in, A.need_lnd, ctx, an);
@@ -81,7 +84,7 @@ __device__ __forceinline__ void do_centroid(const SweepArgs &A, long long c0, Ac
       if (avg == 0) { out[CO_eta] += perc * o.etaVE; out[CO_eta_phys] += perc * o.eta; }
       else if (avg == 1) { out[CO_eta] += perc / o.etaVE; out[CO_eta_phys] += perc / o.eta; }
       else { out[CO_eta] += perc * log(o.etaVE); out[CO_eta_phys] += perc * log(o.eta); }
-      if (ANISO) out[CO_VE] += perc * o.etaVE / eta_e;
+      if (ANISO) out[CO_VE] += perc * o.etaVE * inv_eta_e;
       out[CO_eII_el] += perc * o.Eii_el;
       out[CO_eII_pl] += perc * o.Eii_pl;
       out[CO_eII_pwl] += perc * o.Eii_pwl;
@@ -89,7 +92,7 @@ __device__ __forceinline__ void do_centroid(const SweepArgs &A, long long c0, Ac
       out[CO_eII_lin] += perc * o.Eii_lin;
       out[CO_eII_gbs] += perc * o.Eii_gbs;
       out[CO_eII_cst] += perc * o.Eii_cst;
-      out[CO_d] += perc / o.d1;
+      out[CO_d] += perc * o.inv_d1;
       out[CO_Wtot] += perc * o.Wtot;
       out[CO_Wdiss] += perc * o.Wdiss;
       out[CO_Wel] += perc * o.Wel;
@@ -161,14 +164,16 @@ __device__ __forceinline__ void do_vertex(const SweepArgs &A, long long c1, Acc 
     NodeIn in;
     const double mu = A.vi[VI_mu][c1];
     const double eta_e = (M.elastic == 1) ? M.dt_model * mu : 1.0;
+    const double inv_eta_e = ANISO ? 1.0 / eta_e : 0.0;
     const double el = (M.elastic == 1) ? 1.0 : 0.0;
     const double exxd = A.vi[VI_exxd][c1], ezzd = A.vi[VI_ezzd][c1], exz = A.vi[VI_exz][c1];
     in.Txx0 = A.vi[VI_sxxd0][c1]; in.Tzz0 = A.vi[VI_szzd0][c1]; in.Txz0 = A.vi[VI_sxz0][c1];
     double d1 = 0.0, d2 = 0.0, anif = 1.0;
     if (!ANISO) {
-      in.Exx = exxd + el * in.Txx0 / eta_e / 2.0;
-      in.Ezz = ezzd + el * in.Tzz0 / eta_e / 2.0;
-      in.Exz = exz + el * in.Txz0 / eta_e / 2.0;
+      const double h = el * 0.5 / eta_e;  // el / eta_e / 2
+      in.Exx = exxd + in.Txx0 * h;
+      in.Ezz = ezzd + in.Tzz0 * h;
+      in.Exz = exz + in.Txz0 * h;
     } else {
       d1 = A.vi[VI_d1][c1]; d2 = A.vi[VI_d2][c1]; anif = A.vi[VI_anif][c1];
       double sn, cs;
@@ -180,7 +185,7 @@ __device__ __forceinline__ void do_vertex(const SweepArgs &A, long long c1, Acc 
     in.G = mu; in.T = Ts; in.P = Ps; in.d = ds; in.phi = phis; in.X0 = A.vi[VI_X0][c1];
     in.dil = A.vi[VI_dil][c1]; in.fric = A.vi[VI_fric][c1]; in.C = A.vi[VI_C][c1]; in.P0 = A.vi[VI_p0][c1];
     in.T0 = 0.0; in.beta = A.vi[VI_bet][c1];
-    in.centroid = 0; in.final_update = A.final_update; in.post_process = 1;
+    in.centroid = 0; in.final_update = A.final_update; in.post_process = 1; in.want_rho = 0;
     NodeCtx ctx;
     AnisoNode an;
     if (ANISO) node_setup_aniso(M, in, A.need_lnd, ctx, an);
@@ -203,7 +208,7 @@ __device__ __forceinline__ void do_vertex(const SweepArgs &A, long long c1, Acc 
       if (avg == 0) { eta += perc * o.etaVE; eta_phys += perc * o.eta; }
       else if (avg == 1) { eta += perc / o.etaVE; eta_phys += perc / o.eta; }
       else { eta += perc * log(o.etaVE); eta_phys += perc * log(o.eta); }
-      if (ANISO) VE += perc * o.etaVE / eta_e;
+      if (ANISO) VE += perc * o.etaVE * inv_eta_e;
       X += perc * o.X1;
     }
     if (avg == 1) {
@@ -272,6 +277,7 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArg
     in.G = I.G[i]; in.T = I.T[i]; in.P = I.P[i]; in.d = I.d[i]; in.phi = I.phi[i]; in.X0 = I.X0[i];
     in.dil = I.dil[i]; in.fric = I.fric[i]; in.C = I.C[i]; in.P0 = I.P0[i]; in.T0 = I.T0[i]; in.beta = I.beta[i];
     in.centroid = I.centroid; in.final_update = I.final_update; in.post_process = I.post_process;
+    in.want_rho = 1;
     const int p = I.phase[i];
     PointOut o;
     NodeCtx ctx;

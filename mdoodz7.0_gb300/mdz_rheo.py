@@ -103,7 +103,8 @@ class GridFields(C.Structure):
 class SweepStats(C.Structure):
     _fields_ = [("phase_calls", C.c_uint64), ("newton_iters", C.c_uint64),
                 ("max_newton_iters", C.c_uint32), ("plastic_calls", C.c_uint64),
-                ("status", C.c_int32), ("error_node", C.c_int64), ("elapsed_ms", C.c_double)]
+                ("status", C.c_int32), ("error_node", C.c_int64), ("elapsed_ms", C.c_double),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -217,6 +218,7 @@ def load_library(path: str = LIB_PATH):
                                     C.c_int, C.c_int]
     lib.mdz_rheo_get_iterations.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_abi_sizes.argtypes = [C.POINTER(C.c_size_t)]
+    lib.mdz_rheo_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     _lib = lib
     return lib
 
@@ -234,6 +236,15 @@ def abi_sizes():
     out = (C.c_size_t * 8)()
     lib.mdz_rheo_abi_sizes(out)
     return list(out)
+
+
+def measure_fp64_peak(device: int = 0) -> float:
+    """Measured DFMA throughput of the GPU in TFLOP/s (mdz_rheo_measure_fp64_peak)."""
+    v = C.c_double()
+    rc = load_library().mdz_rheo_measure_fp64_peak(device, C.byref(v))
+    if rc != MDZ_OK:
+        raise RheoError(rc, "mdz_rheo_measure_fp64_peak")
+    return v.value
 
 
 def python_struct_sizes():

@@ -1,0 +1,226 @@
+"""Parity cases shared by the golden-fixture generator and the tests.
+
+GRID_CASES are small grids of the benchmark workloads (all field layouts,
+averaging modes, scalings, air cells, periodicity).  POINT_CASES drive
+ViscosityConcise / ViscosityConciseAniso directly on random points and cover
+the branches the grid workloads do not reach: Popov et al. 2025 plasticity
+(plast=2, with and without the tensile line search), paleowattmeter grain size
+(gs=1), constant and mixed viscosity, grain-boundary sliding, density models,
+the initial step (step=0), no elasticity, and visco-plastic regularisation.
+Every case is deterministic in its seed.
+"""
+import numpy as np
+
+import mdz_rheo as R
+import mdz_workloads as W
+
+
+def _air(w):
+    nx = w.model.Nx
+    ncx = nx - 1
+    w.arrays["BCp_type"][-3 * ncx:] = 30
+    w.arrays["BCp_type"][-4 * ncx:-3 * ncx] = 31
+    w.arrays["BCg_type"][-5 * nx:] = 30
+    return w
+
+
+def _periodic(w):
+    w.model.periodic_x = 1
+    return w
+
+
+GRID_CASES = {
+    # name: (builder, aniso, final_update)
+    "plain_small": (lambda: W.plain_small(seed=0, ncx=12, ncz=10), False, 0),
+    "plain_large": (lambda: W.plain_large(seed=1, ncx=12, ncz=10), False, 0),
+    "plain_large_typical": (lambda: W.plain_large(seed=2, ncx=12, ncz=10, sc=W.TYPICAL), False, 0),
+    "plain_large_harmonic": (lambda: W.plain_large(seed=3, ncx=11, ncz=13, eta_average=1), False, 0),
+    "plain_large_geometric_periodic": (lambda: _periodic(W.plain_large(seed=4, ncx=10, ncz=12, eta_average=2)),
+                                       False, 1),
+    "plain_large_air": (lambda: _air(W.plain_large(seed=5, ncx=12, ncz=12)), False, 0),
+    "aniso": (lambda: W.aniso(seed=6, ncx=12, ncz=10), True, 0),
+    "aniso_typical_harmonic": (lambda: _set(W.aniso(seed=7, ncx=10, ncz=11, sc=W.TYPICAL), eta_average=1), True, 0),
+}
+
+
+def _set(w, **kv):
+    for k, v in kv.items():
+        setattr(w.model, k, v)
+    return w
+
+
+# ---------------------------------------------------------------------------------------
+# point cases
+# ---------------------------------------------------------------------------------------
+def _points(rng, n, nphases, T=(600.0, 1300.0), E=(1e-15, 1e-13), P=(0.0, 3e9), d=(1e-4, 5e-3),
+            stress=5e7, aniso=False):
+    pin = {}
+    pin["phase"] = rng.integers(0, nphases, n).astype(np.int32)
+    pin["G"] = np.full(n, 3e10)
+    pin["T"] = rng.uniform(*T, n)
+    pin["P"] = rng.uniform(*P, n)
+    pin["d"] = W.loguniform(rng, d[0], d[1], n)
+    pin["phi"] = np.zeros(n)
+    pin["X0"] = np.zeros(n)
+    exx = W.signed_loguniform(rng, E[0], E[1], n)
+    pin["Exx"], pin["Ezz"] = exx, -exx
+    pin["Exz"] = W.signed_loguniform(rng, E[0], E[1], n)
+    t0 = rng.uniform(-stress, stress, n)
+    pin["Txx0"], pin["Tzz0"] = t0, -t0
+    pin["Txz0"] = rng.uniform(-stress, stress, n)
+    pin["strain_acc"] = np.zeros(n)
+    pin["dil"] = np.zeros(n)
+    pin["fric"] = np.full(n, 30.0 * W.DEG)
+    pin["C"] = np.full(n, 1e7)
+    pin["P0"] = pin["P"].copy()
+    pin["T0"] = pin["T"].copy()
+    pin["beta"] = np.full(n, 1e-40)
+    pin["div"] = np.zeros(n)
+    if aniso:
+        th = rng.uniform(0, np.pi, n)
+        lay = th - np.pi / 2
+        pin["lxlz"], pin["lx2"] = np.cos(lay) * np.sin(lay), np.cos(lay) ** 2
+        pin["angle"], pin["ani_fac"] = th, W.loguniform(rng, 1.0, 10.0, n)
+    return pin
+
+
+def _popov(ls):
+    def build(seed):
+        rng = np.random.default_rng(seed)
+        m = W.empty_materials(2)
+        W.set_power_law(m, 0, **W.OLIVINE_DRY)
+        W.set_power_law(m, 1, **W.SOFT_QTZ)
+        for p in range(2):
+            m.plast[p] = 2
+            m.T_st[p] = -5e6
+        md = W.make_model(8, 8, 2)
+        md.tensile_line_search = ls
+        pin = _points(rng, 200, 2, P=(-2e7, 2e8), stress=1e8, E=(1e-14, 1e-12))
+        pin["dil"] = np.full(200, 5.0 * W.DEG)
+        pin["beta"] = np.full(200, 1e-11)
+        return md, m, pin
+    return build
+
+
+def _gse(aniso):
+    def build(seed):
+        rng = np.random.default_rng(seed)
+        m = W.empty_materials(2)
+        W.set_power_law(m, 0, **W.OLIVINE_DRY)
+        W.set_linear(m, 0, **W.OLIVINE_DIFF)
+        W.set_power_law(m, 1, **W.OLIVINE_DRY)
+        for p in range(2):
+            m.gs[p] = 1
+            m.Kpzm[p], m.Qpzm[p], m.Gpzm[p], m.Lpzm[p], m.cpzm[p], m.ppzm[p] = 1.5e-5, 2.0e5, 1.0, 0.1, np.pi, 3.0
+        md = W.make_model(8, 8, 2)
+        pin = _points(rng, 120, 2, T=(900.0, 1400.0), E=(1e-15, 1e-13), aniso=aniso)
+        return md, m, pin
+    return build
+
+
+def _constant_mix(seed):
+    rng = np.random.default_rng(seed)
+    m = W.empty_materials(3)
+    m.cstv[0] = 1
+    m.eta0[0] = 1e21
+    m.cstv[1] = 1
+    m.eta0[1] = 5e19
+    W.set_power_law(m, 1, **W.SOFT_QTZ)
+    m.cstv[2] = 1
+    m.eta0[2] = 3e22
+    m.phase_mix[2] = 1
+    m.phase_two[2] = 0
+    m.gbsv[1] = 1
+    m.Qgbs[1], m.Vgbs[1], m.ngbs[1], m.mgbs[1], m.Agbs[1], m.Fgbs[1] = 400e3, 0.0, 3.5, 2.0, 6.5e-40, 1.0
+    md = W.make_model(8, 8, 3)
+    md.diffuse_X = 1
+    md.diffuse_avg = seed % 3
+    pin = _points(rng, 150, 3)
+    pin["X0"] = rng.uniform(0.0, 1.0, 150)
+    return md, m, pin
+
+
+def _density(seed):
+    rng = np.random.default_rng(seed)
+    m = W.materials_plain_large(4)
+    for p, dm in enumerate((0, 1, 3, 5)):
+        m.density_model[p] = dm
+        m.rho[p] = 3000.0 + 100 * p
+        m.alp[p] = 3e-5
+        m.bet[p] = 1e-11
+        m.drho[p] = -300.0
+    md = W.make_model(8, 8, 4)
+    md.density_variations = 1
+    pin = _points(rng, 160, 4)
+    pin["phi"] = rng.uniform(0.0, 0.1, 160)
+    return md, m, pin
+
+
+def _step0(seed):
+    rng = np.random.default_rng(seed)
+    m = W.materials_plain_large(5)
+    md = W.make_model(8, 8, 5)
+    md.step = 0
+    return md, m, _points(rng, 150, 5)
+
+
+def _no_elastic(seed):
+    rng = np.random.default_rng(seed)
+    m = W.materials_plain_large(5)
+    md = W.make_model(8, 8, 5)
+    md.elastic = 0
+    return md, m, _points(rng, 150, 5)
+
+
+def _viscoplastic(seed):
+    rng = np.random.default_rng(seed)
+    m = W.materials_plain_small()
+    for p in range(2):
+        m.eta_vp[p] = 1e20
+        m.Slim[p] = 5e8
+    md = W.make_model(8, 8, 2)
+    pin = _points(rng, 150, 2, E=(1e-14, 1e-12), stress=2e8)
+    pin["dil"] = np.full(150, 2.0 * W.DEG)
+    pin["beta"] = np.full(150, 1e-11)
+    return md, m, pin
+
+
+def _large_mix(aniso):
+    def build(seed):
+        rng = np.random.default_rng(seed)
+        m = W.materials_plain_large(5)
+        if aniso:
+            for p in range(5):
+                m.gs[p] = 0
+        md = W.make_model(8, 8, 5)
+        return md, m, _points(rng, 250, 5, T=(400.0, 1550.0), aniso=aniso)
+    return build
+
+
+POINT_CASES = {
+    # name: (builder(seed), aniso, centroid, final_update)
+    "popov": (_popov(0), False, 1, 0),
+    "popov_line_search": (_popov(1), False, 1, 1),
+    "gse": (_gse(False), False, 1, 0),
+    "gse_aniso": (_gse(True), True, 1, 0),
+    "constant_mix_gbs": (_constant_mix, False, 1, 0),
+    "density_models": (_density, False, 1, 1),
+    "step0": (_step0, False, 1, 0),
+    "no_elastic": (_no_elastic, False, 0, 0),
+    "viscoplastic": (_viscoplastic, False, 1, 0),
+    "large_mix_peierls_cutoff": (_large_mix(False), False, 1, 0),
+    "aniso_mix": (_large_mix(True), True, 1, 0),
+}
+
+
+def point_case(name, seed=0):
+    build, aniso, centroid, fu = POINT_CASES[name]
+    md, m, pin = build(seed)
+    return md, m, pin, aniso, centroid, fu
+
+
+def alloc_point_outputs(n):
+    out = {k: np.zeros(n) for k in R.PT_OUT}
+    out["iters"] = np.zeros(n, np.int32)
+    out["status"] = np.zeros(n, np.int32)
+    return out

@@ -1,0 +1,80 @@
+"""Generate the golden fixtures from MDOODZ7.0's own code.
+
+Runs the reference's NonNewtonianViscosityGrid(Aniso) and ViscosityConcise(Aniso),
+compiled from the MDOODZ7.0 sources by oracle/Makefile (target `ref`), on the
+cases of cases.py and stores their outputs in tests/golden/*.npz.  Inputs are
+regenerated from the seeds by the tests; a SHA-256 of the inputs is stored
+beside the outputs so that a change in the generators is caught.
+
+    python tests/golden/make_golden.py        (needs the reference tree)
+"""
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [os.path.join(REPO, "mdoodz7.0_gb300"), os.path.join(REPO, "oracle"), HERE]
+
+import cases  # noqa: E402
+import mdz_rheo as R  # noqa: E402
+import oracle_lib as O  # noqa: E402
+
+INPUT_GRID = [k for k in R.CEN_IN + R.VER_IN + R.ANI_IN_N + R.ANI_IN_S + ["BCp_type", "BCg_type"]]
+
+
+def digest(arrays, keys):
+    h = hashlib.sha256()
+    for k in keys:
+        v = arrays.get(k)
+        if v is None:
+            continue
+        for x in (v if isinstance(v, list) else [v]):
+            h.update(np.ascontiguousarray(x).tobytes())
+    return h.hexdigest()
+
+
+def grid_inputs_digest(w):
+    return digest(w.arrays, INPUT_GRID + ["phase_perc_n", "phase_perc_s"])
+
+
+def point_inputs_digest(pin):
+    return digest(pin, ["phase"] + R.PT_IN + R.PT_ANI)
+
+
+def grid_outputs(arrays):
+    out = {}
+    for k in R.VER_INTERP + R.CEN_OUT + R.VER_OUT:
+        if k in arrays:
+            out[k] = arrays[k]
+    for k in ("phase_eta_n", "phase_eta_s"):
+        out[k] = np.stack(arrays[k])
+    return out
+
+
+def main():
+    O.build(ref=True)
+    if O.reference() is None:
+        sys.exit("the reference tree is needed to generate golden fixtures")
+    for name, (builder, aniso, fu) in cases.GRID_CASES.items():
+        w = builder()
+        dig = grid_inputs_digest(w)
+        a = {k: ([x.copy() for x in v] if isinstance(v, list) else v.copy()) for k, v in w.arrays.items()}
+        O.ref_sweep(w.model, w.mat, R.FieldSet(a), final_update=fu, aniso=aniso)
+        np.savez_compressed(os.path.join(HERE, f"grid_{name}.npz"), inputs_sha256=dig, **grid_outputs(a))
+        print("grid", name, w.nodes, "nodes")
+    for name in cases.POINT_CASES:
+        md, m, pin, aniso, centroid, fu = cases.point_case(name)
+        n = pin["phase"].size
+        out = cases.alloc_point_outputs(n)
+        pi, po = R.make_points(pin, out, centroid=centroid, final_update=fu)
+        O.ref_points(md, m, pi, po, n, int(aniso))
+        keep = {k: out[k] for k in R.PT_OUT}
+        np.savez_compressed(os.path.join(HERE, f"points_{name}.npz"), inputs_sha256=point_inputs_digest(pin), **keep)
+        print("points", name, n)
+
+
+if __name__ == "__main__":
+    main()

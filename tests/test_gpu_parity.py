@@ -31,8 +31,8 @@ def run_pair(ctx, w, aniso=False, final_update=0, flags=0):
     return rc, st, g, rc2, st2, c
 
 
-def check_close(g, c, label):
-    errs = worst(g, c)
+def check_close(g, c, label, w=None):
+    errs = worst(g, c, None if w is None else w.arrays, None if w is None else w.model)
     bad = {k: v for k, v in errs.items() if v > RTOL}
     print(label, "max scaled error", max(errs.values()), {k: f"{v:.1e}" for k, v in errs.items() if v > 1e-15})
     assert not bad, f"{label}: fields above {RTOL}: {bad}"
@@ -54,7 +54,7 @@ def test_sweep_matches_oracle(ctx, name):
     rc, st, g, rc2, st2, c = run_pair(ctx, w)
     assert rc == rc2 == R.MDZ_OK
     assert st.phase_calls == st2.phase_calls
-    check_close(g, c, name)
+    check_close(g, c, name, w)
     # plastic flags may only flip where rounding moves Tii across the yield stress
     assert abs(int(st.plastic_calls) - int(st2.plastic_calls)) <= max(1, st2.plastic_calls // 10000)
 
@@ -64,7 +64,7 @@ def test_sweep_final_update_and_periodic(ctx):
     w.model.periodic_x = 1
     rc, st, g, rc2, st2, c = run_pair(ctx, w, final_update=1)
     assert rc == rc2 == R.MDZ_OK
-    check_close(g, c, "periodic+final_update")
+    check_close(g, c, "periodic+final_update", w)
 
 
 def test_sweep_air_cells(ctx):
@@ -75,7 +75,7 @@ def test_sweep_air_cells(ctx):
     w.arrays["BCg_type"][-nx * 6:] = 30
     rc, st, g, rc2, st2, c = run_pair(ctx, w)
     assert rc == rc2 == R.MDZ_OK
-    check_close(g, c, "air")
+    check_close(g, c, "air", w)
     assert np.all(g["eta_n"][-200:] == 0.0) and np.all(g["T_s"][-nx * 6:] == 0.0)
 
 
@@ -87,7 +87,7 @@ def test_inactive_phase_keeps_previous_phase_eta(ctx):
     rc, st, g, rc2, st2, c = run_pair(ctx, w)
     assert rc == rc2 == R.MDZ_OK
     assert np.all(g["phase_eta_n"][1][:50] == 123.0)
-    check_close(g, c, "inactive")
+    check_close(g, c, "inactive", w)
 
 
 def test_iteration_counts_match(ctx):
@@ -141,7 +141,7 @@ def test_aniso_sweep_matches_oracle(ctx):
     w = W.aniso(seed=4, ncx=96)
     rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True)
     assert rc == rc2 == R.MDZ_OK
-    check_close(g, c, "aniso")
+    check_close(g, c, "aniso", w)
 
 
 def test_aniso_typical_scale_harmonic(ctx):
@@ -149,4 +149,4 @@ def test_aniso_typical_scale_harmonic(ctx):
     w.model.eta_average = 1
     rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True)
     assert rc == rc2 == R.MDZ_OK
-    check_close(g, c, "aniso-typical-harmonic")
+    check_close(g, c, "aniso-typical-harmonic", w)
