@@ -27,6 +27,7 @@
 #include <stdint.h>
 
 #include "../../include/mdz_rheo.h"
+#include "fp64_math.cuh"
 
 namespace mdz {
 
@@ -113,12 +114,12 @@ __device__ __forceinline__ void set_status(int &st, int code) {
 // node set-up: invariants and switches shared by the phases (RheologyDensity.c:461-496)
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c) {
-  c.lnEii = log(c.Eii);
+  c.lnEii = fast_log(c.Eii);
   c.inv2Eii = 0.5 / c.Eii;
   c.Traw = in.T;
   c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
   c.invT = 1.0 / c.T;
-  c.lnd = need_lnd ? log(in.d) : 0.0;
+  c.lnd = need_lnd ? fast_log(in.d) : 0.0;
   c.inv_d = 0.0;
   sincos(in.fric, &c.sin_fric, &c.cos_fric);
   c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
@@ -184,13 +185,13 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
   L.lnB_pwl = L.lnB_lin = L.lnA_exp = L.ST = L.inv_gbs = 0.0;
   const double Eii = c.Eii, lnEii = c.lnEii;
   if (fl & F_PWL) {
-    // B = pref F A^(-1/n) exp((Q+PV)/(RnT)) d^(m/n) f^(-r/n) exp(-a phi/n);
-    // 1/eta_pwl = Eii^(1-1/n) / B = Eii exp(-lnB - lnEii/n)
+    // B = pref F A^(-1/n) fast_exp((Q+PV)/(RnT)) d^(m/n) f^(-r/n) fast_exp(-a phi/n);
+    // 1/eta_pwl = Eii^(1-1/n) / B = Eii fast_exp(-lnB - lnEii/n)
     double lnB = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
     if (fl & F_PWL_M) lnB += ph.pwl_mn * lnd;
     if (fl & F_PWL_A) lnB -= ph.pwl_an * phi;
     L.lnB_pwl = lnB;
-    L.inv[K_PWL] = Eii * exp(-fma(lnEii, ph.pwl_invn, lnB));
+    L.inv[K_PWL] = Eii * fast_exp(-fma(lnEii, ph.pwl_invn, lnB));
   }
   if (fl & F_LIN) {
     // 1/eta_lin = Eii^(1-1/n) / (B d^(m/n))
@@ -198,21 +199,21 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
     if (fl & F_LIN_A) lnB -= ph.lin_an * phi;
     L.lnB_lin = lnB;
     const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, lnB) : lnB;
-    L.inv[K_LIN] = Eii * exp(-fma(lnEii, ph.lin_invn, lnBd));
+    L.inv[K_LIN] = Eii * fast_exp(-fma(lnEii, ph.lin_invn, lnBd));
   }
   if (peierls) {
-    // Eii_exp(Tii) = A (sqrt3 Tii / (gamma S))^nE, A = (sqrt3/2) E Arr (gamma S)^n;
+    // Eii_fast_exp(Tii) = A (sqrt3 Tii / (gamma S))^nE, A = (sqrt3/2) E Arr (gamma S)^n;
     // isolated: Tii* = (gamma S / sqrt3) (Eii/A)^(1/nE), 1/eta_exp = 2 Eii / Tii*
     L.ST = ph.exp_EaR * c.invT * ph.exp_g2;
     const double nE = L.ST + ph.exp_n;
     L.n[K_EXP] = nE;
     L.lnA_exp = ph.exp_lnA0 - ph.exp_EaR * ph.exp_om2 * c.invT;
-    L.inv[K_EXP] = 2.0 * Eii * ph.exp_s3gS * exp(-(lnEii - L.lnA_exp) / nE);
+    L.inv[K_EXP] = 2.0 * Eii * ph.exp_s3gS * fast_exp(-(lnEii - L.lnA_exp) / nE);
   }
   if (fl & F_GBS) {
     double lnB = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * phi;
     if (ph.gbs_m != 0.0) lnB += ph.gbs_mn * lnd;
-    L.inv_gbs = Eii * exp(-fma(lnEii, ph.gbs_invn, lnB));
+    L.inv_gbs = Eii * fast_exp(-fma(lnEii, ph.gbs_invn, lnB));
   }
 }
 
@@ -270,7 +271,7 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
     const double r_p = 1.0 / inv_p;
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
-      if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * log(L.inv[k] * r_p);
+      if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * fast_log(L.inv[k] * r_p);
   }
 }
 
@@ -278,11 +279,11 @@ __device__ __forceinline__ void ve_eval(const VeCoef &q, double eta, VeState &s,
   double e[K_COUNT] = {0.0, 0.0, 0.0};
   S = 0.0;
   if (q.nl) {
-    const double lx = log(eta * q.inv_p);
+    const double lx = fast_log(eta * q.inv_p);
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
       if (q.nl >> k & 1) {
-        e[k] = q.Eii * exp(fma(q.n[k], lx, q.nc[k]));
+        e[k] = q.Eii * fast_exp(fma(q.n[k], lx, q.nc[k]));
         S = fma(q.n[k], e[k], S);
       }
   }
@@ -629,7 +630,7 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
     if (diffusion) {
       // eta_lin = B pow(Eii_lin, 1/n-1) pow(d1, m/n) = Tii/(2 Eii_lin) (d1/d)^(m/n), d1 = gs_ref
       double inv_lin = e_lin * inv_half_T;
-      if (ph.lin_m != 0.0 && !gs) inv_lin *= exp(ph.lin_mn * (lnd - ph.ln_gs_ref));
+      if (ph.lin_m != 0.0 && !gs) inv_lin *= fast_exp(ph.lin_mn * (lnd - ph.ln_gs_ref));
       inv += inv_lin;
     }
     if (constant) inv += (1.0 / eta_cst);
