@@ -64,6 +64,7 @@ extern "C" {
 #define MDZ_SWEEP_ASYNC      0x1  /* MDZ_MEM_DEVICE only: return after enqueue; call mdz_rheo_sync */
 #define MDZ_SWEEP_WARMSTART  0x2  /* start each local Newton from the learned guess (needs weights) */
 #define MDZ_SWEEP_ITERS      0x4  /* record per-(node,phase) local iteration counts (mdz_rheo_get_iterations) */
+#define MDZ_SWEEP_POLISH     0x8  /* start each local Newton from a few FP32 Newton steps (no network) */
 
 /* ---- per-phase material table -----------------------------------------
  * The subset of `mat_prop` (MDLIB/include/mdoodz.h:152-240) that the local
@@ -155,7 +156,32 @@ typedef struct mdz_sweep_stats {
   uint64_t h2d_bytes;        /* bytes copied host->device by this call (MDZ_MEM_HOST) */
   uint64_t d2h_bytes;        /* bytes copied device->host by this call (MDZ_MEM_HOST) */
   uint32_t kernel_launches;  /* kernels this call launched */
+  uint32_t mma_fault;        /* warm start: a tensor-core wait gave up; those items used the plain start */
 } mdz_sweep_stats;
+
+/* ---- learned warm start ----------------------------------------------
+ * A 10 (anisotropic: 12) -> 64 -> 64 -> 2 perceptron predicting, per (node, phase),
+ * z = ln(eta_up / eta_ve) (eta_up: the reference's start point, the smallest isolated
+ * viscosity; eta_ve: the converged visco-elastic viscosity) and a plastic indicator.
+ * No reference counterpart: the reference always starts from eta_up. */
+#define MDZ_MLP_IN  16  /* padded feature width */
+#define MDZ_MLP_HID 64
+typedef struct mdz_mlp_weights {
+  int32_t n_feat;                                  /* features used: 10 or 12 */
+  float   W1[MDZ_MLP_HID * MDZ_MLP_IN], b1[MDZ_MLP_HID];   /* row-major [out][in] */
+  float   W2[MDZ_MLP_HID * MDZ_MLP_HID], b2[MDZ_MLP_HID];
+  float   W3[2 * MDZ_MLP_HID], b3[2];
+  float   x_shift[MDZ_MLP_IN], x_scale[MDZ_MLP_IN];     /* x' = (x - shift) * scale */
+  float   z_shift, z_scale;                              /* z = out0 * scale + shift */
+} mdz_mlp_weights;
+
+typedef struct mdz_mlp_train_cfg {
+  int32_t  epochs, batch;      /* batch: samples per Adam step (multiple of 128) */
+  float    lr, lr_final;       /* cosine decay from lr to lr_final */
+  float    beta1, beta2, eps;  /* Adam */
+  float    w_pl;               /* weight of the plastic-indicator loss */
+  uint64_t seed;               /* initialisation and sample order */
+} mdz_mlp_train_cfg;
 
 /* ---- point batches (ViscosityConcise / ViscosityConciseAniso per point) -- */
 typedef struct mdz_point_inputs {
@@ -213,6 +239,35 @@ int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materia
  * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
  * inactive.  Host buffers. */
 int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);
+
+/* ---- learned warm start (no reference counterpart) --------------------- */
+/* Install the network used by MDZ_SWEEP_WARMSTART (NULL removes it) and the number of
+ * FP32 Newton steps taken after its guess (also used by MDZ_SWEEP_POLISH). */
+int mdz_rheo_set_warmstart(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, int polish_iters);
+/* A plain sweep (iso or aniso) that also records, for every (phase p, node i) item,
+ * item = p * (Nc + Nv) + i (centroids first), the MDZ_MLP_IN features X[item][.] and
+ * the targets Y[item][0] = ln(eta_up / eta_ve), Y[item][1] = plastic (0/1); Y[item][0]
+ * is NaN for inactive items.  X and Y live in `mem` like the fields. */
+int mdz_rheo_collect(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                     const mdz_grid_fields *f, int final_update, int aniso, int mem, float *X, float *Y,
+                     mdz_sweep_stats *stats);
+/* Train the network on n samples (X: [n][MDZ_MLP_IN], Y: [n][2], memory space `mem`) with
+ * the tcgen05 training kernels.  If w->z_scale != 0 training resumes from *w, else it
+ * starts from a seeded initialisation with normalisation taken from the data.  The
+ * trained weights are written back to *w; loss (may be NULL) receives the mean squared
+ * error of the normalised z per epoch. */
+int mdz_rheo_train_mlp(mdz_rheo_ctx *ctx, const float *X, const float *Y, int64_t n, int n_feat,
+                       const mdz_mlp_train_cfg *cfg, mdz_mlp_weights *w, float *loss, int mem);
+/* Gradient of the training loss (mean over the n samples of (z' - z)^2 + w_pl (pl' - pl)^2,
+ * z normalised by w's z_shift/z_scale) with respect to every weight, computed by the
+ * same tcgen05 kernels as training, without updating: written into the W/b fields of
+ * *grad (its other fields are left alone).  loss (may be NULL) receives the two sums of
+ * squared errors. */
+int mdz_rheo_mlp_gradient(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, const float *X, const float *Y,
+                          int64_t n, float w_pl, mdz_mlp_weights *grad, float *loss, int mem);
+/* Forward pass only: Yp[s] = (z, plastic indicator) for n samples. */
+int mdz_rheo_mlp_predict(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, const float *X, float *Yp, int64_t n,
+                         int mem);
 
 /* ---- measurement helper ----------------------------------------------- */
 /* Measured FP64 FMA throughput of `device` in TFLOP/s (a full-occupancy DFMA

@@ -12,7 +12,11 @@
 #include <mutex>
 #include <vector>
 
+#include "mlp_train.cuh"
 #include "rheo_kernels.cuh"
+
+#include <algorithm>
+#include <random>
 
 using namespace mdz;
 
@@ -34,6 +38,12 @@ struct mdz_rheo_ctx {
   unsigned long long h2d = 0, d2h = 0;
   unsigned launches = 0;
   int block = 128, grid_cap = 0;
+  int sms = 0;
+  // learned warm start
+  void *warm_buf = nullptr;  // tiles W1, W2, W3 + biases b1, b2, b3[16]
+  MlpDevice warm{};
+  int warm_ready = 0, polish_iters = 4;
+  unsigned mma_fault = 0;
 };
 
 namespace {
@@ -181,6 +191,7 @@ int stats_from_device(mdz_rheo_ctx *ctx, mdz_sweep_stats *st, float ms) {
     st->phase_calls = h.calls; st->newton_iters = h.iters; st->max_newton_iters = h.maxit;
     st->plastic_calls = h.plastic; st->status = status; st->error_node = node; st->elapsed_ms = ms;
     st->h2d_bytes = ctx->h2d; st->d2h_bytes = ctx->d2h; st->kernel_launches = ctx->launches;
+    st->mma_fault = h.mma_fault;
   }
   return status;
 }
@@ -238,11 +249,18 @@ struct Mirror {
 };
 
 int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat, const mdz_grid_fields *f,
-               int final_update, int mem, int flags, mdz_sweep_stats *st, bool aniso) {
+               int final_update, int mem, int flags, mdz_sweep_stats *st, bool aniso, float *X = nullptr,
+               float *Y = nullptr) {
   if (!ctx || !md || !mat || !f) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
   if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
-  if (flags & MDZ_SWEEP_WARMSTART) return MDZ_ENOTREADY;
+  if ((flags & MDZ_SWEEP_WARMSTART) && !ctx->warm_ready) return MDZ_ENOTREADY;
+  if ((flags & MDZ_SWEEP_WARMSTART) && ctx->warm.n_feat != (aniso ? kFeatAniso : kFeatIso)) return MDZ_EINVAL;
+  const bool collect = (X != nullptr);
+  int mode = -1;  // plain
+  if (collect) mode = MODE_COLLECT;
+  else if (flags & MDZ_SWEEP_WARMSTART) mode = MODE_WARM;
+  else if (flags & MDZ_SWEEP_POLISH) mode = MODE_POLISH;
   if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
   CK(cudaSetDevice(ctx->device));
   static thread_local SweepArgs A;  // large: keep off the stack
@@ -315,10 +333,39 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   }
   A.stats = ctx->d_stats;
   if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  // collected features / targets (device scratch when the caller's buffers are on the host)
+  const size_t items = (size_t)np * (Nc + Nv);
+  float *dX = X, *dY = Y;
+  struct Scratch {  // freed on every return path
+    DevBuf b;
+    ~Scratch() { if (b.p) cudaFree(b.p); }
+  } tmpX, tmpY;
+  if (collect && host) {
+    if (ensure(tmpX.b, items * kMlpIn * sizeof(float)) != MDZ_OK || ensure(tmpY.b, items * 2 * sizeof(float)) != MDZ_OK)
+      return MDZ_ENOMEM;
+    dX = (float *)tmpX.b.p;
+    dY = (float *)tmpY.b.p;
+  }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  CK(launch_sweep(A, aniso, ctx->stream, ctx->block, ctx->grid_cap));
+  if (mode < 0) {
+    CK(launch_sweep(A, aniso, ctx->stream, ctx->block, ctx->grid_cap));
+  } else {
+    WarmArgs W;
+    memset(&W, 0, sizeof(W));
+    W.mlp = ctx->warm;
+    W.mlp.polish_iters = ctx->polish_iters;
+    W.X_out = dX;
+    W.Y_out = dY;
+    const int grid = ctx->sms * tiles_blocks_per_sm(aniso, mode);
+    CK(launch_sweep_tiles(A, W, aniso, mode, ctx->stream, grid));
+  }
   ctx->launches += 1;
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (collect && host) {
+    CK(cudaMemcpyAsync(X, dX, items * kMlpIn * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(Y, dY, items * 2 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   for (int i = 0; i < CO_COUNT; i++) mi.back(cout[i], S_CO + i, Nc, host);
   for (int i = 0; i < VO_COUNT; i++) mi.back(vout[i], S_VO + i, Nv, host);
   for (int p = 0; p < np; p++) {
@@ -331,6 +378,149 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
     return MDZ_OK;
   }
   return finish(ctx, st);
+}
+
+
+// ---------------------------------------------------------------------------------
+// learned warm start: host-side packing of the BF16 K-major tiles (umma.cuh layout)
+// ---------------------------------------------------------------------------------
+uint16_t f2bf(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return (uint16_t)(u >> 16);
+}
+
+size_t kmajor_off(int r, int k, int K) {
+  return (size_t)((r >> 3) * (16 * K) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// tile[rows_alloc x K] with tile(r, k) = W[r * ldw + k] (or W[k * ldw + r] if transposed)
+void pack_tile(uint8_t *tile, int rows_alloc, int K, const float *W, int rows_used, int k_used, int ldw, bool tr) {
+  memset(tile, 0, (size_t)rows_alloc * K * 2);
+  for (int r = 0; r < rows_used; r++)
+    for (int k = 0; k < k_used; k++) {
+      const uint16_t b = f2bf(tr ? W[(size_t)k * ldw + r] : W[(size_t)r * ldw + k]);
+      memcpy(tile + kmajor_off(r, k, K), &b, 2);
+    }
+}
+
+constexpr size_t kT1 = kMlpHid * kMlpIn * 2, kT2 = kMlpHid * kMlpHid * 2, kT3 = kMlpOut * kMlpHid * 2;
+
+int upload_warm(mdz_rheo_ctx *c, const mdz_mlp_weights *w) {
+  const size_t bytes = kT1 + kT2 + kT3 + (64 + 64 + 16) * sizeof(float);
+  if (!c->warm_buf) CK(cudaMalloc(&c->warm_buf, bytes));
+  std::vector<uint8_t> h(bytes, 0);
+  pack_tile(h.data(), kMlpHid, kMlpIn, w->W1, kMlpHid, w->n_feat, MDZ_MLP_IN, false);
+  pack_tile(h.data() + kT1, kMlpHid, kMlpHid, w->W2, kMlpHid, kMlpHid, MDZ_MLP_HID, false);
+  pack_tile(h.data() + kT1 + kT2, kMlpOut, kMlpHid, w->W3, 2, kMlpHid, MDZ_MLP_HID, false);
+  float *b = (float *)(h.data() + kT1 + kT2 + kT3);
+  memcpy(b, w->b1, 64 * sizeof(float));
+  memcpy(b + 64, w->b2, 64 * sizeof(float));
+  b[128] = w->b3[0];
+  b[129] = w->b3[1];
+  CK(cudaMemcpy(c->warm_buf, h.data(), bytes, cudaMemcpyHostToDevice));
+  uint8_t *d = (uint8_t *)c->warm_buf;
+  c->warm.W1 = (const uint4 *)d;
+  c->warm.W2 = (const uint4 *)(d + kT1);
+  c->warm.W3 = (const uint4 *)(d + kT1 + kT2);
+  const float *db = (const float *)(d + kT1 + kT2 + kT3);
+  c->warm.b1 = db; c->warm.b2 = db + 64; c->warm.b3 = db + 128;
+  for (int j = 0; j < kMlpIn; j++) { c->warm.x_shift[j] = w->x_shift[j]; c->warm.x_scale[j] = w->x_scale[j]; }
+  c->warm.z_shift = w->z_shift;
+  c->warm.z_scale = w->z_scale;
+  c->warm.n_feat = w->n_feat;
+  return MDZ_OK;
+}
+
+// Device state of one training run, in one allocation.
+struct TrainBuffers {
+  void *mem = nullptr;
+  MlpTrainState S{};
+  ~TrainBuffers() { if (mem) cudaFree(mem); }
+};
+
+constexpr int kP1 = kMlpHid * kMlpIn, kP2 = kMlpHid * kMlpHid, kP3 = 2 * kMlpHid;
+
+int alloc_train(TrainBuffers &B) {
+  const int P = kP1 + kP2 + kP3 + 64 + 64 + 16;
+  const size_t fbytes = (size_t)P * 4 * sizeof(float);
+  const size_t tbytes = kT1 + kT2 + kT3 + kT2 + kMlpHid * kMlpOut * 2;
+  CK(cudaMalloc(&B.mem, fbytes + tbytes + 64));
+  CK(cudaMemset(B.mem, 0, fbytes + tbytes + 64));
+  float *f = (float *)B.mem;
+  float **slots[4][6] = {{&B.S.W1, &B.S.W2, &B.S.W3, &B.S.b1, &B.S.b2, &B.S.b3},
+                         {&B.S.mW1, &B.S.mW2, &B.S.mW3, &B.S.mb1, &B.S.mb2, &B.S.mb3},
+                         {&B.S.vW1, &B.S.vW2, &B.S.vW3, &B.S.vb1, &B.S.vb2, &B.S.vb3},
+                         {&B.S.gW1, &B.S.gW2, &B.S.gW3, &B.S.gb1, &B.S.gb2, &B.S.gb3}};
+  const int sizes[6] = {kP1, kP2, kP3, 64, 64, 16};
+  for (int g = 0; g < 4; g++)
+    for (int i = 0; i < 6; i++) { *slots[g][i] = f; f += sizes[i]; }
+  uint8_t *t = (uint8_t *)f;
+  B.S.tW1 = (uint4 *)t; t += kT1;
+  B.S.tW2 = (uint4 *)t; t += kT2;
+  B.S.tW3 = (uint4 *)t; t += kT3;
+  B.S.tW2t = (uint4 *)t; t += kT2;
+  B.S.tW3t = (uint4 *)t; t += kMlpHid * kMlpOut * 2;
+  B.S.loss = (float *)t;
+  B.S.fault = (int *)(t + 16);
+  return MDZ_OK;
+}
+
+int put_weights(TrainBuffers &B, const mdz_mlp_weights *w) {
+  CK(cudaMemcpy(B.S.W1, w->W1, kP1 * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.S.W2, w->W2, kP2 * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.S.W3, w->W3, kP3 * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.S.b1, w->b1, 64 * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.S.b2, w->b2, 64 * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(B.S.b3, w->b3, 2 * sizeof(float), cudaMemcpyHostToDevice));
+  for (int j = 0; j < kMlpIn; j++) { B.S.x_shift[j] = w->x_shift[j]; B.S.x_scale[j] = w->x_scale[j]; }
+  B.S.z_shift = w->z_shift;
+  B.S.z_scale = w->z_scale;
+  return MDZ_OK;
+}
+
+int get_weights(const TrainBuffers &B, mdz_mlp_weights *w) {
+  CK(cudaMemcpy(w->W1, B.S.W1, kP1 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(w->W2, B.S.W2, kP2 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(w->W3, B.S.W3, kP3 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(w->b1, B.S.b1, 64 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(w->b2, B.S.b2, 64 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(w->b3, B.S.b3, 2 * sizeof(float), cudaMemcpyDeviceToHost));
+  return MDZ_OK;
+}
+
+// Seeded initialisation (He-uniform for the hidden layers, small output layer) and
+// feature / target normalisation from the data (finite targets only).
+void init_weights(mdz_mlp_weights *w, const float *X, const float *Y, int64_t n, int n_feat, uint64_t seed) {
+  std::mt19937_64 rng(seed);
+  memset(w, 0, sizeof(*w));
+  w->n_feat = n_feat;
+  auto uni = [&](float a) { return (float)((double)rng() / 18446744073709551616.0 * 2.0 - 1.0) * a; };
+  for (int h = 0; h < kMlpHid; h++)
+    for (int f = 0; f < n_feat; f++) w->W1[h * kMlpIn + f] = uni(sqrtf(6.0f / n_feat));
+  for (int i = 0; i < kP2; i++) w->W2[i] = uni(sqrtf(6.0f / kMlpHid));
+  for (int i = 0; i < kP3; i++) w->W3[i] = uni(0.1f * sqrtf(6.0f / kMlpHid));
+  std::vector<double> s(kMlpIn, 0.0), s2(kMlpIn, 0.0);
+  double zs = 0.0, zs2 = 0.0;
+  int64_t cnt = 0;
+  for (int64_t i = 0; i < n; i++) {
+    const float z = Y[i * 2];
+    if (!std::isfinite(z)) continue;
+    cnt++;
+    zs += z; zs2 += (double)z * z;
+    for (int f = 0; f < n_feat; f++) { const double x = X[i * kMlpIn + f]; s[f] += x; s2[f] += x * x; }
+  }
+  const double c = cnt > 0 ? (double)cnt : 1.0;
+  for (int f = 0; f < kMlpIn; f++) {
+    const double m = s[f] / c, v = s2[f] / c - m * m;
+    w->x_shift[f] = (float)m;
+    w->x_scale[f] = (f < n_feat && v > 1e-20) ? (float)(1.0 / sqrt(v)) : 0.0f;
+  }
+  const double zm = zs / c, zv = zs2 / c - zm * zm;
+  w->z_shift = (float)zm;
+  w->z_scale = (float)(zv > 1e-20 ? sqrt(zv) : 1.0);
 }
 
 }  // namespace
@@ -385,6 +575,7 @@ int mdz_rheo_create(int device, mdz_rheo_ctx **out) {
     return MDZ_ECUDA;
   }
   c->stream = c->own;
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   *out = c;
   return MDZ_OK;
 }
@@ -397,6 +588,7 @@ int mdz_rheo_destroy(mdz_rheo_ctx *c) {
   if (c->d_iters_n) cudaFree(c->d_iters_n);
   if (c->d_iters_s) cudaFree(c->d_iters_s);
   if (c->d_stats) cudaFree(c->d_stats);
+  if (c->warm_buf) cudaFree(c->warm_buf);
   if (c->h_stats) cudaFreeHost(c->h_stats);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -517,6 +709,198 @@ int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {
   CK(cudaStreamSynchronize(c->stream));
   if (out_n) CK(cudaMemcpy(out_n, c->d_iters_n, (size_t)c->last_Nc * c->last_np * sizeof(int32_t), cudaMemcpyDeviceToHost));
   if (out_s) CK(cudaMemcpy(out_s, c->d_iters_s, (size_t)c->last_Nv * c->last_np * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return MDZ_OK;
+}
+
+
+int mdz_rheo_set_warmstart(mdz_rheo_ctx *c, const mdz_mlp_weights *w, int polish_iters) {
+  if (!c || polish_iters < 0 || polish_iters > 64) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  c->polish_iters = polish_iters;
+  if (!w) { c->warm_ready = 0; return MDZ_OK; }
+  if (w->n_feat < 1 || w->n_feat > kMlpIn || !(w->z_scale != 0.0f)) return MDZ_EINVAL;
+  const int rc = upload_warm(c, w);
+  c->warm_ready = (rc == MDZ_OK);
+  return rc;
+}
+
+int mdz_rheo_collect(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m, const mdz_grid_fields *f,
+                     int final_update, int aniso, int mem, float *X, float *Y, mdz_sweep_stats *st) {
+  if (!X || !Y) return MDZ_EINVAL;
+  return sweep_impl(c, md, m, f, final_update, mem, 0, st, aniso != 0, X, Y);
+}
+
+int mdz_rheo_train_mlp(mdz_rheo_ctx *c, const float *X, const float *Y, int64_t n, int n_feat,
+                       const mdz_mlp_train_cfg *cfg, mdz_mlp_weights *w, float *loss, int mem) {
+  if (!c || !X || !Y || !cfg || !w || n < 128 || n_feat < 1 || n_feat > kMlpIn) return MDZ_EINVAL;
+  if (cfg->batch < 128 || cfg->batch % 128 || cfg->epochs < 1) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  // samples with a finite target, on the host for the statistics and the order
+  std::vector<float> hX, hY;
+  const float *pX = X, *pY = Y;
+  if (mem == MDZ_MEM_DEVICE) {
+    hX.resize((size_t)n * kMlpIn);
+    hY.resize((size_t)n * 2);
+    CK(cudaMemcpy(hX.data(), X, hX.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hY.data(), Y, hY.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    pX = hX.data();
+    pY = hY.data();
+  }
+  std::vector<int> keep;
+  keep.reserve((size_t)n);
+  for (int64_t i = 0; i < n; i++)
+    if (std::isfinite(pY[i * 2]) && std::isfinite(pY[i * 2 + 1])) keep.push_back((int)i);
+  if (keep.size() < 128) return MDZ_EINVAL;
+  if (!(w->z_scale != 0.0f)) init_weights(w, pX, pY, n, n_feat, cfg->seed);
+  w->n_feat = n_feat;
+  TrainBuffers B;
+  int rc = alloc_train(B);
+  if (rc != MDZ_OK) return rc;
+  if ((rc = put_weights(B, w)) != MDZ_OK) return rc;
+  void *dXY = nullptr;
+  int *dperm = nullptr;
+  const size_t xb = (size_t)n * kMlpIn * sizeof(float), yb = (size_t)n * 2 * sizeof(float);
+  CK(cudaMalloc(&dXY, xb + yb));
+  if (cudaMalloc(&dperm, keep.size() * sizeof(int)) != cudaSuccess) { cudaFree(dXY); return MDZ_ENOMEM; }
+  CK(cudaMemcpy(dXY, pX, xb, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((char *)dXY + xb, pY, yb, cudaMemcpyHostToDevice));
+  MlpTrainArgs a;
+  memset(&a, 0, sizeof(a));
+  a.W = B.S;
+  a.X = (const float *)dXY;
+  a.Y = (const float *)((char *)dXY + xb);
+  a.perm = dperm;
+  a.n_feat = n_feat;
+  a.w_pl = cfg->w_pl;
+  const size_t smem = mlp_step_smem();
+  cudaFuncSetAttribute(k_mlp_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_mlp_pack<<<(kP2 + 255) / 256, 256, 0, c->stream>>>(a);
+  std::mt19937_64 rng(cfg->seed ^ 0x9e3779b97f4a7c15ull);
+  const long long nk = (long long)keep.size();
+  const long long steps_per_epoch = (nk + cfg->batch - 1) / cfg->batch;
+  const long long total_steps = steps_per_epoch * cfg->epochs;
+  long long step = 0;
+  std::vector<int> order(keep);
+  rc = MDZ_OK;
+  for (int e = 0; e < cfg->epochs && rc == MDZ_OK; e++) {
+    std::shuffle(order.begin(), order.end(), rng);
+    if (cudaMemcpyAsync(dperm, order.data(), nk * sizeof(int), cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
+        cudaMemsetAsync(B.S.loss, 0, 2 * sizeof(float), c->stream) != cudaSuccess) { rc = MDZ_ECUDA; break; }
+    for (long long off = 0; off < nk; off += cfg->batch, step++) {
+      const long long nb = std::min<long long>(cfg->batch, nk - off);
+      a.offset = off;
+      a.n = off + nb;
+      a.inv_batch = 1.0f / (float)nb;
+      k_mlp_step<<<(unsigned)((nb + kMlpTile - 1) / kMlpTile), kMlpTile, smem, c->stream>>>(a);
+      MlpAdam o;
+      const double frac = (double)step / (double)std::max<long long>(1, total_steps - 1);
+      o.lr = (float)(cfg->lr_final + 0.5 * (cfg->lr - cfg->lr_final) * (1.0 + cos(3.14159265358979323846 * frac)));
+      o.beta1 = cfg->beta1; o.beta2 = cfg->beta2; o.eps = cfg->eps;
+      o.bc1 = (float)(1.0 / (1.0 - pow((double)cfg->beta1, (double)(step + 1))));
+      o.bc2 = (float)(1.0 / (1.0 - pow((double)cfg->beta2, (double)(step + 1))));
+      k_mlp_adam<<<(kP2 + 255) / 256, 256, 0, c->stream>>>(a, o);
+    }
+    if (cudaGetLastError() != cudaSuccess) { rc = MDZ_ECUDA; break; }
+    float hl[2];
+    if (cudaMemcpyAsync(hl, B.S.loss, sizeof(hl), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) { rc = MDZ_ECUDA; break; }
+    if (loss) loss[e] = hl[0] / (float)nk;
+  }
+  int fault = 0;
+  cudaMemcpy(&fault, B.S.fault, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(dXY);
+  cudaFree(dperm);
+  if (rc != MDZ_OK) return rc;
+  if (fault) return MDZ_ECUDA;
+  return get_weights(B, w);
+}
+
+int mdz_rheo_mlp_predict(mdz_rheo_ctx *c, const mdz_mlp_weights *w, const float *X, float *Yp, int64_t n, int mem) {
+  if (!c || !w || !X || !Yp || n < 0) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (n == 0) return MDZ_OK;
+  CK(cudaSetDevice(c->device));
+  TrainBuffers B;
+  int rc = alloc_train(B);
+  if (rc != MDZ_OK) return rc;
+  if ((rc = put_weights(B, w)) != MDZ_OK) return rc;
+  const float *dX = X;
+  float *dY = Yp;
+  void *tmp = nullptr;
+  const size_t xb = (size_t)n * kMlpIn * sizeof(float), yb = (size_t)n * 2 * sizeof(float);
+  if (mem == MDZ_MEM_HOST) {
+    CK(cudaMalloc(&tmp, xb + yb));
+    CK(cudaMemcpy(tmp, X, xb, cudaMemcpyHostToDevice));
+    dX = (const float *)tmp;
+    dY = (float *)((char *)tmp + xb);
+  }
+  MlpTrainArgs a;
+  memset(&a, 0, sizeof(a));
+  a.W = B.S;
+  a.X = dX;
+  a.n = n;
+  a.n_feat = w->n_feat;
+  k_mlp_pack<<<(kP2 + 255) / 256, 256, 0, c->stream>>>(a);
+  const size_t smem = mlp_predict_smem();
+  cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const long long tiles = (n + kMlpTile - 1) / kMlpTile;
+  const int grid = (int)std::min<long long>(tiles, (long long)c->sms * 2);
+  k_mlp_predict<<<grid, kMlpTile, smem, c->stream>>>(a, dY);
+  rc = (cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(c->stream) == cudaSuccess) ? MDZ_OK : MDZ_ECUDA;
+  if (rc == MDZ_OK && mem == MDZ_MEM_HOST) rc = (cudaMemcpy(Yp, dY, yb, cudaMemcpyDeviceToHost) == cudaSuccess) ? MDZ_OK : MDZ_ECUDA;
+  int fault = 0;
+  cudaMemcpy(&fault, B.S.fault, sizeof(int), cudaMemcpyDeviceToHost);
+  if (tmp) cudaFree(tmp);
+  return (rc == MDZ_OK && fault) ? MDZ_ECUDA : rc;
+}
+
+
+int mdz_rheo_mlp_gradient(mdz_rheo_ctx *c, const mdz_mlp_weights *w, const float *X, const float *Y, int64_t n,
+                          float w_pl, mdz_mlp_weights *grad, float *loss, int mem) {
+  if (!c || !w || !X || !Y || !grad || n < 1) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  TrainBuffers B;
+  int rc = alloc_train(B);
+  if (rc != MDZ_OK) return rc;
+  if ((rc = put_weights(B, w)) != MDZ_OK) return rc;
+  const float *dX = X, *dY = Y;
+  void *tmp = nullptr;
+  const size_t xb = (size_t)n * kMlpIn * sizeof(float), yb = (size_t)n * 2 * sizeof(float);
+  if (mem == MDZ_MEM_HOST) {
+    CK(cudaMalloc(&tmp, xb + yb));
+    CK(cudaMemcpy(tmp, X, xb, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((char *)tmp + xb, Y, yb, cudaMemcpyHostToDevice));
+    dX = (const float *)tmp;
+    dY = (const float *)((char *)tmp + xb);
+  }
+  MlpTrainArgs a;
+  memset(&a, 0, sizeof(a));
+  a.W = B.S;
+  a.X = dX;
+  a.Y = dY;
+  a.n = n;
+  a.n_feat = w->n_feat;
+  a.inv_batch = 1.0f / (float)n;
+  a.w_pl = w_pl;
+  k_mlp_pack<<<(kP2 + 255) / 256, 256, 0, c->stream>>>(a);
+  const size_t smem = mlp_step_smem();
+  cudaFuncSetAttribute(k_mlp_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_mlp_step<<<(unsigned)((n + kMlpTile - 1) / kMlpTile), kMlpTile, smem, c->stream>>>(a);
+  rc = (cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(c->stream) == cudaSuccess) ? MDZ_OK : MDZ_ECUDA;
+  if (tmp) cudaFree(tmp);
+  if (rc != MDZ_OK) return rc;
+  int fault = 0;
+  CK(cudaMemcpy(&fault, B.S.fault, sizeof(int), cudaMemcpyDeviceToHost));
+  if (fault) return MDZ_ECUDA;
+  CK(cudaMemcpy(grad->W1, B.S.gW1, kP1 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad->W2, B.S.gW2, kP2 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad->W3, B.S.gW3, kP3 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad->b1, B.S.gb1, 64 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad->b2, B.S.gb2, 64 * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad->b3, B.S.gb3, 2 * sizeof(float), cudaMemcpyDeviceToHost));
+  if (loss) CK(cudaMemcpy(loss, B.S.loss, 2 * sizeof(float), cudaMemcpyDeviceToHost));
   return MDZ_OK;
 }
 

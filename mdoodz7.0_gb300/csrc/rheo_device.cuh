@@ -469,15 +469,20 @@ __device__ inline int plastic_popov(const ModelConst &M, const PhaseConst &ph, d
 // ViscosityConcise (RheologyDensity.c:385-1080) for phase `ph` at a node prepared by
 // node_setup_iso.  `warm_eta` > 0 replaces the initial guess eta_up (learned warm start).
 // ---------------------------------------------------------------------------------------
-__device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                 double warm_eta, PointOut &o) {
+// State carried from the set-up of one (node, phase) to its local solve.
+struct IsoState {
+  Laws L;
+  double eta_up, eta_lo, eta_cst, Tyield, C, Ag, lnd;
+};
+
+__device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                 IsoState &S, PointOut &o) {
   const int fl = ph.flags;
-  const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
-  const int gbs = (fl & F_GBS) != 0, gs = (fl & F_GS) != 0;
+  const int constant = (fl & F_CST) != 0, diffusion = (fl & F_LIN) != 0, gs = (fl & F_GS) != 0;
   const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
   const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
   const int elastic = c.elastic;
-  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt;
+  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el;
   o.status = MDZ_OK;
   o.Pcorr = P;
   o.X1 = in.X0;
@@ -490,7 +495,7 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
   o.inv_d1 = ph.inv_gs_ref;
   if (diffusion && ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
 
-  Laws L;
+  Laws &L = S.L;
   creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
   double Tyield = 0.0, C = in.C;
   if (plastic == 1) {  // :530-539
@@ -524,12 +529,30 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
   if (inv_max > 0.0) eta_up = fmin(eta_up, 1.0 / inv_max);
   if (elastic == 1) eta_up = fmin(eta_up, eta_el);
 
+  S.eta_up = eta_up; S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
+}
+
+// Local solve (from eta_start), plastic corrections and post-processing of one (node, phase).
+// eta_conv (may be null) receives the converged visco-elastic viscosity, before plasticity.
+__device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                  IsoState &S, double eta_start, PointOut &o, double *eta_conv = nullptr) {
+  const int fl = ph.flags;
+  const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
+  const int gbs = (fl & F_GBS) != 0, gs = (fl & F_GS) != 0;
+  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
+  const int elastic = c.elastic;
+  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt;
+  Laws &L = S.L;
+  const double eta_up = S.eta_up, eta_cst = S.eta_cst, C = S.C, Ag = S.Ag, lnd = S.lnd;
+  double Tyield = S.Tyield;
+  (void)T;
   double eta_ve, Tii, e_cst, e_pwl, e_exp, e_lin;
   if (!gs) {  // LocalIterationViscoElastic (:646)
     VeCoef q;
     ve_coef(L, c, eta_cst, q);
     VeState s;
-    s.eta = (warm_eta > 0.0) ? warm_eta : eta_up;
+    s.eta = eta_start;
     s.status = MDZ_OK;
     ve_newton(q, s);
     set_status(o.status, s.status);
@@ -561,6 +584,7 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
     o.inv_d1 = 1.0 / dd;
   }
   const double Tii_ve = Tii;
+  if (eta_conv) *eta_conv = eta_ve;
 
   // plastic corrections (:655-930)
   int is_pl = 0;
@@ -668,6 +692,13 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
   o.eta = eta;
 }
 
+__device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                 double warm_eta, PointOut &o) {
+  IsoState S;
+  iso_setup(M, ph, in, c, S, o);
+  iso_finish(M, ph, in, c, S, (warm_eta > 0.0) ? warm_eta : S.eta_up, o);
+}
+
 // ---------------------------------------------------------------------------------------
 // ViscosityConciseAniso (AnisotropyRoutines.c:282-727).  The node context carries the
 // rotated-frame invariant; Er_* are the rotated strain-rate components.
@@ -698,8 +729,8 @@ __device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const Node
   c.inv_d = 1.0 / in.d;
 }
 
-__device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                   const AnisoNode &an, double warm_eta, PointOut &o) {
+__device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                   const AnisoNode &an, IsoState &S, PointOut &o) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
   const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
@@ -715,7 +746,7 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
   o.inv_d1 = c.inv_d;
   if (diffusion && ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
 
-  Laws L;
+  Laws &L = S.L;
   creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
   L.mech &= ~F_GBS;  // the anisotropic path has no grain-boundary sliding
   L.inv_gbs = 0.0;
@@ -735,6 +766,24 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
   if (peierls) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_EXP]);
   if (diffusion) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_LIN]);
 
+  S.eta_up = eta_up; S.eta_lo = eta_lo; S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = Coh; S.Ag = 0.0;
+  S.lnd = c.lnd;
+  (void)an; (void)T; (void)K; (void)dt; (void)min_eta; (void)max_eta;
+}
+
+// Local solve from warm_eta (> 0) or the reference's bisection, plasticity, post-processing.
+__device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                   const AnisoNode &an, IsoState &S, double warm_eta, PointOut &o,
+                                   double *eta_conv = nullptr) {
+  const int fl = ph.flags;
+  const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
+  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int plastic = (fl & F_PLANY) != 0;
+  const int elastic = c.elastic;
+  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
+  const double min_eta = M.min_eta, max_eta = M.max_eta;
+  Laws &L = S.L;
+  const double eta_up = S.eta_up, eta_lo = S.eta_lo, eta_cst = S.eta_cst, Tyield = S.Tyield;
   double eta_ve = eta_up, Tii = 0.0, e_cst = 0.0, e_pwl = 0.0, e_exp = 0.0, e_lin = 0.0;
   if (fl & F_GS) {  // :429-473
     GseIn g;
@@ -787,6 +836,7 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
   if (eta_ve < min_eta) eta_ve = min_eta;  // :589-603
   if (eta_ve > max_eta) eta_ve = max_eta;
   const double Tii_ve = Tii;
+  if (eta_conv) *eta_conv = eta_ve;
   double Tr_xx = 2.0 * eta_ve * an.Er_xx, Tr_zz = 2.0 * eta_ve * an.Er_zz, Tr_xz = 2.0 * eta_ve * an.Er_xz / in.ani_fac;
   double eta_vep = eta_ve, gdot = 0.0, Pc = P;
   const double Ft = Tii - Tyield;
@@ -839,6 +889,13 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
   if (eta > max_eta) eta = max_eta;  // :720-721
   if (eta < min_eta) eta = min_eta;
   o.eta = eta;
+}
+
+__device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                   const AnisoNode &an, double warm_eta, PointOut &o) {
+  IsoState S;
+  aniso_setup(M, ph, in, c, an, S, o);
+  aniso_finish(M, ph, in, c, an, S, warm_eta, o);
 }
 
 // EffectiveStrainRate, RheologyDensity.c:116-146

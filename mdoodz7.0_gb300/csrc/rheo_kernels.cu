@@ -6,8 +6,15 @@
 // thread per node over the index space [centroids | vertices], per-phase tables in the
 // kernel's constant parameter bank (uniform across a warp, so every lookup is a
 // broadcast), SoA loads and stores coalesced along the node index.
+//
+// k_sweep_tiles<ANISO, MODE> walks the same index space in tiles of 128 nodes, one tile
+// per CTA at a time, with the phase loop uniform over the CTA so that a block-wide stage
+// can sit between each phase's set-up and its local solve: the learned warm start
+// (MODE_WARM: tcgen05 MLP + FP32 polish), the FP32 polish alone (MODE_POLISH), or the
+// training-data dump (MODE_COLLECT).
 #include <cuda_runtime.h>
 
+#include "mlp.cuh"
 #include "rheo_kernels.cuh"
 
 namespace mdz {
@@ -24,87 +31,148 @@ struct Acc {
 };
 
 // ---------------------------------------------------------------------------------
-// one centroid (RheologyDensity.c:1156-1316 / AnisotropyRoutines.c:910-1087)
+// one node: load and prepare (RheologyDensity.c:1165-1204, :1324-1340;
+// AnisotropyRoutines.c:917-977, :1097-1131)
 // ---------------------------------------------------------------------------------
+struct Node {
+  long long idx;  // centroid c0, or vertex c1
+  bool centroid, solid;
+  double eta_e, inv_eta_e, d1, d2, anif;
+  double interp[4];  // vertex T_s, P_s, d0_s, phi0_s
+  NodeIn in;
+  NodeCtx ctx;
+  AnisoNode an;
+};
+
 template <bool ANISO>
-__device__ __forceinline__ void do_centroid(const SweepArgs &A, long long c0, Acc &acc) {
+__device__ __forceinline__ void node_prepare(const SweepArgs &A, long long i, Node &n) {
   const ModelConst &M = A.M;
-  const int np = M.np, avg = M.eta_average;
-  double out[CO_COUNT];
+  n.centroid = i < M.Nc;
+  const double el = (M.elastic == 1) ? 1.0 : 0.0;
+  double mu, exxd, ezzd, exz;
+  if (n.centroid) {
+    const long long c0 = i;
+    n.idx = c0;
+    const signed char bc = A.bcp[c0];
+    n.solid = (bc != 30 && bc != 31);
+    if (!n.solid) return;
+    mu = A.ci[CI_mu][c0];
+    exxd = A.ci[CI_exxd][c0]; ezzd = A.ci[CI_ezzd][c0]; exz = A.ci[CI_exz][c0];
+    n.in.Txx0 = A.ci[CI_sxxd0][c0]; n.in.Tzz0 = A.ci[CI_szzd0][c0]; n.in.Txz0 = A.ci[CI_sxz0][c0];
+    n.in.T = A.ci[CI_T][c0]; n.in.P = A.ci[CI_p_in][c0]; n.in.d = A.ci[CI_d0][c0];
+    n.in.phi = A.ci[CI_phi0][c0]; n.in.X0 = A.ci[CI_X0][c0]; n.in.dil = A.ci[CI_dil][c0];
+    n.in.fric = A.ci[CI_fric][c0]; n.in.C = A.ci[CI_C][c0]; n.in.P0 = A.ci[CI_p0][c0]; n.in.T0 = A.ci[CI_T0][c0];
+    n.in.beta = A.ci[CI_bet][c0];
+    if (ANISO) { n.d1 = A.ci[CI_d1][c0]; n.d2 = A.ci[CI_d2][c0]; n.anif = A.ci[CI_anif][c0]; }
+  } else {
+    const long long c1 = i - M.Nc;
+    n.idx = c1;
+    const int Nx = M.Nx, k = (int)(c1 % Nx), l = (int)(c1 / Nx);
+    const signed char bcg = A.bcg[c1];
+    n.solid = (bcg != 30);
+    n.interp[0] = n.interp[1] = n.interp[2] = n.interp[3] = 0.0;
+    if (!n.solid) return;
+    const int idx[4] = {ring_to_centroid(k, l, M.Ncx, M.Ncz, M.periodic_x),
+                        ring_to_centroid(k + 1, l, M.Ncx, M.Ncz, M.periodic_x),
+                        ring_to_centroid(k, l + 1, M.Ncx, M.Ncz, M.periodic_x),
+                        ring_to_centroid(k + 1, l + 1, M.Ncx, M.Ncz, M.periodic_x)};
 #pragma unroll
-  for (int i = 0; i < CO_COUNT; i++) out[i] = 0.0;
-  const signed char bc = A.bcp[c0];
-  if (bc != 30 && bc != 31) {
-    NodeIn in;
-    const double mu = A.ci[CI_mu][c0];
-    const double eta_e = (M.elastic == 1) ? M.dt_model * mu : 1.0;
-    const double inv_eta_e = ANISO ? 1.0 / eta_e : 0.0;
-    const double el = (M.elastic == 1) ? 1.0 : 0.0;
-    const double exxd = A.ci[CI_exxd][c0], ezzd = A.ci[CI_ezzd][c0], exz = A.ci[CI_exz][c0];
-    in.Txx0 = A.ci[CI_sxxd0][c0]; in.Tzz0 = A.ci[CI_szzd0][c0]; in.Txz0 = A.ci[CI_sxz0][c0];
-    double d1 = 0.0, d2 = 0.0, anif = 1.0;
-    if (!ANISO) {
-      const double h = el * 0.5 / eta_e;  // el / eta_e / 2
-      in.Exx = exxd + in.Txx0 * h;
-      in.Ezz = ezzd + in.Tzz0 * h;
-      in.Exz = exz + in.Txz0 * h;
-    } else {
-      d1 = A.ci[CI_d1][c0]; d2 = A.ci[CI_d2][c0]; anif = A.ci[CI_anif][c0];
-      double sn, cs;
-      sincos(A.ci[CI_angle][c0] - M_PI / 2.0, &sn, &cs);
-      in.lxlz = cs * sn; in.lx2 = cs * cs; in.ani_fac = anif;
-      effective_strain_rate(in.Exx, in.Ezz, in.Exz, exxd, ezzd, exz, in.Txx0, in.Tzz0, in.Txz0, d1, d2,
-                            1.0 - 1.0 / anif, eta_e, M.elastic);
+    for (int j = 0; j < 4; j++) {
+      const signed char f = A.bcp[idx[j]];
+      const double w = (f == 30 || f == 31) ? 0.0 : 1.0;
+      n.interp[0] += w * A.ci[CI_T][idx[j]];
+      n.interp[1] += w * A.ci[CI_p_in][idx[j]];
+      n.interp[2] += w * A.ci[CI_d0][idx[j]];
+      n.interp[3] += w * A.ci[CI_phi0][idx[j]];
     }
-    in.G = mu; in.T = A.ci[CI_T][c0]; in.P = A.ci[CI_p_in][c0]; in.d = A.ci[CI_d0][c0];
-    in.phi = A.ci[CI_phi0][c0]; in.X0 = A.ci[CI_X0][c0]; in.dil = A.ci[CI_dil][c0];
-    in.fric = A.ci[CI_fric][c0]; in.C = A.ci[CI_C][c0]; in.P0 = A.ci[CI_p0][c0]; in.T0 = A.ci[CI_T0][c0];
-    in.beta = A.ci[CI_bet][c0];
-    in.centroid = 1; in.final_update = A.final_update; in.post_process = 1;
-    in.want_rho = (M.density_variations == 1);
-    NodeCtx ctx;
-    AnisoNode an;
-    if (ANISO) node_setup_aniso(M, in, A.need_lnd, ctx, an);
-    else node_setup_iso(M, in, A.need_lnd, ctx);
-    int status = MDZ_OK;
-    for (int p = 0; p < np; p++) {
-      const double perc = A.perc_n[p][c0];
-      if (!(fabs(perc) > 1e-13)) {  // :1210-1212
-        if (A.iters_n) A.iters_n[(long long)p * M.Nc + c0] = 0;
-        continue;
-      }
-      PointOut o;
-      if (ANISO) point_aniso(M, A.ph[p], in, ctx, an, 0.0, o);
-      else point_iso(M, A.ph[p], in, ctx, 0.0, o);
-      set_status(status, o.status);
-      acc.calls++; acc.iters += o.iters; acc.plastic += o.is_pl;
-      acc.maxit = max(acc.maxit, (unsigned)o.iters);
-      if (A.iters_n) A.iters_n[(long long)p * M.Nc + c0] = o.iters;
-      A.peta_n[p][c0] = o.etaVE;
-      if (avg == 0) { out[CO_eta] += perc * o.etaVE; out[CO_eta_phys] += perc * o.eta; }
-      else if (avg == 1) { out[CO_eta] += perc / o.etaVE; out[CO_eta_phys] += perc / o.eta; }
-      else { out[CO_eta] += perc * log(o.etaVE); out[CO_eta_phys] += perc * log(o.eta); }
-      if (ANISO) out[CO_VE] += perc * o.etaVE * inv_eta_e;
-      out[CO_eII_el] += perc * o.Eii_el;
-      out[CO_eII_pl] += perc * o.Eii_pl;
-      out[CO_eII_pwl] += perc * o.Eii_pwl;
-      out[CO_eII_exp] += perc * o.Eii_exp;
-      out[CO_eII_lin] += perc * o.Eii_lin;
-      out[CO_eII_gbs] += perc * o.Eii_gbs;
-      out[CO_eII_cst] += perc * o.Eii_cst;
-      out[CO_d] += perc * o.inv_d1;
-      out[CO_Wtot] += perc * o.Wtot;
-      out[CO_Wdiss] += perc * o.Wdiss;
-      out[CO_Wel] += perc * o.Wel;
-      out[CO_p_corr] += perc * o.Pcorr;
-      out[CO_div_el] += perc * o.div_el;
-      out[CO_div_pl] += perc * o.div_pl;
-      out[CO_X] += perc * o.X1;
-      out[CO_OverS] += perc * o.OverS;
-      out[CO_rho] += perc * o.rho;
+#pragma unroll
+    for (int j = 0; j < 4; j++) n.interp[j] *= 0.25;
+    mu = A.vi[VI_mu][c1];
+    exxd = A.vi[VI_exxd][c1]; ezzd = A.vi[VI_ezzd][c1]; exz = A.vi[VI_exz][c1];
+    n.in.Txx0 = A.vi[VI_sxxd0][c1]; n.in.Tzz0 = A.vi[VI_szzd0][c1]; n.in.Txz0 = A.vi[VI_sxz0][c1];
+    n.in.T = n.interp[0]; n.in.P = n.interp[1]; n.in.d = n.interp[2]; n.in.phi = n.interp[3];
+    n.in.X0 = A.vi[VI_X0][c1]; n.in.dil = A.vi[VI_dil][c1]; n.in.fric = A.vi[VI_fric][c1];
+    n.in.C = A.vi[VI_C][c1]; n.in.P0 = A.vi[VI_p0][c1]; n.in.T0 = 0.0; n.in.beta = A.vi[VI_bet][c1];
+    if (ANISO) { n.d1 = A.vi[VI_d1][c1]; n.d2 = A.vi[VI_d2][c1]; n.anif = A.vi[VI_anif][c1]; }
+  }
+  n.in.G = mu;
+  n.eta_e = (M.elastic == 1) ? M.dt_model * mu : 1.0;
+  n.inv_eta_e = ANISO ? 1.0 / n.eta_e : 0.0;
+  if (!ANISO) {
+    const double h = el * 0.5 / n.eta_e;  // el / eta_e / 2
+    n.in.Exx = exxd + n.in.Txx0 * h;
+    n.in.Ezz = ezzd + n.in.Tzz0 * h;
+    n.in.Exz = exz + n.in.Txz0 * h;
+  } else {
+    const double angle = n.centroid ? A.ci[CI_angle][n.idx] : A.vi[VI_angle][n.idx];
+    double sn, cs;
+    sincos(angle - M_PI / 2.0, &sn, &cs);
+    n.in.lxlz = cs * sn; n.in.lx2 = cs * cs; n.in.ani_fac = n.anif;
+    effective_strain_rate(n.in.Exx, n.in.Ezz, n.in.Exz, exxd, ezzd, exz, n.in.Txx0, n.in.Tzz0, n.in.Txz0, n.d1,
+                          n.d2, 1.0 - 1.0 / n.anif, n.eta_e, M.elastic);
+  }
+  n.in.centroid = n.centroid ? 1 : 0;
+  n.in.final_update = A.final_update;
+  n.in.post_process = 1;
+  n.in.want_rho = n.centroid && (M.density_variations == 1);
+  if (ANISO) node_setup_aniso(M, n.in, A.need_lnd, n.ctx, n.an);
+  else node_setup_iso(M, n.in, A.need_lnd, n.ctx);
+}
+
+__device__ __forceinline__ double node_perc(const SweepArgs &A, const Node &n, int p) {
+  return n.centroid ? A.perc_n[p][n.idx] : A.perc_s[p][n.idx];
+}
+
+__device__ __forceinline__ void node_iters(const SweepArgs &A, const Node &n, int p, int it) {
+  if (n.centroid) { if (A.iters_n) A.iters_n[(long long)p * A.M.Nc + n.idx] = it; }
+  else if (A.iters_s) A.iters_s[(long long)p * A.M.Nv + n.idx] = it;
+}
+
+// accumulate one phase's result (RheologyDensity.c:1217-1270, :1359-1378)
+template <bool ANISO>
+__device__ __forceinline__ void node_accumulate(const SweepArgs &A, const Node &n, int p, double perc,
+                                                const PointOut &o, double *out, Acc &acc, int &status) {
+  set_status(status, o.status);
+  acc.calls++; acc.iters += o.iters; acc.plastic += o.is_pl;
+  acc.maxit = max(acc.maxit, (unsigned)o.iters);
+  node_iters(A, n, p, o.iters);
+  if (n.centroid) A.peta_n[p][n.idx] = o.etaVE;
+  else A.peta_s[p][n.idx] = o.etaVE;
+  const int avg = A.M.eta_average;
+  if (avg == 0) { out[CO_eta] += perc * o.etaVE; out[CO_eta_phys] += perc * o.eta; }
+  else if (avg == 1) { out[CO_eta] += perc / o.etaVE; out[CO_eta_phys] += perc / o.eta; }
+  else { out[CO_eta] += perc * log(o.etaVE); out[CO_eta_phys] += perc * log(o.eta); }
+  if (ANISO) out[CO_VE] += perc * o.etaVE * n.inv_eta_e;
+  out[CO_X] += perc * o.X1;
+  if (!n.centroid) return;
+  out[CO_eII_el] += perc * o.Eii_el;
+  out[CO_eII_pl] += perc * o.Eii_pl;
+  out[CO_eII_pwl] += perc * o.Eii_pwl;
+  out[CO_eII_exp] += perc * o.Eii_exp;
+  out[CO_eII_lin] += perc * o.Eii_lin;
+  out[CO_eII_gbs] += perc * o.Eii_gbs;
+  out[CO_eII_cst] += perc * o.Eii_cst;
+  out[CO_d] += perc * o.inv_d1;
+  out[CO_Wtot] += perc * o.Wtot;
+  out[CO_Wdiss] += perc * o.Wdiss;
+  out[CO_Wel] += perc * o.Wel;
+  out[CO_p_corr] += perc * o.Pcorr;
+  out[CO_div_el] += perc * o.div_el;
+  out[CO_div_pl] += perc * o.div_pl;
+  out[CO_OverS] += perc * o.OverS;
+  out[CO_rho] += perc * o.rho;
+}
+
+// finalize the averages and the stress, then store (:1274-1313, :1380-1405)
+template <bool ANISO>
+__device__ __forceinline__ void node_store(const SweepArgs &A, const Node &n, double *out, int status) {
+  const ModelConst &M = A.M;
+  const int avg = M.eta_average;
+  if (n.solid) {
+    if (n.centroid) {
+      out[CO_d] = 1.0 / out[CO_d];
+      if (!ANISO && (isinf(out[CO_d]) || isnan(out[CO_d]))) set_status(status, MDZ_EEMPTY_CELL);
     }
-    out[CO_d] = 1.0 / out[CO_d];
-    if (!ANISO && (isinf(out[CO_d]) || isnan(out[CO_d]))) set_status(status, MDZ_EEMPTY_CELL);
     if (avg == 1) {
       out[CO_eta] = 1.0 / out[CO_eta];
       out[CO_eta_phys] = 1.0 / out[CO_eta_phys];
@@ -114,125 +182,31 @@ __device__ __forceinline__ void do_centroid(const SweepArgs &A, long long c0, Ac
       out[CO_eta_phys] = exp(out[CO_eta_phys]);
     }
     const double eta2 = 2.0 * out[CO_eta];
+    const NodeIn &in = n.in;
     if (!ANISO) {
       out[CO_sxxd] = eta2 * in.Exx; out[CO_szzd] = eta2 * in.Ezz; out[CO_sxz] = eta2 * in.Exz;
     } else {  // AnisotropyRoutines.c:1079-1086
-      const double a = 1.0 - 1.0 / anif;
+      const double a = 1.0 - 1.0 / n.anif, d1 = n.d1, d2 = n.d2;
       out[CO_sxxd] = eta2 * (in.Exx * (1.0 - a * d1) + in.Ezz * a * d1 - 2.0 * in.Exz * a * d2);
       out[CO_szzd] = eta2 * (in.Ezz * (1.0 - a * d1) + in.Exx * a * d1 + 2.0 * in.Exz * a * d2);
       out[CO_sxz] = eta2 * (-in.Exx * a * d2 + in.Ezz * a * d2 + 2 * in.Exz * (a * (d1 - 0.5) + 0.5));
     }
-    record_error(A.stats, c0, status);
-  } else if (A.iters_n) {
-    for (int p = 0; p < np; p++) A.iters_n[(long long)p * M.Nc + c0] = 0;
+    record_error(A.stats, n.centroid ? n.idx : M.Nc + n.idx, status);
+  } else {
+    for (int p = 0; p < M.np; p++) node_iters(A, n, p, 0);
   }
+  if (n.centroid) {
 #pragma unroll
-  for (int i = 0; i < CO_COUNT; i++)
-    if (A.co[i]) A.co[i][c0] = out[i];
-}
-
-// ---------------------------------------------------------------------------------
-// one vertex, with the fused centroid-to-vertex interpolation (GridRoutines.c:108-210)
-// ---------------------------------------------------------------------------------
-template <bool ANISO>
-__device__ __forceinline__ void do_vertex(const SweepArgs &A, long long c1, Acc &acc) {
-  const ModelConst &M = A.M;
-  const int np = M.np, avg = M.eta_average, Nx = M.Nx;
-  const int k = (int)(c1 % Nx), l = (int)(c1 / Nx);
-  const signed char bcg = A.bcg[c1];
-  double Ts = 0.0, Ps = 0.0, ds = 0.0, phis = 0.0;
-  if (bcg != 30) {
-    const int idx[4] = {ring_to_centroid(k, l, M.Ncx, M.Ncz, M.periodic_x),
-                        ring_to_centroid(k + 1, l, M.Ncx, M.Ncz, M.periodic_x),
-                        ring_to_centroid(k, l + 1, M.Ncx, M.Ncz, M.periodic_x),
-                        ring_to_centroid(k + 1, l + 1, M.Ncx, M.Ncz, M.periodic_x)};
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const signed char f = A.bcp[idx[j]];
-      const double w = (f == 30 || f == 31) ? 0.0 : 1.0;
-      Ts += w * A.ci[CI_T][idx[j]];
-      Ps += w * A.ci[CI_p_in][idx[j]];
-      ds += w * A.ci[CI_d0][idx[j]];
-      phis += w * A.ci[CI_phi0][idx[j]];
-    }
-    Ts *= 0.25; Ps *= 0.25; ds *= 0.25; phis *= 0.25;
+    for (int i = 0; i < CO_COUNT; i++)
+      if (A.co[i]) A.co[i][n.idx] = out[i];
+  } else {
+    const long long c1 = n.idx;
+    A.vo[VO_T][c1] = n.interp[0]; A.vo[VO_P][c1] = n.interp[1];
+    A.vo[VO_d0][c1] = n.interp[2]; A.vo[VO_phi0][c1] = n.interp[3];
+    A.vo[VO_sxxd][c1] = out[CO_sxxd]; A.vo[VO_szzd][c1] = out[CO_szzd]; A.vo[VO_sxz][c1] = out[CO_sxz];
+    A.vo[VO_eta_phys][c1] = out[CO_eta_phys]; A.vo[VO_eta][c1] = out[CO_eta]; A.vo[VO_X][c1] = out[CO_X];
+    if (A.vo[VO_VE]) A.vo[VO_VE][c1] = out[CO_VE];
   }
-  A.vo[VO_T][c1] = Ts; A.vo[VO_P][c1] = Ps; A.vo[VO_d0][c1] = ds; A.vo[VO_phi0][c1] = phis;
-
-  double eta = 0.0, eta_phys = 0.0, X = 0.0, VE = 0.0, sxx = 0.0, szz = 0.0, sxz = 0.0;
-  if (bcg != 30) {
-    NodeIn in;
-    const double mu = A.vi[VI_mu][c1];
-    const double eta_e = (M.elastic == 1) ? M.dt_model * mu : 1.0;
-    const double inv_eta_e = ANISO ? 1.0 / eta_e : 0.0;
-    const double el = (M.elastic == 1) ? 1.0 : 0.0;
-    const double exxd = A.vi[VI_exxd][c1], ezzd = A.vi[VI_ezzd][c1], exz = A.vi[VI_exz][c1];
-    in.Txx0 = A.vi[VI_sxxd0][c1]; in.Tzz0 = A.vi[VI_szzd0][c1]; in.Txz0 = A.vi[VI_sxz0][c1];
-    double d1 = 0.0, d2 = 0.0, anif = 1.0;
-    if (!ANISO) {
-      const double h = el * 0.5 / eta_e;  // el / eta_e / 2
-      in.Exx = exxd + in.Txx0 * h;
-      in.Ezz = ezzd + in.Tzz0 * h;
-      in.Exz = exz + in.Txz0 * h;
-    } else {
-      d1 = A.vi[VI_d1][c1]; d2 = A.vi[VI_d2][c1]; anif = A.vi[VI_anif][c1];
-      double sn, cs;
-      sincos(A.vi[VI_angle][c1] - M_PI / 2.0, &sn, &cs);
-      in.lxlz = cs * sn; in.lx2 = cs * cs; in.ani_fac = anif;
-      effective_strain_rate(in.Exx, in.Ezz, in.Exz, exxd, ezzd, exz, in.Txx0, in.Tzz0, in.Txz0, d1, d2,
-                            1.0 - 1.0 / anif, eta_e, M.elastic);
-    }
-    in.G = mu; in.T = Ts; in.P = Ps; in.d = ds; in.phi = phis; in.X0 = A.vi[VI_X0][c1];
-    in.dil = A.vi[VI_dil][c1]; in.fric = A.vi[VI_fric][c1]; in.C = A.vi[VI_C][c1]; in.P0 = A.vi[VI_p0][c1];
-    in.T0 = 0.0; in.beta = A.vi[VI_bet][c1];
-    in.centroid = 0; in.final_update = A.final_update; in.post_process = 1; in.want_rho = 0;
-    NodeCtx ctx;
-    AnisoNode an;
-    if (ANISO) node_setup_aniso(M, in, A.need_lnd, ctx, an);
-    else node_setup_iso(M, in, A.need_lnd, ctx);
-    int status = MDZ_OK;
-    for (int p = 0; p < np; p++) {
-      const double perc = A.perc_s[p][c1];
-      if (!(fabs(perc) > 1e-13)) {
-        if (A.iters_s) A.iters_s[(long long)p * M.Nv + c1] = 0;
-        continue;
-      }
-      PointOut o;
-      if (ANISO) point_aniso(M, A.ph[p], in, ctx, an, 0.0, o);
-      else point_iso(M, A.ph[p], in, ctx, 0.0, o);
-      set_status(status, o.status);
-      acc.calls++; acc.iters += o.iters; acc.plastic += o.is_pl;
-      acc.maxit = max(acc.maxit, (unsigned)o.iters);
-      if (A.iters_s) A.iters_s[(long long)p * M.Nv + c1] = o.iters;
-      A.peta_s[p][c1] = o.etaVE;
-      if (avg == 0) { eta += perc * o.etaVE; eta_phys += perc * o.eta; }
-      else if (avg == 1) { eta += perc / o.etaVE; eta_phys += perc / o.eta; }
-      else { eta += perc * log(o.etaVE); eta_phys += perc * log(o.eta); }
-      if (ANISO) VE += perc * o.etaVE * inv_eta_e;
-      X += perc * o.X1;
-    }
-    if (avg == 1) {
-      eta = 1.0 / eta; eta_phys = 1.0 / eta_phys;
-      if (isinf(eta_phys) || isnan(eta_phys)) set_status(status, MDZ_ENONFINITE);
-    } else if (avg == 2) {
-      eta = exp(eta); eta_phys = exp(eta_phys);
-    }
-    const double eta2 = 2.0 * eta;
-    if (!ANISO) {
-      sxx = eta2 * in.Exx; szz = eta2 * in.Ezz; sxz = eta2 * in.Exz;
-    } else {
-      const double a = 1.0 - 1.0 / anif;
-      sxx = eta2 * (in.Exx * (1.0 - a * d1) + in.Ezz * a * d1 - 2.0 * in.Exz * a * d2);
-      szz = eta2 * (in.Ezz * (1.0 - a * d1) + in.Exx * a * d1 + 2.0 * in.Exz * a * d2);
-      sxz = eta2 * (-in.Exx * a * d2 + in.Ezz * a * d2 + 2 * in.Exz * (a * (d1 - 0.5) + 0.5));
-    }
-    record_error(A.stats, M.Nc + c1, status);
-  } else if (A.iters_s) {
-    for (int p = 0; p < np; p++) A.iters_s[(long long)p * M.Nv + c1] = 0;
-  }
-  A.vo[VO_sxxd][c1] = sxx; A.vo[VO_szzd][c1] = szz; A.vo[VO_sxz][c1] = sxz;
-  A.vo[VO_eta_phys][c1] = eta_phys; A.vo[VO_eta][c1] = eta; A.vo[VO_X][c1] = X;
-  if (A.vo[VO_VE]) A.vo[VO_VE][c1] = VE;
 }
 
 __device__ __forceinline__ void flush_acc(DevStats *st, Acc &acc) {
@@ -251,14 +225,123 @@ __device__ __forceinline__ void flush_acc(DevStats *st, Acc &acc) {
   }
 }
 
+// ---------------------------------------------------------------------------------
+// plain sweep: one thread per node
+// ---------------------------------------------------------------------------------
 template <bool ANISO>
 __global__ void __launch_bounds__(128) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0};
   const long long total = A.M.Nc + A.M.Nv;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-    if (i < A.M.Nc) do_centroid<ANISO>(A, i, acc);
-    else do_vertex<ANISO>(A, i - A.M.Nc, acc);
+    Node n;
+    node_prepare<ANISO>(A, i, n);
+    double out[CO_COUNT];
+#pragma unroll
+    for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
+    int status = MDZ_OK;
+    if (n.solid) {
+      for (int p = 0; p < A.M.np; p++) {
+        const double perc = node_perc(A, n, p);
+        if (!(fabs(perc) > 1e-13)) {  // :1210-1212
+          node_iters(A, n, p, 0);
+          continue;
+        }
+        PointOut o;
+        if (ANISO) point_aniso(A.M, A.ph[p], n.in, n.ctx, n.an, 0.0, o);
+        else point_iso(A.M, A.ph[p], n.in, n.ctx, 0.0, o);
+        node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
+      }
+    }
+    node_store<ANISO>(A, n, out, status);
+  }
+  flush_acc(A.stats, acc);
+}
+
+// ---------------------------------------------------------------------------------
+// tiled sweep with a block-wide stage per phase (learned warm start / data collection)
+// ---------------------------------------------------------------------------------
+template <bool ANISO, int MODE>
+__global__ void __launch_bounds__(128) k_sweep_tiles(const __grid_constant__ SweepArgs A,
+                                                     const __grid_constant__ WarmArgs W) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  MlpShared &S = *reinterpret_cast<MlpShared *>(smem_raw);
+  uint32_t phase = 0;
+  if (MODE == MODE_WARM) mlp_begin(S, W.mlp);
+  Acc acc = {0, 0, 0, 0};
+  const long long total = A.M.Nc + A.M.Nv;
+  const long long ntiles = (total + kMlpTile - 1) / kMlpTile;
+  const int nfeat = ANISO ? kFeatAniso : kFeatIso;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {  // uniform over the CTA
+    const long long i = tile * kMlpTile + threadIdx.x;
+    const bool valid = i < total;
+    Node n;
+    n.solid = false;
+    n.centroid = true;
+    if (valid) node_prepare<ANISO>(A, i, n);
+    double out[CO_COUNT];
+#pragma unroll
+    for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
+    int status = MDZ_OK;
+    for (int p = 0; p < A.M.np; p++) {  // uniform over the CTA
+      const double perc = (valid && n.solid) ? node_perc(A, n, p) : 0.0;
+      const bool active = fabs(perc) > 1e-13;
+      if (valid && n.solid && !active) node_iters(A, n, p, 0);
+      IsoState st;
+      PointOut o;
+      float f[kMlpIn];
+#pragma unroll
+      for (int j = 0; j < kMlpIn; j++) f[j] = 0.0f;
+      double eta_start = 0.0;  // 0: the reference's own start
+      if (active) {
+        if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
+        else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
+        warm_features(A.M, n.in, n.ctx, st, ANISO, f);
+      }
+      if (MODE == MODE_WARM) {
+        float x[kMlpIn];
+#pragma unroll
+        for (int j = 0; j < kMlpIn; j++) x[j] = (j < nfeat) ? (f[j] - W.mlp.x_shift[j]) * W.mlp.x_scale[j] : 0.0f;
+        float y[2];
+        mlp_forward(S, x, y, phase);
+        if (active && !S.fault) {
+          const float z = fmaxf(y[0] * W.mlp.z_scale + W.mlp.z_shift, 0.0f);
+          VeCoef q;
+          ve_coef(st.L, n.ctx, st.eta_cst, q);
+          eta_start = (double)ve_polish_f32(q, st.eta_up, __expf(-z), W.mlp.polish_iters) * st.eta_up;
+        }
+      } else if (MODE == MODE_POLISH) {
+        if (active) {
+          VeCoef q;
+          ve_coef(st.L, n.ctx, st.eta_cst, q);
+          eta_start = (double)ve_polish_f32(q, st.eta_up, 1.0f, W.mlp.polish_iters) * st.eta_up;
+        }
+      }
+      if (!active) continue;
+      double eta_conv = 0.0;
+      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, eta_start, o, &eta_conv);
+      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, eta_start > 0.0 ? eta_start : st.eta_up, o, &eta_conv);
+      node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
+      if (MODE == MODE_COLLECT) {
+        const long long item = (long long)p * total + i;
+        float *xo = W.X_out + item * kMlpIn;
+#pragma unroll
+        for (int j = 0; j < kMlpIn; j++) xo[j] = f[j];
+        W.Y_out[item * 2 + 0] = (eta_conv > 0.0) ? (float)log(st.eta_up / eta_conv) : __int_as_float(0x7fc00000);
+        W.Y_out[item * 2 + 1] = (float)o.is_pl;
+      }
+    }
+    if (valid) node_store<ANISO>(A, n, out, status);
+    if (MODE == MODE_COLLECT && valid) {  // items of inactive phases carry a NaN target
+      for (int p = 0; p < A.M.np; p++) {
+        const double perc = n.solid ? node_perc(A, n, p) : 0.0;
+        if (!(fabs(perc) > 1e-13)) W.Y_out[((long long)p * total + i) * 2] = __int_as_float(0x7fc00000);
+      }
+    }
+  }
+  if (MODE == MODE_WARM) {
+    mlp_end(S);
+    if (threadIdx.x == 0 && S.fault) atomicExch(&A.stats->mma_fault, 1u);
   }
   flush_acc(A.stats, acc);
 }
@@ -316,6 +399,45 @@ cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int blo
   if (aniso) k_sweep<true><<<(unsigned)grid, block, 0, s>>>(a);
   else k_sweep<false><<<(unsigned)grid, block, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+template <bool ANISO, int MODE>
+static cudaError_t launch_tiles_t(const SweepArgs &a, const WarmArgs &w, cudaStream_t s, int grid) {
+  const size_t smem = (MODE == MODE_WARM) ? sizeof(MlpShared) : 0;
+  auto fn = k_sweep_tiles<ANISO, MODE>;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  fn<<<grid, kMlpTile, smem, s>>>(a, w);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_tiles(const SweepArgs &a, const WarmArgs &w, bool aniso, int mode, cudaStream_t s,
+                               int grid) {
+  if (grid < 1) grid = 1;
+  switch (mode * 2 + (aniso ? 1 : 0)) {
+    case MODE_COLLECT * 2: return launch_tiles_t<false, MODE_COLLECT>(a, w, s, grid);
+    case MODE_COLLECT * 2 + 1: return launch_tiles_t<true, MODE_COLLECT>(a, w, s, grid);
+    case MODE_WARM * 2: return launch_tiles_t<false, MODE_WARM>(a, w, s, grid);
+    case MODE_WARM * 2 + 1: return launch_tiles_t<true, MODE_WARM>(a, w, s, grid);
+    case MODE_POLISH * 2: return launch_tiles_t<false, MODE_POLISH>(a, w, s, grid);
+    case MODE_POLISH * 2 + 1: return launch_tiles_t<true, MODE_POLISH>(a, w, s, grid);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int tiles_blocks_per_sm(bool aniso, int mode) {
+  int n = 0;
+  const void *fn = nullptr;
+  switch (mode * 2 + (aniso ? 1 : 0)) {
+    case MODE_COLLECT * 2: fn = (const void *)k_sweep_tiles<false, MODE_COLLECT>; break;
+    case MODE_COLLECT * 2 + 1: fn = (const void *)k_sweep_tiles<true, MODE_COLLECT>; break;
+    case MODE_WARM * 2: fn = (const void *)k_sweep_tiles<false, MODE_WARM>; break;
+    case MODE_WARM * 2 + 1: fn = (const void *)k_sweep_tiles<true, MODE_WARM>; break;
+    case MODE_POLISH * 2: fn = (const void *)k_sweep_tiles<false, MODE_POLISH>; break;
+    default: fn = (const void *)k_sweep_tiles<true, MODE_POLISH>; break;
+  }
+  const size_t smem = (mode == MODE_WARM) ? sizeof(MlpShared) : 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kMlpTile, smem);
+  return n > 0 ? n : 1;
 }
 
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s) {

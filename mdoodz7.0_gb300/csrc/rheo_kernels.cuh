@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "mlp.cuh"
 #include "rheo_device.cuh"
 
 namespace mdz {
@@ -22,6 +23,16 @@ struct DevStats {
   unsigned long long err_key;  // (node << 8) | -status of the lowest failing node; ~0 if none
   unsigned long long calls, iters, plastic;
   unsigned int maxit;
+  unsigned int mma_fault;      // a tensor-core completion wait gave up (warm start)
+};
+
+// modes of the tiled sweep
+enum { MODE_COLLECT = 0, MODE_WARM = 1, MODE_POLISH = 2 };
+
+struct WarmArgs {
+  MlpDevice mlp;
+  float *X_out;  // MODE_COLLECT: features [item][kMlpIn], item = p * (Nc + Nv) + node
+  float *Y_out;  // MODE_COLLECT: targets [item][2] = (ln(eta_up / eta_ve), is_pl); NaN for inactive items
 };
 
 struct SweepArgs {
@@ -54,6 +65,9 @@ struct PointArgs {
 
 cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap);
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s);
+cudaError_t launch_sweep_tiles(const SweepArgs &a, const WarmArgs &w, bool aniso, int mode, cudaStream_t s,
+                               int grid);
+int tiles_blocks_per_sm(bool aniso, int mode);
 void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block);
 
 }  // namespace mdz

@@ -47,6 +47,7 @@ MEM_DEVICE = 1
 SWEEP_ASYNC = 0x1
 SWEEP_WARMSTART = 0x2
 SWEEP_ITERS = 0x4
+SWEEP_POLISH = 0x8
 
 # ---- struct layouts (must follow include/mdz_rheo.h field by field) -------
 MAT_INT = ["cstv", "pwlv", "linv", "gbsv", "expv", "gs", "kin", "plast", "density_model",
@@ -104,10 +105,49 @@ class SweepStats(C.Structure):
     _fields_ = [("phase_calls", C.c_uint64), ("newton_iters", C.c_uint64),
                 ("max_newton_iters", C.c_uint32), ("plastic_calls", C.c_uint64),
                 ("status", C.c_int32), ("error_node", C.c_int64), ("elapsed_ms", C.c_double),
-                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint32)]
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint32),
+                ("mma_fault", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+MLP_IN, MLP_HID = 16, 64
+
+
+class MlpWeights(C.Structure):
+    """mdz_mlp_weights: the warm-start perceptron (row-major [out][in] FP32 weights)."""
+    _fields_ = [("n_feat", C.c_int32),
+                ("W1", C.c_float * (MLP_HID * MLP_IN)), ("b1", C.c_float * MLP_HID),
+                ("W2", C.c_float * (MLP_HID * MLP_HID)), ("b2", C.c_float * MLP_HID),
+                ("W3", C.c_float * (2 * MLP_HID)), ("b3", C.c_float * 2),
+                ("x_shift", C.c_float * MLP_IN), ("x_scale", C.c_float * MLP_IN),
+                ("z_shift", C.c_float), ("z_scale", C.c_float)]
+
+    def arrays(self):
+        return {"W1": np.ctypeslib.as_array(self.W1).reshape(MLP_HID, MLP_IN),
+                "b1": np.ctypeslib.as_array(self.b1),
+                "W2": np.ctypeslib.as_array(self.W2).reshape(MLP_HID, MLP_HID),
+                "b2": np.ctypeslib.as_array(self.b2),
+                "W3": np.ctypeslib.as_array(self.W3).reshape(2, MLP_HID),
+                "b3": np.ctypeslib.as_array(self.b3),
+                "x_shift": np.ctypeslib.as_array(self.x_shift), "x_scale": np.ctypeslib.as_array(self.x_scale)}
+
+    def save(self, path):
+        np.savez(path, raw=np.frombuffer(bytes(self), dtype=np.uint8))
+
+    @classmethod
+    def load(cls, path):
+        raw = np.load(path)["raw"]
+        w = cls()
+        C.memmove(C.addressof(w), raw.tobytes(), C.sizeof(w))
+        return w
+
+
+class MlpTrainCfg(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("lr_final", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float), ("w_pl", C.c_float),
+                ("seed", C.c_uint64)]
 
 
 PT_IN = ["G", "T", "P", "d", "phi", "X0", "Exx", "Ezz", "Exz", "Txx0", "Tzz0", "Txz0", "strain_acc",
@@ -219,6 +259,15 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_get_iterations.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_abi_sizes.argtypes = [C.POINTER(C.c_size_t)]
     lib.mdz_rheo_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
+    lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
+                                     C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SweepStats)]
+    lib.mdz_rheo_train_mlp.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int,
+                                       C.POINTER(MlpTrainCfg), C.POINTER(MlpWeights), C.c_void_p, C.c_int]
+    lib.mdz_rheo_mlp_predict.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_void_p, C.c_void_p, C.c_int64,
+                                         C.c_int]
+    lib.mdz_rheo_mlp_gradient.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_void_p, C.c_void_p,
+                                          C.c_int64, C.c_float, C.POINTER(MlpWeights), C.c_void_p, C.c_int]
     _lib = lib
     return lib
 
@@ -304,6 +353,47 @@ class Context:
     def points(self, model, mat, pin, pout, n, aniso=0, mem=MEM_HOST):
         return self.lib.mdz_rheo_points(self.handle, C.byref(model), C.byref(mat), C.byref(pin),
                                         C.byref(pout), n, aniso, mem)
+
+    # ---- learned warm start
+    def set_warmstart(self, w: Optional[MlpWeights], polish_iters: int = 4):
+        rc = self.lib.mdz_rheo_set_warmstart(self.handle, None if w is None else C.byref(w), polish_iters)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_set_warmstart")
+
+    def collect(self, model, mat, fields, X, Y, aniso=False, final_update=0, mem=MEM_HOST):
+        """A sweep that also records per-(phase, node) features X [items, 16] and targets Y [items, 2]."""
+        st = SweepStats()
+        rc = self.lib.mdz_rheo_collect(self.handle, C.byref(model), C.byref(mat), C.byref(fields.struct),
+                                       final_update, int(aniso), mem, _ptr(X), _ptr(Y), C.byref(st))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_collect")
+        return st
+
+    def train_mlp(self, X, Y, n_feat, cfg: MlpTrainCfg, w: Optional[MlpWeights] = None, mem=MEM_HOST):
+        w = MlpWeights() if w is None else w
+        loss = np.zeros(cfg.epochs, np.float32)
+        rc = self.lib.mdz_rheo_train_mlp(self.handle, _ptr(X), _ptr(Y), int(Y.shape[0]), n_feat, C.byref(cfg),
+                                         C.byref(w), loss.ctypes.data, mem)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_train_mlp")
+        return w, loss
+
+    def mlp_predict(self, w: MlpWeights, X, mem=MEM_HOST):
+        n = int(X.shape[0])
+        Yp = np.zeros((n, 2), np.float32)
+        rc = self.lib.mdz_rheo_mlp_predict(self.handle, C.byref(w), _ptr(X), Yp.ctypes.data, n, mem)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_mlp_predict")
+        return Yp
+
+    def mlp_gradient(self, w: MlpWeights, X, Y, w_pl=1.0, mem=MEM_HOST):
+        g = MlpWeights()
+        loss = np.zeros(2, np.float32)
+        rc = self.lib.mdz_rheo_mlp_gradient(self.handle, C.byref(w), _ptr(X), _ptr(Y), int(Y.shape[0]), w_pl,
+                                            C.byref(g), loss.ctypes.data, mem)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_mlp_gradient")
+        return g, loss
 
     def get_iterations(self, out_n: np.ndarray, out_s: np.ndarray):
         rc = self.lib.mdz_rheo_get_iterations(self.handle, _ptr(out_n), _ptr(out_s))
