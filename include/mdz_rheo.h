@@ -64,7 +64,8 @@ extern "C" {
 #define MDZ_SWEEP_ASYNC      0x1  /* MDZ_MEM_DEVICE only: return after enqueue; call mdz_rheo_sync */
 #define MDZ_SWEEP_WARMSTART  0x2  /* start each local Newton from the learned guess (needs weights) */
 #define MDZ_SWEEP_ITERS      0x4  /* record per-(node,phase) local iteration counts (mdz_rheo_get_iterations) */
-#define MDZ_SWEEP_POLISH     0x8  /* start each local Newton from a few FP32 Newton steps (no network) */
+#define MDZ_SWEEP_REF_START  0x8  /* start each local Newton where the reference does (see below) */
+#define MDZ_DEFAULT_POLISH   4    /* FP32 Newton steps before each FP64 local solve, by default */
 
 /* ---- per-phase material table -----------------------------------------
  * The subset of `mat_prop` (MDLIB/include/mdoodz.h:152-240) that the local
@@ -223,7 +224,14 @@ int mdz_rheo_sync(mdz_rheo_ctx *ctx, mdz_sweep_stats *stats);
 /* ---- the hot path --------------------------------------------------- */
 /* NonNewtonianViscosityGrid: vertex interpolation of T, p_in, d0, phi0, then
  * every centroid and vertex: per active phase local solve, phase averaging,
- * final stress.  `mem` is MDZ_MEM_HOST or MDZ_MEM_DEVICE; `stats` may be NULL. */
+ * final stress.  `mem` is MDZ_MEM_HOST or MDZ_MEM_DEVICE; `stats` may be NULL.
+ * Start of the local solves: the reference starts its visco-elastic Newton at the
+ * smallest isolated viscosity (RheologyDensity.c:582-592; after 10 bisection steps in
+ * the anisotropic routine, AnisotropyRoutines.c:474-497).  By default the FP64 Newton
+ * here starts after MDZ_DEFAULT_POLISH FP32 Newton steps from that point; it still
+ * iterates to the reference's residual tolerance (|r| < 1e-13 Eii), so results agree
+ * with the reference to that tolerance.  MDZ_SWEEP_REF_START starts exactly where the
+ * reference does (same iteration counts). */
 int mdz_rheo_sweep(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                    const mdz_grid_fields *f, int final_update, int mem, int flags,
                    mdz_sweep_stats *stats);
@@ -231,7 +239,8 @@ int mdz_rheo_sweep(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_material
 int mdz_rheo_sweep_aniso(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                          const mdz_grid_fields *f, int final_update, int mem, int flags,
                          mdz_sweep_stats *stats);
-/* ViscosityConcise (aniso=0) or ViscosityConciseAniso (aniso=1) on n points. */
+/* ViscosityConcise (aniso=0) or ViscosityConciseAniso (aniso=1) on n points (start of
+ * the local solves as in mdz_rheo_sweep without flags). */
 int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                     const mdz_point_inputs *in, mdz_point_outputs *out, int64_t n, int aniso,
                     int mem);
@@ -242,7 +251,9 @@ int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);
 
 /* ---- learned warm start (no reference counterpart) --------------------- */
 /* Install the network used by MDZ_SWEEP_WARMSTART (NULL removes it) and the number of
- * FP32 Newton steps taken after its guess (also used by MDZ_SWEEP_POLISH). */
+ * FP32 Newton steps taken before every FP64 local solve (after the network's guess with
+ * MDZ_SWEEP_WARMSTART, from the reference's start point otherwise; 0 = start exactly
+ * where the reference does).  The default is MDZ_DEFAULT_POLISH. */
 int mdz_rheo_set_warmstart(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, int polish_iters);
 /* A plain sweep (iso or aniso) that also records, for every (phase p, node i) item,
  * item = p * (Nc + Nv) + i (centroids first), the MDZ_MLP_IN features X[item][.] and

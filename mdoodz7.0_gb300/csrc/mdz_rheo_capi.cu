@@ -42,7 +42,7 @@ struct mdz_rheo_ctx {
   // learned warm start
   void *warm_buf = nullptr;  // tiles W1, W2, W3 + biases b1, b2, b3[16]
   MlpDevice warm{};
-  int warm_ready = 0, polish_iters = 4;
+  int warm_ready = 0, polish_iters = MDZ_DEFAULT_POLISH;
   unsigned mma_fault = 0;
 };
 
@@ -260,7 +260,6 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   int mode = -1;  // plain
   if (collect) mode = MODE_COLLECT;
   else if (flags & MDZ_SWEEP_WARMSTART) mode = MODE_WARM;
-  else if (flags & MDZ_SWEEP_POLISH) mode = MODE_POLISH;
   if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
   CK(cudaSetDevice(ctx->device));
   static thread_local SweepArgs A;  // large: keep off the stack
@@ -270,6 +269,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   for (int p = 0; p < A.M.np; p++) fold_phase(mat, md, p, A.ph[p]);
   A.final_update = final_update;
   A.need_lnd = need_lnd(mat, A.M.np);
+  A.polish = (flags & MDZ_SWEEP_REF_START) ? 0 : ctx->polish_iters;
   const size_t Nc = (size_t)A.M.Nc, Nv = (size_t)A.M.Nv;
   const int np = A.M.np;
   const bool host = (mem == MDZ_MEM_HOST);
@@ -632,6 +632,7 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
   for (int p = 0; p < A.M.np; p++) fold_phase(m, md, p, A.ph[p]);
   A.n = n;
   A.aniso = aniso;
+  A.polish = c->polish_iters;
   A.stats = c->d_stats;
   if (n == 0) return MDZ_OK;
   const bool host = (mem == MDZ_MEM_HOST);

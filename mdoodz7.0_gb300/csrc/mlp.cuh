@@ -185,38 +185,4 @@ __device__ __forceinline__ void warm_features(const ModelConst &M, const NodeIn 
   }
 }
 
-// FP32 Newton on the normalised residual from s0 = eta / eta_up.  Returns the refined s
-// (or s0 when the FP32 iteration leaves (0, 2]).
-__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, double eta_up, float s0, int iters) {
-  if (iters <= 0) return s0;
-  const float a = (float)(eta_up * q.A / q.Eii);
-  float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
-  if (q.nl) {
-    const float lp = __logf((float)(eta_up * q.inv_p));
-#pragma unroll
-    for (int k = 0; k < K_COUNT; k++)
-      if (q.nl >> k & 1) { n[k] = (float)q.n[k]; c[k] = n[k] * lp + (float)q.nc[k]; }
-  }
-  float s = s0;
-  for (int it = 0; it < iters; it++) {
-    float e = 0.f, S = 0.f;
-    if (q.nl) {
-      const float ls = __logf(s);
-#pragma unroll
-      for (int k = 0; k < K_COUNT; k++)
-        if (q.nl >> k & 1) {
-          const float ek = __expf(fmaf(n[k], ls, c[k]));
-          e += ek;
-          S = fmaf(n[k], ek, S);
-        }
-    }
-    const float r = 1.0f - a * s - e;
-    if (fabsf(r) < 1e-6f) break;
-    const float sn = s + r * s / fmaf(a, s, S);
-    if (!(sn > 0.0f && sn <= 2.0f)) return s0;
-    s = sn;
-  }
-  return s;
-}
-
 }  // namespace mdz

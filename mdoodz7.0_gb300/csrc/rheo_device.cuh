@@ -311,6 +311,43 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, VeState &s) {
   s.eta = eta;
 }
 
+// Start point of the FP64 Newton: a few FP32 Newton steps on the normalised residual
+//     r(s) = 1 - a s - sum_k exp(n_k ln s + c_k),   s = eta / eta_up,
+// every quantity O(1) (a = eta_up A / Eii, c_k = n_k ln(eta_up / eta_p) + nc_k).  The
+// FP64 iteration that follows is unchanged and runs to the same residual tolerance, so
+// these steps only move its start (to within FP32 rounding of the root).
+__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, double eta_up, float s0, int iters) {
+  if (iters <= 0) return s0;
+  const float a = (float)(eta_up * q.A / q.Eii);
+  float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
+  if (q.nl) {
+    const float lp = __logf((float)(eta_up * q.inv_p));
+#pragma unroll
+    for (int k = 0; k < K_COUNT; k++)
+      if (q.nl >> k & 1) { n[k] = (float)q.n[k]; c[k] = n[k] * lp + (float)q.nc[k]; }
+  }
+  float s = s0;
+  for (int it = 0; it < iters; it++) {
+    float e = 0.f, S = 0.f;
+    if (q.nl) {
+      const float ls = __logf(s);
+#pragma unroll
+      for (int k = 0; k < K_COUNT; k++)
+        if (q.nl >> k & 1) {
+          const float ek = __expf(fmaf(n[k], ls, c[k]));
+          e += ek;
+          S = fmaf(n[k], ek, S);
+        }
+    }
+    const float r = 1.0f - a * s - e;
+    if (fabsf(r) < 1e-6f) break;
+    const float sn = s + r * s / fmaf(a, s, S);
+    if (!(sn > 0.0f && sn <= 2.0f)) return s0;
+    s = sn;
+  }
+  return s;
+}
+
 struct GseIn {
   double Eii, eta_el, eta_cst, C_pwl, n_pwl, C_lin, n_lin, m_lin, C_exp, ST, n_exp, eta_up, eta_lo, Ag,
       gam, lam, cg, pg;
@@ -532,10 +569,12 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   S.eta_up = eta_up; S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
 
-// Local solve (from eta_start), plastic corrections and post-processing of one (node, phase).
-// eta_conv (may be null) receives the converged visco-elastic viscosity, before plasticity.
+// Local solve (from eta_start, refined by `polish` FP32 Newton steps), plastic corrections
+// and post-processing of one (node, phase).  eta_conv (may be null) receives the converged
+// visco-elastic viscosity, before plasticity.
 __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                  IsoState &S, double eta_start, PointOut &o, double *eta_conv = nullptr) {
+                                  IsoState &S, double eta_start, int polish, PointOut &o,
+                                  double *eta_conv = nullptr) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
   const int gbs = (fl & F_GBS) != 0, gs = (fl & F_GS) != 0;
@@ -552,7 +591,8 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     VeCoef q;
     ve_coef(L, c, eta_cst, q);
     VeState s;
-    s.eta = eta_start;
+    s.eta = (polish > 0) ? (double)ve_polish_f32(q, eta_up, (float)(eta_start / eta_up), polish) * eta_up
+                         : eta_start;
     s.status = MDZ_OK;
     ve_newton(q, s);
     set_status(o.status, s.status);
@@ -693,10 +733,10 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
 }
 
 __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                 double warm_eta, PointOut &o) {
+                                 int polish, PointOut &o) {
   IsoState S;
   iso_setup(M, ph, in, c, S, o);
-  iso_finish(M, ph, in, c, S, (warm_eta > 0.0) ? warm_eta : S.eta_up, o);
+  iso_finish(M, ph, in, c, S, S.eta_up, polish, o);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -771,9 +811,11 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   (void)an; (void)T; (void)K; (void)dt; (void)min_eta; (void)max_eta;
 }
 
-// Local solve from warm_eta (> 0) or the reference's bisection, plasticity, post-processing.
+// Local solve, plasticity, post-processing.  The Newton starts from the reference's
+// bisection when warm_eta <= 0 and polish == 0; otherwise from warm_eta (eta_up when
+// warm_eta <= 0) refined by `polish` FP32 Newton steps.
 __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                   const AnisoNode &an, IsoState &S, double warm_eta, PointOut &o,
+                                   const AnisoNode &an, IsoState &S, double warm_eta, int polish, PointOut &o,
                                    double *eta_conv = nullptr) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
@@ -807,8 +849,9 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     VeState s;
     s.status = MDZ_OK;
     double r, S;
-    if (warm_eta > 0.0) {
-      eta_ve = warm_eta;
+    if (warm_eta > 0.0 || polish > 0) {
+      const double start = (warm_eta > 0.0) ? warm_eta : eta_up;
+      eta_ve = (polish > 0) ? (double)ve_polish_f32(q, eta_up, (float)(start / eta_up), polish) * eta_up : start;
     } else {
       double lo = min_eta * 1.0e-3, hi = 10.0 * fmax(eta_lo, max_eta);
       for (int bit = 0; bit < 10; bit++) {
@@ -892,10 +935,10 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
 }
 
 __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                   const AnisoNode &an, double warm_eta, PointOut &o) {
+                                   const AnisoNode &an, int polish, PointOut &o) {
   IsoState S;
   aniso_setup(M, ph, in, c, an, S, o);
-  aniso_finish(M, ph, in, c, an, S, warm_eta, o);
+  aniso_finish(M, ph, in, c, an, S, 0.0, polish, o);
 }
 
 // EffectiveStrainRate, RheologyDensity.c:116-146

@@ -10,8 +10,8 @@
 // k_sweep_tiles<ANISO, MODE> walks the same index space in tiles of 128 nodes, one tile
 // per CTA at a time, with the phase loop uniform over the CTA so that a block-wide stage
 // can sit between each phase's set-up and its local solve: the learned warm start
-// (MODE_WARM: tcgen05 MLP + FP32 polish), the FP32 polish alone (MODE_POLISH), or the
-// training-data dump (MODE_COLLECT).
+// (MODE_WARM: tcgen05 MLP guess, then the FP32 polish) or the training-data dump
+// (MODE_COLLECT, from the reference's own start).
 #include <cuda_runtime.h>
 
 #include "mlp.cuh"
@@ -248,8 +248,8 @@ __global__ void __launch_bounds__(128) k_sweep(const __grid_constant__ SweepArgs
           continue;
         }
         PointOut o;
-        if (ANISO) point_aniso(A.M, A.ph[p], n.in, n.ctx, n.an, 0.0, o);
-        else point_iso(A.M, A.ph[p], n.in, n.ctx, 0.0, o);
+        if (ANISO) point_aniso(A.M, A.ph[p], n.in, n.ctx, n.an, A.polish, o);
+        else point_iso(A.M, A.ph[p], n.in, n.ctx, A.polish, o);
         node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
       }
     }
@@ -306,21 +306,14 @@ __global__ void __launch_bounds__(128) k_sweep_tiles(const __grid_constant__ Swe
         mlp_forward(S, x, y, phase);
         if (active && !S.fault) {
           const float z = fmaxf(y[0] * W.mlp.z_scale + W.mlp.z_shift, 0.0f);
-          VeCoef q;
-          ve_coef(st.L, n.ctx, st.eta_cst, q);
-          eta_start = (double)ve_polish_f32(q, st.eta_up, __expf(-z), W.mlp.polish_iters) * st.eta_up;
-        }
-      } else if (MODE == MODE_POLISH) {
-        if (active) {
-          VeCoef q;
-          ve_coef(st.L, n.ctx, st.eta_cst, q);
-          eta_start = (double)ve_polish_f32(q, st.eta_up, 1.0f, W.mlp.polish_iters) * st.eta_up;
+          eta_start = (double)__expf(-z) * st.eta_up;
         }
       }
       if (!active) continue;
       double eta_conv = 0.0;
-      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, eta_start, o, &eta_conv);
-      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, eta_start > 0.0 ? eta_start : st.eta_up, o, &eta_conv);
+      const int polish = (MODE == MODE_WARM) ? W.mlp.polish_iters : 0;
+      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, eta_start, polish, o, &eta_conv);
+      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, eta_start > 0.0 ? eta_start : st.eta_up, polish, o, &eta_conv);
       node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
       if (MODE == MODE_COLLECT) {
         const long long item = (long long)p * total + i;
@@ -352,7 +345,12 @@ __global__ void __launch_bounds__(128) k_sweep_tiles(const __grid_constant__ Swe
 __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArgs A) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Acc acc = {0, 0, 0, 0};
-  if (i < A.n) {
+  const bool bad_phase = (i < A.n) && (A.in.phase[i] < 0 || A.in.phase[i] >= A.M.np);
+  if (bad_phase) {  // phase ids in device memory are only checked here
+    if (A.out.status) A.out.status[i] = MDZ_EINVAL;
+    record_error(A.stats, i, MDZ_EINVAL);
+  }
+  if (i < A.n && !bad_phase) {
     const mdz_point_inputs &I = A.in;
     NodeIn in;
     in.Exx = I.Exx[i]; in.Ezz = I.Ezz[i]; in.Exz = I.Exz[i];
@@ -368,10 +366,10 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArg
       in.lxlz = I.lxlz[i]; in.lx2 = I.lx2[i]; in.ani_fac = I.ani_fac[i];
       AnisoNode an;
       node_setup_aniso(A.M, in, true, ctx, an);
-      point_aniso(A.M, A.ph[p], in, ctx, an, 0.0, o);
+      point_aniso(A.M, A.ph[p], in, ctx, an, A.polish, o);
     } else {
       node_setup_iso(A.M, in, true, ctx);
-      point_iso(A.M, A.ph[p], in, ctx, 0.0, o);
+      point_iso(A.M, A.ph[p], in, ctx, A.polish, o);
     }
     const mdz_point_outputs &O = A.out;
     double *dst[24] = {O.eta, O.Txx, O.Tzz, O.Txz, O.etaVE, O.VEcoeff, O.Eii_el, O.Eii_pl, O.Eii_pwl, O.Eii_exp,
@@ -418,8 +416,6 @@ cudaError_t launch_sweep_tiles(const SweepArgs &a, const WarmArgs &w, bool aniso
     case MODE_COLLECT * 2 + 1: return launch_tiles_t<true, MODE_COLLECT>(a, w, s, grid);
     case MODE_WARM * 2: return launch_tiles_t<false, MODE_WARM>(a, w, s, grid);
     case MODE_WARM * 2 + 1: return launch_tiles_t<true, MODE_WARM>(a, w, s, grid);
-    case MODE_POLISH * 2: return launch_tiles_t<false, MODE_POLISH>(a, w, s, grid);
-    case MODE_POLISH * 2 + 1: return launch_tiles_t<true, MODE_POLISH>(a, w, s, grid);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -431,9 +427,7 @@ int tiles_blocks_per_sm(bool aniso, int mode) {
     case MODE_COLLECT * 2: fn = (const void *)k_sweep_tiles<false, MODE_COLLECT>; break;
     case MODE_COLLECT * 2 + 1: fn = (const void *)k_sweep_tiles<true, MODE_COLLECT>; break;
     case MODE_WARM * 2: fn = (const void *)k_sweep_tiles<false, MODE_WARM>; break;
-    case MODE_WARM * 2 + 1: fn = (const void *)k_sweep_tiles<true, MODE_WARM>; break;
-    case MODE_POLISH * 2: fn = (const void *)k_sweep_tiles<false, MODE_POLISH>; break;
-    default: fn = (const void *)k_sweep_tiles<true, MODE_POLISH>; break;
+    default: fn = (const void *)k_sweep_tiles<true, MODE_WARM>; break;
   }
   const size_t smem = (mode == MODE_WARM) ? sizeof(MlpShared) : 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kMlpTile, smem);

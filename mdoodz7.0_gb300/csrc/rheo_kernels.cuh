@@ -27,7 +27,7 @@ struct DevStats {
 };
 
 // modes of the tiled sweep
-enum { MODE_COLLECT = 0, MODE_WARM = 1, MODE_POLISH = 2 };
+enum { MODE_COLLECT = 0, MODE_WARM = 1 };
 
 struct WarmArgs {
   MlpDevice mlp;
@@ -51,6 +51,7 @@ struct SweepArgs {
   int32_t *iters_n, *iters_s;  // optional [p*N + node]
   DevStats *stats;
   int final_update, need_lnd;
+  int polish;  // FP32 Newton steps before each FP64 local solve (0: the reference's start)
 };
 
 struct PointArgs {
@@ -60,6 +61,7 @@ struct PointArgs {
   mdz_point_outputs out;
   long long n;
   int aniso;
+  int polish;  // as in SweepArgs
   DevStats *stats;
 };
 

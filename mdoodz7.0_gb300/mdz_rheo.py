@@ -47,7 +47,8 @@ MEM_DEVICE = 1
 SWEEP_ASYNC = 0x1
 SWEEP_WARMSTART = 0x2
 SWEEP_ITERS = 0x4
-SWEEP_POLISH = 0x8
+SWEEP_REF_START = 0x8
+DEFAULT_POLISH = 4
 
 # ---- struct layouts (must follow include/mdz_rheo.h field by field) -------
 MAT_INT = ["cstv", "pwlv", "linv", "gbsv", "expv", "gs", "kin", "plast", "density_model",

@@ -125,8 +125,8 @@ def main(argv: Optional[List[str]] = None):
     wl = (W.aniso(seed=args.eval_seed, ncx=args.eval_ncx) if args.aniso
           else W.plain_large(seed=args.eval_seed, ncx=args.eval_ncx))
     ctx.set_warmstart(wts, args.polish)
-    report["plain"] = iterations(ctx, wl, 0, args.aniso)
-    report["polish_only"] = iterations(ctx, wl, R.SWEEP_POLISH, args.aniso)
+    report["reference_start"] = iterations(ctx, wl, R.SWEEP_REF_START, args.aniso)
+    report["polish_only"] = iterations(ctx, wl, 0, args.aniso)
     report["warm"] = iterations(ctx, wl, R.SWEEP_WARMSTART, args.aniso)
     print(json.dumps(report))
     ctx.close()

@@ -48,10 +48,14 @@ CASES = {
 }
 
 
+START = {"polished_start": 0, "reference_start": R.SWEEP_REF_START}
+
+
+@pytest.mark.parametrize("start", list(START))
 @pytest.mark.parametrize("name", list(CASES))
-def test_sweep_matches_oracle(ctx, name):
+def test_sweep_matches_oracle(ctx, name, start):
     w = CASES[name]()
-    rc, st, g, rc2, st2, c = run_pair(ctx, w)
+    rc, st, g, rc2, st2, c = run_pair(ctx, w, flags=START[start])
     assert rc == rc2 == R.MDZ_OK
     assert st.phase_calls == st2.phase_calls
     check_close(g, c, name, w)
@@ -94,7 +98,7 @@ def test_iteration_counts_match(ctx):
     w = W.plain_large(seed=13, ncx=96)
     np_ = w.mat.Nb_phases
     g = clone(w.arrays)
-    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(g), flags=R.SWEEP_ITERS)
+    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(g), flags=R.SWEEP_ITERS | R.SWEEP_REF_START)
     itg_n = np.zeros(np_ * w.Nc, np.int32)
     itg_s = np.zeros(np_ * w.Nv, np.int32)
     ctx.get_iterations(itg_n, itg_s)
@@ -137,9 +141,10 @@ def test_error_status_grain_size_zero(ctx):
     assert rc == rc2 and st.error_node == st2.error_node
 
 
-def test_aniso_sweep_matches_oracle(ctx):
+@pytest.mark.parametrize("start", list(START))
+def test_aniso_sweep_matches_oracle(ctx, start):
     w = W.aniso(seed=4, ncx=96)
-    rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True)
+    rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True, flags=START[start])
     assert rc == rc2 == R.MDZ_OK
     check_close(g, c, "aniso", w)
 

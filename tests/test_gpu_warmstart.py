@@ -113,15 +113,16 @@ def test_training_fits_a_smooth_target(ctx):
     acc = np.mean((Yp[:, 1] > 0.5) == (Yt[:, 1] > 0.5))
     print("held-out normalised rmse", z_rmse, "plastic accuracy", acc)
     assert z_rmse < 0.3 and acc > 0.9
-    # the same seed gives the same initialisation, the same order and the same weights
+    # the same seed gives the same initialisation and sample order; the gradient sums are
+    # FP32 atomics in arrival order, so two runs agree closely but not bit for bit
     w2, loss2 = ctx.train_mlp(X, Y, 10, cfg)
-    assert np.allclose(loss, loss2, rtol=1e-3)
+    assert np.allclose(loss, loss2, rtol=2e-2)
 
 
 def test_collecting_sweep_is_the_plain_sweep(ctx):
     w = W.plain_large(seed=21, ncx=64, ncz=48)
     a, b = clone(w.arrays), clone(w.arrays)
-    ctx.sweep(w.model, w.mat, R.FieldSet(a))
+    ctx.sweep(w.model, w.mat, R.FieldSet(a), flags=R.SWEEP_REF_START)
     items = w.mat.Nb_phases * w.nodes
     X = np.empty((items, R.MLP_IN), np.float32)
     Y = np.empty((items, 2), np.float32)
@@ -161,7 +162,7 @@ def check_close(g, c, label, w):
     assert not bad, f"{label}: fields above {RTOL}: {bad}"
 
 
-@pytest.mark.parametrize("flags", [R.SWEEP_WARMSTART, R.SWEEP_POLISH])
+@pytest.mark.parametrize("flags", [R.SWEEP_WARMSTART, 0])
 def test_warm_sweep_matches_oracle(ctx, trained_iso, flags):
     ctx.set_warmstart(trained_iso, 4)
     w = W.plain_large(seed=1, ncx=129)
@@ -174,10 +175,10 @@ def test_warm_sweep_matches_oracle(ctx, trained_iso, flags):
 def test_warm_start_saves_newton_iterations(ctx, trained_iso):
     ctx.set_warmstart(trained_iso, 4)
     w = W.plain_large(seed=1, ncx=257)
-    plain = WS.iterations(ctx, w, 0)
-    polish = WS.iterations(ctx, w, R.SWEEP_POLISH)
+    plain = WS.iterations(ctx, w, R.SWEEP_REF_START)
+    polish = WS.iterations(ctx, w, 0)
     warm = WS.iterations(ctx, w, R.SWEEP_WARMSTART)
-    print("mean Newton iterations: plain", plain, "polish", polish, "warm", warm)
+    print("mean Newton iterations: reference start", plain, "FP32 polish", polish, "network + polish", warm)
     assert warm["phase_calls"] == plain["phase_calls"]
     assert warm["mean_iters"] < 0.8 * plain["mean_iters"]
     assert warm["mean_iters"] <= polish["mean_iters"]
@@ -191,9 +192,10 @@ def test_aniso_warm_sweep_matches_oracle(ctx):
     rc, st, g, rc2, st2, c = run_pair(ctx, w, R.SWEEP_WARMSTART, aniso=True)
     assert rc == rc2 == R.MDZ_OK and st.mma_fault == 0
     check_close(g, c, "aniso warm", w)
-    plain = WS.iterations(ctx, w, 0, aniso=True)
+    plain = WS.iterations(ctx, w, R.SWEEP_REF_START, aniso=True)
+    polish = WS.iterations(ctx, w, 0, aniso=True)
     warm = WS.iterations(ctx, w, R.SWEEP_WARMSTART, aniso=True)
-    print("aniso mean Newton iterations: plain", plain, "warm", warm)
+    print("aniso mean Newton iterations: reference start", plain, "FP32 polish", polish, "network + polish", warm)
     assert warm["mean_iters"] <= plain["mean_iters"]
 
 
