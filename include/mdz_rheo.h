@@ -285,6 +285,11 @@ int mdz_rheo_mlp_predict(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, const floa
  * loop timed with CUDA events).  The roofline of this FP64-bound path is
  * reported against it.  No reference counterpart. */
 int mdz_rheo_measure_fp64_peak(int device, double *tflops);
+/* Self-check of the device math: for n host arguments x, the table-driven exp and log
+ * used on the hot path and CUDA's own exp and log, each into its host array.  No
+ * reference counterpart. */
+int mdz_rheo_math_selftest(int device, const double *x, int64_t n, double *fast_exp_out,
+                           double *cuda_exp_out, double *fast_log_out, double *cuda_log_out);
 
 #ifdef __cplusplus
 }

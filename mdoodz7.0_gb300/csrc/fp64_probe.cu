@@ -1,12 +1,15 @@
-// fp64_probe.cu -- measured FP64 (DFMA) throughput of the current GPU.
+// fp64_probe.cu -- measurement and self-check helpers.
 //
-// The local rheology update is bound by the FP64 pipe, and the generated peak
-// file holds no FP64 figure, so roofline fractions are reported against this
-// measured rate: every thread of a full-occupancy grid runs independent chains of
-// dependent DFMAs (2 flops each), timed with CUDA events.
+// mdz_rheo_measure_fp64_peak: the local rheology update is bound by the FP64 pipe,
+// so roofline fractions are reported against a measured FP64 rate: every thread of a
+// full-occupancy grid runs independent chains of dependent DFMAs (2 flops each),
+// timed with CUDA events.
+// mdz_rheo_math_selftest: the table-driven exp/log of fp64_math.cuh next to CUDA's
+// exp/log on the same arguments, for the accuracy tests.
 #include <cuda_runtime.h>
 
 #include "../../include/mdz_rheo.h"
+#include "fp64_math.cuh"
 
 namespace {
 
@@ -26,7 +29,38 @@ __global__ void __launch_bounds__(256) k_dfma(double *out, double a, double b, i
   if (s == 12345.678) out[0] = s;  // keep the chains live
 }
 
+__global__ void k_math(const double *x, long long n, double *fe, double *ce, double *fl, double *cl) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = x[i];
+  fe[i] = mdz::fast_exp(v);
+  ce[i] = exp(v);
+  fl[i] = mdz::fast_log(v);
+  cl[i] = log(v);
+}
+
 }  // namespace
+
+extern "C" int mdz_rheo_math_selftest(int device, const double *x, int64_t n, double *fast_exp_out,
+                                      double *cuda_exp_out, double *fast_log_out, double *cuda_log_out) {
+  if (!x || n < 0 || !fast_exp_out || !cuda_exp_out || !fast_log_out || !cuda_log_out) return MDZ_EINVAL;
+  if (n == 0) return MDZ_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return MDZ_ECUDA;
+  const size_t b = (size_t)n * sizeof(double);
+  double *d = nullptr;
+  if (cudaMalloc(&d, 5 * b) != cudaSuccess) return MDZ_ENOMEM;
+  int rc = MDZ_OK;
+  if (cudaMemcpy(d, x, b, cudaMemcpyHostToDevice) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK) {
+    k_math<<<(unsigned)((n + 255) / 256), 256>>>(d, n, d + n, d + 2 * n, d + 3 * n, d + 4 * n);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = MDZ_ECUDA;
+  }
+  double *outs[4] = {fast_exp_out, cuda_exp_out, fast_log_out, cuda_log_out};
+  for (int k = 0; k < 4 && rc == MDZ_OK; k++)
+    if (cudaMemcpy(outs[k], d + (k + 1) * n, b, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
+  cudaFree(d);
+  return rc;
+}
 
 extern "C" int mdz_rheo_measure_fp64_peak(int device, double *tflops) {
   if (!tflops) return MDZ_EINVAL;

@@ -1,0 +1,172 @@
+/*
+ * mdz_rheo_mdoodz.c -- the MDOODZ7.0-side drop-in: NonNewtonianViscosityGrid and
+ * NonNewtonianViscosityGridAniso with the reference's own signatures
+ * (MDLIB/mdoodz-private.h:423 and :437), evaluated on the GPU by
+ * libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
+ *
+ * It is compiled inside the MDOODZ build, against MDLIB/mdoodz-private.h, in place of
+ * the two definitions at MDLIB/RheologyDensity.c:1131 and
+ * MDLIB/AnisotropyRoutines.c:885 (those are compiled out under MDZ_RHEO_GB300).
+ * Each call unpacks `grid`, `mat_prop`, `params` and `scale` into the library's
+ * plain-pointer structs and runs one sweep on host memory: the library uploads the
+ * inputs, runs the kernel and writes every output back into the caller's arrays in
+ * place, as the reference does (including the vertex fields T_s, P_s, d0_s, phi0_s).
+ *
+ * Errors: where the reference logs and calls exit() from inside the local solve,
+ * the library returns a status; this file logs the reference's message for it and
+ * exits with the reference's code (RheologyDensity.c:175-177, :312-315, :839-841,
+ * :1045-1050, :1274-1301; AnisotropyRoutines.c:543, :580-583).
+ *
+ * One library context per process, created on first use on the device named by the
+ * environment variable MDZ_RHEO_DEVICE (default 0).  Like the reference, the calls
+ * are blocking and are made from one host thread.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "mdoodz-private.h"
+#include "mdz_rheo.h"
+
+static mdz_rheo_ctx *s_ctx = NULL;
+
+static mdz_rheo_ctx *mdz_context(void) {
+  if (s_ctx == NULL) {
+    const char *dev = getenv("MDZ_RHEO_DEVICE");
+    const int rc = mdz_rheo_create(dev ? atoi(dev) : 0, &s_ctx);
+    if (rc != MDZ_OK) {
+      fprintf(stderr, "GB300 rheology: cannot open the device context (%s)\n", mdz_rheo_status_string(rc));
+      exit(1);
+    }
+  }
+  return s_ctx;
+}
+
+static void mdz_model_from(mdz_model *md, const grid *mesh, const params *model, const scale *scaling) {
+  memset(md, 0, sizeof(*md));
+  md->Nx = mesh->Nx;
+  md->Nz = mesh->Nz;
+  md->Nb_phases = model->Nb_phases;
+  md->step = model->step;
+  md->elastic = model->elastic;
+  md->eta_average = model->eta_average;
+  md->periodic_x = model->periodic_x;
+  md->density_variations = model->density_variations;
+  md->tensile_line_search = model->tensile_line_search;
+  md->melting = model->melting;
+  md->chemical_production = model->chemical_production;
+  md->diffuse_X = model->diffuse_X;
+  md->diffuse_avg = model->diffuse_avg;
+  md->dt = model->dt;
+  md->min_eta = model->min_eta;
+  md->max_eta = model->max_eta;
+  md->eta_tol = model->eta_tol;
+  md->scale_eta = scaling->eta;
+  md->scale_L = scaling->L;
+  md->scale_T = scaling->T;
+  md->scale_S = scaling->S;
+  md->scale_E = scaling->E;
+}
+
+static void mdz_materials_from(mdz_materials *m, const mat_prop *mp) {
+  memset(m, 0, sizeof(*m));
+  m->Nb_phases = mp->Nb_phases;
+  m->R = mp->R;
+  for (int p = 0; p < MDZ_MAX_PHASES; p++) {
+#define MDZ_COPY(name) m->name[p] = mp->name[p]
+    MDZ_COPY(cstv); MDZ_COPY(pwlv); MDZ_COPY(linv); MDZ_COPY(gbsv); MDZ_COPY(expv); MDZ_COPY(gs);
+    MDZ_COPY(kin); MDZ_COPY(plast); MDZ_COPY(density_model); MDZ_COPY(phase_mix); MDZ_COPY(phase_two);
+    MDZ_COPY(reac_soft); MDZ_COPY(reac_phase); MDZ_COPY(melt);
+    MDZ_COPY(eta0); MDZ_COPY(rho); MDZ_COPY(drho); MDZ_COPY(alp); MDZ_COPY(bet); MDZ_COPY(T0);
+    MDZ_COPY(P0); MDZ_COPY(Slim); MDZ_COPY(eta_vp); MDZ_COPY(n_vp); MDZ_COPY(T_st); MDZ_COPY(gs_ref);
+    MDZ_COPY(Qpwl); MDZ_COPY(Vpwl); MDZ_COPY(npwl); MDZ_COPY(mpwl); MDZ_COPY(rpwl); MDZ_COPY(Apwl);
+    MDZ_COPY(fpwl); MDZ_COPY(apwl); MDZ_COPY(Fpwl); MDZ_COPY(pref_pwl);
+    MDZ_COPY(Qlin); MDZ_COPY(Vlin); MDZ_COPY(nlin); MDZ_COPY(mlin); MDZ_COPY(rlin); MDZ_COPY(Alin);
+    MDZ_COPY(flin); MDZ_COPY(alin); MDZ_COPY(Flin);
+    MDZ_COPY(Qgbs); MDZ_COPY(Vgbs); MDZ_COPY(ngbs); MDZ_COPY(mgbs); MDZ_COPY(rgbs); MDZ_COPY(Agbs);
+    MDZ_COPY(fgbs); MDZ_COPY(agbs); MDZ_COPY(Fgbs);
+    MDZ_COPY(Qexp); MDZ_COPY(Sexp); MDZ_COPY(Eexp); MDZ_COPY(Gexp); MDZ_COPY(nexp);
+    MDZ_COPY(Kpzm); MDZ_COPY(Qpzm); MDZ_COPY(Gpzm); MDZ_COPY(Lpzm); MDZ_COPY(cpzm); MDZ_COPY(ppzm);
+#undef MDZ_COPY
+  }
+}
+
+static void mdz_fields_from(mdz_grid_fields *f, grid *g, int aniso) {
+  memset(f, 0, sizeof(*f));
+  /* centroid inputs */
+  f->mu_n = g->mu_n; f->T = g->T; f->p_in = g->p_in; f->d0_n = g->d0_n; f->phi0_n = g->phi0_n;
+  f->X0_n = g->X0_n; f->exxd = g->exxd; f->ezzd = g->ezzd; f->exz_n = g->exz_n; f->sxxd0 = g->sxxd0;
+  f->szzd0 = g->szzd0; f->sxz0_n = g->sxz0_n; f->strain_n = g->strain_n; f->dil_n = g->dil_n;
+  f->fric_n = g->fric_n; f->C_n = g->C_n; f->p0_n = g->p0_n; f->T0_n = g->T0_n; f->bet_n = g->bet_n;
+  f->div_u = g->div_u;
+  f->phase_perc_n = (const double *const *)g->phase_perc_n;
+  f->BCp_type = g->BCp.type;
+  /* vertex inputs */
+  f->mu_s = g->mu_s; f->X0_s = g->X0_s; f->exxd_s = g->exxd_s; f->ezzd_s = g->ezzd_s; f->exz = g->exz;
+  f->sxxd0_s = g->sxxd0_s; f->szzd0_s = g->szzd0_s; f->sxz0 = g->sxz0; f->strain_s = g->strain_s;
+  f->dil_s = g->dil_s; f->fric_s = g->fric_s; f->C_s = g->C_s; f->p0_s = g->p0_s; f->bet_s = g->bet_s;
+  f->div_u_s = g->div_u_s;
+  f->phase_perc_s = (const double *const *)g->phase_perc_s;
+  f->BCg_type = g->BCg.type;
+  if (aniso) {
+    f->d1_n = g->d1_n; f->d2_n = g->d2_n; f->angle_n = g->angle_n; f->aniso_factor_n = g->aniso_factor_n;
+    f->d1_s = g->d1_s; f->d2_s = g->d2_s; f->angle_s = g->angle_s; f->aniso_factor_s = g->aniso_factor_s;
+  }
+  /* written: interpolated vertex fields and outputs */
+  f->T_s = g->T_s; f->P_s = g->P_s; f->d0_s = g->d0_s; f->phi0_s = g->phi0_s;
+  f->eta_n = g->eta_n; f->eta_phys_n = g->eta_phys_n; f->VE_n = g->VE_n; f->sxxd = g->sxxd;
+  f->szzd = g->szzd; f->sxz_n = g->sxz_n; f->eII_el = g->eII_el; f->eII_pl = g->eII_pl;
+  f->eII_pwl = g->eII_pwl; f->eII_exp = g->eII_exp; f->eII_lin = g->eII_lin; f->eII_gbs = g->eII_gbs;
+  f->eII_cst = g->eII_cst; f->d_n = g->d_n; f->p_corr = g->p_corr; f->div_u_el = g->div_u_el;
+  f->div_u_pl = g->div_u_pl; f->div_u_r = g->div_u_r; f->Wtot = g->Wtot; f->Wel = g->Wel;
+  f->Wdiss = g->Wdiss; f->X_n = g->X_n; f->OverS_n = g->OverS_n; f->rho_n = g->rho_n;
+  f->phase_eta_n = (double *const *)g->phase_eta_n;
+  f->sxxd_s = g->sxxd_s; f->szzd_s = g->szzd_s; f->sxz = g->sxz; f->eta_phys_s = g->eta_phys_s;
+  f->eta_s = g->eta_s; f->X_s = g->X_s; f->VE_s = aniso ? g->VE_s : NULL;
+  f->phase_eta_s = (double *const *)g->phase_eta_s;
+}
+
+/* The reference's message and exit code for a failed sweep. */
+static void mdz_fail(int rc, const mdz_sweep_stats *st) {
+  int code = 1;
+  const char *msg = mdz_rheo_status_string(rc);
+  switch (rc) {
+    case MDZ_EVE_ITER: msg = "Visco-Elastic iterations failed!"; code = 0; break;   /* :175-177 */
+    case MDZ_EGSE_ITER: code = 346; break;                                         /* :312-315, :366-368 */
+    case MDZ_EEMPTY_CELL: msg = "Cell went empty!!! Exiting..."; code = 345; break; /* :1274-1277 */
+    case MDZ_ELINESEARCH: code = 0; break;                                         /* :868-872 */
+    case MDZ_EANISO_ITER: code = 0; break;                                         /* Aniso :580-583 */
+    default: code = 1; break;
+  }
+  fprintf(stderr, "%s (node %lld)\n", msg, (long long)st->error_node);
+  exit(code);
+}
+
+static void mdz_sweep_grid(grid *mesh, mat_prop *materials, params *model, scale *scaling, int final_update,
+                           int aniso) {
+  mdz_model md;
+  mdz_materials mt;
+  mdz_grid_fields f;
+  mdz_sweep_stats st;
+  mdz_model_from(&md, mesh, model, scaling);
+  mdz_materials_from(&mt, materials);
+  mdz_fields_from(&f, mesh, aniso);
+  memset(&st, 0, sizeof(st));
+  const int rc = aniso ? mdz_rheo_sweep_aniso(mdz_context(), &md, &mt, &f, final_update, MDZ_MEM_HOST, 0, &st)
+                       : mdz_rheo_sweep(mdz_context(), &md, &mt, &f, final_update, MDZ_MEM_HOST, 0, &st);
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
+}
+
+void NonNewtonianViscosityGrid(grid *mesh, mat_prop *materials, params *model, Nparams Nmodel, scale *scaling,
+                               int final_update) {
+  (void)Nmodel; /* passed by value and unused, as in the reference */
+  mdz_sweep_grid(mesh, materials, model, scaling, final_update, 0);
+  ApplySetGridDensityOverride(mesh, model); /* RheologyDensity.c:1425 */
+}
+
+void NonNewtonianViscosityGridAniso(grid *mesh, mat_prop *materials, params *model, Nparams Nmodel,
+                                    scale *scaling, int final_update) {
+  (void)Nmodel;
+  mdz_sweep_grid(mesh, materials, model, scaling, final_update, 1);
+  ApplySetGridDensityOverride(mesh, model); /* AnisotropyRoutines.c:1216 */
+}

@@ -260,6 +260,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_get_iterations.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_abi_sizes.argtypes = [C.POINTER(C.c_size_t)]
     lib.mdz_rheo_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    lib.mdz_rheo_math_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64] + [C.c_void_p] * 4
     lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
     lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SweepStats)]
@@ -295,6 +296,16 @@ def measure_fp64_peak(device: int = 0) -> float:
     if rc != MDZ_OK:
         raise RheoError(rc, "mdz_rheo_measure_fp64_peak")
     return v.value
+
+
+def math_selftest(x: np.ndarray, device: int = 0):
+    """(fast_exp, cuda_exp, fast_log, cuda_log) of the float64 array x on the GPU."""
+    x = np.ascontiguousarray(x, np.float64)
+    outs = [np.empty_like(x) for _ in range(4)]
+    rc = load_library().mdz_rheo_math_selftest(device, x.ctypes.data, x.size, *[o.ctypes.data for o in outs])
+    if rc != MDZ_OK:
+        raise RheoError(rc, "mdz_rheo_math_selftest")
+    return outs
 
 
 def python_struct_sizes():

@@ -6,7 +6,9 @@ CPU-baseline leg of bench.py, as the checker.  Two libraries can be loaded:
   * build/librheo_oracle.so -- the C restatement (rheo_oracle.c), built on any
     host by `make -C oracle`;
   * _ref/libmdz_ref.so      -- MDOODZ7.0's own sources plus ref_harness.c,
-    built by `make -C oracle ref` where the reference tree is present.
+    built by `make -C oracle ref` where the reference tree is present;
+  * _ref/libmdz_shimtest.so -- the MDOODZ-side drop-in (host/mdz_rheo_mdoodz.c)
+    over a CPU backend, beside the reference's own sweep (`make -C oracle shim`).
 
 Both take the same plain-pointer structs as the GPU library (include/mdz_rheo.h).
 """
@@ -24,6 +26,7 @@ import mdz_rheo as R  # noqa: E402
 
 ORACLE_SO = os.path.join(HERE, "build", "librheo_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmdz_ref.so")
+SHIM_SO = os.path.join(HERE, "_ref", "libmdz_shimtest.so")
 REF_TREE = os.environ.get("MDZ_REFERENCE_TREE", "/root/reference")
 
 
@@ -31,7 +34,7 @@ def build(ref: bool = False, quiet: bool = True):
     """Build the restatement (and, when asked and the reference tree exists, _ref)."""
     targets = ["all"]
     if ref and os.path.isdir(os.path.join(REF_TREE, "MDLIB")):
-        targets.append("ref")
+        targets += ["ref", "shim"]
     out = subprocess.run(["make", "-C", HERE, f"REF={REF_TREE}", "-j8"] + targets,
                          capture_output=True, text=True)
     if out.returncode != 0:
@@ -103,6 +106,30 @@ def ref_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False):
     if lib is None:
         raise RuntimeError("reference library not built (oracle/_ref)")
     return lib.ref_sweep(C.byref(model), C.byref(mat), C.byref(fs.struct), final_update, int(aniso))
+
+
+_shim = None
+
+
+def shimtest():
+    """The drop-in check library, or None where it was not built."""
+    global _shim
+    if _shim is None and os.path.exists(SHIM_SO):
+        lib = C.CDLL(SHIM_SO)
+        for name in ("shimtest_ref_sweep", "shimtest_shim_sweep"):
+            fn = getattr(lib, name)
+            fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields), C.c_int, C.c_int]
+            fn.restype = C.c_int
+        _shim = lib
+    return _shim
+
+
+def shim_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False, drop_in=True):
+    """NonNewtonianViscosityGrid(Aniso) on a harness-built `grid`: the drop-in's
+    (drop_in=True) or the reference's own."""
+    lib = shimtest()
+    fn = lib.shimtest_shim_sweep if drop_in else lib.shimtest_ref_sweep
+    return fn(C.byref(model), C.byref(mat), C.byref(fs.struct), final_update, int(aniso))
 
 
 def orc_points(model, mat, pin, pout, n, aniso=0):

@@ -1,0 +1,47 @@
+/*
+ * shim_backend.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A CPU stand-in for the context and sweep entry points of libmdz_rheo_gb300.so
+ * (include/mdz_rheo.h) that forwards every sweep to the C restatement
+ * (rheo_oracle.c).  Linked with the MDOODZ-side drop-in
+ * (mdoodz7.0_gb300/host/mdz_rheo_mdoodz.c) and with the reference's own sources
+ * into oracle/_ref/libmdz_shimtest.so, it lets a CPU test run the drop-in's
+ * NonNewtonianViscosityGrid(Aniso) on a real `grid` and compare it with the
+ * reference's, which checks how the drop-in unpacks grid / mat_prop / params /
+ * scale.  The GPU library itself is never part of this build.
+ */
+#include <stdlib.h>
+
+#include "../include/mdz_rheo.h"
+#include "rheo_oracle.h"
+
+struct mdz_rheo_ctx {
+  int device;
+};
+
+int mdz_rheo_create(int device, mdz_rheo_ctx **out) {
+  if (!out) return MDZ_EINVAL;
+  *out = (mdz_rheo_ctx *)calloc(1, sizeof(mdz_rheo_ctx));
+  if (!*out) return MDZ_ENOMEM;
+  (*out)->device = device;
+  return MDZ_OK;
+}
+
+int mdz_rheo_destroy(mdz_rheo_ctx *ctx) {
+  free(ctx);
+  return MDZ_OK;
+}
+
+const char *mdz_rheo_status_string(int status) { return status == MDZ_OK ? "ok" : "error"; }
+
+int mdz_rheo_sweep(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat, const mdz_grid_fields *f,
+                   int final_update, int mem, int flags, mdz_sweep_stats *stats) {
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_sweep(model, mat, f, final_update, NULL, NULL, stats);
+}
+
+int mdz_rheo_sweep_aniso(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                         const mdz_grid_fields *f, int final_update, int mem, int flags, mdz_sweep_stats *stats) {
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_sweep_aniso(model, mat, f, final_update, NULL, NULL, stats);
+}

@@ -1,0 +1,52 @@
+"""Accuracy of the table-driven FP64 exp and log of the hot path (P. T. P. Tang's
+methods, csrc/fp64_math.cuh) against CUDA's exp/log on the same GPU and against
+numpy (glibc), over the argument ranges the rheology reaches and the special values."""
+import numpy as np
+import pytest
+
+import mdz_rheo as R
+
+pytestmark = pytest.mark.gpu
+
+
+def ulps(a, b):
+    """|a - b| in units of the last place of b (float64)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    sp = np.spacing(np.abs(b))
+    return np.where(a == b, 0.0, np.abs(a - b) / sp)
+
+
+def test_exp_accuracy():
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(-700, 700, 400_000), rng.uniform(-1, 1, 200_000),
+                        rng.uniform(-1e-8, 1e-8, 50_000), np.linspace(-745, 709.7, 10_001),
+                        [0.0, -0.0, 1e-300, -1e-300, 700.0, -700.0, 709.78, -745.2, 710.0, -746.0,
+                         np.inf, -np.inf, np.nan]])
+    fe, ce, _, _ = R.math_selftest(x)
+    fin = np.isfinite(ce) & (ce > 1e-300)
+    u_cuda = ulps(fe[fin], ce[fin])
+    u_np = ulps(fe[fin], np.exp(x[fin]))
+    print("exp: max ulp vs CUDA", u_cuda.max(), "vs numpy", u_np.max(), "mean", u_np.mean())
+    assert u_cuda.max() <= 2.0 and u_np.max() <= 2.0
+    special = ~fin
+    assert np.array_equal(fe[special], ce[special], equal_nan=True)
+
+
+def test_log_accuracy():
+    rng = np.random.default_rng(1)
+    x = np.concatenate([10.0 ** rng.uniform(-300, 300, 400_000), rng.uniform(0.5, 2.0, 200_000),
+                        1.0 + rng.uniform(-1e-6, 1e-6, 50_000),
+                        [1.0, 2.0, 0.5, 0.75, 1.5, 1e-310, 5e-324, 0.0, -0.0, -1.0, np.inf, np.nan,
+                         np.finfo(np.float64).max, np.finfo(np.float64).tiny]])
+    _, _, fl, cl = R.math_selftest(x)
+    fin = np.isfinite(cl) & (cl != 0.0)
+    # absolute error near log(1) = 0, relative elsewhere
+    den = np.maximum(np.abs(cl[fin]), 1.0)
+    err_cuda = np.abs(fl[fin] - cl[fin]) / (np.spacing(den))
+    err_np = np.abs(fl[fin] - np.log(x[fin])) / (np.spacing(den))
+    print("log: max error (ulps of max(|log|,1)) vs CUDA", err_cuda.max(), "vs numpy", err_np.max())
+    assert err_cuda.max() <= 2.0 and err_np.max() <= 2.0
+    assert fl[np.where(x == 1.0)[0][0]] == 0.0
+    special = ~fin
+    assert np.array_equal(fl[special], cl[special], equal_nan=True)
