@@ -40,13 +40,16 @@ sys.path.insert(0, os.path.join(REPO, "mdoodz7.0_gb300"))
 METRIC = "rheology point-updates/s on 1 GB300: plain FP64 vs NN warm-start at tol 1e-11"
 UNIT = "point-updates/s"
 
-# FP64 work of the sweep kernel per point-update on this workload, in flops
-# (DFMA = 2, DADD/DMUL = 1), from ncu's thread-level FP64 instruction counters of one
-# k_sweep launch on the same field distributions (profiles/k_sweep_plain_large.md).
-# None until that capture exists; then `roofline.achieved` is this x nodes / launch time.
-FP64_FLOPS_PER_POINT = None
-# DRAM bytes (read + write) per point-update of k_sweep, from the same capture.
-DRAM_BYTES_PER_POINT = None
+# FP64 work of the sweep kernel per point-update on this workload, in flops (DFMA = 2,
+# DADD/DMUL = 1): ncu's thread-level FP64 instruction counters of one k_sweep launch
+# (default start) on the same field distributions at 513 x 513 cells
+# (profiles/k_sweep_plain_large_513.md): 1.181e9 flops / 527,365 nodes.
+# `roofline.achieved` = this x nodes / the CUDA-event time of one launch.
+FP64_FLOPS_PER_POINT = 2240.0
+# DRAM bytes (read + write) per point-update of the same capture (91.3 MB + 50.0 MB over
+# 527,365 nodes), scaled to the launch by its node count; the write count of that small
+# capture misses lines still in L2 when the kernel ends.
+DRAM_BYTES_PER_POINT = 267.9
 
 
 def parse():
