@@ -55,6 +55,7 @@ extern "C" {
 #define MDZ_ELINESEARCH     -17  /* tensile line search alpha<0.01 (:868-872, exit 0) */
 #define MDZ_EANISO_NAN      -18  /* aniso VE residual NaN (AnisotropyRoutines.c:543, exit 1) */
 #define MDZ_EANISO_ITER     -19  /* aniso VE iterations failed (AnisotropyRoutines.c:580-583, exit 0) */
+#define MDZ_ESCRATCH        -20  /* request larger than the static scratch of mdz_rheo_points_static */
 
 /* memory space of the field pointers handed to a sweep */
 #define MDZ_MEM_HOST   0  /* host memory: the library copies in and out (drop-in mode) */
@@ -244,6 +245,32 @@ int mdz_rheo_sweep_aniso(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_ma
 int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                     const mdz_point_inputs *in, mdz_point_outputs *out, int64_t n, int aniso,
                     int mem);
+/* ---- allocation-free variant (no reference counterpart) ----------------
+ * mdz_rheo_points on the CURRENT device without any context and without allocating:
+ * no cudaMalloc / cudaFree / cudaHostAlloc and no allocating library call.  For callers
+ * that must not allocate during a time step: cudaFree synchronises the whole device
+ * (stalling the caller's other streams), and a caller that sizes its device memory once
+ * at start-up (a solver holding most of HBM, a fixed-budget service) cannot absorb
+ * allocations made inside the call.
+ * Staging and statistics live in one file-scope static __device__ array of
+ * MDZ_STATIC_SCRATCH_BYTES (4 MiB, 256-byte aligned) per device:
+ *   bytes needed = 256 (statistics) + for MDZ_MEM_HOST, for every non-NULL input and
+ *   output array, n * element size rounded up to 256; for MDZ_MEM_DEVICE only the 256.
+ * A request above the array returns MDZ_ESCRATCH before anything is enqueued (about
+ * 10,000 points with every input and output present, host memory).
+ * Nothing in the array has to start at zero: the call itself resets the statistics
+ * block (counters 0, error key all ones) on `stream` before its kernel.  Stream 0 / NULL
+ * is the legacy default stream.  The call is blocking: it returns after `stream` has
+ * drained, with outputs (and `stats`, may be NULL) in place.  Two calls that overlapped
+ * on one device would race on the one array; calls are therefore serialised per
+ * process by a lock held until the stream has drained.
+ * The first call on each device looks up the array's address with
+ * cudaGetSymbolAddress (that device current); make it before any stream capture
+ * starts.  Inputs, outputs and return codes are those of mdz_rheo_points. */
+#define MDZ_STATIC_SCRATCH_BYTES (4u << 20)
+int mdz_rheo_points_static(const mdz_model *model, const mdz_materials *mat, const mdz_point_inputs *in,
+                           mdz_point_outputs *out, int64_t n, int aniso, int mem, void *stream,
+                           mdz_sweep_stats *stats);
 /* Per-(phase, node) VE local iteration counts of the last sweep run with
  * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
  * inactive.  Host buffers. */

@@ -382,6 +382,15 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
 
 
 // ---------------------------------------------------------------------------------
+// static scratch of mdz_rheo_points_static: one array per device, its address looked
+// up once per device; the lock serialises the calls that share it
+// ---------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_points_scratch[MDZ_STATIC_SCRATCH_BYTES];
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+void *g_static_addr[kStaticMaxDevices] = {};
+
+// ---------------------------------------------------------------------------------
 // learned warm start: host-side packing of the BF16 K-major tiles (umma.cuh layout)
 // ---------------------------------------------------------------------------------
 uint16_t f2bf(float f) {
@@ -553,6 +562,7 @@ const char *mdz_rheo_status_string(int s) {
     case MDZ_ELINESEARCH: return "tensile plasticity line search failed (alpha < 0.01)";
     case MDZ_EANISO_NAN: return "anisotropic VE residual is NaN";
     case MDZ_EANISO_ITER: return "anisotropic Visco-Elastic iterations failed";
+    case MDZ_ESCRATCH: return "request larger than the static scratch (MDZ_STATIC_SCRATCH_BYTES)";
     default: return "unknown status";
   }
 }
@@ -702,6 +712,115 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
   rc = finish(c, nullptr);
   for (auto d : tmp) cudaFree(d);
   return rc;
+}
+
+int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const mdz_point_inputs *in,
+                           mdz_point_outputs *out, int64_t n, int aniso, int mem, void *stream,
+                           mdz_sweep_stats *st) {
+  if (!md || !m || !in || !out || n < 0) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  const bool host = (mem == MDZ_MEM_HOST);
+  // every input the kernel reads must be present
+  const void *req[] = {in->phase, in->G, in->T, in->P, in->d, in->phi, in->X0, in->Exx, in->Ezz, in->Exz,
+                       in->Txx0, in->Tzz0, in->Txz0, in->dil, in->fric, in->C, in->P0, in->T0, in->beta};
+  for (auto r : req) if (!r) return MDZ_EINVAL;
+  if (aniso && (!in->lxlz || !in->lx2 || !in->ani_fac)) return MDZ_EINVAL;
+  static thread_local PointArgs A;
+  memset(&A, 0, sizeof(A));
+  int rc = fold_model(md, m, A.M);
+  if (rc != MDZ_OK) return rc;
+  for (int p = 0; p < A.M.np; p++) fold_phase(m, md, p, A.ph[p]);
+  if (host)
+    for (int64_t i = 0; i < n; i++)
+      if (in->phase[i] < 0 || in->phase[i] >= A.M.np) return MDZ_EINVAL;
+  A.n = n;
+  A.aniso = aniso;
+  A.polish = MDZ_DEFAULT_POLISH;
+  A.in = *in;
+  A.out = *out;
+  // layout of the array: statistics, then (host memory) one 256-aligned slot per array
+  const size_t nb = (size_t)n * sizeof(double), ni = (size_t)n * sizeof(int32_t);
+  const double **pin[] = {&A.in.G, &A.in.T, &A.in.P, &A.in.d, &A.in.phi, &A.in.X0, &A.in.Exx, &A.in.Ezz,
+                          &A.in.Exz, &A.in.Txx0, &A.in.Tzz0, &A.in.Txz0, &A.in.strain_acc, &A.in.dil,
+                          &A.in.fric, &A.in.C, &A.in.P0, &A.in.T0, &A.in.beta, &A.in.div,
+                          &A.in.lxlz, &A.in.lx2, &A.in.angle, &A.in.ani_fac};
+  double **pout[] = {&A.out.eta, &A.out.Txx, &A.out.Tzz, &A.out.Txz, &A.out.etaVE, &A.out.VEcoeff,
+                     &A.out.Eii_el, &A.out.Eii_pl, &A.out.Eii_pwl, &A.out.Eii_exp, &A.out.Eii_lin,
+                     &A.out.Eii_gbs, &A.out.Eii_cst, &A.out.d1, &A.out.X1, &A.out.OverS, &A.out.Pcorr,
+                     &A.out.rho, &A.out.div_el, &A.out.div_pl, &A.out.div_r, &A.out.Wtot, &A.out.Wel,
+                     &A.out.Wdiss};
+  constexpr size_t kStats = 256;
+  static_assert(sizeof(DevStats) <= kStats, "statistics block");
+  size_t need = kStats;
+  auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  if (host) {
+    need += in->phase ? round256(ni) : 0;
+    for (auto pp : pin) need += *pp ? round256(nb) : 0;
+    for (auto pp : pout) need += *pp ? round256(nb) : 0;
+    need += (out->iters ? round256(ni) : 0) + (out->status ? round256(ni) : 0);
+  }
+  if (need > (size_t)MDZ_STATIC_SCRATCH_BYTES) return MDZ_ESCRATCH;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kStaticMaxDevices) return MDZ_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[dev]) {  // set-up, once per device, with that device current
+    void *a = nullptr;
+    CK(cudaGetSymbolAddress(&a, g_points_scratch));
+    if (!a || ((uintptr_t)a & 255)) return MDZ_ECUDA;
+    g_static_addr[dev] = a;
+  }
+  char *base = (char *)g_static_addr[dev];
+  DevStats *dstats = (DevStats *)base;
+  A.stats = dstats;
+  CK(cudaMemsetAsync(dstats, 0, sizeof(DevStats), s));
+  CK(cudaMemsetAsync(&dstats->err_key, 0xff, sizeof(dstats->err_key), s));
+  if (n > 0) {
+    std::vector<std::pair<void *, const void *>> backs;  // (host destination, device slot)
+    size_t off = kStats;
+    auto stage_in = [&](const void *h, size_t bytes) -> const void * {
+      if (!h || !host) return h;
+      void *d = base + off;
+      off += round256(bytes);
+      if (cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = MDZ_ECUDA;
+      return d;
+    };
+    auto stage_out = [&](void *h, size_t bytes) -> void * {
+      if (!h || !host) return h;
+      void *d = base + off;
+      off += round256(bytes);
+      backs.push_back({h, d});
+      return d;
+    };
+    A.in.phase = (const int32_t *)stage_in(in->phase, ni);
+    for (auto pp : pin) *pp = (const double *)stage_in(*pp, nb);
+    for (auto pp : pout) *pp = (double *)stage_out(*pp, nb);
+    A.out.iters = (int32_t *)stage_out(out->iters, ni);
+    A.out.status = (int32_t *)stage_out(out->status, ni);
+    if (rc != MDZ_OK) return rc;
+    CK(launch_points(A, s));
+    for (auto &b : backs) {
+      const size_t bytes = (b.first == (void *)out->iters || b.first == (void *)out->status) ? ni : nb;
+      CK(cudaMemcpyAsync(b.first, b.second, bytes, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  DevStats h;
+  CK(cudaMemcpyAsync(&h, dstats, sizeof(h), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  int status = MDZ_OK;
+  long long node = -1;
+  if (h.err_key != ~0ull) {
+    status = -(int)(h.err_key & 0xff);
+    node = (long long)(h.err_key >> 8);
+  }
+  if (st) {
+    memset(st, 0, sizeof(*st));
+    st->phase_calls = h.calls; st->newton_iters = h.iters; st->max_newton_iters = h.maxit;
+    st->plastic_calls = h.plastic; st->status = status; st->error_node = node;
+    st->kernel_launches = n > 0 ? 1 : 0;
+  }
+  return status;
 }
 
 int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {

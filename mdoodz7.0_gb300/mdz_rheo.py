@@ -41,6 +41,8 @@ MDZ_EGRAIN_ZERO = -16
 MDZ_ELINESEARCH = -17
 MDZ_EANISO_NAN = -18
 MDZ_EANISO_ITER = -19
+MDZ_ESCRATCH = -20
+STATIC_SCRATCH_BYTES = 4 << 20
 
 MEM_HOST = 0
 MEM_DEVICE = 1
@@ -261,6 +263,9 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_abi_sizes.argtypes = [C.POINTER(C.c_size_t)]
     lib.mdz_rheo_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.mdz_rheo_math_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64] + [C.c_void_p] * 4
+    lib.mdz_rheo_points_static.argtypes = [C.POINTER(Model), C.POINTER(Materials), C.POINTER(PointInputs),
+                                           C.POINTER(PointOutputs), C.c_int64, C.c_int, C.c_int, C.c_void_p,
+                                           C.POINTER(SweepStats)]
     lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
     lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SweepStats)]
@@ -296,6 +301,16 @@ def measure_fp64_peak(device: int = 0) -> float:
     if rc != MDZ_OK:
         raise RheoError(rc, "mdz_rheo_measure_fp64_peak")
     return v.value
+
+
+def points_static(model, mat, pin, pout, n, aniso=0, mem=MEM_HOST, stream=None, lib=None):
+    """mdz_rheo_points_static: the point path on the current device, allocating nothing.
+    Returns (status, SweepStats)."""
+    lib = lib or load_library()
+    st = SweepStats()
+    rc = lib.mdz_rheo_points_static(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso, mem,
+                                    stream, C.byref(st))
+    return rc, st
 
 
 def math_selftest(x: np.ndarray, device: int = 0):
