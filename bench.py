@@ -67,10 +67,8 @@ def parse():
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    import mdz_replicas
+    return mdz_replicas.dist_env()
 
 
 def algorithmic_bytes(w):
@@ -208,15 +206,15 @@ def main():
     import mdz_rheo as R
     import mdz_workloads as W
 
+    import mdz_replicas as REP
     ws, rank, local = dist_env()
     if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
         torch.cuda.set_device(local)
+        REP.init("nccl")
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
 
-    w = W.plain_large(seed=1 + rank, ncx=args.size, nphases=args.phases)
+    w = W.plain_large(seed=REP.replica_seed(1, rank), ncx=args.size, nphases=args.phases)
     d = {k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
          for k, v in w.arrays.items()}
     fs = R.FieldSet(d)
@@ -254,13 +252,9 @@ def main():
         if clk:
             clk.__exit__()
             r["clocks"] = clk.summary()
-        total_ms = e0.elapsed_time(e1)
-        if ws > 1:
-            t = torch.tensor([total_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms = REP.max_over_ranks(e0.elapsed_time(e1), dev)
         r["ms_step"] = total_ms / args.steps
-        r["value"] = ws * w.nodes / (r["ms_step"] * 1e-3)
+        r["value"] = REP.whole_job_rate(w.nodes, ws, r["ms_step"])
         r["mean_iters"] = r["iters"] / max(r["calls"], 1)
         return r
 
@@ -308,17 +302,13 @@ def main():
             bi, bo = st.h2d_bytes, st.d2h_bytes
         e1.record(stream)
         barrier()
-        e2e_ms = e0.elapsed_time(e1) / args.steps
-        if ws > 1:
-            t = torch.tensor([e2e_ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        e2e = {"value": ws * w.nodes / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+        e2e_ms = REP.max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
+        e2e = {"value": REP.whole_job_rate(w.nodes, ws, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo)}
         del h, fh
 
     if rank != 0:
-        torch.distributed.destroy_process_group()
+        REP.finalize()
         return
 
     # ---- roofline of the dominant kernel (k_sweep) ----
@@ -367,7 +357,7 @@ def main():
             "reference_start": ref_r, "warm_start": warm}
     print(json.dumps(line))
     if ws > 1:
-        torch.distributed.destroy_process_group()
+        REP.finalize()
 
 
 if __name__ == "__main__":

@@ -225,6 +225,7 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
 // ---------------------------------------------------------------------------------------
 struct VeCoef {
   double Eii, thr_conv, thr_fail;  // Eii * tol/100, Eii * tol
+  double inv_Eii;                  // 1 / Eii
   double A;                        // sum of the linear coefficients (el, cst, Newtonian laws)
   double a_cst, a_lin1, a_pwl1;    // e_cst = eta a_cst, e_lin = eta a_lin1 (n_lin==1), e_pwl = eta a_pwl1 (n_pwl==1)
   double inv_p;                    // 1/eta of the primary (softest) non-linear law
@@ -241,6 +242,7 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
   const double Eii = c.Eii;
   const double tol = 1.0e-11;  // hard-coded in LocalIterationViscoElastic (:154)
   q.Eii = Eii;
+  q.inv_Eii = 2.0 * c.inv2Eii;
   q.thr_conv = Eii * (tol / 100);
   q.thr_fail = Eii * tol;
   q.a_cst = (L.mech & F_CST) ? Eii / eta_cst : 0.0;
@@ -267,7 +269,7 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
   }
   if (!(inv_p > 0.0)) q.nl = 0;  // every non-linear law underflowed: they carry no strain rate
   q.inv_p = inv_p;
-  if (q.nl) {
+  if (q.nl & (q.nl - 1)) {  // offsets are needed only with two or more non-linear laws
     const double r_p = 1.0 / inv_p;
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
@@ -318,7 +320,7 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, VeState &s) {
 // these steps only move its start (to within FP32 rounding of the root).
 __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, double eta_up, float s0, int iters) {
   if (iters <= 0) return s0;
-  const float a = (float)(eta_up * q.A / q.Eii);
+  const float a = (float)(eta_up * q.A * q.inv_Eii);
   float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
   if (q.nl) {
     const float lp = __logf((float)(eta_up * q.inv_p));
@@ -569,11 +571,12 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   S.eta_up = eta_up; S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
 
-// Local solve (from eta_start, refined by `polish` FP32 Newton steps), plastic corrections
-// and post-processing of one (node, phase).  eta_conv (may be null) receives the converged
-// visco-elastic viscosity, before plasticity.
+// Local solve (from s_start * eta_up, refined by `polish` FP32 Newton steps; s_start = 1
+// and polish = 0 is the reference's start), plastic corrections and post-processing of
+// one (node, phase).  eta_conv (may be null) receives the converged visco-elastic
+// viscosity, before plasticity.
 __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                  IsoState &S, double eta_start, int polish, PointOut &o,
+                                  IsoState &S, float s_start, int polish, PointOut &o,
                                   double *eta_conv = nullptr) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
@@ -591,8 +594,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     VeCoef q;
     ve_coef(L, c, eta_cst, q);
     VeState s;
-    s.eta = (polish > 0) ? (double)ve_polish_f32(q, eta_up, (float)(eta_start / eta_up), polish) * eta_up
-                         : eta_start;
+    s.eta = (double)ve_polish_f32(q, eta_up, s_start, polish) * eta_up;
     s.status = MDZ_OK;
     ve_newton(q, s);
     set_status(o.status, s.status);
@@ -714,7 +716,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     if (plastic == 2) o.OverS = eta_vp * lam_dot * A_tau;
     if (in.centroid == 1) {
       const double T2 = Tii * Tii;
-      o.Wtot = T2 / eta_ve;
+      o.Wtot = T2 * (Eii * inv_half_T);  // T2 / eta_ve, with Tii_ve = 2 eta_ve Eii
       o.Wel = T2 * c.inv_eta_el;
       o.Wdiss = T2 * inv;
       if (o.Wdiss < 0.0) set_status(o.status, MDZ_EWDISS);
@@ -736,7 +738,7 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
                                  int polish, PointOut &o) {
   IsoState S;
   iso_setup(M, ph, in, c, S, o);
-  iso_finish(M, ph, in, c, S, S.eta_up, polish, o);
+  iso_finish(M, ph, in, c, S, 1.0f, polish, o);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -812,10 +814,10 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
 }
 
 // Local solve, plasticity, post-processing.  The Newton starts from the reference's
-// bisection when warm_eta <= 0 and polish == 0; otherwise from warm_eta (eta_up when
-// warm_eta <= 0) refined by `polish` FP32 Newton steps.
+// bisection when s_start <= 0 and polish == 0; otherwise from s_start * eta_up (eta_up
+// when s_start <= 0) refined by `polish` FP32 Newton steps.
 __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                   const AnisoNode &an, IsoState &S, double warm_eta, int polish, PointOut &o,
+                                   const AnisoNode &an, IsoState &S, float s_start, int polish, PointOut &o,
                                    double *eta_conv = nullptr) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
@@ -849,9 +851,8 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     VeState s;
     s.status = MDZ_OK;
     double r, S;
-    if (warm_eta > 0.0 || polish > 0) {
-      const double start = (warm_eta > 0.0) ? warm_eta : eta_up;
-      eta_ve = (polish > 0) ? (double)ve_polish_f32(q, eta_up, (float)(start / eta_up), polish) * eta_up : start;
+    if (s_start > 0.0f || polish > 0) {
+      eta_ve = (double)ve_polish_f32(q, eta_up, (s_start > 0.0f) ? s_start : 1.0f, polish) * eta_up;
     } else {
       double lo = min_eta * 1.0e-3, hi = 10.0 * fmax(eta_lo, max_eta);
       for (int bit = 0; bit < 10; bit++) {
@@ -938,7 +939,7 @@ __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, co
                                    const AnisoNode &an, int polish, PointOut &o) {
   IsoState S;
   aniso_setup(M, ph, in, c, an, S, o);
-  aniso_finish(M, ph, in, c, an, S, 0.0, polish, o);
+  aniso_finish(M, ph, in, c, an, S, 0.0f, polish, o);
 }
 
 // EffectiveStrainRate, RheologyDensity.c:116-146

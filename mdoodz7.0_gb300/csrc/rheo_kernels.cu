@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(128) k_sweep_tiles(const __grid_constant__ Swe
       float f[kMlpIn];
 #pragma unroll
       for (int j = 0; j < kMlpIn; j++) f[j] = 0.0f;
-      double eta_start = 0.0;  // 0: the reference's own start
+      float s_start = ANISO ? 0.0f : 1.0f;  // the reference's own start
       if (active) {
         if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
         else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
@@ -306,14 +306,14 @@ __global__ void __launch_bounds__(128) k_sweep_tiles(const __grid_constant__ Swe
         mlp_forward(S, x, y, phase);
         if (active && !S.fault) {
           const float z = fmaxf(y[0] * W.mlp.z_scale + W.mlp.z_shift, 0.0f);
-          eta_start = (double)__expf(-z) * st.eta_up;
+          s_start = __expf(-z);
         }
       }
       if (!active) continue;
       double eta_conv = 0.0;
       const int polish = (MODE == MODE_WARM) ? W.mlp.polish_iters : 0;
-      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, eta_start, polish, o, &eta_conv);
-      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, eta_start > 0.0 ? eta_start : st.eta_up, polish, o, &eta_conv);
+      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, s_start, polish, o, &eta_conv);
+      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, s_start, polish, o, &eta_conv);
       node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
       if (MODE == MODE_COLLECT) {
         const long long item = (long long)p * total + i;
