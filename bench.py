@@ -40,16 +40,16 @@ sys.path.insert(0, os.path.join(REPO, "mdoodz7.0_gb300"))
 METRIC = "rheology point-updates/s on 1 GB300: plain FP64 vs NN warm-start at tol 1e-11"
 UNIT = "point-updates/s"
 
-# FP64 work of the sweep kernel per point-update on this workload, in flops (DFMA = 2,
-# DADD/DMUL = 1): ncu's thread-level FP64 instruction counters of one k_sweep launch
-# (default start) on the same field distributions at 513 x 513 cells
-# (profiles/k_sweep_plain_large_513.md): 1.181e9 flops / 527,365 nodes.
+# FP64 work of the sweep kernel per point-update, in flops (DFMA = 2, DADD/DMUL = 1):
+# ncu's thread-level FP64 instruction counters of one k_sweep launch (default start) on
+# the same field distributions at 513 x 513 cells (527,365 nodes), per workload
+# (profiles/k_sweep_plain_large_513.md, profiles/k_sweep_aniso_513.md).
 # `roofline.achieved` = this x nodes / the CUDA-event time of one launch.
-FP64_FLOPS_PER_POINT = 2240.0
-# DRAM bytes (read + write) per point-update of the same capture (91.3 MB + 50.0 MB over
-# 527,365 nodes), scaled to the launch by its node count; the write count of that small
-# capture misses lines still in L2 when the kernel ends.
-DRAM_BYTES_PER_POINT = 267.9
+FP64_FLOPS_PER_POINT = {"plain_large": 2047.1, "aniso": 1263.5}
+# DRAM bytes (read + write) per point-update of the same captures, scaled to a launch by
+# its node count; the write count of those small captures misses lines still in L2 when
+# the kernel ends.
+DRAM_BYTES_PER_POINT = {"plain_large": 268.0, "aniso": 268.3}
 
 
 def parse():
@@ -58,12 +58,21 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--size", type=int, default=2049, help="cells per side")
+    ap.add_argument("--size", type=int, default=None,
+                    help="cells per side (default 2049; 4097 for --workload aniso)")
+    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "aniso", "many_grids"],
+                    help="plain_large: the headline; aniso: ViscosityConciseAniso sweep; many_grids: "
+                         "64 uneven grids in one launch and a 20-sweep CUDA graph")
     ap.add_argument("--phases", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm start")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.size is None:
+        args.size = 4097 if args.workload == "aniso" else 2049
+    if args.workload == "aniso" and args.phases == 5:
+        args.phases = 3
+    return args
 
 
 def dist_env():
@@ -71,13 +80,15 @@ def dist_env():
     return mdz_replicas.dist_env()
 
 
-def algorithmic_bytes(w):
+def algorithmic_bytes(w, aniso=False):
     """Compulsory HBM bytes of one sweep: every input field read once, every output
-    written once (field counts of NonNewtonianViscosityGrid, RheologyDensity.c:1131-1426)."""
+    written once (field counts of NonNewtonianViscosityGrid, RheologyDensity.c:1131-1426;
+    the anisotropic sweep adds d1, d2, angle and the anisotropy factor, and VE_s)."""
     np_ = w.mat.Nb_phases
     nc, nv = w.Nc, w.Nv
-    cen = 8 * (18 + np_ + np_) + 1 + 8 * 23          # inputs, phase fractions, phase_eta, BC flag, outputs
-    ver = 8 * (13 + np_ + np_) + 1 + 8 * 6 + 8 * 4   # + the four interpolated fields written
+    extra_in = 4 if aniso else 0
+    cen = 8 * (18 + extra_in + np_ + np_) + 1 + 8 * 23                  # inputs, fractions, phase_eta, BC, outputs
+    ver = 8 * (13 + extra_in + np_ + np_) + 1 + 8 * (6 + int(aniso)) + 8 * 4   # + the four interpolated fields
     return nc * cen + nv * ver
 
 
@@ -131,20 +142,20 @@ class ClockSampler:
                 "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
 
 
-def cpu_baseline(W, O, sample_cells=1025, reps=1):
+def cpu_baseline(W, O, sample_cells=1025, reps=1, aniso=False):
     """The oracle (C restatement of the reference, OpenMP, all host cores) on a bounded
     sample of the same workload distribution."""
     import mdz_rheo as R
-    ws = W.plain_large(seed=101, ncx=sample_cells)
-    O.orc_sweep(ws.model, ws.mat, R.FieldSet(ws.arrays))  # warm-up (page faults, thread pool)
+    ws = W.aniso(seed=101, ncx=sample_cells) if aniso else W.plain_large(seed=101, ncx=sample_cells)
+    O.orc_sweep(ws.model, ws.mat, R.FieldSet(ws.arrays), aniso=aniso)  # warm-up (page faults, threads)
     t0 = time.perf_counter()
     for _ in range(reps):
-        O.orc_sweep(ws.model, ws.mat, R.FieldSet(ws.arrays))
+        O.orc_sweep(ws.model, ws.mat, R.FieldSet(ws.arrays), aniso=aniso)
     dt = (time.perf_counter() - t0) / reps
     lib = O.reference()
     kind = "port"
     return {"value": ws.nodes / dt, "unit": UNIT, "cores": O.oracle().orc_num_threads(), "kind": kind,
-            "sample": f"{sample_cells}x{sample_cells}-cell grid of the same 5-phase workload "
+            "sample": f"{sample_cells}x{sample_cells}-cell grid of the same {ws.mat.Nb_phases}-phase workload "
                       f"({ws.nodes} nodes), {reps} sweep(s), {dt:.2f} s each"}
 
 
@@ -195,10 +206,111 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_many_grids(args):
+    """64 grids of uneven size (65-1025 cells per side, 2-5 phases, dt 1e10-1e12 s, each
+    with its own seed) on one GPU, device-resident.  Three forms of one Picard sweep over
+    all of them: 64 separate sweep calls, one batched launch, and a CUDA graph of 20
+    batched sweeps with the strain rates perturbed by +-5 % before each (the headline
+    `value`: point-updates/s over the graph)."""
+    import torch
+
+    import mdz_replicas as REP
+    import mdz_rheo as R
+    import mdz_workloads as W
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        torch.cuda.set_device(local)
+        REP.init("nccl")
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    t0 = time.perf_counter()
+    grids = W.many_grids(seed=REP.replica_seed(7, rank), n=64)
+    gen_s = time.perf_counter() - t0
+    devs = [{k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
+             for k, v in g.arrays.items()} for g in grids]
+    fss = [R.FieldSet(d) for d in devs]
+    nodes = sum(g.nodes for g in grids)
+    ctx = R.Context(dev)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(step, reps):
+        for _ in range(args.warmup):
+            step()
+        barrier()
+        e0.record(stream)
+        for _ in range(reps):
+            step()
+        e1.record(stream)
+        barrier()
+        return REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps
+
+    def separate():
+        for g, fs in zip(grids, fss):
+            ctx.sweep(g.model, g.mat, fs, mem=R.MEM_DEVICE)
+
+    ms_sep = timed(separate, args.steps)
+    batch = R.Batch(ctx, [g.model for g in grids], [g.mat for g in grids], fss)
+    calls = [0]
+
+    def batched():
+        _, st = batch.sweep()
+        calls[0] = st.phase_calls
+
+    ms_batch = timed(batched, args.steps)
+    nsw, amp = 20, 0.05
+    batch.capture(nsw, amp=amp, seed=2026)
+    stats = []
+
+    def graph():
+        _, st = batch.launch()
+        stats.append(st)
+
+    with ClockSampler(dev) as clk:
+        ms_graph = timed(graph, args.steps)
+    st = stats[-1]
+    batch.close()
+    if rank != 0:
+        REP.finalize()
+        return
+    value = REP.whole_job_rate(nodes * nsw, ws, ms_graph)
+    sides = sorted(g.model.Nx - 1 for g in grids)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"many_grids: 64 grids, {sides[0]}-{sides[-1]} cells per side (log-uniform), "
+                                   "2-5 phases each, dt 1e10-1e12 s; one step = one CUDA graph of 20 batched "
+                                   "sweeps, strain rates x (1 + 0.05 U[-1,1)) before each",
+                       "nodes_per_sweep": nodes, "sweeps_per_step": nsw,
+                       "phase_calls_per_sweep": calls[0],
+                       "mean_newton_iters": st.newton_iters / max(1, st.phase_calls),
+                       "max_newton_iters": int(st.max_newton_iters), "generate_s": gen_s,
+                       "l2": "inputs larger than L2, no flush"},
+            "forms_ms_per_sweep": {"separate_calls": ms_sep, "one_batched_launch": ms_batch,
+                                   "graph": ms_graph / nsw},
+            "separate_vs_graph": ms_sep / (ms_graph / nsw),
+            "roofline": None, "cpu_baseline": None, "e2e": None, "clocks": clk.summary(),
+            "gpu_launches": args.steps * st.kernel_launches}
+    print(json.dumps(line))
+    if ws > 1:
+        REP.finalize()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "many_grids":
+        run_many_grids(args)
         return
     import numpy as np
     import torch
@@ -214,13 +326,18 @@ def main():
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
 
-    w = W.plain_large(seed=REP.replica_seed(1, rank), ncx=args.size, nphases=args.phases)
+    aniso = args.workload == "aniso"
+    if aniso:
+        w = W.aniso(seed=REP.replica_seed(4, rank), ncx=args.size, nphases=args.phases)
+    else:
+        w = W.plain_large(seed=REP.replica_seed(1, rank), ncx=args.size, nphases=args.phases)
     d = {k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
          for k, v in w.arrays.items()}
     fs = R.FieldSet(d)
     ctx = R.Context(dev)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
+    sweep = ctx.sweep_aniso if aniso else ctx.sweep
 
     def barrier():
         if ws > 1:
@@ -233,7 +350,7 @@ def main():
     def timed(flags, clock=False):
         """Device-resident sweeps: W warm-up, then K timed between barriers (max over ranks)."""
         for _ in range(args.warmup):
-            ctx.sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
+            sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
         r = {"kernel_ms": [], "iters": 0, "calls": 0, "launches": 0, "maxit": 0}
         barrier()
         clk = ClockSampler(dev) if clock else None
@@ -241,7 +358,7 @@ def main():
             clk.__enter__()
         e0.record(stream)
         for _ in range(args.steps):
-            rc, st = ctx.sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
+            rc, st = sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
             r["kernel_ms"].append(st.elapsed_ms)
             r["iters"] += st.newton_iters
             r["calls"] += st.phase_calls
@@ -274,10 +391,14 @@ def main():
     if not args.no_warm:
         import mdz_warmstart as WSt
         t0 = time.perf_counter()
-        Xs, Ys = WSt.collect(ctx, [W.plain_large(seed=100 + 1000 * rank, ncx=1025, nphases=args.phases)],
-                             max_pairs=8_000_000)
+        if aniso:
+            src = W.aniso(seed=130 + 1000 * rank, ncx=1449, nphases=args.phases)
+        else:
+            src = W.plain_large(seed=100 + 1000 * rank, ncx=1025, nphases=args.phases)
+        Xs, Ys = WSt.collect(ctx, [src], aniso=aniso, max_pairs=8_000_000)
+        del src
         t1 = time.perf_counter()
-        wts, loss, train_s = WSt.train(ctx, Xs, Ys, WSt.FEAT_ISO)
+        wts, loss, train_s = WSt.train(ctx, Xs, Ys, WSt.FEAT_ANISO if aniso else WSt.FEAT_ISO)
         del Xs, Ys
         ctx.set_warmstart(wts, R.DEFAULT_POLISH)
         warm = summary(timed(R.SWEEP_WARMSTART))
@@ -293,12 +414,12 @@ def main():
                  else torch.from_numpy(v).pin_memory()) for k, v in w.arrays.items()}
         fh = R.FieldSet(h)
         for _ in range(max(1, args.warmup)):
-            ctx.sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
+            sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
         barrier()
         e0.record(stream)
         bi = bo = 0
         for _ in range(args.steps):
-            rc, st = ctx.sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
+            rc, st = sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
             bi, bo = st.h2d_bytes, st.d2h_bytes
         e1.record(stream)
         barrier()
@@ -314,11 +435,12 @@ def main():
     # ---- roofline of the dominant kernel (k_sweep) ----
     launch_ms = statistics.mean(kernel_ms)
     peak_fp64 = R.measure_fp64_peak(dev)
-    if FP64_FLOPS_PER_POINT is not None:
-        achieved = FP64_FLOPS_PER_POINT * w.nodes / (launch_ms * 1e-3) / 1e12
+    default_phases = {"plain_large": 5, "aniso": 3}
+    if args.workload in FP64_FLOPS_PER_POINT and args.phases == default_phases[args.workload]:
+        achieved = FP64_FLOPS_PER_POINT[args.workload] * w.nodes / (launch_ms * 1e-3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": peak_fp64, "unit": "TFLOP/s",
                 "frac": achieved / peak_fp64, "peak_source": "measured (DFMA probe, mdz_rheo_measure_fp64_peak)",
-                "traffic": (DRAM_BYTES_PER_POINT * w.nodes) if DRAM_BYTES_PER_POINT else None}
+                "traffic": DRAM_BYTES_PER_POINT[args.workload] * w.nodes}
     else:
         roof = {"bound": "fp64", "achieved": None, "peak": peak_fp64, "unit": "TFLOP/s", "frac": None,
                 "peak_source": "measured (DFMA probe)", "traffic": None}
@@ -327,7 +449,7 @@ def main():
         hbm = peaks.get("hbm_gbs")
     except Exception:
         hbm = None
-    bytes_alg = algorithmic_bytes(w)
+    bytes_alg = algorithmic_bytes(w, aniso)
     roof["hbm_achieved_gbs"] = bytes_alg / (launch_ms * 1e-3) / 1e9
     roof["hbm_frac"] = (roof["hbm_achieved_gbs"] / hbm) if hbm else None
     roof["algorithmic_bytes_per_launch"] = bytes_alg
@@ -338,19 +460,23 @@ def main():
         try:
             import oracle_lib as O
             O.build(ref=False)
-            cpu = cpu_baseline(W, O)
+            cpu = cpu_baseline(W, O, aniso=aniso)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"plain_large: {args.size}x{args.size} cells, {args.phases} phases "
-                                   "(dislocation, diffusion, Peierls, softened Drucker-Prager), FP64 "
-                                   "local Newton to |r| < 1e-13 Eii started after 4 FP32 Newton steps",
+            "config": {"workload": (f"aniso: {args.size}x{args.size} cells, {args.phases} phases (dislocation, "
+                                    "softened Drucker-Prager), director angle U[0,pi), anisotropy factor "
+                                    "log-U(1,10)" if aniso else
+                                    f"plain_large: {args.size}x{args.size} cells, {args.phases} phases "
+                                    "(dislocation, diffusion, Peierls, softened Drucker-Prager)")
+                                   + "; FP64 local Newton to |r| < 1e-13 Eii started after 4 FP32 Newton steps",
                        "nodes_per_gpu": w.nodes, "phase_calls_per_step": calls // args.steps,
                        "mean_newton_iters": main_r["mean_iters"], "max_newton_iters": main_r["maxit"],
-                       "l2": "inputs larger than L2 (3.3 GB of fields), no flush",
+                       "l2": f"inputs larger than L2 ({algorithmic_bytes(w, aniso) / 1e9:.1f} GB moved per sweep), "
+                             "no flush",
                        "parallelism": f"{ws} independent grid(s), one per GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,

@@ -271,6 +271,32 @@ int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materia
 int mdz_rheo_points_static(const mdz_model *model, const mdz_materials *mat, const mdz_point_inputs *in,
                            mdz_point_outputs *out, int64_t n, int aniso, int mem, void *stream,
                            mdz_sweep_stats *stats);
+/* ---- many grids in one launch (no reference counterpart) ----------------
+ * A batch is n device-resident grids (MDZ_MEM_DEVICE fields), each with its own model,
+ * material table and size, swept together by one kernel launch: the node range of
+ * every grid is cut into tiles of 128 nodes and one CTA takes one tile.  The grids'
+ * arguments are folded and uploaded once, at creation; the field arrays must stay
+ * valid until the batch is destroyed.  `flags` may hold MDZ_SWEEP_REF_START only.
+ * stats->error_node counts nodes through the batch in order (grid 0's centroids, its
+ * vertices, grid 1's centroids, ...). */
+typedef struct mdz_rheo_batch mdz_rheo_batch;
+int mdz_rheo_batch_create(mdz_rheo_ctx *ctx, int n, const mdz_model *models, const mdz_materials *mats,
+                          const mdz_grid_fields *fields, int aniso, int final_update, int flags,
+                          mdz_rheo_batch **out);
+int mdz_rheo_batch_destroy(mdz_rheo_batch *batch);
+/* One sweep of every grid of the batch: one launch on the context's stream, blocking. */
+int mdz_rheo_batch_sweep(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
+/* Capture `nsweeps` consecutive batch sweeps as one CUDA graph (replacing any earlier
+ * capture).  With amp != 0 every sweep is preceded by a perturbation of the strain-rate
+ * inputs IN PLACE (exxd, ezzd, exz_n at centroids; exxd_s, ezzd_s, exz at vertices):
+ * x <- x (1 + amp u), u uniform in [-1, 1) from SplitMix64 of
+ * key = sm(sm(seed ^ sweep) ^ grid), then sm(key ^ (3 node + component)), with
+ * u = (h >> 11) 2^-52 - 1 (all steps rounded, no fused multiply-add).  The statistics
+ * are reset once at the start of the graph and cover all of its sweeps. */
+int mdz_rheo_batch_capture(mdz_rheo_batch *batch, int nsweeps, double amp, uint64_t seed);
+/* Launch the captured graph on the context's stream and wait for it. */
+int mdz_rheo_batch_launch(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
+
 /* Per-(phase, node) VE local iteration counts of the last sweep run with
  * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
  * inactive.  Host buffers. */

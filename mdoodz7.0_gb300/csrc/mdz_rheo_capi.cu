@@ -46,7 +46,23 @@ struct mdz_rheo_ctx {
   unsigned mma_fault = 0;
 };
 
+struct mdz_rheo_batch {
+  mdz_rheo_ctx *ctx = nullptr;
+  int n = 0;
+  bool aniso = false;
+  SweepArgs *d_grids = nullptr;
+  long long *d_tile_start = nullptr;
+  long long tiles = 0, nodes = 0;
+  BatchArgs args{};
+  int grid = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_sweeps = 0, graph_launches = 0;
+};
+
 namespace {
+
+constexpr int kBatchMaxGrids = 4096;
 
 #define CK(x)                                                                 \
   do {                                                                        \
@@ -248,6 +264,45 @@ struct Mirror {
   }
 };
 
+// The field pointers of one sweep in kernel order, checked for presence.
+struct FieldLists {
+  const double *cin[CI_COUNT];
+  const double *vin[VI_COUNT];
+  double *cout[CO_COUNT];
+  double *vout[VO_COUNT];
+  int nci, nvi;
+};
+
+int field_lists(const mdz_model *md, const mdz_grid_fields *f, bool aniso, FieldLists &L) {
+  const double *cin[CI_COUNT] = {f->mu_n, f->T, f->p_in, f->d0_n, f->phi0_n, f->X0_n, f->exxd, f->ezzd, f->exz_n,
+                                 f->sxxd0, f->szzd0, f->sxz0_n, f->fric_n, f->C_n, f->dil_n, f->p0_n, f->T0_n,
+                                 f->bet_n, f->d1_n, f->d2_n, f->angle_n, f->aniso_factor_n};
+  const double *vin[VI_COUNT] = {f->mu_s, f->X0_s, f->exxd_s, f->ezzd_s, f->exz, f->sxxd0_s, f->szzd0_s, f->sxz0,
+                                 f->fric_s, f->C_s, f->dil_s, f->p0_s, f->bet_s, f->d1_s, f->d2_s, f->angle_s,
+                                 f->aniso_factor_s};
+  L.nci = aniso ? CI_COUNT : CI_d1;
+  L.nvi = aniso ? VI_COUNT : VI_d1;
+  for (int i = 0; i < CI_COUNT; i++) L.cin[i] = (i < L.nci) ? cin[i] : nullptr;
+  for (int i = 0; i < VI_COUNT; i++) L.vin[i] = (i < L.nvi) ? vin[i] : nullptr;
+  for (int i = 0; i < L.nci; i++) if (!L.cin[i]) return MDZ_EINVAL;
+  for (int i = 0; i < L.nvi; i++) if (!L.vin[i]) return MDZ_EINVAL;
+  if (!f->phase_perc_n || !f->phase_perc_s || !f->phase_eta_n || !f->phase_eta_s || !f->BCp_type || !f->BCg_type)
+    return MDZ_EINVAL;
+  double *cout[CO_COUNT] = {f->eta_n, f->eta_phys_n, f->VE_n, f->sxxd, f->szzd, f->sxz_n, f->eII_el, f->eII_pl,
+                            f->eII_pwl, f->eII_exp, f->eII_lin, f->eII_gbs, f->eII_cst, f->d_n, f->p_corr,
+                            f->div_u_el, f->div_u_pl, f->div_u_r, f->Wtot, f->Wel, f->Wdiss, f->X_n, f->OverS_n,
+                            md->density_variations == 1 ? f->rho_n : nullptr};
+  for (int i = 0; i < CO_rho; i++) if (!cout[i]) return MDZ_EINVAL;
+  if (md->density_variations == 1 && !f->rho_n) return MDZ_EINVAL;
+  double *vout[VO_COUNT] = {f->sxxd_s, f->szzd_s, f->sxz, f->eta_phys_s, f->eta_s, f->X_s,
+                            aniso ? f->VE_s : nullptr, f->T_s, f->P_s, f->d0_s, f->phi0_s};
+  for (int i = 0; i < VO_COUNT; i++) if (i != VO_VE && !vout[i]) return MDZ_EINVAL;
+  if (aniso && !f->VE_s) return MDZ_EINVAL;
+  for (int i = 0; i < CO_COUNT; i++) L.cout[i] = cout[i];
+  for (int i = 0; i < VO_COUNT; i++) L.vout[i] = vout[i];
+  return MDZ_OK;
+}
+
 int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat, const mdz_grid_fields *f,
                int final_update, int mem, int flags, mdz_sweep_stats *st, bool aniso, float *X = nullptr,
                float *Y = nullptr) {
@@ -273,28 +328,11 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   const size_t Nc = (size_t)A.M.Nc, Nv = (size_t)A.M.Nv;
   const int np = A.M.np;
   const bool host = (mem == MDZ_MEM_HOST);
-  // required inputs
-  const double *cin[CI_COUNT] = {f->mu_n, f->T, f->p_in, f->d0_n, f->phi0_n, f->X0_n, f->exxd, f->ezzd, f->exz_n,
-                                 f->sxxd0, f->szzd0, f->sxz0_n, f->fric_n, f->C_n, f->dil_n, f->p0_n, f->T0_n,
-                                 f->bet_n, f->d1_n, f->d2_n, f->angle_n, f->aniso_factor_n};
-  const double *vin[VI_COUNT] = {f->mu_s, f->X0_s, f->exxd_s, f->ezzd_s, f->exz, f->sxxd0_s, f->szzd0_s, f->sxz0,
-                                 f->fric_s, f->C_s, f->dil_s, f->p0_s, f->bet_s, f->d1_s, f->d2_s, f->angle_s,
-                                 f->aniso_factor_s};
-  const int nci = aniso ? CI_COUNT : CI_d1, nvi = aniso ? VI_COUNT : VI_d1;
-  for (int i = 0; i < nci; i++) if (!cin[i]) return MDZ_EINVAL;
-  for (int i = 0; i < nvi; i++) if (!vin[i]) return MDZ_EINVAL;
-  if (!f->phase_perc_n || !f->phase_perc_s || !f->phase_eta_n || !f->phase_eta_s || !f->BCp_type || !f->BCg_type)
-    return MDZ_EINVAL;
-  double *cout[CO_COUNT] = {f->eta_n, f->eta_phys_n, f->VE_n, f->sxxd, f->szzd, f->sxz_n, f->eII_el, f->eII_pl,
-                            f->eII_pwl, f->eII_exp, f->eII_lin, f->eII_gbs, f->eII_cst, f->d_n, f->p_corr,
-                            f->div_u_el, f->div_u_pl, f->div_u_r, f->Wtot, f->Wel, f->Wdiss, f->X_n, f->OverS_n,
-                            md->density_variations == 1 ? f->rho_n : nullptr};
-  for (int i = 0; i < CO_rho; i++) if (!cout[i]) return MDZ_EINVAL;
-  if (md->density_variations == 1 && !f->rho_n) return MDZ_EINVAL;
-  double *vout[VO_COUNT] = {f->sxxd_s, f->szzd_s, f->sxz, f->eta_phys_s, f->eta_s, f->X_s,
-                            aniso ? f->VE_s : nullptr, f->T_s, f->P_s, f->d0_s, f->phi0_s};
-  for (int i = 0; i < VO_COUNT; i++) if (i != VO_VE && !vout[i]) return MDZ_EINVAL;
-  if (aniso && !f->VE_s) return MDZ_EINVAL;
+  FieldLists L;
+  if ((rc = field_lists(md, f, aniso, L)) != MDZ_OK) return rc;
+  const double *const *cin = L.cin, *const *vin = L.vin;
+  double *const *cout = L.cout, *const *vout = L.vout;
+  const int nci = L.nci, nvi = L.nvi;
 
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
@@ -821,6 +859,146 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
     st->kernel_launches = n > 0 ? 1 : 0;
   }
   return status;
+}
+
+int mdz_rheo_batch_create(mdz_rheo_ctx *c, int n, const mdz_model *models, const mdz_materials *mats,
+                          const mdz_grid_fields *fields, int aniso, int final_update, int flags,
+                          mdz_rheo_batch **out) {
+  if (!c || !models || !mats || !fields || !out || n < 1 || n > kBatchMaxGrids) return MDZ_EINVAL;
+  if (flags & ~MDZ_SWEEP_REF_START) return MDZ_EINVAL;
+  *out = nullptr;
+  CK(cudaSetDevice(c->device));
+  std::vector<SweepArgs> h((size_t)n);
+  std::vector<long long> tile_start((size_t)n + 1, 0);
+  long long nodes = 0;
+  for (int g = 0; g < n; g++) {
+    SweepArgs &A = h[g];
+    memset(&A, 0, sizeof(A));
+    const mdz_model *md = models + g;
+    const mdz_materials *mt = mats + g;
+    const mdz_grid_fields *f = fields + g;
+    if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
+    int rc = fold_model(md, mt, A.M);
+    if (rc != MDZ_OK) return rc;
+    for (int p = 0; p < A.M.np; p++) fold_phase(mt, md, p, A.ph[p]);
+    FieldLists L;
+    if ((rc = field_lists(md, f, aniso != 0, L)) != MDZ_OK) return rc;
+    for (int i = 0; i < L.nci; i++) A.ci[i] = L.cin[i];
+    for (int i = 0; i < L.nvi; i++) A.vi[i] = L.vin[i];
+    for (int i = 0; i < CO_COUNT; i++) A.co[i] = L.cout[i];
+    for (int i = 0; i < VO_COUNT; i++) A.vo[i] = L.vout[i];
+    for (int p = 0; p < A.M.np; p++) {
+      A.perc_n[p] = f->phase_perc_n[p];
+      A.perc_s[p] = f->phase_perc_s[p];
+      A.peta_n[p] = f->phase_eta_n[p];
+      A.peta_s[p] = f->phase_eta_s[p];
+      if (!A.perc_n[p] || !A.perc_s[p] || !A.peta_n[p] || !A.peta_s[p]) return MDZ_EINVAL;
+    }
+    A.bcp = f->BCp_type;
+    A.bcg = f->BCg_type;
+    A.stats = c->d_stats;
+    A.final_update = final_update;
+    A.need_lnd = need_lnd(mt, A.M.np);
+    A.polish = (flags & MDZ_SWEEP_REF_START) ? 0 : c->polish_iters;
+    A.node_base = nodes;
+    const long long ng = A.M.Nc + A.M.Nv;
+    nodes += ng;
+    tile_start[g + 1] = tile_start[g] + (ng + kBatchTile - 1) / kBatchTile;
+  }
+  mdz_rheo_batch *b = new mdz_rheo_batch();
+  b->ctx = c;
+  b->n = n;
+  b->aniso = aniso != 0;
+  b->nodes = nodes;
+  b->tiles = tile_start[n];
+  if (cudaMalloc(&b->d_grids, sizeof(SweepArgs) * n) != cudaSuccess ||
+      cudaMalloc(&b->d_tile_start, sizeof(long long) * (n + 1)) != cudaSuccess ||
+      cudaMemcpy(b->d_grids, h.data(), sizeof(SweepArgs) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_tile_start, tile_start.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice) !=
+          cudaSuccess) {
+    mdz_rheo_batch_destroy(b);
+    return MDZ_ECUDA;
+  }
+  b->args.grids = b->d_grids;
+  b->args.tile_start = b->d_tile_start;
+  b->args.n = n;
+  b->args.tiles = b->tiles;
+  b->args.stats = c->d_stats;
+  b->grid = (int)std::min<long long>(b->tiles, 0x7fffffffLL);
+  *out = b;
+  return MDZ_OK;
+}
+
+int mdz_rheo_batch_destroy(mdz_rheo_batch *b) {
+  if (!b) return MDZ_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->d_grids) cudaFree(b->d_grids);
+  if (b->d_tile_start) cudaFree(b->d_tile_start);
+  delete b;
+  return MDZ_OK;
+}
+
+int mdz_rheo_batch_sweep(mdz_rheo_batch *b, mdz_sweep_stats *st) {
+  if (!b) return MDZ_EINVAL;
+  mdz_rheo_ctx *c = b->ctx;
+  CK(cudaSetDevice(c->device));
+  int rc = reset_stats(c);
+  if (rc != MDZ_OK) return rc;
+  c->h2d = c->d2h = 0;
+  c->launches = 1;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(launch_sweep_batch(b->args, b->aniso, c->stream, b->grid));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  return finish(c, st);
+}
+
+int mdz_rheo_batch_capture(mdz_rheo_batch *b, int nsweeps, double amp, uint64_t seed) {
+  if (!b || nsweeps < 1 || nsweeps > 100000 || !(amp >= 0.0 && amp < 1.0)) return MDZ_EINVAL;
+  mdz_rheo_ctx *c = b->ctx;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+  if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaMemsetAsync(c->d_stats, 0, sizeof(DevStats), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_stats->err_key, 0xff, sizeof(c->d_stats->err_key), c->stream);
+  for (int s = 0; s < nsweeps && e == cudaSuccess; s++) {
+    if (amp != 0.0) e = launch_perturb_batch(b->args, amp, (unsigned long long)seed, s, c->stream, b->grid);
+    if (e == cudaSuccess) e = launch_sweep_batch(b->args, b->aniso, c->stream, b->grid);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return MDZ_ECUDA;
+  }
+  b->graph = g;
+  if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    b->graph = nullptr;
+    b->exec = nullptr;
+    return MDZ_ECUDA;
+  }
+  b->graph_sweeps = nsweeps;
+  b->graph_launches = nsweeps * (amp != 0.0 ? 2 : 1);
+  return MDZ_OK;
+}
+
+int mdz_rheo_batch_launch(mdz_rheo_batch *b, mdz_sweep_stats *st) {
+  if (!b) return MDZ_EINVAL;
+  if (!b->exec) return MDZ_ENOTREADY;
+  mdz_rheo_ctx *c = b->ctx;
+  CK(cudaSetDevice(c->device));
+  c->h2d = c->d2h = 0;
+  c->launches = (unsigned)b->graph_launches;
+  CK(cudaEventRecord(c->ev0, c->stream));
+  CK(cudaGraphLaunch(b->exec, c->stream));
+  CK(cudaEventRecord(c->ev1, c->stream));
+  return finish(c, st);
 }
 
 int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {

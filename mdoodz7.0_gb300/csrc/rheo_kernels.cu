@@ -191,7 +191,7 @@ __device__ __forceinline__ void node_store(const SweepArgs &A, const Node &n, do
       out[CO_szzd] = eta2 * (in.Ezz * (1.0 - a * d1) + in.Exx * a * d1 + 2.0 * in.Exz * a * d2);
       out[CO_sxz] = eta2 * (-in.Exx * a * d2 + in.Ezz * a * d2 + 2 * in.Exz * (a * (d1 - 0.5) + 0.5));
     }
-    record_error(A.stats, n.centroid ? n.idx : M.Nc + n.idx, status);
+    record_error(A.stats, A.node_base + (n.centroid ? n.idx : M.Nc + n.idx), status);
   } else {
     for (int p = 0; p < M.np; p++) node_iters(A, n, p, 0);
   }
@@ -228,41 +228,114 @@ __device__ __forceinline__ void flush_acc(DevStats *st, Acc &acc) {
 // ---------------------------------------------------------------------------------
 // plain sweep: one thread per node
 // ---------------------------------------------------------------------------------
+// One node of one grid: prepare, every active phase's local solve, averaging, store.
+template <bool ANISO>
+__device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc &acc) {
+  Node n;
+  node_prepare<ANISO>(A, i, n);
+  double out[CO_COUNT];
+#pragma unroll
+  for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
+  int status = MDZ_OK;
+  if (n.solid) {
+    for (int p = 0; p < A.M.np; p++) {
+      const double perc = node_perc(A, n, p);
+      if (!(fabs(perc) > 1e-13)) {  // :1210-1212
+        node_iters(A, n, p, 0);
+        continue;
+      }
+      PointOut o;
+      if (ANISO) point_aniso(A.M, A.ph[p], n.in, n.ctx, n.an, A.polish, o);
+      else point_iso(A.M, A.ph[p], n.in, n.ctx, A.polish, o);
+      node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
+    }
+  }
+  node_store<ANISO>(A, n, out, status);
+}
+
 template <bool ANISO>
 __global__ void __launch_bounds__(128) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0};
   const long long total = A.M.Nc + A.M.Nv;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-    Node n;
-    node_prepare<ANISO>(A, i, n);
-    double out[CO_COUNT];
-#pragma unroll
-    for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
-    int status = MDZ_OK;
-    if (n.solid) {
-      for (int p = 0; p < A.M.np; p++) {
-        const double perc = node_perc(A, n, p);
-        if (!(fabs(perc) > 1e-13)) {  // :1210-1212
-          node_iters(A, n, p, 0);
-          continue;
-        }
-        PointOut o;
-        if (ANISO) point_aniso(A.M, A.ph[p], n.in, n.ctx, n.an, A.polish, o);
-        else point_iso(A.M, A.ph[p], n.in, n.ctx, A.polish, o);
-        node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
-      }
-    }
-    node_store<ANISO>(A, n, out, status);
-  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride)
+    sweep_node<ANISO>(A, i, acc);
   flush_acc(A.stats, acc);
+}
+
+// ---------------------------------------------------------------------------------
+// many grids in one launch: the node range of every grid is cut into tiles of
+// kBatchTile nodes, so a CTA's tile lies in one grid; the grid's arguments are read
+// from global memory (uniform over the CTA, served by L1)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ int batch_grid_of(const BatchArgs &B, long long tile) {
+  int lo = 0, hi = B.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&B.tile_start[mid]) <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <bool ANISO>
+__global__ void __launch_bounds__(kBatchTile) k_sweep_batch(const __grid_constant__ BatchArgs B) {
+  Acc acc = {0, 0, 0, 0};
+  for (long long t = blockIdx.x; t < B.tiles; t += gridDim.x) {
+    const int g = batch_grid_of(B, t);
+    const SweepArgs &A = B.grids[g];
+    const long long i = (t - __ldg(&B.tile_start[g])) * kBatchTile + threadIdx.x;
+    if (i < A.M.Nc + A.M.Nv) sweep_node<ANISO>(A, i, acc);
+  }
+  flush_acc(B.stats, acc);
+}
+
+// Multiplicative perturbation of the strain-rate inputs of every grid of a batch:
+// x <- x (1 + amp u), u uniform in [-1, 1) from a counter hash (SplitMix64, Steele et
+// al. 2014) of (seed, sweep, grid, node, component).  Rounded steps without
+// contraction, so a host restatement reproduces the values exactly.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double perturb_factor(unsigned long long key, long long node, int comp, double amp) {
+  const unsigned long long h = splitmix64(key ^ (unsigned long long)(node * 3 + comp));
+  const double u = __dsub_rn(__dmul_rn((double)(h >> 11), 0x1.0p-52), 1.0);  // [-1, 1)
+  return __dadd_rn(1.0, __dmul_rn(amp, u));
+}
+
+__global__ void __launch_bounds__(kBatchTile) k_perturb_batch(const __grid_constant__ BatchArgs B, double amp,
+                                                             unsigned long long seed, int sweep) {
+  for (long long t = blockIdx.x; t < B.tiles; t += gridDim.x) {
+    const int g = batch_grid_of(B, t);
+    const SweepArgs &A = B.grids[g];
+    const long long i = (t - __ldg(&B.tile_start[g])) * kBatchTile + threadIdx.x;
+    const long long Nc = A.M.Nc;
+    if (i >= Nc + A.M.Nv) continue;
+    const unsigned long long key = splitmix64(splitmix64(seed ^ (unsigned long long)sweep) ^ (unsigned long long)g);
+    double *x[3];
+    if (i < Nc) {
+      x[0] = const_cast<double *>(A.ci[CI_exxd]) + i;
+      x[1] = const_cast<double *>(A.ci[CI_ezzd]) + i;
+      x[2] = const_cast<double *>(A.ci[CI_exz]) + i;
+    } else {
+      x[0] = const_cast<double *>(A.vi[VI_exxd]) + (i - Nc);
+      x[1] = const_cast<double *>(A.vi[VI_ezzd]) + (i - Nc);
+      x[2] = const_cast<double *>(A.vi[VI_exz]) + (i - Nc);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) *x[k] = __dmul_rn(*x[k], perturb_factor(key, i, k, amp));
+  }
 }
 
 // ---------------------------------------------------------------------------------
 // tiled sweep with a block-wide stage per phase (learned warm start / data collection)
 // ---------------------------------------------------------------------------------
 template <bool ANISO, int MODE>
-__global__ void __launch_bounds__(128) k_sweep_tiles(const __grid_constant__ SweepArgs A,
+__global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ SweepArgs A,
                                                      const __grid_constant__ WarmArgs W) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   MlpShared &S = *reinterpret_cast<MlpShared *>(smem_raw);
@@ -399,12 +472,22 @@ cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int blo
   return cudaGetLastError();
 }
 
+// The warm-start form keeps its MLP tiles in dynamic shared memory; asking for the
+// largest shared-memory carve-out lets two of its CTAs share an SM (the register file
+// allows two), which the occupancy query then reports.
+template <bool ANISO, int MODE>
+static void tiles_attributes() {
+  if (MODE != MODE_WARM) return;
+  auto fn = k_sweep_tiles<ANISO, MODE>;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpShared));
+  cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+}
+
 template <bool ANISO, int MODE>
 static cudaError_t launch_tiles_t(const SweepArgs &a, const WarmArgs &w, cudaStream_t s, int grid) {
   const size_t smem = (MODE == MODE_WARM) ? sizeof(MlpShared) : 0;
-  auto fn = k_sweep_tiles<ANISO, MODE>;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  fn<<<grid, kMlpTile, smem, s>>>(a, w);
+  tiles_attributes<ANISO, MODE>();
+  k_sweep_tiles<ANISO, MODE><<<grid, kMlpTile, smem, s>>>(a, w);
   return cudaGetLastError();
 }
 
@@ -430,8 +513,26 @@ int tiles_blocks_per_sm(bool aniso, int mode) {
     default: fn = (const void *)k_sweep_tiles<true, MODE_WARM>; break;
   }
   const size_t smem = (mode == MODE_WARM) ? sizeof(MlpShared) : 0;
+  if (mode == MODE_WARM) {
+    if (aniso) tiles_attributes<true, MODE_WARM>();
+    else tiles_attributes<false, MODE_WARM>();
+  }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kMlpTile, smem);
   return n > 0 ? n : 1;
+}
+
+cudaError_t launch_sweep_batch(const BatchArgs &b, bool aniso, cudaStream_t s, int grid) {
+  if (grid < 1) grid = 1;
+  if (aniso) k_sweep_batch<true><<<grid, kBatchTile, 0, s>>>(b);
+  else k_sweep_batch<false><<<grid, kBatchTile, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_perturb_batch(const BatchArgs &b, double amp, unsigned long long seed, int sweep, cudaStream_t s,
+                                 int grid) {
+  if (grid < 1) grid = 1;
+  k_perturb_batch<<<grid, kBatchTile, 0, s>>>(b, amp, seed, sweep);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s) {

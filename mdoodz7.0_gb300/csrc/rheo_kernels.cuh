@@ -52,6 +52,18 @@ struct SweepArgs {
   DevStats *stats;
   int final_update, need_lnd;
   int polish;  // FP32 Newton steps before each FP64 local solve (0: the reference's start)
+  long long node_base;  // added to node indices in error reports (batched grids)
+};
+
+// Many grids in one launch.  Grid g owns tiles [tile_start[g], tile_start[g + 1]) of
+// kBatchTile nodes (centroids first, then vertices, as in one sweep).
+constexpr int kBatchTile = 128;
+struct BatchArgs {
+  const SweepArgs *grids;       // device array [n]
+  const long long *tile_start;  // device array [n + 1]
+  int n;
+  long long tiles;
+  DevStats *stats;
 };
 
 struct PointArgs {
@@ -67,6 +79,9 @@ struct PointArgs {
 
 cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap);
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s);
+cudaError_t launch_sweep_batch(const BatchArgs &b, bool aniso, cudaStream_t s, int grid);
+cudaError_t launch_perturb_batch(const BatchArgs &b, double amp, unsigned long long seed, int sweep, cudaStream_t s,
+                                 int grid);
 cudaError_t launch_sweep_tiles(const SweepArgs &a, const WarmArgs &w, bool aniso, int mode, cudaStream_t s,
                                int grid);
 int tiles_blocks_per_sm(bool aniso, int mode);

@@ -266,6 +266,13 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_points_static.argtypes = [C.POINTER(Model), C.POINTER(Materials), C.POINTER(PointInputs),
                                            C.POINTER(PointOutputs), C.c_int64, C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(SweepStats)]
+    lib.mdz_rheo_batch_create.argtypes = [C.c_void_p, C.c_int, C.POINTER(Model), C.POINTER(Materials),
+                                          C.POINTER(GridFields), C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_void_p)]
+    lib.mdz_rheo_batch_destroy.argtypes = [C.c_void_p]
+    lib.mdz_rheo_batch_sweep.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
+    lib.mdz_rheo_batch_capture.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_uint64]
+    lib.mdz_rheo_batch_launch.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
     lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
     lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SweepStats)]
@@ -326,6 +333,76 @@ def math_selftest(x: np.ndarray, device: int = 0):
 def python_struct_sizes():
     return [C.sizeof(Materials), C.sizeof(Model), C.sizeof(GridFields), C.sizeof(SweepStats),
             C.sizeof(PointInputs), C.sizeof(PointOutputs)]
+
+
+class Batch:
+    """Many device-resident grids swept by one launch (mdz_rheo_batch_*).  `fieldsets` are
+    FieldSets over device tensors; they (and their tensors) must outlive the batch."""
+
+    def __init__(self, ctx: "Context", models, mats, fieldsets, aniso=False, final_update=0, flags=0):
+        n = len(models)
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self._keep = list(fieldsets)
+        self._models = (Model * n)(*models)
+        self._mats = (Materials * n)(*mats)
+        self._fields = (GridFields * n)(*[fs.struct for fs in fieldsets])
+        h = C.c_void_p()
+        rc = self.lib.mdz_rheo_batch_create(ctx.handle, n, self._models, self._mats, self._fields, int(aniso),
+                                            final_update, flags, C.byref(h))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_batch_create")
+        self.handle = h
+
+    def sweep(self, check=True):
+        st = SweepStats()
+        rc = self.lib.mdz_rheo_batch_sweep(self.handle, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_batch_sweep")
+        return rc, st
+
+    def capture(self, nsweeps: int, amp: float = 0.0, seed: int = 0):
+        rc = self.lib.mdz_rheo_batch_capture(self.handle, nsweeps, amp, seed)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_batch_capture")
+
+    def launch(self, check=True):
+        st = SweepStats()
+        rc = self.lib.mdz_rheo_batch_launch(self.handle, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_batch_launch")
+        return rc, st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.mdz_rheo_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def perturb_reference(x: np.ndarray, amp: float, seed: int, sweep: int, grid: int, comp: int,
+                      node_offset: int = 0) -> np.ndarray:
+    """Host statement of the batch strain-rate perturbation (mdz_rheo_batch_capture):
+    x * (1 + amp u) with u from SplitMix64; node index = node_offset + position."""
+    M = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+    def sm(z):
+        z = (np.asarray(z, np.uint64) + np.uint64(0x9e3779b97f4a7c15)) & M
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xbf58476d1ce4e5b9)) & M
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94d049bb133111eb)) & M
+        return z ^ (z >> np.uint64(31))
+
+    with np.errstate(over="ignore"):
+        key = sm(sm(np.uint64(seed) ^ np.uint64(sweep)) ^ np.uint64(grid))
+        node = np.arange(x.size, dtype=np.uint64) + np.uint64(node_offset)
+        h = sm(key ^ (node * np.uint64(3) + np.uint64(comp)))
+    u = (h >> np.uint64(11)).astype(np.float64) * 2.0 ** -52 - 1.0
+    return x * (1.0 + amp * u)
 
 
 class Context:

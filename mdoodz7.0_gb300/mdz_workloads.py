@@ -406,3 +406,20 @@ def aniso(seed: int = 4, ncx: int = 4097, ncz: Optional[int] = None, sc: Scale =
         set_power_law(m, p, sc=sc, **laws[p % 3])
     return grid_workload("aniso", ncx, ncz, m, seed, sc=sc, softening=(30.0, 5.0, 0.0, 1.0),
                          aniso=True)
+
+
+def many_grids(seed: int = 7, n: int = 64, lo: int = 65, hi: int = 1025, sc: Scale = SI) -> List[Workload]:
+    """Many independent grids of uneven size for one batched launch: cells per side
+    log-uniform in [lo, hi], 2-5 phases drawn from the large plain workload's five,
+    dt log-uniform in 1e10-1e12 s, each grid with its own seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for g in range(n):
+        side = int(round(float(loguniform(rng, lo, hi, 1)[0])))
+        nph = int(rng.integers(2, 6))
+        ids = sorted(rng.choice(len(PLAIN_LARGE_PHASES), size=nph, replace=False).tolist())
+        dt = float(loguniform(rng, 1e10, 1e12, 1)[0])
+        mat = materials_plain_large(nph, sc, phase_ids=ids)
+        out.append(grid_workload("many_grids", side, side, mat, seed * 1000 + g, dt=dt, sc=sc,
+                                 grain_size=(1e-5, 1e-2), softening=(30.0, 5.0, 0.0, 1.0)))
+    return out

@@ -24,13 +24,13 @@ def test_exp_accuracy():
                         [0.0, -0.0, 1e-300, -1e-300, 700.0, -700.0, 709.78, -745.2, 710.0, -746.0,
                          np.inf, -np.inf, np.nan]])
     fe, ce, _, _ = R.math_selftest(x)
-    fin = np.isfinite(ce) & (ce > 1e-300)
-    u_cuda = ulps(fe[fin], ce[fin])
-    u_np = ulps(fe[fin], np.exp(x[fin]))
+    # the table path serves |x| < 700; everything else is CUDA's exp itself
+    fast = np.isfinite(x) & (np.abs(x) < 700.0)
+    u_cuda = ulps(fe[fast], ce[fast])
+    u_np = ulps(fe[fast], np.exp(x[fast]))
     print("exp: max ulp vs CUDA", u_cuda.max(), "vs numpy", u_np.max(), "mean", u_np.mean())
     assert u_cuda.max() <= 2.0 and u_np.max() <= 2.0
-    special = ~fin
-    assert np.array_equal(fe[special], ce[special], equal_nan=True)
+    assert np.array_equal(fe[~fast], ce[~fast], equal_nan=True)
 
 
 def test_log_accuracy():
