@@ -297,6 +297,25 @@ int mdz_rheo_batch_capture(mdz_rheo_batch *batch, int nsweeps, double amp, uint6
 /* Launch the captured graph on the context's stream and wait for it. */
 int mdz_rheo_batch_launch(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
 
+/* ---- launch-shape autotuner (no reference counterpart) -----------------
+ * Times the sweep kernel on the caller's own device-resident grid (MDZ_MEM_DEVICE
+ * fields; final_update 0) for every candidate launch shape and keeps the fastest for
+ * later sweeps of that kind (aniso 0/1) on this context.  Candidates, in this order:
+ * 128 then 64 threads per block; for each, one thread per node, then a persistent grid
+ * of 1, 2, 4 or 8 waves of the CTAs resident per SM.  Each candidate runs one warm-up
+ * and `reps` timed sweeps; ms_out (may be NULL) receives MDZ_AUTOTUNE_CANDIDATES mean
+ * kernel times and best_out (may be NULL) the chosen index.  The shape changes no result
+ * bit: every node is computed by one thread, independently of the others.  `flags` may
+ * hold MDZ_SWEEP_REF_START only.  The tuned sweeps overwrite the grid's outputs with the
+ * values one sweep produces. */
+#define MDZ_AUTOTUNE_CANDIDATES 10
+int mdz_rheo_autotune(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                      const mdz_grid_fields *f, int aniso, int flags, int reps, double *ms_out,
+                      int *best_out);
+/* The launch shape sweeps of this kind use now: threads per block and the grid cap
+ * (0: one thread per node). */
+int mdz_rheo_get_launch_shape(mdz_rheo_ctx *ctx, int aniso, int *block, int *grid_cap);
+
 /* Per-(phase, node) VE local iteration counts of the last sweep run with
  * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
  * inactive.  Host buffers. */

@@ -37,7 +37,7 @@ struct mdz_rheo_ctx {
   int last_np = 0, have_iters = 0, pending = 0;
   unsigned long long h2d = 0, d2h = 0;
   unsigned launches = 0;
-  int block = 128, grid_cap = 0;
+  int block[2] = {128, 128}, grid_cap[2] = {0, 0};  // launch shape of k_sweep, [iso, aniso]
   int sms = 0;
   // learned warm start
   void *warm_buf = nullptr;  // tiles W1, W2, W3 + biases b1, b2, b3[16]
@@ -144,6 +144,7 @@ void fold_phase(const mdz_materials *m, const mdz_model *md, int p, PhaseConst &
     c.exp_n = m->nexp[p];
     c.exp_lnA0 = kLnSqrt3 - kLn2 + log(m->Eexp[p]) + (m->nexp[p] != 0.0 ? m->nexp[p] * log(gS) : 0.0);
     c.exp_s3gS = kSqrt3 / gS;
+    c.exp_ln_s3gS = log(c.exp_s3gS);
   }
   c.eta0 = m->eta0[p];
   const int p2 = m->phase_two[p];
@@ -177,6 +178,7 @@ int fold_model(const mdz_model *md, const mdz_materials *m, ModelConst &M) {
   M.Tiimin = 1e5 / md->scale_S;
   M.Eii_floor = 1e-30 / md->scale_E;
   M.eta_up0 = 1.0e100 / md->scale_eta;
+  M.ln_eta_up0 = log(M.eta_up0);
   M.eta_lo0 = -1.0e100 / md->scale_eta;
   M.d_min = 1e-13 / md->scale_L;
   for (int p = 0; p < M.np; p++) {
@@ -386,7 +388,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (mode < 0) {
-    CK(launch_sweep(A, aniso, ctx->stream, ctx->block, ctx->grid_cap));
+    CK(launch_sweep(A, aniso, ctx->stream, ctx->block[aniso], ctx->grid_cap[aniso]));
   } else {
     WarmArgs W;
     memset(&W, 0, sizeof(W));
@@ -999,6 +1001,58 @@ int mdz_rheo_batch_launch(mdz_rheo_batch *b, mdz_sweep_stats *st) {
   CK(cudaGraphLaunch(b->exec, c->stream));
   CK(cudaEventRecord(c->ev1, c->stream));
   return finish(c, st);
+}
+
+int mdz_rheo_autotune(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m, const mdz_grid_fields *f,
+                      int aniso, int flags, int reps, double *ms_out, int *best_out) {
+  if (!c || !md || !m || !f || reps < 1 || reps > 1000) return MDZ_EINVAL;
+  if (flags & (MDZ_SWEEP_ASYNC | MDZ_SWEEP_WARMSTART | MDZ_SWEEP_ITERS)) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  const int a = aniso ? 1 : 0;
+  const int blocks[2] = {128, 64};
+  const int waves[5] = {0, 1, 2, 4, 8};  // 0: one thread per node
+  int regs = 0, smem = 0;
+  double best_ms = 1e300;
+  int best = 0, cand = 0;
+  const int keep_block = c->block[a], keep_cap = c->grid_cap[a];
+  for (int bi = 0; bi < 2; bi++) {
+    int occ = 0;
+    sweep_kernel_info(a, &regs, &smem, &occ, blocks[bi]);
+    for (int wi = 0; wi < 5; wi++, cand++) {
+      c->block[a] = blocks[bi];
+      c->grid_cap[a] = waves[wi] ? c->sms * (occ > 0 ? occ : 1) * waves[wi] : 0;
+      double sum = 0.0;
+      mdz_sweep_stats st;
+      for (int r = 0; r <= reps; r++) {  // the first is a warm-up
+        const int rc = sweep_impl(c, md, m, f, 0, MDZ_MEM_DEVICE, flags, &st, aniso != 0);
+        if (rc != MDZ_OK) {
+          c->block[a] = keep_block;
+          c->grid_cap[a] = keep_cap;
+          return rc;
+        }
+        if (r > 0) sum += st.elapsed_ms;
+      }
+      const double ms = sum / reps;
+      if (ms_out) ms_out[cand] = ms;
+      if (ms < best_ms) { best_ms = ms; best = cand; }
+    }
+  }
+  {
+    int occ = 0;
+    const int bi = best / 5, wi = best % 5;
+    sweep_kernel_info(a, &regs, &smem, &occ, blocks[bi]);
+    c->block[a] = blocks[bi];
+    c->grid_cap[a] = waves[wi] ? c->sms * (occ > 0 ? occ : 1) * waves[wi] : 0;
+  }
+  if (best_out) *best_out = best;
+  return MDZ_OK;
+}
+
+int mdz_rheo_get_launch_shape(mdz_rheo_ctx *c, int aniso, int *block, int *grid_cap) {
+  if (!c || !block || !grid_cap) return MDZ_EINVAL;
+  *block = c->block[aniso ? 1 : 0];
+  *grid_cap = c->grid_cap[aniso ? 1 : 0];
+  return MDZ_OK;
 }
 
 int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {

@@ -170,9 +170,10 @@ __device__ __forceinline__ void warm_features(const ModelConst &M, const NodeIn 
   f[3] = (in.d > 0.0) ? __logf((float)(in.d * M.scale_L)) : -20.0f;
   f[4] = c.elastic ? __logf((float)c.eta_el / eta_up) : 0.0f;
   const float lo = -40.0f;
-  f[5] = (S.L.inv[K_PWL] > 0.0) ? fmaxf(__logf(eta_up * (float)S.L.inv[K_PWL]), lo) : lo;
-  f[6] = (S.L.inv[K_EXP] > 0.0) ? fmaxf(__logf(eta_up * (float)S.L.inv[K_EXP]), lo) : lo;
-  f[7] = (S.L.inv[K_LIN] > 0.0) ? fmaxf(__logf(eta_up * (float)S.L.inv[K_LIN]), lo) : lo;
+  // ln(eta_up / eta_k), formed in FP64 from the logarithms the solve carries
+#pragma unroll
+  for (int k = 0; k < K_COUNT; k++)
+    f[5 + k] = (S.L.ln_inv[k] > -kInf) ? fmaxf((float)(S.ln_eta_up + S.L.ln_inv[k]), lo) : lo;
   f[8] = (S.L.mech & F_CST) ? fmaxf(__logf(eta_up / (float)S.eta_cst), lo) : lo;
   // stress memory: the share of the effective strain rate carried by the old stress
   const float T0 = sqrtf(0.5f * ((float)in.Txx0 * (float)in.Txx0 + (float)in.Tzz0 * (float)in.Tzz0 +

@@ -33,6 +33,7 @@ namespace mdz {
 
 constexpr double kZeroC = 273.15;                 // MDLIB/include/mdoodz.h:4
 constexpr double kLn2 = 0.69314718055994530942;
+constexpr double kInf = __builtin_huge_val();
 constexpr double kLnSqrt3 = 0.54930614433405484570;  // log(sqrt(3))
 constexpr double kSqrt3 = 1.73205080756887729353;
 
@@ -66,7 +67,7 @@ struct PhaseConst {
   // grain-boundary sliding (bracket only: C_gbs is never set by the reference)
   double gbs_n, gbs_invn, gbs_lnK, gbs_Q, gbs_V, gbs_invRn, gbs_m, gbs_mn, gbs_an;
   // Peierls: ST = EaR g2 / T; Eii_exp = exp(lnA0 - EaR om2 / T) (s3gS Tii)^(ST+n)
-  double exp_EaR, exp_g2, exp_om2, exp_n, exp_lnA0, exp_s3gS;
+  double exp_EaR, exp_g2, exp_om2, exp_n, exp_lnA0, exp_s3gS, exp_ln_s3gS;
   // constant viscosity
   double eta0, eta0_two;
   // plasticity
@@ -83,7 +84,7 @@ struct ModelConst {
   long long Nc, Nv;
   double dt, dt_model, min_eta, max_eta, eta_tol, R;
   double scale_eta, scale_L, scale_T, scale_S, scale_E;
-  double TmaxPeierls, Tmin, Tiimin, Eii_floor, eta_up0, eta_lo0, d_min;
+  double TmaxPeierls, Tmin, Tiimin, Eii_floor, eta_up0, ln_eta_up0, eta_lo0, d_min;
 };
 
 // Per-node values shared by all phases of one node.
@@ -97,6 +98,7 @@ struct NodeIn {
 struct NodeCtx {
   double Eii, lnEii, T, Traw, invT, lnd, K, G, dil, eta_el, inv_eta_el, sin_fric, cos_fric, sin_dil;
   double inv2Eii, inv_Kdt, inv_d;
+  double ln_eta_el;         // ln(eta_el), set where elasticity is on
   int elastic, plastic_on;  // plastic_on = (step != 0)
 };
 
@@ -139,6 +141,7 @@ __device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn
   if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; c.K = 1e10; }
   c.eta_el = c.G * M.dt;
   c.inv_eta_el = 1.0 / c.eta_el;
+  c.ln_eta_el = c.elastic ? fast_log(c.eta_el) : 0.0;
   c.inv_Kdt = 1.0 / (c.K * M.dt);
   node_common(M, in, need_lnd, c);
 }
@@ -170,28 +173,32 @@ __device__ __forceinline__ double density(const ModelConst &M, const PhaseConst 
 enum { K_PWL = 0, K_EXP = 1, K_LIN = 2, K_COUNT = 3 };
 
 struct Laws {
-  int mech;            // F_CST | F_PWL | F_EXPV (active) | F_LIN | F_GBS
-  double inv[K_COUNT]; // 1/eta_k at the node's Eii (0 where inactive)
-  double n[K_COUNT];   // exponents n_pwl, ST + n_exp, n_lin
-  double lnB_pwl, lnB_lin, lnA_exp, ST, inv_gbs;
+  int mech;               // F_CST | F_PWL | F_EXPV (active) | F_LIN | F_GBS
+  double ln_inv[K_COUNT]; // ln(1/eta_k) at the node's Eii (-inf where inactive)
+  double n[K_COUNT];      // exponents n_pwl, ST + n_exp, n_lin
+  double lnB_pwl, lnB_lin, lnA_exp, ST, ln_inv_gbs;
 };
+
+// 1/eta_k itself, where a caller needs it in linear form
+__device__ __forceinline__ double law_inv(const Laws &L, int k) { return fast_exp(L.ln_inv[k]); }
 
 __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst &ph, const NodeCtx &c, double P,
                                            double phi, double lnd, int peierls, Laws &L) {
   const int fl = ph.flags;
   L.mech = (fl & (F_CST | F_PWL | F_LIN | F_GBS)) | (peierls ? F_EXPV : 0);
-  L.inv[0] = L.inv[1] = L.inv[2] = 0.0;
+  L.ln_inv[0] = L.ln_inv[1] = L.ln_inv[2] = -kInf;
   L.n[0] = ph.pwl_n; L.n[1] = 0.0; L.n[2] = ph.lin_n;
-  L.lnB_pwl = L.lnB_lin = L.lnA_exp = L.ST = L.inv_gbs = 0.0;
-  const double Eii = c.Eii, lnEii = c.lnEii;
+  L.lnB_pwl = L.lnB_lin = L.lnA_exp = L.ST = 0.0;
+  L.ln_inv_gbs = -kInf;
+  const double lnEii = c.lnEii;
   if (fl & F_PWL) {
-    // B = pref F A^(-1/n) fast_exp((Q+PV)/(RnT)) d^(m/n) f^(-r/n) fast_exp(-a phi/n);
-    // 1/eta_pwl = Eii^(1-1/n) / B = Eii fast_exp(-lnB - lnEii/n)
+    // B = pref F A^(-1/n) exp((Q+PV)/(RnT)) d^(m/n) f^(-r/n) exp(-a phi/n);
+    // 1/eta_pwl = Eii^(1-1/n) / B:  ln(1/eta_pwl) = lnEii - lnEii/n - lnB
     double lnB = ph.pwl_lnK + (ph.pwl_Q + P * ph.pwl_V) * ph.pwl_invRn * c.invT;
     if (fl & F_PWL_M) lnB += ph.pwl_mn * lnd;
     if (fl & F_PWL_A) lnB -= ph.pwl_an * phi;
     L.lnB_pwl = lnB;
-    L.inv[K_PWL] = Eii * fast_exp(-fma(lnEii, ph.pwl_invn, lnB));
+    L.ln_inv[K_PWL] = lnEii - fma(lnEii, ph.pwl_invn, lnB);
   }
   if (fl & F_LIN) {
     // 1/eta_lin = Eii^(1-1/n) / (B d^(m/n))
@@ -199,37 +206,41 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
     if (fl & F_LIN_A) lnB -= ph.lin_an * phi;
     L.lnB_lin = lnB;
     const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, lnB) : lnB;
-    L.inv[K_LIN] = Eii * fast_exp(-fma(lnEii, ph.lin_invn, lnBd));
+    L.ln_inv[K_LIN] = lnEii - fma(lnEii, ph.lin_invn, lnBd);
   }
   if (peierls) {
-    // Eii_fast_exp(Tii) = A (sqrt3 Tii / (gamma S))^nE, A = (sqrt3/2) E Arr (gamma S)^n;
+    // Eii_exp(Tii) = A (sqrt3 Tii / (gamma S))^nE, A = (sqrt3/2) E Arr (gamma S)^n;
     // isolated: Tii* = (gamma S / sqrt3) (Eii/A)^(1/nE), 1/eta_exp = 2 Eii / Tii*
     L.ST = ph.exp_EaR * c.invT * ph.exp_g2;
     const double nE = L.ST + ph.exp_n;
     L.n[K_EXP] = nE;
     L.lnA_exp = ph.exp_lnA0 - ph.exp_EaR * ph.exp_om2 * c.invT;
-    L.inv[K_EXP] = 2.0 * Eii * ph.exp_s3gS * fast_exp(-(lnEii - L.lnA_exp) / nE);
+    L.ln_inv[K_EXP] = (kLn2 + ph.exp_ln_s3gS + lnEii) - (lnEii - L.lnA_exp) / nE;
   }
   if (fl & F_GBS) {
     double lnB = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * phi;
     if (ph.gbs_m != 0.0) lnB += ph.gbs_mn * lnd;
-    L.inv_gbs = Eii * fast_exp(-fma(lnEii, ph.gbs_invn, lnB));
+    L.ln_inv_gbs = lnEii - fma(lnEii, ph.gbs_invn, lnB);
   }
 }
 
 // ---------------------------------------------------------------------------------------
 // Local VE residual  r(eta) = Eii - el Tii/(2 eta_el) - sum_k Eii_k(eta),  Tii = 2 eta Eii
-// (LocalIterationViscoElastic, RheologyDensity.c:152-197).  Linear terms (elasticity,
-// constant viscosity, Newtonian laws) are eta * a_k; non-linear ones
-// Eii exp(n_k (log(eta inv_p) + c_k)).
+// (LocalIterationViscoElastic, RheologyDensity.c:152-197), written in the normalised
+// unknown s = eta / eta_up (eta_up: the reference's start point).  Linear terms
+// (elasticity, constant viscosity, Newtonian laws) are s Aup with Aup = eta_up A;
+// non-linear ones Eii exp(n_k (ln s + lp) + nc_k), where lp = ln(eta_up / eta_p) for
+// the softest non-linear law p and nc_k = n_k ln(eta_p / eta_k) <= 0.  Every quantity
+// in the exponent is O(1) for the terms that carry strain rate, so nothing large cancels.
 // ---------------------------------------------------------------------------------------
 struct VeCoef {
   double Eii, thr_conv, thr_fail;  // Eii * tol/100, Eii * tol
   double inv_Eii;                  // 1 / Eii
-  double A;                        // sum of the linear coefficients (el, cst, Newtonian laws)
+  double eta_up;                   // eta = s eta_up
+  double Aup;                      // eta_up x the sum of the linear coefficients (el, cst, Newtonian laws)
   double a_cst, a_lin1, a_pwl1;    // e_cst = eta a_cst, e_lin = eta a_lin1 (n_lin==1), e_pwl = eta a_pwl1 (n_pwl==1)
-  double inv_p;                    // 1/eta of the primary (softest) non-linear law
-  double n[K_COUNT], nc[K_COUNT];  // exponent and n_k * log(eta_p / eta_k) per non-linear law
+  double lp;                       // ln(eta_up / eta_p)
+  double n[K_COUNT], nc[K_COUNT];  // exponent and n_k * ln(eta_p / eta_k) per non-linear law
   int nl;                          // bit k: law k is non-linear and active
 };
 
@@ -238,18 +249,20 @@ struct VeState {
   int iters, status;
 };
 
-__device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double eta_cst, VeCoef &q) {
+__device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double eta_cst, double eta_up,
+                                        double ln_eta_up, VeCoef &q) {
   const double Eii = c.Eii;
   const double tol = 1.0e-11;  // hard-coded in LocalIterationViscoElastic (:154)
   q.Eii = Eii;
   q.inv_Eii = 2.0 * c.inv2Eii;
   q.thr_conv = Eii * (tol / 100);
   q.thr_fail = Eii * tol;
+  q.eta_up = eta_up;
   q.a_cst = (L.mech & F_CST) ? Eii / eta_cst : 0.0;
-  q.A = (c.elastic ? Eii * c.inv_eta_el : 0.0) + q.a_cst;
+  double A = (c.elastic ? Eii * c.inv_eta_el : 0.0) + q.a_cst;
   q.a_lin1 = q.a_pwl1 = 0.0;
   q.nl = 0;
-  double inv_p = 0.0;
+  double ln_inv_p = -kInf;
   int p = -1;
 #pragma unroll
   for (int k = 0; k < K_COUNT; k++) {
@@ -258,30 +271,28 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
     q.nc[k] = 0.0;
     if (!(L.mech & bit)) continue;
     if (k != K_EXP && L.n[k] == 1.0) {  // Newtonian law: Eii eta / eta_k
-      const double a = Eii * L.inv[k];
+      const double a = Eii * law_inv(L, k);
       if (k == K_LIN) q.a_lin1 = a;
       else q.a_pwl1 = a;
-      q.A += a;
+      A += a;
     } else {
       q.nl |= 1 << k;
-      if (L.inv[k] > inv_p) { inv_p = L.inv[k]; p = k; }
+      if (L.ln_inv[k] > ln_inv_p) { ln_inv_p = L.ln_inv[k]; p = k; }
     }
   }
-  if (!(inv_p > 0.0)) q.nl = 0;  // every non-linear law underflowed: they carry no strain rate
-  q.inv_p = inv_p;
-  if (q.nl & (q.nl - 1)) {  // offsets are needed only with two or more non-linear laws
-    const double r_p = 1.0 / inv_p;
+  if (!(ln_inv_p > -kInf)) q.nl = 0;
+  q.lp = ln_eta_up + ln_inv_p;
 #pragma unroll
-    for (int k = 0; k < K_COUNT; k++)
-      if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * fast_log(L.inv[k] * r_p);
-  }
+  for (int k = 0; k < K_COUNT; k++)
+    if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * (L.ln_inv[k] - ln_inv_p);
+  q.Aup = A * eta_up;
 }
 
-__device__ __forceinline__ void ve_eval(const VeCoef &q, double eta, VeState &s, double &r, double &S) {
+__device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, double &r, double &S) {
   double e[K_COUNT] = {0.0, 0.0, 0.0};
   S = 0.0;
   if (q.nl) {
-    const double lx = fast_log(eta * q.inv_p);
+    const double lx = fast_log(sv) + q.lp;
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
       if (q.nl >> k & 1) {
@@ -289,44 +300,44 @@ __device__ __forceinline__ void ve_eval(const VeCoef &q, double eta, VeState &s,
         S = fma(q.n[k], e[k], S);
       }
   }
+  const double eta = sv * q.eta_up;
   s.e_cst = eta * q.a_cst;
   s.e_pwl = (q.nl >> K_PWL & 1) ? e[K_PWL] : eta * q.a_pwl1;
   s.e_lin = (q.nl >> K_LIN & 1) ? e[K_LIN] : eta * q.a_lin1;
   s.e_exp = e[K_EXP];
   s.Tii = 2.0 * eta * q.Eii;
-  r = q.Eii - eta * q.A - (e[K_PWL] + e[K_EXP] + e[K_LIN]);
+  r = q.Eii - sv * q.Aup - (e[K_PWL] + e[K_EXP] + e[K_LIN]);
 }
 
-// Newton from s.eta: eta <- eta - r / r'(eta),  r' = -A - S/eta  (LocalIterationViscoElastic)
-__device__ __forceinline__ void ve_newton(const VeCoef &q, VeState &s) {
+// Newton on s from sv: s <- s - r / r'(s),  r' = -Aup - S/s  (LocalIterationViscoElastic);
+// returns eta = s eta_up in st.eta.
+__device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s) {
   const int nitmax = 20;
-  double eta = s.eta;
   s.iters = nitmax;
   for (int it = 0; it < nitmax; it++) {
     double r, S;
-    ve_eval(q, eta, s, r, S);
+    ve_eval(q, sv, s, r, S);
     const double ar = fabs(r);
     if (ar < q.thr_conv) { s.iters = it + 1; break; }
     if (it == nitmax - 1 && ar > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
-    eta += r * eta / fma(q.A, eta, S);
+    sv += r * sv / fma(q.Aup, sv, S);
   }
-  s.eta = eta;
+  s.eta = sv * q.eta_up;
 }
 
-// Start point of the FP64 Newton: a few FP32 Newton steps on the normalised residual
-//     r(s) = 1 - a s - sum_k exp(n_k ln s + c_k),   s = eta / eta_up,
-// every quantity O(1) (a = eta_up A / Eii, c_k = n_k ln(eta_up / eta_p) + nc_k).  The
-// FP64 iteration that follows is unchanged and runs to the same residual tolerance, so
-// these steps only move its start (to within FP32 rounding of the root).
-__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, double eta_up, float s0, int iters) {
+// Start point of the FP64 Newton: a few FP32 Newton steps on the same normalised
+// residual r(s)/Eii = 1 - a s - sum_k exp(n_k ln s + c_k), a = Aup/Eii,
+// c_k = n_k lp + nc_k.  The FP64 iteration that follows is unchanged and runs to the same
+// residual tolerance, so these steps only move its start (to within FP32 rounding of the
+// root).  Returns s0 when the FP32 iteration leaves (0, 2].
+__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, float s0, int iters) {
   if (iters <= 0) return s0;
-  const float a = (float)(eta_up * q.A * q.inv_Eii);
+  const float a = (float)(q.Aup * q.inv_Eii);
   float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
   if (q.nl) {
-    const float lp = __logf((float)(eta_up * q.inv_p));
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
-      if (q.nl >> k & 1) { n[k] = (float)q.n[k]; c[k] = n[k] * lp + (float)q.nc[k]; }
+      if (q.nl >> k & 1) { n[k] = (float)q.n[k]; c[k] = (float)fma(q.n[k], q.lp, q.nc[k]); }
   }
   float s = s0;
   for (int it = 0; it < iters; it++) {
@@ -511,8 +522,40 @@ __device__ inline int plastic_popov(const ModelConst &M, const PhaseConst &ph, d
 // State carried from the set-up of one (node, phase) to its local solve.
 struct IsoState {
   Laws L;
-  double eta_up, eta_lo, eta_cst, Tyield, C, Ag, lnd;
+  double eta_up, ln_eta_up, eta_cst, Tyield, C, Ag, lnd;
 };
+
+// Start point of the local solve (RheologyDensity.c:582-592, AnisotropyRoutines.c:409-415):
+// the smallest of the initial bound, eta_cst, the isolated creep viscosities and eta_el,
+// with its logarithm for the normalised residual.
+__device__ __forceinline__ void start_viscosity(const ModelConst &M, double ln_inv_max, bool constant,
+                                                double eta_cst, bool elastic, const NodeCtx &c, double &eta_up,
+                                                double &ln_eta_up) {
+  eta_up = M.eta_up0;
+  ln_eta_up = M.ln_eta_up0;
+  bool from_cst = false;
+  if (constant && eta_cst < eta_up) { eta_up = eta_cst; from_cst = true; }
+  if (ln_inv_max > -kInf) {
+    const double e = fast_exp(-ln_inv_max);
+    if (e < eta_up) { eta_up = e; ln_eta_up = -ln_inv_max; from_cst = false; }
+  }
+  if (elastic && c.eta_el < eta_up) { eta_up = c.eta_el; ln_eta_up = c.ln_eta_el; from_cst = false; }
+  if (from_cst) ln_eta_up = fast_log(eta_cst);
+}
+
+// Lower end of the reference's bracket: the largest of the lower bound, eta_cst, eta_el and
+// the isolated creep viscosities (needed by the grain-size solve and the bisection only).
+__device__ __forceinline__ double lower_viscosity(const ModelConst &M, const Laws &L, bool constant, double eta_cst,
+                                                  bool elastic, double eta_el, bool gbs) {
+  double eta_lo = M.eta_lo0;
+  if (constant) eta_lo = fmax(eta_lo, eta_cst);
+  if (L.mech & F_PWL) eta_lo = fmax(eta_lo, fast_exp(-L.ln_inv[K_PWL]));
+  if (elastic) eta_lo = fmax(eta_lo, eta_el);
+  if (L.mech & F_EXPV) eta_lo = fmax(eta_lo, fast_exp(-L.ln_inv[K_EXP]));
+  if (L.mech & F_LIN) eta_lo = fmax(eta_lo, fast_exp(-L.ln_inv[K_LIN]));
+  if (gbs) eta_lo = fmax(eta_lo, fast_exp(-L.ln_inv_gbs));
+  return eta_lo;
+}
 
 __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
                                  IsoState &S, PointOut &o) {
@@ -552,23 +595,19 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   if (gs) {  // wattmeter grain size before eta_lin (:567-576)
     Ag = ph.Kpzm * exp(-ph.Qpzm / M.R / T);
     const double Tii0 = 2. * eta_el * Eii;
-    const double epwl0 = Tii0 / 2.0 * L.inv[K_PWL];
+    const double epwl0 = Tii0 / 2.0 * law_inv(L, K_PWL);
     const double d = exp(log(Ag * ph.Gpzm / (ph.Lpzm * (1.0 / ph.cpzm) * Tii0 * epwl0 * ph.ppzm)) / (1.0 + ph.ppzm));
     o.d1 = d;
     lnd = log(d);
     if (diffusion) {
       const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, L.lnB_lin) : L.lnB_lin;
-      L.inv[K_LIN] = Eii * exp(-fma(c.lnEii, ph.lin_invn, lnBd));
+      L.ln_inv[K_LIN] = c.lnEii - fma(c.lnEii, ph.lin_invn, lnBd);
     }
   }
   // bracket (:582-592): the smallest isolated viscosity is 1 / the largest reciprocal
-  const double inv_max = fmax(fmax(L.inv[K_PWL], L.inv[K_EXP]), fmax(L.inv[K_LIN], L.inv_gbs));
-  double eta_up = M.eta_up0;
-  if (constant) eta_up = fmin(eta_up, eta_cst);
-  if (inv_max > 0.0) eta_up = fmin(eta_up, 1.0 / inv_max);
-  if (elastic == 1) eta_up = fmin(eta_up, eta_el);
-
-  S.eta_up = eta_up; S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
+  const double ln_inv_max = fmax(fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), fmax(L.ln_inv[K_LIN], L.ln_inv_gbs));
+  start_viscosity(M, ln_inv_max, constant, eta_cst, elastic == 1, c, S.eta_up, S.ln_eta_up);
+  S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
 
 // Local solve (from s_start * eta_up, refined by `polish` FP32 Newton steps; s_start = 1
@@ -592,22 +631,15 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   double eta_ve, Tii, e_cst, e_pwl, e_exp, e_lin;
   if (!gs) {  // LocalIterationViscoElastic (:646)
     VeCoef q;
-    ve_coef(L, c, eta_cst, q);
+    ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
     VeState s;
-    s.eta = (double)ve_polish_f32(q, eta_up, s_start, polish) * eta_up;
     s.status = MDZ_OK;
-    ve_newton(q, s);
+    ve_newton(q, (double)ve_polish_f32(q, s_start, polish), s);
     set_status(o.status, s.status);
     eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
     o.iters = s.iters;
   } else {  // LocalIterationViscoElasticGrainSize (:644)
-    double eta_lo = M.eta_lo0;
-    if (constant) eta_lo = fmax(eta_lo, eta_cst);
-    if (dislocation) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_PWL]);
-    if (elastic == 1) eta_lo = fmax(eta_lo, eta_el);
-    if (peierls) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_EXP]);
-    if (diffusion) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_LIN]);
-    if (gbs) eta_lo = fmax(eta_lo, 1.0 / L.inv_gbs);
+    const double eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic == 1, eta_el, gbs);
     GseIn g;
     g.Eii = Eii; g.eta_el = eta_el; g.eta_cst = eta_cst;
     g.C_pwl = exp(-ph.pwl_n * (kLn2 + L.lnB_pwl)); g.n_pwl = ph.pwl_n;
@@ -766,6 +798,7 @@ __device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const Node
   if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; }
   c.eta_el = c.elastic ? c.G * M.dt_model : 1e20;
   c.inv_eta_el = 1.0 / c.eta_el;
+  c.ln_eta_el = c.elastic ? fast_log(c.eta_el) : 0.0;
   c.inv_Kdt = 1.0 / (c.K * M.dt_model);
   node_common(M, in, need_lnd, c);
   c.inv_d = 1.0 / in.d;
@@ -791,26 +824,19 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   Laws &L = S.L;
   creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
   L.mech &= ~F_GBS;  // the anisotropic path has no grain-boundary sliding
-  L.inv_gbs = 0.0;
+  L.ln_inv_gbs = -kInf;
   double Tyield = 0.0, Coh = in.C;
   if (plastic) {  // :370-377
     Tyield = Coh * c.cos_fric + P * c.sin_fric;
     if (ph.Slim < Tyield) { Coh = ph.Slim; Tyield = ph.Slim; }
   }
   const double eta_cst = constant ? ph.eta0 : 0.0;
-  // bracket (:409-415)
-  const double inv_max = fmax(fmax(L.inv[K_PWL], L.inv[K_EXP]), L.inv[K_LIN]);
-  double eta_up = M.eta_up0, eta_lo = M.eta_lo0;
-  if (constant) { eta_up = fmin(eta_up, eta_cst); eta_lo = fmax(eta_lo, eta_cst); }
-  if (inv_max > 0.0) eta_up = fmin(eta_up, 1.0 / inv_max);
-  if (elastic) { eta_up = fmin(eta_up, eta_el); eta_lo = fmax(eta_lo, eta_el); }
-  if (dislocation) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_PWL]);
-  if (peierls) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_EXP]);
-  if (diffusion) eta_lo = fmax(eta_lo, 1.0 / L.inv[K_LIN]);
-
-  S.eta_up = eta_up; S.eta_lo = eta_lo; S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = Coh; S.Ag = 0.0;
+  // bracket (:409-415); its lower end is formed only where it is used
+  const double ln_inv_max = fmax(fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), L.ln_inv[K_LIN]);
+  start_viscosity(M, ln_inv_max, constant, eta_cst, elastic != 0, c, S.eta_up, S.ln_eta_up);
+  S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = Coh; S.Ag = 0.0;
   S.lnd = c.lnd;
-  (void)an; (void)T; (void)K; (void)dt; (void)min_eta; (void)max_eta;
+  (void)an; (void)T; (void)K; (void)dt; (void)min_eta; (void)max_eta; (void)dislocation; (void)eta_el;
 }
 
 // Local solve, plasticity, post-processing.  The Newton starts from the reference's
@@ -827,7 +853,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
   const double min_eta = M.min_eta, max_eta = M.max_eta;
   Laws &L = S.L;
-  const double eta_up = S.eta_up, eta_lo = S.eta_lo, eta_cst = S.eta_cst, Tyield = S.Tyield;
+  const double eta_up = S.eta_up, eta_cst = S.eta_cst, Tyield = S.Tyield;
   double eta_ve = eta_up, Tii = 0.0, e_cst = 0.0, e_pwl = 0.0, e_exp = 0.0, e_lin = 0.0;
   if (fl & F_GS) {  // :429-473
     GseIn g;
@@ -835,7 +861,8 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     g.C_pwl = exp(-ph.pwl_n * (kLn2 + L.lnB_pwl)); g.n_pwl = ph.pwl_n;
     g.C_lin = exp(-ph.lin_n * (kLn2 + L.lnB_lin)); g.n_lin = ph.lin_n; g.m_lin = ph.lin_m;
     g.C_exp = exp(fma(L.n[K_EXP], log(ph.exp_s3gS), L.lnA_exp)); g.ST = L.ST; g.n_exp = ph.exp_n;
-    g.eta_up = eta_up; g.eta_lo = eta_lo; g.Ag = ph.Kpzm * exp(-ph.Qpzm / (M.R * T));
+    g.eta_up = eta_up; g.eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic != 0, eta_el, false);
+    g.Ag = ph.Kpzm * exp(-ph.Qpzm / (M.R * T));
     g.gam = ph.Gpzm; g.lam = ph.Lpzm; g.cg = ph.cpzm; g.pg = ph.ppzm; g.elastic = elastic; g.constant = constant;
     g.dislocation = dislocation; g.peierls = peierls; g.diffusion = diffusion;
     double dd = in.d;
@@ -847,34 +874,37 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   } else {  // :474-585: 10 log-space bisection steps on [min_eta 1e-3, 10 max(eta_lo, max_eta)], then Newton
     const double tol = 1e-11;
     VeCoef q;
-    ve_coef(L, c, eta_cst, q);
+    ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
     VeState s;
     s.status = MDZ_OK;
-    double r, S;
+    double r, S, sv;  // sv = eta_ve / eta_up
     if (s_start > 0.0f || polish > 0) {
-      eta_ve = (double)ve_polish_f32(q, eta_up, (s_start > 0.0f) ? s_start : 1.0f, polish) * eta_up;
+      sv = (double)ve_polish_f32(q, (s_start > 0.0f) ? s_start : 1.0f, polish);
     } else {
+      const double inv_up = 1.0 / eta_up;
+      const double eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic != 0, eta_el, false);
       double lo = min_eta * 1.0e-3, hi = 10.0 * fmax(eta_lo, max_eta);
       for (int bit = 0; bit < 10; bit++) {
         eta_ve = sqrt(lo * hi);
-        ve_eval(q, eta_ve, s, r, S);
+        ve_eval(q, eta_ve * inv_up, s, r, S);
         if (r > 0.0) lo = eta_ve;
         else hi = eta_ve;
         if (fabs(r) < q.thr_conv) break;
       }
-      eta_ve = sqrt(lo * hi);
+      sv = sqrt(lo * hi) * inv_up;
     }
     o.iters = 50;
     for (int it = 0; it < 50; it++) {
-      ve_eval(q, eta_ve, s, r, S);
+      ve_eval(q, sv, s, r, S);
       if (isnan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
-      eta_ve += r * eta_ve / fma(q.A, eta_ve, S);
-      if (eta_ve <= 0.0) eta_ve = min_eta;
+      sv += r * sv / fma(q.Aup, sv, S);
+      if (sv <= 0.0) sv = min_eta / eta_up;
       const double ar = fabs(r);
       if (ar < q.thr_conv) { o.iters = it + 1; break; }
       if (it == 49 && ar < 10.0 * tol * Eii) break;
       if (it == 49 && ar > q.thr_fail) { set_status(o.status, MDZ_EANISO_ITER); break; }
     }
+    eta_ve = sv * eta_up;
     Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
   }
   if (eta_ve < min_eta) eta_ve = min_eta;  // :589-603

@@ -273,6 +273,9 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_batch_sweep.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
     lib.mdz_rheo_batch_capture.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_uint64]
     lib.mdz_rheo_batch_launch.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
+    lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
+                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
+    lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
     lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SweepStats)]
@@ -457,6 +460,27 @@ class Context:
     def points(self, model, mat, pin, pout, n, aniso=0, mem=MEM_HOST):
         return self.lib.mdz_rheo_points(self.handle, C.byref(model), C.byref(mat), C.byref(pin),
                                         C.byref(pout), n, aniso, mem)
+
+    # ---- launch-shape autotuner
+    AUTOTUNE_CANDIDATES = [(b, w) for b in (128, 64) for w in (0, 1, 2, 4, 8)]  # (threads per block, waves)
+
+    def autotune(self, model, mat, fields, aniso=False, flags=0, reps=3):
+        """Time every launch shape on this device-resident grid and keep the fastest.
+        Returns (ms per candidate, index of the best, (block, grid_cap) now in use)."""
+        ms = np.zeros(len(self.AUTOTUNE_CANDIDATES))
+        best = C.c_int()
+        rc = self.lib.mdz_rheo_autotune(self.handle, C.byref(model), C.byref(mat), C.byref(fields.struct),
+                                        int(aniso), flags, reps, ms.ctypes.data, C.byref(best))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_autotune")
+        return ms, best.value, self.launch_shape(aniso)
+
+    def launch_shape(self, aniso=False):
+        b, g = C.c_int(), C.c_int()
+        rc = self.lib.mdz_rheo_get_launch_shape(self.handle, int(aniso), C.byref(b), C.byref(g))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_get_launch_shape")
+        return b.value, g.value
 
     # ---- learned warm start
     def set_warmstart(self, w: Optional[MlpWeights], polish_iters: int = 4):
