@@ -45,11 +45,11 @@ UNIT = "point-updates/s"
 # the same field distributions at 513 x 513 cells (527,365 nodes), per workload
 # (profiles/k_sweep_plain_large_513.md, profiles/k_sweep_aniso_513.md).
 # `roofline.achieved` = this x nodes / the CUDA-event time of one launch.
-FP64_FLOPS_PER_POINT = {"plain_large": 1986.3, "aniso": 1263.5}
+FP64_FLOPS_PER_POINT = {"plain_large": 1866.8, "aniso": 1233.4}
 # DRAM bytes (read + write) per point-update of the same captures, scaled to a launch by
 # its node count; the write count of those small captures misses lines still in L2 when
 # the kernel ends.
-DRAM_BYTES_PER_POINT = {"plain_large": 267.7, "aniso": 268.3}
+DRAM_BYTES_PER_POINT = {"plain_large": 267.9, "aniso": 268.3}
 
 
 def parse():
@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm start")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     args = ap.parse_args()
     if args.size is None:
         args.size = 4097 if args.workload == "aniso" else 2049
@@ -338,6 +339,13 @@ def main():
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     sweep = ctx.sweep_aniso if aniso else ctx.sweep
+    tune = None
+    if not args.no_autotune:  # launch shape for this grid, before any timed region
+        t_ms, t_best, t_shape = ctx.autotune(w.model, w.mat, fs, aniso=aniso, reps=2)
+        tune = {"candidates": [f"block {b}, " + (f"{v} waves" if v else "one thread per node")
+                               for b, v in R.Context.AUTOTUNE_CANDIDATES],
+                "ms_per_sweep": [float(x) for x in t_ms], "chosen": int(t_best),
+                "block": t_shape[0], "grid_cap": t_shape[1]}
 
     def barrier():
         if ws > 1:
@@ -480,7 +488,7 @@ def main():
                        "parallelism": f"{ws} independent grid(s), one per GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
-            "reference_start": ref_r, "warm_start": warm}
+            "reference_start": ref_r, "warm_start": warm, "autotune": tune}
     print(json.dumps(line))
     if ws > 1:
         REP.finalize()

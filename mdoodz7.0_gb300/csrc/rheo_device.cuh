@@ -7,21 +7,25 @@
 // so the formulation minimises FP64 instructions while keeping every quantity
 // well conditioned:
 //  * per-phase constants (log pre-factors, 1/(R n), 1/n, ...) are folded on the host;
-//  * each creep law k is carried as the reciprocal of its isolated viscosity at the
-//    node's strain rate, 1/eta_k, formed as a product of well-conditioned factors
-//    (one exp); its strain rate at trial viscosity eta is then
+//  * each creep law k is carried as the logarithm of the reciprocal of its isolated
+//    viscosity at the node's strain rate, ln(1/eta_k), a sum of well-conditioned logs
+//    (no exp); its strain rate at trial viscosity eta is then
 //        Eii_k(eta) = Eii (eta / eta_k)^n_k,
 //    the reference's C_k Tii^n_k with Tii = 2 eta Eii rewritten.  The Peierls law is
 //    used in the equivalent physical form A (sqrt(3) Tii / (gamma sigma_P))^(ST+n);
-//  * a Newton step takes one log, of eta / eta_p for the softest non-linear law p;
-//    the other laws are offset from it by log(eta_p / eta_k) <= 0, fixed per call, so
-//    no large logarithms cancel;
+//  * the local Newton iterates on s = eta / eta_up (eta_up: the reference's start
+//    point); a step takes one log, of s, and one exp per non-linear law, with the laws
+//    offset from the softest one p by n_k ln(eta_p / eta_k) <= 0 and from eta_up by
+//    ln(eta_up / eta_p), so no large logarithms cancel;
+//  * once a Newton step is small (|n step| < 1e-5) the next residual carries the law
+//    terms by the binomial series instead of a new log and exps (exact to 2e-16);
 //  * post-processing uses eta_k = Tii / (2 Eii_k), the reference's
 //    B_k pow(Eii_k, 1/n_k - 1) rewritten with the same identity.
 // These are identities of the reference's formulas: results differ only by rounding
 // (a few 1e-14 relative, checked by the parity tests).  The Newton iteration itself
-// (start point, update, stopping test, cap) is the reference's, so iteration counts
-// agree except where rounding moves a residual across the stopping threshold.
+// (start point, update, stopping test, cap) is the reference's, so from the reference's
+// start (MDZ_SWEEP_REF_START) iteration counts agree except where rounding moves a
+// residual across the stopping threshold.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -241,11 +245,14 @@ struct VeCoef {
   double a_cst, a_lin1, a_pwl1;    // e_cst = eta a_cst, e_lin = eta a_lin1 (n_lin==1), e_pwl = eta a_pwl1 (n_pwl==1)
   double lp;                       // ln(eta_up / eta_p)
   double n[K_COUNT], nc[K_COUNT];  // exponent and n_k * ln(eta_p / eta_k) per non-linear law
+  double hn[K_COUNT];              // (n_k - 1) / 2
+  double nmax;                     // largest exponent of the non-linear laws (0 without)
   int nl;                          // bit k: law k is non-linear and active
 };
 
 struct VeState {
   double eta, Tii, e_cst, e_pwl, e_exp, e_lin;
+  double e[K_COUNT];  // strain rates of the non-linear laws at the last evaluated point
   int iters, status;
 };
 
@@ -282,23 +289,44 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
   }
   if (!(ln_inv_p > -kInf)) q.nl = 0;
   q.lp = ln_eta_up + ln_inv_p;
+  q.nmax = 0.0;
 #pragma unroll
-  for (int k = 0; k < K_COUNT; k++)
+  for (int k = 0; k < K_COUNT; k++) {
+    q.hn[k] = 0.5 * (q.n[k] - 1.0);
+    if (q.nl >> k & 1) q.nmax = fmax(q.nmax, q.n[k]);
     if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * (L.ln_inv[k] - ln_inv_p);
+  }
   q.Aup = A * eta_up;
 }
 
-__device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, double &r, double &S) {
-  double e[K_COUNT] = {0.0, 0.0, 0.0};
+// Residual r and S = sum_k n_k Eii_k at sv.  With step >= 0 the non-linear terms are
+// carried from the previous point sv / (1 + step) by the binomial series
+//     (1 + step)^n = 1 + n step (1 + (n - 1) step / 2) + O((n step)^3),
+// used only where |n step| < 1e-5, so the dropped term is below 2e-16 relative: the same
+// residual as a fresh evaluation to rounding, without its log and exps.
+__device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, double &r, double &S,
+                                        double step = -1.0) {
+  double *e = s.e;
   S = 0.0;
-  if (q.nl) {
-    const double lx = fast_log(sv) + q.lp;
+  if (step >= -0.5) {
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
       if (q.nl >> k & 1) {
-        e[k] = q.Eii * fast_exp(fma(q.n[k], lx, q.nc[k]));
+        const double t = step * q.n[k];
+        e[k] = fma(e[k] * t, fma(step, q.hn[k], 1.0), e[k]);
         S = fma(q.n[k], e[k], S);
       }
+  } else {
+    e[0] = e[1] = e[2] = 0.0;
+    if (q.nl) {
+      const double lx = fast_log(sv) + q.lp;
+#pragma unroll
+      for (int k = 0; k < K_COUNT; k++)
+        if (q.nl >> k & 1) {
+          e[k] = q.Eii * fast_exp(fma(q.n[k], lx, q.nc[k]));
+          S = fma(q.n[k], e[k], S);
+        }
+    }
   }
   const double eta = sv * q.eta_up;
   s.e_cst = eta * q.a_cst;
@@ -309,18 +337,21 @@ __device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, 
   r = q.Eii - sv * q.Aup - (e[K_PWL] + e[K_EXP] + e[K_LIN]);
 }
 
-// Newton on s from sv: s <- s - r / r'(s),  r' = -Aup - S/s  (LocalIterationViscoElastic);
-// returns eta = s eta_up in st.eta.
+// Newton on s from sv: s <- s (1 + step), step = r / (Aup s + S), i.e. s - r / r'(s)
+// with r' = -Aup - S/s (LocalIterationViscoElastic); returns eta = s eta_up in st.eta.
 __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s) {
   const int nitmax = 20;
   s.iters = nitmax;
+  double step = -1.0;  // no previous point yet
   for (int it = 0; it < nitmax; it++) {
     double r, S;
-    ve_eval(q, sv, s, r, S);
+    ve_eval(q, sv, s, r, S, step);
     const double ar = fabs(r);
     if (ar < q.thr_conv) { s.iters = it + 1; break; }
     if (it == nitmax - 1 && ar > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
-    sv += r * sv / fma(q.Aup, sv, S);
+    const double d = r / fma(q.Aup, sv, S);
+    sv = fma(sv, d, sv);
+    step = (fabs(d) * q.nmax < 1e-5) ? d : -1.0;
   }
   s.eta = sv * q.eta_up;
 }
@@ -894,11 +925,14 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
       sv = sqrt(lo * hi) * inv_up;
     }
     o.iters = 50;
+    double step = -1.0;  // binomial update of the previous point's terms (see ve_eval)
     for (int it = 0; it < 50; it++) {
-      ve_eval(q, sv, s, r, S);
+      ve_eval(q, sv, s, r, S, step);
       if (isnan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
-      sv += r * sv / fma(q.Aup, sv, S);
-      if (sv <= 0.0) sv = min_eta / eta_up;
+      const double d = r / fma(q.Aup, sv, S);
+      sv = fma(sv, d, sv);
+      step = (fabs(d) * q.nmax < 1e-5) ? d : -1.0;
+      if (sv <= 0.0) { sv = min_eta / eta_up; step = -1.0; }
       const double ar = fabs(r);
       if (ar < q.thr_conv) { o.iters = it + 1; break; }
       if (it == 49 && ar < 10.0 * tol * Eii) break;

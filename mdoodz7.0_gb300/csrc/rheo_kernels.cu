@@ -518,6 +518,18 @@ int tiles_blocks_per_sm(bool aniso, int mode) {
     else tiles_attributes<false, MODE_WARM>();
   }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kMlpTile, smem);
+  // The query has been seen to report one CTA where registers (255 per thread, 2 CTAs
+  // of 128) and the shared-memory carve-out allow two; bound it below by the register
+  // file and shared memory directly.  A larger grid only changes residency, not results.
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && fa.numRegs > 0) {
+    const int regs = (fa.numRegs + 7) & ~7;
+    int by_regs = 65536 / (kMlpTile * regs);
+    int by_smem = (int)((227 * 1024) / (smem + fa.sharedSizeBytes + 1024));
+    const int own = by_regs < by_smem ? by_regs : by_smem;
+    if (own > n) n = own;
+  }
+  cudaGetLastError();
   return n > 0 ? n : 1;
 }
 
