@@ -146,6 +146,16 @@ typedef struct mdz_grid_fields {
   double *const *phase_eta_s;
 } mdz_grid_fields;
 
+/* ---- viscosity tensors of the momentum equations -----------------------
+ * The coefficient fields RheologicalOperators writes (MDLIB/mdoodz-private.h:124-131). */
+typedef struct mdz_operator_fields {
+  /* centroids, (Nx-1)*(Nz-1) each */
+  double *D11_n, *D12_n, *D13_n, *D14_n, *D21_n, *D22_n, *D23_n, *D24_n;
+  double *drhodp_n; /* written by the Newton (jacobian = 1) operator only */
+  /* vertices, Nx*Nz each */
+  double *D31_s, *D32_s, *D33_s, *D34_s;
+} mdz_operator_fields;
+
 /* ---- sweep statistics ----------------------------------------------- */
 typedef struct mdz_sweep_stats {
   uint64_t phase_calls;      /* (node, active phase) local solves */
@@ -245,6 +255,21 @@ int mdz_rheo_sweep_aniso(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_ma
 int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                     const mdz_point_inputs *in, mdz_point_outputs *out, int64_t n, int aniso,
                     int mem);
+/* RheologicalOperators (MDLIB/StokesRoutines.c:75-410): the viscosity tensors D of the
+ * momentum equations from a grid that a sweep has just updated.  It reads the sweep's
+ * inputs and its outputs eta_n, eta_s, phase_eta_n/_s, T_s and P_s.
+ *   jacobian = 0: the Picard operator (from eta and the anisotropy fields only);
+ *   jacobian = 1: the Newton operator.  Its derivatives d(eta)/dE, d(eta)/dP,
+ *     d(div_pl)/dE and d(rho)/dP are central differences over 8 perturbed local solves
+ *     per node and active phase (DerivativesOnTheFly_n / _s and PhaseRheologyLoop_v1,
+ *     MDLIB/FD_Jacobian.c:48-323), all solved on the GPU in one launch.
+ * `compressible` is params.compressible; `flags` may hold MDZ_SWEEP_REF_START, which
+ * starts the perturbed solves where the reference does.  `mem` and `stats` as for the
+ * sweep (stats count the perturbed local solves). */
+int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
+                       const mdz_grid_fields *f, mdz_operator_fields *ops, int jacobian, int compressible,
+                       int aniso, int mem, int flags, mdz_sweep_stats *stats);
+
 /* ---- allocation-free variant (no reference counterpart) ----------------
  * mdz_rheo_points on the CURRENT device without any context and without allocating:
  * no cudaMalloc / cudaFree / cudaHostAlloc and no allocating library call.  For callers

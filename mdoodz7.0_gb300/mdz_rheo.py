@@ -115,6 +115,31 @@ class SweepStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+OPS_N = ["D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n", "drhodp_n"]
+OPS_S = ["D31_s", "D32_s", "D33_s", "D34_s"]
+
+
+class OperatorFields(C.Structure):
+    """mdz_operator_fields: the D coefficients of RheologicalOperators."""
+    _fields_ = [(n, _P) for n in OPS_N + OPS_S]
+
+
+def make_operator_fields(arrays: Dict[str, object]) -> OperatorFields:
+    o = OperatorFields()
+    for name in OPS_N + OPS_S:
+        setattr(o, name, _ptr(arrays.get(name)))
+    return o
+
+
+def alloc_operator_fields(nc: int, nv: int, like=None) -> Dict[str, object]:
+    """Zeroed D arrays (numpy, or torch on the device of `like`)."""
+    if like is not None:
+        import torch
+        return {**{k: torch.zeros(nc, dtype=torch.float64, device=like.device) for k in OPS_N},
+                **{k: torch.zeros(nv, dtype=torch.float64, device=like.device) for k in OPS_S}}
+    return {**{k: np.zeros(nc) for k in OPS_N}, **{k: np.zeros(nv) for k in OPS_S}}
+
+
 MLP_IN, MLP_HID = 16, 64
 
 

@@ -52,6 +52,11 @@ def _bind(lib, prefix):
             fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields), C.c_int,
                            C.c_void_p, C.c_void_p, C.POINTER(R.SweepStats)]
         fn.restype = C.c_int
+    ops = getattr(lib, f"{prefix}_operators", None)
+    if ops is not None:
+        ops.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields),
+                        C.POINTER(R.OperatorFields), C.c_int, C.c_int, C.c_int]
+        ops.restype = C.c_int
     pts = getattr(lib, f"{prefix}_points")
     pts.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.PointInputs),
                     C.POINTER(R.PointOutputs), C.c_int64, C.c_int]
@@ -130,6 +135,23 @@ def shim_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False, drop_i
     lib = shimtest()
     fn = lib.shimtest_shim_sweep if drop_in else lib.shimtest_ref_sweep
     return fn(C.byref(model), C.byref(mat), C.byref(fs.struct), final_update, int(aniso))
+
+
+def orc_operators(model, mat, fs: "R.FieldSet", ops: dict, jacobian=1, compressible=0, aniso=False):
+    """RheologicalOperators on the restatement; `ops` is a dict of numpy D arrays."""
+    o = R.make_operator_fields(ops)
+    return oracle().orc_operators(C.byref(model), C.byref(mat), C.byref(fs.struct), C.byref(o), jacobian,
+                                  compressible, int(aniso))
+
+
+def ref_operators(model, mat, fs: "R.FieldSet", ops: dict, jacobian=1, compressible=0, aniso=False):
+    """RheologicalOperators of the reference build."""
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    o = R.make_operator_fields(ops)
+    return lib.ref_operators(C.byref(model), C.byref(mat), C.byref(fs.struct), C.byref(o), jacobian,
+                             compressible, int(aniso))
 
 
 def orc_points(model, mat, pin, pout, n, aniso=0):

@@ -61,18 +61,10 @@ static void quiet_log(void) {
 
 #define W(x) ((double *)(x))
 
-int ref_sweep(const mdz_model *m, const mdz_materials *mat, const mdz_grid_fields *f,
-              int final_update, int aniso) {
-  quiet_log();
+/* A zeroed `grid` over the caller's arrays, with the identity index maps. */
+static grid *make_grid(const mdz_model *m, const mdz_grid_fields *f) {
   const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1, Nc = Ncx * Ncz, Nv = Nx * Nz;
   grid *g = calloc(1, sizeof(grid));
-  mat_prop *mp = malloc(sizeof(mat_prop));
-  params pm;
-  scale sc;
-  Nparams np;
-  memset(&np, 0, sizeof(np));
-  fill_materials(mp, mat);
-  fill_params(&pm, &sc, m);
   g->Nx = Nx; g->Nz = Nz;
   g->kp = malloc(sizeof(int) * Nc); g->lp = malloc(sizeof(int) * Nc);
   g->kn = malloc(sizeof(int) * Nv); g->ln = malloc(sizeof(int) * Nv);
@@ -109,14 +101,63 @@ int ref_sweep(const mdz_model *m, const mdz_materials *mat, const mdz_grid_field
   g->sxxd_s = f->sxxd_s; g->szzd_s = f->szzd_s; g->sxz = f->sxz; g->eta_phys_s = f->eta_phys_s;
   g->eta_s = f->eta_s; g->X_s = f->X_s; g->VE_s = f->VE_s;
   g->phase_eta_s = (double **)f->phase_eta_s;
+  return g;
+}
 
+static void free_grid(grid *g) {
+  free(g->kp); free(g->lp); free(g->kn); free(g->ln);
+  free(g);
+}
+
+int ref_sweep(const mdz_model *m, const mdz_materials *mat, const mdz_grid_fields *f,
+              int final_update, int aniso) {
+  quiet_log();
+  mat_prop *mp = malloc(sizeof(mat_prop));
+  params pm;
+  scale sc;
+  Nparams np;
+  memset(&np, 0, sizeof(np));
+  fill_materials(mp, mat);
+  fill_params(&pm, &sc, m);
+  grid *g = make_grid(m, f);
   if (aniso) NonNewtonianViscosityGridAniso(g, mp, &pm, np, &sc, final_update);
   else       NonNewtonianViscosityGrid(g, mp, &pm, np, &sc, final_update);
-
-  free(g->kp); free(g->lp); free(g->kn); free(g->ln);
-  free(g); free(mp);
+  free_grid(g);
+  free(mp);
   return 0;
 }
+
+#ifndef MDZ_NO_OPERATORS /* the drop-in check links no StokesRoutines.c */
+/* RheologicalOperators (StokesRoutines.c:75) on the same kind of grid, writing `ops`.
+ * The anisotropic Newton branch reads FS_AR_n / FS_AR_s without using them in the
+ * coefficients; they are set to 1. */
+int ref_operators(const mdz_model *m, const mdz_materials *mat, const mdz_grid_fields *f,
+                  mdz_operator_fields *ops, int jacobian, int compressible, int aniso) {
+  quiet_log();
+  const int Nc = (m->Nx - 1) * (m->Nz - 1), Nv = m->Nx * m->Nz;
+  mat_prop *mp = malloc(sizeof(mat_prop));
+  params pm;
+  scale sc;
+  fill_materials(mp, mat);
+  fill_params(&pm, &sc, m);
+  pm.compressible = compressible;
+  pm.anisotropy = aniso;
+  grid *g = make_grid(m, f);
+  g->D11_n = ops->D11_n; g->D12_n = ops->D12_n; g->D13_n = ops->D13_n; g->D14_n = ops->D14_n;
+  g->D21_n = ops->D21_n; g->D22_n = ops->D22_n; g->D23_n = ops->D23_n; g->D24_n = ops->D24_n;
+  g->D31_s = ops->D31_s; g->D32_s = ops->D32_s; g->D33_s = ops->D33_s; g->D34_s = ops->D34_s;
+  g->drhodp_n = ops->drhodp_n;
+  g->FS_AR_n = malloc(sizeof(double) * Nc);
+  g->FS_AR_s = malloc(sizeof(double) * Nv);
+  for (int i = 0; i < Nc; i++) g->FS_AR_n[i] = 1.0;
+  for (int i = 0; i < Nv; i++) g->FS_AR_s[i] = 1.0;
+  RheologicalOperators(g, &pm, mp, &sc, jacobian, aniso);
+  free(g->FS_AR_n); free(g->FS_AR_s);
+  free_grid(g);
+  free(mp);
+  return 0;
+}
+#endif
 
 int ref_points(const mdz_model *m, const mdz_materials *mat, const mdz_point_inputs *in,
                mdz_point_outputs *out, int64_t n, int aniso) {

@@ -1,11 +1,20 @@
 /* Empty definitions for the MDOODZ7.0 symbols that the compiled rheology
  * sources reference but never reach on the local-rheology path with
- * melting=0 and no HDF5 output (oracle/_ref only).  Deliberately compiled
- * without the MDOODZ headers so their prototypes do not apply. */
+ * melting=0 and no HDF5 output, and for the Stokes solvers that the other
+ * routines of StokesRoutines.c call (oracle/_ref only; RheologicalOperators
+ * reaches none of them).  Deliberately compiled without the MDOODZ headers so
+ * their prototypes do not apply. */
 void AddFieldToGroup(void) {}
 void AddGroupToHDF5(void) {}
+#ifdef MDZ_STUB_APPLYBC /* builds without StokesRoutines.c */
 void ApplyBC(void) {}
+#endif
 void CreateOutputHDF5(void) {}
 void P2Mastah(void) {}
 void PartialMelting(void) {}
 void ScaleBackD(void) {}
+void BuildStokesOperatorDecoupled(void) {}
+void DirectStokesDecoupled(void) {}
+void DirectStokesDecoupledComp(void) {}
+void KSPStokesDecoupled(void) {}
+void KillerSolver(void) {}

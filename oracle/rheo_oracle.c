@@ -1034,3 +1034,209 @@ int orc_points(const mdz_model *m, const mdz_materials *mt, const mdz_point_inpu
   }
   return status;
 }
+
+/* ------------------------------------------------------------------------ */
+/* RheologicalOperators (StokesRoutines.c:75-410) with the finite-difference */
+/* derivatives of DerivativesOnTheFly_n / _s and PhaseRheologyLoop_v1        */
+/* (FD_Jacobian.c:48-323).                                                   */
+/* ------------------------------------------------------------------------ */
+typedef struct {  /* the per-node fields PhaseRheologyLoop_v1 reads */
+  const double *const *vol, *const *eta_phase;
+  const double *G, *T, *P0, *d, *phi, *X0, *txx0, *tzz0, *txz0, *beta, *dil, *fric, *C;
+  double T0;
+} orc_fd_node;
+
+typedef struct { double *detadE, *ddivpdE, *danidE, *drhodP; } orc_fd_acc;
+
+/* PhaseRheologyLoop_v1, FD_Jacobian.c:48-100 */
+static void orc_phase_loop(const mdz_model *m, const mdz_materials *mt, int aniso, int is_centroid, double sign,
+                           double denom, double Exx, double Ezz, double Exz, double P, double ani_fac,
+                           double angle, double lx2, double lxlz, int64_t c, const orc_fd_node *nd,
+                           orc_fd_acc a) {
+  const double ani_vep = 1.0;
+  for (int p = 0; p < m->Nb_phases; p++) {
+    if (!(fabs(nd->vol[p][c]) > 1e-13)) continue;
+    orc_pt pt;
+    memset(&pt, 0, sizeof(pt));
+    pt.phase = p; pt.G = nd->G[c]; pt.T = nd->T[c]; pt.P = P; pt.d = nd->d[c]; pt.phi = nd->phi[c];
+    pt.X0 = nd->X0[c]; pt.Exx = Exx; pt.Ezz = Ezz; pt.Exz = Exz; pt.Txx0 = nd->txx0[c];
+    pt.Tzz0 = nd->tzz0[c]; pt.Txz0 = nd->txz0[c]; pt.dil = nd->dil[c]; pt.fric = nd->fric[c];
+    pt.C = nd->C[c]; pt.P0 = nd->P0[c]; pt.T0 = nd->T0; pt.beta = nd->beta[c];
+    pt.lxlz = lxlz; pt.lx2 = lx2; pt.angle = angle; pt.ani_fac = ani_fac;
+    pt.post_process = 0; pt.centroid = is_centroid; pt.final_update = 0;
+    orc_res r;
+    if (aniso) orc_viscosity_concise_aniso(m, mt, &pt, &r);
+    else       orc_viscosity_concise(m, mt, &pt, &r);
+    const double eta_vep = r.etaVE;
+    if (m->eta_average == 0) *a.detadE += sign * nd->vol[p][c] * eta_vep / (denom);
+    if (m->eta_average == 1) *a.detadE += sign * nd->vol[p][c] * eta_vep / (denom) / pow(nd->eta_phase[p][c], 2.0);
+    if (m->eta_average == 2) *a.detadE += sign * nd->vol[p][c] * eta_vep / (denom) / nd->eta_phase[p][c];
+    *a.danidE += sign * nd->vol[p][c] * ani_vep / (denom);
+    if (is_centroid > 0) *a.ddivpdE += sign * nd->vol[p][c] * r.div_pl / (denom);
+    if (is_centroid == 2) *a.drhodP += sign * nd->vol[p][c] * r.rho / (denom);
+  }
+}
+
+/* DerivativesOnTheFly_n (is_centroid = 1, tol 1e-5) and _s (0, 1e-7): central
+ * differences in Exx, Ezz, Exz (denominator 4 pert: Gxz = 2 Exz) and P. d[0..3] are
+ * d/dExx, d/dEzz, d/dGxz, d/dP of eta; v[], n[] of div_pl and the anisotropy factor. */
+static void orc_fd_derivatives(const mdz_model *m, const mdz_materials *mt, int aniso, int centroid,
+                               double Exx_ref, double Ezz_ref, double Exz_ref, double P_ref, double ani_fac,
+                               double angle, double lx2, double lxlz, int64_t c, const orc_fd_node *nd,
+                               double eta_node, double d[4], double v[4], double an[4], double *drhodp) {
+  const double tol = centroid ? 1e-5 : 1e-7;
+  const double pert_xx = tol * fabs(Exx_ref) + tol / 1e10;
+  const double pert_zz = tol * fabs(Ezz_ref) + tol / 1e10;
+  const double pert_xz = tol * fabs(Exz_ref) + tol / 1e10;
+  const double pert_p = tol * fabs(P_ref) + tol / 1e10;
+  double scratch = 0.0;
+  for (int s = 0; s < 2; s++) {
+    const double sign = s == 0 ? 1.0 : -1.0;
+    orc_fd_acc a = {&d[0], centroid ? &v[0] : &scratch, &an[0], NULL};
+    orc_phase_loop(m, mt, aniso, centroid ? 1 : 0, sign, 2.0 * pert_xx, Exx_ref + sign * pert_xx, Ezz_ref, Exz_ref,
+                   P_ref, ani_fac, angle, lx2, lxlz, c, nd, a);
+  }
+  for (int s = 0; s < 2; s++) {
+    const double sign = s == 0 ? 1.0 : -1.0;
+    orc_fd_acc a = {&d[1], centroid ? &v[1] : &scratch, &an[1], NULL};
+    orc_phase_loop(m, mt, aniso, centroid ? 1 : 0, sign, 2.0 * pert_zz, Exx_ref, Ezz_ref + sign * pert_zz, Exz_ref,
+                   P_ref, ani_fac, angle, lx2, lxlz, c, nd, a);
+  }
+  for (int s = 0; s < 2; s++) {
+    const double sign = s == 0 ? 1.0 : -1.0;
+    orc_fd_acc a = {&d[2], centroid ? &v[2] : &scratch, &an[2], NULL};
+    orc_phase_loop(m, mt, aniso, centroid ? 1 : 0, sign, 4.0 * pert_xz, Exx_ref, Ezz_ref, Exz_ref + sign * pert_xz,
+                   P_ref, ani_fac, angle, lx2, lxlz, c, nd, a);
+  }
+  for (int s = 0; s < 2; s++) {
+    const double sign = s == 0 ? 1.0 : -1.0;
+    orc_fd_acc a = {&d[3], centroid ? &v[3] : &scratch, &an[3], centroid ? drhodp : &scratch};
+    orc_phase_loop(m, mt, aniso, centroid ? 2 : 0, sign, 2.0 * pert_p, Exx_ref, Ezz_ref, Exz_ref,
+                   P_ref + sign * pert_p, ani_fac, angle, lx2, lxlz, c, nd, a);
+  }
+  if (m->eta_average == 1) for (int k = 0; k < 4; k++) d[k] *= pow(eta_node, 2);
+  if (m->eta_average == 2) for (int k = 0; k < 4; k++) d[k] *= eta_node;
+}
+
+int orc_operators(const mdz_model *m, const mdz_materials *mt, const mdz_grid_fields *f,
+                  mdz_operator_fields *ops, int jacobian, int compressible, int aniso) {
+  const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1;
+  const int64_t Nc = (int64_t)Ncx * Ncz, Nv = (int64_t)Nx * Nz;
+  const double dt = m->dt;
+  int status = MDZ_OK;
+  const orc_fd_node nn = {f->phase_perc_n, (const double *const *)f->phase_eta_n, f->mu_n, f->T, f->p0_n, f->d0_n,
+                          f->phi0_n, f->X0_n, f->sxxd0, f->szzd0, f->sxz0_n, f->bet_n, f->dil_n, f->fric_n,
+                          f->C_n, 0.0};
+  const orc_fd_node ns = {f->phase_perc_s, (const double *const *)f->phase_eta_s, f->mu_s, f->T_s, f->p0_s,
+                          f->d0_s, f->phi0_s, f->X0_s, f->sxxd0_s, f->szzd0_s, f->sxz0, f->bet_s, f->dil_s,
+                          f->fric_s, f->C_s, 0.0};
+  /* centroids: StokesRoutines.c:94-120 (Picard), :251-320 (Newton) */
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t k = 0; k < Nc; k++) {
+    double *D[8] = {ops->D11_n, ops->D12_n, ops->D13_n, ops->D14_n, ops->D21_n, ops->D22_n, ops->D23_n, ops->D24_n};
+    if (f->BCp_type[k] == 30 || f->BCp_type[k] == 31) {
+      for (int j = 0; j < 8; j++) D[j][k] = 0.0;
+      continue;
+    }
+    const double eta_vep = f->eta_n[k];
+    double ani_vep = 1.0, aniS_vep = 0.0, d1 = 0.0, d2 = 0.0, angle = 0.0, lxlz = 0.0, lx2 = 0.0;
+    if (aniso) {
+      ani_vep = f->aniso_factor_n[k];
+      aniS_vep = 1.0 - 1.0 / ani_vep;
+      d1 = f->d1_n[k];
+      d2 = f->d2_n[k];
+    }
+    if (!jacobian) {
+      D[0][k] = 2.0 * f->eta_n[k] - 2.0 * aniS_vep * d1 * eta_vep;
+      D[1][k] = 2.0 * aniS_vep * d1 * eta_vep;
+      D[2][k] = -2.0 * aniS_vep * d2 * eta_vep;
+      D[3][k] = 0.0;
+      D[4][k] = 2.0 * aniS_vep * d1 * eta_vep;
+      D[5][k] = 2.0 * f->eta_n[k] - 2.0 * aniS_vep * d1 * eta_vep;
+      D[6][k] = 2.0 * aniS_vep * d2 * eta_vep;
+      D[7][k] = 0.0;
+      continue;
+    }
+    const double eta_e = (m->elastic == 1) ? dt * f->mu_n[k] : 1.0;
+    const double K = (compressible == 1) ? 1.0 / f->bet_n[k] : 0.0;
+    if (aniso) {
+      angle = f->angle_n[k];
+      const double lay_ang = angle - M_PI / 2.0;
+      lxlz = cos(lay_ang) * sin(lay_ang);
+      lx2 = cos(lay_ang) * cos(lay_ang);
+    }
+    double Exx, Ezz, Exz;
+    orc_effective_strain_rate(&Exx, &Ezz, &Exz, f->exxd[k], f->ezzd[k], f->exz_n[k], f->sxxd0[k], f->szzd0[k],
+                              f->sxz0_n[k], d1, d2, aniS_vep, eta_e, m->elastic);
+    const double e_a2 = eta_vep / (ani_vep * ani_vep);
+    const double Gxz = 2.0 * Exz;
+    const double Dxx = Exx * (1.0 - aniS_vep * d1) + Ezz * aniS_vep * d1 - Gxz * aniS_vep * d2;
+    const double Dzz = Ezz * (1.0 - aniS_vep * d1) + Exx * aniS_vep * d1 + Gxz * aniS_vep * d2;
+    const double Axx = -Exx * d1 * e_a2 + Ezz * d1 * e_a2 - Gxz * d2 * e_a2;
+    const double Azz = Exx * d1 * e_a2 - Ezz * d1 * e_a2 + Gxz * d2 * e_a2;
+    double de[4] = {0, 0, 0, 0}, dv[4] = {0, 0, 0, 0}, da[4] = {0, 0, 0, 0}, drhodp = 0.0;
+    orc_fd_node nk = nn;
+    nk.T0 = f->T0_n[k];
+    orc_fd_derivatives(m, mt, aniso, 1, Exx, Ezz, Exz, f->p_in[k], ani_vep, angle, lx2, lxlz, k, &nk, f->eta_n[k],
+                       de, dv, da, &drhodp);
+    if (ops->drhodp_n) ops->drhodp_n[k] = drhodp;
+    D[0][k] = 2.0 * (1.0 - aniS_vep * d1) * eta_vep + 2.0 * de[0] * Dxx - K * dt * dv[0] + 2.0 * da[0] * Axx;
+    D[1][k] = 2.0 * aniS_vep * d1 * eta_vep + 2.0 * de[1] * Dxx - K * dt * dv[1] + 2.0 * da[1] * Axx;
+    D[2][k] = -2.0 * aniS_vep * d2 * eta_vep + 2.0 * de[2] * Dxx - K * dt * dv[2] + 2.0 * da[2] * Axx;
+    D[3][k] = 2.0 * de[3] * Dxx - K * dt * dv[3] + 2.0 * da[3] * Axx;
+    D[4][k] = 2.0 * aniS_vep * d1 * eta_vep + 2.0 * de[0] * Dzz - K * dt * dv[0] + 2.0 * da[0] * Azz;
+    D[5][k] = 2.0 * (1.0 - aniS_vep * d1) * eta_vep + 2.0 * de[1] * Dzz - K * dt * dv[1] + 2.0 * da[1] * Azz;
+    D[6][k] = 2.0 * aniS_vep * d2 * eta_vep + 2.0 * de[2] * Dzz - K * dt * dv[2] + 2.0 * da[2] * Azz;
+    D[7][k] = 2.0 * de[3] * Dzz - K * dt * dv[3] + 2.0 * da[3] * Azz;
+  }
+  /* vertices: StokesRoutines.c:170-200 (Picard), :325-380 (Newton) */
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t k = 0; k < Nv; k++) {
+    double *D[4] = {ops->D31_s, ops->D32_s, ops->D33_s, ops->D34_s};
+    if (f->BCg_type[k] == 30) {
+      for (int j = 0; j < 4; j++) D[j][k] = 0.0;
+      continue;
+    }
+    const double eta_vep = f->eta_s[k];
+    double ani_vep = 1.0, aniS_vep = 0.0, d1 = 0.0, d2 = 0.0, angle = 0.0, lxlz = 0.0, lx2 = 0.0;
+    if (aniso) {
+      ani_vep = f->aniso_factor_s[k];
+      aniS_vep = 1.0 - 1.0 / ani_vep;
+      d1 = f->d1_s[k];
+      d2 = f->d2_s[k];
+    }
+    if (!jacobian) {
+      D[0][k] = -2.0 * aniS_vep * d2 * eta_vep;
+      D[1][k] = 2.0 * aniS_vep * d2 * eta_vep;
+      D[2][k] = eta_vep + 2.0 * aniS_vep * (d1 - 0.5) * eta_vep;
+      D[3][k] = 0.0;
+      continue;
+    }
+    const double eta_e = (m->elastic == 1) ? dt * f->mu_s[k] : 1.0;
+    if (aniso) {
+      angle = f->angle_s[k];
+      const double lay_ang = angle - M_PI / 2.0;
+      lxlz = cos(lay_ang) * sin(lay_ang);
+      lx2 = cos(lay_ang) * cos(lay_ang);
+    }
+    double Exx, Ezz, Exz;
+    orc_effective_strain_rate(&Exx, &Ezz, &Exz, f->exxd_s[k], f->ezzd_s[k], f->exz[k], f->sxxd0_s[k],
+                              f->szzd0_s[k], f->sxz0[k], d1, d2, aniS_vep, eta_e, m->elastic);
+    const double e_a2 = eta_vep / (ani_vep * ani_vep);
+    const double Gxz = 2. * Exz;
+    const double Dxz = -Exx * aniS_vep * d2 + Ezz * aniS_vep * d2 + Gxz * (aniS_vep * (d1 - 0.5) + 0.5);
+    const double Axz = -Exx * d2 * e_a2 + Ezz * d2 * e_a2 + Gxz * e_a2 * (d1 - 0.5);
+    double de[4] = {0, 0, 0, 0}, dv[4] = {0, 0, 0, 0}, da[4] = {0, 0, 0, 0};
+    orc_fd_derivatives(m, mt, aniso, 0, Exx, Ezz, Exz, f->P_s[k], ani_vep, angle, lx2, lxlz, k, &ns, f->eta_s[k],
+                       de, dv, da, NULL);
+    D[0][k] = -2.0 * aniS_vep * d2 * eta_vep + 2.0 * de[0] * Dxz + 2.0 * da[0] * Axz;
+    D[1][k] = 2.0 * aniS_vep * d2 * eta_vep + 2.0 * de[1] * Dxz + 2.0 * da[1] * Axz;
+    D[2][k] = (2.0 * aniS_vep * (d1 - 0.5) + 1.0) * eta_vep + 2.0 * de[2] * Dxz + 2.0 * da[2] * Axz;
+    D[3][k] = 2.0 * de[3] * Dxz + 2.0 * da[3] * Axz;
+    if (isnan(D[3][k]) || isinf(D[3][k])) {  /* :384-385 */
+#pragma omp critical(orc_ops)
+      if (status == MDZ_OK) status = MDZ_ENONFINITE;
+    }
+  }
+  return status;
+}

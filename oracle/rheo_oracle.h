@@ -39,6 +39,11 @@ int orc_sweep_aniso(const mdz_model *model, const mdz_materials *mat, const mdz_
 int orc_points(const mdz_model *model, const mdz_materials *mat, const mdz_point_inputs *in,
                mdz_point_outputs *out, int64_t n, int aniso);
 
+/* RheologicalOperators (StokesRoutines.c:75-410), finite-difference derivatives of
+ * DerivativesOnTheFly_n/_s (FD_Jacobian.c:48-323) when jacobian = 1. */
+int orc_operators(const mdz_model *model, const mdz_materials *mat, const mdz_grid_fields *f,
+                  mdz_operator_fields *ops, int jacobian, int compressible, int aniso);
+
 /* InterpCentroidsToVerticesDouble (GridRoutines.c:108) alone. */
 void orc_interp_c2v(const mdz_model *model, const double *centroid, const signed char *BCp_type,
                     const signed char *BCg_type, double *vertex);
