@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm start")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--no-operators", action="store_true", help="skip the Newton-operator timing")
     args = ap.parse_args()
     if args.size is None:
         args.size = 4097 if args.workload == "aniso" else 2049
@@ -415,6 +416,30 @@ def main():
                      "speedup_vs_reference_start": warm["value"] / ref_r["value"],
                      "iteration_ratio_vs_reference_start": ref_r["mean_newton_iters"] / warm["mean_newton_iters"]})
 
+    # ---- RheologicalOperators, Newton form: 8 perturbed local solves per node and phase ----
+    newton_op = None
+    if not args.no_operators:
+        ops = R.alloc_operator_fields(w.Nc, w.Nv, like=d["eta_n"])
+        sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE)  # the state the operator linearises
+        for _ in range(args.warmup):
+            ctx.operators(w.model, w.mat, fs, ops, jacobian=1, aniso=aniso, mem=R.MEM_DEVICE)
+        barrier()
+        op_ms, op_calls = [], 0
+        e0.record(stream)
+        for _ in range(args.steps):
+            _, ost = ctx.operators(w.model, w.mat, fs, ops, jacobian=1, aniso=aniso, mem=R.MEM_DEVICE)
+            op_ms.append(ost.elapsed_ms)
+            op_calls = ost.phase_calls
+        e1.record(stream)
+        barrier()
+        ms_op = REP.max_over_ranks(e0.elapsed_time(e1), dev) / args.steps
+        newton_op = {"what": "RheologicalOperators(Jacobian=1): D tensors with finite-difference derivatives, "
+                             "8 perturbed local solves per node and active phase",
+                     "ms_per_launch": ms_op, "node_updates_per_s": REP.whole_job_rate(w.nodes, ws, ms_op),
+                     "local_solves_per_launch": int(op_calls),
+                     "local_solves_per_s": op_calls * ws / (ms_op * 1e-3)}
+        del ops
+
     # ---- end to end through the C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -488,7 +513,7 @@ def main():
                        "parallelism": f"{ws} independent grid(s), one per GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
-            "reference_start": ref_r, "warm_start": warm, "autotune": tune}
+            "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op}
     print(json.dumps(line))
     if ws > 1:
         REP.finalize()

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "mlp_train.cuh"
+#include "operators.cuh"
 #include "rheo_kernels.cuh"
 
 #include <algorithm>
@@ -234,7 +235,7 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 // slot numbering of the host-mode mirrors
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
-       S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_COUNT };
+       S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_COUNT = S_OP + OP_COUNT };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -1053,6 +1054,69 @@ int mdz_rheo_get_launch_shape(mdz_rheo_ctx *c, int aniso, int *block, int *grid_
   *block = c->block[aniso ? 1 : 0];
   *grid_cap = c->grid_cap[aniso ? 1 : 0];
   return MDZ_OK;
+}
+
+int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat, const mdz_grid_fields *f,
+                       mdz_operator_fields *ops, int jacobian, int compressible, int aniso, int mem, int flags,
+                       mdz_sweep_stats *st) {
+  if (!ctx || !md || !mat || !f || !ops) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (flags & ~MDZ_SWEEP_REF_START) return MDZ_EINVAL;
+  if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  static thread_local OpArgs A;
+  memset(&A, 0, sizeof(A));
+  int rc = fold_model(md, mat, A.M);
+  if (rc != MDZ_OK) return rc;
+  for (int p = 0; p < A.M.np; p++) fold_phase(mat, md, p, A.ph[p]);
+  A.compressible = compressible != 0;
+  A.need_lnd = need_lnd(mat, A.M.np);
+  A.polish = (flags & MDZ_SWEEP_REF_START) ? 0 : ctx->polish_iters;
+  const size_t Nc = (size_t)A.M.Nc, Nv = (size_t)A.M.Nv;
+  const bool host = (mem == MDZ_MEM_HOST);
+  const bool anis = aniso != 0, jac = jacobian != 0;
+  // inputs: the sweep's inputs (the ones the local solve reads) and its outputs
+  FieldLists L;
+  {
+    // the output lists are not written here; only their presence checks are shared
+    mdz_grid_fields g = *f;
+    if ((rc = field_lists(md, &g, anis, L)) != MDZ_OK) return rc;
+  }
+  if (!f->eta_n || !f->eta_s || !f->T_s || !f->P_s || !f->d0_s || !f->phi0_s) return MDZ_EINVAL;
+  double *dout[OP_COUNT] = {ops->D11_n, ops->D12_n, ops->D13_n, ops->D14_n, ops->D21_n, ops->D22_n, ops->D23_n,
+                            ops->D24_n, jac ? ops->drhodp_n : nullptr, ops->D31_s, ops->D32_s, ops->D33_s,
+                            ops->D34_s};
+  for (int i = 0; i < OP_COUNT; i++) if (i != OP_DRHODP && !dout[i]) return MDZ_EINVAL;
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  Mirror mi{ctx};
+  for (int i = 0; i < L.nci; i++) A.ci[i] = mi.in(L.cin[i], S_CI + i, Nc, host);
+  for (int i = 0; i < L.nvi; i++) A.vi[i] = mi.in(L.vin[i], S_VI + i, Nv, host);
+  for (int p = 0; p < A.M.np; p++) {
+    A.perc_n[p] = mi.in(f->phase_perc_n[p], S_PN + p, Nc, host);
+    A.perc_s[p] = mi.in(f->phase_perc_s[p], S_PS + p, Nv, host);
+    A.peta_n[p] = mi.in((const double *)f->phase_eta_n[p], S_EN + p, Nc, host);
+    A.peta_s[p] = mi.in((const double *)f->phase_eta_s[p], S_ES + p, Nv, host);
+  }
+  A.bcp = mi.in(f->BCp_type, S_BCP, Nc, host);
+  A.bcg = mi.in(f->BCg_type, S_BCG, Nv, host);
+  A.eta_n = mi.in((const double *)f->eta_n, S_CO + CO_eta, Nc, host);
+  A.eta_s = mi.in((const double *)f->eta_s, S_VO + VO_eta, Nv, host);
+  A.T_s = mi.in((const double *)f->T_s, S_VO + VO_T, Nv, host);
+  A.P_s = mi.in((const double *)f->P_s, S_VO + VO_P, Nv, host);
+  A.d0_s = mi.in((const double *)f->d0_s, S_VO + VO_d0, Nv, host);
+  A.phi0_s = mi.in((const double *)f->phi0_s, S_VO + VO_phi0, Nv, host);
+  for (int i = 0; i < OP_COUNT; i++) A.D[i] = mi.out(dout[i], S_OP + i, i < OP_D31 ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  A.stats = ctx->d_stats;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_operators(A, anis, jac, ctx->stream));
+  ctx->launches = 1;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  for (int i = 0; i < OP_COUNT; i++) mi.back(dout[i], S_OP + i, i < OP_D31 ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  return finish(ctx, st);
 }
 
 int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {

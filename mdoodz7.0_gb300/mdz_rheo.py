@@ -298,6 +298,9 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_batch_sweep.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
     lib.mdz_rheo_batch_capture.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_uint64]
     lib.mdz_rheo_batch_launch.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
+    lib.mdz_rheo_operators.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
+                                       C.POINTER(OperatorFields), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.POINTER(SweepStats)]
     lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -485,6 +488,18 @@ class Context:
     def points(self, model, mat, pin, pout, n, aniso=0, mem=MEM_HOST):
         return self.lib.mdz_rheo_points(self.handle, C.byref(model), C.byref(mat), C.byref(pin),
                                         C.byref(pout), n, aniso, mem)
+
+    # ---- viscosity tensors of the momentum equations
+    def operators(self, model, mat, fields, ops: dict, jacobian=1, compressible=0, aniso=False, mem=MEM_HOST,
+                  flags=0, check=True):
+        """RheologicalOperators into the D arrays of `ops` (numpy or device tensors, as `mem`)."""
+        st = SweepStats()
+        o = make_operator_fields(ops)
+        rc = self.lib.mdz_rheo_operators(self.handle, C.byref(model), C.byref(mat), C.byref(fields.struct),
+                                         C.byref(o), jacobian, compressible, int(aniso), mem, flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_operators")
+        return rc, st
 
     # ---- launch-shape autotuner
     AUTOTUNE_CANDIDATES = [(b, w) for b in (128, 64) for w in (0, 1, 2, 4, 8)]  # (threads per block, waves)

@@ -40,7 +40,36 @@ GRID_CASES = {
     "plain_large_air": (lambda: _air(W.plain_large(seed=5, ncx=12, ncz=12)), False, 0),
     "aniso": (lambda: W.aniso(seed=6, ncx=12, ncz=10), True, 0),
     "aniso_typical_harmonic": (lambda: _set(W.aniso(seed=7, ncx=10, ncz=11, sc=W.TYPICAL), eta_average=1), True, 0),
+    "plain_large_dilatant_density": (lambda: _dilatant_density(W.plain_large(seed=8, ncx=12, ncz=11)), False, 0),
 }
+
+# RheologicalOperators on the fields a grid case's sweep produced:
+# name: (grid case, jacobian, compressible)
+OPERATOR_CASES = {
+    "plain_large_picard": ("plain_large", 0, 0),
+    "plain_large_newton": ("plain_large", 1, 0),
+    "plain_large_typical_newton": ("plain_large_typical", 1, 0),
+    "plain_large_harmonic_newton": ("plain_large_harmonic", 1, 0),
+    "plain_large_geometric_periodic_newton": ("plain_large_geometric_periodic", 1, 0),
+    "plain_large_air_newton": ("plain_large_air", 1, 0),
+    "dilatant_density_newton_compressible": ("plain_large_dilatant_density", 1, 1),
+    "aniso_picard": ("aniso", 0, 0),
+    "aniso_newton_compressible": ("aniso", 1, 1),
+    "aniso_typical_harmonic_newton": ("aniso_typical_harmonic", 1, 0),
+}
+
+
+def _dilatant_density(w):
+    """Dilation 10 deg, a finite bulk modulus and a pressure-dependent density, so the
+    plastic-divergence and density derivatives of the Newton operator are exercised."""
+    for k in ("dil_n", "dil_s"):
+        w.arrays[k][:] = 10.0 * W.DEG
+    for k in ("bet_n", "bet_s"):
+        w.arrays[k][:] = 1e-11
+    for p in range(w.mat.Nb_phases):
+        w.mat.density_model[p] = 1
+        w.mat.rho[p], w.mat.alp[p], w.mat.bet[p] = 3300.0, 3e-5, 1e-11
+    return w
 
 
 def _set(w, **kv):

@@ -1,8 +1,9 @@
 """Generate the golden fixtures from MDOODZ7.0's own code.
 
-Runs the reference's NonNewtonianViscosityGrid(Aniso) and ViscosityConcise(Aniso),
-compiled from the MDOODZ7.0 sources by oracle/Makefile (target `ref`), on the
-cases of cases.py and stores their outputs in tests/golden/*.npz.  Inputs are
+Runs the reference's NonNewtonianViscosityGrid(Aniso), RheologicalOperators (on the
+fields the sweep produced) and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
+sources by oracle/Makefile (target `ref`), on the cases of cases.py and stores their
+outputs in tests/golden/*.npz.  Inputs are
 regenerated from the seeds by the tests; a SHA-256 of the inputs is stored
 beside the outputs so that a change in the generators is caught.
 
@@ -65,6 +66,15 @@ def main():
         O.ref_sweep(w.model, w.mat, R.FieldSet(a), final_update=fu, aniso=aniso)
         np.savez_compressed(os.path.join(HERE, f"grid_{name}.npz"), inputs_sha256=dig, **grid_outputs(a))
         print("grid", name, w.nodes, "nodes")
+    for name, (grid_case, jac, comp) in cases.OPERATOR_CASES.items():
+        builder, aniso, fu = cases.GRID_CASES[grid_case]
+        w = builder()
+        O.ref_sweep(w.model, w.mat, R.FieldSet(w.arrays), final_update=fu, aniso=aniso)
+        ops = R.alloc_operator_fields(w.Nc, w.Nv)
+        O.ref_operators(w.model, w.mat, R.FieldSet(w.arrays), ops, jac, comp, aniso)
+        np.savez_compressed(os.path.join(HERE, f"operators_{name}.npz"), inputs_sha256=grid_inputs_digest(builder()),
+                            **ops)
+        print("operators", name)
     for name in cases.POINT_CASES:
         md, m, pin, aniso, centroid, fu = cases.point_case(name)
         n = pin["phase"].size

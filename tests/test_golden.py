@@ -37,3 +37,32 @@ def test_oracle_points_match_golden(name):
     assert O.orc_points(md, m, pi, po, n, int(aniso)) == R.MDZ_OK
     for k in R.PT_OUT:
         assert np.array_equal(out[k].view(np.uint64), g[k].view(np.uint64)), k
+
+
+def swept_grid(grid_case):
+    """The inputs of a grid case with the reference sweep's outputs (from its golden
+    fixture) filled in: the state RheologicalOperators reads."""
+    builder, aniso, fu = cases.GRID_CASES[grid_case]
+    w = builder()
+    g = np.load(os.path.join(GOLDEN, f"grid_{grid_case}.npz"))
+    for k in g.files:
+        if k == "inputs_sha256":
+            continue
+        if k in ("phase_eta_n", "phase_eta_s"):
+            for p in range(w.mat.Nb_phases):
+                w.arrays[k][p][:] = g[k][p]
+        elif w.arrays.get(k) is not None:
+            w.arrays[k][:] = g[k]
+    return w, aniso
+
+
+@pytest.mark.parametrize("name", list(cases.OPERATOR_CASES))
+def test_oracle_operators_match_golden(name):
+    grid_case, jac, comp = cases.OPERATOR_CASES[name]
+    w, aniso = swept_grid(grid_case)
+    g = np.load(os.path.join(GOLDEN, f"operators_{name}.npz"))
+    assert str(g["inputs_sha256"]) == grid_inputs_digest(cases.GRID_CASES[grid_case][0]()), "input generator changed"
+    ops = R.alloc_operator_fields(w.Nc, w.Nv)
+    assert O.orc_operators(w.model, w.mat, R.FieldSet(w.arrays), ops, jac, comp, aniso) == R.MDZ_OK
+    for k in R.OPS_N + R.OPS_S:
+        assert np.array_equal(ops[k].view(np.uint64), g[k].view(np.uint64)), k
