@@ -1106,7 +1106,12 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materia
   A.P_s = mi.in((const double *)f->P_s, S_VO + VO_P, Nv, host);
   A.d0_s = mi.in((const double *)f->d0_s, S_VO + VO_d0, Nv, host);
   A.phi0_s = mi.in((const double *)f->phi0_s, S_VO + VO_phi0, Nv, host);
-  for (int i = 0; i < OP_COUNT; i++) A.D[i] = mi.out(dout[i], S_OP + i, i < OP_D31 ? Nc : Nv, host);
+  for (int i = 0; i < OP_COUNT; i++) {
+    const size_t n = i < OP_D31 ? Nc : Nv;
+    // drhodp_n is not written at air cells, as in the reference: keep the caller's values there
+    A.D[i] = (i == OP_DRHODP) ? (double *)mi.in((const double *)dout[i], S_OP + i, n, host)
+                              : mi.out(dout[i], S_OP + i, n, host);
+  }
   if (mi.err) return mi.err;
   A.stats = ctx->d_stats;
   if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;

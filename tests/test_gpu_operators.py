@@ -59,12 +59,20 @@ def op_errors(got, ref, arrays, model, mat):
         scale = np.where(scale > 0, scale, 1.0)
         e = np.where(g == r, 0.0, np.abs(g - r) / scale)
         out[k] = float(np.max(e)) if e.size else 0.0
+        if e.size and out[k] > 0:
+            i = int(np.argmax(e))
+            WORST[k] = (i, float(g[i]), float(r[i]), float(scale[i]))
     return out
+
+
+WORST = {}
 
 
 def check(errs, label, jac):
     bad = {k: v for k, v in errs.items() if v > (BAR_S if k.endswith("_s") else BAR_N) * (1 if jac else 1e-4)}
     print(label, {k: f"{v:.1e}" for k, v in errs.items()})
+    for k in bad:
+        print("  worst", k, "(node, gpu, reference, scale) =", WORST.get(k))
     assert not bad, f"{label}: {bad}"
 
 
