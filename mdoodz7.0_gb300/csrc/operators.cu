@@ -26,16 +26,11 @@ struct OpNode {
 };
 
 // PhaseRheologyLoop_v1 for one perturbed input: every active phase's local solve,
-// accumulated into the derivative slots.
+// accumulated into the derivative slots.  ctx / an: the node set-up of this input.
 template <bool ANISO>
-__device__ __forceinline__ void phase_loop(const OpArgs &A, const OpNode &nd, const NodeIn &in, int is_centroid,
-                                           double sign, double denom, double &detadE, double &ddivpdE,
-                                           double &danidE, double *drhodP, DevStats *acc_calls) {
-  NodeCtx ctx;
-  AnisoNode an;
-  if (ANISO) node_setup_aniso(A.M, in, A.need_lnd != 0, ctx, an);
-  else node_setup_iso(A.M, in, A.need_lnd != 0, ctx);
-  (void)acc_calls;
+__device__ __forceinline__ void phase_loop(const OpArgs &A, const OpNode &nd, const NodeIn &in, const NodeCtx &ctx,
+                                           const AnisoNode &an, int is_centroid, double sign, double denom,
+                                           double &detadE, double &ddivpdE, double &danidE, double *drhodP) {
   for (int p = 0; p < A.M.np; p++) {
     const double vol = nd.centroid ? A.perc_n[p][nd.idx] : A.perc_s[p][nd.idx];
     if (!(fabs(vol) > 1e-13)) continue;
@@ -66,6 +61,11 @@ __device__ __forceinline__ void fd_derivatives(const OpArgs &A, const OpNode &nd
   const double pert[4] = {tol * fabs(b.Exx) + tol / 1e10, tol * fabs(b.Ezz) + tol / 1e10,
                           tol * fabs(b.Exz) + tol / 1e10, tol * fabs(b.P) + tol / 1e10};
   double vscratch = 0.0;
+  // the node set-up once; a strain-rate perturbation then only changes the invariant
+  NodeCtx base;
+  AnisoNode base_an;
+  if (ANISO) node_setup_aniso(A.M, b, A.need_lnd != 0, base, base_an);
+  else node_setup_iso(A.M, b, A.need_lnd != 0, base);
 #pragma unroll 1
   for (int dir = 0; dir < 4; dir++) {
 #pragma unroll 1
@@ -80,8 +80,15 @@ __device__ __forceinline__ void fd_derivatives(const OpArgs &A, const OpNode &nd
       in.centroid = is_centroid;
       in.want_rho = (is_centroid == 2);
       const double denom = (dir == 2 ? 4.0 : 2.0) * pert[dir];
-      phase_loop<ANISO>(A, nd, in, is_centroid, sign, denom, d[dir], nd.centroid ? v[dir] : vscratch, a[dir],
-                        &drhodp, nullptr);
+      NodeCtx ctx = base;
+      AnisoNode an = base_an;
+      if (dir < 3) {
+        if (ANISO) node_strain_aniso(in, ctx, an);
+        else node_strain_iso(A.M, in, ctx);
+        node_strain_update(ctx);
+      }
+      phase_loop<ANISO>(A, nd, in, ctx, an, is_centroid, sign, denom, d[dir], nd.centroid ? v[dir] : vscratch,
+                        a[dir], &drhodp);
     }
   }
   if (A.M.eta_average == 1)

@@ -119,9 +119,10 @@ __device__ __forceinline__ void set_status(int &st, int code) {
 // ---------------------------------------------------------------------------------------
 // node set-up: invariants and switches shared by the phases (RheologyDensity.c:461-496)
 // ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void node_strain_update(NodeCtx &c);
+
 __device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c) {
-  c.lnEii = fast_log(c.Eii);
-  c.inv2Eii = 0.5 / c.Eii;
+  node_strain_update(c);
   c.Traw = in.T;
   c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
   c.invT = 1.0 / c.T;
@@ -131,12 +132,23 @@ __device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &i
   c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
 }
 
-__device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn &in, bool need_lnd,
-                                               NodeCtx &c) {
+// The strain-rate invariant and what depends on it (RheologyDensity.c:455-459); the
+// rest of the node set-up does not depend on the strain rate.
+__device__ __forceinline__ void node_strain_iso(const ModelConst &M, const NodeIn &in, NodeCtx &c) {
   const double Eyy = -(in.Exx + in.Ezz);
   double Eii = sqrt(0.5 * (in.Exx * in.Exx + in.Ezz * in.Ezz + Eyy * Eyy) + in.Exz * in.Exz);
   if (Eii * M.scale_E < 1e-30) Eii = M.Eii_floor;
   c.Eii = Eii;
+}
+
+__device__ __forceinline__ void node_strain_update(NodeCtx &c) {
+  c.lnEii = fast_log(c.Eii);
+  c.inv2Eii = 0.5 / c.Eii;
+}
+
+__device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn &in, bool need_lnd,
+                                               NodeCtx &c) {
+  node_strain_iso(M, in, c);
   c.elastic = (M.step == 0) ? 0 : M.elastic;
   c.plastic_on = (M.step != 0);
   c.K = 1.0 / in.beta;
@@ -812,8 +824,8 @@ struct AnisoNode {
   double Er_xx, Er_zz, Er_xz, lxlz, lx2;
 };
 
-__device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c,
-                                                 AnisoNode &a) {
+// Rotated strain rate and its invariant (AnisotropyRoutines.c:379-390).
+__device__ __forceinline__ void node_strain_aniso(const NodeIn &in, NodeCtx &c, AnisoNode &a) {
   const double lx2 = in.lx2, lxlz = in.lxlz, nz2 = 1.0 - lx2;  // :379-383
   a.lx2 = lx2; a.lxlz = lxlz;
   a.Er_xx = lx2 * in.Exx + nz2 * in.Ezz + 2. * lxlz * in.Exz;
@@ -821,6 +833,11 @@ __device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const Node
   a.Er_xz = -lxlz * in.Exx + lxlz * in.Ezz + (lx2 - nz2) * in.Exz;
   const double Er_yy = -a.Er_xx - a.Er_zz;
   c.Eii = sqrt(0.5 * (a.Er_xx * a.Er_xx + a.Er_zz * a.Er_zz + Er_yy * Er_yy) + a.Er_xz * a.Er_xz);
+}
+
+__device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c,
+                                                 AnisoNode &a) {
+  node_strain_aniso(in, c, a);
   c.elastic = (M.step == 0) ? 0 : M.elastic;
   c.plastic_on = 1;
   c.K = 1.0 / in.beta;

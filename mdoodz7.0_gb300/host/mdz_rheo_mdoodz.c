@@ -1,12 +1,12 @@
 /*
- * mdz_rheo_mdoodz.c -- the MDOODZ7.0-side drop-in: NonNewtonianViscosityGrid and
- * NonNewtonianViscosityGridAniso with the reference's own signatures
- * (MDLIB/mdoodz-private.h:423 and :437), evaluated on the GPU by
+ * mdz_rheo_mdoodz.c -- the MDOODZ7.0-side drop-in: NonNewtonianViscosityGrid,
+ * NonNewtonianViscosityGridAniso and RheologicalOperators with the reference's own
+ * signatures (MDLIB/mdoodz-private.h:423, :437 and :607), evaluated on the GPU by
  * libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
  *
  * It is compiled inside the MDOODZ build, against MDLIB/mdoodz-private.h, in place of
- * the two definitions at MDLIB/RheologyDensity.c:1131 and
- * MDLIB/AnisotropyRoutines.c:885 (those are compiled out under MDZ_RHEO_GB300).
+ * the definitions at MDLIB/RheologyDensity.c:1131, MDLIB/AnisotropyRoutines.c:885 and
+ * MDLIB/StokesRoutines.c:75 (those are compiled out under MDZ_RHEO_GB300).
  * Each call unpacks `grid`, `mat_prop`, `params` and `scale` into the library's
  * plain-pointer structs and runs one sweep on host memory: the library uploads the
  * inputs, runs the kernel and writes every output back into the caller's arrays in
@@ -162,6 +162,29 @@ void NonNewtonianViscosityGrid(grid *mesh, mat_prop *materials, params *model, N
   (void)Nmodel; /* passed by value and unused, as in the reference */
   mdz_sweep_grid(mesh, materials, model, scaling, final_update, 0);
   ApplySetGridDensityOverride(mesh, model); /* RheologyDensity.c:1425 */
+}
+
+/* RheologicalOperators (StokesRoutines.c:75): the D tensors, with the Newton operator's
+ * finite-difference derivatives (FD_Jacobian.c) solved on the GPU. */
+void RheologicalOperators(grid *mesh, params *model, mat_prop *materials, scale *scaling, int Jacobian,
+                          int anisotropy) {
+  mdz_model md;
+  mdz_materials mt;
+  mdz_grid_fields f;
+  mdz_operator_fields ops;
+  mdz_sweep_stats st;
+  mdz_model_from(&md, mesh, model, scaling);
+  mdz_materials_from(&mt, materials);
+  mdz_fields_from(&f, mesh, anisotropy);
+  ops.D11_n = mesh->D11_n; ops.D12_n = mesh->D12_n; ops.D13_n = mesh->D13_n; ops.D14_n = mesh->D14_n;
+  ops.D21_n = mesh->D21_n; ops.D22_n = mesh->D22_n; ops.D23_n = mesh->D23_n; ops.D24_n = mesh->D24_n;
+  ops.drhodp_n = mesh->drhodp_n;
+  ops.D31_s = mesh->D31_s; ops.D32_s = mesh->D32_s; ops.D33_s = mesh->D33_s; ops.D34_s = mesh->D34_s;
+  memset(&st, 0, sizeof(st));
+  const int rc = mdz_rheo_operators(mdz_context(), &md, &mt, &f, &ops, Jacobian, (int)model->compressible,
+                                    anisotropy, MDZ_MEM_HOST, 0, &st);
+  if (rc == MDZ_ENONFINITE) { fprintf(stderr, "EXIT: D34 is NAN!\n"); exit(1); } /* :384-385 */
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
 }
 
 void NonNewtonianViscosityGridAniso(grid *mesh, mat_prop *materials, params *model, Nparams Nmodel,

@@ -125,6 +125,11 @@ def shimtest():
             fn = getattr(lib, name)
             fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields), C.c_int, C.c_int]
             fn.restype = C.c_int
+        for name in ("shimtest_ref_operators", "shimtest_shim_operators"):
+            fn = getattr(lib, name)
+            fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields),
+                           C.POINTER(R.OperatorFields), C.c_int, C.c_int, C.c_int]
+            fn.restype = C.c_int
         _shim = lib
     return _shim
 
@@ -152,6 +157,15 @@ def ref_operators(model, mat, fs: "R.FieldSet", ops: dict, jacobian=1, compressi
     o = R.make_operator_fields(ops)
     return lib.ref_operators(C.byref(model), C.byref(mat), C.byref(fs.struct), C.byref(o), jacobian,
                              compressible, int(aniso))
+
+
+def shim_operators(model, mat, fs: "R.FieldSet", ops: dict, jacobian=1, compressible=0, aniso=False,
+                   drop_in=True):
+    """RheologicalOperators on a harness-built `grid`: the drop-in's or the reference's."""
+    lib = shimtest()
+    fn = lib.shimtest_shim_operators if drop_in else lib.shimtest_ref_operators
+    return fn(C.byref(model), C.byref(mat), C.byref(fs.struct), C.byref(R.make_operator_fields(ops)), jacobian,
+              compressible, int(aniso))
 
 
 def orc_points(model, mat, pin, pout, n, aniso=0):

@@ -127,7 +127,6 @@ int ref_sweep(const mdz_model *m, const mdz_materials *mat, const mdz_grid_field
   return 0;
 }
 
-#ifndef MDZ_NO_OPERATORS /* the drop-in check links no StokesRoutines.c */
 /* RheologicalOperators (StokesRoutines.c:75) on the same kind of grid, writing `ops`.
  * The anisotropic Newton branch reads FS_AR_n / FS_AR_s without using them in the
  * coefficients; they are set to 1. */
@@ -157,7 +156,6 @@ int ref_operators(const mdz_model *m, const mdz_materials *mat, const mdz_grid_f
   free(mp);
   return 0;
 }
-#endif
 
 int ref_points(const mdz_model *m, const mdz_materials *mat, const mdz_point_inputs *in,
                mdz_point_outputs *out, int64_t n, int aniso) {

@@ -6,9 +6,6 @@
  * their prototypes do not apply. */
 void AddFieldToGroup(void) {}
 void AddGroupToHDF5(void) {}
-#ifdef MDZ_STUB_APPLYBC /* builds without StokesRoutines.c */
-void ApplyBC(void) {}
-#endif
 void CreateOutputHDF5(void) {}
 void P2Mastah(void) {}
 void PartialMelting(void) {}

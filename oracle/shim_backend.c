@@ -45,3 +45,11 @@ int mdz_rheo_sweep_aniso(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_ma
   if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
   return orc_sweep_aniso(model, mat, f, final_update, NULL, NULL, stats);
 }
+
+int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat, const mdz_grid_fields *f,
+                       mdz_operator_fields *ops, int jacobian, int compressible, int aniso, int mem, int flags,
+                       mdz_sweep_stats *stats) {
+  (void)stats;
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_operators(model, mat, f, ops, jacobian, compressible, aniso);
+}

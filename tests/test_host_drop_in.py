@@ -54,3 +54,16 @@ def test_periodic_and_air():
     for k in OUT_FIELDS:
         if a.get(k) is not None:
             assert np.array_equal(field(b, k), field(a, k), equal_nan=True), k
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("jacobian", [0, 1])
+def test_drop_in_operators_match_reference(aniso, jacobian):
+    w = W.aniso(seed=9, ncx=20) if aniso else W.plain_large(seed=9, ncx=22, ncz=18)
+    O.shim_sweep(w.model, w.mat, R.FieldSet(w.arrays), 0, aniso, drop_in=False)
+    a = R.alloc_operator_fields(w.Nc, w.Nv)
+    b = R.alloc_operator_fields(w.Nc, w.Nv)
+    assert O.shim_operators(w.model, w.mat, R.FieldSet(clone(w.arrays)), a, jacobian, 1, aniso, drop_in=False) == 0
+    assert O.shim_operators(w.model, w.mat, R.FieldSet(clone(w.arrays)), b, jacobian, 1, aniso, drop_in=True) == 0
+    for k in a:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
