@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm start")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--no-operators", action="store_true", help="skip the Newton-operator timing")
+    ap.add_argument("--no-strain-rates", action="store_true", help="skip the StrainRateComponents timing")
     args = ap.parse_args()
     if args.size is None:
         args.size = 4097 if args.workload == "aniso" else 2049
@@ -92,6 +93,14 @@ def algorithmic_bytes(w, aniso=False):
     cen = 8 * (18 + extra_in + np_ + np_) + 1 + 8 * 23                  # inputs, fractions, phase_eta, BC, outputs
     ver = 8 * (13 + extra_in + np_ + np_) + 1 + 8 * (6 + int(aniso)) + 8 * 4   # + the four interpolated fields
     return nc * cen + nv * ver
+
+
+def strain_rate_bytes(nx, nz):
+    """Compulsory HBM bytes of one StrainRateComponents launch (RheologyDensity.c:2001-2097)
+    on a grid without air: u_in (Nx*(Nz+1)) and v_in ((Nx+1)*Nz) read, BCp and BCg read
+    (1 byte each), five centroid and five vertex fields written once."""
+    nc, nv = (nx - 1) * (nz - 1), nx * nz
+    return 8 * (nx * (nz + 1) + (nx + 1) * nz) + nc + nv + 8 * 5 * (nc + nv)
 
 
 class ClockSampler:
@@ -440,6 +449,35 @@ def main():
                      "local_solves_per_s": op_calls * ws / (ms_op * 1e-3)}
         del ops
 
+    # ---- StrainRateComponents on the same grid: the step before the sweep ----
+    strain = None
+    if not args.no_strain_rates:
+        vf = W.velocity_field(seed=REP.replica_seed(9, rank), ncx=args.size)
+        sr = {k: torch.from_numpy(v).to(dev) for k, v in vf.arrays.items()}
+        sr_args = (vf.model, vf.info["dx"], vf.info["dz"], sr)
+        for _ in range(max(3, args.warmup)):
+            ctx.strain_rates(*sr_args, mem=R.MEM_DEVICE)
+        barrier()
+        reps = 20 * args.steps  # ~0.2 ms each: more launches for a stable mean
+        sr_ms = []
+        e0.record(stream)
+        for _ in range(reps):
+            _, sst = ctx.strain_rates(*sr_args, mem=R.MEM_DEVICE)
+            sr_ms.append(sst.elapsed_ms)
+        e1.record(stream)
+        barrier()
+        ms_sr = REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps
+        sr_launch_ms = statistics.mean(sr_ms)
+        sr_bytes = strain_rate_bytes(vf.model.Nx, vf.model.Nz)
+        strain = {"what": "StrainRateComponents: velocity gradients, divergence, deviatoric normal rates, shear "
+                          "rate and spin, centroid averages and vertex interpolation in one launch",
+                  "grid": f"{args.size}x{args.size} cells", "ms_per_call": ms_sr,
+                  "kernel_ms_per_launch": sr_launch_ms,
+                  "algorithmic_bytes_per_launch": sr_bytes,
+                  "hbm_achieved_gbs": sr_bytes / (sr_launch_ms * 1e-3) / 1e9,
+                  "l2": f"{sr_bytes / 1e9:.2f} GB per launch, larger than L2; no flush"}
+        del sr, vf
+
     # ---- end to end through the C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -486,6 +524,8 @@ def main():
     roof["hbm_achieved_gbs"] = bytes_alg / (launch_ms * 1e-3) / 1e9
     roof["hbm_frac"] = (roof["hbm_achieved_gbs"] / hbm) if hbm else None
     roof["algorithmic_bytes_per_launch"] = bytes_alg
+    if strain is not None:
+        strain["hbm_frac"] = strain["hbm_achieved_gbs"] / hbm if hbm else None
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -513,7 +553,8 @@ def main():
                        "parallelism": f"{ws} independent grid(s), one per GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
-            "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op}
+            "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op,
+            "strain_rates": strain}
     print(json.dumps(line))
     if ws > 1:
         REP.finalize()

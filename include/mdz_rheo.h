@@ -270,6 +270,31 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_mate
                        const mdz_grid_fields *f, mdz_operator_fields *ops, int jacobian, int compressible,
                        int aniso, int mem, int flags, mdz_sweep_stats *stats);
 
+/* ---- strain rates from the velocity field -------------------------------
+ * The arrays StrainRateComponents (MDLIB/RheologyDensity.c:2001-2097) reads and
+ * writes, in the staggered layout of `grid`: u_in holds Nx*(Nz+1) x-velocity nodes
+ * (u node k + l*Nx), v_in holds (Nx+1)*Nz z-velocity nodes (v node k + l*(Nx+1)).
+ * wxz is written at vertices with BCg_type != 30 only; elsewhere it keeps its value. */
+typedef struct mdz_strain_rate_fields {
+  const double *u_in, *v_in;
+  const signed char *BCp_type, *BCg_type;
+  double *div_u, *exxd, *ezzd, *exz_n, *wxz_n;   /* centroids, (Nx-1)*(Nz-1) each */
+  double *exz, *wxz, *exxd_s, *ezzd_s, *div_u_s; /* vertices, Nx*Nz each */
+} mdz_strain_rate_fields;
+
+/* StrainRateComponents (MDLIB/RheologyDensity.c:2001-2097, the first step of
+ * UpdateNonLinearity, MDLIB/StokesRoutines.c:55-58): velocity gradients, divergence
+ * and deviatoric normal strain rates at centroids, shear strain rate and spin at
+ * vertices, their 4-point centroid averages, and the vertex interpolation of exxd,
+ * ezzd, div_u (InterpCentroidsToVerticesDouble, MDLIB/GridRoutines.c:108-210), in one
+ * launch.  dx, dz are mesh->dx, mesh->dz; out_of_plane and compressible are
+ * params.out_of_plane and params.compressible; model supplies Nx, Nz and periodic_x.
+ * Results are those of the reference to the last bit.  `mem` as for the sweep;
+ * `flags` may hold MDZ_SWEEP_ASYNC (device memory only); `stats` may be NULL. */
+int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *model, double dx, double dz, int out_of_plane,
+                          double compressible, mdz_strain_rate_fields *sr, int mem, int flags,
+                          mdz_sweep_stats *stats);
+
 /* ---- allocation-free variant (no reference counterpart) ----------------
  * mdz_rheo_points on the CURRENT device without any context and without allocating:
  * no cudaMalloc / cudaFree / cudaHostAlloc and no allocating library call.  For callers

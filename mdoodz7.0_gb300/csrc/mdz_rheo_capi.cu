@@ -15,6 +15,7 @@
 #include "mlp_train.cuh"
 #include "operators.cuh"
 #include "rheo_kernels.cuh"
+#include "strain_rates.cuh"
 
 #include <algorithm>
 #include <random>
@@ -235,7 +236,8 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 // slot numbering of the host-mode mirrors
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
-       S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_COUNT = S_OP + OP_COUNT };
+       S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
+       S_SRU = S_SR + SR_COUNT, S_SRV, S_COUNT };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -1121,6 +1123,57 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materia
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   for (int i = 0; i < OP_COUNT; i++) mi.back(dout[i], S_OP + i, i < OP_D31 ? Nc : Nv, host);
   if (mi.err) return mi.err;
+  return finish(ctx, st);
+}
+
+int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *md, double dx, double dz, int out_of_plane,
+                          double compressible, mdz_strain_rate_fields *sr, int mem, int flags, mdz_sweep_stats *st) {
+  if (!ctx || !md || !sr) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
+  if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
+  double *out[SR_COUNT] = {sr->div_u, sr->exxd, sr->ezzd, sr->exz_n, sr->wxz_n,
+                           sr->exz, sr->wxz, sr->exxd_s, sr->ezzd_s, sr->div_u_s};
+  if (!sr->u_in || !sr->v_in || !sr->BCp_type || !sr->BCg_type) return MDZ_EINVAL;
+  for (int i = 0; i < SR_COUNT; i++) if (!out[i]) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  StrainArgs A;
+  memset(&A, 0, sizeof(A));
+  A.Nx = md->Nx; A.Nz = md->Nz; A.Ncx = md->Nx - 1; A.Ncz = md->Nz - 1;
+  A.periodic_x = md->periodic_x;
+  A.dx = dx; A.dz = dz;
+  A.oop_half = (out_of_plane == 1) ? 0.5 : 0.0;  // RheologyDensity.c:2006, :2033
+  A.comp3 = compressible * 1.0 / 3.0;             // RheologyDensity.c:2039-2040
+  const size_t Nx = (size_t)md->Nx, Nz = (size_t)md->Nz;
+  const size_t Nc = (Nx - 1) * (Nz - 1), Nv = Nx * Nz;
+  const bool host = (mem == MDZ_MEM_HOST);
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  Mirror mi{ctx};
+  A.u = mi.in(sr->u_in, S_SRU, Nx * (Nz + 1), host);
+  A.v = mi.in(sr->v_in, S_SRV, (Nx + 1) * Nz, host);
+  A.bcp = mi.in(sr->BCp_type, S_BCP, Nc, host);
+  A.bcg = mi.in(sr->BCg_type, S_BCG, Nv, host);
+  for (int i = 0; i < SR_COUNT; i++) {
+    const size_t n = i < SR_EXZ ? Nc : Nv;
+    // wxz is not written at air vertices, as in the reference: keep the caller's values there
+    A.out[i] = (i == SR_WXZ) ? (double *)mi.in((const double *)out[i], S_SR + i, n, host)
+                             : mi.out(out[i], S_SR + i, n, host);
+  }
+  if (mi.err) return mi.err;
+  int rc;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_strain_rates(A, ctx->stream));
+  ctx->launches = 1;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  for (int i = 0; i < SR_COUNT; i++) mi.back(out[i], S_SR + i, i < SR_EXZ ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  if (flags & MDZ_SWEEP_ASYNC) {
+    ctx->pending = 1;
+    return MDZ_OK;
+  }
   return finish(ctx, st);
 }
 

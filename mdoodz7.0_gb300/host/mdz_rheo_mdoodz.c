@@ -1,12 +1,13 @@
 /*
  * mdz_rheo_mdoodz.c -- the MDOODZ7.0-side drop-in: NonNewtonianViscosityGrid,
- * NonNewtonianViscosityGridAniso and RheologicalOperators with the reference's own
- * signatures (MDLIB/mdoodz-private.h:423, :437 and :607), evaluated on the GPU by
- * libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
+ * NonNewtonianViscosityGridAniso, RheologicalOperators and StrainRateComponents with
+ * the reference's own signatures (MDLIB/mdoodz-private.h:423, :437, :607 and :426),
+ * evaluated on the GPU by libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
  *
  * It is compiled inside the MDOODZ build, against MDLIB/mdoodz-private.h, in place of
- * the definitions at MDLIB/RheologyDensity.c:1131, MDLIB/AnisotropyRoutines.c:885 and
- * MDLIB/StokesRoutines.c:75 (those are compiled out under MDZ_RHEO_GB300).
+ * the definitions at MDLIB/RheologyDensity.c:1131, MDLIB/AnisotropyRoutines.c:885,
+ * MDLIB/StokesRoutines.c:75 and MDLIB/RheologyDensity.c:2001 (those are compiled out
+ * under MDZ_RHEO_GB300).
  * Each call unpacks `grid`, `mat_prop`, `params` and `scale` into the library's
  * plain-pointer structs and runs one sweep on host memory: the library uploads the
  * inputs, runs the kernel and writes every output back into the caller's arrays in
@@ -184,6 +185,27 @@ void RheologicalOperators(grid *mesh, params *model, mat_prop *materials, scale 
   const int rc = mdz_rheo_operators(mdz_context(), &md, &mt, &f, &ops, Jacobian, (int)model->compressible,
                                     anisotropy, MDZ_MEM_HOST, 0, &st);
   if (rc == MDZ_ENONFINITE) { fprintf(stderr, "EXIT: D34 is NAN!\n"); exit(1); } /* :384-385 */
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
+}
+
+/* StrainRateComponents (RheologyDensity.c:2001): strain rates, spin and their vertex /
+ * centroid interpolations from u_in, v_in, in one GPU launch.  `scaling` is unused, as
+ * in the reference. */
+void StrainRateComponents(grid *mesh, scale scaling, params *model) {
+  (void)scaling;
+  mdz_model md;
+  mdz_strain_rate_fields sr;
+  mdz_sweep_stats st;
+  memset(&md, 0, sizeof(md));
+  md.Nx = mesh->Nx; md.Nz = mesh->Nz; md.periodic_x = model->periodic_x;
+  sr.u_in = mesh->u_in; sr.v_in = mesh->v_in;
+  sr.BCp_type = mesh->BCp.type; sr.BCg_type = mesh->BCg.type;
+  sr.div_u = mesh->div_u; sr.exxd = mesh->exxd; sr.ezzd = mesh->ezzd; sr.exz_n = mesh->exz_n;
+  sr.wxz_n = mesh->wxz_n; sr.exz = mesh->exz; sr.wxz = mesh->wxz; sr.exxd_s = mesh->exxd_s;
+  sr.ezzd_s = mesh->ezzd_s; sr.div_u_s = mesh->div_u_s;
+  memset(&st, 0, sizeof(st));
+  const int rc = mdz_rheo_strain_rates(mdz_context(), &md, mesh->dx, mesh->dz, model->out_of_plane,
+                                       model->compressible, &sr, MDZ_MEM_HOST, 0, &st);
   if (rc != MDZ_OK) mdz_fail(rc, &st);
 }
 

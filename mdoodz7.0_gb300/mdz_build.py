@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "build")
 LIB = os.path.join(BUILD, "libmdz_rheo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["rheo_kernels.cu", "mdz_rheo_capi.cu", "fp64_probe.cu", "mlp_train.cu", "operators.cu"]
+SOURCES = ["rheo_kernels.cu", "mdz_rheo_capi.cu", "fp64_probe.cu", "mlp_train.cu", "operators.cu",
+           "strain_rates.cu"]
 
 
 def nvcc() -> str:

@@ -140,6 +140,31 @@ def alloc_operator_fields(nc: int, nv: int, like=None) -> Dict[str, object]:
     return {**{k: np.zeros(nc) for k in OPS_N}, **{k: np.zeros(nv) for k in OPS_S}}
 
 
+SR_N = ["div_u", "exxd", "ezzd", "exz_n", "wxz_n"]
+SR_S = ["exz", "wxz", "exxd_s", "ezzd_s", "div_u_s"]
+
+
+class StrainRateFields(C.Structure):
+    """mdz_strain_rate_fields: velocities in, strain rates and spin out (StrainRateComponents)."""
+    _fields_ = [("u_in", _P), ("v_in", _P), ("BCp_type", _P), ("BCg_type", _P)] + [(n, _P) for n in SR_N + SR_S]
+
+
+def make_strain_rate_fields(arrays: Dict[str, object]) -> StrainRateFields:
+    o = StrainRateFields()
+    for name, _ in StrainRateFields._fields_:
+        setattr(o, name, _ptr(arrays.get(name)))
+    return o
+
+
+def alloc_strain_rate_fields(nc: int, nv: int, like=None) -> Dict[str, object]:
+    """Zeroed output arrays of StrainRateComponents (numpy, or torch on the device of `like`)."""
+    if like is not None:
+        import torch
+        return {**{k: torch.zeros(nc, dtype=torch.float64, device=like.device) for k in SR_N},
+                **{k: torch.zeros(nv, dtype=torch.float64, device=like.device) for k in SR_S}}
+    return {**{k: np.zeros(nc) for k in SR_N}, **{k: np.zeros(nv) for k in SR_S}}
+
+
 MLP_IN, MLP_HID = 16, 64
 
 
@@ -301,6 +326,9 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_operators.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                        C.POINTER(OperatorFields), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(SweepStats)]
+    lib.mdz_rheo_strain_rates.argtypes = [C.c_void_p, C.POINTER(Model), C.c_double, C.c_double, C.c_int,
+                                          C.c_double, C.POINTER(StrainRateFields), C.c_int, C.c_int,
+                                          C.POINTER(SweepStats)]
     lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -499,6 +527,18 @@ class Context:
                                          C.byref(o), jacobian, compressible, int(aniso), mem, flags, C.byref(st))
         if check and rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_operators")
+        return rc, st
+
+    def strain_rates(self, model, dx, dz, sr: dict, out_of_plane=0, compressible=0.0, mem=MEM_HOST, flags=0,
+                     check=True):
+        """StrainRateComponents: `sr` holds u_in, v_in, BCp_type, BCg_type and the ten
+        output arrays (numpy or device tensors, as `mem`)."""
+        st = SweepStats()
+        o = make_strain_rate_fields(sr)
+        rc = self.lib.mdz_rheo_strain_rates(self.handle, C.byref(model), dx, dz, out_of_plane, float(compressible),
+                                            C.byref(o), mem, flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_strain_rates")
         return rc, st
 
     # ---- launch-shape autotuner

@@ -423,3 +423,51 @@ def many_grids(seed: int = 7, n: int = 64, lo: int = 65, hi: int = 1025, sc: Sca
         out.append(grid_workload("many_grids", side, side, mat, seed * 1000 + g, dt=dt, sc=sc,
                                  grain_size=(1e-5, 1e-2), softening=(30.0, 5.0, 0.0, 1.0)))
     return out
+
+
+def velocity_field(seed: int = 9, ncx: int = 2049, ncz: Optional[int] = None, air: float = 0.0,
+                   periodic: int = 0, sc: Scale = SI, L: float = 1e5, v0: float = 1e-9) -> Workload:
+    """Input of StrainRateComponents on ncx x ncz cells: staggered velocities of a smooth
+    random flow, u at Nx x (Nz+1) nodes and v at (Nx+1) x Nz nodes (rows include the
+    ghost nodes of MDOODZ's staggered grid), about v0 m/s plus 1 % node-scale noise, on a
+    square L x L domain.  With air > 0 the top part of the domain above a wavy surface at
+    height 1 - air (fraction of L) is air: those cells have BCp_type 30, those of the row
+    just below the surface 31, vertices above it BCg_type 30.  Output arrays are filled
+    with a sentinel (wxz keeps it at air vertices).  dx and dz are in `info`."""
+    ncz = ncx if ncz is None else ncz
+    rng = np.random.default_rng(seed)
+    nx, nz = ncx + 1, ncz + 1
+    nc, nv = ncx * ncz, nx * nz
+    dx, dz = L / ncx / sc.L, L / ncz / sc.L
+    vs = v0 / (sc.L / sc.t)
+
+    def flow(xs, zs):
+        f = smooth_fields(rng, 1, xs, zs)[0]
+        return vs * (f + 0.01 * rng.standard_normal(f.shape))
+
+    # u node (k, l): x = k / ncx, z = (l - 0.5) / ncz; v node (k, l): x = (k - 0.5) / ncx, z = l / ncz
+    u = flow(np.arange(nx) / ncx, (np.arange(nz + 1) - 0.5) / ncz)
+    v = flow((np.arange(nx + 1) - 0.5) / ncx, np.arange(nz) / ncz)
+    a: Dict[str, object] = {"u_in": np.ascontiguousarray(u.ravel()), "v_in": np.ascontiguousarray(v.ravel())}
+    bcp = np.full((ncz, ncx), -1, dtype=np.int8)
+    bcg = np.full((nz, nx), -1, dtype=np.int8)
+    if air > 0.0:
+        ph = rng.uniform(0, 2 * np.pi)
+        xc, zc = (np.arange(ncx) + 0.5) / ncx, (np.arange(ncz) + 0.5) / ncz
+        h = 1.0 - air + 0.05 * np.sin(4.0 * np.pi * xc + ph)
+        above = zc[:, None] > h[None, :]
+        bcp[above] = 30
+        below = (~above) & (zc[:, None] > h[None, :] - 1.0 / ncz)
+        bcp[below] = 31
+        xv, zv = np.arange(nx) / ncx, np.arange(nz) / ncz
+        hv = 1.0 - air + 0.05 * np.sin(4.0 * np.pi * xv + ph)
+        bcg[zv[:, None] > hv[None, :]] = 30
+    a["BCp_type"] = bcp.ravel()
+    a["BCg_type"] = bcg.ravel()
+    for k in R.SR_N:
+        a[k] = np.full(nc, -7.0)
+    for k in R.SR_S:
+        a[k] = np.full(nv, -7.0)
+    model = make_model(ncx, ncz, 1, sc=sc)
+    model.periodic_x = periodic
+    return Workload("velocity_field", model, None, a, info=dict(seed=seed, ncx=ncx, ncz=ncz, dx=dx, dz=dz))

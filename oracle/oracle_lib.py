@@ -168,6 +168,35 @@ def shim_operators(model, mat, fs: "R.FieldSet", ops: dict, jacobian=1, compress
               compressible, int(aniso))
 
 
+def _strain_fn(lib, name):
+    fn = getattr(lib, name)
+    fn.argtypes = [C.POINTER(R.Model), C.c_double, C.c_double, C.c_int, C.c_double, C.POINTER(R.StrainRateFields)]
+    fn.restype = C.c_int
+    return fn
+
+
+def orc_strain_rates(model, dx, dz, sr: dict, out_of_plane=0, compressible=0.0):
+    """StrainRateComponents on the restatement; `sr` is a dict of numpy arrays."""
+    return _strain_fn(oracle(), "orc_strain_rates")(C.byref(model), dx, dz, out_of_plane, float(compressible),
+                                                    C.byref(R.make_strain_rate_fields(sr)))
+
+
+def ref_strain_rates(model, dx, dz, sr: dict, out_of_plane=0, compressible=0.0):
+    """StrainRateComponents of the reference build."""
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    return _strain_fn(lib, "ref_strain_rates")(C.byref(model), dx, dz, out_of_plane, float(compressible),
+                                               C.byref(R.make_strain_rate_fields(sr)))
+
+
+def shim_strain_rates(model, dx, dz, sr: dict, out_of_plane=0, compressible=0.0, drop_in=True):
+    """StrainRateComponents on a harness-built `grid`: the drop-in's or the reference's."""
+    name = "shimtest_shim_strain_rates" if drop_in else "shimtest_ref_strain_rates"
+    return _strain_fn(shimtest(), name)(C.byref(model), dx, dz, out_of_plane, float(compressible),
+                                        C.byref(R.make_strain_rate_fields(sr)))
+
+
 def orc_points(model, mat, pin, pout, n, aniso=0):
     return oracle().orc_points(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso)
 

@@ -1,7 +1,7 @@
 /*
- * ref_harness.c -- drives the reference's own NonNewtonianViscosityGrid(Aniso)
- * and ViscosityConcise(Aniso), compiled from the MDOODZ7.0 sources, from the
- * plain-pointer structs of include/mdz_rheo.h.
+ * ref_harness.c -- drives the reference's own NonNewtonianViscosityGrid(Aniso),
+ * ViscosityConcise(Aniso), RheologicalOperators and StrainRateComponents, compiled
+ * from the MDOODZ7.0 sources, from the plain-pointer structs of include/mdz_rheo.h.
  *
  * TEST INFRASTRUCTURE ONLY: it is built by oracle/Makefile (target `ref`)
  * into oracle/_ref/ when the reference tree is present, and is used to pin the
@@ -154,6 +154,29 @@ int ref_operators(const mdz_model *m, const mdz_materials *mat, const mdz_grid_f
   free(g->FS_AR_n); free(g->FS_AR_s);
   free_grid(g);
   free(mp);
+  return 0;
+}
+
+/* StrainRateComponents (RheologyDensity.c:2001) on a grid holding only the arrays it
+ * touches. */
+int ref_strain_rates(const mdz_model *m, double dx, double dz, int out_of_plane, double compressible,
+                     mdz_strain_rate_fields *sr) {
+  quiet_log();
+  params pm;
+  scale sc;
+  fill_params(&pm, &sc, m);
+  pm.out_of_plane = out_of_plane;
+  pm.compressible = compressible;
+  mdz_grid_fields none;
+  memset(&none, 0, sizeof(none));
+  grid *g = make_grid(m, &none);
+  g->dx = dx; g->dz = dz;
+  g->u_in = W(sr->u_in); g->v_in = W(sr->v_in);
+  g->BCp.type = (signed char *)sr->BCp_type; g->BCg.type = (signed char *)sr->BCg_type;
+  g->div_u = sr->div_u; g->exxd = sr->exxd; g->ezzd = sr->ezzd; g->exz_n = sr->exz_n; g->wxz_n = sr->wxz_n;
+  g->exz = sr->exz; g->wxz = sr->wxz; g->exxd_s = sr->exxd_s; g->ezzd_s = sr->ezzd_s; g->div_u_s = sr->div_u_s;
+  StrainRateComponents(g, sc, &pm);
+  free_grid(g);
   return 0;
 }
 

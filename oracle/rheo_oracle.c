@@ -1240,3 +1240,62 @@ int orc_operators(const mdz_model *m, const mdz_materials *mt, const mdz_grid_fi
   }
   return status;
 }
+
+/* ------------------------------------------------------------------------ */
+/* StrainRateComponents, RheologyDensity.c:2001-2097: the reference's four    */
+/* passes in its order -- centroid divergence and deviatoric normal rates,    */
+/* vertex shear rate and spin (wxz is left alone at air vertices), their      */
+/* 4-vertex centroid averages, and the vertex interpolation of exxd, ezzd and */
+/* div_u (InterpCentroidsToVerticesDouble, restated above).                   */
+/* ------------------------------------------------------------------------ */
+int orc_strain_rates(const mdz_model *m, double dx, double dz, int out_of_plane, double compressible,
+                     mdz_strain_rate_fields *sr) {
+  if (m->Nx < 2 || m->Nz < 2) return MDZ_EINVAL;
+  const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1;
+  const double oop = (out_of_plane == 1) ? 1.0 : 0.0;
+  const double *u = sr->u_in, *v = sr->v_in;
+  const signed char *BCp = sr->BCp_type, *BCg = sr->BCg_type;
+#pragma omp parallel for
+  for (int c0 = 0; c0 < Ncx * Ncz; c0++) {
+    const int k = c0 % Ncx, l = c0 / Ncx, c1 = k + l * Nx, c2 = k + l * (Nx + 1);
+    sr->div_u[c0] = 0.0;
+    sr->exxd[c0] = 0.0;
+    sr->ezzd[c0] = 0.0;
+    if (BCp[c0] != 30 && BCp[c0] != 31) {
+      const double dvxdx = (u[c1 + 1 + Nx] - u[c1 + Nx]) / dx;
+      const double dvzdz = (v[c2 + Nx + 1 + 1] - v[c2 + 1]) / dz;
+      const double dvydy = oop * 0.5 * (dvxdx + dvzdz);
+      sr->div_u[c0] = dvxdx + dvzdz + dvydy;
+      sr->exxd[c0] = dvxdx - compressible * 1.0 / 3.0 * sr->div_u[c0];
+      sr->ezzd[c0] = dvzdz - compressible * 1.0 / 3.0 * sr->div_u[c0];
+    }
+  }
+#pragma omp parallel for
+  for (int c1 = 0; c1 < Nx * Nz; c1++) {
+    const int k = c1 % Nx, l = c1 / Nx, c2 = k + l * (Nx + 1);
+    sr->exz[c1] = 0.0;
+    if (BCg[c1] != 30) {
+      const double dvxdz = (u[c1 + Nx] - u[c1]) / dz;
+      const double dvzdx = (v[c2 + 1] - v[c2]) / dx;
+      sr->exz[c1] = 0.5 * (dvxdz + dvzdx);
+      sr->wxz[c1] = 0.5 * (dvzdx - dvxdz);
+    }
+  }
+#pragma omp parallel for
+  for (int c0 = 0; c0 < Ncx * Ncz; c0++) {
+    const int k = c0 % Ncx, l = c0 / Ncx, c1 = k + l * Nx;
+    const int corner[4] = {c1, c1 + 1, c1 + Nx, c1 + Nx + 1};
+    sr->exz_n[c0] = 0.0;
+    sr->wxz_n[c0] = 0.0;
+    if (BCp[c0] != 30 && BCp[c0] != 31) {
+      for (int q = 0; q < 4; q++)
+        if (BCg[corner[q]] != 30) sr->exz_n[c0] += 0.25 * sr->exz[corner[q]];
+      for (int q = 0; q < 4; q++)
+        if (BCg[corner[q]] != 30) sr->wxz_n[c0] += 0.25 * sr->wxz[corner[q]];
+    }
+  }
+  orc_interp_c2v(m, sr->exxd, BCp, BCg, sr->exxd_s);
+  orc_interp_c2v(m, sr->ezzd, BCp, BCg, sr->ezzd_s);
+  orc_interp_c2v(m, sr->div_u, BCp, BCg, sr->div_u_s);
+  return MDZ_OK;
+}

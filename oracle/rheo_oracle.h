@@ -7,9 +7,10 @@
  *
  * It restates, in plain C and in the reference's floating-point evaluation
  * order, MDLIB/RheologyDensity.c:116-1426 and MDLIB/AnisotropyRoutines.c:
- * 257-727, 885-1217, plus InterpCentroidsToVerticesDouble
- * (MDLIB/GridRoutines.c:108-210).  Built with -ffp-contract=off it is
- * bit-identical to the reference compiled from its own sources on x86-64
+ * 257-727, 885-1217, MDLIB/StokesRoutines.c:75-410 with MDLIB/FD_Jacobian.c:48-323,
+ * StrainRateComponents (MDLIB/RheologyDensity.c:2001-2097), plus
+ * InterpCentroidsToVerticesDouble (MDLIB/GridRoutines.c:108-210).  Built with
+ * -ffp-contract=off it is bit-identical to the reference compiled from its own sources on x86-64
  * (pinned by tests/test_oracle_vs_reference.py and the committed golden
  * fixtures).  Unlike the reference it never calls exit(): errors come back as
  * MDZ_* status codes, and it also reports local iteration counts.
@@ -43,6 +44,10 @@ int orc_points(const mdz_model *model, const mdz_materials *mat, const mdz_point
  * DerivativesOnTheFly_n/_s (FD_Jacobian.c:48-323) when jacobian = 1. */
 int orc_operators(const mdz_model *model, const mdz_materials *mat, const mdz_grid_fields *f,
                   mdz_operator_fields *ops, int jacobian, int compressible, int aniso);
+
+/* StrainRateComponents (RheologyDensity.c:2001-2097). */
+int orc_strain_rates(const mdz_model *model, double dx, double dz, int out_of_plane, double compressible,
+                     mdz_strain_rate_fields *sr);
 
 /* InterpCentroidsToVerticesDouble (GridRoutines.c:108) alone. */
 void orc_interp_c2v(const mdz_model *model, const double *centroid, const signed char *BCp_type,

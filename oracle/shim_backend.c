@@ -1,14 +1,14 @@
 /*
  * shim_backend.c -- TEST INFRASTRUCTURE ONLY.
  *
- * A CPU stand-in for the context and sweep entry points of libmdz_rheo_gb300.so
- * (include/mdz_rheo.h) that forwards every sweep to the C restatement
- * (rheo_oracle.c).  Linked with the MDOODZ-side drop-in
+ * A CPU stand-in for the context, sweep, operator and strain-rate entry points of
+ * libmdz_rheo_gb300.so (include/mdz_rheo.h) that forwards every call to the C
+ * restatement (rheo_oracle.c).  Linked with the MDOODZ-side drop-in
  * (mdoodz7.0_gb300/host/mdz_rheo_mdoodz.c) and with the reference's own sources
  * into oracle/_ref/libmdz_shimtest.so, it lets a CPU test run the drop-in's
- * NonNewtonianViscosityGrid(Aniso) on a real `grid` and compare it with the
- * reference's, which checks how the drop-in unpacks grid / mat_prop / params /
- * scale.  The GPU library itself is never part of this build.
+ * NonNewtonianViscosityGrid(Aniso), RheologicalOperators and StrainRateComponents
+ * on a real `grid` and compare them with the reference's, which checks how the
+ * drop-in unpacks grid / mat_prop / params / scale.  The GPU library itself is never part of this build.
  */
 #include <stdlib.h>
 
@@ -52,4 +52,12 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_mate
   (void)stats;
   if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
   return orc_operators(model, mat, f, ops, jacobian, compressible, aniso);
+}
+
+int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *model, double dx, double dz, int out_of_plane,
+                          double compressible, mdz_strain_rate_fields *sr, int mem, int flags,
+                          mdz_sweep_stats *stats) {
+  (void)stats;
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_strain_rates(model, dx, dz, out_of_plane, compressible, sr);
 }

@@ -1,7 +1,9 @@
 """Parity cases shared by the golden-fixture generator and the tests.
 
 GRID_CASES are small grids of the benchmark workloads (all field layouts,
-averaging modes, scalings, air cells, periodicity).  POINT_CASES drive
+averaging modes, scalings, air cells, periodicity); OPERATOR_CASES run
+RheologicalOperators on what a grid case's sweep produced; STRAIN_CASES run
+StrainRateComponents on velocity fields (air, periodicity, one cell, ragged).  POINT_CASES drive
 ViscosityConcise / ViscosityConciseAniso directly on random points and cover
 the branches the grid workloads do not reach: Popov et al. 2025 plasticity
 (plast=2, with and without the tensile line search), paleowattmeter grain size
@@ -58,6 +60,16 @@ OPERATOR_CASES = {
     "aniso_typical_harmonic_newton": ("aniso_typical_harmonic", 1, 0),
 }
 
+
+# StrainRateComponents on velocity fields:
+# name: (builder, out_of_plane, compressible)
+STRAIN_CASES = {
+    "basic": (lambda: W.velocity_field(seed=11, ncx=12, ncz=10), 0, 0.0),
+    "air_compressible_oop": (lambda: W.velocity_field(seed=12, ncx=13, ncz=12, air=0.3), 1, 1.0),
+    "periodic_air": (lambda: W.velocity_field(seed=13, ncx=11, ncz=14, air=0.25, periodic=1), 0, 1.0),
+    "one_cell": (lambda: W.velocity_field(seed=14, ncx=1, ncz=1), 1, 1.0),
+    "ragged_periodic": (lambda: W.velocity_field(seed=15, ncx=45, ncz=3, air=0.4, periodic=1), 1, 0.0),
+}
 
 def _dilatant_density(w):
     """Dilation 10 deg, a finite bulk modulus and a pressure-dependent density, so the

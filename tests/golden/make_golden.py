@@ -1,7 +1,7 @@
 """Generate the golden fixtures from MDOODZ7.0's own code.
 
 Runs the reference's NonNewtonianViscosityGrid(Aniso), RheologicalOperators (on the
-fields the sweep produced) and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
+fields the sweep produced), StrainRateComponents and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
 sources by oracle/Makefile (target `ref`), on the cases of cases.py and stores their
 outputs in tests/golden/*.npz.  Inputs are
 regenerated from the seeds by the tests; a SHA-256 of the inputs is stored
@@ -24,6 +24,7 @@ import mdz_rheo as R  # noqa: E402
 import oracle_lib as O  # noqa: E402
 
 INPUT_GRID = [k for k in R.CEN_IN + R.VER_IN + R.ANI_IN_N + R.ANI_IN_S + ["BCp_type", "BCg_type"]]
+STRAIN_INPUTS = ["u_in", "v_in", "BCp_type", "BCg_type", "wxz"]
 
 
 def digest(arrays, keys):
@@ -75,6 +76,13 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"operators_{name}.npz"), inputs_sha256=grid_inputs_digest(builder()),
                             **ops)
         print("operators", name)
+    for name, (builder, oop, comp) in cases.STRAIN_CASES.items():
+        w = builder()
+        dig = digest(w.arrays, STRAIN_INPUTS)
+        O.ref_strain_rates(w.model, w.info["dx"], w.info["dz"], w.arrays, oop, comp)
+        np.savez_compressed(os.path.join(HERE, f"strain_rates_{name}.npz"), inputs_sha256=dig,
+                            **{k: w.arrays[k] for k in R.SR_N + R.SR_S})
+        print("strain rates", name)
     for name in cases.POINT_CASES:
         md, m, pin, aniso, centroid, fu = cases.point_case(name)
         n = pin["phase"].size
