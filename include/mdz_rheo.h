@@ -18,6 +18,10 @@
  *                              RheologyDensity.c:2194 GenerateDeformationMaps)
  *   (vertex fields T_s,P_s,d0_s,phi0_s)  <- InterpCentroidsToVerticesDouble
  *                              MDLIB/GridRoutines.c:108, fused into the sweep
+ *   mdz_rheo_operators      <- RheologicalOperators (with FD_Jacobian.c's derivatives)
+ *                              MDLIB/mdoodz-private.h:607, def MDLIB/StokesRoutines.c:75
+ *   mdz_rheo_strain_rates   <- StrainRateComponents
+ *                              MDLIB/mdoodz-private.h:426, def MDLIB/RheologyDensity.c:2001
  *
  * All arithmetic is IEEE binary64.  Unless a call says otherwise it is
  * synchronous (returns after the results are in the caller's buffers), like
@@ -412,6 +416,11 @@ int mdz_rheo_measure_fp64_peak(int device, double *tflops);
  * reference counterpart. */
 int mdz_rheo_math_selftest(int device, const double *x, int64_t n, double *fast_exp_out,
                            double *cuda_exp_out, double *fast_log_out, double *cuda_log_out);
+/* Self-check of the division by a mesh spacing used by mdz_rheo_strain_rates: a[i] / b
+ * by that method and by CUDA's division, for n host numerators.  No reference
+ * counterpart. */
+int mdz_rheo_div_selftest(int device, const double *a, int64_t n, double b, double *fast_out,
+                          double *cuda_out);
 
 #ifdef __cplusplus
 }

@@ -6,9 +6,12 @@
 // timed with CUDA events.
 // mdz_rheo_math_selftest: the table-driven exp/log of fp64_math.cuh next to CUDA's
 // exp/log on the same arguments, for the accuracy tests.
+// mdz_rheo_div_selftest: the division by a known divisor of fp64_div.cuh next to CUDA's
+// division, for the bit-for-bit test.
 #include <cuda_runtime.h>
 
 #include "../../include/mdz_rheo.h"
+#include "fp64_div.cuh"
 #include "fp64_math.cuh"
 
 namespace {
@@ -39,7 +42,34 @@ __global__ void k_math(const double *x, long long n, double *fe, double *ce, dou
   cl[i] = log(v);
 }
 
+__global__ void k_div(const double *a, long long n, mdz::Divisor d, double *fast, double *plain) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fast[i] = mdz::div_by(a[i], d);
+  plain[i] = a[i] / d.b;
+}
+
 }  // namespace
+
+extern "C" int mdz_rheo_div_selftest(int device, const double *a, int64_t n, double b, double *fast_out,
+                                     double *cuda_out) {
+  if (!a || n < 0 || !fast_out || !cuda_out) return MDZ_EINVAL;
+  if (n == 0) return MDZ_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return MDZ_ECUDA;
+  const size_t bytes = (size_t)n * sizeof(double);
+  double *d = nullptr;
+  if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return MDZ_ENOMEM;
+  int rc = MDZ_OK;
+  if (cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK) {
+    k_div<<<(unsigned)((n + 255) / 256), 256>>>(d, n, mdz::make_divisor(b), d + n, d + 2 * n);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = MDZ_ECUDA;
+  }
+  if (rc == MDZ_OK && cudaMemcpy(fast_out, d + n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK && cudaMemcpy(cuda_out, d + 2 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
+  cudaFree(d);
+  return rc;
+}
 
 extern "C" int mdz_rheo_math_selftest(int device, const double *x, int64_t n, double *fast_exp_out,
                                       double *cuda_exp_out, double *fast_log_out, double *cuda_log_out) {

@@ -1142,7 +1142,7 @@ int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *md, double dx, dou
   memset(&A, 0, sizeof(A));
   A.Nx = md->Nx; A.Nz = md->Nz; A.Ncx = md->Nx - 1; A.Ncz = md->Nz - 1;
   A.periodic_x = md->periodic_x;
-  A.dx = dx; A.dz = dz;
+  A.dx = make_divisor(dx); A.dz = make_divisor(dz);
   A.oop_half = (out_of_plane == 1) ? 0.5 : 0.0;  // RheologyDensity.c:2006, :2033
   A.comp3 = compressible * 1.0 / 3.0;             // RheologyDensity.c:2039-2040
   const size_t Nx = (size_t)md->Nx, Nz = (size_t)md->Nz;

@@ -9,13 +9,15 @@
 // values at the ghost-ring cells (ring cell (i, j) maps to one centroid, as in the
 // reference's ringed copy) and vertex values -- then forms the averages and the
 // interpolation from shared memory and writes every output once.  Each velocity is
-// read from HBM about once and every output written once; the halo costs 1 + 1/32 +
-// 1/8 extra evaluations per node.
+// read from HBM about once and every output written once; the halo adds
+// (kSrTx + kSrTz + 1) / (kSrTx * kSrTz) evaluations per node.  The kernel is bound by
+// the FP64 pipe (GB300 runs FP64 at 1/64 of the FP32 rate), so the forms below keep
+// the FP64 instruction count low wherever that leaves every result bit unchanged.
 //
-// Every operation rounds as the reference's does (double division is correctly
-// rounded; the products and sums that a compiler could contract into an FMA are
-// written with explicit round-to-nearest intrinsics), so the results are bitwise
-// those of the reference.
+// Every operation rounds as the reference's does (divisions by the mesh spacing are
+// correctly rounded, fp64_div.cuh; the products and sums that a compiler could contract
+// into an FMA are written with explicit round-to-nearest intrinsics), so the results
+// are bitwise those of the reference.
 #include "strain_rates.cuh"
 
 namespace mdz {
@@ -37,17 +39,30 @@ __device__ __forceinline__ int ring_row(int j, int Ncz) {
 constexpr int kW = kSrTx + 1, kH = kSrTz + 1;  // tile plus the one-node halo
 
 struct SrShared {
-  double div[kH][kW], exx[kH][kW], ezz[kH][kW];  // centroid values at ring cells (k0+i, l0+j)
-  double exz[kH][kW], wxz[kH][kW];                // vertex values at vertices (k0+i, l0+j)
+  double div[kH][kW], exx[kH][kW], ezz[kH][kW];  // centroid values at ring cells (k0+i, l0+j); +0.0 at air
+  double exz[kH][kW], wxz[kH][kW];                // vertex values at vertices (k0+i, l0+j); +0.0 at air
   unsigned char cin[kH][kW];                      // ring cell's centroid is not air (BCp not 30/31)
-  unsigned char vin[kH][kW];                      // vertex is not air (BCg != 30)
+  unsigned char vin[kH][kW];                      // bit 0: vertex not air (BCg != 30); bit 1: exz, wxz tame
 };
+
+// x == 0 or 2^-1000 <= |x| <= 2^1000: the range in which a quarter of a sum of such
+// values rounds exactly like the sum of their quarters (no subnormal, no overflow)
+__device__ __forceinline__ bool tame(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  return (e - 23u) <= 2000u || (b << 1) == 0ull;
+}
+
+// +0.0 in place of -0.0 (the reference's averages start from +0.0 and never end at -0.0)
+__device__ __forceinline__ double no_negative_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
 
 __global__ void __launch_bounds__(kSrTx * kSrTz) k_strain_rates(const StrainArgs A) {
   __shared__ SrShared S;
   const int Nx = A.Nx, Nz = A.Nz, Ncx = A.Ncx, Ncz = A.Ncz;
   const int k0 = blockIdx.x * kSrTx, l0 = blockIdx.y * kSrTz;
-  const double dx = A.dx, dz = A.dz;
+  const Divisor dx = A.dx, dz = A.dz;
 
   // ---- per-node values of the tile and its halo
   for (int t = threadIdx.x; t < kW * kH; t += blockDim.x) {
@@ -62,8 +77,8 @@ __global__ void __launch_bounds__(kSrTx * kSrTz) k_strain_rates(const StrainArgs
       double dv = 0.0, ex = 0.0, ez = 0.0;
       if (in) {
         const long long c1 = ck + (long long)cl * Nx, c2 = ck + (long long)cl * (Nx + 1);
-        const double dvxdx = (A.u[c1 + 1 + Nx] - A.u[c1 + Nx]) / dx;
-        const double dvzdz = (A.v[c2 + Nx + 2] - A.v[c2 + 1]) / dz;
+        const double dvxdx = div_by(A.u[c1 + 1 + Nx] - A.u[c1 + Nx], dx);
+        const double dvzdz = div_by(A.v[c2 + Nx + 2] - A.v[c2 + 1], dz);
         const double s = __dadd_rn(dvxdx, dvzdz);
         dv = __dadd_rn(s, __dmul_rn(A.oop_half, s));
         ex = __dsub_rn(dvxdx, __dmul_rn(A.comp3, dv));
@@ -78,13 +93,13 @@ __global__ void __launch_bounds__(kSrTx * kSrTz) k_strain_rates(const StrainArgs
       const bool in = A.bcg[c1] != 30;
       double e = 0.0, w = 0.0;
       if (in) {
-        const double dvxdz = (A.u[c1 + Nx] - A.u[c1]) / dz;
-        const double dvzdx = (A.v[c2 + 1] - A.v[c2]) / dx;
+        const double dvxdz = div_by(A.u[c1 + Nx] - A.u[c1], dz);
+        const double dvzdx = div_by(A.v[c2 + 1] - A.v[c2], dx);
         e = 0.5 * (dvxdz + dvzdx);
         w = 0.5 * (dvzdx - dvxdz);
       }
       S.exz[j][i] = e; S.wxz[j][i] = w;
-      S.vin[j][i] = in;
+      S.vin[j][i] = (unsigned char)(in | ((tame(e) && tame(w)) << 1));
     }
   }
   __syncthreads();
@@ -93,16 +108,15 @@ __global__ void __launch_bounds__(kSrTx * kSrTz) k_strain_rates(const StrainArgs
   const int k = k0 + tx, l = l0 + tz;
   if (k < Nx && l < Nz) {
     // vertex outputs: exz, wxz, and exxd_s / ezzd_s / div_u_s from the four ring cells
-    // (k..k+1, l..l+1) as in GridRoutines.c:185-206
+    // (k..k+1, l..l+1), GridRoutines.c:185-206.  The reference weights each ring value
+    // by 0 (air) or 1; air ring cells hold +0.0 here, so the weighted and the plain sums
+    // agree bit for bit and the weights are left out.
     const long long c1 = k + (long long)l * Nx;
     double xs = 0.0, zs = 0.0, ds = 0.0;
-    if (S.vin[tz][tx]) {
-      const double wSW = S.cin[tz][tx], wSE = S.cin[tz][tx + 1];
-      const double wNW = S.cin[tz + 1][tx], wNE = S.cin[tz + 1][tx + 1];
-#define MDZ_RING4(F)                                                                                      \
-  __dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(wSW, S.F[tz][tx]), __dmul_rn(wSE, S.F[tz][tx + 1])), \
-                                      __dmul_rn(wNW, S.F[tz + 1][tx])),                                   \
-                            __dmul_rn(wNE, S.F[tz + 1][tx + 1])))
+    if (S.vin[tz][tx] & 1) {
+#define MDZ_RING4(F)                                                                                  \
+  __dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(S.F[tz][tx], S.F[tz][tx + 1]), S.F[tz + 1][tx]), \
+                            S.F[tz + 1][tx + 1]))
       xs = MDZ_RING4(exx);
       zs = MDZ_RING4(ezz);
       ds = MDZ_RING4(div);
@@ -116,17 +130,36 @@ __global__ void __launch_bounds__(kSrTx * kSrTz) k_strain_rates(const StrainArgs
   }
   if (k < Ncx && l < Ncz) {
     // centroid outputs: own values (ring cell (k+1, l+1)) and the averages of the four
-    // vertices (k..k+1, l..l+1) that are not air (RheologyDensity.c:2067-2089)
+    // vertices (k..k+1, l..l+1) that are not air, RheologyDensity.c:2067-2089
     const long long c0 = k + (long long)l * Ncx;
     double en = 0.0, wn = 0.0;
     if (S.cin[tz + 1][tx + 1]) {
+      const unsigned char f0 = S.vin[tz][tx], f1 = S.vin[tz][tx + 1];
+      const unsigned char f2 = S.vin[tz + 1][tx], f3 = S.vin[tz + 1][tx + 1];
+      if (((f0 | f1 | f2 | f3) & 1) == 0) {
+        // no vertex counts: both stay +0.0
+      } else if ((f0 == 1) | (f1 == 1) | (f2 == 1) | (f3 == 1)) {
+        // a counted value outside the tame range: the reference's sequence of
+        // quarter-value additions, from +0.0, in SW, SE, NW, NE order
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int a = tx + (q & 1), b = tz + (q >> 1);  // SW, SE, NW, NE
-        if (S.vin[b][a]) {
-          en = __dadd_rn(en, __dmul_rn(0.25, S.exz[b][a]));
-          wn = __dadd_rn(wn, __dmul_rn(0.25, S.wxz[b][a]));
+        for (int q = 0; q < 4; q++) {
+          const int a = tx + (q & 1), b = tz + (q >> 1);
+          if (S.vin[b][a] & 1) {
+            en = __dadd_rn(en, __dmul_rn(0.25, S.exz[b][a]));
+            wn = __dadd_rn(wn, __dmul_rn(0.25, S.wxz[b][a]));
+          }
         }
+      } else {
+        // every counted value is tame and air vertices hold +0.0: a quarter of the plain
+        // sum equals the reference's sum of quarters bit for bit, up to the sign of a
+        // zero result
+#define MDZ_QUAD4(F)                                                                                   \
+  no_negative_zero(__dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(S.F[tz][tx], S.F[tz][tx + 1]),         \
+                                                       S.F[tz + 1][tx]),                               \
+                                             S.F[tz + 1][tx + 1])))
+        en = MDZ_QUAD4(exz);
+        wn = MDZ_QUAD4(wxz);
+#undef MDZ_QUAD4
       }
     }
     A.out[SR_DIV][c0] = S.div[tz + 1][tx + 1];

@@ -313,6 +313,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_abi_sizes.argtypes = [C.POINTER(C.c_size_t)]
     lib.mdz_rheo_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.mdz_rheo_math_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64] + [C.c_void_p] * 4
+    lib.mdz_rheo_div_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_points_static.argtypes = [C.POINTER(Model), C.POINTER(Materials), C.POINTER(PointInputs),
                                            C.POINTER(PointOutputs), C.c_int64, C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(SweepStats)]
@@ -387,6 +388,16 @@ def math_selftest(x: np.ndarray, device: int = 0):
     if rc != MDZ_OK:
         raise RheoError(rc, "mdz_rheo_math_selftest")
     return outs
+
+
+def div_selftest(a: np.ndarray, b: float, device: int = 0):
+    """(known-divisor division, CUDA's division) of the float64 array a by b on the GPU."""
+    a = np.ascontiguousarray(a, np.float64)
+    fast, plain = np.empty_like(a), np.empty_like(a)
+    rc = load_library().mdz_rheo_div_selftest(device, a.ctypes.data, a.size, b, fast.ctypes.data, plain.ctypes.data)
+    if rc != MDZ_OK:
+        raise RheoError(rc, "mdz_rheo_div_selftest")
+    return fast, plain
 
 
 def python_struct_sizes():

@@ -50,3 +50,37 @@ def test_log_accuracy():
     assert fl[np.where(x == 1.0)[0][0]] == 0.0
     special = ~fin
     assert np.array_equal(fl[special], cl[special], equal_nan=True)
+
+
+def _near_midpoints(rng, b, n):
+    """Numerators whose quotient by b lies as close as binary64 allows to a midpoint
+    between two doubles (the hardest cases for rounding), and their neighbours."""
+    from fractions import Fraction
+    q = rng.uniform(1.0, 2.0, n) * 2.0 ** rng.integers(-30, 30, n)
+    out = []
+    for v in q:
+        mid = Fraction(float(v)) + Fraction(float(np.spacing(v))) / 2
+        a = float(Fraction(b) * mid)
+        out += [a, np.nextafter(a, np.inf), np.nextafter(a, -np.inf)]
+    return np.array(out)
+
+
+@pytest.mark.parametrize("b", [1e5 / 2049, 1e5 / 4097, 0.1, 1.0 / 3.0, 3.0, 7.0, 1.0, 0.5, 1024.0,
+                               1.9999999999999998, 1.0000000000000002, 48.80429477794046, 2.0 ** -399,
+                               2.0 ** 399, -6.25e-3, 1e-200])
+def test_known_divisor_division_is_exact(b):
+    """The division by a mesh spacing (csrc/fp64_div.cuh) against CUDA's division and
+    numpy's: bit for bit on random numerators of every scale, near-midpoint quotients and
+    the special values (which take CUDA's division itself)."""
+    rng = np.random.default_rng(int(abs(b) * 1e6) % 2 ** 32)
+    a = np.concatenate([rng.standard_normal(1_000_000) * 10.0 ** rng.uniform(-300, 300, 1_000_000),
+                        rng.uniform(-1.0, 1.0, 200_000) * 1e-12,
+                        _near_midpoints(rng, b, 5_000),
+                        [0.0, -0.0, 5e-324, -5e-324, 2.0 ** -500, 2.0 ** 500, 2.0 ** -501, 2.0 ** 501,
+                         1.7976931348623157e308, np.inf, -np.inf, np.nan]])
+    fast, plain = R.div_selftest(a, b)
+    with np.errstate(all="ignore"):
+        host = a / b
+    assert np.array_equal(fast.view(np.uint64)[~np.isnan(a)], plain.view(np.uint64)[~np.isnan(a)])
+    assert np.array_equal(fast.view(np.uint64)[~np.isnan(a)], host.view(np.uint64)[~np.isnan(a)])
+    assert np.isnan(fast[np.isnan(a)]).all()

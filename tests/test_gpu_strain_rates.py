@@ -62,6 +62,18 @@ def test_gpu_strain_rates_device_match_oracle(ctx, ncx, ncz, air, per, oop, comp
         assert same_bits(d[k].cpu().numpy(), ref[k]), k
 
 
+@pytest.mark.parametrize("v0,L", [(1e303, 1e3), (1e-300, 1e7), (3e-308, 1e3)])
+def test_gpu_strain_rates_extreme_magnitudes(ctx, v0, L):
+    """Rates near overflow and in the subnormal range take the kernel's exact
+    reference-order averaging; the results stay bitwise those of the oracle."""
+    w = W.velocity_field(seed=41, ncx=90, ncz=70, air=0.2, v0=v0, L=L)
+    ref = {k: v.copy() for k, v in w.arrays.items()}
+    assert O.orc_strain_rates(w.model, w.info["dx"], w.info["dz"], ref, 1, 1.0) == R.MDZ_OK
+    ctx.strain_rates(w.model, w.info["dx"], w.info["dz"], w.arrays, out_of_plane=1, compressible=1.0)
+    for k in R.SR_N + R.SR_S:
+        assert same_bits(w.arrays[k], ref[k]), k
+
+
 def test_gpu_strain_rates_async_and_errors(ctx):
     w = W.velocity_field(seed=3, ncx=70, ncz=50, air=0.2)
     d = to_dev(w.arrays)

@@ -26,6 +26,8 @@ CASES = {
     "one_column": (lambda: W.velocity_field(seed=6, ncx=1, ncz=17), 1, 1.0),
     "one_row_periodic": (lambda: W.velocity_field(seed=7, ncx=19, ncz=1, periodic=1), 0, 1.0),
     "scaled": (lambda: W.velocity_field(seed=8, ncx=30, ncz=25, air=0.3, sc=W.TYPICAL), 1, 1.0),
+    "near_overflow": (lambda: W.velocity_field(seed=9, ncx=20, ncz=20, air=0.2, v0=1e303, L=1e3), 1, 1.0),
+    "subnormal": (lambda: W.velocity_field(seed=10, ncx=20, ncz=20, air=0.2, v0=3e-308, L=1e3), 1, 1.0),
 }
 
 
