@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--no-operators", action="store_true", help="skip the Newton-operator timing")
     ap.add_argument("--no-strain-rates", action="store_true", help="skip the StrainRateComponents timing")
+    ap.add_argument("--no-prep", action="store_true", help="skip the Softening / ShearModCompExpGrid timing")
     args = ap.parse_args()
     if args.size is None:
         args.size = 4097 if args.workload == "aniso" else 2049
@@ -101,6 +102,17 @@ def strain_rate_bytes(nx, nz):
     (1 byte each), five centroid and five vertex fields written once."""
     nc, nv = (nx - 1) * (nz - 1), nx * nz
     return 8 * (nx * (nz + 1) + (nx + 1) * nz) + nc + nv + 8 * 5 * (nc + nv)
+
+
+def prep_bytes(step, nc, nv, nphases):
+    """Compulsory HBM bytes of one preparation launch on a grid without air: every phase
+    fraction and BC flag read once; softening also reads the plastic strain and the noise
+    (8 + 8 B) and writes fric, dil, C (24 B) per node; the shear modulus writes mu, bet,
+    alp at centroids (24 B) and mu, bet at vertices (16 B)."""
+    reads = (nc + nv) * (8 * nphases + 1)
+    if step == "softening":
+        return reads + (nc + nv) * (16 + 24)
+    return reads + nc * 24 + nv * 16
 
 
 class ClockSampler:
@@ -478,6 +490,36 @@ def main():
                   "l2": f"{sr_bytes / 1e9:.2f} GB per launch, larger than L2; no flush"}
         del sr, vf
 
+    # ---- the sweep's input preparation on the same grid: Softening, ShearModCompExpGrid ----
+    prep = None
+    if not args.no_prep:
+        pw = W.prep_workload(seed=REP.replica_seed(13, rank), ncx=args.size, nphases=args.phases)
+        pd = {k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
+              for k, v in pw.arrays.items()}
+        pfs = R.PrepFieldSet(pd)
+        steps = {"softening": lambda: ctx.softening(pw.model, pw.mat, pfs, marker_noise=1, mem=R.MEM_DEVICE),
+                 "shear_modulus": lambda: ctx.shear_modulus(pw.model, pw.mat, pfs, mem=R.MEM_DEVICE)}
+        prep = {}
+        for name, call in steps.items():
+            for _ in range(max(3, args.warmup)):
+                call()
+            barrier()
+            reps = 20 * args.steps
+            k_ms = []
+            e0.record(stream)
+            for _ in range(reps):
+                _, pst = call()
+                k_ms.append(pst.elapsed_ms)
+            e1.record(stream)
+            barrier()
+            ms = REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps
+            nbytes = prep_bytes(name, pw.Nc, pw.Nv, args.phases)
+            prep[name] = {"ms_per_call": ms, "kernel_ms_per_launch": statistics.mean(k_ms),
+                          "algorithmic_bytes_per_launch": nbytes,
+                          "hbm_achieved_gbs": nbytes / (statistics.mean(k_ms) * 1e-3) / 1e9}
+        prep["grid"] = f"{args.size}x{args.size} cells, {args.phases} phases, piecewise-linear softening with marker noise"
+        del pd, pfs, pw
+
     # ---- end to end through the C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -526,6 +568,9 @@ def main():
     roof["algorithmic_bytes_per_launch"] = bytes_alg
     if strain is not None:
         strain["hbm_frac"] = strain["hbm_achieved_gbs"] / hbm if hbm else None
+    for v in (prep or {}).values():
+        if isinstance(v, dict):
+            v["hbm_frac"] = v["hbm_achieved_gbs"] / hbm if hbm else None
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -554,7 +599,7 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
             "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op,
-            "strain_rates": strain}
+            "strain_rates": strain, "input_preparation": prep}
     print(json.dumps(line))
     if ws > 1:
         REP.finalize()

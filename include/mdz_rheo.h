@@ -22,6 +22,9 @@
  *                              MDLIB/mdoodz-private.h:607, def MDLIB/StokesRoutines.c:75
  *   mdz_rheo_strain_rates   <- StrainRateComponents
  *                              MDLIB/mdoodz-private.h:426, def MDLIB/RheologyDensity.c:2001
+ *   mdz_rheo_softening      <- CohesionFrictionDilationGrid after its P2Mastah step
+ *                              def MDLIB/RheologyDensity.c:1539 (Softening :1432)
+ *   mdz_rheo_shear_modulus  <- ShearModCompExpGrid, def MDLIB/RheologyDensity.c:1634
  *
  * All arithmetic is IEEE binary64.  Unless a call says otherwise it is
  * synchronous (returns after the results are in the caller's buffers), like
@@ -60,6 +63,7 @@ extern "C" {
 #define MDZ_EANISO_NAN      -18  /* aniso VE residual NaN (AnisotropyRoutines.c:543, exit 1) */
 #define MDZ_EANISO_ITER     -19  /* aniso VE iterations failed (AnisotropyRoutines.c:580-583, exit 0) */
 #define MDZ_ESCRATCH        -20  /* request larger than the static scratch of mdz_rheo_points_static */
+#define MDZ_ESHEAR_INF      -21  /* infinite centroid shear modulus (RheologyDensity.c:1688-1690, exit 32) */
 
 /* memory space of the field pointers handed to a sweep */
 #define MDZ_MEM_HOST   0  /* host memory: the library copies in and out (drop-in mode) */
@@ -298,6 +302,53 @@ typedef struct mdz_strain_rate_fields {
 int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *model, double dx, double dz, int out_of_plane,
                           double compressible, mdz_strain_rate_fields *sr, int mem, int flags,
                           mdz_sweep_stats *stats);
+
+/* ---- per-node input preparation of the sweep ---------------------------
+ * The `mat_prop` fields (MDLIB/include/mdoodz.h:152-240) that Softening,
+ * CohesionFrictionDilationGrid and ShearModCompExpGrid read, same names and units. */
+typedef struct mdz_prep_materials {
+  int    Nb_phases;
+  double G[MDZ_MAX_PHASES], bet[MDZ_MAX_PHASES], alp[MDZ_MAX_PHASES];
+  double C[MDZ_MAX_PHASES], phi[MDZ_MAX_PHASES], psi[MDZ_MAX_PHASES], H_c[MDZ_MAX_PHASES];
+  double C_end[MDZ_MAX_PHASES], phi_end[MDZ_MAX_PHASES], psi_end[MDZ_MAX_PHASES];
+  double pls_start[MDZ_MAX_PHASES], pls_end[MDZ_MAX_PHASES];
+  int    phi_soft[MDZ_MAX_PHASES], psi_soft[MDZ_MAX_PHASES], coh_soft[MDZ_MAX_PHASES];
+} mdz_prep_materials;
+
+/* Grid arrays of the preparation steps (layout of mdz_grid_fields). */
+typedef struct mdz_prep_fields {
+  const double *const *phase_perc_n, *const *phase_perc_s;
+  const signed char *BCp_type, *BCg_type;
+  /* accumulated plastic strain on the grid: what P2Mastah interpolates from the markers
+   * in CohesionFrictionDilationGrid (RheologyDensity.c:1558, :1595) */
+  const double *strain_pl_n, *strain_pl_s;
+  const double *noise_n, *noise_s;               /* read when marker_noise == 1 */
+  double *fric_n, *dil_n, *C_n, *fric_s, *dil_s, *C_s;  /* softening outputs */
+  double *mu_n, *bet_n, *alp, *mu_s, *bet_s;             /* shear modulus outputs */
+} mdz_prep_fields;
+
+/* CohesionFrictionDilationGrid (MDLIB/RheologyDensity.c:1539-1628) after its particle
+ * interpolation: Softening (:1432-1532) of friction, dilation and cohesion against the
+ * plastic strain at every centroid and vertex, arithmetic phase average, marker noise
+ * on the cohesion.  The style follows params: 1 when smooth_softening == 1 (erfc form),
+ * 2 when hardening_modulus == 1 (linear hardening of C), else 0 (piecewise linear).
+ * Styles 0 and 2 are the reference's results to the last bit; style 1 agrees to the
+ * accuracy of erfc (CUDA's on the device, the C library's in the reference).
+ * Reads phase_perc_n/_s, BC flags, strain_pl_n/_s (and noise_n/_s); writes fric, dil,
+ * C at centroids and vertices.  `mem`, `flags` (MDZ_SWEEP_ASYNC) and `stats` as for
+ * mdz_rheo_strain_rates. */
+int mdz_rheo_softening(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_prep_materials *mat,
+                       mdz_prep_fields *f, int smooth_softening, int hardening_modulus, int marker_noise,
+                       int mem, int flags, mdz_sweep_stats *stats);
+
+/* ShearModCompExpGrid (MDLIB/RheologyDensity.c:1634-1755): harmonic phase averages of
+ * the shear modulus G and the compressibility bet at centroids and vertices, arithmetic
+ * average of the expansivity alp at centroids, and the periodic averaging of the first
+ * and last vertex columns.  An infinite centroid shear modulus returns
+ * MDZ_ESHEAR_INF (the reference exits with code 32).  Bit for bit the reference's.
+ * Reads phase_perc_n/_s and the BC flags; writes mu_n, bet_n, alp, mu_s, bet_s. */
+int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_prep_materials *mat,
+                           mdz_prep_fields *f, int mem, int flags, mdz_sweep_stats *stats);
 
 /* ---- allocation-free variant (no reference counterpart) ----------------
  * mdz_rheo_points on the CURRENT device without any context and without allocating:

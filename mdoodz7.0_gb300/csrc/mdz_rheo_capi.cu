@@ -15,6 +15,7 @@
 #include "mlp_train.cuh"
 #include "operators.cuh"
 #include "rheo_kernels.cuh"
+#include "prep.cuh"
 #include "strain_rates.cuh"
 
 #include <algorithm>
@@ -237,7 +238,7 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
        S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
-       S_SRU = S_SR + SR_COUNT, S_SRV, S_COUNT };
+       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_COUNT = S_PREP + 16 };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -425,6 +426,54 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
 
 
 // ---------------------------------------------------------------------------------
+// input preparation: Softening over the grid, ShearModCompExpGrid (helpers)
+// ---------------------------------------------------------------------------------
+
+// the per-phase constants of Softening, by the reference's own expressions
+// (RheologyDensity.c:1448-1470, :1493-1497)
+void fold_soft(const mdz_prep_materials *m, int p, SoftPhase &P) {
+  P.phi = m->phi[p]; P.psi = m->psi[p]; P.C = m->C[p];
+  P.phi_end = m->phi_end[p]; P.psi_end = m->psi_end[p]; P.C_end = m->C_end[p];
+  P.pls_start = m->pls_start[p]; P.pls_end = m->pls_end[p]; P.Hc = m->H_c[p];
+  P.phi_soft = m->phi_soft[p]; P.psi_soft = m->psi_soft[p]; P.coh_soft = m->coh_soft[p];
+  const double dstrain = m->pls_end[p] - m->pls_start[p];
+  P.q_phi = (m->phi_end[p] - m->phi[p]) / dstrain;
+  P.q_psi = (m->psi_end[p] - m->psi[p]) / dstrain;
+  P.q_C = (m->C_end[p] - m->C[p]) / dstrain;
+  P.mu_strain = 0.5 * (m->pls_end[p] + m->pls_start[p]);
+  P.dstrain = make_divisor(dstrain);
+  const double e0 = erfc(-(0.0 - P.mu_strain) / dstrain);
+  const double x[3] = {m->phi[p], m->psi[p], m->C[p]}, xe[3] = {m->phi_end[p], m->psi_end[p], m->C_end[p]};
+  for (int k = 0; k < 3; k++) {
+    const double d = x[k] - xe[k];
+    const double half = d / 2.0;
+    const double t = half * e0;
+    const double x0 = (x[k] - t) - xe[k];
+    P.d[k] = d; P.half_d[k] = half; P.x_end_[k] = xe[k];
+    P.x0[k] = make_divisor(x0);
+  }
+}
+
+bool prep_common(const mdz_model *md, const mdz_prep_materials *mat, const mdz_prep_fields *f, int mem, int flags) {
+  if (!md || !mat || !f) return false;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return false;
+  if (flags & ~MDZ_SWEEP_ASYNC) return false;
+  if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return false;
+  if (md->Nx < 2 || md->Nz < 2 || md->Nb_phases < 1 || md->Nb_phases > MDZ_MAX_PHASES) return false;
+  if (!f->phase_perc_n || !f->phase_perc_s || !f->BCp_type || !f->BCg_type) return false;
+  for (int p = 0; p < md->Nb_phases; p++) if (!f->phase_perc_n[p] || !f->phase_perc_s[p]) return false;
+  return true;
+}
+
+int prep_finish(mdz_rheo_ctx *ctx, int flags, mdz_sweep_stats *st) {
+  if (flags & MDZ_SWEEP_ASYNC) {
+    ctx->pending = 1;
+    return MDZ_OK;
+  }
+  return finish(ctx, st);
+}
+
+// ---------------------------------------------------------------------------------
 // static scratch of mdz_rheo_points_static: one array per device, its address looked
 // up once per device; the lock serialises the calls that share it
 // ---------------------------------------------------------------------------------
@@ -606,6 +655,7 @@ const char *mdz_rheo_status_string(int s) {
     case MDZ_EANISO_NAN: return "anisotropic VE residual is NaN";
     case MDZ_EANISO_ITER: return "anisotropic Visco-Elastic iterations failed";
     case MDZ_ESCRATCH: return "request larger than the static scratch (MDZ_STATIC_SCRATCH_BYTES)";
+    case MDZ_ESHEAR_INF: return "infinite shear modulus at a cell centre";
     default: return "unknown status";
   }
 }
@@ -1175,6 +1225,107 @@ int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *md, double dx, dou
     return MDZ_OK;
   }
   return finish(ctx, st);
+}
+
+// input preparation: Softening over the grid, ShearModCompExpGrid
+int mdz_rheo_softening(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_prep_materials *mat, mdz_prep_fields *f,
+                       int smooth_softening, int hardening_modulus, int marker_noise, int mem, int flags,
+                       mdz_sweep_stats *st) {
+  if (!ctx || !prep_common(md, mat, f, mem, flags)) return MDZ_EINVAL;
+  if (!f->strain_pl_n || !f->strain_pl_s || !f->fric_n || !f->dil_n || !f->C_n || !f->fric_s || !f->dil_s ||
+      !f->C_s)
+    return MDZ_EINVAL;
+  if (marker_noise == 1 && (!f->noise_n || !f->noise_s)) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  static thread_local SoftArgs A;
+  memset(&A, 0, sizeof(A));
+  const size_t Nc = (size_t)(md->Nx - 1) * (md->Nz - 1), Nv = (size_t)md->Nx * md->Nz;
+  A.Nc = (long long)Nc; A.Nv = (long long)Nv;
+  A.np = md->Nb_phases;
+  // CohesionFrictionDilationGrid (RheologyDensity.c:1545-1546): the later switch wins
+  A.style = 0;
+  if (smooth_softening == 1) A.style = 1;
+  if (hardening_modulus == 1) A.style = 2;
+  A.noise = marker_noise == 1;
+  for (int p = 0; p < A.np; p++) fold_soft(mat, p, A.ph[p]);
+  const bool host = (mem == MDZ_MEM_HOST);
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  Mirror mi{ctx};
+  for (int p = 0; p < A.np; p++) {
+    A.perc_n[p] = mi.in(f->phase_perc_n[p], S_PN + p, Nc, host);
+    A.perc_s[p] = mi.in(f->phase_perc_s[p], S_PS + p, Nv, host);
+  }
+  A.bcp = mi.in(f->BCp_type, S_BCP, Nc, host);
+  A.bcg = mi.in(f->BCg_type, S_BCG, Nv, host);
+  A.strain_n = mi.in(f->strain_pl_n, S_PREP + 0, Nc, host);
+  A.strain_s = mi.in(f->strain_pl_s, S_PREP + 1, Nv, host);
+  if (A.noise) {
+    A.noise_n = mi.in(f->noise_n, S_PREP + 2, Nc, host);
+    A.noise_s = mi.in(f->noise_s, S_PREP + 3, Nv, host);
+  }
+  double *outs[6] = {f->fric_n, f->dil_n, f->C_n, f->fric_s, f->dil_s, f->C_s};
+  double *dev[6];
+  for (int k = 0; k < 6; k++) dev[k] = mi.out(outs[k], S_PREP + 4 + k, k < 3 ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  A.fric_n = dev[0]; A.dil_n = dev[1]; A.C_n = dev[2]; A.fric_s = dev[3]; A.dil_s = dev[4]; A.C_s = dev[5];
+  int rc;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_softening(A, ctx->stream));
+  ctx->launches = 1;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  for (int k = 0; k < 6; k++) mi.back(outs[k], S_PREP + 4 + k, k < 3 ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  return prep_finish(ctx, flags, st);
+}
+
+int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_prep_materials *mat,
+                           mdz_prep_fields *f, int mem, int flags, mdz_sweep_stats *st) {
+  if (!ctx || !prep_common(md, mat, f, mem, flags)) return MDZ_EINVAL;
+  if (!f->mu_n || !f->bet_n || !f->alp || !f->mu_s || !f->bet_s) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  static thread_local ModArgs A;
+  memset(&A, 0, sizeof(A));
+  const size_t Nc = (size_t)(md->Nx - 1) * (md->Nz - 1), Nv = (size_t)md->Nx * md->Nz;
+  A.Nc = (long long)Nc; A.Nv = (long long)Nv;
+  A.Nx = md->Nx;
+  A.np = md->Nb_phases;
+  A.periodic_x = md->periodic_x;
+  A.skip_zero = 1;
+  for (int p = 0; p < A.np; p++) {
+    A.G[p] = make_divisor(mat->G[p]);
+    A.bet[p] = make_divisor(mat->bet[p]);
+    A.alp[p] = mat->alp[p];
+    if (!(std::isfinite(mat->G[p]) && mat->G[p] != 0.0 && std::isfinite(mat->bet[p]) && mat->bet[p] != 0.0 &&
+          std::isfinite(mat->alp[p])))
+      A.skip_zero = 0;
+  }
+  const bool host = (mem == MDZ_MEM_HOST);
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  Mirror mi{ctx};
+  for (int p = 0; p < A.np; p++) {
+    A.perc_n[p] = mi.in(f->phase_perc_n[p], S_PN + p, Nc, host);
+    A.perc_s[p] = mi.in(f->phase_perc_s[p], S_PS + p, Nv, host);
+  }
+  A.bcp = mi.in(f->BCp_type, S_BCP, Nc, host);
+  A.bcg = mi.in(f->BCg_type, S_BCG, Nv, host);
+  double *outs[5] = {f->mu_n, f->bet_n, f->alp, f->mu_s, f->bet_s};
+  double *dev[5];
+  for (int k = 0; k < 5; k++) dev[k] = mi.out(outs[k], S_PREP + 10 + k, k < 3 ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  A.mu_n = dev[0]; A.bet_n = dev[1]; A.alp_n = dev[2]; A.mu_s = dev[3]; A.bet_s = dev[4];
+  A.stats = ctx->d_stats;
+  int rc;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_moduli(A, ctx->stream));
+  ctx->launches = 1;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  for (int k = 0; k < 5; k++) mi.back(outs[k], S_PREP + 10 + k, k < 3 ? Nc : Nv, host);
+  if (mi.err) return mi.err;
+  return prep_finish(ctx, flags, st);
 }
 
 int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {

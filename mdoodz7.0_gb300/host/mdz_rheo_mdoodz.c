@@ -1,12 +1,13 @@
 /*
  * mdz_rheo_mdoodz.c -- the MDOODZ7.0-side drop-in: NonNewtonianViscosityGrid,
- * NonNewtonianViscosityGridAniso, RheologicalOperators and StrainRateComponents with
- * the reference's own signatures (MDLIB/mdoodz-private.h:423, :437, :607 and :426),
- * evaluated on the GPU by libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
+ * NonNewtonianViscosityGridAniso, RheologicalOperators, StrainRateComponents,
+ * CohesionFrictionDilationGrid and ShearModCompExpGrid with the reference's own
+ * signatures (MDLIB/mdoodz-private.h:423, :437, :607, :426, :417 and :416), evaluated on
+ * the GPU by libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
  *
  * It is compiled inside the MDOODZ build, against MDLIB/mdoodz-private.h, in place of
- * the definitions at MDLIB/RheologyDensity.c:1131, MDLIB/AnisotropyRoutines.c:885,
- * MDLIB/StokesRoutines.c:75 and MDLIB/RheologyDensity.c:2001 (those are compiled out
+ * the definitions at MDLIB/RheologyDensity.c:1131, :1539, :1634, :2001,
+ * MDLIB/AnisotropyRoutines.c:885 and MDLIB/StokesRoutines.c:75 (those are compiled out
  * under MDZ_RHEO_GB300).
  * Each call unpacks `grid`, `mat_prop`, `params` and `scale` into the library's
  * plain-pointer structs and runs one sweep on host memory: the library uploads the
@@ -206,6 +207,81 @@ void StrainRateComponents(grid *mesh, scale scaling, params *model) {
   memset(&st, 0, sizeof(st));
   const int rc = mdz_rheo_strain_rates(mdz_context(), &md, mesh->dx, mesh->dz, model->out_of_plane,
                                        model->compressible, &sr, MDZ_MEM_HOST, 0, &st);
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
+}
+
+/* The mat_prop fields of the preparation steps. */
+static void mdz_prep_materials_from(mdz_prep_materials *m, const mat_prop *mp, int nphases) {
+  memset(m, 0, sizeof(*m));
+  m->Nb_phases = nphases;
+  for (int p = 0; p < MDZ_MAX_PHASES; p++) {
+    m->G[p] = mp->G[p]; m->bet[p] = mp->bet[p]; m->alp[p] = mp->alp[p];
+    m->C[p] = mp->C[p]; m->phi[p] = mp->phi[p]; m->psi[p] = mp->psi[p]; m->H_c[p] = mp->H_c[p];
+    m->C_end[p] = mp->C_end[p]; m->phi_end[p] = mp->phi_end[p]; m->psi_end[p] = mp->psi_end[p];
+    m->pls_start[p] = mp->pls_start[p]; m->pls_end[p] = mp->pls_end[p];
+    m->phi_soft[p] = mp->phi_soft[p]; m->psi_soft[p] = mp->psi_soft[p]; m->coh_soft[p] = mp->coh_soft[p];
+  }
+}
+
+static void mdz_prep_fields_from(mdz_prep_fields *f, grid *g) {
+  memset(f, 0, sizeof(*f));
+  f->phase_perc_n = (const double *const *)g->phase_perc_n;
+  f->phase_perc_s = (const double *const *)g->phase_perc_s;
+  f->BCp_type = g->BCp.type; f->BCg_type = g->BCg.type;
+  f->noise_n = g->noise_n; f->noise_s = g->noise_s;
+  f->fric_n = g->fric_n; f->dil_n = g->dil_n; f->C_n = g->C_n;
+  f->fric_s = g->fric_s; f->dil_s = g->dil_s; f->C_s = g->C_s;
+  f->mu_n = g->mu_n; f->bet_n = g->bet_n; f->alp = g->alp; f->mu_s = g->mu_s; f->bet_s = g->bet_s;
+}
+
+/* CohesionFrictionDilationGrid (RheologyDensity.c:1539): the markers' plastic strain is
+ * interpolated to the centroids and vertices by the reference's own P2Mastah, exactly as
+ * there (:1557-1558, :1594-1595); Softening of every node then runs on the GPU. */
+void CohesionFrictionDilationGrid(grid *mesh, markers *particles, mat_prop materials, params model, scale scaling) {
+  (void)scaling;
+  mdz_model md;
+  mdz_prep_materials pm;
+  mdz_prep_fields f;
+  mdz_sweep_stats st;
+  double *strain_n = DoodzCalloc((model.Nx - 1) * (model.Nz - 1), sizeof(double));
+  P2Mastah(&model, *particles, particles->strain_pl, mesh, strain_n, (char *)mesh->BCp.type, 1, 0, 0, 1,
+           model.interp_stencil, NULL);
+  double *strain_s = DoodzCalloc(model.Nx * model.Nz, sizeof(double));
+  P2Mastah(&model, *particles, particles->strain_pl, mesh, strain_s, (char *)mesh->BCg.type, 1, 0, 0, 0,
+           model.interp_stencil, NULL);
+  memset(&md, 0, sizeof(md));
+  md.Nx = mesh->Nx; md.Nz = mesh->Nz; md.Nb_phases = model.Nb_phases; md.periodic_x = model.periodic_x;
+  mdz_prep_materials_from(&pm, &materials, model.Nb_phases);
+  mdz_prep_fields_from(&f, mesh);
+  f.strain_pl_n = strain_n; f.strain_pl_s = strain_s;
+  memset(&st, 0, sizeof(st));
+  const int rc = mdz_rheo_softening(mdz_context(), &md, &pm, &f, model.smooth_softening, model.hardening_modulus,
+                                    model.marker_noise, MDZ_MEM_HOST, 0, &st);
+  DoodzFree(strain_n);
+  DoodzFree(strain_s);
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
+}
+
+/* ShearModCompExpGrid (RheologyDensity.c:1634): harmonic phase averages of G and bet,
+ * arithmetic alp, on the GPU.  An infinite centroid modulus gets the reference's message
+ * and exit code 32 (:1688-1690). */
+void ShearModCompExpGrid(grid *mesh, mat_prop *materials, params *model, scale scaling) {
+  mdz_model md;
+  mdz_prep_materials pm;
+  mdz_prep_fields f;
+  mdz_sweep_stats st;
+  memset(&md, 0, sizeof(md));
+  md.Nx = mesh->Nx; md.Nz = mesh->Nz; md.Nb_phases = model->Nb_phases; md.periodic_x = model->periodic_x;
+  mdz_prep_materials_from(&pm, materials, model->Nb_phases);
+  mdz_prep_fields_from(&f, mesh);
+  memset(&st, 0, sizeof(st));
+  const int rc = mdz_rheo_shear_modulus(mdz_context(), &md, &pm, &f, MDZ_MEM_HOST, 0, &st);
+  if (rc == MDZ_ESHEAR_INF) {
+    const int Ncx = mesh->Nx - 1, c0 = (int)st.error_node, k = c0 % Ncx, l = c0 / Ncx;
+    fprintf(stderr, "%f x = %2.6e z = %2.6e - BCp %d BCt %d\n", mesh->mu_n[c0], mesh->xc_coord[k] * scaling.L,
+            mesh->zc_coord[l] * scaling.L, mesh->BCp.type[c0], mesh->BCt.type[c0]);
+    exit(32);
+  }
   if (rc != MDZ_OK) mdz_fail(rc, &st);
 }
 

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "build")
 LIB = os.path.join(BUILD, "libmdz_rheo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["rheo_kernels.cu", "mdz_rheo_capi.cu", "fp64_probe.cu", "mlp_train.cu", "operators.cu",
-           "strain_rates.cu"]
+           "strain_rates.cu", "prep.cu"]
 
 
 def nvcc() -> str:
@@ -28,7 +28,9 @@ def nvcc() -> str:
 
 
 def flags(verbose_ptxas: bool = False):
-    f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+    # host code folds constants with the reference's expressions: no FMA contraction there
+    f = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                "--expt-relaxed-constexpr",
                 "-I", CSRC]
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]

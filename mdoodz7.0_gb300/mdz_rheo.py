@@ -42,6 +42,7 @@ MDZ_ELINESEARCH = -17
 MDZ_EANISO_NAN = -18
 MDZ_EANISO_ITER = -19
 MDZ_ESCRATCH = -20
+MDZ_ESHEAR_INF = -21
 STATIC_SCRATCH_BYTES = 4 << 20
 
 MEM_HOST = 0
@@ -264,6 +265,43 @@ class FieldSet:
         return self.arrays[k]
 
 
+PREP_MAT_DBL = ["G", "bet", "alp", "C", "phi", "psi", "H_c", "C_end", "phi_end", "psi_end", "pls_start", "pls_end"]
+PREP_MAT_INT = ["phi_soft", "psi_soft", "coh_soft"]
+SOFT_N, SOFT_S = ["fric_n", "dil_n", "C_n"], ["fric_s", "dil_s", "C_s"]
+MOD_N, MOD_S = ["mu_n", "bet_n", "alp"], ["mu_s", "bet_s"]
+
+
+class PrepMaterials(C.Structure):
+    """mdz_prep_materials: the mat_prop fields of Softening and ShearModCompExpGrid."""
+    _fields_ = ([("Nb_phases", C.c_int)] + [(n, C.c_double * MAX_PHASES) for n in PREP_MAT_DBL]
+                + [(n, C.c_int * MAX_PHASES) for n in PREP_MAT_INT])
+
+
+class PrepFields(C.Structure):
+    """mdz_prep_fields: grid arrays of the preparation steps."""
+    _fields_ = ([("phase_perc_n", _PP), ("phase_perc_s", _PP), ("BCp_type", _P), ("BCg_type", _P),
+                 ("strain_pl_n", _P), ("strain_pl_s", _P), ("noise_n", _P), ("noise_s", _P)]
+                + [(n, _P) for n in SOFT_N + SOFT_S + MOD_N + MOD_S])
+
+
+class PrepFieldSet:
+    """A dict of preparation arrays (phase_perc_n/_s are lists) and the struct over it."""
+
+    def __init__(self, arrays: Dict[str, object]):
+        self.arrays = arrays
+        s = PrepFields()
+        self._keep = []
+        for name, _ in PrepFields._fields_:
+            v = arrays.get(name)
+            if name.startswith("phase_"):
+                pa = _ptr_array(v)
+                self._keep.append(pa)
+                setattr(s, name, C.cast(pa, _PP) if pa is not None else None)
+            else:
+                setattr(s, name, _ptr(v))
+        self.struct = s
+
+
 def make_points(inputs: Dict[str, object], outputs: Dict[str, object], post_process=1, centroid=1,
                 final_update=0):
     pi = PointInputs()
@@ -330,6 +368,10 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_strain_rates.argtypes = [C.c_void_p, C.POINTER(Model), C.c_double, C.c_double, C.c_int,
                                           C.c_double, C.POINTER(StrainRateFields), C.c_int, C.c_int,
                                           C.POINTER(SweepStats)]
+    lib.mdz_rheo_softening.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(PrepMaterials), C.POINTER(PrepFields),
+                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(SweepStats)]
+    lib.mdz_rheo_shear_modulus.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(PrepMaterials),
+                                           C.POINTER(PrepFields), C.c_int, C.c_int, C.POINTER(SweepStats)]
     lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -550,6 +592,25 @@ class Context:
                                             C.byref(o), mem, flags, C.byref(st))
         if check and rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_strain_rates")
+        return rc, st
+
+    def softening(self, model, pmat, fields: "PrepFieldSet", smooth_softening=0, hardening_modulus=0,
+                  marker_noise=0, mem=MEM_HOST, flags=0, check=True):
+        """CohesionFrictionDilationGrid after its marker interpolation (mdz_rheo_softening)."""
+        st = SweepStats()
+        rc = self.lib.mdz_rheo_softening(self.handle, C.byref(model), C.byref(pmat), C.byref(fields.struct),
+                                         smooth_softening, hardening_modulus, marker_noise, mem, flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_softening")
+        return rc, st
+
+    def shear_modulus(self, model, pmat, fields: "PrepFieldSet", mem=MEM_HOST, flags=0, check=True):
+        """ShearModCompExpGrid (mdz_rheo_shear_modulus)."""
+        st = SweepStats()
+        rc = self.lib.mdz_rheo_shear_modulus(self.handle, C.byref(model), C.byref(pmat), C.byref(fields.struct), mem,
+                                             flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_shear_modulus")
         return rc, st
 
     # ---- launch-shape autotuner

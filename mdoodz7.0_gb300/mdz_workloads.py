@@ -471,3 +471,91 @@ def velocity_field(seed: int = 9, ncx: int = 2049, ncz: Optional[int] = None, ai
     model = make_model(ncx, ncz, 1, sc=sc)
     model.periodic_x = periodic
     return Workload("velocity_field", model, None, a, info=dict(seed=seed, ncx=ncx, ncz=ncz, dx=dx, dz=dz))
+
+
+def prep_materials(rng, nphases: int, sc: Scale = SI) -> R.PrepMaterials:
+    """Per-phase constants of the sweep's input preparation (Softening and
+    ShearModCompExpGrid): shear modulus 1e10-8e10 Pa, compressibility 1e-12-1e-10 1/Pa,
+    expansivity 1e-5-4e-5 1/K, cohesion 1e6-5e7 Pa softening to 5-50 % of it, friction
+    20-35 deg softening to 2-10 deg, dilation 0-10 deg softening to 0, softening between
+    plastic strains U(0, 0.2) and that + U(0.3, 1), linear cohesion hardening -1e6..-1e7 Pa
+    (negative: weakening), each softening switch on with probability 0.7."""
+    m = R.PrepMaterials()
+    m.Nb_phases = nphases
+    for p in range(nphases):
+        m.G[p] = float(loguniform(rng, 1e10, 8e10, 1)[0]) / sc.S
+        m.bet[p] = float(loguniform(rng, 1e-12, 1e-10, 1)[0]) * sc.S
+        m.alp[p] = float(rng.uniform(1e-5, 4e-5)) * sc.T
+        m.C[p] = float(loguniform(rng, 1e6, 5e7, 1)[0]) / sc.S
+        m.C_end[p] = m.C[p] * float(rng.uniform(0.05, 0.5))
+        m.phi[p] = float(rng.uniform(20.0, 35.0)) * DEG
+        m.phi_end[p] = float(rng.uniform(2.0, 10.0)) * DEG
+        m.psi[p] = float(rng.uniform(0.0, 10.0)) * DEG
+        m.psi_end[p] = 0.0
+        m.pls_start[p] = float(rng.uniform(0.0, 0.2))
+        m.pls_end[p] = m.pls_start[p] + float(rng.uniform(0.3, 1.0))
+        m.H_c[p] = -float(loguniform(rng, 1e6, 1e7, 1)[0]) / sc.S
+        m.phi_soft[p], m.psi_soft[p], m.coh_soft[p] = [int(x) for x in rng.random(3) < 0.7]
+    return m
+
+
+def prep_workload(seed: int = 13, ncx: int = 2049, ncz: Optional[int] = None, nphases: int = 5, air: float = 0.0,
+                  periodic: int = 0, markers_per_cell: int = 0, sc: Scale = SI, L: float = 1e5) -> Workload:
+    """Input of the sweep's preparation steps on ncx x ncz cells: phase fractions from
+    smooth random fields (softmax, fractions below 3 % set to exactly zero and the rest
+    renormalised, as marker interpolation leaves many exact zeros), plastic strain from a
+    smooth field in [0, 1.5) with 1 % of the nodes exactly at phase 0's pls_start and 1 %
+    at its pls_end, marker noise U(-0.1, 0.1), air above a wavy surface as in
+    velocity_field.  With markers_per_cell > 0, `info["markers"]` also holds that many
+    markers per cell at uniform random positions (phase and plastic strain attached) on an
+    L x L domain, for the reference's own marker-to-grid interpolation."""
+    ncz = ncx if ncz is None else ncz
+    rng = np.random.default_rng(seed)
+    nx, nz = ncx + 1, ncz + 1
+    nc, nv = ncx * ncz, nx * nz
+    pm = prep_materials(rng, nphases, sc)
+    xc, zc = (np.arange(ncx) + 0.5) / ncx, (np.arange(ncz) + 0.5) / ncz
+    xv, zv = np.arange(nx) / ncx, np.arange(nz) / ncz
+    a: Dict[str, object] = {}
+    for suffix, xs, zs in (("n", xc, zc), ("s", xv, zv)):
+        frac = phase_fractions(smooth_fields(rng, nphases, xs, zs)).reshape(nphases, -1)
+        frac[frac < 0.03] = 0.0
+        frac /= frac.sum(axis=0, keepdims=True)
+        a["phase_perc_" + suffix] = [np.ascontiguousarray(frac[p]) for p in range(nphases)]
+        st = 0.75 * (1.0 + np.tanh(smooth_fields(rng, 1, xs, zs)[0])).ravel()
+        k = rng.permutation(st.size)
+        st[k[: st.size // 100]] = pm.pls_start[0]
+        st[k[st.size // 100: st.size // 50]] = pm.pls_end[0]
+        a["strain_pl_" + suffix] = st
+        a["noise_" + suffix] = rng.uniform(-0.1, 0.1, st.size)
+    bcp = np.full((ncz, ncx), -1, dtype=np.int8)
+    bcg = np.full((nz, nx), -1, dtype=np.int8)
+    if air > 0.0:
+        ph = rng.uniform(0, 2 * np.pi)
+        h = 1.0 - air + 0.05 * np.sin(4.0 * np.pi * xc + ph)
+        above = zc[:, None] > h[None, :]
+        bcp[above] = 30
+        bcp[(~above) & (zc[:, None] > h[None, :] - 1.0 / ncz)] = 31
+        hv = 1.0 - air + 0.05 * np.sin(4.0 * np.pi * xv + ph)
+        bcg[zv[:, None] > hv[None, :]] = 30
+    a["BCp_type"], a["BCg_type"] = bcp.ravel(), bcg.ravel()
+    for k in R.SOFT_N + R.MOD_N:
+        a[k] = np.full(nc, -7.0)
+    for k in R.SOFT_S + R.MOD_S:
+        a[k] = np.full(nv, -7.0)
+    model = make_model(ncx, ncz, nphases, sc=sc)
+    model.periodic_x = periodic
+    info = dict(seed=seed, ncx=ncx, ncz=ncz)
+    if markers_per_cell > 0:
+        n = nc * markers_per_cell
+        dx, dz = L / ncx / sc.L, L / ncz / sc.L
+        x = rng.uniform(0.0, ncx * dx, n)
+        z = rng.uniform(0.0, ncz * dz, n)
+        phase = rng.integers(0, nphases, n).astype(np.int32)
+        g = smooth_fields(rng, 1, np.linspace(0, 1, 64), np.linspace(0, 1, 64))[0]
+        ix = np.minimum((x / (ncx * dx) * 64).astype(int), 63)
+        iz = np.minimum((z / (ncz * dz) * 64).astype(int), 63)
+        strain = 0.75 * (1.0 + np.tanh(g[iz, ix])) * rng.uniform(0.8, 1.2, n)
+        info["markers"] = dict(x=x, z=z, phase=phase, strain_pl=strain, xmin=0.0, zmin=0.0, dx=dx, dz=dz,
+                               interp_stencil=1)
+    return Workload("prep", model, pm, a, info=info)

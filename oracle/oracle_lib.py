@@ -197,6 +197,65 @@ def shim_strain_rates(model, dx, dz, sr: dict, out_of_plane=0, compressible=0.0,
                                         C.byref(R.make_strain_rate_fields(sr)))
 
 
+def orc_softening(model, pmat, fs: "R.PrepFieldSet", smooth_softening=0, hardening_modulus=0, marker_noise=0):
+    fn = oracle().orc_softening
+    fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.PrepMaterials), C.POINTER(R.PrepFields), C.c_int, C.c_int, C.c_int]
+    return fn(C.byref(model), C.byref(pmat), C.byref(fs.struct), smooth_softening, hardening_modulus, marker_noise)
+
+
+def orc_shear_modulus(model, pmat, fs: "R.PrepFieldSet"):
+    fn = oracle().orc_shear_modulus
+    fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.PrepMaterials), C.POINTER(R.PrepFields)]
+    return fn(C.byref(model), C.byref(pmat), C.byref(fs.struct))
+
+
+def _markers_call(fn, model, pmat, fs, mk, smooth_softening, hardening_modulus, marker_noise):
+    import numpy as np
+    fn.argtypes = ([C.POINTER(R.Model), C.POINTER(R.PrepMaterials), C.POINTER(R.PrepFields), C.c_int64]
+                   + [C.c_void_p] * 4 + [C.c_double] * 4 + [C.c_int] * 4 + [C.c_void_p] * 2)
+    nc, nv = (model.Nx - 1) * (model.Nz - 1), model.Nx * model.Nz
+    sn, ss = np.zeros(nc), np.zeros(nv)
+    rc = fn(C.byref(model), C.byref(pmat), C.byref(fs.struct), mk["x"].size, mk["x"].ctypes.data,
+            mk["z"].ctypes.data, mk["phase"].ctypes.data, mk["strain_pl"].ctypes.data, mk["xmin"], mk["zmin"],
+            mk["dx"], mk["dz"], mk["interp_stencil"], smooth_softening, hardening_modulus, marker_noise,
+            sn.ctypes.data, ss.ctypes.data)
+    return rc, sn, ss
+
+
+def ref_softening_markers(model, pmat, fs: "R.PrepFieldSet", mk: dict, smooth_softening=0, hardening_modulus=0,
+                          marker_noise=0):
+    """The reference's CohesionFrictionDilationGrid with markers `mk` (x, z, phase, strain_pl,
+    xmin, zmin, dx, dz, interp_stencil); returns (rc, strain_pl_n, strain_pl_s) -- the plastic
+    strain its P2Mastah put on the grid."""
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    return _markers_call(lib.ref_softening_markers, model, pmat, fs, mk, smooth_softening, hardening_modulus,
+                         marker_noise)
+
+
+def shim_softening_markers(model, pmat, fs: "R.PrepFieldSet", mk: dict, smooth_softening=0, hardening_modulus=0,
+                           marker_noise=0, drop_in=True):
+    name = "shimtest_shim_softening_markers" if drop_in else "shimtest_ref_softening_markers"
+    return _markers_call(getattr(shimtest(), name), model, pmat, fs, mk, smooth_softening, hardening_modulus,
+                         marker_noise)
+
+
+def ref_shear_modulus(model, pmat, fs: "R.PrepFieldSet"):
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    fn = lib.ref_shear_modulus
+    fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.PrepMaterials), C.POINTER(R.PrepFields)]
+    return fn(C.byref(model), C.byref(pmat), C.byref(fs.struct))
+
+
+def shim_shear_modulus(model, pmat, fs: "R.PrepFieldSet", drop_in=True):
+    fn = getattr(shimtest(), "shimtest_shim_shear_modulus" if drop_in else "shimtest_ref_shear_modulus")
+    fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.PrepMaterials), C.POINTER(R.PrepFields)]
+    return fn(C.byref(model), C.byref(pmat), C.byref(fs.struct))
+
+
 def orc_points(model, mat, pin, pout, n, aniso=0):
     return oracle().orc_points(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso)
 

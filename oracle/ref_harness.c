@@ -1,7 +1,9 @@
 /*
  * ref_harness.c -- drives the reference's own NonNewtonianViscosityGrid(Aniso),
- * ViscosityConcise(Aniso), RheologicalOperators and StrainRateComponents, compiled
- * from the MDOODZ7.0 sources, from the plain-pointer structs of include/mdz_rheo.h.
+ * ViscosityConcise(Aniso), RheologicalOperators, StrainRateComponents,
+ * CohesionFrictionDilationGrid (with its marker interpolation) and ShearModCompExpGrid,
+ * compiled from the MDOODZ7.0 sources, from the plain-pointer structs of
+ * include/mdz_rheo.h.
  *
  * TEST INFRASTRUCTURE ONLY: it is built by oracle/Makefile (target `ref`)
  * into oracle/_ref/ when the reference tree is present, and is used to pin the
@@ -177,6 +179,97 @@ int ref_strain_rates(const mdz_model *m, double dx, double dz, int out_of_plane,
   g->exz = sr->exz; g->wxz = sr->wxz; g->exxd_s = sr->exxd_s; g->ezzd_s = sr->ezzd_s; g->div_u_s = sr->div_u_s;
   StrainRateComponents(g, sc, &pm);
   free_grid(g);
+  return 0;
+}
+
+/* The mat_prop fields of Softening and ShearModCompExpGrid. */
+static mat_prop *prep_materials(const mdz_prep_materials *m) {
+  mat_prop *mp = calloc(1, sizeof(mat_prop));
+  mp->Nb_phases = m->Nb_phases;
+  for (int p = 0; p < MDZ_MAX_PHASES; p++) {
+#define CP(name) mp->name[p] = m->name[p]
+    CP(G); CP(bet); CP(alp); CP(C); CP(phi); CP(psi); CP(H_c); CP(C_end); CP(phi_end); CP(psi_end);
+    CP(pls_start); CP(pls_end); CP(phi_soft); CP(psi_soft); CP(coh_soft);
+#undef CP
+  }
+  return mp;
+}
+
+/* A grid with mesh spacing, node coordinates from (xmin, zmin) and the preparation
+ * fields of `f`. */
+static grid *prep_grid(const mdz_model *m, mdz_prep_fields *f, double xmin, double zmin, double dx, double dz) {
+  mdz_grid_fields none;
+  memset(&none, 0, sizeof(none));
+  grid *g = make_grid(m, &none);
+  const int Nx = m->Nx, Nz = m->Nz;
+  g->dx = dx; g->dz = dz;
+  g->xg_coord = malloc(sizeof(double) * Nx); g->zg_coord = malloc(sizeof(double) * Nz);
+  g->xc_coord = malloc(sizeof(double) * (Nx - 1)); g->zc_coord = malloc(sizeof(double) * (Nz - 1));
+  for (int k = 0; k < Nx; k++) g->xg_coord[k] = xmin + k * dx;
+  for (int l = 0; l < Nz; l++) g->zg_coord[l] = zmin + l * dz;
+  for (int k = 0; k < Nx - 1; k++) g->xc_coord[k] = xmin + 0.5 * dx + k * dx;
+  for (int l = 0; l < Nz - 1; l++) g->zc_coord[l] = zmin + 0.5 * dz + l * dz;
+  g->BCp.type = (signed char *)f->BCp_type; g->BCg.type = (signed char *)f->BCg_type;
+  g->BCt.type = (signed char *)f->BCp_type;
+  g->phase_perc_n = (double **)f->phase_perc_n; g->phase_perc_s = (double **)f->phase_perc_s;
+  g->noise_n = W(f->noise_n); g->noise_s = W(f->noise_s);
+  g->fric_n = f->fric_n; g->dil_n = f->dil_n; g->C_n = f->C_n;
+  g->fric_s = f->fric_s; g->dil_s = f->dil_s; g->C_s = f->C_s;
+  g->mu_n = f->mu_n; g->bet_n = f->bet_n; g->alp = f->alp; g->mu_s = f->mu_s; g->bet_s = f->bet_s;
+  return g;
+}
+
+static void free_prep_grid(grid *g) {
+  free(g->xg_coord); free(g->zg_coord); free(g->xc_coord); free(g->zc_coord);
+  free_grid(g);
+}
+
+/* CohesionFrictionDilationGrid (RheologyDensity.c:1539) itself, markers included: its
+ * P2Mastah interpolates the markers' plastic strain to centroids and vertices, then
+ * Softening runs per node.  The same two P2Mastah calls (:1558, :1595) are repeated
+ * here into strain_n / strain_s, the plastic strain the GPU path and the restatement
+ * take as input. */
+int ref_softening_markers(const mdz_model *m, const mdz_prep_materials *pmat, mdz_prep_fields *f, int64_t n_part,
+                          const double *px, const double *pz, const int *pphase, const double *pstrain, double xmin,
+                          double zmin, double dx, double dz, int interp_stencil, int smooth_softening,
+                          int hardening_modulus, int marker_noise, double *strain_n, double *strain_s) {
+  quiet_log();
+  mat_prop *mp = prep_materials(pmat);
+  params pm;
+  scale sc;
+  fill_params(&pm, &sc, m);
+  pm.interp_stencil = interp_stencil;
+  pm.smooth_softening = smooth_softening;
+  pm.hardening_modulus = hardening_modulus;
+  pm.marker_noise = marker_noise;
+  grid *g = prep_grid(m, f, xmin, zmin, dx, dz);
+  markers P;
+  memset(&P, 0, sizeof(P));
+  P.Nb_part = (int)n_part;
+  P.x = (double *)px; P.z = (double *)pz; P.phase = (int *)pphase; P.strain_pl = (double *)pstrain;
+  CohesionFrictionDilationGrid(g, &P, *mp, pm, sc);
+  const int Nc = (m->Nx - 1) * (m->Nz - 1), Nv = m->Nx * m->Nz;
+  memset(strain_n, 0, sizeof(double) * Nc);
+  memset(strain_s, 0, sizeof(double) * Nv);
+  P2Mastah(&pm, P, P.strain_pl, g, strain_n, (char *)g->BCp.type, 1, 0, 0, 1, pm.interp_stencil, NULL);
+  P2Mastah(&pm, P, P.strain_pl, g, strain_s, (char *)g->BCg.type, 1, 0, 0, 0, pm.interp_stencil, NULL);
+  free_prep_grid(g);
+  free(mp);
+  return 0;
+}
+
+/* ShearModCompExpGrid (RheologyDensity.c:1634).  The reference exits on an infinite
+ * centroid modulus, so callers only hand it inputs without one. */
+int ref_shear_modulus(const mdz_model *m, const mdz_prep_materials *pmat, mdz_prep_fields *f) {
+  quiet_log();
+  mat_prop *mp = prep_materials(pmat);
+  params pm;
+  scale sc;
+  fill_params(&pm, &sc, m);
+  grid *g = prep_grid(m, f, 0.0, 0.0, 1.0, 1.0);
+  ShearModCompExpGrid(g, mp, &pm, sc);
+  free_prep_grid(g);
+  free(mp);
   return 0;
 }
 

@@ -7,7 +7,7 @@
 void AddFieldToGroup(void) {}
 void AddGroupToHDF5(void) {}
 void CreateOutputHDF5(void) {}
-void P2Mastah(void) {}
+void isoutPart(void) {}
 void PartialMelting(void) {}
 void ScaleBackD(void) {}
 void BuildStokesOperatorDecoupled(void) {}

@@ -1299,3 +1299,134 @@ int orc_strain_rates(const mdz_model *m, double dx, double dz, int out_of_plane,
   orc_interp_c2v(m, sr->div_u, BCp, BCg, sr->div_u_s);
   return MDZ_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Softening (RheologyDensity.c:1432-1532) as CohesionFrictionDilationGrid    */
+/* (:1539-1628) applies it, after P2Mastah: arithmetic phase average          */
+/* (average = 0, :1541), marker noise on the cohesion, zeros at air nodes.    */
+/* ------------------------------------------------------------------------ */
+static void orc_soften(const mdz_prep_materials *m, int p, int style, double s, double *fric, double *dil,
+                       double *C) {
+  *fric = m->phi[p];
+  *dil = m->psi[p];
+  *C = m->C[p];
+  const double dstrain = m->pls_end[p] - m->pls_start[p];
+  if (style == 1) {
+    const double mu_strain = 0.5 * (m->pls_end[p] + m->pls_start[p]);
+    if (m->phi_soft[p] == 1) {
+      const double dfric = m->phi[p] - m->phi_end[p];
+      double f = m->phi[p] - dfric / 2.0 * erfc(-(s - mu_strain) / dstrain) - m->phi_end[p];
+      const double f0 = m->phi[p] - dfric / 2.0 * erfc(-(0.0 - mu_strain) / dstrain) - m->phi_end[p];
+      *fric = f * dfric / f0 + m->phi_end[p];
+    }
+    if (m->psi_soft[p] == 1) {
+      const double ddil = m->psi[p] - m->psi_end[p];
+      double d = m->psi[p] - ddil / 2.0 * erfc(-(s - mu_strain) / dstrain) - m->psi_end[p];
+      const double d0 = m->psi[p] - ddil / 2.0 * erfc(-(0.0 - mu_strain) / dstrain) - m->psi_end[p];
+      *dil = d * ddil / d0 + m->psi_end[p];
+    }
+    if (m->coh_soft[p] == 1) {
+      const double dcoh = m->C[p] - m->C_end[p];
+      double c = m->C[p] - dcoh / 2.0 * erfc(-(s - mu_strain) / dstrain) - m->C_end[p];
+      const double c0 = m->C[p] - dcoh / 2.0 * erfc(-(0.0 - mu_strain) / dstrain) - m->C_end[p];
+      *C = c * dcoh / c0 + m->C_end[p];
+    }
+  } else if (style == 2) {
+    *C = fmax(m->C[p] + m->H_c[p] * s, m->C_end[p]);
+  } else {
+    if (s < m->pls_start[p]) {
+      if (m->phi_soft[p] == 1) *fric = m->phi[p];
+      if (m->psi_soft[p] == 1) *dil = m->psi[p];
+      if (m->coh_soft[p] == 1) *C = m->C[p];
+    }
+    if (s >= m->pls_end[p]) {
+      if (m->phi_soft[p] == 1) *fric = m->phi_end[p];
+      if (m->psi_soft[p] == 1) *dil = m->psi_end[p];
+      if (m->coh_soft[p] == 1) *C = m->C_end[p];
+    }
+    if (s >= m->pls_start[p] && s < m->pls_end[p]) {
+      if (m->phi_soft[p] == 1) *fric = m->phi[p] + (m->phi_end[p] - m->phi[p]) / dstrain * s;
+      if (m->psi_soft[p] == 1) *dil = m->psi[p] + (m->psi_end[p] - m->psi[p]) / dstrain * s;
+      if (m->coh_soft[p] == 1) *C = m->C[p] + (m->C_end[p] - m->C[p]) / dstrain * s;
+    }
+  }
+}
+
+static void orc_soften_node(const mdz_prep_materials *m, int np, int style, int noise, const double *const *perc,
+                            int64_t i, int solid, double s, const double *nz, double *fric, double *dil, double *C) {
+  fric[i] = 0.0;
+  dil[i] = 0.0;
+  C[i] = 0.0;
+  if (!solid) return;
+  for (int p = 0; p < np; p++) {
+    double f, d, c;
+    orc_soften(m, p, style, s, &f, &d, &c);
+    fric[i] += perc[p][i] * f;
+    dil[i] += perc[p][i] * d;
+    C[i] += perc[p][i] * c;
+  }
+  if (noise == 1) C[i] += nz[i] * C[i];
+}
+
+int orc_softening(const mdz_model *md, const mdz_prep_materials *m, mdz_prep_fields *f, int smooth_softening,
+                  int hardening_modulus, int marker_noise) {
+  if (md->Nx < 2 || md->Nz < 2 || md->Nb_phases < 1 || md->Nb_phases > MDZ_MAX_PHASES) return MDZ_EINVAL;
+  const int64_t Nc = (int64_t)(md->Nx - 1) * (md->Nz - 1), Nv = (int64_t)md->Nx * md->Nz;
+  int style = 0;
+  if (smooth_softening == 1) style = 1;
+  if (hardening_modulus == 1) style = 2;
+#pragma omp parallel for
+  for (int64_t c0 = 0; c0 < Nc; c0++)
+    orc_soften_node(m, md->Nb_phases, style, marker_noise, f->phase_perc_n, c0,
+                    f->BCp_type[c0] != 30 && f->BCp_type[c0] != 31, f->strain_pl_n[c0], f->noise_n, f->fric_n,
+                    f->dil_n, f->C_n);
+#pragma omp parallel for
+  for (int64_t c1 = 0; c1 < Nv; c1++)
+    orc_soften_node(m, md->Nb_phases, style, marker_noise, f->phase_perc_s, c1, f->BCg_type[c1] != 30,
+                    f->strain_pl_s[c1], f->noise_s, f->fric_s, f->dil_s, f->C_s);
+  return MDZ_OK;
+}
+
+/* ShearModCompExpGrid, RheologyDensity.c:1634-1755 (average = 1, :1637). */
+int orc_shear_modulus(const mdz_model *md, const mdz_prep_materials *m, mdz_prep_fields *f) {
+  if (md->Nx < 2 || md->Nz < 2 || md->Nb_phases < 1 || md->Nb_phases > MDZ_MAX_PHASES) return MDZ_EINVAL;
+  const int Nx = md->Nx, Nz = md->Nz, Ncx = Nx - 1, Ncz = Nz - 1, np = md->Nb_phases;
+  int64_t bad = -1;
+  for (int64_t c0 = 0; c0 < (int64_t)Ncx * Ncz; c0++) {
+    f->mu_n[c0] = 0.0;
+    f->bet_n[c0] = 0.0;
+    f->alp[c0] = 0.0;
+    if (f->BCp_type[c0] != 30 && f->BCp_type[c0] != 31) {
+      for (int p = 0; p < np; p++) {
+        f->mu_n[c0] += f->phase_perc_n[p][c0] * 1.0 / m->G[p];
+        f->bet_n[c0] += f->phase_perc_n[p][c0] * 1.0 / m->bet[p];
+        f->alp[c0] += f->phase_perc_n[p][c0] * m->alp[p];
+      }
+      f->mu_n[c0] = 1.0 / f->mu_n[c0];
+      f->bet_n[c0] = 1.0 / f->bet_n[c0];
+    }
+    if (isinf(f->mu_n[c0]) && bad < 0) bad = c0;
+  }
+  for (int64_t c1 = 0; c1 < (int64_t)Nx * Nz; c1++) {
+    f->mu_s[c1] = 0.0;
+    f->bet_s[c1] = 0.0;
+    if (f->BCg_type[c1] != 30) {
+      for (int p = 0; p < np; p++) {
+        f->mu_s[c1] += f->phase_perc_s[p][c1] * 1.0 / m->G[p];
+        f->bet_s[c1] += f->phase_perc_s[p][c1] * 1.0 / m->bet[p];
+      }
+      f->mu_s[c1] = 1.0 / f->mu_s[c1];
+      f->bet_s[c1] = 1.0 / f->bet_s[c1];
+    }
+  }
+  if (md->periodic_x == 1) {
+    for (int l = 0; l < Nz; l++) {
+      const int64_t c1 = (int64_t)l * Nx + Nx - 1, c = (int64_t)l * Nx;
+      double av = 0.5 * (f->mu_s[c1] + f->mu_s[c]);
+      f->mu_s[c1] = av; f->mu_s[c] = av;
+      av = 0.5 * (f->bet_s[c1] + f->bet_s[c]);
+      f->bet_s[c1] = av; f->bet_s[c] = av;
+    }
+  }
+  return bad >= 0 ? MDZ_ESHEAR_INF : MDZ_OK;
+}

@@ -8,7 +8,8 @@
  * It restates, in plain C and in the reference's floating-point evaluation
  * order, MDLIB/RheologyDensity.c:116-1426 and MDLIB/AnisotropyRoutines.c:
  * 257-727, 885-1217, MDLIB/StokesRoutines.c:75-410 with MDLIB/FD_Jacobian.c:48-323,
- * StrainRateComponents (MDLIB/RheologyDensity.c:2001-2097), plus
+ * StrainRateComponents (MDLIB/RheologyDensity.c:2001-2097), Softening /
+ * CohesionFrictionDilationGrid and ShearModCompExpGrid (:1432-1755), plus
  * InterpCentroidsToVerticesDouble (MDLIB/GridRoutines.c:108-210).  Built with
  * -ffp-contract=off it is bit-identical to the reference compiled from its own sources on x86-64
  * (pinned by tests/test_oracle_vs_reference.py and the committed golden
@@ -48,6 +49,15 @@ int orc_operators(const mdz_model *model, const mdz_materials *mat, const mdz_gr
 /* StrainRateComponents (RheologyDensity.c:2001-2097). */
 int orc_strain_rates(const mdz_model *model, double dx, double dz, int out_of_plane, double compressible,
                      mdz_strain_rate_fields *sr);
+
+/* CohesionFrictionDilationGrid (RheologyDensity.c:1539-1628) after its P2Mastah step:
+ * Softening (:1432-1532) of every node from f->strain_pl_n/_s. */
+int orc_softening(const mdz_model *model, const mdz_prep_materials *mat, mdz_prep_fields *f, int smooth_softening,
+                  int hardening_modulus, int marker_noise);
+
+/* ShearModCompExpGrid (RheologyDensity.c:1634-1755); MDZ_ESHEAR_INF where the
+ * reference exits with code 32. */
+int orc_shear_modulus(const mdz_model *model, const mdz_prep_materials *mat, mdz_prep_fields *f);
 
 /* InterpCentroidsToVerticesDouble (GridRoutines.c:108) alone. */
 void orc_interp_c2v(const mdz_model *model, const double *centroid, const signed char *BCp_type,

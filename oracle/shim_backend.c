@@ -1,7 +1,7 @@
 /*
  * shim_backend.c -- TEST INFRASTRUCTURE ONLY.
  *
- * A CPU stand-in for the context, sweep, operator and strain-rate entry points of
+ * A CPU stand-in for the context, sweep, operator, strain-rate and preparation entry points of
  * libmdz_rheo_gb300.so (include/mdz_rheo.h) that forwards every call to the C
  * restatement (rheo_oracle.c).  Linked with the MDOODZ-side drop-in
  * (mdoodz7.0_gb300/host/mdz_rheo_mdoodz.c) and with the reference's own sources
@@ -60,4 +60,18 @@ int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *model, double dx, 
   (void)stats;
   if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
   return orc_strain_rates(model, dx, dz, out_of_plane, compressible, sr);
+}
+
+int mdz_rheo_softening(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_prep_materials *mat, mdz_prep_fields *f,
+                       int smooth_softening, int hardening_modulus, int marker_noise, int mem, int flags,
+                       mdz_sweep_stats *stats) {
+  (void)stats;
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_softening(model, mat, f, smooth_softening, hardening_modulus, marker_noise);
+}
+
+int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_prep_materials *mat,
+                           mdz_prep_fields *f, int mem, int flags, mdz_sweep_stats *stats) {
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_shear_modulus(model, mat, f);
 }

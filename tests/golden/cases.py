@@ -3,7 +3,8 @@
 GRID_CASES are small grids of the benchmark workloads (all field layouts,
 averaging modes, scalings, air cells, periodicity); OPERATOR_CASES run
 RheologicalOperators on what a grid case's sweep produced; STRAIN_CASES run
-StrainRateComponents on velocity fields (air, periodicity, one cell, ragged).  POINT_CASES drive
+StrainRateComponents on velocity fields (air, periodicity, one cell, ragged);
+SOFTENING_CASES and SHEAR_CASES the sweep's input preparation.  POINT_CASES drive
 ViscosityConcise / ViscosityConciseAniso directly on random points and cover
 the branches the grid workloads do not reach: Popov et al. 2025 plasticity
 (plast=2, with and without the tensile line search), paleowattmeter grain size
@@ -69,6 +70,26 @@ STRAIN_CASES = {
     "periodic_air": (lambda: W.velocity_field(seed=13, ncx=11, ncz=14, air=0.25, periodic=1), 0, 1.0),
     "one_cell": (lambda: W.velocity_field(seed=14, ncx=1, ncz=1), 1, 1.0),
     "ragged_periodic": (lambda: W.velocity_field(seed=15, ncx=45, ncz=3, air=0.4, periodic=1), 1, 0.0),
+}
+
+# CohesionFrictionDilationGrid with markers (the reference's own marker-to-grid
+# interpolation runs when the fixture is made; the fixture keeps the plastic strain it
+# put on the grid as the GPU path's input):
+# name: (builder, smooth_softening, hardening_modulus, marker_noise, interp_stencil)
+SOFTENING_CASES = {
+    "piecewise": (lambda: W.prep_workload(seed=21, ncx=14, ncz=11, nphases=4, markers_per_cell=6), 0, 0, 0, 1),
+    "piecewise_air_periodic_noise": (lambda: W.prep_workload(seed=22, ncx=13, ncz=12, nphases=5, air=0.3,
+                                                            periodic=1, markers_per_cell=6), 0, 0, 1, 1),
+    "erfc": (lambda: W.prep_workload(seed=23, ncx=12, ncz=12, nphases=3, air=0.2, markers_per_cell=6), 1, 0, 1, 1),
+    "hardening_stencil9": (lambda: W.prep_workload(seed=24, ncx=15, ncz=10, nphases=4, air=0.2,
+                                                  markers_per_cell=6), 0, 1, 0, 9),
+}
+
+# ShearModCompExpGrid: name: builder
+SHEAR_CASES = {
+    "basic": lambda: W.prep_workload(seed=31, ncx=12, ncz=10, nphases=5),
+    "air_periodic": lambda: W.prep_workload(seed=32, ncx=13, ncz=11, nphases=4, air=0.3, periodic=1),
+    "one_phase_typical": lambda: W.prep_workload(seed=33, ncx=9, ncz=14, nphases=1, sc=W.TYPICAL),
 }
 
 def _dilatant_density(w):

@@ -1,7 +1,8 @@
 """Generate the golden fixtures from MDOODZ7.0's own code.
 
 Runs the reference's NonNewtonianViscosityGrid(Aniso), RheologicalOperators (on the
-fields the sweep produced), StrainRateComponents and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
+fields the sweep produced), StrainRateComponents, CohesionFrictionDilationGrid (with
+markers), ShearModCompExpGrid and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
 sources by oracle/Makefile (target `ref`), on the cases of cases.py and stores their
 outputs in tests/golden/*.npz.  Inputs are
 regenerated from the seeds by the tests; a SHA-256 of the inputs is stored
@@ -25,6 +26,8 @@ import oracle_lib as O  # noqa: E402
 
 INPUT_GRID = [k for k in R.CEN_IN + R.VER_IN + R.ANI_IN_N + R.ANI_IN_S + ["BCp_type", "BCg_type"]]
 STRAIN_INPUTS = ["u_in", "v_in", "BCp_type", "BCg_type", "wxz"]
+PREP_INPUTS = ["phase_perc_n", "phase_perc_s", "BCp_type", "BCg_type", "strain_pl_n", "strain_pl_s", "noise_n",
+               "noise_s"]
 
 
 def digest(arrays, keys):
@@ -40,6 +43,16 @@ def digest(arrays, keys):
 
 def grid_inputs_digest(w):
     return digest(w.arrays, INPUT_GRID + ["phase_perc_n", "phase_perc_s"])
+
+
+def prep_inputs_digest(w):
+    """Grid inputs and materials of a preparation case (and its markers, if any)."""
+    h = hashlib.sha256(digest(w.arrays, PREP_INPUTS).encode())
+    h.update(bytes(w.mat))
+    for k in ("x", "z", "phase", "strain_pl"):
+        if "markers" in w.info:
+            h.update(np.ascontiguousarray(w.info["markers"][k]).tobytes())
+    return h.hexdigest()
 
 
 def point_inputs_digest(pin):
@@ -83,6 +96,21 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"strain_rates_{name}.npz"), inputs_sha256=dig,
                             **{k: w.arrays[k] for k in R.SR_N + R.SR_S})
         print("strain rates", name)
+    for name, (builder, smooth, hard, noise, stencil) in cases.SOFTENING_CASES.items():
+        w = builder()
+        mk = dict(w.info["markers"], interp_stencil=stencil)
+        dig = prep_inputs_digest(w)
+        rc, sn, ss = O.ref_softening_markers(w.model, w.mat, R.PrepFieldSet(w.arrays), mk, smooth, hard, noise)
+        np.savez_compressed(os.path.join(HERE, f"softening_{name}.npz"), inputs_sha256=dig, strain_pl_n=sn,
+                            strain_pl_s=ss, **{k: w.arrays[k] for k in R.SOFT_N + R.SOFT_S})
+        print("softening", name)
+    for name, builder in cases.SHEAR_CASES.items():
+        w = builder()
+        dig = prep_inputs_digest(w)
+        O.ref_shear_modulus(w.model, w.mat, R.PrepFieldSet(w.arrays))
+        np.savez_compressed(os.path.join(HERE, f"shear_modulus_{name}.npz"), inputs_sha256=dig,
+                            **{k: w.arrays[k] for k in R.MOD_N + R.MOD_S})
+        print("shear modulus", name)
     for name in cases.POINT_CASES:
         md, m, pin, aniso, centroid, fu = cases.point_case(name)
         n = pin["phase"].size
