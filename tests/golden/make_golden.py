@@ -55,6 +55,33 @@ def prep_inputs_digest(w):
     return h.hexdigest()
 
 
+def prep_inputs(w):
+    """The inputs of a preparation case, stored beside its outputs: the fixture then needs
+    no generator (numpy's transcendental functions differ between hosts in the last bits,
+    and these cases run on hosts other than the one that made them)."""
+    out = {k: np.array(w.arrays[k]) for k in PREP_INPUTS if not k.startswith("phase_")}
+    for k in ("phase_perc_n", "phase_perc_s"):
+        out[k] = np.stack(w.arrays[k])
+    out["model_bytes"] = np.frombuffer(bytes(w.model), np.uint8)
+    out["materials_bytes"] = np.frombuffer(bytes(w.mat), np.uint8)
+    return out
+
+
+def load_prep_inputs(g):
+    """(model, materials, arrays) of a preparation fixture, outputs set to a sentinel."""
+    model = R.Model.from_buffer_copy(g["model_bytes"].tobytes())
+    mat = R.PrepMaterials.from_buffer_copy(g["materials_bytes"].tobytes())
+    a = {k: np.array(g[k]) for k in PREP_INPUTS if not k.startswith("phase_")}
+    for k in ("phase_perc_n", "phase_perc_s"):
+        a[k] = [np.ascontiguousarray(x) for x in g[k]]
+    nc, nv = (model.Nx - 1) * (model.Nz - 1), model.Nx * model.Nz
+    for k in R.SOFT_N + R.MOD_N:
+        a[k] = np.full(nc, -7.0)
+    for k in R.SOFT_S + R.MOD_S:
+        a[k] = np.full(nv, -7.0)
+    return model, mat, a
+
+
 def point_inputs_digest(pin):
     return digest(pin, ["phase"] + R.PT_IN + R.PT_ANI)
 
@@ -100,15 +127,18 @@ def main():
         w = builder()
         mk = dict(w.info["markers"], interp_stencil=stencil)
         dig = prep_inputs_digest(w)
+        inputs = prep_inputs(w)
         rc, sn, ss = O.ref_softening_markers(w.model, w.mat, R.PrepFieldSet(w.arrays), mk, smooth, hard, noise)
-        np.savez_compressed(os.path.join(HERE, f"softening_{name}.npz"), inputs_sha256=dig, strain_pl_n=sn,
-                            strain_pl_s=ss, **{k: w.arrays[k] for k in R.SOFT_N + R.SOFT_S})
+        inputs.update(strain_pl_n=sn, strain_pl_s=ss)
+        np.savez_compressed(os.path.join(HERE, f"softening_{name}.npz"), inputs_sha256=dig, **inputs,
+                            **{k: w.arrays[k] for k in R.SOFT_N + R.SOFT_S})
         print("softening", name)
     for name, builder in cases.SHEAR_CASES.items():
         w = builder()
         dig = prep_inputs_digest(w)
+        inputs = prep_inputs(w)
         O.ref_shear_modulus(w.model, w.mat, R.PrepFieldSet(w.arrays))
-        np.savez_compressed(os.path.join(HERE, f"shear_modulus_{name}.npz"), inputs_sha256=dig,
+        np.savez_compressed(os.path.join(HERE, f"shear_modulus_{name}.npz"), inputs_sha256=dig, **inputs,
                             **{k: w.arrays[k] for k in R.MOD_N + R.MOD_S})
         print("shear modulus", name)
     for name in cases.POINT_CASES:

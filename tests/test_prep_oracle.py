@@ -6,6 +6,7 @@ own marker interpolation (P2Mastah) puts on the grid, and must equal the referen
 whole CohesionFrictionDilationGrid bit for bit; ShearModCompExpGrid likewise.  Then the
 golden fixtures, the drop-in over the CPU backend and the error status."""
 import os
+import platform
 
 import numpy as np
 import pytest
@@ -15,7 +16,7 @@ import mdz_workloads as W
 import oracle_lib as O
 from common import clone
 from golden import cases
-from golden.make_golden import prep_inputs_digest
+from golden.make_golden import load_prep_inputs, prep_inputs_digest
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 need_ref = pytest.mark.skipif(O.reference() is None, reason="reference build absent (oracle/_ref)")
@@ -75,16 +76,20 @@ def test_shear_modulus_restatement_is_the_reference(name):
 
 
 def golden_prep(name, kind):
-    if kind == "softening":
-        builder = cases.SOFTENING_CASES[name][0]
-    else:
-        builder = cases.SHEAR_CASES[name]
-    w = builder()
+    """A preparation fixture: its stored inputs (as a workload) and the reference's outputs."""
     g = np.load(os.path.join(GOLDEN, f"{kind}_{name}.npz"))
-    assert str(g["inputs_sha256"]) == prep_inputs_digest(w), "input generator changed"
-    if kind == "softening":
-        w.arrays["strain_pl_n"], w.arrays["strain_pl_s"] = g["strain_pl_n"], g["strain_pl_s"]
-    return w, g
+    model, mat, arrays = load_prep_inputs(g)
+    return W.Workload(kind, model, mat, arrays), g
+
+
+@pytest.mark.skipif(platform.machine() != "x86_64", reason="the fixtures were generated on an x86-64 host")
+@pytest.mark.parametrize("kind,name", [("softening", n) for n in cases.SOFTENING_CASES]
+                         + [("shear_modulus", n) for n in cases.SHEAR_CASES])
+def test_prep_fixture_inputs_are_the_generators(kind, name):
+    """On the host that made them, the stored inputs are what the case generators give."""
+    builder = cases.SOFTENING_CASES[name][0] if kind == "softening" else cases.SHEAR_CASES[name]
+    g = np.load(os.path.join(GOLDEN, f"{kind}_{name}.npz"))
+    assert str(g["inputs_sha256"]) == prep_inputs_digest(builder()), "input generator changed"
 
 
 @pytest.mark.parametrize("name", list(cases.SOFTENING_CASES))
