@@ -24,9 +24,14 @@ namespace {
 __device__ __forceinline__ bool finite(double x) {
   return (((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffull) != 0x7ffull;
 }
+__device__ __forceinline__ bool is_zero(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
+}
 
-// Softening of one phase at plastic strain s (RheologyDensity.c:1440-1502)
-__device__ __forceinline__ void soften(const SoftPhase &P, int style, double s, double &f, double &d, double &c) {
+// Softening of one phase at plastic strain s (RheologyDensity.c:1440-1502); ks is
+// order_key(s) and s_nan whether s is NaN, for the comparisons of style 0
+__device__ __forceinline__ void soften(const SoftPhase &P, int style, double s, unsigned long long ks, bool s_nan,
+                                       double &f, double &d, double &c) {
   f = P.phi; d = P.psi; c = P.C;
   if (style == 1) {
     // erfc form (:1446-1470); the three fields share the erfc argument
@@ -45,18 +50,23 @@ __device__ __forceinline__ void soften(const SoftPhase &P, int style, double s, 
   } else if (style == 2) {
     c = fmax(__dadd_rn(P.C, __dmul_rn(P.Hc, s)), P.C_end);  // :1472-1475
   } else {
-    // piecewise linear (:1478-1499): three tests applied in turn, as in the reference
-    if (s < P.pls_start) {
+    // piecewise linear (:1478-1499): three tests applied in turn, as in the reference;
+    // the comparisons run on integer keys (IEEE semantics: false when either side is NaN)
+    const bool below_start = !s_nan && !P.start_nan && ks < P.key_start;
+    const bool from_end = !s_nan && !P.end_nan && ks >= P.key_end;
+    const bool from_start = !s_nan && !P.start_nan && ks >= P.key_start;
+    const bool below_end = !s_nan && !P.end_nan && ks < P.key_end;
+    if (below_start) {
       if (P.phi_soft == 1) f = P.phi;
       if (P.psi_soft == 1) d = P.psi;
       if (P.coh_soft == 1) c = P.C;
     }
-    if (s >= P.pls_end) {
+    if (from_end) {
       if (P.phi_soft == 1) f = P.phi_end;
       if (P.psi_soft == 1) d = P.psi_end;
       if (P.coh_soft == 1) c = P.C_end;
     }
-    if (s >= P.pls_start && s < P.pls_end) {
+    if (from_start && below_end) {
       if (P.phi_soft == 1) f = __dadd_rn(P.phi, __dmul_rn(P.q_phi, s));
       if (P.psi_soft == 1) d = __dadd_rn(P.psi, __dmul_rn(P.q_psi, s));
       if (P.coh_soft == 1) c = __dadd_rn(P.C, __dmul_rn(P.q_C, s));
@@ -73,12 +83,14 @@ __global__ void __launch_bounds__(256) k_softening(const SoftArgs A) {
   double fric = 0.0, dil = 0.0, C = 0.0;
   if (solid) {
     const double s = cen ? A.strain_n[n] : A.strain_s[n];
+    const unsigned long long ks = order_key(s);
+    const bool s_nan = is_nan_bits(s);
     for (int p = 0; p < A.np; p++) {
       const double w = cen ? A.perc_n[p][n] : A.perc_s[p][n];
       double f, d, c;
-      soften(A.ph[p], A.style, s, f, d, c);
+      soften(A.ph[p], A.style, s, ks, s_nan, f, d, c);
       // a zero fraction of finite values adds a zero, which leaves the sums unchanged
-      if (w == 0.0 && finite(f) && finite(d) && finite(c)) continue;
+      if (is_zero(w) && finite(f) && finite(d) && finite(c)) continue;
       fric = __dadd_rn(fric, __dmul_rn(w, f));
       dil = __dadd_rn(dil, __dmul_rn(w, d));
       C = __dadd_rn(C, __dmul_rn(w, c));
@@ -102,7 +114,7 @@ __device__ __forceinline__ void harmonic(const ModArgs &A, const double *const *
   double a = 0.0;
   for (int p = 0; p < A.np; p++) {
     const double w = perc[p][n];
-    if (A.skip_zero && w == 0.0) continue;
+    if (A.skip_zero && is_zero(w)) continue;
     mu = __dadd_rn(mu, div_by(w, A.G[p]));
     bet = __dadd_rn(bet, div_by(w, A.bet[p]));
     if (alp) a = __dadd_rn(a, __dmul_rn(w, A.alp[p]));
@@ -125,7 +137,8 @@ __global__ void __launch_bounds__(256) k_moduli(const ModArgs A) {
     double mu = 0.0, bet = 0.0, alp = 0.0;
     const signed char bc = A.bcp[c0];
     if (bc != 30 && bc != 31) harmonic(A, A.perc_n, c0, mu, bet, &alp);
-    if (isinf(mu)) {  // :1688-1690
+    if (((unsigned long long)__double_as_longlong(mu) & 0x7fffffffffffffffull) == 0x7ff0000000000000ull) {
+      // isinf, :1688-1690
       const unsigned long long key = ((unsigned long long)c0 << 8) | (unsigned long long)(-MDZ_ESHEAR_INF);
       atomicMin(&A.stats->err_key, key);
     }
