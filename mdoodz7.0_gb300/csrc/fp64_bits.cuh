@@ -1,0 +1,68 @@
+// fp64_bits.cuh -- tests on the bits of a double that stay on the integer pipe.
+//
+// GB300 runs FP64 instructions, compares included, at 1/64 of the FP32 rate, and the
+// grid kernels of this library are bound by that pipe.  A test such as "x is finite" or
+// "x is zero" written on the bit pattern is cheap integer work, but a compiler that sees
+// the bitcast may turn it back into an FP64 compare (DSETP).  The two 32-bit words are
+// therefore taken through an opaque register move, after which the tests are plain
+// integer operations.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace mdz {
+
+__device__ __forceinline__ void fp64_words(double x, unsigned &lo, unsigned &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+}
+
+__device__ __forceinline__ unsigned fp64_hi(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  return hi;
+}
+
+// biased exponent field, 0..2047
+__device__ __forceinline__ unsigned fp64_exponent(double x) { return (fp64_hi(x) >> 20) & 0x7ffu; }
+
+// not Inf or NaN
+__device__ __forceinline__ bool fp64_finite(double x) { return fp64_exponent(x) != 0x7ffu; }
+
+// +0 or -0
+__device__ __forceinline__ bool fp64_is_zero(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  return ((hi << 1) | lo) == 0u;
+}
+
+// +Inf or -Inf
+__device__ __forceinline__ bool fp64_is_inf(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  return (hi & 0x7fffffffu) == 0x7ff00000u && lo == 0u;
+}
+
+// NaN
+__device__ __forceinline__ bool fp64_is_nan(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  return (hi & 0x7fffffffu) > 0x7ff00000u || ((hi & 0x7fffffffu) == 0x7ff00000u && lo != 0u);
+}
+
+// -0 exactly
+__device__ __forceinline__ bool fp64_is_negative_zero(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  return hi == 0x80000000u && lo == 0u;
+}
+
+// for x, y not NaN: x < y exactly when fp64_order_key(x) < fp64_order_key(y) (unsigned);
+// -0 and +0 share a key, as they compare equal
+__device__ __forceinline__ unsigned long long fp64_order_key(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  unsigned long long b = ((unsigned long long)hi << 32) | lo;
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+}  // namespace mdz

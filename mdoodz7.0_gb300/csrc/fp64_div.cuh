@@ -17,6 +17,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "fp64_bits.cuh"
+
 namespace mdz {
 
 // a divisor b, its rounded reciprocal and whether the fast form may be used with it
@@ -36,8 +38,7 @@ inline Divisor make_divisor(double b) {
 }
 
 __device__ __forceinline__ double div_by(double a, const Divisor &d) {
-  const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ffu;
-  if (d.fast && e - (1023u - 500u) <= 1000u) {
+  if (d.fast && fp64_exponent(a) - (1023u - 500u) <= 1000u) {
     double q = __dmul_rn(a, d.y);
     q = __fma_rn(__fma_rn(-q, d.b, a), d.y, q);
     return __fma_rn(__fma_rn(-q, d.b, a), d.y, q);

@@ -435,8 +435,8 @@ void fold_soft(const mdz_prep_materials *m, int p, SoftPhase &P) {
   P.phi = m->phi[p]; P.psi = m->psi[p]; P.C = m->C[p];
   P.phi_end = m->phi_end[p]; P.psi_end = m->psi_end[p]; P.C_end = m->C_end[p];
   P.pls_start = m->pls_start[p]; P.pls_end = m->pls_end[p]; P.Hc = m->H_c[p];
-  P.key_start = order_key(m->pls_start[p]); P.key_end = order_key(m->pls_end[p]);
-  P.start_nan = is_nan_bits(m->pls_start[p]); P.end_nan = is_nan_bits(m->pls_end[p]);
+  P.key_start = order_key_host(m->pls_start[p]); P.key_end = order_key_host(m->pls_end[p]);
+  P.start_nan = is_nan_host(m->pls_start[p]); P.end_nan = is_nan_host(m->pls_end[p]);
   P.phi_soft = m->phi_soft[p]; P.psi_soft = m->psi_soft[p]; P.coh_soft = m->coh_soft[p];
   const double dstrain = m->pls_end[p] - m->pls_start[p];
   P.q_phi = (m->phi_end[p] - m->phi[p]) / dstrain;

@@ -11,7 +11,8 @@
 //
 // One thread per node, centroids first, then vertices; every access is coalesced.
 // Both kernels are short per node and bound by the FP64 pipe (divisions by the phase
-// constants use the host reciprocal form of fp64_div.cuh).  Every product and sum is
+// constants use the host reciprocal form of fp64_div.cuh; tests on the bits of a double
+// run on the integer pipe, fp64_bits.cuh).  Every product and sum is
 // written with explicit round-to-nearest intrinsics, so no FMA contraction changes a
 // bit against the reference; the per-phase constants are folded on the host with the
 // reference's own expressions.
@@ -21,15 +22,14 @@ namespace mdz {
 
 namespace {
 
-__device__ __forceinline__ bool finite(double x) {
-  return (((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffull) != 0x7ffull;
-}
-__device__ __forceinline__ bool is_zero(double x) {
-  return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
+// one field of the erfc form: ((x - (dX/2) t) - x_end) dX / x0 + x_end (:1451-1454)
+__device__ __forceinline__ double erfc_soften(const SoftPhase &P, int k, double x, double t) {
+  const double v = __dsub_rn(__dsub_rn(x, __dmul_rn(P.half_d[k], t)), P.x_end_[k]);
+  return __dadd_rn(div_by(__dmul_rn(v, P.d[k]), P.x0[k]), P.x_end_[k]);
 }
 
 // Softening of one phase at plastic strain s (RheologyDensity.c:1440-1502); ks is
-// order_key(s) and s_nan whether s is NaN, for the comparisons of style 0
+// fp64_order_key(s) and s_nan whether s is NaN, for the comparisons of style 0
 __device__ __forceinline__ void soften(const SoftPhase &P, int style, double s, unsigned long long ks, bool s_nan,
                                        double &f, double &d, double &c) {
   f = P.phi; d = P.psi; c = P.C;
@@ -37,15 +37,9 @@ __device__ __forceinline__ void soften(const SoftPhase &P, int style, double s, 
     // erfc form (:1446-1470); the three fields share the erfc argument
     if (P.phi_soft == 1 || P.psi_soft == 1 || P.coh_soft == 1) {
       const double t = erfc(div_by(-__dsub_rn(s, P.mu_strain), P.dstrain));
-      double *out[3] = {&f, &d, &c};
-      const int soft[3] = {P.phi_soft, P.psi_soft, P.coh_soft};
-      const double x0v[3] = {P.phi, P.psi, P.C};
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        if (soft[k] != 1) continue;
-        const double x = __dsub_rn(__dsub_rn(x0v[k], __dmul_rn(P.half_d[k], t)), P.x_end_[k]);
-        *out[k] = __dadd_rn(div_by(__dmul_rn(x, P.d[k]), P.x0[k]), P.x_end_[k]);
-      }
+      if (P.phi_soft == 1) f = erfc_soften(P, 0, P.phi, t);
+      if (P.psi_soft == 1) d = erfc_soften(P, 1, P.psi, t);
+      if (P.coh_soft == 1) c = erfc_soften(P, 2, P.C, t);
     }
   } else if (style == 2) {
     c = fmax(__dadd_rn(P.C, __dmul_rn(P.Hc, s)), P.C_end);  // :1472-1475
@@ -83,14 +77,14 @@ __global__ void __launch_bounds__(256) k_softening(const SoftArgs A) {
   double fric = 0.0, dil = 0.0, C = 0.0;
   if (solid) {
     const double s = cen ? A.strain_n[n] : A.strain_s[n];
-    const unsigned long long ks = order_key(s);
-    const bool s_nan = is_nan_bits(s);
+    const unsigned long long ks = fp64_order_key(s);
+    const bool s_nan = fp64_is_nan(s);
     for (int p = 0; p < A.np; p++) {
       const double w = cen ? A.perc_n[p][n] : A.perc_s[p][n];
       double f, d, c;
       soften(A.ph[p], A.style, s, ks, s_nan, f, d, c);
       // a zero fraction of finite values adds a zero, which leaves the sums unchanged
-      if (is_zero(w) && finite(f) && finite(d) && finite(c)) continue;
+      if (fp64_is_zero(w) && fp64_finite(f) && fp64_finite(d) && fp64_finite(c)) continue;
       fric = __dadd_rn(fric, __dmul_rn(w, f));
       dil = __dadd_rn(dil, __dmul_rn(w, d));
       C = __dadd_rn(C, __dmul_rn(w, c));
@@ -114,7 +108,7 @@ __device__ __forceinline__ void harmonic(const ModArgs &A, const double *const *
   double a = 0.0;
   for (int p = 0; p < A.np; p++) {
     const double w = perc[p][n];
-    if (A.skip_zero && is_zero(w)) continue;
+    if (A.skip_zero && fp64_is_zero(w)) continue;
     mu = __dadd_rn(mu, div_by(w, A.G[p]));
     bet = __dadd_rn(bet, div_by(w, A.bet[p]));
     if (alp) a = __dadd_rn(a, __dmul_rn(w, A.alp[p]));
@@ -137,8 +131,7 @@ __global__ void __launch_bounds__(256) k_moduli(const ModArgs A) {
     double mu = 0.0, bet = 0.0, alp = 0.0;
     const signed char bc = A.bcp[c0];
     if (bc != 30 && bc != 31) harmonic(A, A.perc_n, c0, mu, bet, &alp);
-    if (((unsigned long long)__double_as_longlong(mu) & 0x7fffffffffffffffull) == 0x7ff0000000000000ull) {
-      // isinf, :1688-1690
+    if (fp64_is_inf(mu)) {  // :1688-1690
       const unsigned long long key = ((unsigned long long)c0 << 8) | (unsigned long long)(-MDZ_ESHEAR_INF);
       atomicMin(&A.stats->err_key, key);
     }

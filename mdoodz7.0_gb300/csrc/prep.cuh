@@ -6,21 +6,20 @@
 #include <cstring>
 
 #include "../../include/mdz_rheo.h"
+#include "fp64_bits.cuh"
 #include "fp64_div.cuh"
 #include "rheo_kernels.cuh"
 
 namespace mdz {
 
-// Order of doubles on the integer pipe: for x, y not NaN, x < y exactly when
-// order_key(x) < order_key(y) as unsigned integers (-0 and +0 share a key, as they compare
-// equal).  Lets a kernel bound by the FP64 pipe test its thresholds off that pipe.
-__host__ __device__ inline unsigned long long order_key(double x) {
+// host side of fp64_order_key (fp64_bits.cuh): the same key, for the folded thresholds
+inline unsigned long long order_key_host(double x) {
   unsigned long long b;
   memcpy(&b, &x, sizeof(b));
   if (b == 0x8000000000000000ull) b = 0;
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
-__host__ __device__ inline bool is_nan_bits(double x) {
+inline bool is_nan_host(double x) {
   unsigned long long b;
   memcpy(&b, &x, sizeof(b));
   return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
@@ -30,7 +29,7 @@ __host__ __device__ inline bool is_nan_bits(double x) {
 // with the reference's own expressions so every folded value is bitwise the same
 struct SoftPhase {
   double phi, psi, C, phi_end, psi_end, C_end, pls_start, pls_end, Hc;
-  unsigned long long key_start, key_end;  // order_key of pls_start / pls_end
+  unsigned long long key_start, key_end;  // fp64_order_key of pls_start / pls_end
   int start_nan, end_nan;                 // a NaN bound makes its comparisons false
   double q_phi, q_psi, q_C;              // style 0: (x_end - x) / (pls_end - pls_start)
   double mu_strain;                      // style 1: 0.5 * (pls_end + pls_start)

@@ -20,6 +20,8 @@
 // are bitwise those of the reference.
 #include "strain_rates.cuh"
 
+#include "fp64_bits.cuh"
+
 namespace mdz {
 
 namespace {
@@ -48,15 +50,11 @@ struct SrShared {
 // x == 0 or 2^-1000 <= |x| <= 2^1000: the range in which a quarter of a sum of such
 // values rounds exactly like the sum of their quarters (no subnormal, no overflow)
 __device__ __forceinline__ bool tame(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
-  return (e - 23u) <= 2000u || (b << 1) == 0ull;
+  return (fp64_exponent(x) - 23u) <= 2000u || fp64_is_zero(x);
 }
 
 // +0.0 in place of -0.0 (the reference's averages start from +0.0 and never end at -0.0)
-__device__ __forceinline__ double no_negative_zero(double x) {
-  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
-}
+__device__ __forceinline__ double no_negative_zero(double x) { return fp64_is_negative_zero(x) ? 0.0 : x; }
 
 __global__ void __launch_bounds__(kSrTx * kSrTz) k_strain_rates(const StrainArgs A) {
   __shared__ SrShared S;
