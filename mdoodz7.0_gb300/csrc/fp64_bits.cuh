@@ -65,4 +65,49 @@ __device__ __forceinline__ unsigned long long fp64_order_key(double x) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// The 64-bit pattern of x (through the same opaque unpack).
+__device__ __forceinline__ unsigned long long fp64_bits(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+constexpr unsigned long long kFp64AbsMask = 0x7fffffffffffffffull, kFp64InfBits = 0x7ff0000000000000ull;
+
+__device__ __forceinline__ unsigned long long fp64_key_of_bits(unsigned long long b) {
+  if (b == 0x8000000000000000ull) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// IEEE comparisons of two doubles on the integer pipe, with the IEEE results for every
+// input: false when either side is NaN, -0 equal to +0.
+__device__ __forceinline__ bool fp64_lt(double a, double b) {
+  const unsigned long long ba = fp64_bits(a), bb = fp64_bits(b);
+  if ((ba & kFp64AbsMask) > kFp64InfBits || (bb & kFp64AbsMask) > kFp64InfBits) return false;
+  return fp64_key_of_bits(ba) < fp64_key_of_bits(bb);
+}
+__device__ __forceinline__ bool fp64_le(double a, double b) {
+  const unsigned long long ba = fp64_bits(a), bb = fp64_bits(b);
+  if ((ba & kFp64AbsMask) > kFp64InfBits || (bb & kFp64AbsMask) > kFp64InfBits) return false;
+  return fp64_key_of_bits(ba) <= fp64_key_of_bits(bb);
+}
+__device__ __forceinline__ bool fp64_gt(double a, double b) { return fp64_lt(b, a); }
+__device__ __forceinline__ bool fp64_ge(double a, double b) { return fp64_le(b, a); }
+
+// |x| < t, IEEE, for any x and t
+__device__ __forceinline__ bool fp64_abs_lt(double x, double t) {
+  const unsigned long long ax = fp64_bits(x) & kFp64AbsMask, bt = fp64_bits(t);
+  if (ax > kFp64InfBits || (bt & kFp64AbsMask) > kFp64InfBits) return false;
+  return fp64_key_of_bits(ax) < fp64_key_of_bits(bt);
+}
+// |x| > t, IEEE, for any x and t
+__device__ __forceinline__ bool fp64_abs_gt(double x, double t) {
+  const unsigned long long ax = fp64_bits(x) & kFp64AbsMask, bt = fp64_bits(t);
+  if (ax > kFp64InfBits || (bt & kFp64AbsMask) > kFp64InfBits) return false;
+  return fp64_key_of_bits(ax) > fp64_key_of_bits(bt);
+}
+
+// x == y as IEEE numbers, for a y that is neither NaN nor zero (bit equality then)
+__device__ __forceinline__ bool fp64_eq_nonzero(double x, double y) { return fp64_bits(x) == fp64_bits(y); }
+
 }  // namespace mdz

@@ -33,7 +33,7 @@ __device__ __forceinline__ void phase_loop(const OpArgs &A, const OpNode &nd, co
                                            double &detadE, double &ddivpdE, double &danidE, double *drhodP) {
   for (int p = 0; p < A.M.np; p++) {
     const double vol = nd.centroid ? A.perc_n[p][nd.idx] : A.perc_s[p][nd.idx];
-    if (!(fabs(vol) > 1e-13)) continue;
+    if (!fp64_abs_gt(vol, 1e-13)) continue;
     PointOut o;
     if (ANISO) point_aniso(A.M, A.ph[p], in, ctx, an, A.polish, o);
     else point_iso(A.M, A.ph[p], in, ctx, A.polish, o);
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(128) k_operators(const __grid_constant__ OpArg
     fd_derivatives<ANISO>(A, nd, dE, dV, dA, drhodp);
     for (int p = 0; p < M.np; p++) {
       const double vol = nd.centroid ? A.perc_n[p][c] : A.perc_s[p][c];
-      if (fabs(vol) > 1e-13) calls += 8;
+      if (fp64_abs_gt(vol, 1e-13)) calls += 8;
     }
     if (nd.centroid) {
       const double K = A.compressible ? 1.0 / in.beta : 0.0, Kdt = K * M.dt_model;

@@ -31,6 +31,7 @@
 #include <stdint.h>
 
 #include "../../include/mdz_rheo.h"
+#include "fp64_bits.cuh"
 #include "fp64_math.cuh"
 
 namespace mdz {
@@ -124,12 +125,12 @@ __device__ __forceinline__ void node_strain_update(NodeCtx &c);
 __device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &in, bool need_lnd, NodeCtx &c) {
   node_strain_update(c);
   c.Traw = in.T;
-  c.T = (in.T < M.Tmin) ? M.Tmin : in.T;
+  c.T = fp64_lt(in.T, M.Tmin) ? M.Tmin : in.T;
   c.invT = 1.0 / c.T;
   c.lnd = need_lnd ? fast_log(in.d) : 0.0;
   c.inv_d = 0.0;
   sincos(in.fric, &c.sin_fric, &c.cos_fric);
-  c.sin_dil = (c.dil == 0.0) ? 0.0 : sin(c.dil);
+  c.sin_dil = fp64_is_zero(c.dil) ? 0.0 : sin(c.dil);
 }
 
 // The strain-rate invariant and what depends on it (RheologyDensity.c:455-459); the
@@ -137,7 +138,7 @@ __device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &i
 __device__ __forceinline__ void node_strain_iso(const ModelConst &M, const NodeIn &in, NodeCtx &c) {
   const double Eyy = -(in.Exx + in.Ezz);
   double Eii = sqrt(0.5 * (in.Exx * in.Exx + in.Ezz * in.Ezz + Eyy * Eyy) + in.Exz * in.Exz);
-  if (Eii * M.scale_E < 1e-30) Eii = M.Eii_floor;
+  if (fp64_lt(Eii * M.scale_E, 1e-30)) Eii = M.Eii_floor;
   c.Eii = Eii;
 }
 
@@ -221,7 +222,7 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
     double lnB = ph.lin_lnK + (ph.lin_Q + P * ph.lin_V) * ph.lin_invRn * c.invT;
     if (fl & F_LIN_A) lnB -= ph.lin_an * phi;
     L.lnB_lin = lnB;
-    const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, lnB) : lnB;
+    const double lnBd = !fp64_is_zero(ph.lin_m) ? fma(ph.lin_mn, lnd, lnB) : lnB;
     L.ln_inv[K_LIN] = lnEii - fma(lnEii, ph.lin_invn, lnBd);
   }
   if (peierls) {
@@ -235,7 +236,7 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
   }
   if (fl & F_GBS) {
     double lnB = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * phi;
-    if (ph.gbs_m != 0.0) lnB += ph.gbs_mn * lnd;
+    if (!fp64_is_zero(ph.gbs_m)) lnB += ph.gbs_mn * lnd;
     L.ln_inv_gbs = lnEii - fma(lnEii, ph.gbs_invn, lnB);
   }
 }
@@ -289,17 +290,17 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
     q.n[k] = L.n[k];
     q.nc[k] = 0.0;
     if (!(L.mech & bit)) continue;
-    if (k != K_EXP && L.n[k] == 1.0) {  // Newtonian law: Eii eta / eta_k
+    if (k != K_EXP && fp64_eq_nonzero(L.n[k], 1.0)) {  // Newtonian law: Eii eta / eta_k
       const double a = Eii * law_inv(L, k);
       if (k == K_LIN) q.a_lin1 = a;
       else q.a_pwl1 = a;
       A += a;
     } else {
       q.nl |= 1 << k;
-      if (L.ln_inv[k] > ln_inv_p) { ln_inv_p = L.ln_inv[k]; p = k; }
+      if (fp64_gt(L.ln_inv[k], ln_inv_p)) { ln_inv_p = L.ln_inv[k]; p = k; }
     }
   }
-  if (!(ln_inv_p > -kInf)) q.nl = 0;
+  if (!fp64_gt(ln_inv_p, -kInf)) q.nl = 0;
   q.lp = ln_eta_up + ln_inv_p;
   q.nmax = 0.0;
 #pragma unroll
@@ -320,7 +321,7 @@ __device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, 
                                         double step = -1.0) {
   double *e = s.e;
   S = 0.0;
-  if (step >= -0.5) {
+  if (fp64_ge(step, -0.5)) {
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
       if (q.nl >> k & 1) {
@@ -358,12 +359,11 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s
   for (int it = 0; it < nitmax; it++) {
     double r, S;
     ve_eval(q, sv, s, r, S, step);
-    const double ar = fabs(r);
-    if (ar < q.thr_conv) { s.iters = it + 1; break; }
-    if (it == nitmax - 1 && ar > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
+    if (fp64_abs_lt(r, q.thr_conv)) { s.iters = it + 1; break; }
+    if (it == nitmax - 1 && fabs(r) > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
     const double d = r / fma(q.Aup, sv, S);
     sv = fma(sv, d, sv);
-    step = (fabs(d) * q.nmax < 1e-5) ? d : -1.0;
+    step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
   }
   s.eta = sv * q.eta_up;
 }
@@ -577,12 +577,12 @@ __device__ __forceinline__ void start_viscosity(const ModelConst &M, double ln_i
   eta_up = M.eta_up0;
   ln_eta_up = M.ln_eta_up0;
   bool from_cst = false;
-  if (constant && eta_cst < eta_up) { eta_up = eta_cst; from_cst = true; }
-  if (ln_inv_max > -kInf) {
+  if (constant && fp64_lt(eta_cst, eta_up)) { eta_up = eta_cst; from_cst = true; }
+  if (fp64_gt(ln_inv_max, -kInf)) {
     const double e = fast_exp(-ln_inv_max);
-    if (e < eta_up) { eta_up = e; ln_eta_up = -ln_inv_max; from_cst = false; }
+    if (fp64_lt(e, eta_up)) { eta_up = e; ln_eta_up = -ln_inv_max; from_cst = false; }
   }
-  if (elastic && c.eta_el < eta_up) { eta_up = c.eta_el; ln_eta_up = c.ln_eta_el; from_cst = false; }
+  if (elastic && fp64_lt(c.eta_el, eta_up)) { eta_up = c.eta_el; ln_eta_up = c.ln_eta_el; from_cst = false; }
   if (from_cst) ln_eta_up = fast_log(eta_cst);
 }
 
@@ -604,7 +604,7 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
                                  IsoState &S, PointOut &o) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, diffusion = (fl & F_LIN) != 0, gs = (fl & F_GS) != 0;
-  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
   const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
   const int elastic = c.elastic;
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el;
@@ -618,14 +618,14 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   o.rho = 0.0;
   o.d1 = ph.gs_ref;
   o.inv_d1 = ph.inv_gs_ref;
-  if (diffusion && ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
+  if (diffusion && fp64_gt(ph.lin_m, 0.0) && fp64_lt(in.d, M.d_min)) set_status(o.status, MDZ_EGRAIN_ZERO);
 
   Laws &L = S.L;
   creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
   double Tyield = 0.0, C = in.C;
   if (plastic == 1) {  // :530-539
     Tyield = C * c.cos_fric + P * c.sin_fric;
-    if (ph.Slim < Tyield) { C = ph.Slim; Tyield = ph.Slim; }
+    if (fp64_lt(ph.Slim, Tyield)) { C = ph.Slim; Tyield = ph.Slim; }
   }
   double eta_cst = 0.0, Ag = 0.0, lnd = c.lnd;
   if (constant) eta_cst = ph.eta0;
@@ -663,7 +663,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
   const int gbs = (fl & F_GBS) != 0, gs = (fl & F_GS) != 0;
-  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
   const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
   const int elastic = c.elastic;
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt;
@@ -708,7 +708,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   double gdot = 0.0, divp = 0.0, Pc = P, eta_vep = 0.0, lam_dot = 0.0, A_tau = 1.0, eta_vp = ph.eta_vp;
   if (plastic == 1) {
     double F = Tii - Tyield;
-    if (F > 1e-17) {
+    if (fp64_gt(F, 1e-17)) {
       const double tol = M.eta_tol, eta_vp0 = ph.eta_vp, n_vp = ph.n_vp;
       const bool vp1 = (fl & F_VP1) != 0;
       const double ksd = K * dt * c.sin_fric * c.sin_dil;
@@ -724,11 +724,10 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
         Tyield = Tyield + gdot * eta_vp;
         Tiic = Tii - eta_ve * gdot;
         F = Tiic - Tyield;
-        const double res = fabs(F);
-        if (res < tol || res < tol * F0) break;
+        if (fp64_abs_lt(F, tol) || fp64_abs_lt(F, tol * F0)) break;
         gdot -= F / (-eta_ve - eta_vp / n_vp - ksd);
       }
-      if (Tiic < 0.0) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }  // :697-704
+      if (fp64_lt(Tiic, 0.0)) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }  // :697-704
       o.Pcorr = Pc;
       eta_vep = Tiic * c.inv2Eii;
       Tii = Tiic;
@@ -771,7 +770,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     if (diffusion) {
       // eta_lin = B pow(Eii_lin, 1/n-1) pow(d1, m/n) = Tii/(2 Eii_lin) (d1/d)^(m/n), d1 = gs_ref
       double inv_lin = e_lin * inv_half_T;
-      if (ph.lin_m != 0.0 && !gs) inv_lin *= fast_exp(ph.lin_mn * (lnd - ph.ln_gs_ref));
+      if (!fp64_is_zero(ph.lin_m) && !gs) inv_lin *= fast_exp(ph.lin_mn * (lnd - ph.ln_gs_ref));
       inv += inv_lin;
     }
     if (constant) inv += (1.0 / eta_cst);
@@ -794,7 +793,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
       o.Wtot = T2 * (Eii * inv_half_T);  // T2 / eta_ve, with Tii_ve = 2 eta_ve Eii
       o.Wel = T2 * c.inv_eta_el;
       o.Wdiss = T2 * inv;
-      if (o.Wdiss < 0.0) set_status(o.status, MDZ_EWDISS);
+      if (fp64_lt(o.Wdiss, 0.0)) set_status(o.status, MDZ_EWDISS);
     }
   } else {
     o.Eii_pl = 0.0;
@@ -802,10 +801,10 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     o.div_el = 0.0;
   }
   // limiters (:1058-1073)
-  if (o.etaVE > M.max_eta) o.etaVE = M.max_eta;
-  if (o.etaVE < M.min_eta) o.etaVE = M.min_eta;
-  if (eta > M.max_eta) eta = M.max_eta;
-  if (eta < M.min_eta) eta = M.min_eta;
+  if (fp64_gt(o.etaVE, M.max_eta)) o.etaVE = M.max_eta;
+  if (fp64_lt(o.etaVE, M.min_eta)) o.etaVE = M.min_eta;
+  if (fp64_gt(eta, M.max_eta)) eta = M.max_eta;
+  if (fp64_lt(eta, M.min_eta)) eta = M.min_eta;
   o.eta = eta;
 }
 
@@ -856,7 +855,7 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
                                    const AnisoNode &an, IsoState &S, PointOut &o) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
-  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
   const int plastic = (fl & F_PLANY) != 0;
   const int elastic = c.elastic;
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
@@ -867,7 +866,7 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   o.OverS = 0.0; o.Wtot = o.Wel = o.Wdiss = 0.0;
   o.d1 = in.d;
   o.inv_d1 = c.inv_d;
-  if (diffusion && ph.lin_m > 0.0 && in.d < M.d_min) set_status(o.status, MDZ_EGRAIN_ZERO);
+  if (diffusion && fp64_gt(ph.lin_m, 0.0) && fp64_lt(in.d, M.d_min)) set_status(o.status, MDZ_EGRAIN_ZERO);
 
   Laws &L = S.L;
   creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
@@ -895,7 +894,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
                                    double *eta_conv = nullptr) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
-  const int peierls = ((fl & F_EXPV) != 0) && (c.Traw < M.TmaxPeierls);
+  const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
   const int plastic = (fl & F_PLANY) != 0;
   const int elastic = c.elastic;
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
@@ -945,28 +944,28 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     double step = -1.0;  // binomial update of the previous point's terms (see ve_eval)
     for (int it = 0; it < 50; it++) {
       ve_eval(q, sv, s, r, S, step);
-      if (isnan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
+      if (fp64_is_nan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
       const double d = r / fma(q.Aup, sv, S);
       sv = fma(sv, d, sv);
-      step = (fabs(d) * q.nmax < 1e-5) ? d : -1.0;
-      if (sv <= 0.0) { sv = min_eta / eta_up; step = -1.0; }
+      step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
+      if (fp64_le(sv, 0.0)) { sv = min_eta / eta_up; step = -1.0; }
       const double ar = fabs(r);
-      if (ar < q.thr_conv) { o.iters = it + 1; break; }
+      if (fp64_abs_lt(r, q.thr_conv)) { o.iters = it + 1; break; }
       if (it == 49 && ar < 10.0 * tol * Eii) break;
       if (it == 49 && ar > q.thr_fail) { set_status(o.status, MDZ_EANISO_ITER); break; }
     }
     eta_ve = sv * eta_up;
     Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
   }
-  if (eta_ve < min_eta) eta_ve = min_eta;  // :589-603
-  if (eta_ve > max_eta) eta_ve = max_eta;
+  if (fp64_lt(eta_ve, min_eta)) eta_ve = min_eta;  // :589-603
+  if (fp64_gt(eta_ve, max_eta)) eta_ve = max_eta;
   const double Tii_ve = Tii;
   if (eta_conv) *eta_conv = eta_ve;
   double Tr_xx = 2.0 * eta_ve * an.Er_xx, Tr_zz = 2.0 * eta_ve * an.Er_zz, Tr_xz = 2.0 * eta_ve * an.Er_xz / in.ani_fac;
   double eta_vep = eta_ve, gdot = 0.0, Pc = P;
   const double Ft = Tii - Tyield;
   int is_pl = 0;
-  if (Ft > 1e-17 && plastic) {  // :625-648
+  if (fp64_gt(Ft, 1e-17) && plastic) {  // :625-648
     is_pl = 1;
     gdot = Ft / (eta_ve + ph.eta_vp + K * dt * c.sin_dil * c.sin_fric);
     const double Tiic = Tii - gdot * eta_ve;
@@ -984,8 +983,8 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   o.Tzz = nz2 * Tr_xx + lx2 * Tr_zz + 2. * lxlz * Tr_xz;
   o.Txz = lxlz * Tr_xx - lxlz * Tr_zz + (lx2 - nz2) * Tr_xz;
   o.Pcorr = Pc;
-  if (eta_vep < min_eta) eta_vep = min_eta;
-  if (eta_vep > max_eta) eta_vep = max_eta;
+  if (fp64_lt(eta_vep, min_eta)) eta_vep = min_eta;
+  if (fp64_gt(eta_vep, max_eta)) eta_vep = max_eta;
   o.etaVE = eta_vep;
   o.is_pl = is_pl;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
@@ -1011,8 +1010,8 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
       o.Wdiss = T2 * inv;
     }
   }
-  if (eta > max_eta) eta = max_eta;  // :720-721
-  if (eta < min_eta) eta = min_eta;
+  if (fp64_gt(eta, max_eta)) eta = max_eta;  // :720-721
+  if (fp64_lt(eta, min_eta)) eta = min_eta;
   o.eta = eta;
 }
 

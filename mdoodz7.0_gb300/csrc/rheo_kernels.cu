@@ -171,12 +171,12 @@ __device__ __forceinline__ void node_store(const SweepArgs &A, const Node &n, do
   if (n.solid) {
     if (n.centroid) {
       out[CO_d] = 1.0 / out[CO_d];
-      if (!ANISO && (isinf(out[CO_d]) || isnan(out[CO_d]))) set_status(status, MDZ_EEMPTY_CELL);
+      if (!ANISO && !fp64_finite(out[CO_d])) set_status(status, MDZ_EEMPTY_CELL);
     }
     if (avg == 1) {
       out[CO_eta] = 1.0 / out[CO_eta];
       out[CO_eta_phys] = 1.0 / out[CO_eta_phys];
-      if (isinf(out[CO_eta_phys]) || isnan(out[CO_eta_phys])) set_status(status, MDZ_ENONFINITE);
+      if (!fp64_finite(out[CO_eta_phys])) set_status(status, MDZ_ENONFINITE);
     } else if (avg == 2) {
       out[CO_eta] = exp(out[CO_eta]);
       out[CO_eta_phys] = exp(out[CO_eta_phys]);
@@ -240,7 +240,7 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
   if (n.solid) {
     for (int p = 0; p < A.M.np; p++) {
       const double perc = node_perc(A, n, p);
-      if (!(fabs(perc) > 1e-13)) {  // :1210-1212
+      if (!fp64_abs_gt(perc, 1e-13)) {  // :1210-1212
         node_iters(A, n, p, 0);
         continue;
       }
@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
     int status = MDZ_OK;
     for (int p = 0; p < A.M.np; p++) {  // uniform over the CTA
       const double perc = (valid && n.solid) ? node_perc(A, n, p) : 0.0;
-      const bool active = fabs(perc) > 1e-13;
+      const bool active = fp64_abs_gt(perc, 1e-13);
       if (valid && n.solid && !active) node_iters(A, n, p, 0);
       IsoState st;
       PointOut o;
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
     if (MODE == MODE_COLLECT && valid) {  // items of inactive phases carry a NaN target
       for (int p = 0; p < A.M.np; p++) {
         const double perc = n.solid ? node_perc(A, n, p) : 0.0;
-        if (!(fabs(perc) > 1e-13)) W.Y_out[((long long)p * total + i) * 2] = __int_as_float(0x7fc00000);
+        if (!fp64_abs_gt(perc, 1e-13)) W.Y_out[((long long)p * total + i) * 2] = __int_as_float(0x7fc00000);
       }
     }
   }
