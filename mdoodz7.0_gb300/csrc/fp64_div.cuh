@@ -46,4 +46,17 @@ __device__ __forceinline__ double div_by(double a, const Divisor &d) {
   return a / d.b;
 }
 
+// r / den for a Newton update, where a correctly rounded quotient is not needed (the
+// iteration corrects a step's error on the next evaluation): the hardware reciprocal
+// estimate (PTX rcp.approx.ftz.f64) refined by one Newton step, y (2 - den y), then
+// r y -- three FP64 instructions in place of the general division.  den outside
+// [2^-1000, 2^1000] (zero, subnormal, huge, Inf, NaN) takes the IEEE division.
+__device__ __forceinline__ double newton_quotient(double r, double den) {
+  if (fp64_exponent(den) - 23u > 2000u) return r / den;
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(den));
+  y = __fma_rn(y, __fma_rn(-den, y, 1.0), y);
+  return __dmul_rn(r, y);
+}
+
 }  // namespace mdz

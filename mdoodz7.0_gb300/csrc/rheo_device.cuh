@@ -32,6 +32,7 @@
 
 #include "../../include/mdz_rheo.h"
 #include "fp64_bits.cuh"
+#include "fp64_div.cuh"
 #include "fp64_math.cuh"
 
 namespace mdz {
@@ -361,7 +362,7 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s
     ve_eval(q, sv, s, r, S, step);
     if (fp64_abs_lt(r, q.thr_conv)) { s.iters = it + 1; break; }
     if (it == nitmax - 1 && fabs(r) > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
-    const double d = r / fma(q.Aup, sv, S);
+    const double d = newton_quotient(r, fma(q.Aup, sv, S));
     sv = fma(sv, d, sv);
     step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
   }
@@ -945,7 +946,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     for (int it = 0; it < 50; it++) {
       ve_eval(q, sv, s, r, S, step);
       if (fp64_is_nan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
-      const double d = r / fma(q.Aup, sv, S);
+      const double d = newton_quotient(r, fma(q.Aup, sv, S));
       sv = fma(sv, d, sv);
       step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
       if (fp64_le(sv, 0.0)) { sv = min_eta / eta_up; step = -1.0; }
