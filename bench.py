@@ -45,7 +45,7 @@ UNIT = "point-updates/s"
 # the same field distributions at 513 x 513 cells (527,365 nodes), per workload
 # (profiles/k_sweep_plain_large_513.md, profiles/k_sweep_aniso_513.md).
 # `roofline.achieved` = this x nodes / the CUDA-event time of one launch.
-FP64_FLOPS_PER_POINT = {"plain_large": 1817.4, "aniso": 1233.4}
+FP64_FLOPS_PER_POINT = {"plain_large": 1817.4, "aniso": 1171.9}
 # DRAM bytes (read + write) per point-update of the same captures, scaled to a launch by
 # its node count; the write count of those small captures misses lines still in L2 when
 # the kernel ends.
