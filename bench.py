@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-operators", action="store_true", help="skip the Newton-operator timing")
     ap.add_argument("--no-strain-rates", action="store_true", help="skip the StrainRateComponents timing")
     ap.add_argument("--no-prep", action="store_true", help="skip the Softening / ShearModCompExpGrid timing")
+    ap.add_argument("--no-markers", action="store_true", help="skip the UpdateParticleStress timing")
     args = ap.parse_args()
     if args.size is None:
         args.size = 4097 if args.workload == "aniso" else 2049
@@ -113,6 +114,20 @@ def prep_bytes(step, nc, nv, nphases):
     if step == "softening":
         return reads + (nc + nv) * (16 + 24)
     return reads + nc * 24 + nv * 16
+
+
+def marker_bytes(n, nx, nz, director):
+    """Compulsory HBM bytes of one UpdateParticleStress call (RheologyParticles.c:1725-2004)
+    on a grid without air: per marker x, z and phase read (20 B) and its three stresses
+    read and written (48 B), with the director its two components read and written
+    (32 B); the grid's new and old centroid stresses (32 B) and BCp read once, the new
+    and old vertex shear stress (16 B) and BCg read and wxz read and written (16 B), and
+    with the director u_in and v_in read.  The vertex weight-sum scratch is not counted."""
+    nc, nv = (nx - 1) * (nz - 1), nx * nz
+    b = n * (20 + 48 + (32 if director else 0)) + nc * 33 + nv * 33
+    if director:
+        b += 8 * (nx * (nz + 1) + (nx + 1) * nz)
+    return b
 
 
 class ClockSampler:
@@ -520,6 +535,39 @@ def main():
         prep["grid"] = f"{args.size}x{args.size} cells, {args.phases} phases, piecewise-linear softening with marker noise"
         del pd, pfs, pw
 
+    # ---- UpdateParticleStress: grid stress increments to the markers ----
+    markers = None
+    if not args.no_markers:
+        mw = W.marker_workload(seed=REP.replica_seed(17, rank), ncx=args.size, markers_per_cell=16)
+        gd = {k: torch.from_numpy(v).to(dev) for k, v in mw.arrays.items()}
+        md = {k: torch.from_numpy(v).to(dev) for k, v in mw.info["markers"].items()}
+        nmk = int(mw.info["markers"]["x"].size)
+        markers = {"grid": f"{args.size}x{args.size} cells, 16 markers per cell ({nmk} markers, cell by cell), "
+                           "2 % inactive, no air"}
+        variants = {"jaumann_stencil1": (1, 1, 0, 1, 1), "analytical_director_stencil9": (1, 2, 1, 1, 9)}
+        for name, o in variants.items():
+            opts = R.MarkerOpts()
+            opts.elastic, opts.stress_rotation, opts.anisotropy, opts.advection, opts.interp_stencil = o
+            call = lambda: ctx.marker_stress(mw.model, opts, gd, md, mw.info["dx"], mw.info["dz"], mem=R.MEM_DEVICE)
+            for _ in range(max(3, args.warmup)):
+                call()
+            barrier()
+            reps = 5 * args.steps
+            k_ms = []
+            e0.record(stream)
+            for _ in range(reps):
+                _, mst = call()
+                k_ms.append(mst.elapsed_ms)
+            e1.record(stream)
+            barrier()
+            ms = REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps
+            nbytes = marker_bytes(nmk, mw.model.Nx, mw.model.Nz, o[2] == 1)
+            markers[name] = {"ms_per_call": ms, "kernel_ms_per_call": statistics.mean(k_ms),
+                             "markers_per_s": REP.whole_job_rate(nmk, ws, ms),
+                             "algorithmic_bytes_per_call": nbytes,
+                             "hbm_achieved_gbs": nbytes / (statistics.mean(k_ms) * 1e-3) / 1e9}
+        del gd, md, mw
+
     # ---- end to end through the C ABI with pinned host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -568,7 +616,7 @@ def main():
     roof["algorithmic_bytes_per_launch"] = bytes_alg
     if strain is not None:
         strain["hbm_frac"] = strain["hbm_achieved_gbs"] / hbm if hbm else None
-    for v in (prep or {}).values():
+    for v in list((prep or {}).values()) + list((markers or {}).values()):
         if isinstance(v, dict):
             v["hbm_frac"] = v["hbm_achieved_gbs"] / hbm if hbm else None
 
@@ -599,7 +647,7 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
             "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op,
-            "strain_rates": strain, "input_preparation": prep}
+            "strain_rates": strain, "input_preparation": prep, "marker_stress": markers}
     print(json.dumps(line))
     if ws > 1:
         REP.finalize()

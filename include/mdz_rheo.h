@@ -25,6 +25,8 @@
  *   mdz_rheo_softening      <- CohesionFrictionDilationGrid after its P2Mastah step
  *                              def MDLIB/RheologyDensity.c:1539 (Softening :1432)
  *   mdz_rheo_shear_modulus  <- ShearModCompExpGrid, def MDLIB/RheologyDensity.c:1634
+ *   mdz_rheo_marker_stress  <- UpdateParticleStress (subgrid_diffusion 0/1)
+ *                              MDLIB/mdoodz-private.h:415, def MDLIB/RheologyParticles.c:1725
  *
  * All arithmetic is IEEE binary64.  Unless a call says otherwise it is
  * synchronous (returns after the results are in the caller's buffers), like
@@ -64,6 +66,7 @@ extern "C" {
 #define MDZ_EANISO_ITER     -19  /* aniso VE iterations failed (AnisotropyRoutines.c:580-583, exit 0) */
 #define MDZ_ESCRATCH        -20  /* request larger than the static scratch of mdz_rheo_points_static */
 #define MDZ_ESHEAR_INF      -21  /* infinite centroid shear modulus (RheologyDensity.c:1688-1690, exit 32) */
+#define MDZ_EMARKER_OUT     -22  /* marker beyond the vertex grid in x (ParticleRoutines.c:1258-1266, exit 89) */
 
 /* memory space of the field pointers handed to a sweep */
 #define MDZ_MEM_HOST   0  /* host memory: the library copies in and out (drop-in mode) */
@@ -349,6 +352,56 @@ int mdz_rheo_softening(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_prep
  * Reads phase_perc_n/_s and the BC flags; writes mu_n, bet_n, alp, mu_s, bet_s. */
 int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_prep_materials *mat,
                            mdz_prep_fields *f, int mem, int flags, mdz_sweep_stats *stats);
+
+/* ---- marker feedback of the sweep: UpdateParticleStress -----------------
+ * The markers (`markers`, MDLIB/mdoodz-private.h:30-49) the stress update reads and
+ * writes.  Inactive markers have phase -1. */
+typedef struct mdz_markers {
+  int64_t        n;                  /* Nb_part */
+  const double  *x, *z;
+  const int32_t *phase;
+  double        *sxxd, *szzd, *sxz;  /* marker stresses, updated in place */
+  double        *nx, *nz;            /* director, updated when anisotropy and advection are on */
+} mdz_markers;
+
+/* The grid side of UpdateParticleStress: spacing, node coordinates as the reference
+ * builds them (GridRoutines.c:270-315: xg/zg vertex coordinates, Nx and Nz of them;
+ * xvz/zvx the centroid coordinates with one ghost at each end, Nx+1 and Nz+1 of them),
+ * the sweep's new and old stresses, and the velocities (director rotation only). */
+typedef struct mdz_marker_grid {
+  double dx, dz;
+  const double *xg_coord, *zg_coord, *xvz_coord, *zvx_coord;
+  const signed char *BCp_type, *BCg_type;
+  const double *sxxd, *szzd, *sxxd0, *szzd0;  /* centroids */
+  const double *sxz, *sxz0;                   /* vertices */
+  const double *u_in, *v_in;                  /* staggered velocities (layout of mdz_strain_rate_fields) */
+  double *wxz;                                /* vertices; rewritten as the reference rewrites it (below) */
+} mdz_marker_grid;
+
+/* The params switches of UpdateParticleStress (MDLIB/include/mdoodz.h:49-139). */
+typedef struct mdz_marker_opts {
+  int elastic, subgrid_diffusion, stress_rotation, anisotropy, advection, interp_stencil;
+} mdz_marker_opts;
+
+/* UpdateParticleStress (MDLIB/RheologyParticles.c:1725-2004) without its subgrid stress
+ * diffusion (subgrid_diffusion 0 or 1; 2 returns MDZ_EUNSUPPORTED):
+ *   - with anisotropy and advection on, the director of every active marker turns with
+ *     the velocity gradients interpolated from the grid (:1784-1802);
+ *   - with elastic on, every marker takes the grid's stress increments sxxd - sxxd0,
+ *     szzd - szzd0 (centroids, Interp_Grid2P_centroids2) and sxz - sxz0 (vertices,
+ *     Interp_Grid2P) (:1919-1966), then the stress rotation of stress_rotation 1
+ *     (Jaumann) or 2 (analytical) (:1967-1992).  The reference rotates with a marker
+ *     spin that its P2Mastah call fills the other way round (markers -> grid, from a
+ *     zeroed marker array), so the rotation turns by zero and wxz is overwritten with
+ *     zeros wherever markers reach a vertex; both are reproduced.
+ * model supplies Nx, Nz, periodic_x and dt.  Results are those of the reference to the
+ * last bit, except the director, whose normalisation squares by multiplication where
+ * the reference calls pow (a few ulp).  A marker outside the vertex grid in x returns
+ * MDZ_EMARKER_OUT (the reference exits with code 89).  `mem`, `flags` (MDZ_SWEEP_ASYNC)
+ * and `stats` as for mdz_rheo_strain_rates. */
+int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_opts *opts,
+                           mdz_marker_grid *grid, mdz_markers *markers, int mem, int flags,
+                           mdz_sweep_stats *stats);
 
 /* ---- allocation-free variant (no reference counterpart) ----------------
  * mdz_rheo_points on the CURRENT device without any context and without allocating:

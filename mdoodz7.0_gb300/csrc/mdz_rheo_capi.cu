@@ -15,6 +15,7 @@
 #include "mlp_train.cuh"
 #include "operators.cuh"
 #include "rheo_kernels.cuh"
+#include "markers.cuh"
 #include "prep.cuh"
 #include "strain_rates.cuh"
 
@@ -238,7 +239,7 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
        S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
-       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_COUNT = S_PREP + 16 };
+       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_COUNT = S_MK + 22 };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -658,6 +659,7 @@ const char *mdz_rheo_status_string(int s) {
     case MDZ_EANISO_ITER: return "anisotropic Visco-Elastic iterations failed";
     case MDZ_ESCRATCH: return "request larger than the static scratch (MDZ_STATIC_SCRATCH_BYTES)";
     case MDZ_ESHEAR_INF: return "infinite shear modulus at a cell centre";
+    case MDZ_EMARKER_OUT: return "marker beyond the grid";
     default: return "unknown status";
   }
 }
@@ -1227,6 +1229,97 @@ int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *md, double dx, dou
     return MDZ_OK;
   }
   return finish(ctx, st);
+}
+
+int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_marker_opts *o, mdz_marker_grid *g,
+                           mdz_markers *mk, int mem, int flags, mdz_sweep_stats *st) {
+  if (!ctx || !md || !o || !g || !mk) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
+  if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (md->Nx < 2 || md->Nz < 2 || mk->n < 0 || mk->n > 0x7fffffffLL) return MDZ_EINVAL;
+  if (o->subgrid_diffusion == 2) return MDZ_EUNSUPPORTED;
+  if (o->interp_stencil != 1 && o->interp_stencil != 9) return MDZ_EINVAL;
+  const bool el = (o->elastic == 1), dir = (o->anisotropy == 1 && o->advection == 1);
+  if (!g->xg_coord || !g->zg_coord || !g->xvz_coord || !g->zvx_coord || !g->BCp_type || !g->BCg_type ||
+      !mk->x || !mk->z || !mk->phase)
+    return MDZ_EINVAL;
+  if (el && (!g->sxxd || !g->szzd || !g->sxxd0 || !g->szzd0 || !g->sxz || !g->sxz0 || !g->wxz || !mk->sxxd ||
+             !mk->szzd || !mk->sxz))
+    return MDZ_EINVAL;
+  if (dir && (!g->u_in || !g->v_in || !mk->nx || !mk->nz)) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  MarkerArgs A;
+  memset(&A, 0, sizeof(A));
+  const size_t Nx = (size_t)md->Nx, Nz = (size_t)md->Nz, Nc = (Nx - 1) * (Nz - 1), Nv = Nx * Nz;
+  const size_t n = (size_t)mk->n;
+  A.n = mk->n; A.Nx = md->Nx; A.Nz = md->Nz; A.periodic_x = md->periodic_x;
+  A.elastic = o->elastic; A.rotation = o->stress_rotation; A.director = dir; A.stencil = o->interp_stencil;
+  A.dt = md->dt;
+  A.dx = make_divisor(g->dx); A.dz = make_divisor(g->dz);
+  // P2Mastah's weight lengths, by its own expressions (ParticleRoutines.c:2218-2221)
+  A.dx_itp = make_divisor(o->interp_stencil == 9 ? 3.0 * g->dx / 2.0 : g->dx / 2.0);
+  A.dz_itp = make_divisor(o->interp_stencil == 9 ? 3.0 * g->dz / 2.0 : g->dz / 2.0);
+  const bool host = (mem == MDZ_MEM_HOST);
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  Mirror mi{ctx};
+  A.xg = mi.in(g->xg_coord, S_MK + 8, Nx, host);
+  A.zg = mi.in(g->zg_coord, S_MK + 9, Nz, host);
+  A.xvz = mi.in(g->xvz_coord, S_MK + 10, Nx + 1, host);
+  A.zvx = mi.in(g->zvx_coord, S_MK + 11, Nz + 1, host);
+  A.bcp = mi.in(g->BCp_type, S_BCP, Nc, host);
+  A.bcg = mi.in(g->BCg_type, S_BCG, Nv, host);
+  A.x = mi.in(mk->x, S_MK + 0, n, host);
+  A.z = mi.in(mk->z, S_MK + 1, n, host);
+  A.phase = mi.in((const int *)mk->phase, S_MK + 2, n, host);
+  if (el) {
+    A.sxxd = mi.in(g->sxxd, S_MK + 12, Nc, host);
+    A.szzd = mi.in(g->szzd, S_MK + 13, Nc, host);
+    A.sxxd0 = mi.in(g->sxxd0, S_MK + 14, Nc, host);
+    A.szzd0 = mi.in(g->szzd0, S_MK + 15, Nc, host);
+    A.sxz = mi.in(g->sxz, S_MK + 16, Nv, host);
+    A.sxz0 = mi.in(g->sxz0, S_MK + 17, Nv, host);
+    A.wxz = (double *)mi.in((const double *)g->wxz, S_MK + 20, Nv, host);  // kept where not rewritten
+    A.m_sxxd = (double *)mi.in((const double *)mk->sxxd, S_MK + 3, n, host);
+    A.m_szzd = (double *)mi.in((const double *)mk->szzd, S_MK + 4, n, host);
+    A.m_sxz = (double *)mi.in((const double *)mk->sxz, S_MK + 5, n, host);
+  }
+  if (dir) {
+    A.u = mi.in(g->u_in, S_MK + 18, Nx * (Nz + 1), host);
+    A.v = mi.in(g->v_in, S_MK + 19, (Nx + 1) * Nz, host);
+    A.m_nx = (double *)mi.in((const double *)mk->nx, S_MK + 6, n, host);
+    A.m_nz = (double *)mi.in((const double *)mk->nz, S_MK + 7, n, host);
+  }
+  if (mi.err) return mi.err;
+  if (el) {
+    if (ensure(ctx->bufs[S_MK + 21], Nv * sizeof(double)) != MDZ_OK) return MDZ_ENOMEM;
+    A.WM = (double *)ctx->bufs[S_MK + 21].p;
+  }
+  A.stats = ctx->d_stats;
+  int rc;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  if (el) CK(cudaMemsetAsync(A.WM, 0, Nv * sizeof(double), ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_marker_update(A, ctx->stream));
+  ctx->launches = 1;
+  if (el) {
+    CK(launch_marker_wxz(A, ctx->stream));
+    ctx->launches = 2;
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (el) {
+    mi.back(mk->sxxd, S_MK + 3, n, host);
+    mi.back(mk->szzd, S_MK + 4, n, host);
+    mi.back(mk->sxz, S_MK + 5, n, host);
+    mi.back(g->wxz, S_MK + 20, Nv, host);
+  }
+  if (dir) {
+    mi.back(mk->nx, S_MK + 6, n, host);
+    mi.back(mk->nz, S_MK + 7, n, host);
+  }
+  if (mi.err) return mi.err;
+  return prep_finish(ctx, flags, st);
 }
 
 // input preparation: Softening over the grid, ShearModCompExpGrid

@@ -1,14 +1,15 @@
 /*
  * mdz_rheo_mdoodz.c -- the MDOODZ7.0-side drop-in: NonNewtonianViscosityGrid,
  * NonNewtonianViscosityGridAniso, RheologicalOperators, StrainRateComponents,
- * CohesionFrictionDilationGrid and ShearModCompExpGrid with the reference's own
- * signatures (MDLIB/mdoodz-private.h:423, :437, :607, :426, :417 and :416), evaluated on
- * the GPU by libmdz_rheo_gb300.so through the C ABI of include/mdz_rheo.h.
+ * CohesionFrictionDilationGrid, ShearModCompExpGrid and UpdateParticleStress with the
+ * reference's own signatures (MDLIB/mdoodz-private.h:423, :437, :607, :426, :417, :416
+ * and :415), evaluated on the GPU by libmdz_rheo_gb300.so through the C ABI of
+ * include/mdz_rheo.h.
  *
  * It is compiled inside the MDOODZ build, against MDLIB/mdoodz-private.h, in place of
  * the definitions at MDLIB/RheologyDensity.c:1131, :1539, :1634, :2001,
- * MDLIB/AnisotropyRoutines.c:885 and MDLIB/StokesRoutines.c:75 (those are compiled out
- * under MDZ_RHEO_GB300).
+ * MDLIB/AnisotropyRoutines.c:885, MDLIB/StokesRoutines.c:75 and
+ * MDLIB/RheologyParticles.c:1725 (those are compiled out under MDZ_RHEO_GB300).
  * Each call unpacks `grid`, `mat_prop`, `params` and `scale` into the library's
  * plain-pointer structs and runs one sweep on host memory: the library uploads the
  * inputs, runs the kernel and writes every output back into the caller's arrays in
@@ -281,6 +282,48 @@ void ShearModCompExpGrid(grid *mesh, mat_prop *materials, params *model, scale s
     fprintf(stderr, "%f x = %2.6e z = %2.6e - BCp %d BCt %d\n", mesh->mu_n[c0], mesh->xc_coord[k] * scaling.L,
             mesh->zc_coord[l] * scaling.L, mesh->BCp.type[c0], mesh->BCt.type[c0]);
     exit(32);
+  }
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
+}
+
+/* UpdateParticleStress (RheologyParticles.c:1725): the markers' stress update from the
+ * grid's stress change, the stress rotation and the director rotation, on the GPU.
+ * subgrid_diffusion 2 is not built; it stops with a message. */
+void UpdateParticleStress(grid *mesh, markers *particles, params *model, mat_prop *materials, scale *scaling) {
+  (void)materials;
+  (void)scaling;
+  mdz_model md;
+  mdz_marker_opts o;
+  mdz_marker_grid g;
+  mdz_markers mk;
+  mdz_sweep_stats st;
+  memset(&md, 0, sizeof(md));
+  md.Nx = mesh->Nx; md.Nz = mesh->Nz; md.periodic_x = model->periodic_x; md.dt = model->dt;
+  o.elastic = model->elastic; o.subgrid_diffusion = model->subgrid_diffusion;
+  o.stress_rotation = model->stress_rotation; o.anisotropy = model->anisotropy;
+  o.advection = model->advection; o.interp_stencil = model->interp_stencil;
+  g.dx = mesh->dx; g.dz = mesh->dz;
+  g.xg_coord = mesh->xg_coord; g.zg_coord = mesh->zg_coord;
+  g.xvz_coord = mesh->xvz_coord; g.zvx_coord = mesh->zvx_coord;
+  g.BCp_type = mesh->BCp.type; g.BCg_type = mesh->BCg.type;
+  g.sxxd = mesh->sxxd; g.szzd = mesh->szzd; g.sxxd0 = mesh->sxxd0; g.szzd0 = mesh->szzd0;
+  g.sxz = mesh->sxz; g.sxz0 = mesh->sxz0;
+  g.u_in = mesh->u_in; g.v_in = mesh->v_in;
+  g.wxz = mesh->wxz;
+  mk.n = particles->Nb_part;
+  mk.x = particles->x; mk.z = particles->z; mk.phase = particles->phase;
+  mk.sxxd = particles->sxxd; mk.szzd = particles->szzd; mk.sxz = particles->sxz;
+  mk.nx = particles->nx; mk.nz = particles->nz;
+  memset(&st, 0, sizeof(st));
+  const int rc = mdz_rheo_marker_stress(mdz_context(), &md, &o, &g, &mk, MDZ_MEM_HOST, 0, &st);
+  if (rc == MDZ_EUNSUPPORTED) {
+    fprintf(stderr, "GB300 rheology: UpdateParticleStress with subgrid_diffusion = %d is not built\n",
+            model->subgrid_diffusion);
+    exit(1);
+  }
+  if (rc == MDZ_EMARKER_OUT) {
+    fprintf(stderr, "marker beyond the grid in x (UpdateParticleStress)\n"); /* ParticleRoutines.c:1261-1265 */
+    exit(89);
   }
   if (rc != MDZ_OK) mdz_fail(rc, &st);
 }

@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "build")
 LIB = os.path.join(BUILD, "libmdz_rheo_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["rheo_kernels.cu", "mdz_rheo_capi.cu", "fp64_probe.cu", "mlp_train.cu", "operators.cu",
-           "strain_rates.cu", "prep.cu"]
+           "strain_rates.cu", "prep.cu", "markers.cu"]
 
 
 def nvcc() -> str:

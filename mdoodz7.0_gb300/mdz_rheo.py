@@ -43,6 +43,7 @@ MDZ_EANISO_NAN = -18
 MDZ_EANISO_ITER = -19
 MDZ_ESCRATCH = -20
 MDZ_ESHEAR_INF = -21
+MDZ_EMARKER_OUT = -22
 STATIC_SCRATCH_BYTES = 4 << 20
 
 MEM_HOST = 0
@@ -302,6 +303,41 @@ class PrepFieldSet:
         self.struct = s
 
 
+class Markers(C.Structure):
+    """mdz_markers: the marker arrays of UpdateParticleStress."""
+    _fields_ = [("n", C.c_int64), ("x", _P), ("z", _P), ("phase", _P), ("sxxd", _P), ("szzd", _P), ("sxz", _P),
+                ("nx", _P), ("nz", _P)]
+
+
+MARKER_GRID_IN = ["xg_coord", "zg_coord", "xvz_coord", "zvx_coord", "BCp_type", "BCg_type", "sxxd", "szzd", "sxxd0",
+                  "szzd0", "sxz", "sxz0", "u_in", "v_in", "wxz"]
+MARKER_ARRAYS = ["x", "z", "phase", "sxxd", "szzd", "sxz", "nx", "nz"]
+
+
+class MarkerGrid(C.Structure):
+    """mdz_marker_grid: the grid side of UpdateParticleStress."""
+    _fields_ = [("dx", C.c_double), ("dz", C.c_double)] + [(n, _P) for n in MARKER_GRID_IN]
+
+
+class MarkerOpts(C.Structure):
+    """mdz_marker_opts: the params switches of UpdateParticleStress."""
+    _fields_ = [(n, C.c_int) for n in ("elastic", "subgrid_diffusion", "stress_rotation", "anisotropy", "advection",
+                                        "interp_stencil")]
+
+
+def make_marker_structs(grid: Dict[str, object], markers: Dict[str, object], dx: float, dz: float):
+    g = MarkerGrid()
+    g.dx, g.dz = dx, dz
+    for n in MARKER_GRID_IN:
+        setattr(g, n, _ptr(grid.get(n)))
+    m = Markers()
+    x = markers["x"]
+    m.n = int(x.numel() if hasattr(x, "numel") else x.size)
+    for n in MARKER_ARRAYS:
+        setattr(m, n, _ptr(markers.get(n)))
+    return g, m
+
+
 def make_points(inputs: Dict[str, object], outputs: Dict[str, object], post_process=1, centroid=1,
                 final_update=0):
     pi = PointInputs()
@@ -372,6 +408,8 @@ def load_library(path: str = LIB_PATH):
                                        C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(SweepStats)]
     lib.mdz_rheo_shear_modulus.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(PrepMaterials),
                                            C.POINTER(PrepFields), C.c_int, C.c_int, C.POINTER(SweepStats)]
+    lib.mdz_rheo_marker_stress.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(MarkerOpts), C.POINTER(MarkerGrid),
+                                           C.POINTER(Markers), C.c_int, C.c_int, C.POINTER(SweepStats)]
     lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -611,6 +649,17 @@ class Context:
                                              flags, C.byref(st))
         if check and rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_shear_modulus")
+        return rc, st
+
+    def marker_stress(self, model, opts, grid: dict, markers: dict, dx, dz, mem=MEM_HOST, flags=0, check=True):
+        """UpdateParticleStress (mdz_rheo_marker_stress): updates the marker stresses (and
+        directors) of `markers` and wxz of `grid` in place."""
+        st = SweepStats()
+        g, m = make_marker_structs(grid, markers, dx, dz)
+        rc = self.lib.mdz_rheo_marker_stress(self.handle, C.byref(model), C.byref(opts), C.byref(g), C.byref(m), mem,
+                                             flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_marker_stress")
         return rc, st
 
     # ---- launch-shape autotuner

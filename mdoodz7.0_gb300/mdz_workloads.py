@@ -565,3 +565,56 @@ def prep_workload(seed: int = 13, ncx: int = 2049, ncz: Optional[int] = None, np
         info["markers"] = dict(x=x, z=z, phase=phase, strain_pl=strain, xmin=0.0, zmin=0.0, dx=dx, dz=dz,
                                interp_stencil=1)
     return Workload("prep", model, pm, a, info=info)
+
+
+def marker_workload(seed: int = 17, ncx: int = 2049, ncz: Optional[int] = None, markers_per_cell: int = 4,
+                    air: float = 0.0, periodic: int = 0, inactive: float = 0.02, sc: Scale = SI,
+                    L: float = 1e5) -> Workload:
+    """Input of UpdateParticleStress on ncx x ncz cells of an L x L domain at x in
+    [-L/2, L/2], z in [-L, 0]: node coordinates built as the reference builds them
+    (running sums of dx from xmin, GridRoutines.c:270-315), the sweep's new and old
+    deviatoric stresses (normal, 10 MPa spread, with increments of 1 %), smooth random
+    velocities as in velocity_field, a spin field wxz to be overwritten, and markers
+    per cell at uniform random positions with random stresses and unit directors, a
+    fraction `inactive` of them with phase -1, laid out cell by cell as MDOODZ seeds them.
+    Air above a wavy surface as in velocity_field.  `arrays` holds the grid fields, `info` the markers, dx and dz."""
+    ncz = ncx if ncz is None else ncz
+    rng = np.random.default_rng(seed)
+    nx, nz = ncx + 1, ncz + 1
+    nc, nv = ncx * ncz, nx * nz
+    dx, dz = L / ncx / sc.L, L / ncz / sc.L
+    xmin, zmin = -0.5 * L / sc.L, -L / sc.L
+
+    def running(x0, step, n):
+        out = np.empty(n)
+        out[0] = x0
+        for i in range(1, n):
+            out[i] = out[i - 1] + step
+        return out
+
+    a: Dict[str, object] = {"xg_coord": running(xmin, dx, nx), "zg_coord": running(zmin, dz, nz),
+                            "xvz_coord": running(xmin - dx / 2.0, dx, nx + 1),
+                            "zvx_coord": running(zmin - dz / 2.0, dz, nz + 1)}
+    S = 1e7 / sc.S
+    a["sxxd"], a["szzd"] = S * rng.standard_normal(nc), S * rng.standard_normal(nc)
+    a["sxxd0"] = a["sxxd"] * (1.0 + 0.01 * rng.standard_normal(nc))
+    a["szzd0"] = a["szzd"] * (1.0 + 0.01 * rng.standard_normal(nc))
+    a["sxz"] = S * rng.standard_normal(nv)
+    a["sxz0"] = a["sxz"] * (1.0 + 0.01 * rng.standard_normal(nv))
+    vel = velocity_field(seed=seed + 1, ncx=ncx, ncz=ncz, air=air, periodic=periodic, sc=sc, L=L)
+    for k in ("u_in", "v_in", "BCp_type", "BCg_type"):
+        a[k] = vel.arrays[k]
+    a["wxz"] = rng.standard_normal(nv) * 1e-14 * sc.t
+    n = nc * markers_per_cell
+    phase = rng.integers(0, 3, n).astype(np.int32)
+    phase[rng.random(n) < inactive] = -1
+    th = rng.uniform(0.0, 2.0 * np.pi, n)
+    # cell by cell, as MDOODZ seeds them (uniform within each cell)
+    cell = np.repeat(np.arange(nc), markers_per_cell)
+    mk = {"x": xmin + ((cell % ncx) + rng.random(n)) * dx, "z": zmin + ((cell // ncx) + rng.random(n)) * dz,
+          "phase": phase,
+          "sxxd": S * rng.standard_normal(n), "szzd": S * rng.standard_normal(n), "sxz": S * rng.standard_normal(n),
+          "nx": np.cos(th), "nz": np.sin(th)}
+    model = make_model(ncx, ncz, 3, sc=sc)  # marker phases 0..2
+    model.periodic_x = periodic
+    return Workload("markers", model, None, a, info=dict(seed=seed, ncx=ncx, ncz=ncz, dx=dx, dz=dz, markers=mk))

@@ -256,6 +256,31 @@ def shim_shear_modulus(model, pmat, fs: "R.PrepFieldSet", drop_in=True):
     return fn(C.byref(model), C.byref(pmat), C.byref(fs.struct))
 
 
+def _marker_call(fn, model, opts, grid, markers, dx, dz):
+    fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.MarkerOpts), C.POINTER(R.MarkerGrid), C.POINTER(R.Markers)]
+    fn.restype = C.c_int
+    g, m = R.make_marker_structs(grid, markers, dx, dz)
+    return fn(C.byref(model), C.byref(opts), C.byref(g), C.byref(m))
+
+
+def orc_marker_stress(model, opts, grid: dict, markers: dict, dx, dz):
+    """UpdateParticleStress on the restatement (numpy arrays, updated in place)."""
+    return _marker_call(oracle().orc_marker_stress, model, opts, grid, markers, dx, dz)
+
+
+def ref_marker_stress(model, opts, grid: dict, markers: dict, dx, dz):
+    """The reference's UpdateParticleStress (numpy arrays, updated in place)."""
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    return _marker_call(lib.ref_marker_stress, model, opts, grid, markers, dx, dz)
+
+
+def shim_marker_stress(model, opts, grid: dict, markers: dict, dx, dz, drop_in=True):
+    name = "shimtest_shim_marker_stress" if drop_in else "shimtest_ref_marker_stress"
+    return _marker_call(getattr(shimtest(), name), model, opts, grid, markers, dx, dz)
+
+
 def orc_points(model, mat, pin, pout, n, aniso=0):
     return oracle().orc_points(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso)
 

@@ -1,7 +1,8 @@
 /*
  * ref_harness.c -- drives the reference's own NonNewtonianViscosityGrid(Aniso),
  * ViscosityConcise(Aniso), RheologicalOperators, StrainRateComponents,
- * CohesionFrictionDilationGrid (with its marker interpolation) and ShearModCompExpGrid,
+ * CohesionFrictionDilationGrid (with its marker interpolation), ShearModCompExpGrid and
+ * UpdateParticleStress,
  * compiled from the MDOODZ7.0 sources, from the plain-pointer structs of
  * include/mdz_rheo.h.
  *
@@ -269,6 +270,39 @@ int ref_shear_modulus(const mdz_model *m, const mdz_prep_materials *pmat, mdz_pr
   grid *g = prep_grid(m, f, 0.0, 0.0, 1.0, 1.0);
   ShearModCompExpGrid(g, mp, &pm, sc);
   free_prep_grid(g);
+  free(mp);
+  return 0;
+}
+
+/* UpdateParticleStress (RheologyParticles.c:1725) on a grid and marker set holding the
+ * arrays it touches; the marker arrays are updated in place, wxz likewise. */
+int ref_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_grid *mg, mdz_markers *mk) {
+  quiet_log();
+  mat_prop *mp = calloc(1, sizeof(mat_prop));
+  params pm;
+  scale sc;
+  fill_params(&pm, &sc, m);
+  pm.dx = mg->dx; pm.dz = mg->dz;
+  pm.elastic = o->elastic; pm.subgrid_diffusion = o->subgrid_diffusion; pm.stress_rotation = o->stress_rotation;
+  pm.anisotropy = o->anisotropy; pm.advection = o->advection; pm.interp_stencil = o->interp_stencil;
+  mdz_grid_fields none;
+  memset(&none, 0, sizeof(none));
+  grid *g = make_grid(m, &none);
+  g->dx = mg->dx; g->dz = mg->dz;
+  g->xg_coord = W(mg->xg_coord); g->zg_coord = W(mg->zg_coord);
+  g->xvz_coord = W(mg->xvz_coord); g->zvx_coord = W(mg->zvx_coord);
+  g->BCp.type = (signed char *)mg->BCp_type; g->BCg.type = (signed char *)mg->BCg_type;
+  g->sxxd = W(mg->sxxd); g->szzd = W(mg->szzd); g->sxxd0 = W(mg->sxxd0); g->szzd0 = W(mg->szzd0);
+  g->sxz = W(mg->sxz); g->sxz0 = W(mg->sxz0);
+  g->u_in = W(mg->u_in); g->v_in = W(mg->v_in);
+  g->wxz = mg->wxz;
+  markers P;
+  memset(&P, 0, sizeof(P));
+  P.Nb_part = (int)mk->n;
+  P.x = (double *)mk->x; P.z = (double *)mk->z; P.phase = (int *)mk->phase;
+  P.sxxd = mk->sxxd; P.szzd = mk->szzd; P.sxz = mk->sxz; P.nx = mk->nx; P.nz = mk->nz;
+  UpdateParticleStress(g, &P, &pm, mp, &sc);
+  free_grid(g);
   free(mp);
   return 0;
 }

@@ -1430,3 +1430,254 @@ int orc_shear_modulus(const mdz_model *md, const mdz_prep_materials *m, mdz_prep
   }
   return bad >= 0 ? MDZ_ESHEAR_INF : MDZ_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* UpdateParticleStress, RheologyParticles.c:1725-2004, for subgrid_diffusion */
+/* 0 or 1, with the grid <-> marker interpolations it calls.                  */
+/* ------------------------------------------------------------------------ */
+
+/* The four centroid corners of a marker in the ghost-extended centroid frame
+ * (Interp_Grid2P_centroids2, ParticleRoutines.c:1349-1514; Centers2Particle, :270-430):
+ * Nx, Nz count centroids, X/Z hold Nx+1 / Nz+1 coordinates (one ghost at each end).
+ * Returns 0, or -1 where the marker lies outside every case the reference handles. */
+static int orc_cell_corners(double x, double z, const double *X, const double *Z, int Nx, int Nz, double dx,
+                            double dz, int per, int *jp, int *ip, int c[4]) {
+  const int j = (int)ceil((x - X[0]) / dx) - 1, i = (int)ceil((z - Z[0]) / dz) - 1;
+  int SW, SE, NW, NE;
+  *jp = j; *ip = i;
+  if (j > 0 && j < Nx && i > 0 && i < Nz) {
+    SW = (j - 1) + (i - 1) * Nx; SE = SW + 1; NW = SW + Nx; NE = NW + 1;
+  } else if (j == 0 && i > 0 && i < Nz) {
+    if (per == 1) { SW = (Nx - 1) + (i - 1) * Nx; SE = (i - 1) * Nx; NW = (Nx - 1) + i * Nx; NE = i * Nx; }
+    else { SW = SE = (i - 1) * Nx; NW = NE = i * Nx; }
+  } else if (j == Nx && i > 0 && i < Nz) {
+    if (per == 1) { SW = (Nx - 1) + (i - 1) * Nx; SE = (i - 1) * Nx; NW = (Nx - 1) + i * Nx; NE = i * Nx; }
+    else { SW = SE = (Nx - 1) + (i - 1) * Nx; NW = NE = (Nx - 1) + i * Nx; }
+  } else if (i == 0 && j > 0 && j < Nx) {
+    SW = NW = j - 1; SE = NE = j;
+  } else if (i == Nz && j > 0 && j < Nx) {
+    SW = NW = (j - 1) + (Nz - 1) * Nx; SE = NE = SW + 1;
+  } else if (i == 0 && j == 0) {
+    if (per == 1) { SW = NW = Nx - 1; SE = NE = 0; }
+    else SW = SE = NW = NE = 0;
+  } else if (i == 0 && j == Nx) {
+    if (per == 1) { SW = NW = Nx - 1; SE = NE = 0; }
+    else SW = SE = NW = NE = Nx - 1;
+  } else if (i == Nz && j == 0) {
+    if (per == 1) { SW = NW = (Nx - 1) + (Nz - 1) * Nx; SE = NE = (Nz - 1) * Nx; }
+    else SW = SE = NW = NE = (Nz - 1) * Nx;
+  } else if (i == Nz && j == Nx) {
+    if (per == 1) { SW = NW = (Nx - 1) + (Nz - 1) * Nx; SE = NE = (Nz - 1) * Nx; }
+    else SW = SE = NW = NE = (Nx - 1) + (Nz - 1) * Nx;
+  } else {
+    return -1;
+  }
+  c[0] = SW; c[1] = SE; c[2] = NW; c[3] = NE;
+  return 0;
+}
+
+static int orc_air(signed char t) { return t == 30 || t == 31; }
+
+/* the bilinear weights of the four corners, in the reference's order (SW, SE, NW, NE) */
+static void orc_weights(double dxm, double dzm, double dx, double dz, double w[4]) {
+  w[0] = (1.0 - dxm / dx) * (1.0 - dzm / dz);
+  w[1] = (dxm / dx) * (1.0 - dzm / dz);
+  w[2] = (1.0 - dxm / dx) * (dzm / dz);
+  w[3] = (dxm / dx) * (dzm / dz);
+}
+
+/* Interp_Grid2P_centroids2 (ParticleRoutines.c:1332-1573) for one active marker: an air
+ * corner lends its weight to the corner across (SW<->NW, SE<->NE); divided by the weight
+ * sum when that exceeds 1e-13.  `field(c)` is the centroid value. */
+static double orc_c2p_sub(const double *F, const signed char *tag, const int c[4], const double w[4]) {
+  const int alt[4] = {c[2], c[3], c[0], c[1]};
+  double v = 0.0, sw = 0.0;
+  for (int q = 0; q < 4; q++) {
+    v += w[q] * F[orc_air(tag[c[q]]) ? alt[q] : c[q]];
+    sw += w[q];
+  }
+  if (sw > 1e-13) v /= sw;
+  return v;
+}
+
+/* Centers2Particle / Vertices2Particle (ParticleRoutines.c:262-455, :464-536): air corners
+ * are left out. */
+static double orc_c2p_skip(const double *F, const signed char *tag, const int c[4], const double w[4]) {
+  double v = 0.0, sw = 0.0;
+  for (int q = 0; q < 4; q++)
+    if (!orc_air(tag[c[q]])) { v += w[q] * F[c[q]]; sw += w[q]; }
+  if (sw > 1e-13) v /= sw;
+  return v;
+}
+
+int orc_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_grid *g, mdz_markers *mk) {
+  if (m->Nx < 2 || m->Nz < 2) return MDZ_EINVAL;
+  if (o->subgrid_diffusion == 2) return MDZ_EUNSUPPORTED;
+  const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1, per = m->periodic_x;
+  const int64_t Nc = (int64_t)Ncx * Ncz, Nv = (int64_t)Nx * Nz, n = mk->n;
+  const double dx = g->dx, dz = g->dz, dt = m->dt;
+  const double *u = g->u_in, *v = g->v_in;
+  int status = MDZ_OK;
+  /* velocity gradients: centroids and vertices below the surface, else 0 (:1751-1782) */
+  const int director = (o->anisotropy == 1 && o->advection == 1);
+  double *dudx_n = NULL, *dvdz_n = NULL, *dudz_s = NULL, *dvdx_s = NULL;
+  if (director) {
+    dudx_n = calloc(Nc, sizeof(double)); dvdz_n = calloc(Nc, sizeof(double));
+    dudz_s = calloc(Nv, sizeof(double)); dvdx_s = calloc(Nv, sizeof(double));
+    for (int64_t c1 = 0; c1 < Nv; c1++) {
+      const int64_t k = c1 % Nx, l = c1 / Nx, c3 = k + l * (Nx + 1);
+      if (g->BCg_type[c1] != 30) {
+        dudz_s[c1] = (u[c1 + Nx] - u[c1]) / dz;
+        dvdx_s[c1] = (v[c3 + 1] - v[c3]) / dx;
+      }
+    }
+    for (int64_t c0 = 0; c0 < Nc; c0++) {
+      const int64_t k = c0 % Ncx, l = c0 / Ncx, c1 = k + l * Nx, c2 = k + l * (Nx + 1);
+      if (!orc_air(g->BCp_type[c0])) {
+        dudx_n[c0] = (u[c1 + 1 + Nx] - u[c1 + Nx]) / dx;
+        dvdz_n[c0] = (v[c2 + 1 + (Nx + 1)] - v[c2 + 1]) / dz;
+      }
+    }
+  }
+  for (int64_t p = 0; p < n; p++) {
+    if (mk->phase[p] == -1) continue;
+    const double x = mk->x[p], z = mk->z[p];
+    if (director) { /* :1784-1802 */
+      int jp, ip, c[4];
+      double w[4];
+      double mdudx = 0.0, mdvdz = 0.0, mdudz = 0.0, mdvdx = 0.0;
+      if (orc_cell_corners(x, z, g->xvz_coord, g->zvx_coord, Ncx, Ncz, dx, dz, per, &jp, &ip, c) != 0) {
+        status = MDZ_EMARKER_OUT;
+        continue;
+      }
+      orc_weights(x - g->xvz_coord[jp], z - g->zvx_coord[ip], dx, dz, w);
+      mdudx = orc_c2p_skip(dudx_n, g->BCp_type, c, w);
+      mdvdz = orc_c2p_skip(dvdz_n, g->BCp_type, c, w);
+      /* Vertices2Particle: cell from |x - X0|, clamped to the grid */
+      int j = (int)ceil(fabs(x - g->xg_coord[0]) / dx) - 1, i = (int)ceil(fabs(z - g->zg_coord[0]) / dz) - 1;
+      if (j < 0) j = 0;
+      if (j > Nx - 2) j = Nx - 2;
+      if (i < 0) i = 0;
+      if (i > Nz - 2) i = Nz - 2;
+      const int cv[4] = {j + i * Nx, j + i * Nx + 1, j + (i + 1) * Nx, j + (i + 1) * Nx + 1};
+      orc_weights(x - g->xg_coord[j], z - g->zg_coord[i], dx, dz, w);
+      mdudz = orc_c2p_skip(dudz_s, g->BCg_type, cv, w);
+      mdvdx = orc_c2p_skip(dvdx_s, g->BCg_type, cv, w);
+      const double nx = mk->nx[p], nz = mk->nz[p];
+      mk->nx[p] += dt * (-(mdudx - mdvdz) * nx * nz - mdvdx * nz * nz + mdudz * nx * nx) * nz;
+      mk->nz[p] += dt * ((mdudx - mdvdz) * nx * nz + mdvdx * nz * nz - mdudz * nx * nx) * nx;
+      const double norm = sqrt(pow(mk->nx[p], 2) + pow(mk->nz[p], 2));
+      mk->nx[p] /= norm;
+      mk->nz[p] /= norm;
+    }
+  }
+  free(dudx_n); free(dvdz_n); free(dudz_s); free(dvdx_s);
+  if (o->elastic != 1) return status;
+
+  /* stress increments grid -> markers (:1919-1966), then ArrayPlusArray on every marker */
+  for (int64_t p = 0; p < n; p++) {
+    double dsx = 0.0, dsz = 0.0, dsxz = 0.0;
+    if (mk->phase[p] != -1) {
+      const double x = mk->x[p], z = mk->z[p];
+      int jp, ip, c[4];
+      double w[4];
+      if (orc_cell_corners(x, z, g->xvz_coord, g->zvx_coord, Ncx, Ncz, dx, dz, per, &jp, &ip, c) != 0) {
+        status = MDZ_EMARKER_OUT;
+      } else {
+        double fx[4], fz[4];
+        const int alt[4] = {c[2], c[3], c[0], c[1]};
+        orc_weights(x - g->xvz_coord[jp], z - g->zvx_coord[ip], dx, dz, w);
+        double sw = 0.0;
+        for (int q = 0; q < 4; q++) {
+          const int cc = orc_air(g->BCp_type[c[q]]) ? alt[q] : c[q];
+          /* dsxxd / dszzd: the change at cells below the surface, else 0 (calloc) */
+          fx[q] = orc_air(g->BCp_type[cc]) ? 0.0 : g->sxxd[cc] - g->sxxd0[cc];
+          fz[q] = orc_air(g->BCp_type[cc]) ? 0.0 : g->szzd[cc] - g->szzd0[cc];
+          dsx += w[q] * fx[q];
+          dsz += w[q] * fz[q];
+          sw += w[q];
+        }
+        if (sw > 1e-13) { dsx /= sw; dsz /= sw; }
+        if (isinf(dsx) || isinf(dsz)) status = MDZ_ENONFINITE; /* ParticleRoutines.c:1565-1569, exit 1 */
+      }
+      /* Interp_Grid2P (ParticleRoutines.c:1223-1321): vertex cell clamped to the grid */
+      int j = (int)ceil((x - g->xg_coord[0]) / dx) - 1;
+      if (j < 0) j = 0;
+      if (j > Nx - 2) { j = Nx - 2; status = MDZ_EMARKER_OUT; }
+      int i = (int)ceil((z - g->zg_coord[0]) / dz) - 1;
+      if (i < 0) i = 0;
+      if (i > Nz - 2) i = Nz - 2;
+      const int cv[4] = {j + i * Nx, j + i * Nx + 1, j + (i + 1) * Nx, j + (i + 1) * Nx + 1};
+      const int alt[4] = {cv[2], cv[3], cv[0], cv[1]};
+      orc_weights(fabs(x - g->xg_coord[j]), fabs(z - g->zg_coord[i]), dx, dz, w);
+      for (int q = 0; q < 4; q++) {
+        const int cc = orc_air(g->BCg_type[cv[q]]) ? alt[q] : cv[q];
+        const double d = (g->BCg_type[cc] != 30) ? g->sxz[cc] - g->sxz0[cc] : 0.0;
+        dsxz += w[q] * d;
+      }
+    }
+    mk->sxxd[p] = mk->sxxd[p] + dsx;
+    mk->szzd[p] = mk->szzd[p] + dsz;
+    mk->sxz[p] = mk->sxz[p] + dsxz;
+  }
+
+  /* :1967-1992: P2Mastah of a zeroed marker array onto wxz (vertices), so wxz becomes
+   * 0 / (sum of marker weights) wherever that sum reaches 1e-30 below the surface; the
+   * marker spin stays zero and the rotation below turns by zero */
+  double *WM = calloc(Nv, sizeof(double));
+  const double dx_itp = (o->interp_stencil == 9) ? 3.0 * dx / 2.0 : dx / 2.0;
+  const double dz_itp = (o->interp_stencil == 9) ? 3.0 * dz / 2.0 : dz / 2.0;
+  for (int64_t p = 0; p < n; p++) {
+    if (mk->phase[p] == -1) continue;
+    const double x = mk->x[p], z = mk->z[p];
+    int ip = (int)ceil((x - g->xg_coord[0]) / dx + 0.5) - 1, jp = (int)ceil((z - g->zg_coord[0]) / dz + 0.5) - 1;
+    if (ip < 0) ip = 0;
+    if (ip > Nx - 1) ip = Nx - 1;
+    if (jp < 0) jp = 0;
+    if (jp > Nz - 1) jp = Nz - 1;
+    const double X = g->xg_coord[ip], Z = g->zg_coord[jp];
+    WM[ip + jp * Nx] += (1.0 - fabs(X - x) / dx_itp) * (1.0 - fabs(Z - z) / dz_itp);
+    if (o->interp_stencil == 9) { /* ParticleRoutines.c:2378-2575 */
+      const int peE = (ip == Nx - 1 && per == 1), peW = (ip == 0 && per == 1);
+      const double xE = X + dx, xW = X - dx, zN = Z + dz, zS = Z - dz;
+      const int kE = ip + 1 - peE * Nx, kW = ip - 1 + peW * Nx;
+#define ORC_W(cond, kk, xx, zz) \
+      if (cond) WM[kk] += (1.0 - fabs(xx - x) / dx_itp) * (1.0 - fabs(zz - z) / dz_itp)
+      /* N, S, E, W, SW, NW, NE, SE, as in the reference */
+      ORC_W(jp < Nz - 1, ip + (jp + 1) * Nx, X, zN);
+      ORC_W(jp > 0, ip + (jp - 1) * Nx, X, zS);
+      ORC_W(ip < Nx - 1 || peE, kE + jp * Nx, xE, Z);
+      ORC_W(ip > 0 || peW, kW + jp * Nx, xW, Z);
+      ORC_W(jp > 0 && (ip > 0 || peW), kW + (jp - 1) * Nx, xW, zS);
+      ORC_W(jp < Nz - 1 && (ip > 0 || peW), kW + (jp + 1) * Nx, xW, zN);
+      ORC_W(jp < Nz - 1 && (ip < Nx - 1 || peE), kE + (jp + 1) * Nx, xE, zN);
+      ORC_W(jp > 0 && (ip < Nx - 1 || peE), kE + (jp - 1) * Nx, xE, zS);
+#undef ORC_W
+    }
+  }
+  for (int64_t c1 = 0; c1 < Nv; c1++)
+    if (!(fabs(WM[c1]) < 1e-30 || orc_air(g->BCg_type[c1]))) g->wxz[c1] = 0.0 / WM[c1];
+  if (per == 1)
+    for (int l = 0; l < Nz; l++) {
+      const int64_t c1 = (int64_t)l * Nx + Nx - 1, c = (int64_t)l * Nx;
+      const double av = 0.5 * (g->wxz[c1] + g->wxz[c]);
+      g->wxz[c1] = av; g->wxz[c] = av;
+    }
+  free(WM);
+  for (int64_t p = 0; p < n; p++) {
+    if (mk->phase[p] == -1) continue;
+    const double txx = mk->sxxd[p], tzz = mk->szzd[p], txz = mk->sxz[p], wxzm = 0.0;
+    if (o->stress_rotation == 1) { /* Jaumann rate */
+      mk->sxxd[p] -= dt * 2.0 * txz * wxzm;
+      mk->szzd[p] -= -dt * 2.0 * txz * wxzm;
+      mk->sxz[p] -= dt * (tzz - txx) * wxzm;
+    }
+    if (o->stress_rotation == 2) { /* analytical rotation */
+      const double angle = dt * wxzm;
+      mk->sxxd[p] = (txx * cos(angle) + txz * sin(angle)) * cos(angle) + (txz * cos(angle) + tzz * sin(angle)) * sin(angle);
+      mk->szzd[p] = -(-txx * sin(angle) + txz * cos(angle)) * sin(angle) + (-txz * sin(angle) + tzz * cos(angle)) * cos(angle);
+      mk->sxz[p] = -(txx * cos(angle) + txz * sin(angle)) * sin(angle) + (txz * cos(angle) + tzz * sin(angle)) * cos(angle);
+    }
+  }
+  return status;
+}

@@ -9,7 +9,8 @@
  * order, MDLIB/RheologyDensity.c:116-1426 and MDLIB/AnisotropyRoutines.c:
  * 257-727, 885-1217, MDLIB/StokesRoutines.c:75-410 with MDLIB/FD_Jacobian.c:48-323,
  * StrainRateComponents (MDLIB/RheologyDensity.c:2001-2097), Softening /
- * CohesionFrictionDilationGrid and ShearModCompExpGrid (:1432-1755), plus
+ * CohesionFrictionDilationGrid and ShearModCompExpGrid (:1432-1755),
+ * UpdateParticleStress (MDLIB/RheologyParticles.c:1725-2004), plus
  * InterpCentroidsToVerticesDouble (MDLIB/GridRoutines.c:108-210).  Built with
  * -ffp-contract=off it is bit-identical to the reference compiled from its own sources on x86-64
  * (pinned by tests/test_oracle_vs_reference.py and the committed golden
@@ -58,6 +59,9 @@ int orc_softening(const mdz_model *model, const mdz_prep_materials *mat, mdz_pre
 /* ShearModCompExpGrid (RheologyDensity.c:1634-1755); MDZ_ESHEAR_INF where the
  * reference exits with code 32. */
 int orc_shear_modulus(const mdz_model *model, const mdz_prep_materials *mat, mdz_prep_fields *f);
+
+/* UpdateParticleStress (RheologyParticles.c:1725-2004), subgrid_diffusion 0 or 1. */
+int orc_marker_stress(const mdz_model *model, const mdz_marker_opts *opts, mdz_marker_grid *grid, mdz_markers *mk);
 
 /* InterpCentroidsToVerticesDouble (GridRoutines.c:108) alone. */
 void orc_interp_c2v(const mdz_model *model, const double *centroid, const signed char *BCp_type,

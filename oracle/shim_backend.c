@@ -1,9 +1,9 @@
 /*
  * shim_backend.c -- TEST INFRASTRUCTURE ONLY.
  *
- * A CPU stand-in for the context, sweep, operator, strain-rate and preparation entry points of
- * libmdz_rheo_gb300.so (include/mdz_rheo.h) that forwards every call to the C
- * restatement (rheo_oracle.c).  Linked with the MDOODZ-side drop-in
+ * A CPU stand-in for the context, sweep, operator, strain-rate, preparation and marker
+ * entry points of libmdz_rheo_gb300.so (include/mdz_rheo.h) that forwards every call to
+ * the C restatement (rheo_oracle.c).  Linked with the MDOODZ-side drop-in
  * (mdoodz7.0_gb300/host/mdz_rheo_mdoodz.c) and with the reference's own sources
  * into oracle/_ref/libmdz_shimtest.so, it lets a CPU test run the drop-in's
  * NonNewtonianViscosityGrid(Aniso), RheologicalOperators and StrainRateComponents
@@ -74,4 +74,11 @@ int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_
                            mdz_prep_fields *f, int mem, int flags, mdz_sweep_stats *stats) {
   if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
   return orc_shear_modulus(model, mat, f);
+}
+
+int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_opts *opts,
+                           mdz_marker_grid *grid, mdz_markers *markers, int mem, int flags, mdz_sweep_stats *stats) {
+  (void)stats;
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_marker_stress(model, opts, grid, markers);
 }

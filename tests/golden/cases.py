@@ -4,7 +4,8 @@ GRID_CASES are small grids of the benchmark workloads (all field layouts,
 averaging modes, scalings, air cells, periodicity); OPERATOR_CASES run
 RheologicalOperators on what a grid case's sweep produced; STRAIN_CASES run
 StrainRateComponents on velocity fields (air, periodicity, one cell, ragged);
-SOFTENING_CASES and SHEAR_CASES the sweep's input preparation.  POINT_CASES drive
+SOFTENING_CASES and SHEAR_CASES the sweep's input preparation; MARKER_CASES the
+markers' stress update (UpdateParticleStress).  POINT_CASES drive
 ViscosityConcise / ViscosityConciseAniso directly on random points and cover
 the branches the grid workloads do not reach: Popov et al. 2025 plasticity
 (plast=2, with and without the tensile line search), paleowattmeter grain size
@@ -90,6 +91,19 @@ SHEAR_CASES = {
     "basic": lambda: W.prep_workload(seed=31, ncx=12, ncz=10, nphases=5),
     "air_periodic": lambda: W.prep_workload(seed=32, ncx=13, ncz=11, nphases=4, air=0.3, periodic=1),
     "one_phase_typical": lambda: W.prep_workload(seed=33, ncx=9, ncz=14, nphases=1, sc=W.TYPICAL),
+}
+
+# UpdateParticleStress: name: (builder, elastic, stress_rotation, anisotropy, advection, interp_stencil)
+MARKER_CASES = {
+    "jaumann": (lambda: W.marker_workload(seed=41, ncx=14, ncz=11, markers_per_cell=4), 1, 1, 0, 1, 1),
+    "analytical_director_air_periodic": (lambda: W.marker_workload(seed=42, ncx=13, ncz=12, markers_per_cell=5,
+                                                                   air=0.3, periodic=1), 1, 2, 1, 1, 1),
+    "stencil9_director_air": (lambda: W.marker_workload(seed=43, ncx=12, ncz=14, markers_per_cell=6, air=0.2),
+                              1, 1, 1, 1, 9),
+    "no_rotation_periodic_stencil9": (lambda: W.marker_workload(seed=44, ncx=15, ncz=10, markers_per_cell=4,
+                                                                periodic=1), 1, 0, 0, 1, 9),
+    "director_only": (lambda: W.marker_workload(seed=45, ncx=11, ncz=13, markers_per_cell=4, air=0.25),
+                      0, 1, 1, 1, 1),
 }
 
 def _dilatant_density(w):

@@ -2,7 +2,7 @@
 
 Runs the reference's NonNewtonianViscosityGrid(Aniso), RheologicalOperators (on the
 fields the sweep produced), StrainRateComponents, CohesionFrictionDilationGrid (with
-markers), ShearModCompExpGrid and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
+markers), ShearModCompExpGrid, UpdateParticleStress and ViscosityConcise(Aniso), compiled from the MDOODZ7.0
 sources by oracle/Makefile (target `ref`), on the cases of cases.py and stores their
 outputs in tests/golden/*.npz.  Inputs are
 regenerated from the seeds by the tests; a SHA-256 of the inputs is stored
@@ -82,6 +82,30 @@ def load_prep_inputs(g):
     return model, mat, a
 
 
+def marker_opts(elastic, rot, aniso, adv, stencil):
+    o = R.MarkerOpts()
+    o.elastic, o.subgrid_diffusion, o.stress_rotation = elastic, 0, rot
+    o.anisotropy, o.advection, o.interp_stencil = aniso, adv, stencil
+    return o
+
+
+def marker_inputs(w):
+    """The inputs of a marker case, stored beside the reference's outputs."""
+    out = {"grid_" + k: np.array(v) for k, v in w.arrays.items()}
+    out.update({"mk_" + k: np.array(v) for k, v in w.info["markers"].items()})
+    out["model_bytes"] = np.frombuffer(bytes(w.model), np.uint8)
+    out["spacing"] = np.array([w.info["dx"], w.info["dz"]])
+    return out
+
+
+def load_marker_inputs(g):
+    """(model, grid arrays, marker arrays, dx, dz) of a marker fixture."""
+    model = R.Model.from_buffer_copy(g["model_bytes"].tobytes())
+    grid = {k[5:]: np.array(g[k]) for k in g.files if k.startswith("grid_")}
+    mk = {k[3:]: np.array(g[k]) for k in g.files if k.startswith("mk_")}
+    return model, grid, mk, float(g["spacing"][0]), float(g["spacing"][1])
+
+
 def point_inputs_digest(pin):
     return digest(pin, ["phase"] + R.PT_IN + R.PT_ANI)
 
@@ -141,6 +165,16 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"shear_modulus_{name}.npz"), inputs_sha256=dig, **inputs,
                             **{k: w.arrays[k] for k in R.MOD_N + R.MOD_S})
         print("shear modulus", name)
+    for name, (builder, elastic, rot, aniso, adv, stencil) in cases.MARKER_CASES.items():
+        w = builder()
+        opts = marker_opts(elastic, rot, aniso, adv, stencil)
+        inputs = marker_inputs(w)
+        grid = {k: w.arrays[k].copy() for k in w.arrays}
+        mk = {k: v.copy() for k, v in w.info["markers"].items()}
+        O.ref_marker_stress(w.model, opts, grid, mk, w.info["dx"], w.info["dz"])
+        np.savez_compressed(os.path.join(HERE, f"markers_{name}.npz"), **inputs,
+                            **{"out_" + k: mk[k] for k in ("sxxd", "szzd", "sxz", "nx", "nz")}, out_wxz=grid["wxz"])
+        print("markers", name)
     for name in cases.POINT_CASES:
         md, m, pin, aniso, centroid, fu = cases.point_case(name)
         n = pin["phase"].size

@@ -1,0 +1,129 @@
+"""UpdateParticleStress (RheologyParticles.c:1725-2004) on the CPU: the C restatement
+against the reference compiled from its own sources (bit for bit: marker stresses,
+directors and the rewritten wxz), against the golden fixtures, the drop-in over the CPU
+backend, and the status of markers the reference cannot place."""
+import os
+
+import numpy as np
+import pytest
+
+import mdz_rheo as R
+import mdz_workloads as W
+import oracle_lib as O
+from golden import cases
+from golden.make_golden import load_marker_inputs, marker_opts
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+need_ref = pytest.mark.skipif(O.reference() is None, reason="reference build absent (oracle/_ref)")
+need_shim = pytest.mark.skipif(O.shimtest() is None, reason="drop-in check library not built")
+OUT = ("sxxd", "szzd", "sxz", "nx", "nz")
+
+
+def same(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.array_equal(a.view(np.uint64), b.view(np.uint64)) if a.dtype == np.float64 else np.array_equal(a, b)
+
+
+def run(fn, w, opts):
+    grid = {k: v.copy() for k, v in w.arrays.items()}
+    mk = {k: v.copy() for k, v in w.info["markers"].items()}
+    rc = fn(w.model, opts, grid, mk, w.info["dx"], w.info["dz"])
+    return rc, grid, mk
+
+
+def boundary_workload():
+    """Markers exactly on vertex and centroid coordinates, on the domain edges and at its
+    corners: the cell and weight arithmetic must place them as the reference does."""
+    w = W.marker_workload(seed=70, ncx=40, ncz=30, markers_per_cell=2, air=0.2, periodic=1)
+    mk = w.info["markers"]
+    xg, zg, xc, zc = w.arrays["xg_coord"], w.arrays["zg_coord"], w.arrays["xvz_coord"], w.arrays["zvx_coord"]
+    rng = np.random.default_rng(1)
+    pick = rng.choice(mk["x"].size, 600, replace=False)
+    mk["x"][pick[:150]] = rng.choice(xg, 150)
+    mk["z"][pick[150:300]] = rng.choice(zg, 150)
+    mk["x"][pick[300:450]] = rng.choice(xc[1:-1], 150)
+    mk["z"][pick[450:600]] = rng.choice(zc[1:-1], 150)
+    mk["x"][:4] = [xg[0], xg[-1], xg[0], xg[-1]]
+    mk["z"][:4] = [zg[0], zg[0], zg[-1], zg[-1]]
+    return w
+
+
+CASES = {
+    # name: (builder, elastic, stress_rotation, anisotropy, advection, interp_stencil)
+    "jaumann": (lambda: W.marker_workload(seed=1, ncx=31, ncz=24), 1, 1, 0, 1, 1),
+    "analytical_director": (lambda: W.marker_workload(seed=2, ncx=27, ncz=30, air=0.3), 1, 2, 1, 1, 1),
+    "periodic_stencil9_director": (lambda: W.marker_workload(seed=3, ncx=25, ncz=19, markers_per_cell=9,
+                                                             air=0.2, periodic=1), 1, 1, 1, 1, 9),
+    "no_rotation": (lambda: W.marker_workload(seed=4, ncx=20, ncz=22, air=0.25), 1, 0, 0, 1, 1),
+    "elastic_off_director": (lambda: W.marker_workload(seed=5, ncx=18, ncz=21, periodic=1), 0, 1, 1, 1, 1),
+    "no_advection": (lambda: W.marker_workload(seed=6, ncx=19, ncz=17, air=0.3), 1, 1, 1, 0, 9),
+    "typical_scale_dense": (lambda: W.marker_workload(seed=7, ncx=16, ncz=16, markers_per_cell=16, sc=W.TYPICAL),
+                            1, 2, 1, 1, 1),
+    "one_column_of_cells": (lambda: W.marker_workload(seed=8, ncx=1, ncz=9, markers_per_cell=6), 1, 1, 1, 1, 1),
+    "markers_on_boundaries": (boundary_workload, 1, 1, 1, 1, 9),
+}
+
+
+@need_ref
+@pytest.mark.parametrize("name", list(CASES))
+def test_marker_stress_restatement_is_the_reference(name):
+    make, *o = CASES[name]
+    w = make()
+    opts = marker_opts(*o)
+    ra, ga, ma = run(O.ref_marker_stress, w, opts)
+    rb, gb, mb = run(O.orc_marker_stress, w, opts)
+    assert ra == 0 and rb == R.MDZ_OK
+    for k in OUT:
+        assert same(ma[k], mb[k]), k
+    assert same(ga["wxz"], gb["wxz"])
+    if o[0] == 1:
+        assert np.any(ma["sxxd"] != w.info["markers"]["sxxd"]) and np.any(ga["wxz"] != w.arrays["wxz"])
+
+
+@pytest.mark.parametrize("name", list(cases.MARKER_CASES))
+def test_oracle_marker_stress_matches_golden(name):
+    g = np.load(os.path.join(GOLDEN, f"markers_{name}.npz"))
+    model, grid, mk, dx, dz = load_marker_inputs(g)
+    opts = marker_opts(*cases.MARKER_CASES[name][1:])
+    assert O.orc_marker_stress(model, opts, grid, mk, dx, dz) == R.MDZ_OK
+    for k in OUT:
+        assert same(mk[k], g["out_" + k]), k
+    assert same(grid["wxz"], g["out_wxz"])
+
+
+@need_shim
+@pytest.mark.parametrize("name", ["analytical_director", "periodic_stencil9_director"])
+def test_drop_in_marker_stress_matches_reference(name):
+    make, *o = CASES[name]
+    w = make()
+    opts = marker_opts(*o)
+    _, ga, ma = run(lambda *a: O.shim_marker_stress(*a, drop_in=False), w, opts)
+    _, gb, mb = run(lambda *a: O.shim_marker_stress(*a, drop_in=True), w, opts)
+    for k in OUT:
+        assert same(ma[k], mb[k]), k
+    assert same(ga["wxz"], gb["wxz"])
+
+
+def test_unchanged_grid_stress_leaves_markers():
+    """No stress change on the grid and no rotation: every marker keeps its stress, and
+    the director stays a unit vector."""
+    w = W.marker_workload(seed=9, ncx=20, ncz=20, air=0.2)
+    w.arrays["sxxd0"], w.arrays["szzd0"], w.arrays["sxz0"] = (w.arrays["sxxd"].copy(), w.arrays["szzd"].copy(),
+                                                              w.arrays["sxz"].copy())
+    rc, g, mk = run(O.orc_marker_stress, w, marker_opts(1, 0, 1, 1, 1))
+    assert rc == R.MDZ_OK
+    for k in ("sxxd", "szzd", "sxz"):
+        assert np.array_equal(mk[k], w.info["markers"][k]), k
+    act = mk["phase"] != -1
+    assert np.allclose(np.hypot(mk["nx"][act], mk["nz"][act]), 1.0, rtol=0, atol=4e-16)
+
+
+def test_marker_beyond_grid_and_subgrid_diffusion_status():
+    w = W.marker_workload(seed=10, ncx=12, ncz=10)
+    w.info["markers"]["x"][5] = w.arrays["xg_coord"][-1] + 0.7 * w.info["dx"]
+    rc, _, _ = run(O.orc_marker_stress, w, marker_opts(1, 1, 0, 1, 1))
+    assert rc == R.MDZ_EMARKER_OUT
+    o = marker_opts(1, 1, 0, 1, 1)
+    o.subgrid_diffusion = 2
+    rc, _, _ = run(O.orc_marker_stress, W.marker_workload(seed=11, ncx=8, ncz=8), o)
+    assert rc == R.MDZ_EUNSUPPORTED
