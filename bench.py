@@ -50,6 +50,10 @@ FP64_FLOPS_PER_POINT = {"plain_large": 1817.4, "aniso": 1171.9}
 # its node count; the write count of those small captures misses lines still in L2 when
 # the kernel ends.
 DRAM_BYTES_PER_POINT = {"plain_large": 267.9, "aniso": 268.3}
+# FP64 work of k_marker_update per marker (inactive ones included), same convention:
+# thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
+# (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
+FP64_FLOPS_PER_MARKER = {"jaumann_stencil1": 98.34, "analytical_director_stencil9": 226.16}
 
 
 def parse():
@@ -195,6 +199,24 @@ def cpu_baseline(W, O, sample_cells=1025, reps=1, aniso=False):
     return {"value": ws.nodes / dt, "unit": UNIT, "cores": O.oracle().orc_num_threads(), "kind": kind,
             "sample": f"{sample_cells}x{sample_cells}-cell grid of the same {ws.mat.Nb_phases}-phase workload "
                       f"({ws.nodes} nodes), {reps} sweep(s), {dt:.2f} s each"}
+
+
+def marker_cpu_baseline(W, O, sample_cells=1025):
+    """UpdateParticleStress on the oracle (the C restatement, one thread) on a bounded
+    sample of the marker workload, Jaumann rotation and the 1-cell stencil."""
+    import mdz_rheo as R
+    mw = W.marker_workload(seed=103, ncx=sample_cells, markers_per_cell=16)
+    opts = R.MarkerOpts()
+    opts.elastic, opts.stress_rotation, opts.anisotropy, opts.advection, opts.interp_stencil = 1, 1, 0, 1, 1
+    grid = {k: v.copy() for k, v in mw.arrays.items()}
+    mk = {k: v.copy() for k, v in mw.info["markers"].items()}
+    t0 = time.perf_counter()
+    O.orc_marker_stress(mw.model, opts, grid, mk, mw.info["dx"], mw.info["dz"])
+    dt = time.perf_counter() - t0
+    n = int(mk["x"].size)
+    return {"value": n / dt, "unit": "markers/s", "cores": 1, "kind": "port",
+            "sample": f"{sample_cells}x{sample_cells} cells, 16 markers per cell ({n} markers), one call, "
+                      f"{dt:.2f} s"}
 
 
 def run_reference(args):
@@ -562,7 +584,7 @@ def main():
             barrier()
             ms = REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps
             nbytes = marker_bytes(nmk, mw.model.Nx, mw.model.Nz, o[2] == 1)
-            markers[name] = {"ms_per_call": ms, "kernel_ms_per_call": statistics.mean(k_ms),
+            markers[name] = {"ms_per_call": ms, "kernel_ms_per_call": statistics.mean(k_ms), "markers_per_call": nmk,
                              "markers_per_s": REP.whole_job_rate(nmk, ws, ms),
                              "algorithmic_bytes_per_call": nbytes,
                              "hbm_achieved_gbs": nbytes / (statistics.mean(k_ms) * 1e-3) / 1e9}
@@ -619,6 +641,12 @@ def main():
     for v in list((prep or {}).values()) + list((markers or {}).values()):
         if isinstance(v, dict):
             v["hbm_frac"] = v["hbm_achieved_gbs"] / hbm if hbm else None
+    for name, v in (markers or {}).items():
+        if name in FP64_FLOPS_PER_MARKER:
+            nmk = v["markers_per_call"]
+            v["fp64_flops_per_marker"] = FP64_FLOPS_PER_MARKER[name]
+            v["fp64_achieved_tflops"] = FP64_FLOPS_PER_MARKER[name] * nmk / (v["kernel_ms_per_call"] * 1e-3) / 1e12
+            v["fp64_frac"] = v["fp64_achieved_tflops"] / peak_fp64
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -627,6 +655,8 @@ def main():
             import oracle_lib as O
             O.build(ref=False)
             cpu = cpu_baseline(W, O, aniso=aniso)
+            if markers is not None:
+                markers["cpu_baseline"] = marker_cpu_baseline(W, O)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
 

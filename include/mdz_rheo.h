@@ -525,6 +525,10 @@ int mdz_rheo_math_selftest(int device, const double *x, int64_t n, double *fast_
  * counterpart. */
 int mdz_rheo_div_selftest(int device, const double *a, int64_t n, double b, double *fast_out,
                           double *cuda_out);
+/* Self-check of the cell-index ceil used by mdz_rheo_marker_stress: ceil(q[i]) from the
+ * bits of q (saturated to +-2^30 beyond that range and for NaN) and CUDA's ceil, for n
+ * host arguments.  No reference counterpart. */
+int mdz_rheo_ceil_selftest(int device, const double *q, int64_t n, int32_t *fast_out, double *cuda_out);
 
 #ifdef __cplusplus
 }

@@ -110,4 +110,28 @@ __device__ __forceinline__ bool fp64_abs_gt(double x, double t) {
 // x == y as IEEE numbers, for a y that is neither NaN nor zero (bit equality then)
 __device__ __forceinline__ bool fp64_eq_nonzero(double x, double y) { return fp64_bits(x) == fp64_bits(y); }
 
+constexpr int kFp64CeilSat = 1 << 30;
+
+// ceil(q) as an int, from the fields of q: |q| = m 2^(e-52) with m the 53-bit
+// significand, so for 0 <= e < 30 the integer part is m >> (52 - e) and any bit below
+// it is a fraction.  |q| >= 2^30 and Inf saturate to +-2^30 and NaN to +2^30 -- the
+// same decisions as the FP64 ceil and int conversion for every cell index of a grid,
+// without an FP64 instruction.
+__device__ __forceinline__ int fp64_ceil_int(double q) {
+  unsigned lo, hi;
+  fp64_words(q, lo, hi);
+  const bool neg = (hi >> 31) != 0u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+  if (e >= 30) {
+    const bool nan = (hi & 0x7fffffffu) > 0x7ff00000u || ((hi & 0x7fffffffu) == 0x7ff00000u && lo != 0u);
+    return (neg && !nan) ? -kFp64CeilSat : kFp64CeilSat;
+  }
+  if (e < 0) return (!neg && ((hi << 1) | lo) != 0u) ? 1 : 0;  // (0, 1) -> 1; (-1, 0] and -0 -> 0
+  const unsigned long long m = ((unsigned long long)(hi & 0xfffffu) << 32 | lo) | (1ull << 52);
+  const int sh = 52 - e;
+  const int ip = (int)(m >> sh);
+  const bool frac = (m & ((1ull << sh) - 1ull)) != 0ull;
+  return neg ? -ip : ip + (frac ? 1 : 0);
+}
+
 }  // namespace mdz

@@ -8,6 +8,7 @@
 // exp/log on the same arguments, for the accuracy tests.
 // mdz_rheo_div_selftest: the division by a known divisor of fp64_div.cuh next to CUDA's
 // division, for the bit-for-bit test.
+// mdz_rheo_ceil_selftest: the integer-pipe ceil of fp64_bits.cuh next to CUDA's ceil.
 #include <cuda_runtime.h>
 
 #include "../../include/mdz_rheo.h"
@@ -49,7 +50,35 @@ __global__ void k_div(const double *a, long long n, mdz::Divisor d, double *fast
   plain[i] = a[i] / d.b;
 }
 
+__global__ void k_ceil(const double *q, long long n, int *fast, double *plain) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fast[i] = mdz::fp64_ceil_int(q[i]);
+  plain[i] = ceil(q[i]);
+}
+
 }  // namespace
+
+extern "C" int mdz_rheo_ceil_selftest(int device, const double *q, int64_t n, int32_t *fast_out, double *cuda_out) {
+  if (!q || n < 0 || !fast_out || !cuda_out) return MDZ_EINVAL;
+  if (n == 0) return MDZ_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return MDZ_ECUDA;
+  const size_t bytes = (size_t)n * sizeof(double);
+  double *d = nullptr;
+  if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return MDZ_ENOMEM;
+  int *di = (int *)(d + 2 * n);
+  int rc = MDZ_OK;
+  if (cudaMemcpy(d, q, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK) {
+    k_ceil<<<(unsigned)((n + 255) / 256), 256>>>(d, n, di, d + n);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = MDZ_ECUDA;
+  }
+  if (rc == MDZ_OK && cudaMemcpy(fast_out, di, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = MDZ_ECUDA;
+  if (rc == MDZ_OK && cudaMemcpy(cuda_out, d + n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
+  cudaFree(d);
+  return rc;
+}
 
 extern "C" int mdz_rheo_div_selftest(int device, const double *a, int64_t n, double b, double *fast_out,
                                      double *cuda_out) {

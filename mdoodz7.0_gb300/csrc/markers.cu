@@ -1,21 +1,36 @@
 // markers.cu -- UpdateParticleStress (MDLIB/RheologyParticles.c:1725-2004) on the GPU,
 // for subgrid_diffusion 0 and 1.
 //
-// k_marker_update: one thread per marker.  It gathers what it needs from the grid
-// directly -- the stress increments sxxd - sxxd0, szzd - szzd0 at the four centroid
-// corners (Interp_Grid2P_centroids2, ParticleRoutines.c:1332-1573) and sxz - sxz0 at
-// the four vertex corners (Interp_Grid2P, :1223-1321), the velocity gradients for the
-// director (Centers2Particle, Vertices2Particle, :262-536) -- instead of building the
-// reference's full-grid temporaries, then updates the marker and scatters its
-// P2Mastah weights (:2170-2600) into WM.
-// k_marker_wxz: one thread per vertex.  The reference's P2Mastah call at
-// RheologyParticles.c:1971 interpolates a zeroed marker array onto wxz, so every vertex
-// below the surface whose weight sum reaches 1e-30 gets 0 / WM; with periodic x, the
-// first and last vertex of each row take their mean.  The marker spin stays zero, so
-// the stress rotation that follows turns by zero; its arithmetic is kept as written.
+// k_marker_grid: one thread per centroid and per vertex.  It forms the per-node fields
+// the reference builds before interpolating to the markers -- the stress increments
+// sxxd - sxxd0, szzd - szzd0, sxz - sxz0 and, for the director, the velocity gradients
+// of RheologyParticles.c:1751-1782 -- once per node instead of once per marker and
+// corner, and clears the scratch of the P2Mastah step.
+// k_marker_update: one thread per marker.  Its centroid cell and weights
+// (Interp_Grid2P_centroids2, ParticleRoutines.c:1332-1573, and Centers2Particle,
+// :262-455) and its vertex cell and weights (Interp_Grid2P, :1223-1321, and
+// Vertices2Particle, :464-536) are formed once and shared by the director and the
+// stress update wherever the reference's expressions give the same bits; the column
+// quotient (x - xg[0]) / dx also gives P2Mastah's nearest vertex (:2301-2311).
+// P2Mastah at RheologyParticles.c:1971 interpolates a zeroed marker array onto wxz:
+// every vertex below the surface whose weight sum WM reaches 1e-30 gets 0 / WM, the
+// others keep wxz.  Every weight is non-negative for a marker on the grid, and a
+// rounded sum of non-negative numbers is at least its largest term, so a vertex is
+// decided by whether some weight reaches 1e-30: a byte flag, set with a plain store,
+// replaces the reference's summation.  A weight is surely >= 1e-30 when the marker
+// lies inside its support by more than 2^-40 of the weight length on both axes,
+// tested without a division; a weight below 1e-30 that is not zero, or one that is not
+// finite, sets *exotic, and k_marker_weights then forms the exact sums with atomics as
+// P2Mastah does.
+// k_marker_wxz: one thread per vertex; with periodic x the first and last vertex of
+// each row take their mean.  The marker spin stays zero, so the stress rotation turns
+// by zero; its arithmetic is kept as written, with cos(+-0) = 1 and sin(+-0) = +-0
+// taken as the exact values they are.
 //
 // Every division by the mesh spacing or by the weight length is correctly rounded
-// (fp64_div.cuh) and every product and sum is written with round-to-nearest intrinsics,
+// (fp64_div.cuh), every product and sum is written with round-to-nearest intrinsics,
+// cell indices come from fp64_ceil_int (the reference's ceil, on the integer pipe), and
+// a division by a weight sum that is exactly 1 is skipped (it returns its numerator),
 // so positions, weights and results are the reference's to the last bit.  The director
 // normalisation squares by multiplication where the reference calls pow.
 #include "markers.cuh"
@@ -32,12 +47,58 @@ __device__ __forceinline__ void report(const MarkerArgs &A, long long k, int cod
   atomicMin(&A.stats->err_key, ((unsigned long long)k << 8) | (unsigned long long)(-code));
 }
 
-// ceil(q) - 1 as the reference converts it to int, saturated far outside the grid (and
-// for NaN) so that no conversion overflows; such markers fall outside every case
-__device__ __forceinline__ int cell_of(double q) {
-  const double c = ceil(q) - 1.0;
-  if (!fp64_abs_lt(c, 1e9)) return fp64_lt(c, 0.0) ? -1000000000 : 1000000000;
-  return (int)c;
+// ceil(q) - 1 as the reference converts it to int; beyond 2^30 in magnitude (and for
+// NaN) saturated, which falls outside every case and every clamp the same way
+__device__ __forceinline__ int cell_of(double q) { return fp64_ceil_int(q) - 1; }
+
+__device__ __forceinline__ bool sign_clear(double v) { return (fp64_hi(v) >> 31) == 0u; }
+
+// (a / sw, b / sw) as the reference writes them.  For sw == 1 a division returns its
+// numerator; the bilinear weights of a cell without air sum to exactly 1 for most
+// markers, and the divisions stay out of line so that a warp whose markers all have
+// sw == 1 branches past them.
+__device__ __noinline__ double2 div_pair(double a, double b, double sw) { return make_double2(a / sw, b / sw); }
+
+__device__ __forceinline__ void div_sum(double &a, double &b, double sw) {
+  if (fp64_bits(sw) != 0x3ff0000000000000ull) {
+    const double2 q = div_pair(a, b, sw);
+    a = q.x;
+    b = q.y;
+  }
+}
+
+// ceil(RN(t/b)) - 1 and ceil(RN(RN(t/b) + 1/2)) - 1: the cell of a marker at distance t
+// from the first node of a frame, and (for the vertex frame) P2Mastah's nearest node
+struct CellPair {
+  int c, h;
+};
+
+__device__ __noinline__ CellPair cell_pair_exact(double t, Divisor d) {
+  const double q = div_by(t, d);
+  return {cell_of(q), cell_of(__dadd_rn(q, 0.5))};
+}
+
+// q0 = RN(t y) lies within 1.5 ulp of t/b (y = RN(1/b)), and RN(t/b) within half an
+// ulp of it.  When q0 >= 1 lies more than 16 of its ulps from every integer and every
+// half-integer, RN(t/b) and RN(RN(t/b) + 1/2) (whose rounding moves by at most one ulp
+// of q0 more) have the ceilings of q0 and q0 + 1/2, which the integer pipe reads from
+// the bits of q0; otherwise the correctly rounded quotient decides.
+__device__ __forceinline__ CellPair cell_pair(double t, const Divisor &d) {
+  const double q0 = __dmul_rn(t, d.y);
+  unsigned lo, hi;
+  fp64_words(q0, lo, hi);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+  if (d.fast && (hi >> 31) == 0u && e >= 0 && e < 29) {
+    const unsigned long long m = ((unsigned long long)(hi & 0xfffffu) << 32 | lo) | (1ull << 52);
+    const int sh = 52 - e;  // fraction bits of q0
+    const unsigned long long one = 1ull << sh, half = one >> 1, f = m & (one - 1ull);
+    const unsigned long long dh = f > half ? f - half : half - f;
+    if (f > 16ull && one - f > 16ull && dh > 16ull) {
+      const int ip = (int)(m >> sh);
+      return {ip, ip + (f > half ? 1 : 0)};
+    }
+  }
+  return cell_pair_exact(t, d);
 }
 
 // bilinear weights in the reference's order SW, SE, NW, NE: a = dxm/dx, b = dzm/dz
@@ -49,11 +110,13 @@ __device__ __forceinline__ void weights(double a, double b, double w[4]) {
   w[3] = __dmul_rn(a, b);
 }
 
+__device__ __forceinline__ int clamp_to(int v, int hi) { return v < 0 ? 0 : (v > hi ? hi : v); }
+
 // Corners of a marker in the ghost-extended centroid frame (Interp_Grid2P_centroids2,
 // Centers2Particle): Ncx, Ncz centroids; returns false outside every handled case.
 __device__ __forceinline__ bool cell_corners(const MarkerArgs &A, double x, double z, int &jp, int &ip, int c[4]) {
   const int Nx = A.Nx - 1, Nz = A.Nz - 1, per = A.periodic_x;
-  const int j = cell_of(div_by(__dsub_rn(x, A.xvz[0]), A.dx)), i = cell_of(div_by(__dsub_rn(z, A.zvx[0]), A.dz));
+  const int j = cell_pair(__dsub_rn(x, A.xvz[0]), A.dx).c, i = cell_pair(__dsub_rn(z, A.zvx[0]), A.dz).c;
   jp = j; ip = i;
   int SW, SE, NW, NE;
   if (j > 0 && j < Nx && i > 0 && i < Nz) {
@@ -77,57 +140,29 @@ __device__ __forceinline__ bool cell_corners(const MarkerArgs &A, double x, doub
   return true;
 }
 
-// Centers2Particle / Vertices2Particle: air corners left out, divided by the weight sum
-// where it exceeds 1e-13
-template <class F>
-__device__ __forceinline__ double gather_skip(const signed char *tag, const int c[4], const double w[4], F field) {
-  double v = 0.0, sw = 0.0;
+// Centers2Particle / Vertices2Particle for a pair of fields: air corners left out, each
+// sum divided by the weight sum where that exceeds 1e-13
+__device__ __forceinline__ double2 gather_skip(const signed char *tag, const double2 *f, const int c[4],
+                                               const double w[4]) {
+  double a = 0.0, b = 0.0, sw = 0.0;
 #pragma unroll
   for (int q = 0; q < 4; q++)
     if (!air(tag[c[q]])) {
-      v = __dadd_rn(v, __dmul_rn(w[q], field(c[q])));
+      const double2 v = f[c[q]];
+      a = __dadd_rn(a, __dmul_rn(w[q], v.x));
+      b = __dadd_rn(b, __dmul_rn(w[q], v.y));
       sw = __dadd_rn(sw, w[q]);
     }
-  if (fp64_gt(sw, 1e-13)) v = v / sw;
-  return v;
+  if (fp64_gt(sw, 1e-13)) div_sum(a, b, sw);
+  return make_double2(a, b);
 }
 
-// velocity gradients of StrainRateComponents' layout, zero at air nodes
-// (RheologyParticles.c:1751-1782)
-__device__ __forceinline__ double dudx_n(const MarkerArgs &A, int c0) {
-  const int Ncx = A.Nx - 1, k = c0 % Ncx, l = c0 / Ncx;
-  const long long c1 = k + (long long)l * A.Nx;
-  return air(A.bcp[c0]) ? 0.0 : div_by(__dsub_rn(A.u[c1 + 1 + A.Nx], A.u[c1 + A.Nx]), A.dx);
-}
-__device__ __forceinline__ double dvdz_n(const MarkerArgs &A, int c0) {
-  const int Ncx = A.Nx - 1, k = c0 % Ncx, l = c0 / Ncx;
-  const long long c2 = k + (long long)l * (A.Nx + 1);
-  return air(A.bcp[c0]) ? 0.0 : div_by(__dsub_rn(A.v[c2 + 1 + (A.Nx + 1)], A.v[c2 + 1]), A.dz);
-}
-__device__ __forceinline__ double dudz_s(const MarkerArgs &A, int c1) {
-  return (A.bcg[c1] == 30) ? 0.0 : div_by(__dsub_rn(A.u[c1 + A.Nx], A.u[c1]), A.dz);
-}
-__device__ __forceinline__ double dvdx_s(const MarkerArgs &A, int c1) {
-  const int k = c1 % A.Nx, l = c1 / A.Nx;
-  const long long c3 = k + (long long)l * (A.Nx + 1);
-  return (A.bcg[c1] == 30) ? 0.0 : div_by(__dsub_rn(A.v[c3 + 1], A.v[c3]), A.dx);
-}
-
-__device__ __forceinline__ void director(const MarkerArgs &A, long long k, double x, double z) {
-  int jp, ip, c[4];
-  double w[4];
-  if (!cell_corners(A, x, z, jp, ip, c)) { report(A, k, MDZ_EMARKER_OUT); return; }
-  weights(div_by(__dsub_rn(x, A.xvz[jp]), A.dx), div_by(__dsub_rn(z, A.zvx[ip]), A.dz), w);
-  const double mdudx = gather_skip(A.bcp, c, w, [&](int i) { return dudx_n(A, i); });
-  const double mdvdz = gather_skip(A.bcp, c, w, [&](int i) { return dvdz_n(A, i); });
-  int j = cell_of(div_by(fabs(__dsub_rn(x, A.xg[0])), A.dx)), i = cell_of(div_by(fabs(__dsub_rn(z, A.zg[0])), A.dz));
-  j = j < 0 ? 0 : (j > A.Nx - 2 ? A.Nx - 2 : j);
-  i = i < 0 ? 0 : (i > A.Nz - 2 ? A.Nz - 2 : i);
-  const int cv[4] = {j + i * A.Nx, j + i * A.Nx + 1, j + (i + 1) * A.Nx, j + (i + 1) * A.Nx + 1};
-  weights(div_by(__dsub_rn(x, A.xg[j]), A.dx), div_by(__dsub_rn(z, A.zg[i]), A.dz), w);
-  const double mdudz = gather_skip(A.bcg, cv, w, [&](int q) { return dudz_s(A, q); });
-  const double mdvdx = gather_skip(A.bcg, cv, w, [&](int q) { return dvdx_s(A, q); });
-  // :1795-1800 with the operations in the reference's order
+// :1784-1802 with the operations in the reference's order
+__device__ __forceinline__ void director(const MarkerArgs &A, long long k, const int c[4], const double wc[4],
+                                         const int cv[4], const double wv[4]) {
+  const double2 gn = gather_skip(A.bcp, A.grad_n, c, wc);   // du/dx, dv/dz
+  const double2 gs = gather_skip(A.bcg, A.grad_s, cv, wv);  // du/dz, dv/dx
+  const double mdudx = gn.x, mdvdz = gn.y, mdudz = gs.x, mdvdx = gs.y;
   const double nx = A.m_nx[k], nz = A.m_nz[k], d = __dsub_rn(mdudx, mdvdz);
   const double E = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(-d, nx), nz), __dmul_rn(__dmul_rn(mdvdx, nz), nz)),
                              __dmul_rn(__dmul_rn(mdudz, nx), nx));
@@ -140,130 +175,237 @@ __device__ __forceinline__ void director(const MarkerArgs &A, long long k, doubl
   A.m_nz[k] = nz1 / norm;
 }
 
+// P2Mastah's weight (1 - ax/dx_itp) (1 - az/dz_itp) for the distances ax = |X - x|,
+// az = |Z - z| of a marker to a vertex (ParticleRoutines.c:2320-2575)
+__device__ __forceinline__ double p2m_weight(const MarkerArgs &A, double ax, double az) {
+  return __dmul_rn(__dsub_rn(1.0, div_by(ax, A.dx_itp)), __dsub_rn(1.0, div_by(az, A.dz_itp)));
+}
+
+__device__ __forceinline__ void p2m_mark(const MarkerArgs &A, long long v, double ax, double az) {
+  if (fp64_le(ax, A.near_x) && fp64_le(az, A.near_z)) {
+    A.hit[v] = 1;
+    return;
+  }
+  const double w = p2m_weight(A, ax, az);
+  if (fp64_ge(w, 1e-30) && fp64_finite(w)) A.hit[v] = 1;
+  else if (!fp64_is_zero(w)) *A.exotic = 1;
+}
+
+// The vertices P2Mastah gives a marker a weight at: its nearest vertex (ipx, jpz) and,
+// with the 9-node stencil, the eight around it, wrapped in x when periodic
+// (:2301-2575); hx, hz are ceil((x - xg[0]) / dx + 1/2) - 1 and its z twin, unclamped
+template <class F>
+__device__ __forceinline__ void p2m_vertices(const MarkerArgs &A, double x, double z, int hx, int hz, F visit) {
+  const int ipx = clamp_to(hx, A.Nx - 1), jpz = clamp_to(hz, A.Nz - 1);
+  const double X = A.xg[ipx], Z = A.zg[jpz];
+  const double axc = fabs(__dsub_rn(X, x)), azc = fabs(__dsub_rn(Z, z));
+  visit(ipx + (long long)jpz * A.Nx, axc, azc);
+  if (A.stencil != 9) return;
+  const int Nx = A.Nx, Nz = A.Nz, per = A.periodic_x;
+  const bool peE = (ipx == Nx - 1 && per == 1), peW = (ipx == 0 && per == 1);
+  const double axE = fabs(__dsub_rn(__dadd_rn(X, A.dx.b), x)), axW = fabs(__dsub_rn(__dsub_rn(X, A.dx.b), x));
+  const double azN = fabs(__dsub_rn(__dadd_rn(Z, A.dz.b), z)), azS = fabs(__dsub_rn(__dsub_rn(Z, A.dz.b), z));
+  const int kE = peE ? 0 : ipx + 1, kW = peW ? Nx - 1 : ipx - 1;
+  const bool N = jpz < Nz - 1, S = jpz > 0, E = ipx < Nx - 1 || peE, Wst = ipx > 0 || peW;
+  if (N) visit(ipx + (long long)(jpz + 1) * Nx, axc, azN);
+  if (S) visit(ipx + (long long)(jpz - 1) * Nx, axc, azS);
+  if (E) visit(kE + (long long)jpz * Nx, axE, azc);
+  if (Wst) visit(kW + (long long)jpz * Nx, axW, azc);
+  if (S && Wst) visit(kW + (long long)(jpz - 1) * Nx, axW, azS);
+  if (N && Wst) visit(kW + (long long)(jpz + 1) * Nx, axW, azN);
+  if (N && E) visit(kE + (long long)(jpz + 1) * Nx, axE, azN);
+  if (S && E) visit(kE + (long long)(jpz - 1) * Nx, axE, azS);
+}
+
+// The rotation of :1972-1989 by the marker spin, which UpdateParticleStress leaves at
+// zero, with the arithmetic as written.  For stresses that are nonzero and below 2^500
+// in magnitude and a finite dt below 2^500, every product with the zero spin is a
+// signed zero and every sum returns its nonzero term (Jaumann, rotation 1); with
+// cos(0) = 1 and sin(+-0) = +-0 the same holds for finite nonzero stresses (rotation 2):
+// the rotation is then the identity, and the caller skips this function.
+__device__ __noinline__ void rotate(int rotation, double dt, double &txx, double &tzz, double &txz) {
+  const double wm = 0.0;
+  if (rotation == 1) {
+    const double a = __dsub_rn(txx, __dmul_rn(__dmul_rn(__dmul_rn(dt, 2.0), txz), wm));
+    const double b = __dsub_rn(tzz, __dmul_rn(__dmul_rn(__dmul_rn(-dt, 2.0), txz), wm));
+    const double r = __dsub_rn(txz, __dmul_rn(__dmul_rn(dt, __dsub_rn(tzz, txx)), wm));
+    txx = a; tzz = b; txz = r;
+  } else {
+    const double ang = __dmul_rn(dt, wm);
+    double cs, sn;
+    if (fp64_is_zero(ang)) { cs = 1.0; sn = ang; }
+    else { cs = cos(ang); sn = sin(ang); }
+    const double a = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(txx, cs), __dmul_rn(txz, sn)), cs),
+                               __dmul_rn(__dadd_rn(__dmul_rn(txz, cs), __dmul_rn(tzz, sn)), sn));
+    const double b = __dadd_rn(__dmul_rn(-__dadd_rn(__dmul_rn(-txx, sn), __dmul_rn(txz, cs)), sn),
+                               __dmul_rn(__dadd_rn(__dmul_rn(-txz, sn), __dmul_rn(tzz, cs)), cs));
+    const double r = __dadd_rn(__dmul_rn(-__dadd_rn(__dmul_rn(txx, cs), __dmul_rn(txz, sn)), sn),
+                               __dmul_rn(__dadd_rn(__dmul_rn(txz, cs), __dmul_rn(tzz, sn)), cs));
+    txx = a; tzz = b; txz = r;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_marker_grid(const MarkerArgs A) {
+  const long long Nc = (long long)(A.Nx - 1) * (A.Nz - 1), Nv = (long long)A.Nx * A.Nz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0 && A.elastic == 1) *A.exotic = 0;
+  if (t < Nc) {
+    const long long c0 = t;
+    const bool a = air(A.bcp[c0]);
+    if (A.elastic == 1)
+      A.inc_n[c0] = a ? make_double2(0.0, 0.0)
+                      : make_double2(__dsub_rn(A.sxxd[c0], A.sxxd0[c0]), __dsub_rn(A.szzd[c0], A.szzd0[c0]));
+    if (A.director) {
+      // RheologyParticles.c:1751-1766 in the layout of the velocity arrays
+      const int Ncx = A.Nx - 1, k = (int)(c0 % Ncx), l = (int)(c0 / Ncx);
+      const long long c1 = k + (long long)l * A.Nx, c2 = k + (long long)l * (A.Nx + 1);
+      A.grad_n[c0] = a ? make_double2(0.0, 0.0)
+                       : make_double2(div_by(__dsub_rn(A.u[c1 + 1 + A.Nx], A.u[c1 + A.Nx]), A.dx),
+                                      div_by(__dsub_rn(A.v[c2 + 1 + (A.Nx + 1)], A.v[c2 + 1]), A.dz));
+    }
+  } else if (t < Nc + Nv) {
+    const long long c1 = t - Nc;
+    const bool wall = A.bcg[c1] == 30;
+    if (A.elastic == 1) {
+      A.inc_s[c1] = wall ? 0.0 : __dsub_rn(A.sxz[c1], A.sxz0[c1]);
+      A.hit[c1] = 0;
+      A.WM[c1] = 0.0;
+    }
+    if (A.director) {
+      // :1768-1782
+      const int k = (int)(c1 % A.Nx), l = (int)(c1 / A.Nx);
+      const long long c3 = k + (long long)l * (A.Nx + 1);
+      A.grad_s[c1] = wall ? make_double2(0.0, 0.0)
+                          : make_double2(div_by(__dsub_rn(A.u[c1 + A.Nx], A.u[c1]), A.dz),
+                                         div_by(__dsub_rn(A.v[c3 + 1], A.v[c3]), A.dx));
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) k_marker_update(const MarkerArgs A) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= A.n) return;
-  const bool active = A.phase[k] != -1;
-  const double x = A.x[k], z = A.z[k];
-  if (active && A.director) director(A, k, x, z);
-  if (A.elastic != 1) return;
-  double dsx = 0.0, dsz = 0.0, dsxz = 0.0;
-  if (active) {
-    int jp, ip, c[4];
-    double w[4];
-    if (!cell_corners(A, x, z, jp, ip, c)) {
-      report(A, k, MDZ_EMARKER_OUT);
-    } else {
-      weights(div_by(__dsub_rn(x, A.xvz[jp]), A.dx), div_by(__dsub_rn(z, A.zvx[ip]), A.dz), w);
-      const int alt[4] = {c[2], c[3], c[0], c[1]};
-      double sw = 0.0;
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        // an air corner lends its weight to the corner across; dsxxd, dszzd are 0 at air
-        const int cc = air(A.bcp[c[q]]) ? alt[q] : c[q];
-        const bool solid = !air(A.bcp[cc]);
-        const double fx = solid ? __dsub_rn(A.sxxd[cc], A.sxxd0[cc]) : 0.0;
-        const double fz = solid ? __dsub_rn(A.szzd[cc], A.szzd0[cc]) : 0.0;
-        dsx = __dadd_rn(dsx, __dmul_rn(w[q], fx));
-        dsz = __dadd_rn(dsz, __dmul_rn(w[q], fz));
-        sw = __dadd_rn(sw, w[q]);
-      }
-      if (fp64_gt(sw, 1e-13)) { dsx = dsx / sw; dsz = dsz / sw; }
-      if (fp64_is_inf(dsx) || fp64_is_inf(dsz)) report(A, k, MDZ_ENONFINITE);  // ParticleRoutines.c:1565-1569
+  if (A.phase[k] == -1) {
+    // ArrayPlusArray adds the (zero) increment of an inactive marker too (:1954-1956)
+    if (A.elastic == 1) {
+      A.m_sxxd[k] = __dadd_rn(A.m_sxxd[k], 0.0);
+      A.m_szzd[k] = __dadd_rn(A.m_szzd[k], 0.0);
+      A.m_sxz[k] = __dadd_rn(A.m_sxz[k], 0.0);
     }
-    // Interp_Grid2P: vertex cell clamped to the grid; beyond it in x the reference exits (89)
-    int j = cell_of(div_by(__dsub_rn(x, A.xg[0]), A.dx));
-    if (j < 0) j = 0;
-    if (j > A.Nx - 2) { j = A.Nx - 2; report(A, k, MDZ_EMARKER_OUT); }
-    int i = cell_of(div_by(__dsub_rn(z, A.zg[0]), A.dz));
-    i = i < 0 ? 0 : (i > A.Nz - 2 ? A.Nz - 2 : i);
-    const int cv[4] = {j + i * A.Nx, j + i * A.Nx + 1, j + (i + 1) * A.Nx, j + (i + 1) * A.Nx + 1};
+    return;
+  }
+  const double x = A.x[k], z = A.z[k];
+  // centroid frame
+  int jp, ip, c[4];
+  double wc[4];
+  const bool inside = cell_corners(A, x, z, jp, ip, c);
+  if (inside) weights(div_by(__dsub_rn(x, A.xvz[jp]), A.dx), div_by(__dsub_rn(z, A.zvx[ip]), A.dz), wc);
+  else report(A, k, MDZ_EMARKER_OUT);
+  // vertex frame of Interp_Grid2P: cell clamped to the grid; beyond it in x the reference exits (89)
+  const double tx = __dsub_rn(x, A.xg[0]), tz = __dsub_rn(z, A.zg[0]);
+  const CellPair px = cell_pair(tx, A.dx), pz = cell_pair(tz, A.dz);
+  const bool beyond = px.c > A.Nx - 2;
+  const int j = clamp_to(px.c, A.Nx - 2), i = clamp_to(pz.c, A.Nz - 2);
+  const double ex = __dsub_rn(x, A.xg[j]), ez = __dsub_rn(z, A.zg[i]);
+  double wv[4];
+  weights(div_by(fabs(ex), A.dx), div_by(fabs(ez), A.dz), wv);
+  const int cv[4] = {j + i * A.Nx, j + i * A.Nx + 1, j + (i + 1) * A.Nx, j + (i + 1) * A.Nx + 1};
+
+  if (A.director && inside) {
+    // Vertices2Particle takes the cell of |x - xg[0]| and the weights of x - xg[j]: the
+    // bits above whenever those differences carry no sign
+    int jd = j, id = i;
+    double wd[4] = {wv[0], wv[1], wv[2], wv[3]};
+    if (!(sign_clear(tx) && sign_clear(tz) && sign_clear(ex) && sign_clear(ez))) {
+      jd = clamp_to(cell_of(div_by(fabs(tx), A.dx)), A.Nx - 2);
+      id = clamp_to(cell_of(div_by(fabs(tz), A.dz)), A.Nz - 2);
+      weights(div_by(__dsub_rn(x, A.xg[jd]), A.dx), div_by(__dsub_rn(z, A.zg[id]), A.dz), wd);
+    }
+    const int cd[4] = {jd + id * A.Nx, jd + id * A.Nx + 1, jd + (id + 1) * A.Nx, jd + (id + 1) * A.Nx + 1};
+    director(A, k, c, wc, cd, wd);
+  }
+  if (A.elastic != 1) return;
+
+  double dsx = 0.0, dsz = 0.0, dsxz = 0.0;
+  if (inside) {
+    const int alt[4] = {c[2], c[3], c[0], c[1]};
+    double sw = 0.0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      // an air corner lends its weight to the corner across; the increments are 0 at air
+      const int cc = air(A.bcp[c[q]]) ? alt[q] : c[q];
+      const double2 f = A.inc_n[cc];
+      dsx = __dadd_rn(dsx, __dmul_rn(wc[q], f.x));
+      dsz = __dadd_rn(dsz, __dmul_rn(wc[q], f.y));
+      sw = __dadd_rn(sw, wc[q]);
+    }
+    if (fp64_gt(sw, 1e-13)) div_sum(dsx, dsz, sw);
+    if (fp64_is_inf(dsx) || fp64_is_inf(dsz)) report(A, k, MDZ_ENONFINITE);  // ParticleRoutines.c:1565-1569
+  }
+  if (beyond) report(A, k, MDZ_EMARKER_OUT);
+  {
     const int alt[4] = {cv[2], cv[3], cv[0], cv[1]};
-    weights(div_by(fabs(__dsub_rn(x, A.xg[j])), A.dx), div_by(fabs(__dsub_rn(z, A.zg[i])), A.dz), w);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       const int cc = air(A.bcg[cv[q]]) ? alt[q] : cv[q];
-      const double d = (A.bcg[cc] != 30) ? __dsub_rn(A.sxz[cc], A.sxz0[cc]) : 0.0;
-      dsxz = __dadd_rn(dsxz, __dmul_rn(w[q], d));
+      dsxz = __dadd_rn(dsxz, __dmul_rn(wv[q], A.inc_s[cc]));
     }
   }
-  // ArrayPlusArray on every marker (:1954-1956)
+  // ArrayPlusArray (:1954-1956)
   double txx = __dadd_rn(A.m_sxxd[k], dsx), tzz = __dadd_rn(A.m_szzd[k], dsz), txz = __dadd_rn(A.m_sxz[k], dsxz);
-  if (active) {
-    // rotation by the zeroed marker spin (:1972-1989), arithmetic as written
-    const double wm = 0.0;
-    if (A.rotation == 1) {
-      const double a = __dsub_rn(txx, __dmul_rn(__dmul_rn(__dmul_rn(A.dt, 2.0), txz), wm));
-      const double b = __dsub_rn(tzz, __dmul_rn(__dmul_rn(__dmul_rn(-A.dt, 2.0), txz), wm));
-      const double c = __dsub_rn(txz, __dmul_rn(__dmul_rn(A.dt, __dsub_rn(tzz, txx)), wm));
-      txx = a; tzz = b; txz = c;
-    } else if (A.rotation == 2) {
-      const double ang = __dmul_rn(A.dt, wm);
-      const double cs = cos(ang), sn = sin(ang);
-      const double a = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(txx, cs), __dmul_rn(txz, sn)), cs),
-                                 __dmul_rn(__dadd_rn(__dmul_rn(txz, cs), __dmul_rn(tzz, sn)), sn));
-      const double b = __dadd_rn(__dmul_rn(-__dadd_rn(__dmul_rn(-txx, sn), __dmul_rn(txz, cs)), sn),
-                                 __dmul_rn(__dadd_rn(__dmul_rn(-txz, sn), __dmul_rn(tzz, cs)), cs));
-      const double c = __dadd_rn(__dmul_rn(-__dadd_rn(__dmul_rn(txx, cs), __dmul_rn(txz, sn)), sn),
-                                 __dmul_rn(__dadd_rn(__dmul_rn(txz, cs), __dmul_rn(tzz, sn)), cs));
-      txx = a; tzz = b; txz = c;
-    }
-    // P2Mastah weights of this marker at its nearest vertex and, with the 9-node
-    // stencil, the eight around it (ParticleRoutines.c:2288-2575)
-    int ipx = cell_of(__dadd_rn(div_by(__dsub_rn(x, A.xg[0]), A.dx), 0.5));
-    int jpz = cell_of(__dadd_rn(div_by(__dsub_rn(z, A.zg[0]), A.dz), 0.5));
-    ipx = ipx < 0 ? 0 : (ipx > A.Nx - 1 ? A.Nx - 1 : ipx);
-    jpz = jpz < 0 ? 0 : (jpz > A.Nz - 1 ? A.Nz - 1 : jpz);
-    const double X = A.xg[ipx], Z = A.zg[jpz];
-    auto w_at = [&](double xn, double zn) {
-      return __dmul_rn(__dsub_rn(1.0, div_by(fabs(__dsub_rn(xn, x)), A.dx_itp)),
-                       __dsub_rn(1.0, div_by(fabs(__dsub_rn(zn, z)), A.dz_itp)));
-    };
-    atomicAdd(&A.WM[ipx + (long long)jpz * A.Nx], w_at(X, Z));
-    if (A.stencil == 9) {
-      const int Nx = A.Nx, Nz = A.Nz, per = A.periodic_x;
-      const bool peE = (ipx == Nx - 1 && per == 1), peW = (ipx == 0 && per == 1);
-      const double xE = __dadd_rn(X, A.dx.b), xW = __dsub_rn(X, A.dx.b);
-      const double zN = __dadd_rn(Z, A.dz.b), zS = __dsub_rn(Z, A.dz.b);
-      const int kE = peE ? 0 : ipx + 1, kW = peW ? Nx - 1 : ipx - 1;
-      const bool N = jpz < Nz - 1, S = jpz > 0, E = ipx < Nx - 1 || peE, Wst = ipx > 0 || peW;
-      if (N) atomicAdd(&A.WM[ipx + (long long)(jpz + 1) * Nx], w_at(X, zN));
-      if (S) atomicAdd(&A.WM[ipx + (long long)(jpz - 1) * Nx], w_at(X, zS));
-      if (E) atomicAdd(&A.WM[kE + (long long)jpz * Nx], w_at(xE, Z));
-      if (Wst) atomicAdd(&A.WM[kW + (long long)jpz * Nx], w_at(xW, Z));
-      if (S && Wst) atomicAdd(&A.WM[kW + (long long)(jpz - 1) * Nx], w_at(xW, zS));
-      if (N && Wst) atomicAdd(&A.WM[kW + (long long)(jpz + 1) * Nx], w_at(xW, zN));
-      if (N && E) atomicAdd(&A.WM[kE + (long long)(jpz + 1) * Nx], w_at(xE, zN));
-      if (S && E) atomicAdd(&A.WM[kE + (long long)(jpz - 1) * Nx], w_at(xE, zS));
-    }
+  // rotation by the zeroed marker spin (:1972-1989)
+  if (A.rotation == 1 || A.rotation == 2) {
+    const unsigned exx = fp64_exponent(txx), ezz = fp64_exponent(tzz), exz = fp64_exponent(txz);
+    const bool plain = exx - 1u < 1522u && ezz - 1u < 1522u && exz - 1u < 1522u;
+    const bool identity = plain && (A.rotation == 1 ? fp64_exponent(A.dt) < 1523u : fp64_is_zero(__dmul_rn(A.dt, 0.0)));
+    if (!identity) rotate(A.rotation, A.dt, txx, tzz, txz);
   }
   A.m_sxxd[k] = txx;
   A.m_szzd[k] = tzz;
   A.m_sxz[k] = txz;
+  p2m_vertices(A, x, z, px.h, pz.h, [&](long long v, double ax, double az) { p2m_mark(A, v, ax, az); });
+}
+
+// The exact P2Mastah weight sums, only after a weight below 1e-30 that is not zero (or
+// one that is not finite) was seen; otherwise every CTA reads the flag and returns
+__global__ void __launch_bounds__(256) k_marker_weights(const MarkerArgs A) {
+  if (*A.exotic == 0) return;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < A.n;
+       k += (long long)gridDim.x * blockDim.x) {
+    if (A.phase[k] == -1) continue;
+    const double x = A.x[k], z = A.z[k];
+    const int hx = cell_pair(__dsub_rn(x, A.xg[0]), A.dx).h, hz = cell_pair(__dsub_rn(z, A.zg[0]), A.dz).h;
+    p2m_vertices(A, x, z, hx, hz,
+                 [&](long long v, double ax, double az) { atomicAdd(&A.WM[v], p2m_weight(A, ax, az)); });
+  }
 }
 
 // the value P2Mastah leaves at vertex c1 (:2603-2631)
-__device__ __forceinline__ double wxz_after(const MarkerArgs &A, long long c1) {
-  const double W = A.WM[c1];
-  if (fp64_abs_lt(W, 1e-30) || air(A.bcg[c1])) return A.wxz[c1];
-  return 0.0 / W;
+__device__ __forceinline__ double wxz_after(const MarkerArgs &A, long long c1, bool exact) {
+  if (air(A.bcg[c1])) return A.wxz[c1];
+  if (exact) {
+    const double W = A.WM[c1];
+    return fp64_abs_lt(W, 1e-30) ? A.wxz[c1] : 0.0 / W;
+  }
+  return A.hit[c1] ? 0.0 : A.wxz[c1];
 }
 
 __global__ void __launch_bounds__(256) k_marker_wxz(const MarkerArgs A) {
   const long long c1 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c1 >= (long long)A.Nx * A.Nz) return;
+  const bool exact = *A.exotic != 0;
   const int k = (int)(c1 % A.Nx);
   if (A.periodic_x == 1) {
     if (k == A.Nx - 1) return;  // written by the row's first vertex
     if (k == 0) {
       // :2633-2641: both ends of the row take the mean of the two
-      const double av = 0.5 * (wxz_after(A, c1 + A.Nx - 1) + wxz_after(A, c1));
+      const double av = 0.5 * (wxz_after(A, c1 + A.Nx - 1, exact) + wxz_after(A, c1, exact));
       A.wxz[c1] = av;
       A.wxz[c1 + A.Nx - 1] = av;
       return;
     }
   }
-  A.wxz[c1] = wxz_after(A, c1);
+  A.wxz[c1] = wxz_after(A, c1, exact);
 }
 
 unsigned blocks_for(long long n) {
@@ -273,8 +415,20 @@ unsigned blocks_for(long long n) {
 
 }  // namespace
 
+cudaError_t launch_marker_grid(const MarkerArgs &a, cudaStream_t s) {
+  k_marker_grid<<<blocks_for((long long)(a.Nx - 1) * (a.Nz - 1) + (long long)a.Nx * a.Nz), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_marker_update(const MarkerArgs &a, cudaStream_t s) {
   if (a.n > 0) k_marker_update<<<blocks_for(a.n), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_marker_weights(const MarkerArgs &a, cudaStream_t s) {
+  // four CTAs per SM at most: in the common case each reads one flag and returns
+  const unsigned g = blocks_for(a.n), cap = 152u * 4u;
+  if (a.n > 0) k_marker_weights<<<g < cap ? g : cap, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -239,7 +239,7 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
        S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
-       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_COUNT = S_MK + 22 };
+       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_COUNT = S_MK + 28 };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -1292,20 +1292,41 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
     A.m_nz = (double *)mi.in((const double *)mk->nz, S_MK + 7, n, host);
   }
   if (mi.err) return mi.err;
-  if (el) {
-    if (ensure(ctx->bufs[S_MK + 21], Nv * sizeof(double)) != MDZ_OK) return MDZ_ENOMEM;
-    A.WM = (double *)ctx->bufs[S_MK + 21].p;
+  // scratch: per-node increments and gradients, P2Mastah flags and exact sums
+  const size_t scratch[6] = {el ? Nv * sizeof(double) : 0, el ? Nc * sizeof(double2) : 0, el ? Nv * sizeof(double) : 0,
+                             dir ? Nc * sizeof(double2) : 0, dir ? Nv * sizeof(double2) : 0,
+                             el ? Nv + sizeof(int) : 0};
+  void *sp[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int b = 0; b < 6; b++) {
+    if (!scratch[b]) continue;
+    if (ensure(ctx->bufs[S_MK + 21 + b], scratch[b]) != MDZ_OK) return MDZ_ENOMEM;
+    sp[b] = ctx->bufs[S_MK + 21 + b].p;
   }
+  A.WM = (double *)sp[0];
+  A.inc_n = (double2 *)sp[1];
+  A.inc_s = (double *)sp[2];
+  A.grad_n = (double2 *)sp[3];
+  A.grad_s = (double2 *)sp[4];
+  A.exotic = (int *)sp[5];
+  A.hit = sp[5] ? (unsigned char *)sp[5] + sizeof(int) : nullptr;
+  // A marker at most L (1 - 2^-40) from a vertex, L the weight length, has 1 - d/L >=
+  // 2^-41 on that axis once rounded, so a P2Mastah weight >= 2^-82 > 1e-30
+  const auto near = [](double L) { return (L >= 0x1p-900 && L <= 0x1p900) ? L - L * 0x1p-40 : -1.0; };
+  A.near_x = near(A.dx_itp.b);
+  A.near_z = near(A.dz_itp.b);
   A.stats = ctx->d_stats;
   int rc;
   if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
-  if (el) CK(cudaMemsetAsync(A.WM, 0, Nv * sizeof(double), ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  CK(launch_marker_update(A, ctx->stream));
-  ctx->launches = 1;
-  if (el) {
-    CK(launch_marker_wxz(A, ctx->stream));
+  if (el || dir) {
+    CK(launch_marker_grid(A, ctx->stream));
+    CK(launch_marker_update(A, ctx->stream));
     ctx->launches = 2;
+  }
+  if (el) {
+    CK(launch_marker_weights(A, ctx->stream));
+    CK(launch_marker_wxz(A, ctx->stream));
+    ctx->launches = 4;
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if (el) {

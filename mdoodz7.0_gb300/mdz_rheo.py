@@ -388,6 +388,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_measure_fp64_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     lib.mdz_rheo_math_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64] + [C.c_void_p] * 4
     lib.mdz_rheo_div_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
+    lib.mdz_rheo_ceil_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_points_static.argtypes = [C.POINTER(Model), C.POINTER(Materials), C.POINTER(PointInputs),
                                            C.POINTER(PointOutputs), C.c_int64, C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(SweepStats)]
@@ -477,6 +478,16 @@ def div_selftest(a: np.ndarray, b: float, device: int = 0):
     rc = load_library().mdz_rheo_div_selftest(device, a.ctypes.data, a.size, b, fast.ctypes.data, plain.ctypes.data)
     if rc != MDZ_OK:
         raise RheoError(rc, "mdz_rheo_div_selftest")
+    return fast, plain
+
+
+def ceil_selftest(q: np.ndarray, device: int = 0):
+    """(integer-pipe ceil as int32, CUDA's ceil) of the float64 array q on the GPU."""
+    q = np.ascontiguousarray(q, np.float64)
+    fast, plain = np.empty(q.size, np.int32), np.empty_like(q)
+    rc = load_library().mdz_rheo_ceil_selftest(device, q.ctypes.data, q.size, fast.ctypes.data, plain.ctypes.data)
+    if rc != MDZ_OK:
+        raise RheoError(rc, "mdz_rheo_ceil_selftest")
     return fast, plain
 
 

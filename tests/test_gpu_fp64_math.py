@@ -84,3 +84,25 @@ def test_known_divisor_division_is_exact(b):
     assert np.array_equal(fast.view(np.uint64)[~np.isnan(a)], plain.view(np.uint64)[~np.isnan(a)])
     assert np.array_equal(fast.view(np.uint64)[~np.isnan(a)], host.view(np.uint64)[~np.isnan(a)])
     assert np.isnan(fast[np.isnan(a)]).all()
+
+
+def test_integer_pipe_ceil_matches_cuda():
+    """The cell-index ceil read from the bits of a double (csrc/fp64_bits.cuh) against
+    CUDA's ceil: equal on every argument below 2^30 in magnitude -- integers, their
+    neighbours one ulp away, halves, signed zeros, subnormals, random values of every
+    scale -- and saturated to +-2^30 beyond (NaN to +2^30)."""
+    rng = np.random.default_rng(5)
+    ints = np.arange(-5000.0, 5000.0)
+    q = np.concatenate([ints, np.nextafter(ints, np.inf), np.nextafter(ints, -np.inf), ints + 0.5,
+                        rng.uniform(-3e4, 3e4, 1_000_000),
+                        rng.standard_normal(200_000) * 10.0 ** rng.uniform(-320, 12, 200_000),
+                        [0.0, -0.0, 5e-324, -5e-324, 0.9999999999999999, -0.9999999999999999,
+                         2.0 ** 30 - 0.5, -(2.0 ** 30) + 0.5, 2.0 ** 30, -(2.0 ** 30), 2.0 ** 52 + 1.0,
+                         1e300, -1e300, np.inf, -np.inf, np.nan]])
+    fast, plain = R.ceil_selftest(q)
+    small = np.abs(q) < 2.0 ** 30
+    assert np.array_equal(fast[small].astype(np.float64), plain[small])
+    assert np.array_equal(plain[small], np.ceil(q[small]))
+    big = ~small & ~np.isnan(q)
+    assert np.array_equal(fast[big], np.where(q[big] < 0, -(2 ** 30), 2 ** 30))
+    assert (fast[np.isnan(q)] == 2 ** 30).all()

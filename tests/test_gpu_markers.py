@@ -12,7 +12,7 @@ import mdz_workloads as W
 import oracle_lib as O
 from golden import cases
 from golden.make_golden import load_marker_inputs, marker_opts
-from test_markers_oracle import boundary_workload
+from test_markers_oracle import boundary_workload, tiny_weight_workload
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -52,7 +52,7 @@ def test_gpu_marker_stress_matches_golden(ctx, name):
     model, grid, mk, dx, dz = load_marker_inputs(g)
     opts = marker_opts(*cases.MARKER_CASES[name][1:])
     rc, st = ctx.marker_stress(model, opts, grid, mk, dx, dz)
-    assert rc == R.MDZ_OK and st.kernel_launches == (2 if opts.elastic == 1 else 1)
+    assert rc == R.MDZ_OK and st.kernel_launches == (4 if opts.elastic == 1 else 2)
     check(mk, grid["wxz"], {k: g["out_" + k] for k in ("sxxd", "szzd", "sxz", "nx", "nz")}, g["out_wxz"])
 
 
@@ -78,6 +78,20 @@ def test_gpu_markers_on_cell_boundaries(ctx):
     g, m = copies(w)
     ctx.marker_stress(w.model, opts, g, m, w.info["dx"], w.info["dz"])
     check(m, g["wxz"], m_ref, g_ref["wxz"])
+
+
+@pytest.mark.parametrize("stencil", [1, 9])
+def test_gpu_tiny_weights_take_the_exact_sums(ctx, stencil):
+    """P2Mastah weights below 1e-30 that are not zero: the exact per-vertex sums, as the
+    reference forms them, decide which vertices keep wxz."""
+    w = tiny_weight_workload()
+    opts = marker_opts(1, 1, 0, 1, stencil)
+    g_ref, m_ref = copies(w)
+    assert O.orc_marker_stress(w.model, opts, g_ref, m_ref, w.info["dx"], w.info["dz"]) == R.MDZ_OK
+    g, m = copies(w)
+    ctx.marker_stress(w.model, opts, g, m, w.info["dx"], w.info["dz"])
+    check(m, g["wxz"], m_ref, g_ref["wxz"])
+    assert np.sum(g_ref["wxz"] == w.arrays["wxz"]) > 0
 
 
 def test_gpu_marker_stress_status_and_async(ctx):

@@ -48,6 +48,27 @@ def boundary_workload():
     return w
 
 
+def tiny_weight_workload():
+    """Markers at the edge of their nearest vertex's support in both axes: P2Mastah
+    weights of magnitude 1e-31 to 1e-29, negative (one ulp past the edge once rounded)
+    or positive, below the 1e-30 threshold but not zero, at vertices few other active
+    markers reach -- the exact weight sums decide wxz there."""
+    w = W.marker_workload(seed=71, ncx=24, ncz=18, markers_per_cell=2, air=0.2)
+    mk = w.info["markers"]
+    xg, zg, dx, dz = w.arrays["xg_coord"], w.arrays["zg_coord"], w.info["dx"], w.info["dz"]
+    rng = np.random.default_rng(2)
+    mk["phase"][rng.random(mk["phase"].size) < 0.9] = -1
+    n = 40
+    jx, iz = rng.integers(1, xg.size - 2, n), rng.integers(1, zg.size - 2, n)
+    hx, hz = dx / 2, dz / 2
+    mk["x"][:n] = np.nextafter(xg[jx] + hx, xg[jx])
+    mk["z"][:n] = np.nextafter(zg[iz] + hz, zg[iz])
+    mk["x"][n // 2:n] = xg[jx[n // 2:]] + hx * (1 - 2.0 ** -51)
+    mk["z"][n // 2:n] = zg[iz[n // 2:]] + hz * (1 - 2.0 ** -51)
+    mk["phase"][:n] = 0
+    return w
+
+
 CASES = {
     # name: (builder, elastic, stress_rotation, anisotropy, advection, interp_stencil)
     "jaumann": (lambda: W.marker_workload(seed=1, ncx=31, ncz=24), 1, 1, 0, 1, 1),
@@ -61,6 +82,7 @@ CASES = {
                             1, 2, 1, 1, 1),
     "one_column_of_cells": (lambda: W.marker_workload(seed=8, ncx=1, ncz=9, markers_per_cell=6), 1, 1, 1, 1, 1),
     "markers_on_boundaries": (boundary_workload, 1, 1, 1, 1, 9),
+    "tiny_weights": (tiny_weight_workload, 1, 1, 0, 1, 1),
 }
 
 
