@@ -242,6 +242,10 @@ int mdz_rheo_destroy(mdz_rheo_ctx *ctx);
 int mdz_rheo_set_stream(mdz_rheo_ctx *ctx, void *stream);
 /* Wait for an MDZ_SWEEP_ASYNC sweep and fetch its statistics. */
 int mdz_rheo_sync(mdz_rheo_ctx *ctx, mdz_sweep_stats *stats);
+/* Sweeps of host arrays (MDZ_MEM_HOST) run in bands of grid rows, so that the copies of
+ * one band overlap the kernels of the others (with page-locked host arrays).  bands = 0
+ * picks rows / 128, at most 16; 1 to 16 fixes the count.  Results do not depend on it. */
+int mdz_rheo_set_host_bands(mdz_rheo_ctx *ctx, int bands);
 
 /* ---- the hot path --------------------------------------------------- */
 /* NonNewtonianViscosityGrid: vertex interpolation of T, p_in, d0, phi0, then

@@ -42,6 +42,10 @@ struct mdz_rheo_ctx {
   unsigned long long h2d = 0, d2h = 0;
   unsigned launches = 0;
   int block[2] = {128, 128}, grid_cap[2] = {0, 0};  // launch shape of k_sweep, [iso, aniso]
+  // host-memory sweeps in row bands: copies in, kernels and copies out overlap
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, compute2 = nullptr;
+  cudaEvent_t band_ev[2 * 16 + 3] = {};
+  int bands = 0;  // 0: automatic (rows / 128, at most 16); else this many
   int sms = 0;
   // learned warm start
   void *warm_buf = nullptr;  // tiles W1, W2, W3 + biases b1, b2, b3[16]
@@ -310,6 +314,131 @@ int field_lists(const mdz_model *md, const mdz_grid_fields *f, bool aniso, Field
   return MDZ_OK;
 }
 
+constexpr int kMaxBands = 16;
+
+int host_bands(const mdz_rheo_ctx *ctx, int Nz) {
+  int b = ctx->bands > 0 ? ctx->bands : Nz / 128;
+  if (b > kMaxBands) b = kMaxBands;
+  if (b > Nz) b = Nz;
+  return b < 1 ? 1 : b;
+}
+
+// Row boundaries of B bands over Nz vertex rows: band sizes in the ratio
+// min(2^b, 2^(B-1-b), 8), so the first band's upload (before any kernel) and the last
+// band's download (after every kernel) are short, and each band's upload stays shorter
+// than the kernel before it while the bands grow; at least one row per band.
+void band_rows(int Nz, int B, int *a) {
+  double cum[kMaxBands + 1];
+  cum[0] = 0.0;
+  for (int b = 0; b < B; b++) {
+    const int up = b < 3 ? b : 3, down = (B - 1 - b) < 3 ? (B - 1 - b) : 3;
+    cum[b + 1] = cum[b] + (double)(1 << (up < down ? up : down));
+  }
+  a[0] = 0;
+  for (int b = 1; b < B; b++) {
+    long long r = llround(cum[b] / cum[B] * Nz);
+    if (r < a[b - 1] + 1) r = a[b - 1] + 1;
+    if (r > Nz - (B - b)) r = Nz - (B - b);
+    a[b] = (int)r;
+  }
+  a[B] = Nz;
+}
+
+// A sweep of host arrays in B bands of vertex rows [a_b, a_{b+1}) with the centroid rows
+// of the same indices.  Band b's inputs go up on copy_in; its kernel waits for them, on
+// the context stream for even b and on a second stream for odd b (a band's kernel fills
+// the SMs its predecessor's tail leaves idle); its outputs come back on copy_out once the
+// kernel is done.  The copies of one band thus overlap the kernels of the others.  A
+// vertex row l reads the centroid rows l - 1 and l, which bands up to b have uploaded by
+// then (copy_in runs in order), and every node writes only its own outputs.
+int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &L, const mdz_grid_fields *f,
+                 int B) {
+  const int Nx = A.M.Nx, Nz = A.M.Nz, Ncx = A.M.Ncx, Ncz = A.M.Ncz, np = A.M.np;
+  const size_t Nc = (size_t)A.M.Nc, Nv = (size_t)A.M.Nv;
+  if (!ctx->copy_in) {
+    CK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->compute2, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : ctx->band_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  int rows[kMaxBands + 1];
+  band_rows(Nz, B, rows);
+  // device arrays, full size, in the same slots as the one-shot path
+  auto slot = [&](int s, size_t bytes) -> void * {
+    return ensure(ctx->bufs[s], bytes) == MDZ_OK ? ctx->bufs[s].p : nullptr;
+  };
+  bool ok = true;
+  for (int i = 0; i < L.nci; i++) ok = ok && (A.ci[i] = (const double *)slot(S_CI + i, Nc * 8));
+  for (int i = 0; i < L.nvi; i++) ok = ok && (A.vi[i] = (const double *)slot(S_VI + i, Nv * 8));
+  for (int p = 0; p < np; p++) {
+    ok = ok && (A.perc_n[p] = (const double *)slot(S_PN + p, Nc * 8)) && (A.perc_s[p] = (const double *)slot(S_PS + p, Nv * 8));
+    ok = ok && (A.peta_n[p] = (double *)slot(S_EN + p, Nc * 8)) && (A.peta_s[p] = (double *)slot(S_ES + p, Nv * 8));
+  }
+  ok = ok && (A.bcp = (const signed char *)slot(S_BCP, Nc)) && (A.bcg = (const signed char *)slot(S_BCG, Nv));
+  for (int i = 0; i < CO_COUNT; i++) A.co[i] = L.cout[i] ? (double *)slot(S_CO + i, Nc * 8) : nullptr;
+  for (int i = 0; i < VO_COUNT; i++) A.vo[i] = L.vout[i] ? (double *)slot(S_VO + i, Nv * 8) : nullptr;
+  for (int i = 0; i < CO_COUNT; i++) ok = ok && (!L.cout[i] || A.co[i]);
+  for (int i = 0; i < VO_COUNT; i++) ok = ok && (!L.vout[i] || A.vo[i]);
+  if (!ok) return MDZ_ENOMEM;
+  // [0] start, [1 + b] band b uploaded, [1 + B + b] band b swept, [1 + 2B] downloads
+  // done, [2 + 2B] kernels of the second stream done
+  cudaEvent_t *ev = ctx->band_ev;
+  auto up = [&](const void *dst, const void *src, size_t off, size_t n, size_t es) -> cudaError_t {
+    if (!src || !n) return cudaSuccess;
+    ctx->h2d += n * es;
+    return cudaMemcpyAsync((char *)dst + off * es, (const char *)src + off * es, n * es, cudaMemcpyHostToDevice,
+                           ctx->copy_in);
+  };
+  auto down = [&](void *dst, const void *src, size_t off, size_t n, size_t es) -> cudaError_t {
+    if (!dst || !n) return cudaSuccess;
+    ctx->d2h += n * es;
+    return cudaMemcpyAsync((char *)dst + off * es, (const char *)src + off * es, n * es, cudaMemcpyDeviceToHost,
+                           ctx->copy_out);
+  };
+  CK(cudaEventRecord(ev[0], ctx->stream));  // earlier work on these buffers comes first
+  CK(cudaStreamWaitEvent(ctx->copy_in, ev[0], 0));
+  CK(cudaStreamWaitEvent(ctx->copy_out, ev[0], 0));
+  for (int b = 0; b < B; b++) {
+    const int vr0 = rows[b], vr1 = rows[b + 1];
+    const int cr0 = vr0 < Ncz ? vr0 : Ncz, cr1 = vr1 < Ncz ? vr1 : Ncz;
+    const size_t coff = (size_t)cr0 * Ncx, cn = (size_t)(cr1 - cr0) * Ncx;
+    const size_t voff = (size_t)vr0 * Nx, vn = (size_t)(vr1 - vr0) * Nx;
+    for (int i = 0; i < L.nci; i++) CK(up(A.ci[i], L.cin[i], coff, cn, 8));
+    for (int i = 0; i < L.nvi; i++) CK(up(A.vi[i], L.vin[i], voff, vn, 8));
+    for (int p = 0; p < np; p++) {
+      CK(up(A.perc_n[p], f->phase_perc_n[p], coff, cn, 8));
+      CK(up(A.perc_s[p], f->phase_perc_s[p], voff, vn, 8));
+      CK(up(A.peta_n[p], f->phase_eta_n[p], coff, cn, 8));
+      CK(up(A.peta_s[p], f->phase_eta_s[p], voff, vn, 8));
+    }
+    CK(up(A.bcp, f->BCp_type, coff, cn, 1));
+    CK(up(A.bcg, f->BCg_type, voff, vn, 1));
+    CK(cudaEventRecord(ev[1 + b], ctx->copy_in));
+    cudaStream_t ks = (b & 1) ? ctx->compute2 : ctx->stream;
+    CK(cudaStreamWaitEvent(ks, ev[1 + b], 0));
+    if (b == 0) CK(cudaEventRecord(ctx->ev0, ks));
+    A.ranged = 1;
+    A.c_lo = (long long)coff; A.c_n = (long long)cn; A.v_lo = (long long)voff; A.v_n = (long long)vn;
+    CK(launch_sweep(A, aniso, ks, ctx->block[aniso], ctx->grid_cap[aniso]));
+    ctx->launches += 1;
+    CK(cudaEventRecord(ev[1 + B + b], ks));
+    CK(cudaStreamWaitEvent(ctx->copy_out, ev[1 + B + b], 0));
+    for (int i = 0; i < CO_COUNT; i++) CK(down(L.cout[i], A.co[i], coff, cn, 8));
+    for (int i = 0; i < VO_COUNT; i++) CK(down(L.vout[i], A.vo[i], voff, vn, 8));
+    for (int p = 0; p < np; p++) {
+      CK(down(f->phase_eta_n[p], A.peta_n[p], coff, cn, 8));
+      CK(down(f->phase_eta_s[p], A.peta_s[p], voff, vn, 8));
+    }
+  }
+  A.ranged = 0;
+  CK(cudaEventRecord(ev[2 + 2 * B], ctx->compute2));
+  CK(cudaStreamWaitEvent(ctx->stream, ev[2 + 2 * B], 0));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventRecord(ev[1 + 2 * B], ctx->copy_out));
+  CK(cudaStreamWaitEvent(ctx->stream, ev[1 + 2 * B], 0));
+  return MDZ_OK;
+}
+
 int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat, const mdz_grid_fields *f,
                int final_update, int mem, int flags, mdz_sweep_stats *st, bool aniso, float *X = nullptr,
                float *Y = nullptr) {
@@ -343,6 +472,13 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
 
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
+  const int bands = (host && mode < 0 && !(flags & MDZ_SWEEP_ITERS)) ? host_bands(ctx, md->Nz) : 1;
+  if (bands > 1) {
+    A.stats = ctx->d_stats;
+    if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+    if ((rc = banded_sweep(ctx, A, aniso, L, f, bands)) != MDZ_OK) return rc;
+    return finish(ctx, st);
+  }
   Mirror mi{ctx};
   for (int i = 0; i < nci; i++) A.ci[i] = mi.in(cin[i], S_CI + i, Nc, host);
   for (int i = 0; i < nvi; i++) A.vi[i] = mi.in(vin[i], S_VI + i, Nv, host);
@@ -699,8 +835,18 @@ int mdz_rheo_destroy(mdz_rheo_ctx *c) {
   if (c->h_stats) cudaFreeHost(c->h_stats);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t e : c->band_ev) if (e) cudaEventDestroy(e);
+  if (c->copy_in) { cudaStreamSynchronize(c->copy_in); cudaStreamDestroy(c->copy_in); }
+  if (c->copy_out) { cudaStreamSynchronize(c->copy_out); cudaStreamDestroy(c->copy_out); }
+  if (c->compute2) { cudaStreamSynchronize(c->compute2); cudaStreamDestroy(c->compute2); }
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
+  return MDZ_OK;
+}
+
+int mdz_rheo_set_host_bands(mdz_rheo_ctx *c, int bands) {
+  if (!c || bands < 0 || bands > kMaxBands) return MDZ_EINVAL;
+  c->bands = bands;
   return MDZ_OK;
 }
 

@@ -256,10 +256,11 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
 template <bool ANISO>
 __global__ void __launch_bounds__(128) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0};
-  const long long total = A.M.Nc + A.M.Nv;
+  const long long nc = A.ranged ? A.c_n : A.M.Nc, total = nc + (A.ranged ? A.v_n : A.M.Nv);
+  const long long c_lo = A.ranged ? A.c_lo : 0, v_lo = A.M.Nc + (A.ranged ? A.v_lo : 0);
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride)
-    sweep_node<ANISO>(A, i, acc);
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride)
+    sweep_node<ANISO>(A, j < nc ? c_lo + j : v_lo + (j - nc), acc);
   flush_acc(A.stats, acc);
 }
 
@@ -463,7 +464,7 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArg
 }
 
 cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap) {
-  const long long total = a.M.Nc + a.M.Nv;
+  const long long total = a.ranged ? a.c_n + a.v_n : a.M.Nc + a.M.Nv;
   long long grid = (total + block - 1) / block;
   if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
   if (grid < 1) grid = 1;

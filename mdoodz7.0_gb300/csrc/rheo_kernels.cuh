@@ -53,6 +53,10 @@ struct SweepArgs {
   int final_update, need_lnd;
   int polish;  // FP32 Newton steps before each FP64 local solve (0: the reference's start)
   long long node_base;  // added to node indices in error reports (batched grids)
+  // k_sweep over a band of rows only: centroids [c_lo, c_lo + c_n) and vertices
+  // [v_lo, v_lo + v_n); 0 sweeps every node
+  int ranged;
+  long long c_lo, c_n, v_lo, v_n;
 };
 
 // Many grids in one launch.  Grid g owns tiles [tile_start[g], tile_start[g + 1]) of

@@ -376,6 +376,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
     lib.mdz_rheo_destroy.argtypes = [C.c_void_p]
     lib.mdz_rheo_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    lib.mdz_rheo_set_host_bands.argtypes = [C.c_void_p, C.c_int]
     lib.mdz_rheo_sync.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
     for fn in (lib.mdz_rheo_sweep, lib.mdz_rheo_sweep_aniso):
         fn.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
@@ -592,6 +593,12 @@ class Context:
         rc = self.lib.mdz_rheo_set_stream(self.handle, stream_ptr)
         if rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_set_stream")
+
+    def set_host_bands(self, bands: int = 0):
+        """Row bands of host-memory sweeps (0: automatic)."""
+        rc = self.lib.mdz_rheo_set_host_bands(self.handle, bands)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_set_host_bands")
 
     def _sweep(self, fn, model, mat, fields, final_update, mem, flags, check):
         st = SweepStats()

@@ -1,0 +1,92 @@
+"""Sweeps of host arrays in row bands (copies overlapping the kernels) against the
+one-shot host sweep and the device-resident sweep: every output bit for bit, for any
+band count, with periodic x, air rows and uneven band edges."""
+import numpy as np
+import pytest
+
+import mdz_rheo as R
+import mdz_workloads as W
+from common import clone
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = R.Context(0)
+    yield c
+    c.set_host_bands(0)
+    c.close()
+
+
+def with_air_and_periodic(w, air_rows=9):
+    """Air above the top `air_rows` rows (BCp 31, BCg 30) and periodic x."""
+    m, a = w.model, w.arrays
+    a["BCp_type"].reshape(m.Nz - 1, m.Nx - 1)[-air_rows:, :] = 31
+    a["BCg_type"].reshape(m.Nz, m.Nx)[-air_rows:, :] = 30
+    m.periodic_x = 1
+    return w
+
+
+CASES = {
+    "plain_large_96x257": (lambda: W.plain_large(seed=21, ncx=96, ncz=257), False),
+    "plain_large_air_periodic": (lambda: with_air_and_periodic(W.plain_large(seed=22, ncx=70, ncz=131)), False),
+    "aniso_80x150_air_periodic": (lambda: with_air_and_periodic(W.aniso(seed=23, ncx=80, ncz=150)), True),
+}
+
+
+def same(a, b):
+    for k in a:
+        x, y = a[k], b[k]
+        if isinstance(x, list):
+            for i, (u, v) in enumerate(zip(x, y)):
+                assert np.array_equal(np.asarray(u).view(np.uint8), np.asarray(v).view(np.uint8)), (k, i)
+        else:
+            assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8)), k
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_banded_host_sweep_is_the_one_shot_sweep(ctx, name):
+    make, aniso = CASES[name]
+    w = make()
+    fn = ctx.sweep_aniso if aniso else ctx.sweep
+    ctx.set_host_bands(1)
+    one = clone(w.arrays)
+    _, st1 = fn(w.model, w.mat, R.FieldSet(one))
+    assert st1.kernel_launches == 1
+    # the device-resident sweep on the same inputs
+    dev = {k: ([torch.from_numpy(x.copy()).cuda() for x in v] if isinstance(v, list) else
+               torch.from_numpy(v.copy()).cuda()) for k, v in w.arrays.items()}
+    fn(w.model, w.mat, R.FieldSet(dev), mem=R.MEM_DEVICE)
+    same(one, {k: ([x.cpu().numpy() for x in v] if isinstance(v, list) else v.cpu().numpy()) for k, v in dev.items()})
+    for bands in (2, 3, 7, 16):
+        ctx.set_host_bands(bands)
+        got = clone(w.arrays)
+        _, st = fn(w.model, w.mat, R.FieldSet(got))
+        assert st.kernel_launches == min(bands, w.model.Nz)
+        assert st.phase_calls == st1.phase_calls and st.newton_iters == st1.newton_iters
+        assert st.h2d_bytes == st1.h2d_bytes and st.d2h_bytes == st1.d2h_bytes
+        same(one, got)
+    ctx.set_host_bands(0)
+
+
+def test_banded_sweep_reports_the_failing_node(ctx):
+    """A node whose local solve fails in a later band: the same status and node as the
+    one-shot sweep."""
+    w = W.plain_large(seed=24, ncx=40, ncz=200)
+    c1 = w.model.Nx * 150 + 7  # a vertex in the fourth of five bands
+    w.arrays["exz"][c1] = np.nan
+    ctx.set_host_bands(1)
+    rc1, st1 = ctx.sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), check=False)
+    ctx.set_host_bands(5)
+    rc5, st5 = ctx.sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), check=False)
+    ctx.set_host_bands(0)
+    assert rc1 == rc5 and st1.status == st5.status and st1.error_node == st5.error_node
+
+
+def test_host_bands_argument_checked(ctx):
+    with pytest.raises(R.RheoError):
+        ctx.set_host_bands(17)
+    with pytest.raises(R.RheoError):
+        ctx.set_host_bands(-1)
