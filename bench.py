@@ -59,7 +59,7 @@ FP64_FLOPS_PER_MARKER = {"jaumann_stencil1": 98.34, "analytical_director_stencil
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=None,
@@ -566,10 +566,14 @@ def main():
         nmk = int(mw.info["markers"]["x"].size)
         markers = {"grid": f"{args.size}x{args.size} cells, 16 markers per cell ({nmk} markers, cell by cell), "
                            "2 % inactive, no air"}
-        variants = {"jaumann_stencil1": (1, 1, 0, 1, 1), "analytical_director_stencil9": (1, 2, 1, 1, 9)}
+        # (elastic, rotation, anisotropy, advection, stencil, subgrid_diffusion)
+        variants = {"jaumann_stencil1": (1, 1, 0, 1, 1, 0), "analytical_director_stencil9": (1, 2, 1, 1, 9, 0),
+                    "subgrid2_jaumann_stencil1": (1, 1, 0, 1, 1, 2)}
         for name, o in variants.items():
             opts = R.MarkerOpts()
-            opts.elastic, opts.stress_rotation, opts.anisotropy, opts.advection, opts.interp_stencil = o
+            (opts.elastic, opts.stress_rotation, opts.anisotropy, opts.advection, opts.interp_stencil,
+             opts.subgrid_diffusion) = o
+            opts.set_G(mw.info["G"])
             call = lambda: ctx.marker_stress(mw.model, opts, gd, md, mw.info["dx"], mw.info["dz"], mem=R.MEM_DEVICE)
             for _ in range(max(3, args.warmup)):
                 call()
@@ -693,6 +697,7 @@ def main():
                        "parallelism": f"{ws} independent grid(s), one per GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
             "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
+            "median_kernel_ms_per_sweep": statistics.median(kernel_ms),
             "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op,
             "strain_rates": strain, "input_preparation": prep, "marker_stress": markers}
     print(json.dumps(line))

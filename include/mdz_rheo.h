@@ -25,7 +25,7 @@
  *   mdz_rheo_softening      <- CohesionFrictionDilationGrid after its P2Mastah step
  *                              def MDLIB/RheologyDensity.c:1539 (Softening :1432)
  *   mdz_rheo_shear_modulus  <- ShearModCompExpGrid, def MDLIB/RheologyDensity.c:1634
- *   mdz_rheo_marker_stress  <- UpdateParticleStress (subgrid_diffusion 0/1)
+ *   mdz_rheo_marker_stress  <- UpdateParticleStress
  *                              MDLIB/mdoodz-private.h:415, def MDLIB/RheologyParticles.c:1725
  *
  * All arithmetic is IEEE binary64.  Unless a call says otherwise it is
@@ -370,8 +370,10 @@ typedef struct mdz_markers {
 
 /* The grid side of UpdateParticleStress: spacing, node coordinates as the reference
  * builds them (GridRoutines.c:270-315: xg/zg vertex coordinates, Nx and Nz of them;
- * xvz/zvx the centroid coordinates with one ghost at each end, Nx+1 and Nz+1 of them),
- * the sweep's new and old stresses, and the velocities (director rotation only). */
+ * xvz/zvx the centroid coordinates with one ghost at each end, Nx+1 and Nz+1 of them;
+ * xc/zc the centroid coordinates, Nx-1 and Nz-1 of them), the sweep's new and old
+ * stresses, the velocities (director rotation only) and the vertex viscosity (subgrid
+ * stress diffusion only). */
 typedef struct mdz_marker_grid {
   double dx, dz;
   const double *xg_coord, *zg_coord, *xvz_coord, *zvx_coord;
@@ -380,29 +382,42 @@ typedef struct mdz_marker_grid {
   const double *sxz, *sxz0;                   /* vertices */
   const double *u_in, *v_in;                  /* staggered velocities (layout of mdz_strain_rate_fields) */
   double *wxz;                                /* vertices; rewritten as the reference rewrites it (below) */
+  const double *xc_coord, *zc_coord;          /* subgrid_diffusion 2 */
+  const double *eta_phys_s;                   /* vertices; subgrid_diffusion 2 */
 } mdz_marker_grid;
 
-/* The params switches of UpdateParticleStress (MDLIB/include/mdoodz.h:49-139). */
+/* The params switches of UpdateParticleStress (MDLIB/include/mdoodz.h:49-139), and for
+ * subgrid_diffusion 2 the shear modulus of every phase (mat_prop G, host memory,
+ * model->Nb_phases entries). */
 typedef struct mdz_marker_opts {
   int elastic, subgrid_diffusion, stress_rotation, anisotropy, advection, interp_stencil;
+  const double *G;
 } mdz_marker_opts;
 
-/* UpdateParticleStress (MDLIB/RheologyParticles.c:1725-2004) without its subgrid stress
- * diffusion (subgrid_diffusion 0 or 1; 2 returns MDZ_EUNSUPPORTED):
+/* UpdateParticleStress (MDLIB/RheologyParticles.c:1725-2004):
  *   - with anisotropy and advection on, the director of every active marker turns with
  *     the velocity gradients interpolated from the grid (:1784-1802);
- *   - with elastic on, every marker takes the grid's stress increments sxxd - sxxd0,
- *     szzd - szzd0 (centroids, Interp_Grid2P_centroids2) and sxz - sxz0 (vertices,
- *     Interp_Grid2P) (:1919-1966), then the stress rotation of stress_rotation 1
- *     (Jaumann) or 2 (analytical) (:1967-1992).  The reference rotates with a marker
- *     spin that its P2Mastah call fills the other way round (markers -> grid, from a
- *     zeroed marker array), so the rotation turns by zero and wxz is overwritten with
- *     zeros wherever markers reach a vertex; both are reproduced.
- * model supplies Nx, Nz, periodic_x and dt.  Results are those of the reference to the
- * last bit, except the director, whose normalisation squares by multiplication where
- * the reference calls pow (a few ulp).  A marker outside the vertex grid in x returns
- * MDZ_EMARKER_OUT (the reference exits with code 89).  `mem`, `flags` (MDZ_SWEEP_ASYNC)
- * and `stats` as for mdz_rheo_strain_rates. */
+ *   - with elastic on and subgrid_diffusion 0 or 1, every marker takes the grid's stress
+ *     increments sxxd - sxxd0, szzd - szzd0 (centroids, Interp_Grid2P_centroids2) and
+ *     sxz - sxz0 (vertices, Interp_Grid2P) (:1919-1966);
+ *   - with elastic on and subgrid_diffusion 2 (:1811-1903), every active marker relaxes
+ *     towards the old grid stress interpolated to it over its Maxwell time eta_phys_s/G
+ *     (the subgrid increment), the subgrid increments go to the grid by P2Mastah, and
+ *     the rest of the grid's increment comes back to the markers;
+ *   - then the stress rotation of stress_rotation 1 (Jaumann) or 2 (analytical)
+ *     (:1967-1992).  The reference rotates with a marker spin that its P2Mastah call
+ *     fills the other way round (markers -> grid, from a zeroed marker array), so the
+ *     rotation turns by zero and wxz is overwritten with zeros wherever markers reach a
+ *     vertex; both are reproduced.
+ * model supplies Nx, Nz, periodic_x, dt and (subgrid_diffusion 2) Nb_phases.  Results
+ * are those of the reference to the last bit, except the director, whose normalisation
+ * squares by multiplication where the reference calls pow (a few ulp), and subgrid
+ * diffusion 2, whose P2Mastah sums run in another order (the reference's own order
+ * depends on its thread count) and whose exp is CUDA's: within 1e-12 of the stress
+ * scale.  A marker outside the vertex grid in x returns MDZ_EMARKER_OUT (the reference
+ * exits with code 89); a non-finite increment MDZ_ENONFINITE (exit 1); a marker phase
+ * outside [0, Nb_phases) with subgrid_diffusion 2, MDZ_EINVAL.  `mem`, `flags`
+ * (MDZ_SWEEP_ASYNC) and `stats` as for mdz_rheo_strain_rates. */
 int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_opts *opts,
                            mdz_marker_grid *grid, mdz_markers *markers, int mem, int flags,
                            mdz_sweep_stats *stats);

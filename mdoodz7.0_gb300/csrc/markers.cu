@@ -27,6 +27,15 @@
 // by zero; its arithmetic is kept as written, with cos(+-0) = 1 and sin(+-0) = +-0
 // taken as the exact values they are.
 //
+// subgrid_diffusion 2 (RheologyParticles.c:1811-1903) adds two launches between the grid
+// kernel and the update.  k_marker_subgrid, per marker: the old grid stresses and the
+// vertex viscosity at the marker, its subgrid increment -(s - s0)(1 - exp(-dt/t_M)) with
+// t_M = eta/G, and P2Mastah's sums of those increments on the centroid and vertex grids
+// (atomics; the reference's own order depends on its thread count).  k_marker_remainder,
+// per node: the grid's increment less the subgrid increment P2Mastah gives the node.
+// k_marker_update then interpolates the remainders exactly as the plain increments and
+// adds both to the marker; k_marker_wxz takes its vertex weight sums from the same P2Mastah.
+//
 // Every division by the mesh spacing or by the weight length is correctly rounded
 // (fp64_div.cuh), every product and sum is written with round-to-nearest intrinsics,
 // cell indices come from fp64_ceil_int (the reference's ceil, on the integer pipe), and
@@ -36,6 +45,7 @@
 #include "markers.cuh"
 
 #include "fp64_bits.cuh"
+#include "fp64_math.cuh"
 
 namespace mdz {
 
@@ -245,16 +255,76 @@ __device__ __noinline__ void rotate(int rotation, double dt, double &txx, double
   }
 }
 
+// P2Mastah's exact weights of a marker on a grid of Nxn x Nzn nodes at X, Z (:2301-2575),
+// visit(node, w) in the reference's order.  hx, hz are ceil((x - X[0]) / dx + 1/2) - 1 and
+// its z twin, unclamped.  The nine weights share three quotients per axis.
+template <class F>
+__device__ __forceinline__ void p2m_exact(const MarkerArgs &A, const double *X, const double *Z, int Nxn, int Nzn,
+                                          double x, double z, int hx, int hz, F visit) {
+  const int ip = clamp_to(hx, Nxn - 1), jp = clamp_to(hz, Nzn - 1);
+  const double Xp = X[ip], Zp = Z[jp];
+  const double fc = __dsub_rn(1.0, div_by(fabs(__dsub_rn(Xp, x)), A.dx_itp));
+  const double gc = __dsub_rn(1.0, div_by(fabs(__dsub_rn(Zp, z)), A.dz_itp));
+  visit(ip + (long long)jp * Nxn, __dmul_rn(fc, gc));
+  if (A.stencil != 9) return;
+  const int per = A.periodic_x;
+  const bool peE = (ip == Nxn - 1 && per == 1), peW = (ip == 0 && per == 1);
+  const double fE = __dsub_rn(1.0, div_by(fabs(__dsub_rn(__dadd_rn(Xp, A.dx.b), x)), A.dx_itp));
+  const double fW = __dsub_rn(1.0, div_by(fabs(__dsub_rn(__dsub_rn(Xp, A.dx.b), x)), A.dx_itp));
+  const double gN = __dsub_rn(1.0, div_by(fabs(__dsub_rn(__dadd_rn(Zp, A.dz.b), z)), A.dz_itp));
+  const double gS = __dsub_rn(1.0, div_by(fabs(__dsub_rn(__dsub_rn(Zp, A.dz.b), z)), A.dz_itp));
+  const int kE = peE ? 0 : ip + 1, kW = peW ? Nxn - 1 : ip - 1;
+  const bool N = jp < Nzn - 1, S = jp > 0, E = ip < Nxn - 1 || peE, Wst = ip > 0 || peW;
+  if (N) visit(ip + (long long)(jp + 1) * Nxn, __dmul_rn(fc, gN));
+  if (S) visit(ip + (long long)(jp - 1) * Nxn, __dmul_rn(fc, gS));
+  if (E) visit(kE + (long long)jp * Nxn, __dmul_rn(fE, gc));
+  if (Wst) visit(kW + (long long)jp * Nxn, __dmul_rn(fW, gc));
+  if (S && Wst) visit(kW + (long long)(jp - 1) * Nxn, __dmul_rn(fW, gS));
+  if (N && Wst) visit(kW + (long long)(jp + 1) * Nxn, __dmul_rn(fW, gN));
+  if (N && E) visit(kE + (long long)(jp + 1) * Nxn, __dmul_rn(fE, gN));
+  if (S && E) visit(kE + (long long)(jp - 1) * Nxn, __dmul_rn(fE, gS));
+}
+
+// Interp_Grid2P_centroids2 of two raw centroid fields: an air corner takes the value of
+// the corner across, the sum is divided by the weight sum where that exceeds 1e-13
+__device__ __forceinline__ double2 gather_sub(const MarkerArgs &A, const double *fa, const double *fb, const int c[4],
+                                              const double w[4]) {
+  const int alt[4] = {c[2], c[3], c[0], c[1]};
+  double a = 0.0, b = 0.0, sw = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const int cc = air(A.bcp[c[q]]) ? alt[q] : c[q];
+    a = __dadd_rn(a, __dmul_rn(w[q], fa[cc]));
+    b = __dadd_rn(b, __dmul_rn(w[q], fb[cc]));
+    sw = __dadd_rn(sw, w[q]);
+  }
+  if (fp64_gt(sw, 1e-13)) div_sum(a, b, sw);
+  return make_double2(a, b);
+}
+
+// Interp_Grid2P of a raw vertex field: an air corner takes the value of the corner across
+__device__ __forceinline__ double gather_vertex(const MarkerArgs &A, const double *f, const int cv[4],
+                                                const double w[4]) {
+  const int alt[4] = {cv[2], cv[3], cv[0], cv[1]};
+  double v = 0.0;
+#pragma unroll
+  for (int q = 0; q < 4; q++) v = __dadd_rn(v, __dmul_rn(w[q], f[air(A.bcg[cv[q]]) ? alt[q] : cv[q]]));
+  return v;
+}
+
 __global__ void __launch_bounds__(256) k_marker_grid(const MarkerArgs A) {
   const long long Nc = (long long)(A.Nx - 1) * (A.Nz - 1), Nv = (long long)A.Nx * A.Nz;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t == 0 && A.elastic == 1) *A.exotic = 0;
+  if (t == 0 && A.elastic == 1 && !A.subgrid) *A.exotic = 0;
   if (t < Nc) {
     const long long c0 = t;
     const bool a = air(A.bcp[c0]);
-    if (A.elastic == 1)
+    if (A.elastic == 1 && A.subgrid) {
+      A.sum_n[c0] = 0.0; A.sum_n[Nc + c0] = 0.0; A.sum_n[2 * Nc + c0] = 0.0;
+    } else if (A.elastic == 1) {
       A.inc_n[c0] = a ? make_double2(0.0, 0.0)
                       : make_double2(__dsub_rn(A.sxxd[c0], A.sxxd0[c0]), __dsub_rn(A.szzd[c0], A.szzd0[c0]));
+    }
     if (A.director) {
       // RheologyParticles.c:1751-1766 in the layout of the velocity arrays
       const int Ncx = A.Nx - 1, k = (int)(c0 % Ncx), l = (int)(c0 / Ncx);
@@ -266,7 +336,9 @@ __global__ void __launch_bounds__(256) k_marker_grid(const MarkerArgs A) {
   } else if (t < Nc + Nv) {
     const long long c1 = t - Nc;
     const bool wall = A.bcg[c1] == 30;
-    if (A.elastic == 1) {
+    if (A.elastic == 1 && A.subgrid) {
+      A.sum_s[c1] = 0.0; A.sum_s[Nv + c1] = 0.0;
+    } else if (A.elastic == 1) {
       A.inc_s[c1] = wall ? 0.0 : __dsub_rn(A.sxz[c1], A.sxz0[c1]);
       A.hit[c1] = 0;
       A.WM[c1] = 0.0;
@@ -282,12 +354,100 @@ __global__ void __launch_bounds__(256) k_marker_grid(const MarkerArgs A) {
   }
 }
 
+// subgrid diffusion 2, markers (:1822-1861)
+__global__ void __launch_bounds__(256) k_marker_subgrid(const MarkerArgs A) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.n) return;
+  const int ph = A.phase[k];
+  if (ph == -1) return;
+  if (ph < 0 || ph >= A.np) { report(A, k, MDZ_EINVAL); return; }
+  const double x = A.x[k], z = A.z[k];
+  int jp, ip, c[4];
+  double txx0 = 0.0, tzz0 = 0.0;
+  if (cell_corners(A, x, z, jp, ip, c)) {
+    double wc[4];
+    weights(div_by(__dsub_rn(x, A.xvz[jp]), A.dx), div_by(__dsub_rn(z, A.zvx[ip]), A.dz), wc);
+    const double2 t0 = gather_sub(A, A.sxxd0, A.szzd0, c, wc);
+    txx0 = t0.x; tzz0 = t0.y;
+    if (fp64_is_inf(txx0) || fp64_is_inf(tzz0)) report(A, k, MDZ_ENONFINITE);  // ParticleRoutines.c:1565-1569
+  } else {
+    report(A, k, MDZ_EMARKER_OUT);
+  }
+  const double tx = __dsub_rn(x, A.xg[0]), tz = __dsub_rn(z, A.zg[0]);
+  const CellPair px = cell_pair(tx, A.dx), pz = cell_pair(tz, A.dz);
+  if (px.c > A.Nx - 2) report(A, k, MDZ_EMARKER_OUT);
+  const int j = clamp_to(px.c, A.Nx - 2), i = clamp_to(pz.c, A.Nz - 2);
+  double wv[4];
+  weights(div_by(fabs(__dsub_rn(x, A.xg[j])), A.dx), div_by(fabs(__dsub_rn(z, A.zg[i])), A.dz), wv);
+  const int cv[4] = {j + i * A.Nx, j + i * A.Nx + 1, j + (i + 1) * A.Nx, j + (i + 1) * A.Nx + 1};
+  const double txz0 = gather_vertex(A, A.sxz0, cv, wv), etam = gather_vertex(A, A.eta_s, cv, wv);
+  // -(s - s0) (1 - exp(-d dt / t_M)), d = 1, t_M = eta / G (:1844-1846); the table-driven
+  // exp of fp64_math.cuh (about 1 ulp from the C library's)
+  const double tM = div_by(etam, A.G[ph]);
+  const double f = __dsub_rn(1.0, fast_exp(-A.dt / tM));
+  const double dxx = __dmul_rn(-__dsub_rn(A.m_sxxd[k], txx0), f);
+  const double dzz = __dmul_rn(-__dsub_rn(A.m_szzd[k], tzz0), f);
+  const double dxz = __dmul_rn(-__dsub_rn(A.m_sxz[k], txz0), f);
+  if (!fp64_finite(dxx)) report(A, k, MDZ_ENONFINITE);  // :1847-1855, exit 1
+  A.m_sub[k] = dxx;
+  A.m_sub[A.n + k] = dzz;
+  A.m_sub[2 * A.n + k] = dxz;
+  // P2Mastah's sums (:1859-1861): centroids at xc, zc, vertices at xg, zg
+  const int Ncx = A.Nx - 1, Ncz = A.Nz - 1;
+  const long long Nc = (long long)Ncx * Ncz, Nv = (long long)A.Nx * A.Nz;
+  const CellPair qx = cell_pair(__dsub_rn(x, A.xc[0]), A.dx), qz = cell_pair(__dsub_rn(z, A.zc[0]), A.dz);
+  p2m_exact(A, A.xc, A.zc, Ncx, Ncz, x, z, qx.h, qz.h, [&](long long v, double w) {
+    atomicAdd(&A.sum_n[v], w);
+    atomicAdd(&A.sum_n[Nc + v], __dmul_rn(dxx, w));
+    atomicAdd(&A.sum_n[2 * Nc + v], __dmul_rn(dzz, w));
+  });
+  p2m_exact(A, A.xg, A.zg, A.Nx, A.Nz, x, z, px.h, pz.h, [&](long long v, double w) {
+    atomicAdd(&A.sum_s[v], w);
+    atomicAdd(&A.sum_s[Nv + v], __dmul_rn(dxz, w));
+  });
+}
+
+// P2Mastah's node value BMWM / WM where |WM| reaches 1e-30 away from air, else 0 (the
+// reference's zeroed target), for one sum pair (:2603-2631)
+__device__ __forceinline__ double p2m_value(double W, double BM, bool air_node) {
+  return (air_node || fp64_abs_lt(W, 1e-30)) ? 0.0 : BM / W;
+}
+
+// subgrid diffusion 2, grid (:1864-1872): what remains of each node's increment
+__global__ void __launch_bounds__(256) k_marker_remainder(const MarkerArgs A) {
+  const long long Nc = (long long)(A.Nx - 1) * (A.Nz - 1), Nv = (long long)A.Nx * A.Nz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < Nc) {
+    const long long c0 = t;
+    if (air(A.bcp[c0])) {
+      A.inc_n[c0] = make_double2(0.0, 0.0);
+      return;
+    }
+    const double W = A.sum_n[c0];
+    const double gxx = p2m_value(W, A.sum_n[Nc + c0], false), gzz = p2m_value(W, A.sum_n[2 * Nc + c0], false);
+    A.inc_n[c0] = make_double2(__dsub_rn(__dsub_rn(A.sxxd[c0], A.sxxd0[c0]), gxx),
+                               __dsub_rn(__dsub_rn(A.szzd[c0], A.szzd0[c0]), gzz));
+  } else if (t < Nc + Nv) {
+    const long long c1 = t - Nc;
+    const int k = (int)(c1 % A.Nx);
+    double g = p2m_value(A.sum_s[c1], A.sum_s[Nv + c1], air(A.bcg[c1]));
+    if (A.periodic_x == 1 && (k == 0 || k == A.Nx - 1)) {
+      // :2633-2641: both ends of the row take the mean of the two
+      const long long last = c1 - k + A.Nx - 1, first = c1 - k;
+      g = 0.5 * (p2m_value(A.sum_s[last], A.sum_s[Nv + last], air(A.bcg[last])) +
+                 p2m_value(A.sum_s[first], A.sum_s[Nv + first], air(A.bcg[first])));
+    }
+    A.inc_s[c1] = (A.bcg[c1] == 30) ? 0.0 : __dsub_rn(__dsub_rn(A.sxz[c1], A.sxz0[c1]), g);
+  }
+}
+
 __global__ void __launch_bounds__(256) k_marker_update(const MarkerArgs A) {
   const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= A.n) return;
   if (A.phase[k] == -1) {
-    // ArrayPlusArray adds the (zero) increment of an inactive marker too (:1954-1956)
-    if (A.elastic == 1) {
+    // ArrayPlusArray adds the (zero) increment of an inactive marker too (:1954-1956);
+    // the subgrid update leaves it alone (:1878-1884)
+    if (A.elastic == 1 && !A.subgrid) {
       A.m_sxxd[k] = __dadd_rn(A.m_sxxd[k], 0.0);
       A.m_szzd[k] = __dadd_rn(A.m_szzd[k], 0.0);
       A.m_sxz[k] = __dadd_rn(A.m_sxz[k], 0.0);
@@ -351,8 +511,14 @@ __global__ void __launch_bounds__(256) k_marker_update(const MarkerArgs A) {
       dsxz = __dadd_rn(dsxz, __dmul_rn(wv[q], A.inc_s[cc]));
     }
   }
-  // ArrayPlusArray (:1954-1956)
-  double txx = __dadd_rn(A.m_sxxd[k], dsx), tzz = __dadd_rn(A.m_szzd[k], dsz), txz = __dadd_rn(A.m_sxz[k], dsxz);
+  // ArrayPlusArray (:1954-1956), or the subgrid update s + ds_sub + ds_rest (:1878-1884)
+  double txx = A.m_sxxd[k], tzz = A.m_szzd[k], txz = A.m_sxz[k];
+  if (A.subgrid) {
+    txx = __dadd_rn(txx, A.m_sub[k]);
+    tzz = __dadd_rn(tzz, A.m_sub[A.n + k]);
+    txz = __dadd_rn(txz, A.m_sub[2 * A.n + k]);
+  }
+  txx = __dadd_rn(txx, dsx); tzz = __dadd_rn(tzz, dsz); txz = __dadd_rn(txz, dsxz);
   // rotation by the zeroed marker spin (:1972-1989)
   if (A.rotation == 1 || A.rotation == 2) {
     const unsigned exx = fp64_exponent(txx), ezz = fp64_exponent(tzz), exz = fp64_exponent(txz);
@@ -363,7 +529,8 @@ __global__ void __launch_bounds__(256) k_marker_update(const MarkerArgs A) {
   A.m_sxxd[k] = txx;
   A.m_szzd[k] = tzz;
   A.m_sxz[k] = txz;
-  p2m_vertices(A, x, z, px.h, pz.h, [&](long long v, double ax, double az) { p2m_mark(A, v, ax, az); });
+  if (!A.subgrid)
+    p2m_vertices(A, x, z, px.h, pz.h, [&](long long v, double ax, double az) { p2m_mark(A, v, ax, az); });
 }
 
 // The exact P2Mastah weight sums, only after a weight below 1e-30 that is not zero (or
@@ -384,7 +551,7 @@ __global__ void __launch_bounds__(256) k_marker_weights(const MarkerArgs A) {
 __device__ __forceinline__ double wxz_after(const MarkerArgs &A, long long c1, bool exact) {
   if (air(A.bcg[c1])) return A.wxz[c1];
   if (exact) {
-    const double W = A.WM[c1];
+    const double W = A.subgrid ? A.sum_s[c1] : A.WM[c1];
     return fp64_abs_lt(W, 1e-30) ? A.wxz[c1] : 0.0 / W;
   }
   return A.hit[c1] ? 0.0 : A.wxz[c1];
@@ -393,7 +560,7 @@ __device__ __forceinline__ double wxz_after(const MarkerArgs &A, long long c1, b
 __global__ void __launch_bounds__(256) k_marker_wxz(const MarkerArgs A) {
   const long long c1 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c1 >= (long long)A.Nx * A.Nz) return;
-  const bool exact = *A.exotic != 0;
+  const bool exact = A.subgrid || *A.exotic != 0;
   const int k = (int)(c1 % A.Nx);
   if (A.periodic_x == 1) {
     if (k == A.Nx - 1) return;  // written by the row's first vertex
@@ -417,6 +584,16 @@ unsigned blocks_for(long long n) {
 
 cudaError_t launch_marker_grid(const MarkerArgs &a, cudaStream_t s) {
   k_marker_grid<<<blocks_for((long long)(a.Nx - 1) * (a.Nz - 1) + (long long)a.Nx * a.Nz), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_marker_subgrid(const MarkerArgs &a, cudaStream_t s) {
+  if (a.n > 0) k_marker_subgrid<<<blocks_for(a.n), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_marker_remainder(const MarkerArgs &a, cudaStream_t s) {
+  k_marker_remainder<<<blocks_for((long long)(a.Nx - 1) * (a.Nz - 1) + (long long)a.Nx * a.Nz), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -12,6 +12,9 @@ struct MarkerArgs {
   int Nx, Nz, periodic_x;           // vertices
   int elastic, rotation, director;  // switches (director: anisotropy and advection on)
   int stencil;                      // P2Mastah's interpolation stencil, 1 or 9
+  int subgrid;                      // subgrid_diffusion 2: relaxation of marker stresses (elastic only)
+  int np;                           // phases (subgrid diffusion 2)
+  Divisor G[MDZ_MAX_PHASES];        // shear modulus per phase (subgrid diffusion 2)
   double dt;
   Divisor dx, dz;                   // mesh spacing
   Divisor dx_itp, dz_itp;           // P2Mastah's weight lengths: dx/2 (stencil 1) or 3 dx/2 (stencil 9)
@@ -31,11 +34,20 @@ struct MarkerArgs {
   unsigned char *hit;  // vertex received a P2Mastah weight >= 1e-30
   double *WM;          // exact per-vertex weight sums, filled only when *exotic is set
   int *exotic;         // a weight below 1e-30 that is not zero, or not finite, was seen
+  // subgrid diffusion 2
+  const double *xc, *zc, *eta_s;  // centroid coordinates (Ncx, Ncz), vertex viscosity
+  double *m_sub;                  // per marker: the subgrid increments of sxxd, szzd, sxz [3][n]
+  double *sum_n;                  // centroids: P2Mastah's WM, BMWM of dsxx, BMWM of dszz [3][Nc]
+  double *sum_s;                  // vertices: WM, BMWM of dsxz [2][Nv]
   DevStats *stats;
 };
 
 // grid: stress increments and velocity gradients per node, scratch cleared
 cudaError_t launch_marker_grid(const MarkerArgs &a, cudaStream_t s);
+// markers (subgrid diffusion 2): the subgrid increments and their P2Mastah sums
+cudaError_t launch_marker_subgrid(const MarkerArgs &a, cudaStream_t s);
+// grid (subgrid diffusion 2): the grid's increments less the subgrid ones
+cudaError_t launch_marker_remainder(const MarkerArgs &a, cudaStream_t s);
 // markers: director, stress increments, rotation, and the P2Mastah hit flags
 cudaError_t launch_marker_update(const MarkerArgs &a, cudaStream_t s);
 // markers again, only when *exotic is set: the exact P2Mastah weight sums

@@ -243,7 +243,7 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
        S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
-       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_COUNT = S_MK + 28 };
+       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_COUNT = S_MK + 33 };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -1384,9 +1384,12 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
   if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
   if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
   if (md->Nx < 2 || md->Nz < 2 || mk->n < 0 || mk->n > 0x7fffffffLL) return MDZ_EINVAL;
-  if (o->subgrid_diffusion == 2) return MDZ_EUNSUPPORTED;
   if (o->interp_stencil != 1 && o->interp_stencil != 9) return MDZ_EINVAL;
   const bool el = (o->elastic == 1), dir = (o->anisotropy == 1 && o->advection == 1);
+  const bool sub = el && o->subgrid_diffusion == 2;
+  if (sub && (!o->G || !g->xc_coord || !g->zc_coord || !g->eta_phys_s || md->Nb_phases < 1 ||
+              md->Nb_phases > MDZ_MAX_PHASES))
+    return MDZ_EINVAL;
   if (!g->xg_coord || !g->zg_coord || !g->xvz_coord || !g->zvx_coord || !g->BCp_type || !g->BCg_type ||
       !mk->x || !mk->z || !mk->phase)
     return MDZ_EINVAL;
@@ -1401,6 +1404,11 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
   const size_t n = (size_t)mk->n;
   A.n = mk->n; A.Nx = md->Nx; A.Nz = md->Nz; A.periodic_x = md->periodic_x;
   A.elastic = o->elastic; A.rotation = o->stress_rotation; A.director = dir; A.stencil = o->interp_stencil;
+  A.subgrid = sub ? 1 : 0;
+  if (sub) {
+    A.np = md->Nb_phases;
+    for (int p = 0; p < A.np; p++) A.G[p] = make_divisor(o->G[p]);
+  }
   A.dt = md->dt;
   A.dx = make_divisor(g->dx); A.dz = make_divisor(g->dz);
   // P2Mastah's weight lengths, by its own expressions (ParticleRoutines.c:2218-2221)
@@ -1431,6 +1439,11 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
     A.m_szzd = (double *)mi.in((const double *)mk->szzd, S_MK + 4, n, host);
     A.m_sxz = (double *)mi.in((const double *)mk->sxz, S_MK + 5, n, host);
   }
+  if (sub) {
+    A.xc = mi.in(g->xc_coord, S_MK + 27, Nx - 1, host);
+    A.zc = mi.in(g->zc_coord, S_MK + 28, Nz - 1, host);
+    A.eta_s = mi.in(g->eta_phys_s, S_MK + 29, Nv, host);
+  }
   if (dir) {
     A.u = mi.in(g->u_in, S_MK + 18, Nx * (Nz + 1), host);
     A.v = mi.in(g->v_in, S_MK + 19, (Nx + 1) * Nz, host);
@@ -1455,6 +1468,15 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
   A.grad_s = (double2 *)sp[4];
   A.exotic = (int *)sp[5];
   A.hit = sp[5] ? (unsigned char *)sp[5] + sizeof(int) : nullptr;
+  if (sub) {
+    if (ensure(ctx->bufs[S_MK + 30], (n > 0 ? 3 * n : 1) * sizeof(double)) != MDZ_OK ||
+        ensure(ctx->bufs[S_MK + 31], 3 * Nc * sizeof(double)) != MDZ_OK ||
+        ensure(ctx->bufs[S_MK + 32], 2 * Nv * sizeof(double)) != MDZ_OK)
+      return MDZ_ENOMEM;
+    A.m_sub = (double *)ctx->bufs[S_MK + 30].p;
+    A.sum_n = (double *)ctx->bufs[S_MK + 31].p;
+    A.sum_s = (double *)ctx->bufs[S_MK + 32].p;
+  }
   // A marker at most L (1 - 2^-40) from a vertex, L the weight length, has 1 - d/L >=
   // 2^-41 on that axis once rounded, so a P2Mastah weight >= 2^-82 > 1e-30
   const auto near = [](double L) { return (L >= 0x1p-900 && L <= 0x1p900) ? L - L * 0x1p-40 : -1.0; };
@@ -1466,13 +1488,24 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (el || dir) {
     CK(launch_marker_grid(A, ctx->stream));
+    ctx->launches += 1;
+  }
+  if (sub) {
+    CK(launch_marker_subgrid(A, ctx->stream));
+    CK(launch_marker_remainder(A, ctx->stream));
+    ctx->launches += 2;
+  }
+  if (el || dir) {
     CK(launch_marker_update(A, ctx->stream));
-    ctx->launches = 2;
+    ctx->launches += 1;
   }
   if (el) {
-    CK(launch_marker_weights(A, ctx->stream));
+    if (!sub) {
+      CK(launch_marker_weights(A, ctx->stream));
+      ctx->launches += 1;
+    }
     CK(launch_marker_wxz(A, ctx->stream));
-    ctx->launches = 4;
+    ctx->launches += 1;
   }
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if (el) {

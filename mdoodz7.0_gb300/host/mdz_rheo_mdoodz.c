@@ -287,10 +287,9 @@ void ShearModCompExpGrid(grid *mesh, mat_prop *materials, params *model, scale s
 }
 
 /* UpdateParticleStress (RheologyParticles.c:1725): the markers' stress update from the
- * grid's stress change, the stress rotation and the director rotation, on the GPU.
- * subgrid_diffusion 2 is not built; it stops with a message. */
+ * grid's stress change (with subgrid stress diffusion when subgrid_diffusion is 2), the
+ * stress rotation and the director rotation, on the GPU. */
 void UpdateParticleStress(grid *mesh, markers *particles, params *model, mat_prop *materials, scale *scaling) {
-  (void)materials;
   (void)scaling;
   mdz_model md;
   mdz_marker_opts o;
@@ -299,6 +298,8 @@ void UpdateParticleStress(grid *mesh, markers *particles, params *model, mat_pro
   mdz_sweep_stats st;
   memset(&md, 0, sizeof(md));
   md.Nx = mesh->Nx; md.Nz = mesh->Nz; md.periodic_x = model->periodic_x; md.dt = model->dt;
+  md.Nb_phases = model->Nb_phases;
+  o.G = materials->G;
   o.elastic = model->elastic; o.subgrid_diffusion = model->subgrid_diffusion;
   o.stress_rotation = model->stress_rotation; o.anisotropy = model->anisotropy;
   o.advection = model->advection; o.interp_stencil = model->interp_stencil;
@@ -310,17 +311,14 @@ void UpdateParticleStress(grid *mesh, markers *particles, params *model, mat_pro
   g.sxz = mesh->sxz; g.sxz0 = mesh->sxz0;
   g.u_in = mesh->u_in; g.v_in = mesh->v_in;
   g.wxz = mesh->wxz;
+  g.xc_coord = mesh->xc_coord; g.zc_coord = mesh->zc_coord;
+  g.eta_phys_s = mesh->eta_phys_s;
   mk.n = particles->Nb_part;
   mk.x = particles->x; mk.z = particles->z; mk.phase = particles->phase;
   mk.sxxd = particles->sxxd; mk.szzd = particles->szzd; mk.sxz = particles->sxz;
   mk.nx = particles->nx; mk.nz = particles->nz;
   memset(&st, 0, sizeof(st));
   const int rc = mdz_rheo_marker_stress(mdz_context(), &md, &o, &g, &mk, MDZ_MEM_HOST, 0, &st);
-  if (rc == MDZ_EUNSUPPORTED) {
-    fprintf(stderr, "GB300 rheology: UpdateParticleStress with subgrid_diffusion = %d is not built\n",
-            model->subgrid_diffusion);
-    exit(1);
-  }
   if (rc == MDZ_EMARKER_OUT) {
     fprintf(stderr, "marker beyond the grid in x (UpdateParticleStress)\n"); /* ParticleRoutines.c:1261-1265 */
     exit(89);

@@ -310,7 +310,7 @@ class Markers(C.Structure):
 
 
 MARKER_GRID_IN = ["xg_coord", "zg_coord", "xvz_coord", "zvx_coord", "BCp_type", "BCg_type", "sxxd", "szzd", "sxxd0",
-                  "szzd0", "sxz", "sxz0", "u_in", "v_in", "wxz"]
+                  "szzd0", "sxz", "sxz0", "u_in", "v_in", "wxz", "xc_coord", "zc_coord", "eta_phys_s"]
 MARKER_ARRAYS = ["x", "z", "phase", "sxxd", "szzd", "sxz", "nx", "nz"]
 
 
@@ -320,9 +320,15 @@ class MarkerGrid(C.Structure):
 
 
 class MarkerOpts(C.Structure):
-    """mdz_marker_opts: the params switches of UpdateParticleStress."""
+    """mdz_marker_opts: the params switches of UpdateParticleStress and, for subgrid
+    diffusion 2, the per-phase shear modulus (`set_G` keeps the array alive)."""
     _fields_ = [(n, C.c_int) for n in ("elastic", "subgrid_diffusion", "stress_rotation", "anisotropy", "advection",
-                                        "interp_stencil")]
+                                        "interp_stencil")] + [("G", _P)]
+
+    def set_G(self, G):
+        self._G = np.ascontiguousarray(G, np.float64)
+        self.G = self._G.ctypes.data
+        return self
 
 
 def make_marker_structs(grid: Dict[str, object], markers: Dict[str, object], dx: float, dz: float):

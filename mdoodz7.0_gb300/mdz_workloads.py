@@ -577,7 +577,8 @@ def marker_workload(seed: int = 17, ncx: int = 2049, ncz: Optional[int] = None, 
     velocities as in velocity_field, a spin field wxz to be overwritten, and markers
     per cell at uniform random positions with random stresses and unit directors, a
     fraction `inactive` of them with phase -1, laid out cell by cell as MDOODZ seeds them.
-    Air above a wavy surface as in velocity_field.  `arrays` holds the grid fields, `info` the markers, dx and dz."""
+    Air above a wavy surface as in velocity_field.  `arrays` holds the grid fields, `info` the
+    markers, dx, dz and the per-phase shear modulus G."""
     ncz = ncx if ncz is None else ncz
     rng = np.random.default_rng(seed)
     nx, nz = ncx + 1, ncz + 1
@@ -615,6 +616,13 @@ def marker_workload(seed: int = 17, ncx: int = 2049, ncz: Optional[int] = None, 
           "phase": phase,
           "sxxd": S * rng.standard_normal(n), "szzd": S * rng.standard_normal(n), "sxz": S * rng.standard_normal(n),
           "nx": np.cos(th), "nz": np.sin(th)}
+    # for subgrid stress diffusion: centroid coordinates, the vertex viscosity (Maxwell
+    # times eta/G from 1e-2 to 1e2 of dt = 1e11 s) and the shear modulus of the 3 phases
+    a["xc_coord"], a["zc_coord"] = running(xmin + dx / 2.0, dx, ncx), running(zmin + dz / 2.0, dz, ncz)
+    rng2 = np.random.default_rng(seed + 7)
+    a["eta_phys_s"] = 10.0 ** rng2.uniform(19.0, 23.0, nv) / sc.eta
+    G = np.array([3e10, 2.5e10, 4e10]) / sc.S
     model = make_model(ncx, ncz, 3, sc=sc)  # marker phases 0..2
     model.periodic_x = periodic
-    return Workload("markers", model, None, a, info=dict(seed=seed, ncx=ncx, ncz=ncz, dx=dx, dz=dz, markers=mk))
+    return Workload("markers", model, None, a,
+                    info=dict(seed=seed, ncx=ncx, ncz=ncz, dx=dx, dz=dz, markers=mk, G=G))

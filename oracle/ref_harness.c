@@ -21,6 +21,7 @@
 
 #include "mdoodz-private.h"
 #include "../include/mdz_rheo.h"
+#include <omp.h>
 
 static void fill_materials(mat_prop *mp, const mdz_materials *m) {
   memset(mp, 0, sizeof(*mp));
@@ -296,12 +297,22 @@ int ref_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_g
   g->sxz = W(mg->sxz); g->sxz0 = W(mg->sxz0);
   g->u_in = W(mg->u_in); g->v_in = W(mg->v_in);
   g->wxz = mg->wxz;
+  g->xc_coord = W(mg->xc_coord); g->zc_coord = W(mg->zc_coord);
+  g->eta_phys_s = W(mg->eta_phys_s);
+  if (o->G)
+    for (int p = 0; p < m->Nb_phases && p < 20; p++) mp->G[p] = o->G[p];
   markers P;
   memset(&P, 0, sizeof(P));
   P.Nb_part = (int)mk->n;
   P.x = (double *)mk->x; P.z = (double *)mk->z; P.phase = (int *)mk->phase;
   P.sxxd = mk->sxxd; P.szzd = mk->szzd; P.sxz = mk->sxz; P.nx = mk->nx; P.nz = mk->nz;
+  /* one thread: P2Mastah's sums (subgrid diffusion 2) then run in marker order, the
+   * order the restatement sums in; with more threads the reference's own result moves
+   * in the last bits with the thread count */
+  const int threads = omp_get_max_threads();
+  omp_set_num_threads(1);
   UpdateParticleStress(g, &P, &pm, mp, &sc);
+  omp_set_num_threads(threads);
   free_grid(g);
   free(mp);
   return 0;

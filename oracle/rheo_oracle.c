@@ -1510,9 +1510,167 @@ static double orc_c2p_skip(const double *F, const signed char *tag, const int c[
   return v;
 }
 
+/* Interp_Grid2P (ParticleRoutines.c:1223-1321) for one active marker: the vertex cell of
+ * (x - X[0]) / dx clamped to the grid (beyond it in x the reference exits with 89), the
+ * weights of |x - X[j]|, an air corner (30, 31) replaced by the corner across, no
+ * normalisation. */
+static double orc_v2p(const double *F, const signed char *tag, double x, double z, const double *X, const double *Z,
+                      int Nx, int Nz, double dx, double dz, int *status) {
+  int j = (int)ceil((x - X[0]) / dx) - 1;
+  if (j < 0) j = 0;
+  if (j > Nx - 2) { j = Nx - 2; *status = MDZ_EMARKER_OUT; }
+  int i = (int)ceil((z - Z[0]) / dz) - 1;
+  if (i < 0) i = 0;
+  if (i > Nz - 2) i = Nz - 2;
+  const int cv[4] = {j + i * Nx, j + i * Nx + 1, j + (i + 1) * Nx, j + (i + 1) * Nx + 1};
+  const int alt[4] = {cv[2], cv[3], cv[0], cv[1]};
+  double w[4];
+  orc_weights(fabs(x - X[j]), fabs(z - Z[i]), dx, dz, w);
+  double v = 0.0;
+  for (int q = 0; q < 4; q++) v += w[q] * F[orc_air(tag[cv[q]]) ? alt[q] : cv[q]];
+  return v;
+}
+
+/* P2Mastah's sums (ParticleRoutines.c:2288-2575) over the active markers in order, on a
+ * grid of Nxn x Nzn nodes at X, Z: WM += w and, when BM is given, BM += val * w at the
+ * marker's nearest node and, with the 9-node stencil, the eight around it (N, S, E, W,
+ * SW, NW, NE, SE, as in the reference), wrapped in x when periodic.  One thread of the
+ * reference sums in this order. */
+static void orc_p2m(const mdz_markers *mk, const double *val, const double *X, const double *Z, int Nxn, int Nzn,
+                    double dx, double dz, int stencil, int per, double *WM, double *BM) {
+  const double dx_itp = (stencil == 9) ? 3.0 * dx / 2.0 : dx / 2.0;
+  const double dz_itp = (stencil == 9) ? 3.0 * dz / 2.0 : dz / 2.0;
+  for (int64_t p = 0; p < mk->n; p++) {
+    if (mk->phase[p] == -1) continue;
+    const double x = mk->x[p], z = mk->z[p], mv = val ? val[p] : 0.0;
+    int ip = (int)ceil((x - X[0]) / dx + 0.5) - 1, jp = (int)ceil((z - Z[0]) / dz + 0.5) - 1;
+    if (ip < 0) ip = 0;
+    if (ip > Nxn - 1) ip = Nxn - 1;
+    if (jp < 0) jp = 0;
+    if (jp > Nzn - 1) jp = Nzn - 1;
+    const double Xp = X[ip], Zp = Z[jp];
+#define ORC_W(cond, kk, xx, zz)                                                        \
+    if (cond) {                                                                        \
+      const int64_t kp_ = (kk);                                                        \
+      const double w_ = (1.0 - fabs(xx - x) / dx_itp) * (1.0 - fabs(zz - z) / dz_itp); \
+      WM[kp_] += w_;                                                                   \
+      if (BM) BM[kp_] += mv * w_;                                                      \
+    }
+    ORC_W(1, ip + (int64_t)jp * Nxn, Xp, Zp);
+    if (stencil == 9) {
+      const int peE = (ip == Nxn - 1 && per == 1), peW = (ip == 0 && per == 1);
+      const double xE = Xp + dx, xW = Xp - dx, zN = Zp + dz, zS = Zp - dz;
+      const int kE = ip + 1 - peE * Nxn, kW = ip - 1 + peW * Nxn;
+      ORC_W(jp < Nzn - 1, ip + (int64_t)(jp + 1) * Nxn, Xp, zN);
+      ORC_W(jp > 0, ip + (int64_t)(jp - 1) * Nxn, Xp, zS);
+      ORC_W(ip < Nxn - 1 || peE, kE + (int64_t)jp * Nxn, xE, Zp);
+      ORC_W(ip > 0 || peW, kW + (int64_t)jp * Nxn, xW, Zp);
+      ORC_W(jp > 0 && (ip > 0 || peW), kW + (int64_t)(jp - 1) * Nxn, xW, zS);
+      ORC_W(jp < Nzn - 1 && (ip > 0 || peW), kW + (int64_t)(jp + 1) * Nxn, xW, zN);
+      ORC_W(jp < Nzn - 1 && (ip < Nxn - 1 || peE), kE + (int64_t)(jp + 1) * Nxn, xE, zN);
+      ORC_W(jp > 0 && (ip < Nxn - 1 || peE), kE + (int64_t)(jp - 1) * Nxn, xE, zS);
+    }
+#undef ORC_W
+  }
+}
+
+/* P2Mastah's node values (flag 1, avg 0; :2603-2641): BM / WM where |WM| reaches 1e-30
+ * away from air, else F keeps its value; with periodic x the two ends of each row of a
+ * vertex field take their mean. */
+static void orc_p2m_nodes(double *F, const double *WM, const double *BM, const signed char *tag, int Nxn, int Nzn,
+                          int vertex, int per) {
+  for (int64_t i = 0; i < (int64_t)Nxn * Nzn; i++)
+    if (!(fabs(WM[i]) < 1e-30 || orc_air(tag[i]))) F[i] = BM[i] / WM[i];
+  if (vertex && per == 1)
+    for (int l = 0; l < Nzn; l++) {
+      const int64_t c1 = (int64_t)l * Nxn + Nxn - 1, c = (int64_t)l * Nxn;
+      const double av = 0.5 * (F[c1] + F[c]);
+      F[c1] = av; F[c] = av;
+    }
+}
+
+/* UpdateParticleStress with subgrid_diffusion 2 (RheologyParticles.c:1811-1903): the old
+ * grid stresses and the vertex viscosity go to the markers; each active marker relaxes
+ * towards the old stress over its Maxwell time (the subgrid increment); P2Mastah takes
+ * the subgrid increments to the grid; what remains of the grid's increment comes back
+ * to the markers, and both are added to the marker stress. */
+static int orc_subgrid_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_grid *g, mdz_markers *mk,
+                              int status) {
+  const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1, per = m->periodic_x;
+  const int64_t Nc = (int64_t)Ncx * Ncz, Nv = (int64_t)Nx * Nz, n = mk->n;
+  const double dx = g->dx, dz = g->dz, dt = m->dt, d = 1.0;
+  double *ms = calloc(3 * (size_t)(n > 0 ? n : 1), sizeof(double)); /* dtxxms, dtzzms, dtxzms */
+  double *gs = calloc(4 * (size_t)Nc + 2 * (size_t)Nv, sizeof(double)); /* 4 centroid, 2 vertex fields */
+  double *wmc = calloc(3 * (size_t)Nc, sizeof(double)), *wmv = calloc(2 * (size_t)Nv, sizeof(double));
+  double *dtxxms = ms, *dtzzms = ms + n, *dtxzms = ms + 2 * n;
+  double *dtxxgs = gs, *dtzzgs = gs + Nc, *dtxzgs = gs + 2 * Nc, *dtxxgr = gs + 2 * Nc + Nv,
+         *dtzzgr = dtxxgr + Nc, *dtxzgr = dtzzgr + Nc;
+  for (int64_t p = 0; p < n; p++) {
+    if (mk->phase[p] == -1) continue;
+    const int ph = mk->phase[p];
+    if (ph < 0 || ph >= m->Nb_phases) { status = MDZ_EINVAL; continue; }
+    const double x = mk->x[p], z = mk->z[p];
+    int jp, ip, c[4];
+    double w[4], txxm0 = 0.0, tzzm0 = 0.0;
+    if (orc_cell_corners(x, z, g->xvz_coord, g->zvx_coord, Ncx, Ncz, dx, dz, per, &jp, &ip, c) != 0) {
+      status = MDZ_EMARKER_OUT;
+    } else {
+      orc_weights(x - g->xvz_coord[jp], z - g->zvx_coord[ip], dx, dz, w);
+      txxm0 = orc_c2p_sub(g->sxxd0, g->BCp_type, c, w);
+      tzzm0 = orc_c2p_sub(g->szzd0, g->BCp_type, c, w);
+      if (isinf(txxm0) || isinf(tzzm0)) status = MDZ_ENONFINITE; /* ParticleRoutines.c:1565-1569 */
+    }
+    const double txzm0 = orc_v2p(g->sxz0, g->BCg_type, x, z, g->xg_coord, g->zg_coord, Nx, Nz, dx, dz, &status);
+    const double etam = orc_v2p(g->eta_phys_s, g->BCg_type, x, z, g->xg_coord, g->zg_coord, Nx, Nz, dx, dz, &status);
+    const double dtaum = etam / o->G[ph];
+    const double f = 1.0 - exp(-d * dt / dtaum);
+    dtxxms[p] = -(mk->sxxd[p] - txxm0) * f;
+    dtzzms[p] = -(mk->szzd[p] - tzzm0) * f;
+    dtxzms[p] = -(mk->sxz[p] - txzm0) * f;
+    if (isinf(dtxxms[p]) || isnan(dtxxms[p])) status = MDZ_ENONFINITE; /* :1846-1855, exit 1 */
+  }
+  /* subgrid increments markers -> grid, three P2Mastah calls (:1859-1861) */
+  orc_p2m(mk, dtxxms, g->xc_coord, g->zc_coord, Ncx, Ncz, dx, dz, o->interp_stencil, per, wmc, wmc + Nc);
+  orc_p2m_nodes(dtxxgs, wmc, wmc + Nc, g->BCp_type, Ncx, Ncz, 0, per);
+  memset(wmc, 0, 2 * (size_t)Nc * sizeof(double));
+  orc_p2m(mk, dtzzms, g->xc_coord, g->zc_coord, Ncx, Ncz, dx, dz, o->interp_stencil, per, wmc, wmc + Nc);
+  orc_p2m_nodes(dtzzgs, wmc, wmc + Nc, g->BCp_type, Ncx, Ncz, 0, per);
+  orc_p2m(mk, dtxzms, g->xg_coord, g->zg_coord, Nx, Nz, dx, dz, o->interp_stencil, per, wmv, wmv + Nv);
+  orc_p2m_nodes(dtxzgs, wmv, wmv + Nv, g->BCg_type, Nx, Nz, 1, per);
+  /* remaining increments on the grid (:1864-1872) */
+  for (int64_t c0 = 0; c0 < Nc; c0++)
+    if (!orc_air(g->BCp_type[c0])) {
+      dtxxgr[c0] = (g->sxxd[c0] - g->sxxd0[c0]) - dtxxgs[c0];
+      dtzzgr[c0] = (g->szzd[c0] - g->szzd0[c0]) - dtzzgs[c0];
+    }
+  for (int64_t c1 = 0; c1 < Nv; c1++)
+    if (g->BCg_type[c1] != 30) dtxzgr[c1] = (g->sxz[c1] - g->sxz0[c1]) - dtxzgs[c1];
+  /* remaining increments grid -> markers and the final update (:1875-1885) */
+  for (int64_t p = 0; p < n; p++) {
+    if (mk->phase[p] == -1) continue;
+    const double x = mk->x[p], z = mk->z[p];
+    int jp, ip, c[4];
+    double w[4], dtxxmr = 0.0, dtzzmr = 0.0;
+    if (orc_cell_corners(x, z, g->xvz_coord, g->zvx_coord, Ncx, Ncz, dx, dz, per, &jp, &ip, c) == 0) {
+      orc_weights(x - g->xvz_coord[jp], z - g->zvx_coord[ip], dx, dz, w);
+      dtxxmr = orc_c2p_sub(dtxxgr, g->BCp_type, c, w);
+      dtzzmr = orc_c2p_sub(dtzzgr, g->BCp_type, c, w);
+      if (isinf(dtxxmr) || isinf(dtzzmr)) status = MDZ_ENONFINITE;
+    }
+    const double dtxzmr = orc_v2p(dtxzgr, g->BCg_type, x, z, g->xg_coord, g->zg_coord, Nx, Nz, dx, dz, &status);
+    mk->sxxd[p] = mk->sxxd[p] + dtxxms[p] + dtxxmr;
+    mk->szzd[p] = mk->szzd[p] + dtzzms[p] + dtzzmr;
+    mk->sxz[p] = mk->sxz[p] + dtxzms[p] + dtxzmr;
+  }
+  free(ms); free(gs); free(wmc); free(wmv);
+  return status;
+}
+
 int orc_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_grid *g, mdz_markers *mk) {
   if (m->Nx < 2 || m->Nz < 2) return MDZ_EINVAL;
-  if (o->subgrid_diffusion == 2) return MDZ_EUNSUPPORTED;
+  if (o->elastic == 1 && o->subgrid_diffusion == 2 &&
+      (!o->G || !g->xc_coord || !g->zc_coord || !g->eta_phys_s || m->Nb_phases < 1))
+    return MDZ_EINVAL;
   const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1, per = m->periodic_x;
   const int64_t Nc = (int64_t)Ncx * Ncz, Nv = (int64_t)Nx * Nz, n = mk->n;
   const double dx = g->dx, dz = g->dz, dt = m->dt;
@@ -1574,8 +1732,9 @@ int orc_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_g
   free(dudx_n); free(dvdz_n); free(dudz_s); free(dvdx_s);
   if (o->elastic != 1) return status;
 
+  if (o->subgrid_diffusion == 2) status = orc_subgrid_stress(m, o, g, mk, status);
   /* stress increments grid -> markers (:1919-1966), then ArrayPlusArray on every marker */
-  for (int64_t p = 0; p < n; p++) {
+  for (int64_t p = 0; p < n && o->subgrid_diffusion != 2; p++) {
     double dsx = 0.0, dsz = 0.0, dsxz = 0.0;
     if (mk->phase[p] != -1) {
       const double x = mk->x[p], z = mk->z[p];
@@ -1625,36 +1784,7 @@ int orc_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_g
    * 0 / (sum of marker weights) wherever that sum reaches 1e-30 below the surface; the
    * marker spin stays zero and the rotation below turns by zero */
   double *WM = calloc(Nv, sizeof(double));
-  const double dx_itp = (o->interp_stencil == 9) ? 3.0 * dx / 2.0 : dx / 2.0;
-  const double dz_itp = (o->interp_stencil == 9) ? 3.0 * dz / 2.0 : dz / 2.0;
-  for (int64_t p = 0; p < n; p++) {
-    if (mk->phase[p] == -1) continue;
-    const double x = mk->x[p], z = mk->z[p];
-    int ip = (int)ceil((x - g->xg_coord[0]) / dx + 0.5) - 1, jp = (int)ceil((z - g->zg_coord[0]) / dz + 0.5) - 1;
-    if (ip < 0) ip = 0;
-    if (ip > Nx - 1) ip = Nx - 1;
-    if (jp < 0) jp = 0;
-    if (jp > Nz - 1) jp = Nz - 1;
-    const double X = g->xg_coord[ip], Z = g->zg_coord[jp];
-    WM[ip + jp * Nx] += (1.0 - fabs(X - x) / dx_itp) * (1.0 - fabs(Z - z) / dz_itp);
-    if (o->interp_stencil == 9) { /* ParticleRoutines.c:2378-2575 */
-      const int peE = (ip == Nx - 1 && per == 1), peW = (ip == 0 && per == 1);
-      const double xE = X + dx, xW = X - dx, zN = Z + dz, zS = Z - dz;
-      const int kE = ip + 1 - peE * Nx, kW = ip - 1 + peW * Nx;
-#define ORC_W(cond, kk, xx, zz) \
-      if (cond) WM[kk] += (1.0 - fabs(xx - x) / dx_itp) * (1.0 - fabs(zz - z) / dz_itp)
-      /* N, S, E, W, SW, NW, NE, SE, as in the reference */
-      ORC_W(jp < Nz - 1, ip + (jp + 1) * Nx, X, zN);
-      ORC_W(jp > 0, ip + (jp - 1) * Nx, X, zS);
-      ORC_W(ip < Nx - 1 || peE, kE + jp * Nx, xE, Z);
-      ORC_W(ip > 0 || peW, kW + jp * Nx, xW, Z);
-      ORC_W(jp > 0 && (ip > 0 || peW), kW + (jp - 1) * Nx, xW, zS);
-      ORC_W(jp < Nz - 1 && (ip > 0 || peW), kW + (jp + 1) * Nx, xW, zN);
-      ORC_W(jp < Nz - 1 && (ip < Nx - 1 || peE), kE + (jp + 1) * Nx, xE, zN);
-      ORC_W(jp > 0 && (ip < Nx - 1 || peE), kE + (jp - 1) * Nx, xE, zS);
-#undef ORC_W
-    }
-  }
+  orc_p2m(mk, NULL, g->xg_coord, g->zg_coord, Nx, Nz, dx, dz, o->interp_stencil, per, WM, NULL);
   for (int64_t c1 = 0; c1 < Nv; c1++)
     if (!(fabs(WM[c1]) < 1e-30 || orc_air(g->BCg_type[c1]))) g->wxz[c1] = 0.0 / WM[c1];
   if (per == 1)

@@ -104,6 +104,10 @@ MARKER_CASES = {
                                                                 periodic=1), 1, 0, 0, 1, 9),
     "director_only": (lambda: W.marker_workload(seed=45, ncx=11, ncz=13, markers_per_cell=4, air=0.25),
                       0, 1, 1, 1, 1),
+    # (builder, elastic, rotation, anisotropy, advection, stencil, subgrid_diffusion)
+    "subgrid2_jaumann": (lambda: W.marker_workload(seed=46, ncx=14, ncz=12, markers_per_cell=4), 1, 1, 0, 1, 1, 2),
+    "subgrid2_stencil9_director_air_periodic": (lambda: W.marker_workload(seed=47, ncx=13, ncz=11, markers_per_cell=6,
+                                                                          air=0.25, periodic=1), 1, 2, 1, 1, 9, 2),
 }
 
 def _dilatant_density(w):

@@ -82,10 +82,12 @@ def load_prep_inputs(g):
     return model, mat, a
 
 
-def marker_opts(elastic, rot, aniso, adv, stencil):
+def marker_opts(elastic, rot, aniso, adv, stencil, subgrid=0, G=None):
     o = R.MarkerOpts()
-    o.elastic, o.subgrid_diffusion, o.stress_rotation = elastic, 0, rot
+    o.elastic, o.subgrid_diffusion, o.stress_rotation = elastic, subgrid, rot
     o.anisotropy, o.advection, o.interp_stencil = aniso, adv, stencil
+    if G is not None:
+        o.set_G(G)
     return o
 
 
@@ -95,7 +97,13 @@ def marker_inputs(w):
     out.update({"mk_" + k: np.array(v) for k, v in w.info["markers"].items()})
     out["model_bytes"] = np.frombuffer(bytes(w.model), np.uint8)
     out["spacing"] = np.array([w.info["dx"], w.info["dz"]])
+    out["mat_G"] = np.array(w.info["G"])
     return out
+
+
+def load_marker_G(g):
+    """The per-phase shear modulus of a marker fixture (None for fixtures without one)."""
+    return np.array(g["mat_G"]) if "mat_G" in g.files else None
 
 
 def load_marker_inputs(g):
@@ -120,11 +128,15 @@ def grid_outputs(arrays):
     return out
 
 
-def main():
+def main(only=()):
+    """Every fixture group, or only the groups named (grid, operators, strain_rates,
+    softening, shear_modulus, markers, points)."""
     O.build(ref=True)
     if O.reference() is None:
         sys.exit("the reference tree is needed to generate golden fixtures")
     for name, (builder, aniso, fu) in cases.GRID_CASES.items():
+        if only and "grid" not in only:
+            break
         w = builder()
         dig = grid_inputs_digest(w)
         a = {k: ([x.copy() for x in v] if isinstance(v, list) else v.copy()) for k, v in w.arrays.items()}
@@ -132,6 +144,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"grid_{name}.npz"), inputs_sha256=dig, **grid_outputs(a))
         print("grid", name, w.nodes, "nodes")
     for name, (grid_case, jac, comp) in cases.OPERATOR_CASES.items():
+        if only and "operators" not in only:
+            break
         builder, aniso, fu = cases.GRID_CASES[grid_case]
         w = builder()
         O.ref_sweep(w.model, w.mat, R.FieldSet(w.arrays), final_update=fu, aniso=aniso)
@@ -141,6 +155,8 @@ def main():
                             **ops)
         print("operators", name)
     for name, (builder, oop, comp) in cases.STRAIN_CASES.items():
+        if only and "strain_rates" not in only:
+            break
         w = builder()
         dig = digest(w.arrays, STRAIN_INPUTS)
         O.ref_strain_rates(w.model, w.info["dx"], w.info["dz"], w.arrays, oop, comp)
@@ -148,6 +164,8 @@ def main():
                             **{k: w.arrays[k] for k in R.SR_N + R.SR_S})
         print("strain rates", name)
     for name, (builder, smooth, hard, noise, stencil) in cases.SOFTENING_CASES.items():
+        if only and "softening" not in only:
+            break
         w = builder()
         mk = dict(w.info["markers"], interp_stencil=stencil)
         dig = prep_inputs_digest(w)
@@ -158,6 +176,8 @@ def main():
                             **{k: w.arrays[k] for k in R.SOFT_N + R.SOFT_S})
         print("softening", name)
     for name, builder in cases.SHEAR_CASES.items():
+        if only and "shear_modulus" not in only:
+            break
         w = builder()
         dig = prep_inputs_digest(w)
         inputs = prep_inputs(w)
@@ -165,9 +185,11 @@ def main():
         np.savez_compressed(os.path.join(HERE, f"shear_modulus_{name}.npz"), inputs_sha256=dig, **inputs,
                             **{k: w.arrays[k] for k in R.MOD_N + R.MOD_S})
         print("shear modulus", name)
-    for name, (builder, elastic, rot, aniso, adv, stencil) in cases.MARKER_CASES.items():
+    for name, (builder, *o) in cases.MARKER_CASES.items():
+        if only and "markers" not in only:
+            break
         w = builder()
-        opts = marker_opts(elastic, rot, aniso, adv, stencil)
+        opts = marker_opts(*o, G=w.info["G"])
         inputs = marker_inputs(w)
         grid = {k: w.arrays[k].copy() for k in w.arrays}
         mk = {k: v.copy() for k, v in w.info["markers"].items()}
@@ -176,6 +198,8 @@ def main():
                             **{"out_" + k: mk[k] for k in ("sxxd", "szzd", "sxz", "nx", "nz")}, out_wxz=grid["wxz"])
         print("markers", name)
     for name in cases.POINT_CASES:
+        if only and "points" not in only:
+            break
         md, m, pin, aniso, centroid, fu = cases.point_case(name)
         n = pin["phase"].size
         out = cases.alloc_point_outputs(n)
@@ -187,4 +211,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

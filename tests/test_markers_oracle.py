@@ -11,7 +11,7 @@ import mdz_rheo as R
 import mdz_workloads as W
 import oracle_lib as O
 from golden import cases
-from golden.make_golden import load_marker_inputs, marker_opts
+from golden.make_golden import load_marker_G, load_marker_inputs, marker_opts
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 need_ref = pytest.mark.skipif(O.reference() is None, reason="reference build absent (oracle/_ref)")
@@ -83,22 +83,35 @@ CASES = {
     "one_column_of_cells": (lambda: W.marker_workload(seed=8, ncx=1, ncz=9, markers_per_cell=6), 1, 1, 1, 1, 1),
     "markers_on_boundaries": (boundary_workload, 1, 1, 1, 1, 9),
     "tiny_weights": (tiny_weight_workload, 1, 1, 0, 1, 1),
+    # subgrid_diffusion 2, the last element
+    "subgrid2_jaumann_air": (lambda: W.marker_workload(seed=12, ncx=23, ncz=19, air=0.2), 1, 1, 0, 1, 1, 2),
+    "subgrid2_periodic_stencil9_director": (lambda: W.marker_workload(seed=13, ncx=21, ncz=17, markers_per_cell=9,
+                                                                      periodic=1, air=0.15), 1, 2, 1, 1, 9, 2),
+    "subgrid2_typical_scale": (lambda: W.marker_workload(seed=14, ncx=16, ncz=18, markers_per_cell=8, sc=W.TYPICAL),
+                               1, 0, 0, 1, 1, 2),
+    "subgrid2_markers_on_boundaries": (boundary_workload, 1, 1, 0, 1, 9, 2),
+    "subgrid2_tiny_weights": (tiny_weight_workload, 1, 1, 0, 1, 1, 2),
+    "subgrid2_one_column_of_cells": (lambda: W.marker_workload(seed=15, ncx=1, ncz=9, markers_per_cell=6),
+                                     1, 1, 0, 1, 9, 2),
 }
+
+
+def opts_of(name, w):
+    return marker_opts(*CASES[name][1:], G=w.info["G"])
 
 
 @need_ref
 @pytest.mark.parametrize("name", list(CASES))
 def test_marker_stress_restatement_is_the_reference(name):
-    make, *o = CASES[name]
-    w = make()
-    opts = marker_opts(*o)
+    w = CASES[name][0]()
+    opts = opts_of(name, w)
     ra, ga, ma = run(O.ref_marker_stress, w, opts)
     rb, gb, mb = run(O.orc_marker_stress, w, opts)
     assert ra == 0 and rb == R.MDZ_OK
     for k in OUT:
         assert same(ma[k], mb[k]), k
     assert same(ga["wxz"], gb["wxz"])
-    if o[0] == 1:
+    if opts.elastic == 1:
         assert np.any(ma["sxxd"] != w.info["markers"]["sxxd"]) and np.any(ga["wxz"] != w.arrays["wxz"])
 
 
@@ -106,7 +119,7 @@ def test_marker_stress_restatement_is_the_reference(name):
 def test_oracle_marker_stress_matches_golden(name):
     g = np.load(os.path.join(GOLDEN, f"markers_{name}.npz"))
     model, grid, mk, dx, dz = load_marker_inputs(g)
-    opts = marker_opts(*cases.MARKER_CASES[name][1:])
+    opts = marker_opts(*cases.MARKER_CASES[name][1:], G=load_marker_G(g))
     assert O.orc_marker_stress(model, opts, grid, mk, dx, dz) == R.MDZ_OK
     for k in OUT:
         assert same(mk[k], g["out_" + k]), k
@@ -114,11 +127,11 @@ def test_oracle_marker_stress_matches_golden(name):
 
 
 @need_shim
-@pytest.mark.parametrize("name", ["analytical_director", "periodic_stencil9_director"])
+@pytest.mark.parametrize("name", ["analytical_director", "periodic_stencil9_director",
+                                  "subgrid2_periodic_stencil9_director"])
 def test_drop_in_marker_stress_matches_reference(name):
-    make, *o = CASES[name]
-    w = make()
-    opts = marker_opts(*o)
+    w = CASES[name][0]()
+    opts = opts_of(name, w)
     _, ga, ma = run(lambda *a: O.shim_marker_stress(*a, drop_in=False), w, opts)
     _, gb, mb = run(lambda *a: O.shim_marker_stress(*a, drop_in=True), w, opts)
     for k in OUT:
@@ -145,7 +158,30 @@ def test_marker_beyond_grid_and_subgrid_diffusion_status():
     w.info["markers"]["x"][5] = w.arrays["xg_coord"][-1] + 0.7 * w.info["dx"]
     rc, _, _ = run(O.orc_marker_stress, w, marker_opts(1, 1, 0, 1, 1))
     assert rc == R.MDZ_EMARKER_OUT
-    o = marker_opts(1, 1, 0, 1, 1)
-    o.subgrid_diffusion = 2
-    rc, _, _ = run(O.orc_marker_stress, W.marker_workload(seed=11, ncx=8, ncz=8), o)
-    assert rc == R.MDZ_EUNSUPPORTED
+    rc, _, _ = run(O.orc_marker_stress, w, marker_opts(1, 1, 0, 1, 1, 2, G=w.info["G"]))
+    assert rc == R.MDZ_EMARKER_OUT
+    w = W.marker_workload(seed=11, ncx=8, ncz=8)
+    rc, _, _ = run(O.orc_marker_stress, w, marker_opts(1, 1, 0, 1, 1, 2))  # no shear modulus
+    assert rc == R.MDZ_EINVAL
+    w.info["markers"]["phase"][3] = 3  # a phase the model does not have
+    rc, _, _ = run(O.orc_marker_stress, w, marker_opts(1, 1, 0, 1, 1, 2, G=w.info["G"]))
+    assert rc == R.MDZ_EINVAL
+    w.info["markers"]["phase"][3] = 0
+    w.arrays["eta_phys_s"][:] = 0.0  # zero Maxwell time: exp(-inf) = 0, a full relaxation, still finite
+    rc, _, _ = run(O.orc_marker_stress, w, marker_opts(1, 1, 0, 1, 1, 2, G=w.info["G"]))
+    assert rc == R.MDZ_OK
+
+
+@pytest.mark.parametrize("stencil", [1, 9])
+def test_subgrid_diffusion_without_relaxation_is_the_plain_update(stencil):
+    """With Maxwell times so long that exp(-dt/t) rounds to 1, the subgrid increments
+    are zero, P2Mastah brings zeros to the grid, and what comes back is the grid's whole
+    increment: the update of subgrid_diffusion 0, bit for bit."""
+    w = W.marker_workload(seed=16, ncx=19, ncz=15, air=0.2, periodic=1)
+    w.arrays["eta_phys_s"][:] = 1e40
+    r0, g0, m0 = run(O.orc_marker_stress, w, marker_opts(1, 1, 1, 1, stencil))
+    r2, g2, m2 = run(O.orc_marker_stress, w, marker_opts(1, 1, 1, 1, stencil, 2, G=w.info["G"]))
+    assert r0 == r2 == R.MDZ_OK
+    for k in OUT:
+        assert same(m0[k], m2[k]), k
+    assert same(g0["wxz"], g2["wxz"])
