@@ -27,6 +27,8 @@
  *   mdz_rheo_shear_modulus  <- ShearModCompExpGrid, def MDLIB/RheologyDensity.c:1634
  *   mdz_rheo_marker_stress  <- UpdateParticleStress
  *                              MDLIB/mdoodz-private.h:415, def MDLIB/RheologyParticles.c:1725
+ *   mdz_rheo_p2mastah       <- P2Mastah for marker arrays onto centroids or vertices
+ *                              MDLIB/mdoodz-private.h:350, def MDLIB/ParticleRoutines.c:2170
  *
  * All arithmetic is IEEE binary64.  Unless a call says otherwise it is
  * synchronous (returns after the results are in the caller's buffers), like
@@ -421,6 +423,24 @@ typedef struct mdz_marker_opts {
 int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_opts *opts,
                            mdz_marker_grid *grid, mdz_markers *markers, int mem, int flags,
                            mdz_sweep_stats *stats);
+
+/* P2Mastah (MDLIB/ParticleRoutines.c:2170-2665) for a marker array (flag 1) onto the
+ * centroids (node_n, Nx-1 by Nz-1, at xc_coord/zc_coord, skipping BCp air) and/or the
+ * vertices (node_s, Nx by Nz, at xg_coord/zg_coord, skipping BCg air): every active
+ * marker spreads its value with the weights (1 - |X - x|/L)(1 - |Z - z|/L') over its
+ * nearest node (interp_stencil 1, L = dx/2) or the 3 x 3 nodes around it (9, L = 3dx/2);
+ * a node whose weight sum WM reaches 1e-30 takes sum(w v) / WM (avg 0), the harmonic
+ * mean (avg 1: values 1/v, node 1/mean) or the geometric mean (avg 2: log v, exp of the
+ * mean); other nodes keep their value.  With periodic_x the two ends of each vertex row
+ * take their mean.  Used by CohesionFrictionDilationGrid (RheologyDensity.c:1552-1553)
+ * for the plastic strain.  The reference sums per OpenMP thread, so its last bits follow
+ * its thread count; these sums run in another order: results within 1e-13 of the
+ * field's scale.  model supplies Nx, Nz, Nb_phases (marker phases must be below it:
+ * MDZ_EINVAL) and periodic_x; grid the spacing, coordinates and BC flags; markers x, z,
+ * phase and n.  `mem`, `flags` and `stats` as for mdz_rheo_strain_rates. */
+int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_grid *grid,
+                      const mdz_markers *markers, const double *values, int avg, int interp_stencil,
+                      double *node_n, double *node_s, int mem, int flags, mdz_sweep_stats *stats);
 
 /* ---- allocation-free variant (no reference counterpart) ----------------
  * mdz_rheo_points on the CURRENT device without any context and without allocating:

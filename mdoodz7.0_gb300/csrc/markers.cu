@@ -575,6 +575,67 @@ __global__ void __launch_bounds__(256) k_marker_wxz(const MarkerArgs A) {
   A.wxz[c1] = wxz_after(A, c1, exact);
 }
 
+// P2Mastah of a marker array (ParticleRoutines.c:2288-2575): the sums of w and w v on
+// the centroids (sum_n) and vertices (sum_s), v the marker's value, 1/v or log v
+__global__ void __launch_bounds__(256) k_p2m_scatter(const MarkerArgs A) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= A.n) return;
+  const int ph = A.phase[k];
+  if (ph == -1) return;
+  if (ph < 0 || ph >= A.np) { report(A, k, MDZ_EINVAL); return; }
+  const double x = A.x[k], z = A.z[k];
+  double v = A.val[k];
+  if (A.avg == 1) v = 1.0 / v;
+  else if (A.avg == 2) v = log(v);
+  if (A.out_n) {
+    const int Ncx = A.Nx - 1, Ncz = A.Nz - 1;
+    const long long Nc = (long long)Ncx * Ncz;
+    const int hx = cell_pair(__dsub_rn(x, A.xc[0]), A.dx).h, hz = cell_pair(__dsub_rn(z, A.zc[0]), A.dz).h;
+    p2m_exact(A, A.xc, A.zc, Ncx, Ncz, x, z, hx, hz, [&](long long node, double w) {
+      atomicAdd(&A.sum_n[node], w);
+      atomicAdd(&A.sum_n[Nc + node], __dmul_rn(v, w));
+    });
+  }
+  if (A.out_s) {
+    const long long Nv = (long long)A.Nx * A.Nz;
+    const int hx = cell_pair(__dsub_rn(x, A.xg[0]), A.dx).h, hz = cell_pair(__dsub_rn(z, A.zg[0]), A.dz).h;
+    p2m_exact(A, A.xg, A.zg, A.Nx, A.Nz, x, z, hx, hz, [&](long long node, double w) {
+      atomicAdd(&A.sum_s[node], w);
+      atomicAdd(&A.sum_s[Nv + node], __dmul_rn(v, w));
+    });
+  }
+}
+
+// the node value P2Mastah writes (:2603-2631), or the one the node keeps
+__device__ __forceinline__ double p2m_node(const MarkerArgs &A, double W, double BM, bool air_node, double old) {
+  if (air_node || fp64_abs_lt(W, 1e-30)) return old;
+  const double m = BM / W;
+  return A.avg == 1 ? 1.0 / m : (A.avg == 2 ? exp(m) : m);
+}
+
+__global__ void __launch_bounds__(256) k_p2m_nodes(const MarkerArgs A) {
+  const long long Nc = (long long)(A.Nx - 1) * (A.Nz - 1), Nv = (long long)A.Nx * A.Nz;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < Nc) {
+    if (A.out_n) A.out_n[t] = p2m_node(A, A.sum_n[t], A.sum_n[Nc + t], air(A.bcp[t]), A.out_n[t]);
+  } else if (t < Nc + Nv && A.out_s) {
+    const long long c1 = t - Nc;
+    const int k = (int)(c1 % A.Nx);
+    if (A.periodic_x == 1 && (k == 0 || k == A.Nx - 1)) {
+      if (k == A.Nx - 1) return;  // written with the row's first vertex
+      // :2633-2641: both ends of the row take the mean of the two
+      const long long last = c1 + A.Nx - 1;
+      const double fl = p2m_node(A, A.sum_s[last], A.sum_s[Nv + last], air(A.bcg[last]), A.out_s[last]);
+      const double ff = p2m_node(A, A.sum_s[c1], A.sum_s[Nv + c1], air(A.bcg[c1]), A.out_s[c1]);
+      const double av = 0.5 * (fl + ff);
+      A.out_s[c1] = av;
+      A.out_s[last] = av;
+      return;
+    }
+    A.out_s[c1] = p2m_node(A, A.sum_s[c1], A.sum_s[Nv + c1], air(A.bcg[c1]), A.out_s[c1]);
+  }
+}
+
 unsigned blocks_for(long long n) {
   const long long g = (n + 255) / 256;
   return (unsigned)(g > 0x7fffffffLL ? 0x7fffffffLL : (g < 1 ? 1 : g));
@@ -606,6 +667,16 @@ cudaError_t launch_marker_weights(const MarkerArgs &a, cudaStream_t s) {
   // four CTAs per SM at most: in the common case each reads one flag and returns
   const unsigned g = blocks_for(a.n), cap = 152u * 4u;
   if (a.n > 0) k_marker_weights<<<g < cap ? g : cap, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_p2m_scatter(const MarkerArgs &a, cudaStream_t s) {
+  if (a.n > 0) k_p2m_scatter<<<blocks_for(a.n), 256, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_p2m_nodes(const MarkerArgs &a, cudaStream_t s) {
+  k_p2m_nodes<<<blocks_for((long long)(a.Nx - 1) * (a.Nz - 1) + (long long)a.Nx * a.Nz), 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -39,6 +39,10 @@ struct MarkerArgs {
   double *m_sub;                  // per marker: the subgrid increments of sxxd, szzd, sxz [3][n]
   double *sum_n;                  // centroids: P2Mastah's WM, BMWM of dsxx, BMWM of dszz [3][Nc]
   double *sum_s;                  // vertices: WM, BMWM of dsxz [2][Nv]
+  // P2Mastah of a marker array (mdz_rheo_p2mastah)
+  const double *val;              // per marker
+  int avg;                        // 0 arithmetic, 1 harmonic, 2 geometric
+  double *out_n, *out_s;          // node fields (either may be null)
   DevStats *stats;
 };
 
@@ -54,5 +58,8 @@ cudaError_t launch_marker_update(const MarkerArgs &a, cudaStream_t s);
 cudaError_t launch_marker_weights(const MarkerArgs &a, cudaStream_t s);
 // vertices: wxz where the weight sum reaches 1e-30, and the periodic column average
 cudaError_t launch_marker_wxz(const MarkerArgs &a, cudaStream_t s);
+// P2Mastah of a marker array: the weight sums (markers), then the node values (nodes)
+cudaError_t launch_p2m_scatter(const MarkerArgs &a, cudaStream_t s);
+cudaError_t launch_p2m_nodes(const MarkerArgs &a, cudaStream_t s);
 
 }  // namespace mdz

@@ -243,7 +243,7 @@ int finish(mdz_rheo_ctx *ctx, mdz_sweep_stats *st) {
 enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + CO_COUNT,
        S_PN = S_VO + VO_COUNT, S_PS = S_PN + MDZ_MAX_PHASES, S_EN = S_PS + MDZ_MAX_PHASES,
        S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
-       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_COUNT = S_MK + 33 };
+       S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_P2M = S_MK + 33, S_COUNT = S_P2M + 12 };
 
 struct Mirror {
   mdz_rheo_ctx *ctx;
@@ -1518,6 +1518,71 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
     mi.back(mk->nx, S_MK + 6, n, host);
     mi.back(mk->nz, S_MK + 7, n, host);
   }
+  if (mi.err) return mi.err;
+  return prep_finish(ctx, flags, st);
+}
+
+int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_marker_grid *g, const mdz_markers *mk,
+                      const double *values, int avg, int interp_stencil, double *node_n, double *node_s, int mem,
+                      int flags, mdz_sweep_stats *st) {
+  if (!ctx || !md || !g || !mk || !values || (!node_n && !node_s)) return MDZ_EINVAL;
+  if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
+  if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
+  if (md->Nx < 2 || md->Nz < 2 || md->Nb_phases < 1 || mk->n < 0 || mk->n > 0x7fffffffLL) return MDZ_EINVAL;
+  if (avg < 0 || avg > 2 || (interp_stencil != 1 && interp_stencil != 9)) return MDZ_EINVAL;
+  if (!mk->x || !mk->z || !mk->phase) return MDZ_EINVAL;
+  if (node_n && (!g->xc_coord || !g->zc_coord || !g->BCp_type)) return MDZ_EINVAL;
+  if (node_s && (!g->xg_coord || !g->zg_coord || !g->BCg_type)) return MDZ_EINVAL;
+  CK(cudaSetDevice(ctx->device));
+  MarkerArgs A;
+  memset(&A, 0, sizeof(A));
+  const size_t Nx = (size_t)md->Nx, Nz = (size_t)md->Nz, Nc = (Nx - 1) * (Nz - 1), Nv = Nx * Nz;
+  const size_t n = (size_t)mk->n;
+  A.n = mk->n; A.Nx = md->Nx; A.Nz = md->Nz; A.periodic_x = md->periodic_x; A.np = md->Nb_phases;
+  A.stencil = interp_stencil; A.avg = avg;
+  A.dx = make_divisor(g->dx); A.dz = make_divisor(g->dz);
+  // P2Mastah's weight lengths, by its own expressions (ParticleRoutines.c:2218-2221)
+  A.dx_itp = make_divisor(interp_stencil == 9 ? 3.0 * g->dx / 2.0 : g->dx / 2.0);
+  A.dz_itp = make_divisor(interp_stencil == 9 ? 3.0 * g->dz / 2.0 : g->dz / 2.0);
+  const bool host = (mem == MDZ_MEM_HOST);
+  ctx->h2d = ctx->d2h = 0;
+  ctx->launches = 0;
+  Mirror mi{ctx};
+  A.x = mi.in(mk->x, S_P2M + 0, n, host);
+  A.z = mi.in(mk->z, S_P2M + 1, n, host);
+  A.phase = mi.in((const int *)mk->phase, S_P2M + 2, n, host);
+  A.val = mi.in(values, S_P2M + 3, n, host);
+  if (node_n) {
+    A.xc = mi.in(g->xc_coord, S_P2M + 4, Nx - 1, host);
+    A.zc = mi.in(g->zc_coord, S_P2M + 5, Nz - 1, host);
+    A.bcp = mi.in(g->BCp_type, S_BCP, Nc, host);
+    A.out_n = (double *)mi.in((const double *)node_n, S_P2M + 6, Nc, host);  // nodes P2Mastah skips keep theirs
+  }
+  if (node_s) {
+    A.xg = mi.in(g->xg_coord, S_P2M + 7, Nx, host);
+    A.zg = mi.in(g->zg_coord, S_P2M + 8, Nz, host);
+    A.bcg = mi.in(g->BCg_type, S_BCG, Nv, host);
+    A.out_s = (double *)mi.in((const double *)node_s, S_P2M + 9, Nv, host);
+  }
+  if (mi.err) return mi.err;
+  if ((node_n && ensure(ctx->bufs[S_P2M + 10], 2 * Nc * sizeof(double)) != MDZ_OK) ||
+      (node_s && ensure(ctx->bufs[S_P2M + 11], 2 * Nv * sizeof(double)) != MDZ_OK))
+    return MDZ_ENOMEM;
+  A.sum_n = node_n ? (double *)ctx->bufs[S_P2M + 10].p : nullptr;
+  A.sum_s = node_s ? (double *)ctx->bufs[S_P2M + 11].p : nullptr;
+  A.stats = ctx->d_stats;
+  int rc;
+  if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
+  if (node_n) CK(cudaMemsetAsync(A.sum_n, 0, 2 * Nc * sizeof(double), ctx->stream));
+  if (node_s) CK(cudaMemsetAsync(A.sum_s, 0, 2 * Nv * sizeof(double), ctx->stream));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  CK(launch_p2m_scatter(A, ctx->stream));
+  CK(launch_p2m_nodes(A, ctx->stream));
+  ctx->launches = 2;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  if (node_n) mi.back(node_n, S_P2M + 6, Nc, host);
+  if (node_s) mi.back(node_s, S_P2M + 9, Nv, host);
   if (mi.err) return mi.err;
   return prep_finish(ctx, flags, st);
 }

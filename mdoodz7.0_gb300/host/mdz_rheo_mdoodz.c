@@ -245,19 +245,31 @@ void CohesionFrictionDilationGrid(grid *mesh, markers *particles, mat_prop mater
   mdz_prep_fields f;
   mdz_sweep_stats st;
   double *strain_n = DoodzCalloc((model.Nx - 1) * (model.Nz - 1), sizeof(double));
-  P2Mastah(&model, *particles, particles->strain_pl, mesh, strain_n, (char *)mesh->BCp.type, 1, 0, 0, 1,
-           model.interp_stencil, NULL);
   double *strain_s = DoodzCalloc(model.Nx * model.Nz, sizeof(double));
-  P2Mastah(&model, *particles, particles->strain_pl, mesh, strain_s, (char *)mesh->BCg.type, 1, 0, 0, 0,
-           model.interp_stencil, NULL);
   memset(&md, 0, sizeof(md));
   md.Nx = mesh->Nx; md.Nz = mesh->Nz; md.Nb_phases = model.Nb_phases; md.periodic_x = model.periodic_x;
+  /* the plastic strain on the centroids and vertices: the two P2Mastah calls of
+   * RheologyDensity.c:1552-1553 (arithmetic, interpolated), on the GPU */
+  mdz_marker_grid mg;
+  mdz_markers mk;
+  memset(&mg, 0, sizeof(mg));
+  memset(&mk, 0, sizeof(mk));
+  mg.dx = mesh->dx; mg.dz = mesh->dz;
+  mg.xg_coord = mesh->xg_coord; mg.zg_coord = mesh->zg_coord;
+  mg.xc_coord = mesh->xc_coord; mg.zc_coord = mesh->zc_coord;
+  mg.BCp_type = mesh->BCp.type; mg.BCg_type = mesh->BCg.type;
+  mk.n = particles->Nb_part;
+  mk.x = particles->x; mk.z = particles->z; mk.phase = particles->phase;
+  memset(&st, 0, sizeof(st));
+  int rc = mdz_rheo_p2mastah(mdz_context(), &md, &mg, &mk, particles->strain_pl, 0, model.interp_stencil, strain_n,
+                             strain_s, MDZ_MEM_HOST, 0, &st);
+  if (rc != MDZ_OK) mdz_fail(rc, &st);
   mdz_prep_materials_from(&pm, &materials, model.Nb_phases);
   mdz_prep_fields_from(&f, mesh);
   f.strain_pl_n = strain_n; f.strain_pl_s = strain_s;
   memset(&st, 0, sizeof(st));
-  const int rc = mdz_rheo_softening(mdz_context(), &md, &pm, &f, model.smooth_softening, model.hardening_modulus,
-                                    model.marker_noise, MDZ_MEM_HOST, 0, &st);
+  rc = mdz_rheo_softening(mdz_context(), &md, &pm, &f, model.smooth_softening, model.hardening_modulus,
+                          model.marker_noise, MDZ_MEM_HOST, 0, &st);
   DoodzFree(strain_n);
   DoodzFree(strain_s);
   if (rc != MDZ_OK) mdz_fail(rc, &st);

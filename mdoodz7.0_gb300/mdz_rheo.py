@@ -418,6 +418,9 @@ def load_library(path: str = LIB_PATH):
                                            C.POINTER(PrepFields), C.c_int, C.c_int, C.POINTER(SweepStats)]
     lib.mdz_rheo_marker_stress.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(MarkerOpts), C.POINTER(MarkerGrid),
                                            C.POINTER(Markers), C.c_int, C.c_int, C.POINTER(SweepStats)]
+    lib.mdz_rheo_p2mastah.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(MarkerGrid), C.POINTER(Markers),
+                                      C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                      C.POINTER(SweepStats)]
     lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -684,6 +687,18 @@ class Context:
                                              flags, C.byref(st))
         if check and rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_marker_stress")
+        return rc, st
+
+    def p2mastah(self, model, grid: dict, markers: dict, values, avg, stencil, node_n, node_s, dx, dz,
+                 mem=MEM_HOST, flags=0, check=True):
+        """P2Mastah of a marker array onto centroids (node_n) and/or vertices (node_s),
+        updated in place (mdz_rheo_p2mastah)."""
+        st = SweepStats()
+        g, m = make_marker_structs(grid, markers, dx, dz)
+        rc = self.lib.mdz_rheo_p2mastah(self.handle, C.byref(model), C.byref(g), C.byref(m), _ptr(values), avg,
+                                        stencil, _ptr(node_n), _ptr(node_s), mem, flags, C.byref(st))
+        if check and rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_p2mastah")
         return rc, st
 
     # ---- launch-shape autotuner

@@ -281,6 +281,27 @@ def shim_marker_stress(model, opts, grid: dict, markers: dict, dx, dz, drop_in=T
     return _marker_call(getattr(shimtest(), name), model, opts, grid, markers, dx, dz)
 
 
+def _p2m_call(fn, model, grid, markers, values, avg, stencil, node_n, node_s, dx, dz):
+    fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.MarkerGrid), C.POINTER(R.Markers), C.c_void_p, C.c_int, C.c_int,
+                   C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    g, m = R.make_marker_structs(grid, markers, dx, dz)
+    return fn(C.byref(model), C.byref(g), C.byref(m), R._ptr(values), avg, stencil, R._ptr(node_n), R._ptr(node_s))
+
+
+def orc_p2mastah(model, grid: dict, markers: dict, values, avg, stencil, node_n, node_s, dx, dz):
+    """P2Mastah of a marker array on the restatement (node arrays updated in place)."""
+    return _p2m_call(oracle().orc_p2mastah, model, grid, markers, values, avg, stencil, node_n, node_s, dx, dz)
+
+
+def ref_p2mastah(model, grid: dict, markers: dict, values, avg, stencil, node_n, node_s, dx, dz):
+    """The reference's P2Mastah of a marker array, on one thread (node arrays updated in place)."""
+    lib = reference()
+    if lib is None:
+        raise RuntimeError("reference library not built (oracle/_ref)")
+    return _p2m_call(lib.ref_p2mastah, model, grid, markers, values, avg, stencil, node_n, node_s, dx, dz)
+
+
 def orc_points(model, mat, pin, pout, n, aniso=0):
     return oracle().orc_points(C.byref(model), C.byref(mat), C.byref(pin), C.byref(pout), n, aniso)
 

@@ -249,12 +249,16 @@ int ref_softening_markers(const mdz_model *m, const mdz_prep_materials *pmat, md
   memset(&P, 0, sizeof(P));
   P.Nb_part = (int)n_part;
   P.x = (double *)px; P.z = (double *)pz; P.phase = (int *)pphase; P.strain_pl = (double *)pstrain;
+  /* one OpenMP thread: P2Mastah's per-thread partial sums then run in marker order */
+  const int threads = omp_get_max_threads();
+  omp_set_num_threads(1);
   CohesionFrictionDilationGrid(g, &P, *mp, pm, sc);
   const int Nc = (m->Nx - 1) * (m->Nz - 1), Nv = m->Nx * m->Nz;
   memset(strain_n, 0, sizeof(double) * Nc);
   memset(strain_s, 0, sizeof(double) * Nv);
   P2Mastah(&pm, P, P.strain_pl, g, strain_n, (char *)g->BCp.type, 1, 0, 0, 1, pm.interp_stencil, NULL);
   P2Mastah(&pm, P, P.strain_pl, g, strain_s, (char *)g->BCg.type, 1, 0, 0, 0, pm.interp_stencil, NULL);
+  omp_set_num_threads(threads);
   free_prep_grid(g);
   free(mp);
   return 0;
@@ -315,6 +319,34 @@ int ref_marker_stress(const mdz_model *m, const mdz_marker_opts *o, mdz_marker_g
   omp_set_num_threads(threads);
   free_grid(g);
   free(mp);
+  return 0;
+}
+
+/* The reference's P2Mastah (flag 1, prop 0) of a marker array onto the centroids and/or
+ * vertices, on one OpenMP thread (its per-thread partial sums then run in marker order). */
+int ref_p2mastah(const mdz_model *m, const mdz_marker_grid *mg, const mdz_markers *mk, const double *val, int avg,
+                 int stencil, double *node_n, double *node_s) {
+  quiet_log();
+  params pm;
+  scale sc;
+  fill_params(&pm, &sc, m);
+  pm.dx = mg->dx; pm.dz = mg->dz; pm.interp_stencil = stencil;
+  mdz_grid_fields none;
+  memset(&none, 0, sizeof(none));
+  grid *g = make_grid(m, &none);
+  g->dx = mg->dx; g->dz = mg->dz;
+  g->xg_coord = W(mg->xg_coord); g->zg_coord = W(mg->zg_coord);
+  g->xc_coord = W(mg->xc_coord); g->zc_coord = W(mg->zc_coord);
+  markers P;
+  memset(&P, 0, sizeof(P));
+  P.Nb_part = (int)mk->n;
+  P.x = (double *)mk->x; P.z = (double *)mk->z; P.phase = (int *)mk->phase;
+  const int threads = omp_get_max_threads();
+  omp_set_num_threads(1);
+  if (node_n) P2Mastah(&pm, P, (double *)val, g, node_n, (char *)mg->BCp_type, 1, avg, 0, 1, stencil, NULL);
+  if (node_s) P2Mastah(&pm, P, (double *)val, g, node_s, (char *)mg->BCg_type, 1, avg, 0, 0, stencil, NULL);
+  omp_set_num_threads(threads);
+  free_grid(g);
   return 0;
 }
 

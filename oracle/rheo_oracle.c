@@ -1574,19 +1574,56 @@ static void orc_p2m(const mdz_markers *mk, const double *val, const double *X, c
   }
 }
 
-/* P2Mastah's node values (flag 1, avg 0; :2603-2641): BM / WM where |WM| reaches 1e-30
- * away from air, else F keeps its value; with periodic x the two ends of each row of a
- * vertex field take their mean. */
-static void orc_p2m_nodes(double *F, const double *WM, const double *BM, const signed char *tag, int Nxn, int Nzn,
-                          int vertex, int per) {
+/* P2Mastah's node values (flag 1; :2603-2641): BM / WM where |WM| reaches 1e-30 away
+ * from air (its reciprocal for avg 1, its exponential for avg 2), else F keeps its value;
+ * with periodic x the two ends of each row of a vertex field take their mean. */
+static void orc_p2m_nodes_avg(double *F, const double *WM, const double *BM, const signed char *tag, int Nxn,
+                              int Nzn, int vertex, int per, int avg) {
   for (int64_t i = 0; i < (int64_t)Nxn * Nzn; i++)
-    if (!(fabs(WM[i]) < 1e-30 || orc_air(tag[i]))) F[i] = BM[i] / WM[i];
+    if (!(fabs(WM[i]) < 1e-30 || orc_air(tag[i]))) {
+      F[i] = BM[i] / WM[i];
+      if (avg == 1) F[i] = 1.0 / F[i];
+      if (avg == 2) F[i] = exp(F[i]);
+    }
   if (vertex && per == 1)
     for (int l = 0; l < Nzn; l++) {
       const int64_t c1 = (int64_t)l * Nxn + Nxn - 1, c = (int64_t)l * Nxn;
       const double av = 0.5 * (F[c1] + F[c]);
       F[c1] = av; F[c] = av;
     }
+}
+
+static void orc_p2m_nodes(double *F, const double *WM, const double *BM, const signed char *tag, int Nxn, int Nzn,
+                          int vertex, int per) {
+  orc_p2m_nodes_avg(F, WM, BM, tag, Nxn, Nzn, vertex, per, 0);
+}
+
+/* P2Mastah of a marker array (flag 1, prop 0) onto the centroids and/or vertices, avg 0,
+ * 1 or 2 (ParticleRoutines.c:2170-2665): the values go in as v, 1/v or log v
+ * (:2346-2352) and the node means come back as m, 1/m or exp m. */
+int orc_p2mastah(const mdz_model *m, const mdz_marker_grid *g, const mdz_markers *mk, const double *val, int avg,
+                 int stencil, double *node_n, double *node_s) {
+  if (m->Nx < 2 || m->Nz < 2 || avg < 0 || avg > 2 || (stencil != 1 && stencil != 9)) return MDZ_EINVAL;
+  const int Nx = m->Nx, Nz = m->Nz, Ncx = Nx - 1, Ncz = Nz - 1, per = m->periodic_x;
+  const int64_t Nc = (int64_t)Ncx * Ncz, Nv = (int64_t)Nx * Nz, n = mk->n;
+  for (int64_t p = 0; p < n; p++)
+    if (mk->phase[p] != -1 && (mk->phase[p] < 0 || mk->phase[p] >= m->Nb_phases)) return MDZ_EINVAL;
+  double *v = malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+  for (int64_t p = 0; p < n; p++) v[p] = avg == 1 ? 1.0 / val[p] : (avg == 2 ? log(val[p]) : val[p]);
+  if (node_n) {
+    double *s = calloc(2 * (size_t)Nc, sizeof(double));
+    orc_p2m(mk, v, g->xc_coord, g->zc_coord, Ncx, Ncz, g->dx, g->dz, stencil, per, s, s + Nc);
+    orc_p2m_nodes_avg(node_n, s, s + Nc, g->BCp_type, Ncx, Ncz, 0, per, avg);
+    free(s);
+  }
+  if (node_s) {
+    double *s = calloc(2 * (size_t)Nv, sizeof(double));
+    orc_p2m(mk, v, g->xg_coord, g->zg_coord, Nx, Nz, g->dx, g->dz, stencil, per, s, s + Nv);
+    orc_p2m_nodes_avg(node_s, s, s + Nv, g->BCg_type, Nx, Nz, 1, per, avg);
+    free(s);
+  }
+  free(v);
+  return MDZ_OK;
 }
 
 /* UpdateParticleStress with subgrid_diffusion 2 (RheologyParticles.c:1811-1903): the old

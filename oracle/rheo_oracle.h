@@ -62,6 +62,9 @@ int orc_shear_modulus(const mdz_model *model, const mdz_prep_materials *mat, mdz
 
 /* UpdateParticleStress (RheologyParticles.c:1725-2004), subgrid_diffusion 0 or 1. */
 int orc_marker_stress(const mdz_model *model, const mdz_marker_opts *opts, mdz_marker_grid *grid, mdz_markers *mk);
+/* P2Mastah of a marker array (ParticleRoutines.c:2170-2665), serial order */
+int orc_p2mastah(const mdz_model *m, const mdz_marker_grid *g, const mdz_markers *mk, const double *val, int avg,
+                 int stencil, double *node_n, double *node_s);
 
 /* InterpCentroidsToVerticesDouble (GridRoutines.c:108) alone. */
 void orc_interp_c2v(const mdz_model *model, const double *centroid, const signed char *BCp_type,

@@ -76,6 +76,14 @@ int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_
   return orc_shear_modulus(model, mat, f);
 }
 
+int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_grid *grid,
+                      const mdz_markers *markers, const double *values, int avg, int interp_stencil,
+                      double *node_n, double *node_s, int mem, int flags, mdz_sweep_stats *stats) {
+  (void)stats;
+  if (!ctx || mem != MDZ_MEM_HOST || flags != 0) return MDZ_EINVAL;
+  return orc_p2mastah(model, grid, markers, values, avg, interp_stencil, node_n, node_s);
+}
+
 int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marker_opts *opts,
                            mdz_marker_grid *grid, mdz_markers *markers, int mem, int flags, mdz_sweep_stats *stats) {
   (void)stats;
