@@ -12,10 +12,19 @@ larger quantities is only defined to that tolerance in the reference too:
     deformation is mostly elastic);
   * dissipation Wdiss: scale max(|ref|, Wtot);
   * everything else: scale max(|ref|, 1e-3 max|field|) (signed fields near 0).
+
+The eta_phys scale is formed from the node's averages.  Where one phase of a node is
+near its yield stress, its plastic strain rate is a small difference whose last bits the
+local solve's own tolerance leaves open, and its dissipative viscosity can dominate the
+node's average while the averaged eta_VE hides it.  `eta_phys_phase_scale` forms the same
+scale phase by phase (each phase's eta_phys and eta_VE from the oracle's ViscosityConcise
+at that node), sum_p |d node / d eta_p| eta_p max(1, eta_p / eta_VE_p); the full-size
+tests use it at the nodes the node-average scale flags.
 """
 import numpy as np
 
 import mdz_rheo as R
+import oracle_lib as O
 
 OUT_FIELDS = R.VER_INTERP + R.CEN_OUT + R.VER_OUT + ["phase_eta_n", "phase_eta_s"]
 RTOL = 1e-12
@@ -85,3 +94,53 @@ def worst(a, b, ref_arrays=None, model=None, fields=OUT_FIELDS):
             e = rel_err(x, ref)
         out[k] = float(np.max(e))
     return out
+
+
+def eta_phys_phase_scale(w, ref, nodes, where="s", phases=False):
+    """Per-node scale of eta_phys at centroid ("n") or vertex ("s") indices `nodes`, from
+    every phase's dissipative viscosity eta_p and eta_VE_p (the oracle's ViscosityConcise
+    on that node's inputs, prepared as NonNewtonianViscosityGrid prepares them:
+    RheologyDensity.c:1199-1204, :1335-1340), combined by the model's phase average."""
+    m, mat, a = w.model, w.mat, w.arrays
+    nodes = np.asarray(nodes, np.int64)
+    npn, np_ = nodes.size, mat.Nb_phases
+    if npn == 0:
+        return np.zeros(0)
+    cen = where == "n"
+    if cen:
+        src = {"G": a["mu_n"], "T": a["T"], "P": a["p_in"], "d": a["d0_n"], "phi": a["phi0_n"], "X0": a["X0_n"],
+               "Txx0": a["sxxd0"], "Tzz0": a["szzd0"], "Txz0": a["sxz0_n"], "strain_acc": a["strain_n"],
+               "dil": a["dil_n"], "fric": a["fric_n"], "C": a["C_n"], "P0": a["p0_n"], "T0": a["T0_n"],
+               "beta": a["bet_n"], "div": a["div_u"]}
+        exx, ezz, exz = a["exxd"], a["ezzd"], a["exz_n"]
+    else:
+        src = {"G": a["mu_s"], "T": ref["T_s"], "P": ref["P_s"], "d": ref["d0_s"], "phi": ref["phi0_s"],
+               "X0": a["X0_s"], "Txx0": a["sxxd0_s"], "Tzz0": a["szzd0_s"], "Txz0": a["sxz0"],
+               "strain_acc": a["strain_s"], "dil": a["dil_s"], "fric": a["fric_s"], "C": a["C_s"], "P0": a["p0_s"],
+               "T0": np.zeros_like(a["mu_s"]), "beta": a["bet_s"], "div": a["div_u_s"]}
+        exx, ezz, exz = a["exxd_s"], a["ezzd_s"], a["exz"]
+    pin = {k: np.repeat(v[nodes], np_) for k, v in src.items()}
+    el = 1.0 if m.elastic == 1 else 0.0
+    eta_e = m.dt * pin["G"] if m.elastic == 1 else np.ones(npn * np_)
+    pin["Exx"] = np.repeat(exx[nodes], np_) + el * pin["Txx0"] / eta_e / 2.0
+    pin["Ezz"] = np.repeat(ezz[nodes], np_) + el * pin["Tzz0"] / eta_e / 2.0
+    pin["Exz"] = np.repeat(exz[nodes], np_) + el * pin["Txz0"] / eta_e / 2.0
+    pin["phase"] = np.tile(np.arange(np_, dtype=np.int32), npn)
+    out = {k: np.zeros(npn * np_) for k in R.PT_OUT}
+    pi, po = R.make_points(pin, out, centroid=1 if cen else 0)
+    O.orc_points(m, mat, pi, po, npn * np_, 0)
+    eta = out["eta"].reshape(npn, np_)
+    eve = out["etaVE"].reshape(npn, np_)
+    perc = np.stack([a["phase_perc_n" if cen else "phase_perc_s"][p][nodes] for p in range(np_)], axis=1)
+    active = np.abs(perc) > 1e-13
+    kappa = np.maximum(1.0, np.abs(eta / eve))
+    if m.eta_average == 1:  # harmonic: node = 1 / sum perc / eta_p
+        node = 1.0 / np.sum(np.where(active, perc / eta, 0.0), axis=1)
+        terms = node[:, None] ** 2 * perc / np.abs(eta) * kappa
+    elif m.eta_average == 2:  # geometric: node = exp(sum perc ln eta_p)
+        node = np.exp(np.sum(np.where(active, perc * np.log(eta), 0.0), axis=1))
+        terms = node[:, None] * np.abs(perc) * kappa
+    else:  # arithmetic: node = sum perc eta_p
+        terms = np.abs(perc * eta) * kappa
+    scale = np.sum(np.where(active, terms, 0.0), axis=1)
+    return (scale, eta, eve, perc) if phases else scale

@@ -11,7 +11,7 @@ import pytest
 import mdz_rheo as R
 import mdz_workloads as W
 import oracle_lib as O
-from common import RTOL, clone, field, rel_err, worst
+from common import RTOL, clone, eta_phys_phase_scale, field, rel_err, scaled_error, worst
 
 pytestmark = pytest.mark.gpu
 
@@ -155,3 +155,50 @@ def test_aniso_typical_scale_harmonic(ctx):
     rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=True)
     assert rc == rc2 == R.MDZ_OK
     check_close(g, c, "aniso-typical-harmonic", w)
+
+
+ANISO_SOLVE_TOL = 1e-11  # tol of ViscosityConciseAniso's local Newton (AnisotropyRoutines.c:507-583)
+
+FULL = {
+    # the headline sweep: 2049 x 2049 cells, 5 phases, 8,400,901 nodes (host memory, in row bands)
+    "plain_large_2049": (lambda: W.plain_large(seed=1, ncx=2049), False),
+    # the anisotropic sweep: 4097 x 4097 cells, 3 phases, 33.6 M nodes
+    "aniso_4097": (lambda: W.aniso(seed=4, ncx=4097), True),
+}
+
+
+@pytest.mark.parametrize("name", list(FULL))
+def test_full_size_sweep_matches_oracle(ctx, name):
+    """The benchmark workloads at their full sizes, every node against the oracle (which
+    runs with OpenMP on the host cores), with the same parity bar as the small cases; the
+    few nodes whose eta_phys the node-average scale flags are measured with the per-phase
+    scale (common.eta_phys_phase_scale)."""
+    make, aniso = FULL[name]
+    w = make()
+    rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=aniso)
+    assert rc == rc2 == R.MDZ_OK
+    assert st.phase_calls == st2.phase_calls
+    errs = worst(g, c, w.arrays, w.model)
+    print(name, {k: f"{v:.1e}" for k, v in errs.items() if v > 1e-15})
+    for k, v in errs.items():
+        if v <= RTOL:
+            continue
+        if aniso:
+            # ViscosityConciseAniso documents that its residual loses about 12 digits where
+            # deformation is mostly elastic and accepts an iterate at |r/Eii| < 10 tol
+            # (AnisotropyRoutines.c:568-583): the plastic part and the dissipative
+            # viscosity are only defined to its tolerance, 1e-11, there
+            assert k in ("eta_phys_n", "eta_phys_s", "eII_pl") and v <= ANISO_SOLVE_TOL, (k, v)
+            continue
+        assert k in ("eta_phys_n", "eta_phys_s"), (k, v)
+        where = k[-1]
+        x, ref = g[k], c[k]
+        e = scaled_error(x, ref, np.abs(ref) * np.maximum(1.0, np.abs(ref) / np.abs(c["eta_" + where])))
+        flagged = np.flatnonzero(e > RTOL)
+        print(k, "nodes flagged by the node-average scale:", flagged.size)
+        assert flagged.size <= 1000
+        scale = eta_phys_phase_scale(w, c, flagged, where)
+        pe = np.abs(x[flagged] - ref[flagged]) / scale
+        print(k, "largest per-phase scaled error:", float(pe.max()))
+        assert float(pe.max()) <= RTOL
+    del g, c

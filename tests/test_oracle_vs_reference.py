@@ -50,3 +50,23 @@ def test_restatement_bit_identical_on_points(name, seed):
     O.ref_points(md, m, pi, po, n, int(aniso))
     for k in R.PT_OUT:
         assert np.array_equal(oo[k].view(np.uint64), ro[k].view(np.uint64)), k
+
+
+@pytest.mark.parametrize("where", ["n", "s"])
+def test_eta_phys_phase_scale_rebuilds_the_node_values(where):
+    """The per-phase eta_phys scale of the parity tests evaluates every phase of a node
+    from that node's inputs: its phase average must give back the sweep's eta_phys and
+    its eta_VE the sweep's phase_eta."""
+    from common import clone, eta_phys_phase_scale
+    w = W.plain_large(seed=3, ncx=40)
+    c = clone(w.arrays)
+    O.orc_sweep(w.model, w.mat, R.FieldSet(c))
+    nodes = np.arange(0, 1600, 7)
+    scale, eta, eve, perc = eta_phys_phase_scale(w, c, nodes, where, phases=True)
+    node = np.sum(np.where(np.abs(perc) > 1e-13, perc * eta, 0.0), axis=1)
+    ref = c["eta_phys_" + where][nodes]
+    assert np.allclose(node, ref, rtol=1e-14, atol=0)
+    pe = np.stack([c["phase_eta_" + where][p][nodes] for p in range(w.mat.Nb_phases)], axis=1)
+    act = np.abs(perc) > 1e-13
+    assert np.array_equal(eve[act], pe[act])
+    assert np.all(scale >= 0.999 * ref)
