@@ -13,18 +13,28 @@
 // The theorem holds without underflow or overflow; the fast form is used for
 // 2^-500 <= |a| <= 2^500 and a divisor in [2^-400, 2^400] (so every intermediate is a
 // normal number), and the plain division otherwise (zero, subnormal, huge, Inf, NaN).
+// The second correction is mostly a no-op: q1 already is RN(a/b) whenever the remainder
+// r1 = a - b q1 (exact, q1 being faithful) is below half an ulp of q1 times |b|, that is
+// |r1| < |b| 2^(e(q1) - 53), the bound of the rounding interval around a q1 that is not a
+// power of two.  That test runs on the integer pipe (b's significand with the exponent
+// e(b) + e(q1) - 53, compared with |r1| as bit patterns), so the common case costs one
+// multiply and three fused multiply-adds; ties, powers of two, and thresholds outside
+// the normal range take the full second correction.
 // Checked bit for bit against CUDA's division by mdz_rheo_div_selftest.
 #pragma once
 #include <cuda_runtime.h>
+#include <string.h>
 
 #include "fp64_bits.cuh"
 
 namespace mdz {
 
-// a divisor b, its rounded reciprocal and whether the fast form may be used with it
+// a divisor b, its rounded reciprocal, whether the fast form may be used with it, and
+// the biased exponent and significand field of |b| (for the remainder test)
 struct Divisor {
   double b, y;
-  int fast;
+  int fast, eb;
+  unsigned long long bman;
 };
 
 // host side: the divisor as the kernels use it
@@ -34,14 +44,29 @@ inline Divisor make_divisor(double b) {
   d.y = 1.0 / b;
   const double m = b < 0 ? -b : b;
   d.fast = (m >= 0x1p-400 && m <= 0x1p400) ? 1 : 0;
+  unsigned long long bits;
+  memcpy(&bits, &m, sizeof(bits));
+  d.eb = (int)((bits >> 52) & 0x7ffu);
+  d.bman = bits & 0xfffffffffffffull;
   return d;
 }
 
+// the second correction, out of line: taken where the remainder test cannot decide
+static __device__ __noinline__ double div_by_correct(double r1, double y, double q1) { return __fma_rn(r1, y, q1); }
+
 __device__ __forceinline__ double div_by(double a, const Divisor &d) {
   if (d.fast && fp64_exponent(a) - (1023u - 500u) <= 1000u) {
-    double q = __dmul_rn(a, d.y);
-    q = __fma_rn(__fma_rn(-q, d.b, a), d.y, q);
-    return __fma_rn(__fma_rn(-q, d.b, a), d.y, q);
+    const double q0 = __dmul_rn(a, d.y);
+    const double q1 = __fma_rn(__fma_rn(-q0, d.b, a), d.y, q0);
+    const double r1 = __fma_rn(-q1, d.b, a);
+    unsigned lo, hi;
+    fp64_words(q1, lo, hi);
+    const int te = d.eb + (int)((hi >> 20) & 0x7ffu) - 1023 - 53;  // exponent of |b| ulp(q1) / 2
+    const bool pow2 = ((hi & 0xfffffu) | lo) == 0u;
+    if (!pow2 && te > 0 && te < 0x7ff &&
+        (fp64_bits(r1) & kFp64AbsMask) < (((unsigned long long)te << 52) | d.bman))
+      return q1;
+    return div_by_correct(r1, d.y, q1);
   }
   return a / d.b;
 }
