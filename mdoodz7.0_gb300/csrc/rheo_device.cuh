@@ -374,14 +374,36 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s
 // c_k = n_k lp + nc_k.  The FP64 iteration that follows is unchanged and runs to the same
 // residual tolerance, so these steps only move its start (to within FP32 rounding of the
 // root).  Returns s0 when the FP32 iteration leaves (0, 2].
+//
+// The coefficients go to FP32 by truncating their bit patterns on the integer pipe (a
+// starting guess needs no rounding), since GB300 runs the FP32<->FP64 conversions on its
+// FP64 pipe: values beyond the FP32 range become +-FLT_MAX (NaN too) and the step guard
+// below returns s0 should they upset the iteration; values below it become 0.
+__device__ __forceinline__ float f32_trunc(double x) {
+  unsigned lo, hi;
+  fp64_words(x, lo, hi);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f7fffffu);
+  return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+
+// x as a double, exactly, from the bits of a normal x (the conversion otherwise)
+__device__ __forceinline__ double f64_of_f32(float x) {
+  const unsigned b = __float_as_uint(x), e = (b >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)x;
+  return __hiloint2double((int)((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3)), (int)(b << 29));
+}
+
 __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, float s0, int iters) {
   if (iters <= 0) return s0;
-  const float a = (float)(q.Aup * q.inv_Eii);
+  const float a = f32_trunc(q.Aup * q.inv_Eii);
   float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
   if (q.nl) {
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
-      if (q.nl >> k & 1) { n[k] = (float)q.n[k]; c[k] = (float)fma(q.n[k], q.lp, q.nc[k]); }
+      if (q.nl >> k & 1) { n[k] = f32_trunc(q.n[k]); c[k] = f32_trunc(fma(q.n[k], q.lp, q.nc[k])); }
   }
   float s = s0;
   for (int it = 0; it < iters; it++) {
@@ -678,7 +700,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
     VeState s;
     s.status = MDZ_OK;
-    ve_newton(q, (double)ve_polish_f32(q, s_start, polish), s);
+    ve_newton(q, f64_of_f32(ve_polish_f32(q, s_start, polish)), s);
     set_status(o.status, s.status);
     eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
     o.iters = s.iters;
@@ -927,7 +949,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     s.status = MDZ_OK;
     double r, S, sv;  // sv = eta_ve / eta_up
     if (s_start > 0.0f || polish > 0) {
-      sv = (double)ve_polish_f32(q, (s_start > 0.0f) ? s_start : 1.0f, polish);
+      sv = f64_of_f32(ve_polish_f32(q, (s_start > 0.0f) ? s_start : 1.0f, polish));
     } else {
       const double inv_up = 1.0 / eta_up;
       const double eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic != 0, eta_el, false);
