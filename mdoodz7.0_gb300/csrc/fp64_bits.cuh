@@ -110,6 +110,16 @@ __device__ __forceinline__ bool fp64_abs_gt(double x, double t) {
 // x == y as IEEE numbers, for a y that is neither NaN nor zero (bit equality then)
 __device__ __forceinline__ bool fp64_eq_nonzero(double x, double y) { return fp64_bits(x) == fp64_bits(y); }
 
+// fmax(a, b) on the integer pipe: a NaN operand yields the other one, +0 wins a tie with
+// -0, otherwise the larger by order key
+__device__ __forceinline__ double fp64_fmax(double a, double b) {
+  const unsigned long long ba = fp64_bits(a), bb = fp64_bits(b);
+  if ((ba & kFp64AbsMask) > kFp64InfBits) return b;
+  if ((bb & kFp64AbsMask) > kFp64InfBits) return a;
+  const unsigned long long ka = fp64_key_of_bits(ba), kb = fp64_key_of_bits(bb);
+  return (ka > kb || (ka == kb && (ba >> 63) == 0ull)) ? a : b;
+}
+
 constexpr int kFp64CeilSat = 1 << 30;
 
 // ceil(q) as an int, from the fields of q: |q| = m 2^(e-52) with m the 53-bit

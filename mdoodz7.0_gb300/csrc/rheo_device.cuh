@@ -307,7 +307,7 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
 #pragma unroll
   for (int k = 0; k < K_COUNT; k++) {
     q.hn[k] = 0.5 * (q.n[k] - 1.0);
-    if (q.nl >> k & 1) q.nmax = fmax(q.nmax, q.n[k]);
+    if (q.nl >> k & 1) q.nmax = fp64_fmax(q.nmax, q.n[k]);
     if ((q.nl >> k & 1) && k != p) q.nc[k] = q.n[k] * (L.ln_inv[k] - ln_inv_p);
   }
   q.Aup = A * eta_up;
@@ -671,7 +671,8 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
     }
   }
   // bracket (:582-592): the smallest isolated viscosity is 1 / the largest reciprocal
-  const double ln_inv_max = fmax(fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), fmax(L.ln_inv[K_LIN], L.ln_inv_gbs));
+  const double ln_inv_max =
+      fp64_fmax(fp64_fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), fp64_fmax(L.ln_inv[K_LIN], L.ln_inv_gbs));
   start_viscosity(M, ln_inv_max, constant, eta_cst, elastic == 1, c, S.eta_up, S.ln_eta_up);
   S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
