@@ -98,6 +98,9 @@ struct NodeIn {
   double Exx, Ezz, Exz, Txx0, Tzz0, Txz0;
   double G, T, P, d, phi, X0, dil, fric, C, P0, T0, beta;
   double lxlz, lx2, ani_fac;  // anisotropic nodes
+  // post_process: 0 none, 1 every output (ViscosityConcise's post_process = 1), 2 only what
+  // the sweep keeps of a vertex (etaVE, the dissipative viscosity, X): the per-phase stress
+  // components, strain-rate partition, divergences and overstress are left unset
   int centroid, final_update, post_process, want_rho;
 };
 
@@ -389,10 +392,13 @@ __device__ __forceinline__ float f32_trunc(double x) {
   return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
 }
 
-// x as a double, exactly, from the bits of a normal x (the conversion otherwise)
+// x as a double, exactly, from the bits of a normal x; zero, subnormal, Inf and NaN take
+// the conversion instruction, out of line so that the common case does not execute it too
+static __device__ __noinline__ double f64_of_f32_rare(float x) { return (double)x; }
+
 __device__ __forceinline__ double f64_of_f32(float x) {
   const unsigned b = __float_as_uint(x), e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (double)x;
+  if (e == 0u || e == 0xffu) return f64_of_f32_rare(x);
   return __hiloint2double((int)((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3)), (int)(b << 29));
 }
 
@@ -666,7 +672,7 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
     o.d1 = d;
     lnd = log(d);
     if (diffusion) {
-      const double lnBd = (ph.lin_m != 0.0) ? fma(ph.lin_mn, lnd, L.lnB_lin) : L.lnB_lin;
+      const double lnBd = !fp64_is_zero(ph.lin_m) ? fma(ph.lin_mn, lnd, L.lnB_lin) : L.lnB_lin;
       L.ln_inv[K_LIN] = c.lnEii - fma(c.lnEii, ph.lin_invn, lnBd);
     }
   }
@@ -780,14 +786,10 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   else if (plastic == 1) { o.etaVE = eta_vep; inv_eta_pl = gdot / Tii; }
   else { o.etaVE = eta_vep; inv_eta_pl = 2.0 * lam_dot * A_tau / Tii; }
   o.is_pl = is_pl;
-  o.Txx = 2.0 * o.etaVE * in.Exx;
-  o.Tzz = 2.0 * o.etaVE * in.Ezz;
-  o.Txz = 2.0 * o.etaVE * in.Exz;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
-
-  double eta = 0.0;
-  if (in.post_process == 1) {  // :986-1053
-    const double inv_half_T = 2.0 / Tii_ve;  // 1/eta_k = 2 Eii_k / Tii
+  // the dissipative viscosity: 1 / eta = sum_k 2 Eii_k / Tii (+ 1/eta_cst, 1/eta_pl)
+  const auto dissipative = [&](double &inv_half_T) {
+    inv_half_T = 2.0 / Tii_ve;  // 1/eta_k = 2 Eii_k / Tii
     double inv = 0.0;
     if (peierls) inv += e_exp * inv_half_T;
     if (dislocation) inv += e_pwl * inv_half_T;
@@ -799,30 +801,45 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     }
     if (constant) inv += (1.0 / eta_cst);
     if (is_pl == 1) inv += inv_eta_pl;
-    eta = 1.0 / inv;
-    if (elastic) {
-      const double h = 0.5 * c.inv_eta_el;
-      const double Tyy = -(o.Txx + o.Tzz), Tyy0 = -(in.Txx0 + in.Tzz0);
-      const double ex = (o.Txx - in.Txx0) * h, ez = (o.Tzz - in.Tzz0) * h;
-      const double ey = (Tyy - Tyy0) * h, exz = (o.Txz - in.Txz0) * h;
-      o.Eii_el = sqrt(0.5 * (ex * ex + ez * ez + ey * ey) + exz * exz);
-    }
-    o.Eii_pl = (is_pl && plastic == 1) ? gdot / 2.0 : ((is_pl && plastic == 2) ? lam_dot * A_tau : 0.0);
-    o.div_pl = divp;
-    o.div_el = -(Pc - in.P0) * c.inv_Kdt;
-    if (plastic == 1) o.OverS = eta_vp * gdot;
-    if (plastic == 2) o.OverS = eta_vp * lam_dot * A_tau;
-    if (in.centroid == 1) {
-      const double T2 = Tii * Tii;
-      o.Wtot = T2 * (Eii * inv_half_T);  // T2 / eta_ve, with Tii_ve = 2 eta_ve Eii
-      o.Wel = T2 * c.inv_eta_el;
-      o.Wdiss = T2 * inv;
-      if (fp64_lt(o.Wdiss, 0.0)) set_status(o.status, MDZ_EWDISS);
-    }
+    return inv;
+  };
+
+  double eta = 0.0;
+  if (in.post_process == 2) {  // a vertex of the sweep: only etaVE, eta and X are kept
+    double inv_half_T;
+    eta = 1.0 / dissipative(inv_half_T);
   } else {
-    o.Eii_pl = 0.0;
-    o.div_pl = (is_pl ? divp : 0.0);
-    o.div_el = 0.0;
+    o.Txx = 2.0 * o.etaVE * in.Exx;
+    o.Tzz = 2.0 * o.etaVE * in.Ezz;
+    o.Txz = 2.0 * o.etaVE * in.Exz;
+    if (in.post_process == 1) {  // :986-1053
+      double inv_half_T;
+      const double inv = dissipative(inv_half_T);
+      eta = 1.0 / inv;
+      if (elastic) {
+        const double h = 0.5 * c.inv_eta_el;
+        const double Tyy = -(o.Txx + o.Tzz), Tyy0 = -(in.Txx0 + in.Tzz0);
+        const double ex = (o.Txx - in.Txx0) * h, ez = (o.Tzz - in.Tzz0) * h;
+        const double ey = (Tyy - Tyy0) * h, exz = (o.Txz - in.Txz0) * h;
+        o.Eii_el = sqrt(0.5 * (ex * ex + ez * ez + ey * ey) + exz * exz);
+      }
+      o.Eii_pl = (is_pl && plastic == 1) ? gdot / 2.0 : ((is_pl && plastic == 2) ? lam_dot * A_tau : 0.0);
+      o.div_pl = divp;
+      o.div_el = -(Pc - in.P0) * c.inv_Kdt;
+      if (plastic == 1) o.OverS = eta_vp * gdot;
+      if (plastic == 2) o.OverS = eta_vp * lam_dot * A_tau;
+      if (in.centroid == 1) {
+        const double T2 = Tii * Tii;
+        o.Wtot = T2 * (Eii * inv_half_T);  // T2 / eta_ve, with Tii_ve = 2 eta_ve Eii
+        o.Wel = T2 * c.inv_eta_el;
+        o.Wdiss = T2 * inv;
+        if (fp64_lt(o.Wdiss, 0.0)) set_status(o.status, MDZ_EWDISS);
+      }
+    } else {
+      o.Eii_pl = 0.0;
+      o.div_pl = (is_pl ? divp : 0.0);
+      o.div_el = 0.0;
+    }
   }
   // limiters (:1058-1073)
   if (fp64_gt(o.etaVE, M.max_eta)) o.etaVE = M.max_eta;
@@ -903,7 +920,7 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   }
   const double eta_cst = constant ? ph.eta0 : 0.0;
   // bracket (:409-415); its lower end is formed only where it is used
-  const double ln_inv_max = fmax(fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), L.ln_inv[K_LIN]);
+  const double ln_inv_max = fp64_fmax(fp64_fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), L.ln_inv[K_LIN]);
   start_viscosity(M, ln_inv_max, constant, eta_cst, elastic != 0, c, S.eta_up, S.ln_eta_up);
   S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = Coh; S.Ag = 0.0;
   S.lnd = c.lnd;
@@ -1002,10 +1019,12 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     o.Eii_pl = gdot / 2.0;
     Tii = Tiic;
   }
-  const double lx2 = an.lx2, lxlz = an.lxlz, nz2 = 1.0 - lx2;  // :650-652
-  o.Txx = lx2 * Tr_xx + nz2 * Tr_zz - 2. * lxlz * Tr_xz;
-  o.Tzz = nz2 * Tr_xx + lx2 * Tr_zz + 2. * lxlz * Tr_xz;
-  o.Txz = lxlz * Tr_xx - lxlz * Tr_zz + (lx2 - nz2) * Tr_xz;
+  if (in.post_process != 2) {
+    const double lx2 = an.lx2, lxlz = an.lxlz, nz2 = 1.0 - lx2;  // :650-652
+    o.Txx = lx2 * Tr_xx + nz2 * Tr_zz - 2. * lxlz * Tr_xz;
+    o.Tzz = nz2 * Tr_xx + lx2 * Tr_zz + 2. * lxlz * Tr_xz;
+    o.Txz = lxlz * Tr_xx - lxlz * Tr_zz + (lx2 - nz2) * Tr_xz;
+  }
   o.Pcorr = Pc;
   if (fp64_lt(eta_vep, min_eta)) eta_vep = min_eta;
   if (fp64_gt(eta_vep, max_eta)) eta_vep = max_eta;
@@ -1013,15 +1032,17 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   o.is_pl = is_pl;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
   double eta = eta_vep;
-  if (in.post_process == 1) {  // :681-714 (eta_lin uses *d, the same d as the Newton: no correction)
+  double inv = 0.0;
+  if (in.post_process != 0) {  // :681-714 (eta_lin uses *d, the same d as the Newton: no correction)
     const double inv_half_T = 2.0 / Tii_ve;
-    double inv = 0.0;
     if (diffusion) inv += e_lin * inv_half_T;
     if (peierls) inv += e_exp * inv_half_T;
     if (dislocation) inv += e_pwl * inv_half_T;
     if (constant) inv += 1.0 / eta_cst;
     if (is_pl) inv += gdot / Tii;
     eta = 1.0 / inv;
+  }
+  if (in.post_process == 1) {
     if (elastic) o.Eii_el = Tii * Tii * (0.25 * c.inv_eta_el * c.inv_eta_el);
     if (is_pl) o.Eii_pl = gdot / 2.0;
     o.div_pl = gdot * c.sin_dil;

@@ -113,7 +113,7 @@ __device__ __forceinline__ void node_prepare(const SweepArgs &A, long long i, No
   }
   n.in.centroid = n.centroid ? 1 : 0;
   n.in.final_update = A.final_update;
-  n.in.post_process = 1;
+  n.in.post_process = n.centroid ? 1 : 2;  // a vertex keeps only etaVE, eta_phys and X
   n.in.want_rho = n.centroid && (M.density_variations == 1);
   if (ANISO) node_setup_aniso(M, n.in, A.need_lnd, n.ctx, n.an);
   else node_setup_iso(M, n.in, A.need_lnd, n.ctx);
