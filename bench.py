@@ -45,11 +45,11 @@ UNIT = "point-updates/s"
 # the same field distributions at 513 x 513 cells (527,365 nodes), per workload
 # (profiles/k_sweep_plain_large_513.md, profiles/k_sweep_aniso_513.md).
 # `roofline.achieved` = this x nodes / the CUDA-event time of one launch.
-FP64_FLOPS_PER_POINT = {"plain_large": 1817.4, "aniso": 1171.9}
+FP64_FLOPS_PER_POINT = {"plain_large": 1692.9, "aniso": 1163.8}
 # DRAM bytes (read + write) per point-update of the same captures, scaled to a launch by
 # its node count; the write count of those small captures misses lines still in L2 when
 # the kernel ends.
-DRAM_BYTES_PER_POINT = {"plain_large": 267.9, "aniso": 268.3}
+DRAM_BYTES_PER_POINT = {"plain_large": 270.0, "aniso": 269.3}
 # FP64 work of k_marker_update per marker (inactive ones included), same convention:
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
