@@ -40,16 +40,17 @@ sys.path.insert(0, os.path.join(REPO, "mdoodz7.0_gb300"))
 METRIC = "rheology point-updates/s on 1 GB300: plain FP64 vs NN warm-start at tol 1e-11"
 UNIT = "point-updates/s"
 
-# FP64 work of the sweep kernel per point-update, in flops (DFMA = 2, DADD/DMUL = 1):
-# ncu's thread-level FP64 instruction counters of one k_sweep launch (default start) on
-# the same field distributions at 513 x 513 cells (527,365 nodes), per workload
-# (profiles/k_sweep_plain_large_513.md, profiles/k_sweep_aniso_513.md).
-# `roofline.achieved` = this x nodes / the CUDA-event time of one launch.
-FP64_FLOPS_PER_POINT = {"plain_large": 1692.9, "aniso": 1163.8}
-# DRAM bytes (read + write) per point-update of the same captures, scaled to a launch by
-# its node count; the write count of those small captures misses lines still in L2 when
-# the kernel ends.
-DRAM_BYTES_PER_POINT = {"plain_large": 270.0, "aniso": 269.3}
+# FP64 work of the sweep per point-update, in flops (DFMA = 2, DADD/DMUL = 1): ncu's
+# thread-level FP64 instruction counters of one sweep's two k_sweep launches (centroids,
+# then vertices; default start), summed, on the same field distributions at 513 x 513
+# cells (527,365 nodes), per workload (profiles/k_sweep_plain_large_513.md,
+# profiles/k_sweep_aniso_513.md).  `roofline.achieved` = this x nodes / the CUDA-event
+# time of one sweep (events before the first launch and after the second).
+FP64_FLOPS_PER_POINT = {"plain_large": 1697.3, "aniso": 1143.8}
+# DRAM bytes (read + write) per point-update of the same captures (both launches), scaled
+# to a sweep by its node count; the write count of those small captures misses lines still
+# in L2 when each kernel ends.
+DRAM_BYTES_PER_POINT = {"plain_large": 199.2, "aniso": 200.0}
 # FP64 work of k_marker_update per marker (inactive ones included), same convention:
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
@@ -445,7 +446,7 @@ def main():
     def summary(r):
         return {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms_step"],
                 "mean_newton_iters": r["mean_iters"], "max_newton_iters": r["maxit"],
-                "kernel_ms_per_launch": statistics.mean(r["kernel_ms"])}
+                "kernel_ms_per_sweep": statistics.mean(r["kernel_ms"])}
 
     # ---- the default path: the headline ----
     main_r = timed(0, clock=True)
@@ -469,7 +470,9 @@ def main():
         e1.record(stream)
         barrier()
         e2e_ms = REP.max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
-        bands = st.kernel_launches
+        # a vertex kernel per band, a centroid kernel per band with centroid rows (all but
+        # possibly the last)
+        bands = (st.kernel_launches + 1) // 2
         # the same calls with the copies in one piece before and after the kernel
         ctx.set_host_bands(1)
         sweep(w.model, w.mat, fh, mem=R.MEM_HOST)
@@ -720,7 +723,8 @@ def main():
                              "no flush",
                        "parallelism": f"{ws} independent grid(s), one per GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk_summary,
-            "gpu_launches": launches, "kernel_ms_per_launch": launch_ms,
+            "gpu_launches": launches, "kernel_ms_per_sweep": launch_ms,
+            "sweep_kernels": "k_sweep over the centroids, then k_sweep over the vertices: 2 launches per sweep",
             "median_kernel_ms_per_sweep": statistics.median(kernel_ms),
             "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op,
             "strain_rates": strain, "input_preparation": prep, "marker_stress": markers}

@@ -420,7 +420,7 @@ int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &
     A.ranged = 1;
     A.c_lo = (long long)coff; A.c_n = (long long)cn; A.v_lo = (long long)voff; A.v_n = (long long)vn;
     CK(launch_sweep(A, aniso, ks, ctx->block[aniso], ctx->grid_cap[aniso]));
-    ctx->launches += 1;
+    ctx->launches += sweep_kernel_count(A);
     CK(cudaEventRecord(ev[1 + B + b], ks));
     CK(cudaStreamWaitEvent(ctx->copy_out, ev[1 + B + b], 0));
     for (int i = 0; i < CO_COUNT; i++) CK(down(L.cout[i], A.co[i], coff, cn, 8));
@@ -540,7 +540,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
     const int grid = ctx->sms * tiles_blocks_per_sm(aniso, mode);
     CK(launch_sweep_tiles(A, W, aniso, mode, ctx->stream, grid));
   }
-  ctx->launches += 1;
+  ctx->launches += sweep_kernel_count(A);
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   if (collect && host) {
     CK(cudaMemcpyAsync(X, dX, items * kMlpIn * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1074,7 +1074,7 @@ int mdz_rheo_batch_create(mdz_rheo_ctx *c, int n, const mdz_model *models, const
   *out = nullptr;
   CK(cudaSetDevice(c->device));
   std::vector<SweepArgs> h((size_t)n);
-  std::vector<long long> tile_start((size_t)n + 1, 0);
+  std::vector<long long> tile_start((size_t)n + 1, 0), tile_n((size_t)n + 1, 0), tile_s((size_t)n + 1, 0);
   long long nodes = 0;
   for (int g = 0; g < n; g++) {
     SweepArgs &A = h[g];
@@ -1109,6 +1109,8 @@ int mdz_rheo_batch_create(mdz_rheo_ctx *c, int n, const mdz_model *models, const
     const long long ng = A.M.Nc + A.M.Nv;
     nodes += ng;
     tile_start[g + 1] = tile_start[g] + (ng + kBatchTile - 1) / kBatchTile;
+    tile_n[g + 1] = tile_n[g] + (A.M.Nc + kBatchTile - 1) / kBatchTile;
+    tile_s[g + 1] = tile_s[g] + (A.M.Nv + kBatchTile - 1) / kBatchTile;
   }
   mdz_rheo_batch *b = new mdz_rheo_batch();
   b->ctx = c;
@@ -1117,17 +1119,25 @@ int mdz_rheo_batch_create(mdz_rheo_ctx *c, int n, const mdz_model *models, const
   b->nodes = nodes;
   b->tiles = tile_start[n];
   if (cudaMalloc(&b->d_grids, sizeof(SweepArgs) * n) != cudaSuccess ||
-      cudaMalloc(&b->d_tile_start, sizeof(long long) * (n + 1)) != cudaSuccess ||
+      cudaMalloc(&b->d_tile_start, sizeof(long long) * 3 * (n + 1)) != cudaSuccess ||
       cudaMemcpy(b->d_grids, h.data(), sizeof(SweepArgs) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->d_tile_start, tile_start.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice) !=
-          cudaSuccess) {
+          cudaSuccess ||
+      cudaMemcpy(b->d_tile_start + (n + 1), tile_n.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMemcpy(b->d_tile_start + 2 * (n + 1), tile_s.data(), sizeof(long long) * (n + 1),
+                 cudaMemcpyHostToDevice) != cudaSuccess) {
     mdz_rheo_batch_destroy(b);
     return MDZ_ECUDA;
   }
   b->args.grids = b->d_grids;
   b->args.tile_start = b->d_tile_start;
+  b->args.tile_start_n = b->d_tile_start + (n + 1);
+  b->args.tile_start_s = b->d_tile_start + 2 * (n + 1);
   b->args.n = n;
   b->args.tiles = b->tiles;
+  b->args.tiles_n = tile_n[n];
+  b->args.tiles_s = tile_s[n];
   b->args.stats = c->d_stats;
   b->grid = (int)std::min<long long>(b->tiles, 0x7fffffffLL);
   *out = b;
@@ -1153,7 +1163,7 @@ int mdz_rheo_batch_sweep(mdz_rheo_batch *b, mdz_sweep_stats *st) {
   int rc = reset_stats(c);
   if (rc != MDZ_OK) return rc;
   c->h2d = c->d2h = 0;
-  c->launches = 1;
+  c->launches = batch_kernel_count(b->args);
   CK(cudaEventRecord(c->ev0, c->stream));
   CK(launch_sweep_batch(b->args, b->aniso, c->stream, b->grid));
   CK(cudaEventRecord(c->ev1, c->stream));
@@ -1189,7 +1199,7 @@ int mdz_rheo_batch_capture(mdz_rheo_batch *b, int nsweeps, double amp, uint64_t 
     return MDZ_ECUDA;
   }
   b->graph_sweeps = nsweeps;
-  b->graph_launches = nsweeps * (amp != 0.0 ? 2 : 1);
+  b->graph_launches = nsweeps * ((amp != 0.0 ? 1 : 0) + (int)batch_kernel_count(b->args));
   return MDZ_OK;
 }
 

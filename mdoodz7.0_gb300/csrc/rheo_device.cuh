@@ -652,8 +652,8 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   Laws &L = S.L;
   creep_laws(M, ph, c, P, in.phi, c.lnd, peierls, L);
   double Tyield = 0.0, C = in.C;
-  if (plastic == 1) {  // :530-539
-    Tyield = C * c.cos_fric + P * c.sin_fric;
+  if (plastic == 1) {  // :530-539 (products and sum rounded apart: the same bits in every kernel)
+    Tyield = __dadd_rn(__dmul_rn(C, c.cos_fric), __dmul_rn(P, c.sin_fric));
     if (fp64_lt(ph.Slim, Tyield)) { C = ph.Slim; Tyield = ph.Slim; }
   }
   double eta_cst = 0.0, Ag = 0.0, lnd = c.lnd;
@@ -741,18 +741,23 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     if (fp64_gt(F, 1e-17)) {
       const double tol = M.eta_tol, eta_vp0 = ph.eta_vp, n_vp = ph.n_vp;
       const bool vp1 = (fl & F_VP1) != 0;
-      const double ksd = K * dt * c.sin_fric * c.sin_dil;
+      // The products and sums of this return are rounded one by one (explicit intrinsics, which
+      // the compiler never fuses), as the reference's unfused arithmetic does: left to the
+      // compiler, whether a product fused into the following sum depended on the kernel the
+      // function was inlined into, and the iteration magnified that last bit.
+      const double Kdt = __dmul_rn(K, dt);
+      const double ksd = __dmul_rn(__dmul_rn(Kdt, c.sin_fric), c.sin_dil);
       double Tiic = 0.0;
       is_pl = 1;
       eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
       gdot = F / (eta_ve + eta_vp + ksd);
       const double F0 = F;
       for (int it = 0; it < 20; it++) {
-        divp = gdot * c.sin_dil;
-        Pc = P + K * dt * divp;
+        divp = __dmul_rn(gdot, c.sin_dil);
+        Pc = __dadd_rn(P, __dmul_rn(Kdt, divp));
         eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
-        Tyield = Tyield + gdot * eta_vp;
-        Tiic = Tii - eta_ve * gdot;
+        Tyield = __dadd_rn(Tyield, __dmul_rn(gdot, eta_vp));
+        Tiic = __dsub_rn(Tii, __dmul_rn(eta_ve, gdot));
         F = Tiic - Tyield;
         if (fp64_abs_lt(F, tol) || fp64_abs_lt(F, tol * F0)) break;
         gdot -= F / (-eta_ve - eta_vp / n_vp - ksd);
@@ -791,8 +796,8 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   const auto dissipative = [&](double &inv_half_T) {
     inv_half_T = 2.0 / Tii_ve;  // 1/eta_k = 2 Eii_k / Tii
     double inv = 0.0;
-    if (peierls) inv += e_exp * inv_half_T;
-    if (dislocation) inv += e_pwl * inv_half_T;
+    if (peierls) inv = __fma_rn(e_exp, inv_half_T, inv);
+    if (dislocation) inv = __fma_rn(e_pwl, inv_half_T, inv);
     if (diffusion) {
       // eta_lin = B pow(Eii_lin, 1/n-1) pow(d1, m/n) = Tii/(2 Eii_lin) (d1/d)^(m/n), d1 = gs_ref
       double inv_lin = e_lin * inv_half_T;
@@ -821,7 +826,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
         const double Tyy = -(o.Txx + o.Tzz), Tyy0 = -(in.Txx0 + in.Tzz0);
         const double ex = (o.Txx - in.Txx0) * h, ez = (o.Tzz - in.Tzz0) * h;
         const double ey = (Tyy - Tyy0) * h, exz = (o.Txz - in.Txz0) * h;
-        o.Eii_el = sqrt(0.5 * (ex * ex + ez * ez + ey * ey) + exz * exz);
+        o.Eii_el = sqrt(__fma_rn(0.5, __fma_rn(ey, ey, __fma_rn(ez, ez, __dmul_rn(ex, ex))), __dmul_rn(exz, exz)));
       }
       o.Eii_pl = (is_pl && plastic == 1) ? gdot / 2.0 : ((is_pl && plastic == 2) ? lam_dot * A_tau : 0.0);
       o.div_pl = divp;
@@ -914,8 +919,8 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   L.mech &= ~F_GBS;  // the anisotropic path has no grain-boundary sliding
   L.ln_inv_gbs = -kInf;
   double Tyield = 0.0, Coh = in.C;
-  if (plastic) {  // :370-377
-    Tyield = Coh * c.cos_fric + P * c.sin_fric;
+  if (plastic) {  // :370-377 (products and sum rounded apart: the same bits in every kernel)
+    Tyield = __dadd_rn(__dmul_rn(Coh, c.cos_fric), __dmul_rn(P, c.sin_fric));
     if (ph.Slim < Tyield) { Coh = ph.Slim; Tyield = ph.Slim; }
   }
   const double eta_cst = constant ? ph.eta0 : 0.0;
@@ -1008,9 +1013,11 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   int is_pl = 0;
   if (fp64_gt(Ft, 1e-17) && plastic) {  // :625-648
     is_pl = 1;
-    gdot = Ft / (eta_ve + ph.eta_vp + K * dt * c.sin_dil * c.sin_fric);
-    const double Tiic = Tii - gdot * eta_ve;
-    Pc = P + K * dt * c.sin_dil * gdot;
+    // rounded one by one, as in the isotropic return
+    const double Kdt_sd = __dmul_rn(__dmul_rn(K, dt), c.sin_dil);
+    gdot = Ft / __dadd_rn(__dadd_rn(eta_ve, ph.eta_vp), __dmul_rn(Kdt_sd, c.sin_fric));
+    const double Tiic = __dsub_rn(Tii, __dmul_rn(gdot, eta_ve));
+    Pc = __dadd_rn(P, __dmul_rn(Kdt_sd, gdot));
     eta_vep = Tiic * c.inv2Eii;
     Tr_xx = 2.0 * eta_vep * an.Er_xx;
     Tr_zz = 2.0 * eta_vep * an.Er_zz;

@@ -1,13 +1,16 @@
 // rheo_kernels.cu -- sweep and point kernels of the local rheology update (sm_103a).
 //
-// k_sweep<ANISO> is NonNewtonianViscosityGrid (MDLIB/RheologyDensity.c:1131-1426) /
+// k_sweep<ANISO, NODES> is NonNewtonianViscosityGrid (MDLIB/RheologyDensity.c:1131-1426) /
 // NonNewtonianViscosityGridAniso (MDLIB/AnisotropyRoutines.c:885-1217) with the four
 // InterpCentroidsToVerticesDouble calls (:1150-1153) fused into the vertex pass: one
-// thread per node over the index space [centroids | vertices], per-phase tables in the
+// thread per node over the index space [centroids | vertices], launched once over the
+// centroids (NODES 1) and once over the vertices (NODES 2) so that each kernel carries only
+// its own kind's work (vertices skip the per-phase outputs only centroids keep), per-phase
+// tables in the
 // kernel's constant parameter bank (uniform across a warp, so every lookup is a
 // broadcast), SoA loads and stores coalesced along the node index.
 //
-// k_sweep_tiles<ANISO, MODE> walks the same index space in tiles of 128 nodes, one tile
+// k_sweep_tiles<ANISO, MODE, NODES> walks the same index space in tiles of 128 nodes, one tile
 // per CTA at a time, with the phase loop uniform over the CTA so that a block-wide stage
 // can sit between each phase's set-up and its local solve: the learned warm start
 // (MODE_WARM: tcgen05 MLP guess, then the FP32 polish) or the training-data dump
@@ -44,10 +47,12 @@ struct Node {
   AnisoNode an;
 };
 
-template <bool ANISO>
+// NODES: 0 either kind (index i decides), 1 centroids only, 2 vertices only; a kernel
+// specialised to one kind of node drops the other kind's code and registers
+template <bool ANISO, int NODES = 0>
 __device__ __forceinline__ void node_prepare(const SweepArgs &A, long long i, Node &n) {
   const ModelConst &M = A.M;
-  n.centroid = i < M.Nc;
+  n.centroid = NODES == 1 ? true : (NODES == 2 ? false : i < M.Nc);
   const double el = (M.elastic == 1) ? 1.0 : 0.0;
   double mu, exxd, ezzd, exz;
   if (n.centroid) {
@@ -229,10 +234,10 @@ __device__ __forceinline__ void flush_acc(DevStats *st, Acc &acc) {
 // plain sweep: one thread per node
 // ---------------------------------------------------------------------------------
 // One node of one grid: prepare, every active phase's local solve, averaging, store.
-template <bool ANISO>
+template <bool ANISO, int NODES = 0>
 __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc &acc) {
   Node n;
-  node_prepare<ANISO>(A, i, n);
+  node_prepare<ANISO, NODES>(A, i, n);
   double out[CO_COUNT];
 #pragma unroll
   for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
@@ -253,14 +258,16 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
   node_store<ANISO>(A, n, out, status);
 }
 
-template <bool ANISO>
+// One sweep is two launches: the centroids (NODES 1), then the vertices (NODES 2), each
+// over its whole range or over the band of rows a banded sweep gives it.
+template <bool ANISO, int NODES>
 __global__ void __launch_bounds__(128) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0};
-  const long long nc = A.ranged ? A.c_n : A.M.Nc, total = nc + (A.ranged ? A.v_n : A.M.Nv);
-  const long long c_lo = A.ranged ? A.c_lo : 0, v_lo = A.M.Nc + (A.ranged ? A.v_lo : 0);
+  const long long total = NODES == 1 ? (A.ranged ? A.c_n : A.M.Nc) : (A.ranged ? A.v_n : A.M.Nv);
+  const long long lo = NODES == 1 ? (A.ranged ? A.c_lo : 0) : A.M.Nc + (A.ranged ? A.v_lo : 0);
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride)
-    sweep_node<ANISO>(A, j < nc ? c_lo + j : v_lo + (j - nc), acc);
+    sweep_node<ANISO, NODES>(A, lo + j, acc);
   flush_acc(A.stats, acc);
 }
 
@@ -269,24 +276,29 @@ __global__ void __launch_bounds__(128) k_sweep(const __grid_constant__ SweepArgs
 // kBatchTile nodes, so a CTA's tile lies in one grid; the grid's arguments are read
 // from global memory (uniform over the CTA, served by L1)
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ int batch_grid_of(const BatchArgs &B, long long tile) {
-  int lo = 0, hi = B.n - 1;
+__device__ __forceinline__ int batch_grid_of(const long long *tile_start, int n, long long tile) {
+  int lo = 0, hi = n - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&B.tile_start[mid]) <= tile) lo = mid;
+    if (__ldg(&tile_start[mid]) <= tile) lo = mid;
     else hi = mid - 1;
   }
   return lo;
 }
 
-template <bool ANISO>
+// One kernel per kind of node, as for a single grid (and with the same node body, so a
+// grid swept here gives the single-grid results to the bit): the centroid tiles of every
+// grid (NODES 1), then the vertex tiles (NODES 2).
+template <bool ANISO, int NODES>
 __global__ void __launch_bounds__(kBatchTile) k_sweep_batch(const __grid_constant__ BatchArgs B) {
   Acc acc = {0, 0, 0, 0};
-  for (long long t = blockIdx.x; t < B.tiles; t += gridDim.x) {
-    const int g = batch_grid_of(B, t);
+  const long long *ts = NODES == 1 ? B.tile_start_n : B.tile_start_s;
+  const long long tiles = NODES == 1 ? B.tiles_n : B.tiles_s;
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int g = batch_grid_of(ts, B.n, t);
     const SweepArgs &A = B.grids[g];
-    const long long i = (t - __ldg(&B.tile_start[g])) * kBatchTile + threadIdx.x;
-    if (i < A.M.Nc + A.M.Nv) sweep_node<ANISO>(A, i, acc);
+    const long long j = (t - __ldg(&ts[g])) * kBatchTile + threadIdx.x;
+    if (j < (NODES == 1 ? A.M.Nc : A.M.Nv)) sweep_node<ANISO, NODES>(A, NODES == 1 ? j : A.M.Nc + j, acc);
   }
   flush_acc(B.stats, acc);
 }
@@ -311,7 +323,7 @@ __device__ __forceinline__ double perturb_factor(unsigned long long key, long lo
 __global__ void __launch_bounds__(kBatchTile) k_perturb_batch(const __grid_constant__ BatchArgs B, double amp,
                                                              unsigned long long seed, int sweep) {
   for (long long t = blockIdx.x; t < B.tiles; t += gridDim.x) {
-    const int g = batch_grid_of(B, t);
+    const int g = batch_grid_of(B.tile_start, B.n, t);
     const SweepArgs &A = B.grids[g];
     const long long i = (t - __ldg(&B.tile_start[g])) * kBatchTile + threadIdx.x;
     const long long Nc = A.M.Nc;
@@ -335,7 +347,9 @@ __global__ void __launch_bounds__(kBatchTile) k_perturb_batch(const __grid_const
 // ---------------------------------------------------------------------------------
 // tiled sweep with a block-wide stage per phase (learned warm start / data collection)
 // ---------------------------------------------------------------------------------
-template <bool ANISO, int MODE>
+// NODES 1 sweeps the centroids, NODES 2 the vertices (one launch each, with the node
+// bodies of the plain sweep's two kernels).
+template <bool ANISO, int MODE, int NODES>
 __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ SweepArgs A,
                                                      const __grid_constant__ WarmArgs W) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -344,15 +358,17 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
   if (MODE == MODE_WARM) mlp_begin(S, W.mlp);
   Acc acc = {0, 0, 0, 0};
   const long long total = A.M.Nc + A.M.Nv;
-  const long long ntiles = (total + kMlpTile - 1) / kMlpTile;
+  const long long count = NODES == 1 ? A.M.Nc : A.M.Nv, base = NODES == 1 ? 0 : A.M.Nc;
+  const long long ntiles = (count + kMlpTile - 1) / kMlpTile;
   const int nfeat = ANISO ? kFeatAniso : kFeatIso;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {  // uniform over the CTA
-    const long long i = tile * kMlpTile + threadIdx.x;
-    const bool valid = i < total;
+    const long long j = tile * kMlpTile + threadIdx.x;
+    const bool valid = j < count;
+    const long long i = base + j;
     Node n;
     n.solid = false;
-    n.centroid = true;
-    if (valid) node_prepare<ANISO>(A, i, n);
+    n.centroid = NODES == 1;
+    if (valid) node_prepare<ANISO, NODES>(A, i, n);
     double out[CO_COUNT];
 #pragma unroll
     for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
@@ -464,22 +480,28 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArg
 }
 
 cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap) {
-  const long long total = a.ranged ? a.c_n + a.v_n : a.M.Nc + a.M.Nv;
-  long long grid = (total + block - 1) / block;
-  if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
-  if (grid < 1) grid = 1;
-  if (aniso) k_sweep<true><<<(unsigned)grid, block, 0, s>>>(a);
-  else k_sweep<false><<<(unsigned)grid, block, 0, s>>>(a);
-  return cudaGetLastError();
+  const long long counts[2] = {a.ranged ? a.c_n : a.M.Nc, a.ranged ? a.v_n : a.M.Nv};
+  for (int kind = 0; kind < 2; kind++) {
+    if (counts[kind] <= 0) continue;
+    long long grid = (counts[kind] + block - 1) / block;
+    if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
+    if (kind == 0 && aniso) k_sweep<true, 1><<<(unsigned)grid, block, 0, s>>>(a);
+    else if (kind == 0) k_sweep<false, 1><<<(unsigned)grid, block, 0, s>>>(a);
+    else if (aniso) k_sweep<true, 2><<<(unsigned)grid, block, 0, s>>>(a);
+    else k_sweep<false, 2><<<(unsigned)grid, block, 0, s>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 // The warm-start form keeps its MLP tiles in dynamic shared memory; asking for the
 // largest shared-memory carve-out lets two of its CTAs share an SM (the register file
 // allows two), which the occupancy query then reports.
-template <bool ANISO, int MODE>
+template <bool ANISO, int MODE, int NODES>
 static void tiles_attributes() {
   if (MODE != MODE_WARM) return;
-  auto fn = k_sweep_tiles<ANISO, MODE>;
+  auto fn = k_sweep_tiles<ANISO, MODE, NODES>;
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpShared));
   cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
 }
@@ -487,8 +509,14 @@ static void tiles_attributes() {
 template <bool ANISO, int MODE>
 static cudaError_t launch_tiles_t(const SweepArgs &a, const WarmArgs &w, cudaStream_t s, int grid) {
   const size_t smem = (MODE == MODE_WARM) ? sizeof(MlpShared) : 0;
-  tiles_attributes<ANISO, MODE>();
-  k_sweep_tiles<ANISO, MODE><<<grid, kMlpTile, smem, s>>>(a, w);
+  const long long tiles[2] = {(a.M.Nc + kMlpTile - 1) / kMlpTile, (a.M.Nv + kMlpTile - 1) / kMlpTile};
+  tiles_attributes<ANISO, MODE, 1>();
+  tiles_attributes<ANISO, MODE, 2>();
+  if (tiles[0] > 0)
+    k_sweep_tiles<ANISO, MODE, 1><<<(unsigned)(tiles[0] < grid ? tiles[0] : grid), kMlpTile, smem, s>>>(a, w);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || tiles[1] <= 0) return e;
+  k_sweep_tiles<ANISO, MODE, 2><<<(unsigned)(tiles[1] < grid ? tiles[1] : grid), kMlpTile, smem, s>>>(a, w);
   return cudaGetLastError();
 }
 
@@ -508,15 +536,15 @@ int tiles_blocks_per_sm(bool aniso, int mode) {
   int n = 0;
   const void *fn = nullptr;
   switch (mode * 2 + (aniso ? 1 : 0)) {
-    case MODE_COLLECT * 2: fn = (const void *)k_sweep_tiles<false, MODE_COLLECT>; break;
-    case MODE_COLLECT * 2 + 1: fn = (const void *)k_sweep_tiles<true, MODE_COLLECT>; break;
-    case MODE_WARM * 2: fn = (const void *)k_sweep_tiles<false, MODE_WARM>; break;
-    default: fn = (const void *)k_sweep_tiles<true, MODE_WARM>; break;
+    case MODE_COLLECT * 2: fn = (const void *)k_sweep_tiles<false, MODE_COLLECT, 1>; break;
+    case MODE_COLLECT * 2 + 1: fn = (const void *)k_sweep_tiles<true, MODE_COLLECT, 1>; break;
+    case MODE_WARM * 2: fn = (const void *)k_sweep_tiles<false, MODE_WARM, 1>; break;
+    default: fn = (const void *)k_sweep_tiles<true, MODE_WARM, 1>; break;
   }
   const size_t smem = (mode == MODE_WARM) ? sizeof(MlpShared) : 0;
   if (mode == MODE_WARM) {
-    if (aniso) tiles_attributes<true, MODE_WARM>();
-    else tiles_attributes<false, MODE_WARM>();
+    if (aniso) tiles_attributes<true, MODE_WARM, 1>();
+    else tiles_attributes<false, MODE_WARM, 1>();
   }
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kMlpTile, smem);
   // The query has been seen to report one CTA where registers (255 per thread, 2 CTAs
@@ -535,9 +563,16 @@ int tiles_blocks_per_sm(bool aniso, int mode) {
 }
 
 cudaError_t launch_sweep_batch(const BatchArgs &b, bool aniso, cudaStream_t s, int grid) {
-  if (grid < 1) grid = 1;
-  if (aniso) k_sweep_batch<true><<<grid, kBatchTile, 0, s>>>(b);
-  else k_sweep_batch<false><<<grid, kBatchTile, 0, s>>>(b);
+  // one CTA per tile, up to `grid`, per kind
+  const long long gn = b.tiles_n < grid ? b.tiles_n : grid, gs = b.tiles_s < grid ? b.tiles_s : grid;
+  if (gn > 0) {
+    if (aniso) k_sweep_batch<true, 1><<<(unsigned)gn, kBatchTile, 0, s>>>(b);
+    else k_sweep_batch<false, 1><<<(unsigned)gn, kBatchTile, 0, s>>>(b);
+  }
+  if (gs > 0) {
+    if (aniso) k_sweep_batch<true, 2><<<(unsigned)gs, kBatchTile, 0, s>>>(b);
+    else k_sweep_batch<false, 2><<<(unsigned)gs, kBatchTile, 0, s>>>(b);
+  }
   return cudaGetLastError();
 }
 
@@ -557,7 +592,8 @@ cudaError_t launch_points(const PointArgs &a, cudaStream_t s) {
 
 void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block) {
   cudaFuncAttributes fa;
-  const void *fn = aniso ? (const void *)k_sweep<true> : (const void *)k_sweep<false>;
+  // the centroid kernel: the larger of the two, it sets the launch shape
+  const void *fn = aniso ? (const void *)k_sweep<true, 1> : (const void *)k_sweep<false, 1>;
   cudaFuncGetAttributes(&fa, fn);
   *regs = fa.numRegs;
   *smem = (int)fa.sharedSizeBytes;

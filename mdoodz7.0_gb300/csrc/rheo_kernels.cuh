@@ -64,9 +64,12 @@ struct SweepArgs {
 constexpr int kBatchTile = 128;
 struct BatchArgs {
   const SweepArgs *grids;       // device array [n]
-  const long long *tile_start;  // device array [n + 1]
+  const long long *tile_start;  // device array [n + 1]: tiles over each grid's nodes
+  // the same cut over the centroids and over the vertices separately, for the sweep's
+  // two kernels (device arrays [n + 1])
+  const long long *tile_start_n, *tile_start_s;
   int n;
-  long long tiles;
+  long long tiles, tiles_n, tiles_s;
   DevStats *stats;
 };
 
@@ -82,6 +85,14 @@ struct PointArgs {
 };
 
 cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap);
+// kernels launch_sweep issues for these arguments: one per kind of node (centroids,
+// vertices) with nodes in range; launch_sweep_tiles issues the same over the whole grid
+inline unsigned sweep_kernel_count(const SweepArgs &a) {
+  const long long nc = a.ranged ? a.c_n : a.M.Nc, nv = a.ranged ? a.v_n : a.M.Nv;
+  return (nc > 0 ? 1u : 0u) + (nv > 0 ? 1u : 0u);
+}
+// kernels launch_sweep_batch issues: one per kind of node with tiles
+inline unsigned batch_kernel_count(const BatchArgs &b) { return (b.tiles_n > 0 ? 1u : 0u) + (b.tiles_s > 0 ? 1u : 0u); }
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s);
 cudaError_t launch_sweep_batch(const BatchArgs &b, bool aniso, cudaStream_t s, int grid);
 cudaError_t launch_perturb_batch(const BatchArgs &b, double amp, unsigned long long seed, int sweep, cudaStream_t s,

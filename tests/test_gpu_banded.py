@@ -54,7 +54,7 @@ def test_banded_host_sweep_is_the_one_shot_sweep(ctx, name):
     ctx.set_host_bands(1)
     one = clone(w.arrays)
     _, st1 = fn(w.model, w.mat, R.FieldSet(one))
-    assert st1.kernel_launches == 1
+    assert st1.kernel_launches == 2  # the centroid kernel and the vertex kernel
     # the device-resident sweep on the same inputs
     dev = {k: ([torch.from_numpy(x.copy()).cuda() for x in v] if isinstance(v, list) else
                torch.from_numpy(v.copy()).cuda()) for k, v in w.arrays.items()}
@@ -64,7 +64,9 @@ def test_banded_host_sweep_is_the_one_shot_sweep(ctx, name):
         ctx.set_host_bands(bands)
         got = clone(w.arrays)
         _, st = fn(w.model, w.mat, R.FieldSet(got))
-        assert st.kernel_launches == min(bands, w.model.Nz)
+        # a vertex kernel per band and a centroid kernel per band with centroid rows (all but
+        # a last band holding only the last vertex row)
+        assert 2 * min(bands, w.model.Nz) - 1 <= st.kernel_launches <= 2 * min(bands, w.model.Nz)
         assert st.phase_calls == st1.phase_calls and st.newton_iters == st1.newton_iters
         assert st.h2d_bytes == st1.h2d_bytes and st.d2h_bytes == st1.d2h_bytes
         same(one, got)
