@@ -470,8 +470,9 @@ int mdz_rheo_points_static(const mdz_model *model, const mdz_materials *mat, con
                            mdz_sweep_stats *stats);
 /* ---- many grids in one launch (no reference counterpart) ----------------
  * A batch is n device-resident grids (MDZ_MEM_DEVICE fields), each with its own model,
- * material table and size, swept together by one kernel launch: the node range of
- * every grid is cut into tiles of 128 nodes and one CTA takes one tile.  The grids'
+ * material table and size, swept together by two kernel launches, one over every grid's
+ * centroids and one over every grid's vertices: each grid's centroids (vertices) are
+ * cut into tiles of 128 nodes and one CTA takes one tile.  The grids'
  * arguments are folded and uploaded once, at creation; the field arrays must stay
  * valid until the batch is destroyed.  `flags` may hold MDZ_SWEEP_REF_START only.
  * stats->error_node counts nodes through the batch in order (grid 0's centroids, its
@@ -481,7 +482,8 @@ int mdz_rheo_batch_create(mdz_rheo_ctx *ctx, int n, const mdz_model *models, con
                           const mdz_grid_fields *fields, int aniso, int final_update, int flags,
                           mdz_rheo_batch **out);
 int mdz_rheo_batch_destroy(mdz_rheo_batch *batch);
-/* One sweep of every grid of the batch: one launch on the context's stream, blocking. */
+/* One sweep of every grid of the batch: the centroid and the vertex launch on the
+ * context's stream, blocking. */
 int mdz_rheo_batch_sweep(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
 /* Capture `nsweeps` consecutive batch sweeps as one CUDA graph (replacing any earlier
  * capture).  With amp != 0 every sweep is preceded by a perturbation of the strain-rate

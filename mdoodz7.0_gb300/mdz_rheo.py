@@ -507,7 +507,7 @@ def python_struct_sizes():
 
 
 class Batch:
-    """Many device-resident grids swept by one launch (mdz_rheo_batch_*).  `fieldsets` are
+    """Many device-resident grids swept together, one launch per kind of node (mdz_rheo_batch_*).  `fieldsets` are
     FieldSets over device tensors; they (and their tensors) must outlive the batch."""
 
     def __init__(self, ctx: "Context", models, mats, fieldsets, aniso=False, final_update=0, flags=0):
