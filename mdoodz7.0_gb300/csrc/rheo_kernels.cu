@@ -260,12 +260,12 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
 
 // One sweep is two launches: the centroids (NODES 1), then the vertices (NODES 2), each
 // over its whole range or over the band of rows a banded sweep gives it.
-// Three CTAs of 128 per SM for the vertex kernel (168 registers and a few hundred bytes of
-// spills: 12 warps per SM hide more of the FP64 pipe's latency than the spills cost, 1.6 %
-// faster at 2049 x 2049 cells); two for the centroid kernel, whose larger body spills too
-// much at 168.
+// Three CTAs of 128 per SM (168 registers, and a few hundred bytes of spills: 336 B for the
+// vertex kernel, 532 B for the centroid kernel).  Twelve warps per SM hide more of the FP64
+// pipe's latency than the spills cost: at 2049 x 2049 cells the default-start sweep takes
+// 22.47 ms against 23.12 ms with two CTAs per SM and no spills.
 template <bool ANISO, int NODES>
-__global__ void __launch_bounds__(128, NODES == 2 ? 3 : 2) k_sweep(const __grid_constant__ SweepArgs A) {
+__global__ void __launch_bounds__(128, 3) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0};
   const long long total = NODES == 1 ? (A.ranged ? A.c_n : A.M.Nc) : (A.ranged ? A.v_n : A.M.Nv);
   const long long lo = NODES == 1 ? (A.ranged ? A.c_lo : 0) : A.M.Nc + (A.ranged ? A.v_lo : 0);
@@ -294,7 +294,7 @@ __device__ __forceinline__ int batch_grid_of(const long long *tile_start, int n,
 // grid swept here gives the single-grid results to the bit): the centroid tiles of every
 // grid (NODES 1), then the vertex tiles (NODES 2).
 template <bool ANISO, int NODES>
-__global__ void __launch_bounds__(kBatchTile, NODES == 2 ? 3 : 2) k_sweep_batch(const __grid_constant__ BatchArgs B) {
+__global__ void __launch_bounds__(kBatchTile, 3) k_sweep_batch(const __grid_constant__ BatchArgs B) {
   Acc acc = {0, 0, 0, 0};
   const long long *ts = NODES == 1 ? B.tile_start_n : B.tile_start_s;
   const long long tiles = NODES == 1 ? B.tiles_n : B.tiles_s;
