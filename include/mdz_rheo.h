@@ -80,6 +80,12 @@ extern "C" {
 #define MDZ_SWEEP_ITERS      0x4  /* record per-(node,phase) local iteration counts (mdz_rheo_get_iterations) */
 #define MDZ_SWEEP_REF_START  0x8  /* start each local Newton where the reference does (see below) */
 #define MDZ_DEFAULT_POLISH   4    /* FP32 Newton steps before each FP64 local solve, by default */
+/* Start descriptor of the local solves (mdz_rheo_set_warmstart): FP32 Newton steps in the
+ * low byte, plus MDZ_START_DD for one Halley step evaluated in double-float (FP32 pairs)
+ * after them.  The default takes both, which puts the FP64 Newton's start within its
+ * stopping tolerance, so it stops at its first evaluation. */
+#define MDZ_START_DD         0x100
+#define MDZ_DEFAULT_START    (MDZ_DEFAULT_POLISH | MDZ_START_DD)
 
 /* ---- per-phase material table -----------------------------------------
  * The subset of `mat_prop` (MDLIB/include/mdoodz.h:152-240) that the local
@@ -256,10 +262,11 @@ int mdz_rheo_set_host_bands(mdz_rheo_ctx *ctx, int bands);
  * Start of the local solves: the reference starts its visco-elastic Newton at the
  * smallest isolated viscosity (RheologyDensity.c:582-592; after 10 bisection steps in
  * the anisotropic routine, AnisotropyRoutines.c:474-497).  By default the FP64 Newton
- * here starts after MDZ_DEFAULT_POLISH FP32 Newton steps from that point; it still
- * iterates to the reference's residual tolerance (|r| < 1e-13 Eii), so results agree
- * with the reference to that tolerance.  MDZ_SWEEP_REF_START starts exactly where the
- * reference does (same iteration counts). */
+ * here starts after MDZ_DEFAULT_POLISH FP32 Newton steps from that point and one
+ * double-float Halley step (MDZ_DEFAULT_START); it still iterates to the reference's
+ * residual tolerance (|r| < 1e-13 Eii), so results agree with the reference to that
+ * tolerance.  MDZ_SWEEP_REF_START starts exactly where the reference does (same
+ * iteration counts). */
 int mdz_rheo_sweep(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                    const mdz_grid_fields *f, int final_update, int mem, int flags,
                    mdz_sweep_stats *stats);
@@ -521,10 +528,11 @@ int mdz_rheo_get_launch_shape(mdz_rheo_ctx *ctx, int aniso, int *block, int *gri
 int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);
 
 /* ---- learned warm start (no reference counterpart) --------------------- */
-/* Install the network used by MDZ_SWEEP_WARMSTART (NULL removes it) and the number of
- * FP32 Newton steps taken before every FP64 local solve (after the network's guess with
- * MDZ_SWEEP_WARMSTART, from the reference's start point otherwise; 0 = start exactly
- * where the reference does).  The default is MDZ_DEFAULT_POLISH. */
+/* Install the network used by MDZ_SWEEP_WARMSTART (NULL removes it) and the start
+ * descriptor of every FP64 local solve: FP32 Newton steps (0..64) in the low byte,
+ * optionally | MDZ_START_DD (after the network's guess with MDZ_SWEEP_WARMSTART, from the
+ * reference's start point otherwise; 0 = start exactly where the reference does).  The
+ * default is MDZ_DEFAULT_START. */
 int mdz_rheo_set_warmstart(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, int polish_iters);
 /* A plain sweep (iso or aniso) that also records, for every (phase p, node i) item,
  * item = p * (Nc + Nv) + i (centroids first), the MDZ_MLP_IN features X[item][.] and
@@ -570,6 +578,11 @@ int mdz_rheo_div_selftest(int device, const double *a, int64_t n, double b, doub
  * bits of q (saturated to +-2^30 beyond that range and for NaN) and CUDA's ceil, for n
  * host arguments.  No reference counterpart. */
 int mdz_rheo_ceil_selftest(int device, const double *q, int64_t n, int32_t *fast_out, double *cuda_out);
+/* Self-check of the double-float arithmetic of the local solve's start: for n host
+ * arguments x, out[6 i ..] = the (hi, lo) FP32 pairs of x, of exp(x) and of log(x
+ * rounded to FP32) (0 where that is not a positive normal FP32 number).  No reference
+ * counterpart. */
+int mdz_rheo_dd_selftest(int device, const double *x, int64_t n, float *out);
 
 #ifdef __cplusplus
 }

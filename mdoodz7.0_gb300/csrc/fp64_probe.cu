@@ -9,9 +9,12 @@
 // mdz_rheo_div_selftest: the division by a known divisor of fp64_div.cuh next to CUDA's
 // division, for the bit-for-bit test.
 // mdz_rheo_ceil_selftest: the integer-pipe ceil of fp64_bits.cuh next to CUDA's ceil.
+// mdz_rheo_dd_selftest: the double-float conversion, exp and log of dd_math.cuh, for the
+// accuracy tests.
 #include <cuda_runtime.h>
 
 #include "../../include/mdz_rheo.h"
+#include "dd_math.cuh"
 #include "fp64_div.cuh"
 #include "fp64_math.cuh"
 
@@ -57,7 +60,40 @@ __global__ void k_ceil(const double *q, long long n, int *fast, double *plain) {
   plain[i] = ceil(q[i]);
 }
 
+// per argument: dd_of_f64(x), dd_exp(dd_of_f64(x)), dd_log_f(x rounded to FP32), as
+// (hi, lo) pairs
+__global__ void k_dd(const double *x, long long n, float *out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const mdz::f2 a = mdz::dd_of_f64(x[i]);
+  const mdz::f2 e = mdz::dd_exp(a);
+  const float s = __double2float_rn(x[i]);
+  const mdz::f2 l = (s > 1.17549435e-38f && s < 3.4e38f) ? mdz::dd_log_f(s) : mdz::f2{0.0f, 0.0f};
+  float *o = out + 6 * i;
+  o[0] = a.hi; o[1] = a.lo; o[2] = e.hi; o[3] = e.lo; o[4] = l.hi; o[5] = l.lo;
+}
+
 }  // namespace
+
+extern "C" int mdz_rheo_dd_selftest(int device, const double *x, int64_t n, float *out) {
+  if (!x || n < 0 || !out) return MDZ_EINVAL;
+  if (n == 0) return MDZ_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return MDZ_ECUDA;
+  const size_t bx = (size_t)n * sizeof(double), bo = (size_t)n * 6 * sizeof(float);
+  void *d = nullptr;
+  if (cudaMalloc(&d, bx + bo) != cudaSuccess) return MDZ_ENOMEM;
+  double *dx = (double *)d;
+  float *dout = (float *)((char *)d + bx);
+  int rc = MDZ_OK;
+  if (cudaMemcpy(dx, x, bx, cudaMemcpyHostToDevice) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK) {
+    k_dd<<<(unsigned)((n + 255) / 256), 256>>>(dx, n, dout);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = MDZ_ECUDA;
+  }
+  if (rc == MDZ_OK && cudaMemcpy(out, dout, bo, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
+  cudaFree(d);
+  return rc;
+}
 
 extern "C" int mdz_rheo_ceil_selftest(int device, const double *q, int64_t n, int32_t *fast_out, double *cuda_out) {
   if (!q || n < 0 || !fast_out || !cuda_out) return MDZ_EINVAL;

@@ -50,7 +50,7 @@ struct mdz_rheo_ctx {
   // learned warm start
   void *warm_buf = nullptr;  // tiles W1, W2, W3 + biases b1, b2, b3[16]
   MlpDevice warm{};
-  int warm_ready = 0, polish_iters = MDZ_DEFAULT_POLISH;
+  int warm_ready = 0, polish_iters = MDZ_DEFAULT_START;
   unsigned mma_fault = 0;
 };
 
@@ -978,7 +978,7 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
       if (in->phase[i] < 0 || in->phase[i] >= A.M.np) return MDZ_EINVAL;
   A.n = n;
   A.aniso = aniso;
-  A.polish = MDZ_DEFAULT_POLISH;
+  A.polish = MDZ_DEFAULT_START;
   A.in = *in;
   A.out = *out;
   // layout of the array: statistics, then (host memory) one 256-aligned slot per array
@@ -1709,7 +1709,8 @@ int mdz_rheo_get_iterations(mdz_rheo_ctx *c, int32_t *out_n, int32_t *out_s) {
 
 
 int mdz_rheo_set_warmstart(mdz_rheo_ctx *c, const mdz_mlp_weights *w, int polish_iters) {
-  if (!c || polish_iters < 0 || polish_iters > 64) return MDZ_EINVAL;
+  if (!c || polish_iters < 0 || (polish_iters & ~(0xff | MDZ_START_DD)) || (polish_iters & 0xff) > 64)
+    return MDZ_EINVAL;
   CK(cudaSetDevice(c->device));
   c->polish_iters = polish_iters;
   if (!w) { c->warm_ready = 0; return MDZ_OK; }

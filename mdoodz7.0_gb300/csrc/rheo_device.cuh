@@ -31,6 +31,7 @@
 #include <stdint.h>
 
 #include "../../include/mdz_rheo.h"
+#include "dd_math.cuh"
 #include "fp64_bits.cuh"
 #include "fp64_div.cuh"
 #include "fp64_math.cuh"
@@ -316,22 +317,20 @@ __device__ __forceinline__ void ve_coef(const Laws &L, const NodeCtx &c, double 
   q.Aup = A * eta_up;
 }
 
-// Residual r and S = sum_k n_k Eii_k at sv.  With step >= 0 the non-linear terms are
-// carried from the previous point sv / (1 + step) by the binomial series
+// Residual r at sv; the strain rates of the non-linear laws stay in s.e.  With step >= 0
+// the non-linear terms are carried from the previous point sv / (1 + step) by the
+// binomial series
 //     (1 + step)^n = 1 + n step (1 + (n - 1) step / 2) + O((n step)^3),
 // used only where |n step| < 1e-5, so the dropped term is below 2e-16 relative: the same
 // residual as a fresh evaluation to rounding, without its log and exps.
-__device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, double &r, double &S,
-                                        double step = -1.0) {
+__device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, double &r, double step = -1.0) {
   double *e = s.e;
-  S = 0.0;
   if (fp64_ge(step, -0.5)) {
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
       if (q.nl >> k & 1) {
         const double t = step * q.n[k];
         e[k] = fma(e[k] * t, fma(step, q.hn[k], 1.0), e[k]);
-        S = fma(q.n[k], e[k], S);
       }
   } else {
     e[0] = e[1] = e[2] = 0.0;
@@ -339,10 +338,7 @@ __device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, 
       const double lx = fast_log(sv) + q.lp;
 #pragma unroll
       for (int k = 0; k < K_COUNT; k++)
-        if (q.nl >> k & 1) {
-          e[k] = q.Eii * fast_exp(fma(q.n[k], lx, q.nc[k]));
-          S = fma(q.n[k], e[k], S);
-        }
+        if (q.nl >> k & 1) e[k] = q.Eii * fast_exp(fma(q.n[k], lx, q.nc[k]));
     }
   }
   const double eta = sv * q.eta_up;
@@ -354,6 +350,15 @@ __device__ __forceinline__ void ve_eval(const VeCoef &q, double sv, VeState &s, 
   r = q.Eii - sv * q.Aup - (e[K_PWL] + e[K_EXP] + e[K_LIN]);
 }
 
+// S = sum_k n_k Eii_k at the last evaluated point (the non-linear part of -s r'(s))
+__device__ __forceinline__ double ve_S(const VeCoef &q, const VeState &s) {
+  double S = 0.0;
+#pragma unroll
+  for (int k = 0; k < K_COUNT; k++)
+    if (q.nl >> k & 1) S = fma(q.n[k], s.e[k], S);
+  return S;
+}
+
 // Newton on s from sv: s <- s (1 + step), step = r / (Aup s + S), i.e. s - r / r'(s)
 // with r' = -Aup - S/s (LocalIterationViscoElastic); returns eta = s eta_up in st.eta.
 __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s) {
@@ -361,55 +366,57 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s
   s.iters = nitmax;
   double step = -1.0;  // no previous point yet
   for (int it = 0; it < nitmax; it++) {
-    double r, S;
-    ve_eval(q, sv, s, r, S, step);
+    double r;
+    ve_eval(q, sv, s, r, step);
     if (fp64_abs_lt(r, q.thr_conv)) { s.iters = it + 1; break; }
     if (it == nitmax - 1 && fabs(r) > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
-    const double d = newton_quotient(r, fma(q.Aup, sv, S));
+    const double d = newton_quotient(r, fma(q.Aup, sv, ve_S(q, s)));
     sv = fma(sv, d, sv);
     step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
   }
   s.eta = sv * q.eta_up;
 }
 
-// Start point of the FP64 Newton: a few FP32 Newton steps on the same normalised
-// residual r(s)/Eii = 1 - a s - sum_k exp(n_k ln s + c_k), a = Aup/Eii,
-// c_k = n_k lp + nc_k.  The FP64 iteration that follows is unchanged and runs to the same
-// residual tolerance, so these steps only move its start (to within FP32 rounding of the
-// root).  Returns s0 when the FP32 iteration leaves (0, 2].
+// Start point of the FP64 Newton, in two stages on the same normalised residual
+//     r(s)/Eii = 1 - a s - sum_k exp(n_k ln s + c_k),   a = Aup/Eii,  c_k = n_k lp + nc_k.
+// The FP64 iteration that follows is unchanged and runs to the same residual tolerance, so
+// these stages only move its start; every quantity in them is O(1).
 //
-// The coefficients go to FP32 by truncating their bit patterns on the integer pipe (a
-// starting guess needs no rounding), since GB300 runs the FP32<->FP64 conversions on its
-// FP64 pipe: values beyond the FP32 range become +-FLT_MAX (NaN too) and the step guard
-// below returns s0 should they upset the iteration; values below it become 0.
-__device__ __forceinline__ float f32_trunc(double x) {
-  unsigned lo, hi;
-  fp64_words(x, lo, hi);
-  const unsigned sign = hi & 0x80000000u;
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  if (e <= 0) return __uint_as_float(sign);
-  if (e >= 255) return __uint_as_float(sign | 0x7f7fffffu);
-  return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+// Stage 1, `fp32` FP32 Newton steps (ve_polish_f32): within FP32 rounding of the root,
+// about 3e-7 relative.  The coefficients go to FP32 by truncating their bit patterns on
+// the integer pipe (a starting guess needs no rounding), since GB300 runs the
+// FP32<->FP64 conversions on its FP64 pipe: values beyond the FP32 range become
+// +-FLT_MAX (NaN too) and the step guard returns s0 should they upset the iteration;
+// values below it become 0.  Newton from above the root (r < 0; the reference's start
+// eta_up is such a point) descends monotonically, as r is concave.
+//
+// Stage 2 (ve_halley_dd): one Halley step whose residual and derivative are evaluated in
+// double-float (dd_math.cuh): s <- s (1 + d / (1 + d Q / (2 D))) with D = a s + sum_k n_k
+// e_k (= -s r'(s)), d = r / D, Q = sum_k n_k (n_k - 1) e_k (= -s^2 r''(s)).  From the FP32
+// root the step's own error is third order (about 1e-20), so the start lands within the
+// double-float evaluation's error (a few 1e-14 of the exponents) of the root, and the
+// FP64 residual there is already below the reference's stopping threshold 1e-13 Eii:
+// the FP64 iteration stops at its first evaluation, whose outputs it returns.  Where it
+// does not (an unresolved polish, a huge exponent), the FP64 Newton simply continues.
+struct StartCoef {
+  double a;              // Aup / Eii
+  double c[K_COUNT];     // n_k lp + nc_k for the non-linear laws
+};
+
+__device__ __forceinline__ void start_coef(const VeCoef &q, StartCoef &sc) {
+  sc.a = q.Aup * q.inv_Eii;
+#pragma unroll
+  for (int k = 0; k < K_COUNT; k++) sc.c[k] = (q.nl >> k & 1) ? fma(q.n[k], q.lp, q.nc[k]) : 0.0;
 }
 
-// x as a double, exactly, from the bits of a normal x; zero, subnormal, Inf and NaN take
-// the conversion instruction, out of line so that the common case does not execute it too
-static __device__ __noinline__ double f64_of_f32_rare(float x) { return (double)x; }
-
-__device__ __forceinline__ double f64_of_f32(float x) {
-  const unsigned b = __float_as_uint(x), e = (b >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return f64_of_f32_rare(x);
-  return __hiloint2double((int)((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3)), (int)(b << 29));
-}
-
-__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, float s0, int iters) {
+__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef &sc, float s0, int iters) {
   if (iters <= 0) return s0;
-  const float a = f32_trunc(q.Aup * q.inv_Eii);
+  const float a = f32_trunc(sc.a);
   float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
   if (q.nl) {
 #pragma unroll
     for (int k = 0; k < K_COUNT; k++)
-      if (q.nl >> k & 1) { n[k] = f32_trunc(q.n[k]); c[k] = f32_trunc(fma(q.n[k], q.lp, q.nc[k])); }
+      if (q.nl >> k & 1) { n[k] = f32_trunc(q.n[k]); c[k] = f32_trunc(sc.c[k]); }
   }
   float s = s0;
   for (int it = 0; it < iters; it++) {
@@ -432,6 +439,57 @@ __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, float s0, int it
   }
   return s;
 }
+
+// Stage 2 from the FP32 point s (see above); returns s itself, widened, when s is not a
+// positive normal number or the correction is not small (the polish did not settle).
+__device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef &sc, float s) {
+  if (!(s >= 1.17549435e-38f && s <= 2.0f)) return f64_of_f32(s);
+  const f2 a = dd_of_f64(sc.a);
+  const f2 as = dd_mul_f(a, s);
+  f2 E = {0.0f, 0.0f}, D = as;
+  float Q = 0.0f;
+  if (q.nl) {
+    const f2 ls = dd_log_f(s);
+#pragma unroll
+    for (int k = 0; k < K_COUNT; k++)
+      if (q.nl >> k & 1) {
+        const f2 nk = dd_of_f64(q.n[k]);
+        const f2 e = dd_exp(dd_add(dd_mul(nk, ls), dd_of_f64(sc.c[k])));
+        const f2 ne = dd_mul(nk, e);
+        E = dd_add(E, e);
+        D = dd_add(D, ne);
+        Q = __fmaf_rn(ne.hi, __fsub_rn(nk.hi, 1.0f), Q);
+      }
+  }
+  const f2 r = dd_add(dd_add_f(dd_neg(as), 1.0f), dd_neg(E));  // 1 - a s - sum_k e_k
+  // d = r / D in double-float: a first quotient and the quotient of its remainder
+  const float q1 = __fdividef(r.hi, D.hi);
+  if (!(fabsf(q1) < 1e-3f)) return f64_of_f32(s);
+  const f2 rem = dd_add(r, dd_neg(dd_mul_f(D, q1)));
+  const float q2 = __fdividef(rem.hi, D.hi);
+  const float h = __fdividef(__fmul_rn(__fmul_rn(q1, q1), Q), 2.0f * D.hi);  // Halley's term d^2 Q / (2 D)
+  // s (1 + d - d^2 Q / (2 D))
+  f2 sn = two_prod(s, q1);
+  sn.lo = __fmaf_rn(s, __fsub_rn(q2, h), sn.lo);
+  sn = dd_add_f(sn, s);
+  return f64_of_dd(sn);
+}
+
+// The start of the FP64 Newton: `fp32` FP32 Newton steps from s0, then, with `dd`, the
+// double-float Halley step.
+__device__ __forceinline__ double ve_start(const VeCoef &q, float s0, int fp32, bool dd) {
+  if (fp32 <= 0 && !dd) return f64_of_f32(s0);
+  StartCoef sc;
+  start_coef(q, sc);
+  const float s = ve_polish_f32(q, sc, s0, fp32);
+  return dd ? ve_halley_dd(q, sc, s) : f64_of_f32(s);
+}
+
+// The start descriptor carried by the kernels' `polish` argument: FP32 Newton steps in the
+// low byte, the double-float Halley step in bit 8 (MDZ_START_DD); 0 is the reference's
+// start.
+__device__ __forceinline__ int start_fp32(int polish) { return polish & 0xff; }
+__device__ __forceinline__ bool start_dd(int polish) { return (polish & MDZ_START_DD) != 0; }
 
 struct GseIn {
   double Eii, eta_el, eta_cst, C_pwl, n_pwl, C_lin, n_lin, m_lin, C_exp, ST, n_exp, eta_up, eta_lo, Ag,
@@ -683,8 +741,8 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
 
-// Local solve (from s_start * eta_up, refined by `polish` FP32 Newton steps; s_start = 1
-// and polish = 0 is the reference's start), plastic corrections and post-processing of
+// Local solve (from s_start * eta_up, moved by the start stages that the descriptor
+// `polish` names (ve_start); s_start = 1 and polish = 0 is the reference's start), plastic corrections and post-processing of
 // one (node, phase).  eta_conv (may be null) receives the converged visco-elastic
 // viscosity, before plasticity.
 __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
@@ -707,7 +765,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
     VeState s;
     s.status = MDZ_OK;
-    ve_newton(q, f64_of_f32(ve_polish_f32(q, s_start, polish)), s);
+    ve_newton(q, ve_start(q, s_start, start_fp32(polish), start_dd(polish)), s);
     set_status(o.status, s.status);
     eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
     o.iters = s.iters;
@@ -934,7 +992,7 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
 
 // Local solve, plasticity, post-processing.  The Newton starts from the reference's
 // bisection when s_start <= 0 and polish == 0; otherwise from s_start * eta_up (eta_up
-// when s_start <= 0) refined by `polish` FP32 Newton steps.
+// when s_start <= 0) moved by the start stages that the descriptor `polish` names.
 __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
                                    const AnisoNode &an, IsoState &S, float s_start, int polish, PointOut &o,
                                    double *eta_conv = nullptr) {
@@ -970,16 +1028,16 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
     VeState s;
     s.status = MDZ_OK;
-    double r, S, sv;  // sv = eta_ve / eta_up
+    double r, sv;  // sv = eta_ve / eta_up
     if (s_start > 0.0f || polish > 0) {
-      sv = f64_of_f32(ve_polish_f32(q, (s_start > 0.0f) ? s_start : 1.0f, polish));
+      sv = ve_start(q, (s_start > 0.0f) ? s_start : 1.0f, start_fp32(polish), start_dd(polish));
     } else {
       const double inv_up = 1.0 / eta_up;
       const double eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic != 0, eta_el, false);
       double lo = min_eta * 1.0e-3, hi = 10.0 * fmax(eta_lo, max_eta);
       for (int bit = 0; bit < 10; bit++) {
         eta_ve = sqrt(lo * hi);
-        ve_eval(q, eta_ve * inv_up, s, r, S);
+        ve_eval(q, eta_ve * inv_up, s, r);
         if (r > 0.0) lo = eta_ve;
         else hi = eta_ve;
         if (fabs(r) < q.thr_conv) break;
@@ -989,9 +1047,9 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     o.iters = 50;
     double step = -1.0;  // binomial update of the previous point's terms (see ve_eval)
     for (int it = 0; it < 50; it++) {
-      ve_eval(q, sv, s, r, S, step);
+      ve_eval(q, sv, s, r, step);
       if (fp64_is_nan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
-      const double d = newton_quotient(r, fma(q.Aup, sv, S));
+      const double d = newton_quotient(r, fma(q.Aup, sv, ve_S(q, s)));
       sv = fma(sv, d, sv);
       step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
       if (fp64_le(sv, 0.0)) { sv = min_eta / eta_up; step = -1.0; }

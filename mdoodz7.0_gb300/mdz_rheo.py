@@ -53,6 +53,8 @@ SWEEP_WARMSTART = 0x2
 SWEEP_ITERS = 0x4
 SWEEP_REF_START = 0x8
 DEFAULT_POLISH = 4
+START_DD = 0x100
+DEFAULT_START = DEFAULT_POLISH | START_DD
 
 # ---- struct layouts (must follow include/mdz_rheo.h field by field) -------
 MAT_INT = ["cstv", "pwlv", "linv", "gbsv", "expv", "gs", "kin", "plast", "density_model",
@@ -396,6 +398,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_math_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64] + [C.c_void_p] * 4
     lib.mdz_rheo_div_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_ceil_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    lib.mdz_rheo_dd_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p]
     lib.mdz_rheo_points_static.argtypes = [C.POINTER(Model), C.POINTER(Materials), C.POINTER(PointInputs),
                                            C.POINTER(PointOutputs), C.c_int64, C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(SweepStats)]
@@ -499,6 +502,17 @@ def ceil_selftest(q: np.ndarray, device: int = 0):
     if rc != MDZ_OK:
         raise RheoError(rc, "mdz_rheo_ceil_selftest")
     return fast, plain
+
+
+def dd_selftest(x: np.ndarray, device: int = 0):
+    """(x, exp(x), log(float32(x))) of the float64 array x as double-float (hi, lo) float32 pairs, each of shape
+    (n, 2), from the GPU."""
+    x = np.ascontiguousarray(x, np.float64)
+    out = np.empty((x.size, 6), np.float32)
+    rc = load_library().mdz_rheo_dd_selftest(device, x.ctypes.data, x.size, out.ctypes.data)
+    if rc != MDZ_OK:
+        raise RheoError(rc, "mdz_rheo_dd_selftest")
+    return out[:, 0:2], out[:, 2:4], out[:, 4:6]
 
 
 def python_struct_sizes():
@@ -723,7 +737,7 @@ class Context:
         return b.value, g.value
 
     # ---- learned warm start
-    def set_warmstart(self, w: Optional[MlpWeights], polish_iters: int = 4):
+    def set_warmstart(self, w: Optional[MlpWeights], polish_iters: int = DEFAULT_START):
         rc = self.lib.mdz_rheo_set_warmstart(self.handle, None if w is None else C.byref(w), polish_iters)
         if rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_set_warmstart")
