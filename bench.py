@@ -419,7 +419,7 @@ def main():
         """Device-resident sweeps: W warm-up, then K timed between barriers (max over ranks)."""
         for _ in range(args.warmup):
             sweep(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
-        r = {"kernel_ms": [], "iters": 0, "calls": 0, "launches": 0, "maxit": 0}
+        r = {"kernel_ms": [], "iters": 0, "calls": 0, "launches": 0, "maxit": 0, "f32": 0, "fault": 0}
         barrier()
         clk = ClockSampler(dev) if clock else None
         if clk:
@@ -432,6 +432,8 @@ def main():
             r["calls"] += st.phase_calls
             r["launches"] += st.kernel_launches
             r["maxit"] = max(r["maxit"], st.max_newton_iters)
+            r["f32"] += st.fp32_steps
+            r["fault"] |= st.mma_fault
         e1.record(stream)
         barrier()
         if clk:
@@ -441,12 +443,13 @@ def main():
         r["ms_step"] = total_ms / args.steps
         r["value"] = REP.whole_job_rate(w.nodes, ws, r["ms_step"])
         r["mean_iters"] = r["iters"] / max(r["calls"], 1)
+        r["mean_f32"] = r["f32"] / max(r["calls"], 1)
         return r
 
     def summary(r):
         return {"value": r["value"], "unit": UNIT, "ms_per_step": r["ms_step"],
                 "mean_newton_iters": r["mean_iters"], "max_newton_iters": r["maxit"],
-                "kernel_ms_per_sweep": statistics.mean(r["kernel_ms"])}
+                "mean_fp32_steps": r["mean_f32"], "kernel_ms_per_sweep": statistics.mean(r["kernel_ms"])}
 
     # ---- the default path: the headline ----
     main_r = timed(0, clock=True)
@@ -495,6 +498,10 @@ def main():
 
     # ---- the reference's own start point (same kernel, same tolerance) ----
     ref_r = summary(timed(R.SWEEP_REF_START))
+    # ---- the FP32 Newton steps without the double-float Halley step ----
+    ctx.set_warmstart(None, R.DEFAULT_POLISH)
+    fp32_r = summary(timed(0))
+    ctx.set_warmstart(None, R.DEFAULT_START)
     # ---- learned warm start ----
     warm = None
     if not args.no_warm:
@@ -509,12 +516,32 @@ def main():
         t1 = time.perf_counter()
         wts, loss, train_s = WSt.train(ctx, Xs, Ys, WSt.FEAT_ANISO if aniso else WSt.FEAT_ISO)
         del Xs, Ys
-        ctx.set_warmstart(wts, R.DEFAULT_POLISH)
+        ctx.set_warmstart(wts, R.DEFAULT_START)
         warm = summary(timed(R.SWEEP_WARMSTART))
-        warm.update({"pairs": 8_000_000, "collect_s": t1 - t0, "train_s": train_s,
-                     "final_train_loss": float(loss[-1]),
-                     "speedup_vs_reference_start": warm["value"] / ref_r["value"],
-                     "iteration_ratio_vs_reference_start": ref_r["mean_newton_iters"] / warm["mean_newton_iters"]})
+        tiles = timed(R.SWEEP_WARMSTART | R.SWEEP_WARM_TILES)
+        tiles_s = summary(tiles)
+        tiles_s["mma_fault"] = int(tiles["fault"])
+        ctx.set_warmstart(wts, R.START_DD)  # the network's guess straight into the double-float step
+        no_fp32 = summary(timed(R.SWEEP_WARMSTART))
+        ctx.set_warmstart(wts, R.DEFAULT_POLISH)  # network + FP32 steps, no double-float step
+        no_dd = summary(timed(R.SWEEP_WARMSTART))
+        ctx.set_warmstart(None, R.DEFAULT_START)
+        base = {"value": value, "ms_per_step": ms_step, "mean_newton_iters": main_r["mean_iters"],
+                "mean_fp32_steps": main_r["mean_f32"]}
+        warm.update({
+            "what": "network guess per (node, phase) on the tensor cores (per-warp mma.sync m16n8k16 BF16, FP32 "
+                    "accumulation) inside the sweep, then up to 4 FP32 Newton steps and the double-float Halley "
+                    "step; the FP64 Newton runs to the reference's tolerance from there",
+            "pairs": 8_000_000, "collect_s": t1 - t0, "train_s": train_s, "final_train_loss": float(loss[-1]),
+            "speedup_vs_reference_start": warm["value"] / ref_r["value"],
+            "iteration_ratio_vs_reference_start": ref_r["mean_newton_iters"] / warm["mean_newton_iters"],
+            "speedup_vs_default_start": warm["value"] / value,
+            "ablation": {
+                "default_start_no_network": base,
+                "network_tcgen05_tiles": tiles_s,
+                "network_then_double_float_only": no_fp32,
+                "network_then_fp32_only": no_dd,
+                "fp32_steps_only_no_network": fp32_r}})
 
     # ---- RheologicalOperators, Newton form: 8 perturbed local solves per node and phase ----
     newton_op = None
@@ -716,9 +743,11 @@ def main():
                                     "log-U(1,10)" if aniso else
                                     f"plain_large: {args.size}x{args.size} cells, {args.phases} phases "
                                     "(dislocation, diffusion, Peierls, softened Drucker-Prager)")
-                                   + "; FP64 local Newton to |r| < 1e-13 Eii started after 4 FP32 Newton steps",
+                                   + "; FP64 local Newton to |r| < 1e-13 Eii started after up to 4 FP32 Newton "
+                                     "steps and one double-float Halley step",
                        "nodes_per_gpu": w.nodes, "phase_calls_per_step": calls // args.steps,
                        "mean_newton_iters": main_r["mean_iters"], "max_newton_iters": main_r["maxit"],
+                       "mean_fp32_steps": main_r["mean_f32"],
                        "l2": f"inputs larger than L2 ({algorithmic_bytes(w, aniso) / 1e9:.1f} GB moved per sweep), "
                              "no flush",
                        "parallelism": f"{ws} independent grid(s), one per GPU"},

@@ -79,6 +79,8 @@ extern "C" {
 #define MDZ_SWEEP_WARMSTART  0x2  /* start each local Newton from the learned guess (needs weights) */
 #define MDZ_SWEEP_ITERS      0x4  /* record per-(node,phase) local iteration counts (mdz_rheo_get_iterations) */
 #define MDZ_SWEEP_REF_START  0x8  /* start each local Newton where the reference does (see below) */
+#define MDZ_SWEEP_WARM_TILES 0x10 /* with MDZ_SWEEP_WARMSTART: evaluate the network CTA-wide on tcgen05
+                                     (128-node tiles, CTA barriers per phase) instead of per warp */
 #define MDZ_DEFAULT_POLISH   4    /* FP32 Newton steps before each FP64 local solve, by default */
 /* Start descriptor of the local solves (mdz_rheo_set_warmstart): FP32 Newton steps in the
  * low byte, plus MDZ_START_DD for one Halley step evaluated in double-float (FP32 pairs)
@@ -188,6 +190,7 @@ typedef struct mdz_sweep_stats {
   uint64_t d2h_bytes;        /* bytes copied device->host by this call (MDZ_MEM_HOST) */
   uint32_t kernel_launches;  /* kernels this call launched */
   uint32_t mma_fault;        /* warm start: a tensor-core wait gave up; those items used the plain start */
+  uint64_t fp32_steps;       /* FP32 Newton steps taken by the starts of the local solves */
 } mdz_sweep_stats;
 
 /* ---- learned warm start ----------------------------------------------
@@ -534,6 +537,12 @@ int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);
  * reference's start point otherwise; 0 = start exactly where the reference does).  The
  * default is MDZ_DEFAULT_START. */
 int mdz_rheo_set_warmstart(mdz_rheo_ctx *ctx, const mdz_mlp_weights *w, int polish_iters);
+/* Test hook of the tcgen05 network form (MDZ_SWEEP_WARM_TILES): the number of polls of
+ * each tensor-core completion wait before the kernel gives up, records the fault
+ * (mdz_sweep_stats.mma_fault), keeps the start without the network and frees its tensor
+ * memory after a bounded wait for the work in flight.  0 gives up at once; a negative
+ * value restores the default (2^24). */
+int mdz_rheo_set_mma_poll_limit(mdz_rheo_ctx *ctx, int32_t limit);
 /* A plain sweep (iso or aniso) that also records, for every (phase p, node i) item,
  * item = p * (Nc + Nv) + i (centroids first), the MDZ_MLP_IN features X[item][.] and
  * the targets Y[item][0] = ln(eta_up / eta_ve), Y[item][1] = plastic (0/1); Y[item][0]

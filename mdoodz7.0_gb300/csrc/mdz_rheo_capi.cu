@@ -52,6 +52,7 @@ struct mdz_rheo_ctx {
   MlpDevice warm{};
   int warm_ready = 0, polish_iters = MDZ_DEFAULT_START;
   unsigned mma_fault = 0;
+  unsigned mma_poll_limit = 1u << 24;  // tcgen05 completion polls before a wait gives up
 };
 
 struct mdz_rheo_batch {
@@ -218,6 +219,7 @@ int stats_from_device(mdz_rheo_ctx *ctx, mdz_sweep_stats *st, float ms) {
     st->plastic_calls = h.plastic; st->status = status; st->error_node = node; st->elapsed_ms = ms;
     st->h2d_bytes = ctx->h2d; st->d2h_bytes = ctx->d2h; st->kernel_launches = ctx->launches;
     st->mma_fault = h.mma_fault;
+    st->fp32_steps = h.f32_steps;
   }
   return status;
 }
@@ -530,11 +532,16 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (mode < 0) {
     CK(launch_sweep(A, aniso, ctx->stream, ctx->block[aniso], ctx->grid_cap[aniso]));
+  } else if (mode == MODE_WARM && !(flags & MDZ_SWEEP_WARM_TILES)) {
+    MlpDevice w = ctx->warm;
+    w.polish_iters = ctx->polish_iters;
+    CK(launch_sweep_warm(A, w, aniso, ctx->stream));
   } else {
     WarmArgs W;
     memset(&W, 0, sizeof(W));
     W.mlp = ctx->warm;
     W.mlp.polish_iters = ctx->polish_iters;
+    W.mlp.poll_limit = ctx->mma_poll_limit;
     W.X_out = dX;
     W.Y_out = dY;
     const int grid = ctx->sms * tiles_blocks_per_sm(aniso, mode);
@@ -648,8 +655,29 @@ void pack_tile(uint8_t *tile, int rows_alloc, int K, const float *W, int rows_us
 
 constexpr size_t kT1 = kMlpHid * kMlpIn * 2, kT2 = kMlpHid * kMlpHid * 2, kT3 = kMlpOut * kMlpHid * 2;
 
+// The B operands of the per-warp MMA (mma.sync m16n8k16, mlp_warp.cuh) in fragment order:
+// entry (j * KC + c) * 32 + lane, lane = 4 g + t, holds the BF16 pairs
+// (W[n][k], W[n][k + 1]) and (W[n][k + 8], W[n][k + 9]) with n = 8 j + g, k = 16 c + 2 t,
+// W row-major [out][in] with `ldw` columns (zero beyond rows_used x k_used).
+void pack_frags(uint32_t *dst, const float *W, int NT, int KC, int rows_used, int k_used, int ldw) {
+  for (int j = 0; j < NT; j++)
+    for (int c = 0; c < KC; c++)
+      for (int lane = 0; lane < 32; lane++) {
+        const int n = 8 * j + (lane >> 2), k = 16 * c + 2 * (lane & 3);
+        auto el = [&](int kk) -> uint32_t {
+          return (n < rows_used && kk < k_used) ? (uint32_t)f2bf(W[(size_t)n * ldw + kk]) : 0u;
+        };
+        uint32_t *o = dst + 2 * ((j * KC + c) * 32 + lane);
+        o[0] = el(k) | (el(k + 1) << 16);
+        o[1] = el(k + 8) | (el(k + 9) << 16);
+      }
+}
+
+constexpr size_t kFB1 = (size_t)kF1 * 8, kFB2 = (size_t)kF2 * 8, kFB3 = (size_t)kF3 * 8;
+
 int upload_warm(mdz_rheo_ctx *c, const mdz_mlp_weights *w) {
-  const size_t bytes = kT1 + kT2 + kT3 + (64 + 64 + 16) * sizeof(float);
+  const size_t fbytes = kFB1 + kFB2 + kFB3;
+  const size_t bytes = kT1 + kT2 + kT3 + (64 + 64 + 16) * sizeof(float) + fbytes;
   if (!c->warm_buf) CK(cudaMalloc(&c->warm_buf, bytes));
   std::vector<uint8_t> h(bytes, 0);
   pack_tile(h.data(), kMlpHid, kMlpIn, w->W1, kMlpHid, w->n_feat, MDZ_MLP_IN, false);
@@ -660,6 +688,10 @@ int upload_warm(mdz_rheo_ctx *c, const mdz_mlp_weights *w) {
   memcpy(b + 64, w->b2, 64 * sizeof(float));
   b[128] = w->b3[0];
   b[129] = w->b3[1];
+  uint8_t *fr = h.data() + kT1 + kT2 + kT3 + (64 + 64 + 16) * sizeof(float);
+  pack_frags((uint32_t *)fr, w->W1, 8, 1, kMlpHid, w->n_feat, MDZ_MLP_IN);
+  pack_frags((uint32_t *)(fr + kFB1), w->W2, 8, 4, kMlpHid, kMlpHid, MDZ_MLP_HID);
+  pack_frags((uint32_t *)(fr + kFB1 + kFB2), w->W3, 1, 4, 2, kMlpHid, MDZ_MLP_HID);
   CK(cudaMemcpy(c->warm_buf, h.data(), bytes, cudaMemcpyHostToDevice));
   uint8_t *d = (uint8_t *)c->warm_buf;
   c->warm.W1 = (const uint4 *)d;
@@ -667,6 +699,10 @@ int upload_warm(mdz_rheo_ctx *c, const mdz_mlp_weights *w) {
   c->warm.W3 = (const uint4 *)(d + kT1 + kT2);
   const float *db = (const float *)(d + kT1 + kT2 + kT3);
   c->warm.b1 = db; c->warm.b2 = db + 64; c->warm.b3 = db + 128;
+  const uint8_t *df = d + kT1 + kT2 + kT3 + (64 + 64 + 16) * sizeof(float);
+  c->warm.F1 = (const uint2 *)df;
+  c->warm.F2 = (const uint2 *)(df + kFB1);
+  c->warm.F3 = (const uint2 *)(df + kFB1 + kFB2);
   for (int j = 0; j < kMlpIn; j++) { c->warm.x_shift[j] = w->x_shift[j]; c->warm.x_scale[j] = w->x_scale[j]; }
   c->warm.z_shift = w->z_shift;
   c->warm.z_scale = w->z_scale;
@@ -1062,6 +1098,7 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
     st->phase_calls = h.calls; st->newton_iters = h.iters; st->max_newton_iters = h.maxit;
     st->plastic_calls = h.plastic; st->status = status; st->error_node = node;
     st->kernel_launches = n > 0 ? 1 : 0;
+    st->fp32_steps = h.f32_steps;
   }
   return status;
 }
@@ -1718,6 +1755,12 @@ int mdz_rheo_set_warmstart(mdz_rheo_ctx *c, const mdz_mlp_weights *w, int polish
   const int rc = upload_warm(c, w);
   c->warm_ready = (rc == MDZ_OK);
   return rc;
+}
+
+int mdz_rheo_set_mma_poll_limit(mdz_rheo_ctx *c, int32_t limit) {
+  if (!c) return MDZ_EINVAL;
+  c->mma_poll_limit = limit < 0 ? (1u << 24) : (unsigned)limit;
+  return MDZ_OK;
 }
 
 int mdz_rheo_collect(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m, const mdz_grid_fields *f,

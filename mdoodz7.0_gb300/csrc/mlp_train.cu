@@ -46,6 +46,7 @@ struct TrainShared {
   alignas(8) uint64_t mbar;
   uint32_t tmem;
   int fault;
+  uint32_t fault_parity;  // the mbarrier phase a wait gave up on (drained before TMEM is freed)
 };
 
 constexpr uint32_t kTrainCols = 256;
@@ -70,7 +71,10 @@ __device__ __forceinline__ void gemm(TrainShared &S, int M, int N, int K, uint32
                      umma::smem_desc(b0 + kk * 256, 128, 16 * K), idesc, kk > 0);
     umma::commit(&S.mbar);
   }
-  if (!S.fault && !umma::mbar_wait(&S.mbar, phase)) S.fault = 1;
+  if (!S.fault && !umma::mbar_wait(&S.mbar, phase)) {  // every writer stores the same values
+    S.fault_parity = phase;
+    S.fault = 1;
+  }
   phase ^= 1;
   umma::fence_after_sync();
 }
@@ -118,7 +122,7 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
   const int t = threadIdx.x, w = t >> 5;
   const MlpTrainState &W = a.W;
   load_weights(S, W);
-  if (t == 0) { umma::mbar_init(&S.mbar, 1); S.fault = 0; }
+  if (t == 0) { umma::mbar_init(&S.mbar, 1); S.fault = 0; S.fault_parity = 0; }
   if (w == 0) umma::tmem_alloc(&S.tmem, kTrainCols);
   sync_mma();
   uint32_t phase = 0;
@@ -245,6 +249,10 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
+  // after a wait that gave up, the group it waited for may still be in flight (no MMA is
+  // issued after a fault, so at most one): wait for it, bounded, before freeing TMEM
+  if (t == 0 && S.fault) umma::mbar_wait(&S.mbar, S.fault_parity);
+  __syncthreads();
   if (w == 0) umma::tmem_free(S.tmem, kTrainCols);
   if (t == 0 && S.fault) atomicExch(W.fault, 1);
 }
@@ -338,7 +346,7 @@ __global__ void __launch_bounds__(128) k_mlp_predict(const __grid_constant__ Mlp
     for (int j = 0; j < kMlpIn; j++)
       x[j] = (s < a.n && j < a.n_feat) ? (a.X[s * kMlpIn + j] - a.W.x_shift[j]) * a.W.x_scale[j] : 0.0f;
     float y[2];
-    mlp_forward(S, x, y, phase);
+    mlp_forward(S, x, y, phase, 1u << 24);
     if (s < a.n) {
       Yp[s * 2 + 0] = y[0] * a.W.z_scale + a.W.z_shift;
       Yp[s * 2 + 1] = y[1];

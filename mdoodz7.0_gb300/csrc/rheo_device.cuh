@@ -116,6 +116,7 @@ struct PointOut {
   double eta, Txx, Tzz, Txz, etaVE, Eii_el, Eii_pl, Eii_pwl, Eii_exp, Eii_lin, Eii_gbs, Eii_cst, d1, inv_d1,
       X1, OverS, Pcorr, rho, div_el, div_pl, Wtot, Wel, Wdiss;
   int iters, is_pl, status;
+  int f32_steps;  // FP32 Newton steps taken by the start of the local solve
 };
 
 __device__ __forceinline__ void set_status(int &st, int code) {
@@ -361,14 +362,26 @@ __device__ __forceinline__ double ve_S(const VeCoef &q, const VeState &s) {
 
 // Newton on s from sv: s <- s (1 + step), step = r / (Aup s + S), i.e. s - r / r'(s)
 // with r' = -Aup - S/s (LocalIterationViscoElastic); returns eta = s eta_up in st.eta.
+// A start moved away from the reference's (sv != 1) that has not converged within the cap
+// is abandoned: the iteration runs again from the reference's start, with the reference's
+// cap, and the evaluations of both runs count.
 __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s) {
   const int nitmax = 20;
-  s.iters = nitmax;
+  s.iters = 0;
+  bool moved = !fp64_eq_nonzero(sv, 1.0);
   double step = -1.0;  // no previous point yet
   for (int it = 0; it < nitmax; it++) {
     double r;
     ve_eval(q, sv, s, r, step);
-    if (fp64_abs_lt(r, q.thr_conv)) { s.iters = it + 1; break; }
+    s.iters++;
+    if (fp64_abs_lt(r, q.thr_conv)) break;
+    if (it == nitmax - 1 && moved) {  // back to the reference's start
+      moved = false;
+      sv = 1.0;
+      step = -1.0;
+      it = -1;
+      continue;
+    }
     if (it == nitmax - 1 && fabs(r) > q.thr_fail) { set_status(s.status, MDZ_EVE_ITER); break; }
     const double d = newton_quotient(r, fma(q.Aup, sv, ve_S(q, s)));
     sv = fma(sv, d, sv);
@@ -386,9 +399,11 @@ __device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s
 // about 3e-7 relative.  The coefficients go to FP32 by truncating their bit patterns on
 // the integer pipe (a starting guess needs no rounding), since GB300 runs the
 // FP32<->FP64 conversions on its FP64 pipe: values beyond the FP32 range become
-// +-FLT_MAX (NaN too) and the step guard returns s0 should they upset the iteration;
-// values below it become 0.  Newton from above the root (r < 0; the reference's start
-// eta_up is such a point) descends monotonically, as r is concave.
+// +-FLT_MAX (NaN too) and the step guard returns 1 should they upset the iteration;
+// values below it become 0.  r is decreasing and concave, so Newton from above the root
+// (r < 0; the reference's start eta_up, s = 1, is such a point) descends monotonically,
+// and from below it (a learned guess may be) the first step lands above it.  A step that
+// leaves (0, 2] abandons the guess for s = 1.
 //
 // Stage 2 (ve_halley_dd): one Halley step whose residual and derivative are evaluated in
 // double-float (dd_math.cuh): s <- s (1 + d / (1 + d Q / (2 D))) with D = a s + sum_k n_k
@@ -409,7 +424,9 @@ __device__ __forceinline__ void start_coef(const VeCoef &q, StartCoef &sc) {
   for (int k = 0; k < K_COUNT; k++) sc.c[k] = (q.nl >> k & 1) ? fma(q.n[k], q.lp, q.nc[k]) : 0.0;
 }
 
-__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef &sc, float s0, int iters) {
+__device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef &sc, float s0, int iters,
+                                               int &taken) {
+  taken = 0;
   if (iters <= 0) return s0;
   const float a = f32_trunc(sc.a);
   float c[K_COUNT] = {0.f, 0.f, 0.f}, n[K_COUNT] = {0.f, 0.f, 0.f};
@@ -434,16 +451,18 @@ __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef 
     const float r = 1.0f - a * s - e;
     if (fabsf(r) < 1e-6f) break;
     const float sn = s + r * s / fmaf(a, s, S);
-    if (!(sn > 0.0f && sn <= 2.0f)) return s0;
+    taken = it + 1;
+    if (!(sn > 0.0f && sn <= 2.0f)) return 1.0f;  // the upper bound eta_up: right of the root
     s = sn;
   }
   return s;
 }
 
-// Stage 2 from the FP32 point s (see above); returns s itself, widened, when s is not a
-// positive normal number or the correction is not small (the polish did not settle).
+// Stage 2 from the FP32 point s (see above).  Where s is not a positive normal number in
+// (0, 2], or the correction is not small (the polish did not settle), the FP64 Newton
+// starts at s itself if s lies above the root and at the upper bound s = 1 otherwise.
 __device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef &sc, float s) {
-  if (!(s >= 1.17549435e-38f && s <= 2.0f)) return f64_of_f32(s);
+  if (!(s >= 1.17549435e-38f && s <= 2.0f)) return 1.0;
   const f2 a = dd_of_f64(sc.a);
   const f2 as = dd_mul_f(a, s);
   f2 E = {0.0f, 0.0f}, D = as;
@@ -464,7 +483,9 @@ __device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef 
   const f2 r = dd_add(dd_add_f(dd_neg(as), 1.0f), dd_neg(E));  // 1 - a s - sum_k e_k
   // d = r / D in double-float: a first quotient and the quotient of its remainder
   const float q1 = __fdividef(r.hi, D.hi);
-  if (!(fabsf(q1) < 1e-3f)) return f64_of_f32(s);
+  // an unsettled point: the FP64 Newton takes it from there if it lies above the root
+  // (r <= 0, monotone descent), from the upper bound s = 1 otherwise
+  if (!(fabsf(q1) < 1e-3f)) return (r.hi > 0.0f) ? 1.0 : f64_of_f32(s);
   const f2 rem = dd_add(r, dd_neg(dd_mul_f(D, q1)));
   const float q2 = __fdividef(rem.hi, D.hi);
   const float h = __fdividef(__fmul_rn(__fmul_rn(q1, q1), Q), 2.0f * D.hi);  // Halley's term d^2 Q / (2 D)
@@ -477,11 +498,12 @@ __device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef 
 
 // The start of the FP64 Newton: `fp32` FP32 Newton steps from s0, then, with `dd`, the
 // double-float Halley step.
-__device__ __forceinline__ double ve_start(const VeCoef &q, float s0, int fp32, bool dd) {
+__device__ __forceinline__ double ve_start(const VeCoef &q, float s0, int fp32, bool dd, int &taken) {
+  taken = 0;
   if (fp32 <= 0 && !dd) return f64_of_f32(s0);
   StartCoef sc;
   start_coef(q, sc);
-  const float s = ve_polish_f32(q, sc, s0, fp32);
+  const float s = ve_polish_f32(q, sc, s0, fp32, taken);
   return dd ? ve_halley_dd(q, sc, s) : f64_of_f32(s);
 }
 
@@ -696,6 +718,7 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   const int elastic = c.elastic;
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el;
   o.status = MDZ_OK;
+  o.f32_steps = 0;
   o.Pcorr = P;
   o.X1 = in.X0;
   o.Eii_gbs = 0.0;  // C_gbs is never set by the reference (:616-642)
@@ -765,7 +788,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
     VeState s;
     s.status = MDZ_OK;
-    ve_newton(q, ve_start(q, s_start, start_fp32(polish), start_dd(polish)), s);
+    ve_newton(q, ve_start(q, s_start, start_fp32(polish), start_dd(polish), o.f32_steps), s);
     set_status(o.status, s.status);
     eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
     o.iters = s.iters;
@@ -809,16 +832,35 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
       is_pl = 1;
       eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
       gdot = F / (eta_ve + eta_vp + ksd);
-      const double F0 = F;
-      for (int it = 0; it < 20; it++) {
+      const double F0 = F, tolF0 = tol * F0;
+      // with n_vp == 1, eta_vp / n_vp is eta_vp exactly and the derivative is a constant
+      const double dF1 = __dsub_rn(__dsub_rn(-eta_ve, eta_vp0), ksd);
+      // The return is a fixed map of the state (gdot, Tyield) entering each iteration.  When
+      // the state that the update produces equals one already entered -- the previous
+      // iteration's (the Newton step rounds away) or the one before (two states alternate
+      // in the last bit) -- every later iteration repeats one already done, and the values
+      // the loop ends with at its cap of 20 are known now: stop there instead of running
+      // the repeats.  The results are those of the full loop, bit for bit.
+      unsigned long long g1 = ~0ull, y1 = ~0ull;  // state entering the previous iteration
+      int last = 19;
+      for (int it = 0; it <= last; it++) {
+        const unsigned long long g0 = fp64_bits(gdot), y0 = fp64_bits(Tyield);
         divp = __dmul_rn(gdot, c.sin_dil);
         Pc = __dadd_rn(P, __dmul_rn(Kdt, divp));
         eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
         Tyield = __dadd_rn(Tyield, __dmul_rn(gdot, eta_vp));
         Tiic = __dsub_rn(Tii, __dmul_rn(eta_ve, gdot));
         F = Tiic - Tyield;
-        if (fp64_abs_lt(F, tol) || fp64_abs_lt(F, tol * F0)) break;
-        gdot -= F / (-eta_ve - eta_vp / n_vp - ksd);
+        if (fp64_abs_lt(F, tol) || fp64_abs_lt(F, tolF0)) break;
+        gdot -= F / (vp1 ? dF1 : (-eta_ve - eta_vp / n_vp - ksd));
+        if (it == last) break;
+        const unsigned long long gn = fp64_bits(gdot), yn = fp64_bits(Tyield);
+        if (gn == g0 && yn == y0) break;  // period 1: iteration 19 would be this one
+        if (gn == g1 && yn == y1) {       // period 2: iteration 19 repeats this one or the next
+          if (((19 - it) & 1) == 0) break;
+          last = it + 1;
+        }
+        g1 = g0; y1 = y0;
       }
       if (fp64_lt(Tiic, 0.0)) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }  // :697-704
       o.Pcorr = Pc;
@@ -962,9 +1004,10 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
   const int plastic = (fl & F_PLANY) != 0;
   const int elastic = c.elastic;
-  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
+  const double T = c.T, P = in.P, eta_el = c.eta_el, K = c.K, dt = M.dt_model;
   const double min_eta = M.min_eta, max_eta = M.max_eta;
   o.status = MDZ_OK;
+  o.f32_steps = 0;
   o.Pcorr = P;
   o.X1 = 0.0; o.rho = 0.0; o.Eii_gbs = 0.0; o.Eii_el = 0.0; o.Eii_pl = 0.0; o.div_pl = 0.0; o.div_el = 0.0;
   o.OverS = 0.0; o.Wtot = o.Wel = o.Wdiss = 0.0;
@@ -1030,7 +1073,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     s.status = MDZ_OK;
     double r, sv;  // sv = eta_ve / eta_up
     if (s_start > 0.0f || polish > 0) {
-      sv = ve_start(q, (s_start > 0.0f) ? s_start : 1.0f, start_fp32(polish), start_dd(polish));
+      sv = ve_start(q, (s_start > 0.0f) ? s_start : 1.0f, start_fp32(polish), start_dd(polish), o.f32_steps);
     } else {
       const double inv_up = 1.0 / eta_up;
       const double eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic != 0, eta_el, false);
@@ -1044,17 +1087,28 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
       }
       sv = sqrt(lo * hi) * inv_up;
     }
-    o.iters = 50;
+    // a moved start (not the bisection's) that has not converged within the cap is
+    // abandoned for the upper bound eta_up, above the root, with a fresh cap
+    bool moved = s_start > 0.0f || polish > 0;
+    o.iters = 0;
     double step = -1.0;  // binomial update of the previous point's terms (see ve_eval)
     for (int it = 0; it < 50; it++) {
       ve_eval(q, sv, s, r, step);
-      if (fp64_is_nan(r)) { set_status(o.status, MDZ_EANISO_NAN); o.iters = it + 1; break; }
+      o.iters++;
+      if (fp64_is_nan(r)) { set_status(o.status, MDZ_EANISO_NAN); break; }
       const double d = newton_quotient(r, fma(q.Aup, sv, ve_S(q, s)));
       sv = fma(sv, d, sv);
       step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
       if (fp64_le(sv, 0.0)) { sv = min_eta / eta_up; step = -1.0; }
       const double ar = fabs(r);
-      if (fp64_abs_lt(r, q.thr_conv)) { o.iters = it + 1; break; }
+      if (fp64_abs_lt(r, q.thr_conv)) break;
+      if (it == 49 && moved && !(ar < 10.0 * tol * Eii)) {
+        moved = false;
+        sv = 1.0;
+        step = -1.0;
+        it = -1;
+        continue;
+      }
       if (it == 49 && ar < 10.0 * tol * Eii) break;
       if (it == 49 && ar > q.thr_fail) { set_status(o.status, MDZ_EANISO_ITER); break; }
     }

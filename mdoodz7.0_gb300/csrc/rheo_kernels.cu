@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "mlp.cuh"
+#include "mlp_warp.cuh"
 #include "rheo_kernels.cuh"
 
 namespace mdz {
@@ -31,6 +32,7 @@ __device__ __forceinline__ void record_error(DevStats *st, long long node, int s
 struct Acc {
   unsigned long long calls, iters, plastic;
   unsigned int maxit;
+  unsigned long long f32;  // FP32 Newton steps of the starts
 };
 
 // ---------------------------------------------------------------------------------
@@ -138,7 +140,7 @@ template <bool ANISO>
 __device__ __forceinline__ void node_accumulate(const SweepArgs &A, const Node &n, int p, double perc,
                                                 const PointOut &o, double *out, Acc &acc, int &status) {
   set_status(status, o.status);
-  acc.calls++; acc.iters += o.iters; acc.plastic += o.is_pl;
+  acc.calls++; acc.iters += o.iters; acc.plastic += o.is_pl; acc.f32 += o.f32_steps;
   acc.maxit = max(acc.maxit, (unsigned)o.iters);
   node_iters(A, n, p, o.iters);
   if (n.centroid) A.peta_n[p][n.idx] = o.etaVE;
@@ -221,12 +223,14 @@ __device__ __forceinline__ void flush_acc(DevStats *st, Acc &acc) {
     acc.iters += __shfl_down_sync(0xffffffffu, acc.iters, o);
     acc.plastic += __shfl_down_sync(0xffffffffu, acc.plastic, o);
     acc.maxit = max(acc.maxit, __shfl_down_sync(0xffffffffu, acc.maxit, o));
+    acc.f32 += __shfl_down_sync(0xffffffffu, acc.f32, o);
   }
   if ((threadIdx.x & 31) == 0) {
     atomicAdd(&st->calls, acc.calls);
     atomicAdd(&st->iters, acc.iters);
     atomicAdd(&st->plastic, acc.plastic);
     atomicMax(&st->maxit, acc.maxit);
+    if (acc.f32) atomicAdd(&st->f32_steps, acc.f32);
   }
 }
 
@@ -266,12 +270,76 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
 // 22.47 ms against 23.12 ms with two CTAs per SM and no spills.
 template <bool ANISO, int NODES>
 __global__ void __launch_bounds__(128, 3) k_sweep(const __grid_constant__ SweepArgs A) {
-  Acc acc = {0, 0, 0, 0};
+  Acc acc = {0, 0, 0, 0, 0};
   const long long total = NODES == 1 ? (A.ranged ? A.c_n : A.M.Nc) : (A.ranged ? A.v_n : A.M.Nv);
   const long long lo = NODES == 1 ? (A.ranged ? A.c_lo : 0) : A.M.Nc + (A.ranged ? A.v_lo : 0);
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride)
     sweep_node<ANISO, NODES>(A, lo + j, acc);
+  flush_acc(A.stats, acc);
+}
+
+// ---------------------------------------------------------------------------------
+// learned warm start, per warp: the plain sweep with the network between each phase's
+// set-up and its local solve, evaluated by the warp's 32 lanes on the tensor cores
+// (mlp_warp.cuh)
+// ---------------------------------------------------------------------------------
+// The network's normalised inputs for one (node, phase) (zeros where the lane has none).
+__device__ __forceinline__ void warm_inputs(const MlpDevice &W, const float *f, int nfeat, float *x) {
+#pragma unroll
+  for (int j = 0; j < kMlpIn; j++) x[j] = (j < nfeat) ? (f[j] - W.x_shift[j]) * W.x_scale[j] : 0.0f;
+}
+
+// One node per lane, the warp's 32 nodes consecutive, so every lane of a warp runs the
+// same number of node iterations and reaches the network at the same phase; lanes past
+// the end or at inactive (node, phase) items feed zeros and discard the output.
+template <bool ANISO, int NODES>
+__global__ void __launch_bounds__(128, 3) k_sweep_warm(const __grid_constant__ SweepArgs A,
+                                                    const __grid_constant__ MlpDevice W) {
+  extern __shared__ __align__(16) unsigned char smem_warm[];
+  MlpWarpShared &S = *reinterpret_cast<MlpWarpShared *>(smem_warm);
+  mlp_warp_load(S, W);
+  Acc acc = {0, 0, 0, 0, 0};
+  const long long total = NODES == 1 ? A.M.Nc : A.M.Nv;
+  const long long lo = NODES == 1 ? 0 : A.M.Nc;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31, nfeat = ANISO ? kFeatAniso : kFeatIso;
+  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+    const long long j = base + lane;
+    const bool valid = j < total;
+    Node n;
+    n.solid = false;
+    n.centroid = NODES == 1;
+    if (valid) node_prepare<ANISO, NODES>(A, lo + j, n);
+    double out[CO_COUNT];
+#pragma unroll
+    for (int k = 0; k < CO_COUNT; k++) out[k] = 0.0;
+    int status = MDZ_OK;
+    for (int p = 0; p < A.M.np; p++) {  // uniform over the warp
+      const double perc = (valid && n.solid) ? node_perc(A, n, p) : 0.0;
+      const bool active = fp64_abs_gt(perc, 1e-13);
+      if (valid && n.solid && !active) node_iters(A, n, p, 0);
+      IsoState st;
+      PointOut o;
+      float f[kMlpIn], x[kMlpIn];
+#pragma unroll
+      for (int k = 0; k < kMlpIn; k++) f[k] = 0.0f;
+      if (active) {
+        if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
+        else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
+        warm_features(A.M, n.in, n.ctx, st, ANISO, f);
+      }
+      warm_inputs(W, f, nfeat, x);
+      __syncwarp();
+      const float y = mlp_warp_predict(S, x);
+      if (!active) continue;
+      const float s_start = warm_start_point(y, W.z_scale, W.z_shift);
+      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, s_start, W.polish_iters, o);
+      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, s_start, W.polish_iters, o);
+      node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
+    }
+    if (valid) node_store<ANISO>(A, n, out, status);
+  }
   flush_acc(A.stats, acc);
 }
 
@@ -295,7 +363,7 @@ __device__ __forceinline__ int batch_grid_of(const long long *tile_start, int n,
 // grid (NODES 1), then the vertex tiles (NODES 2).
 template <bool ANISO, int NODES>
 __global__ void __launch_bounds__(kBatchTile, 3) k_sweep_batch(const __grid_constant__ BatchArgs B) {
-  Acc acc = {0, 0, 0, 0};
+  Acc acc = {0, 0, 0, 0, 0};
   const long long *ts = NODES == 1 ? B.tile_start_n : B.tile_start_s;
   const long long tiles = NODES == 1 ? B.tiles_n : B.tiles_s;
   for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
@@ -360,7 +428,7 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
   MlpShared &S = *reinterpret_cast<MlpShared *>(smem_raw);
   uint32_t phase = 0;
   if (MODE == MODE_WARM) mlp_begin(S, W.mlp);
-  Acc acc = {0, 0, 0, 0};
+  Acc acc = {0, 0, 0, 0, 0};
   const long long total = A.M.Nc + A.M.Nv;
   const long long count = NODES == 1 ? A.M.Nc : A.M.Nv, base = NODES == 1 ? 0 : A.M.Nc;
   const long long ntiles = (count + kMlpTile - 1) / kMlpTile;
@@ -397,10 +465,9 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
 #pragma unroll
         for (int j = 0; j < kMlpIn; j++) x[j] = (j < nfeat) ? (f[j] - W.mlp.x_shift[j]) * W.mlp.x_scale[j] : 0.0f;
         float y[2];
-        mlp_forward(S, x, y, phase);
+        mlp_forward(S, x, y, phase, W.mlp.poll_limit);
         if (active && !S.fault) {
-          const float z = fmaxf(y[0] * W.mlp.z_scale + W.mlp.z_shift, 0.0f);
-          s_start = __expf(-z);
+          s_start = warm_start_point(y[0], W.mlp.z_scale, W.mlp.z_shift);
         }
       }
       if (!active) continue;
@@ -438,7 +505,7 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
 // ---------------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArgs A) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  Acc acc = {0, 0, 0, 0};
+  Acc acc = {0, 0, 0, 0, 0};
   const bool bad_phase = (i < A.n) && (A.in.phase[i] < 0 || A.in.phase[i] >= A.M.np);
   if (bad_phase) {  // phase ids in device memory are only checked here
     if (A.out.status) A.out.status[i] = MDZ_EINVAL;
@@ -478,7 +545,7 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArg
     if (O.iters) O.iters[i] = o.iters;
     if (O.status) O.status[i] = o.status;
     record_error(A.stats, i, o.status);
-    acc.calls = 1; acc.iters = o.iters; acc.plastic = o.is_pl; acc.maxit = o.iters;
+    acc.calls = 1; acc.iters = o.iters; acc.plastic = o.is_pl; acc.maxit = o.iters; acc.f32 = o.f32_steps;
   }
   flush_acc(A.stats, acc);
 }
@@ -497,6 +564,22 @@ cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int blo
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+template <bool ANISO, int NODES>
+static cudaError_t launch_warm_t(const SweepArgs &a, const MlpDevice &w, cudaStream_t s, long long count) {
+  auto fn = k_sweep_warm<ANISO, NODES>;
+  const size_t smem = sizeof(MlpWarpShared);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  fn<<<(unsigned)((count + 127) / 128), 128, smem, s>>>(a, w);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sweep_warm(const SweepArgs &a, const MlpDevice &w, bool aniso, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (a.M.Nc > 0) e = aniso ? launch_warm_t<true, 1>(a, w, s, a.M.Nc) : launch_warm_t<false, 1>(a, w, s, a.M.Nc);
+  if (e != cudaSuccess || a.M.Nv <= 0) return e;
+  return aniso ? launch_warm_t<true, 2>(a, w, s, a.M.Nv) : launch_warm_t<false, 2>(a, w, s, a.M.Nv);
 }
 
 // The warm-start form keeps its MLP tiles in dynamic shared memory; asking for the

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include "mlp.cuh"
+#include "mlp_warp.cuh"
 #include "rheo_device.cuh"
 
 namespace mdz {
@@ -24,6 +25,7 @@ struct DevStats {
   unsigned long long calls, iters, plastic;
   unsigned int maxit;
   unsigned int mma_fault;      // a tensor-core completion wait gave up (warm start)
+  unsigned long long f32_steps;  // FP32 Newton steps taken by the starts of the local solves
 };
 
 // modes of the tiled sweep
@@ -51,7 +53,7 @@ struct SweepArgs {
   int32_t *iters_n, *iters_s;  // optional [p*N + node]
   DevStats *stats;
   int final_update, need_lnd;
-  int polish;  // FP32 Newton steps before each FP64 local solve (0: the reference's start)
+  int polish;  // start descriptor of every local solve: FP32 Newton steps | MDZ_START_DD (0: the reference's start)
   long long node_base;  // added to node indices in error reports (batched grids)
   // k_sweep over a band of rows only: centroids [c_lo, c_lo + c_n) and vertices
   // [v_lo, v_lo + v_n); 0 sweeps every node
@@ -99,6 +101,8 @@ cudaError_t launch_perturb_batch(const BatchArgs &b, double amp, unsigned long l
                                  int grid);
 cudaError_t launch_sweep_tiles(const SweepArgs &a, const WarmArgs &w, bool aniso, int mode, cudaStream_t s,
                                int grid);
+// the learned warm start evaluated per warp (mlp_warp.cuh): one launch per kind of node
+cudaError_t launch_sweep_warm(const SweepArgs &a, const MlpDevice &w, bool aniso, cudaStream_t s);
 int tiles_blocks_per_sm(bool aniso, int mode);
 void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block);
 

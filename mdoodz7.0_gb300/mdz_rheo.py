@@ -52,6 +52,7 @@ SWEEP_ASYNC = 0x1
 SWEEP_WARMSTART = 0x2
 SWEEP_ITERS = 0x4
 SWEEP_REF_START = 0x8
+SWEEP_WARM_TILES = 0x10
 DEFAULT_POLISH = 4
 START_DD = 0x100
 DEFAULT_START = DEFAULT_POLISH | START_DD
@@ -113,7 +114,7 @@ class SweepStats(C.Structure):
                 ("max_newton_iters", C.c_uint32), ("plastic_calls", C.c_uint64),
                 ("status", C.c_int32), ("error_node", C.c_int64), ("elapsed_ms", C.c_double),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("kernel_launches", C.c_uint32),
-                ("mma_fault", C.c_uint32)]
+                ("mma_fault", C.c_uint32), ("fp32_steps", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -428,6 +429,7 @@ def load_library(path: str = LIB_PATH):
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
+    lib.mdz_rheo_set_mma_poll_limit.argtypes = [C.c_void_p, C.c_int32]
     lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                      C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(SweepStats)]
     lib.mdz_rheo_train_mlp.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int,
@@ -741,6 +743,13 @@ class Context:
         rc = self.lib.mdz_rheo_set_warmstart(self.handle, None if w is None else C.byref(w), polish_iters)
         if rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_set_warmstart")
+
+    def set_mma_poll_limit(self, limit: int):
+        """Test hook: polls of each tcgen05 completion wait before giving up (0: at once; negative: the
+        default)."""
+        rc = self.lib.mdz_rheo_set_mma_poll_limit(self.handle, limit)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_set_mma_poll_limit")
 
     def collect(self, model, mat, fields, X, Y, aniso=False, final_update=0, mem=MEM_HOST):
         """A sweep that also records per-(phase, node) features X [items, 16] and targets Y [items, 2]."""

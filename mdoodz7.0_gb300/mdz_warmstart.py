@@ -86,7 +86,8 @@ def iterations(ctx: R.Context, w: W.Workload, flags: int, aniso: bool = False) -
     a = {k: ([x.copy() for x in v] if isinstance(v, list) else v.copy()) for k, v in w.arrays.items()}
     _, st = fn(w.model, w.mat, R.FieldSet(a), flags=flags)
     return {"mean_iters": st.newton_iters / max(1, st.phase_calls), "max_iters": int(st.max_newton_iters),
-            "phase_calls": int(st.phase_calls), "kernel_ms": float(st.elapsed_ms)}
+            "mean_fp32_steps": st.fp32_steps / max(1, st.phase_calls),
+            "phase_calls": int(st.phase_calls), "kernel_ms": float(st.elapsed_ms), "mma_fault": int(st.mma_fault)}
 
 
 def main(argv: Optional[List[str]] = None):
@@ -97,7 +98,8 @@ def main(argv: Optional[List[str]] = None):
     ap.add_argument("--epochs", type=int, default=6)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=3e-3)
-    ap.add_argument("--polish", type=int, default=4)
+    ap.add_argument("--polish", type=int, default=R.DEFAULT_START,
+                    help="start descriptor: FP32 Newton steps, plus 256 for the double-float Halley step")
     ap.add_argument("--out", default=None)
     ap.add_argument("--eval", default=None, help="weights file to evaluate instead of training")
     ap.add_argument("--eval-ncx", type=int, default=1025)
@@ -126,8 +128,9 @@ def main(argv: Optional[List[str]] = None):
           else W.plain_large(seed=args.eval_seed, ncx=args.eval_ncx))
     ctx.set_warmstart(wts, args.polish)
     report["reference_start"] = iterations(ctx, wl, R.SWEEP_REF_START, args.aniso)
-    report["polish_only"] = iterations(ctx, wl, 0, args.aniso)
+    report["default_start"] = iterations(ctx, wl, 0, args.aniso)
     report["warm"] = iterations(ctx, wl, R.SWEEP_WARMSTART, args.aniso)
+    report["warm_tiles"] = iterations(ctx, wl, R.SWEEP_WARMSTART | R.SWEEP_WARM_TILES, args.aniso)
     print(json.dumps(report))
     ctx.close()
     return report
