@@ -77,7 +77,7 @@ extern "C" {
 /* sweep flags */
 #define MDZ_SWEEP_ASYNC      0x1  /* MDZ_MEM_DEVICE only: return after enqueue; call mdz_rheo_sync */
 #define MDZ_SWEEP_WARMSTART  0x2  /* start each local Newton from the learned guess (needs weights) */
-#define MDZ_SWEEP_ITERS      0x4  /* record per-(node,phase) local iteration counts (mdz_rheo_get_iterations) */
+#define MDZ_SWEEP_ITERS      0x4  /* record a word per (node, phase): iterations and mechanisms (mdz_rheo_get_iterations) */
 #define MDZ_SWEEP_REF_START  0x8  /* start each local Newton where the reference does (see below) */
 #define MDZ_SWEEP_WARM_TILES 0x10 /* with MDZ_SWEEP_WARMSTART: evaluate the network CTA-wide on tcgen05
                                      (128-node tiles, CTA barriers per phase) instead of per warp */
@@ -88,6 +88,24 @@ extern "C" {
  * stopping tolerance, so it stops at its first evaluation. */
 #define MDZ_START_DD         0x100
 #define MDZ_DEFAULT_START    (MDZ_DEFAULT_POLISH | MDZ_START_DD)
+
+/* Per-(node, phase) item word recorded by MDZ_SWEEP_ITERS (mdz_rheo_get_iterations): the
+ * local visco-elastic Newton's evaluations in bits 0-7 (at most 255), then the
+ * mechanism switches of that local solve (RheologyDensity.c:471-483,
+ * AnisotropyRoutines.c:322-326; the Peierls switch includes its temperature gate) and
+ * whether it yielded (is_pl, RheologyDensity.c:663, AnisotropyRoutines.c:627); 0 for an
+ * inactive phase. */
+#define MDZ_MECH_CONSTANT    (1 << 8)
+#define MDZ_MECH_DISLOCATION (1 << 9)
+#define MDZ_MECH_PEIERLS     (1 << 10)
+#define MDZ_MECH_DIFFUSION   (1 << 11)
+#define MDZ_MECH_GBS         (1 << 12)
+#define MDZ_MECH_GRAIN_SIZE  (1 << 13)
+#define MDZ_MECH_PLASTIC     (1 << 14)  /* a plastic return is on (plast != 0 and, isotropic, step != 0) */
+#define MDZ_MECH_ELASTIC     (1 << 15)
+#define MDZ_MECH_YIELD       (1 << 16)  /* the point yielded: is_pl */
+#define MDZ_ITEM_ITERS(w)    ((w) & 0xff)
+#define MDZ_ITEM_WORD(iters, mech) ((int32_t)(((iters) > 255 ? 255 : (iters)) | (mech)))
 
 /* ---- per-phase material table -----------------------------------------
  * The subset of `mat_prop` (MDLIB/include/mdoodz.h:152-240) that the local
@@ -461,8 +479,10 @@ int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marke
  * allocations made inside the call.
  * Staging and statistics live in one file-scope static __device__ array of
  * MDZ_STATIC_SCRATCH_BYTES (4 MiB, 256-byte aligned) per device:
- *   bytes needed = 256 (statistics) + for MDZ_MEM_HOST, for every non-NULL input and
- *   output array, n * element size rounded up to 256; for MDZ_MEM_DEVICE only the 256.
+ *   bytes needed = 256 (statistics) + for MDZ_MEM_HOST, for every non-NULL array the
+ *   kernel uses (phase, the 18 inputs, lxlz/lx2/ani_fac when anisotropic, every non-NULL
+ *   output), n * element size rounded up to 256; for MDZ_MEM_DEVICE only the 256.
+ *   strain_acc, div and angle are not read and not staged.
  * A request above the array returns MDZ_ESCRATCH before anything is enqueued (about
  * 10,000 points with every input and output present, host memory).
  * Nothing in the array has to start at zero: the call itself resets the statistics
@@ -473,7 +493,10 @@ int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marke
  * process by a lock held until the stream has drained.
  * The first call on each device looks up the array's address with
  * cudaGetSymbolAddress (that device current); make it before any stream capture
- * starts.  Inputs, outputs and return codes are those of mdz_rheo_points. */
+ * starts.  The address is kept for the life of the process: after a device reset
+ * (cudaDeviceReset) this entry point must not be called again.  Any failure after the
+ * first enqueue also waits for `stream` before the lock is released.  Inputs, outputs
+ * and return codes are those of mdz_rheo_points. */
 #define MDZ_STATIC_SCRATCH_BYTES (4u << 20)
 int mdz_rheo_points_static(const mdz_model *model, const mdz_materials *mat, const mdz_point_inputs *in,
                            mdz_point_outputs *out, int64_t n, int aniso, int mem, void *stream,
@@ -525,7 +548,7 @@ int mdz_rheo_autotune(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_mater
  * (0: one thread per node). */
 int mdz_rheo_get_launch_shape(mdz_rheo_ctx *ctx, int aniso, int *block, int *grid_cap);
 
-/* Per-(phase, node) VE local iteration counts of the last sweep run with
+/* Per-(phase, node) item words (MDZ_ITEM_ITERS, MDZ_MECH_*) of the last sweep run with
  * MDZ_SWEEP_ITERS: out_n[p*Nc + c0], out_s[p*Nv + c1]; 0 where the phase is
  * inactive.  Host buffers. */
 int mdz_rheo_get_iterations(mdz_rheo_ctx *ctx, int32_t *out_n, int32_t *out_s);

@@ -117,6 +117,7 @@ struct PointOut {
       X1, OverS, Pcorr, rho, div_el, div_pl, Wtot, Wel, Wdiss;
   int iters, is_pl, status;
   int f32_steps;  // FP32 Newton steps taken by the start of the local solve
+  int mech;       // MDZ_MECH_* bits of the local solve (its switches, and MDZ_MECH_YIELD)
 };
 
 __device__ __forceinline__ void set_status(int &st, int code) {
@@ -719,6 +720,10 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el;
   o.status = MDZ_OK;
   o.f32_steps = 0;
+  o.mech = (constant ? MDZ_MECH_CONSTANT : 0) | ((fl & F_PWL) ? MDZ_MECH_DISLOCATION : 0) |
+           (peierls ? MDZ_MECH_PEIERLS : 0) | (diffusion ? MDZ_MECH_DIFFUSION : 0) |
+           ((fl & F_GBS) ? MDZ_MECH_GBS : 0) | (gs ? MDZ_MECH_GRAIN_SIZE : 0) |
+           (plastic ? MDZ_MECH_PLASTIC : 0) | (elastic ? MDZ_MECH_ELASTIC : 0);
   o.Pcorr = P;
   o.X1 = in.X0;
   o.Eii_gbs = 0.0;  // C_gbs is never set by the reference (:616-642)
@@ -891,6 +896,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   else if (plastic == 1) { o.etaVE = eta_vep; inv_eta_pl = gdot / Tii; }
   else { o.etaVE = eta_vep; inv_eta_pl = 2.0 * lam_dot * A_tau / Tii; }
   o.is_pl = is_pl;
+  if (is_pl) o.mech |= MDZ_MECH_YIELD;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
   // the dissipative viscosity: 1 / eta = sum_k 2 Eii_k / Tii (+ 1/eta_cst, 1/eta_pl)
   const auto dissipative = [&](double &inv_half_T) {
@@ -1008,6 +1014,10 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   const double min_eta = M.min_eta, max_eta = M.max_eta;
   o.status = MDZ_OK;
   o.f32_steps = 0;
+  o.mech = (constant ? MDZ_MECH_CONSTANT : 0) | (dislocation ? MDZ_MECH_DISLOCATION : 0) |
+           (peierls ? MDZ_MECH_PEIERLS : 0) | (diffusion ? MDZ_MECH_DIFFUSION : 0) |
+           ((fl & F_GS) ? MDZ_MECH_GRAIN_SIZE : 0) | (plastic ? MDZ_MECH_PLASTIC : 0) |
+           (elastic ? MDZ_MECH_ELASTIC : 0);
   o.Pcorr = P;
   o.X1 = 0.0; o.rho = 0.0; o.Eii_gbs = 0.0; o.Eii_el = 0.0; o.Eii_pl = 0.0; o.div_pl = 0.0; o.div_el = 0.0;
   o.OverS = 0.0; o.Wtot = o.Wel = o.Wdiss = 0.0;
@@ -1149,6 +1159,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   if (fp64_gt(eta_vep, max_eta)) eta_vep = max_eta;
   o.etaVE = eta_vep;
   o.is_pl = is_pl;
+  if (is_pl) o.mech |= MDZ_MECH_YIELD;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
   double eta = eta_vep;
   double inv = 0.0;

@@ -142,7 +142,7 @@ __device__ __forceinline__ void node_accumulate(const SweepArgs &A, const Node &
   set_status(status, o.status);
   acc.calls++; acc.iters += o.iters; acc.plastic += o.is_pl; acc.f32 += o.f32_steps;
   acc.maxit = max(acc.maxit, (unsigned)o.iters);
-  node_iters(A, n, p, o.iters);
+  node_iters(A, n, p, MDZ_ITEM_WORD(o.iters, o.mech));
   if (n.centroid) A.peta_n[p][n.idx] = o.etaVE;
   else A.peta_s[p][n.idx] = o.etaVE;
   const int avg = A.M.eta_average;

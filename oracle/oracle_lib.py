@@ -27,7 +27,10 @@ import mdz_rheo as R  # noqa: E402
 ORACLE_SO = os.path.join(HERE, "build", "librheo_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmdz_ref.so")
 SHIM_SO = os.path.join(HERE, "_ref", "libmdz_shimtest.so")
-REF_TREE = os.environ.get("MDZ_REFERENCE_TREE", "/root/reference")
+# The MDOODZ7.0 source tree the pinning build compiles: MDZ_REFERENCE_TREE, else a
+# checkout named `reference` beside this repository.  Absent (as on a machine that only
+# runs the GPU tests), only the restatement is built.
+REF_TREE = os.environ.get("MDZ_REFERENCE_TREE") or os.path.join(os.path.dirname(REPO), "reference")
 
 
 def build(ref: bool = False, quiet: bool = True):

@@ -43,6 +43,7 @@ typedef struct {
   double eta, Txx, Tzz, Txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_exp, Eii_lin, Eii_gbs,
          Eii_cst, d1, X1, OverS, Pcorr, rho, div_el, div_pl, div_r, Wtot, Wel, Wdiss;
   int    iters, is_pl, status;
+  int    mech;  /* MDZ_MECH_* bits: the switches of :471-483 (aniso :322-326) and is_pl */
 } orc_res;
 
 static void set_status(int *st, int code) {
@@ -236,6 +237,9 @@ static void orc_viscosity_concise(const mdz_model *m, const mdz_materials *mt, c
   if (mt->plast[phase] == 1) plastic = 1;
   if (mt->plast[phase] == 2) plastic = 2;
   if (m->step == 0) { elastic = 0; plastic = 0; }
+  o->mech = constant * MDZ_MECH_CONSTANT | dislocation * MDZ_MECH_DISLOCATION | peierls * MDZ_MECH_PEIERLS |
+            diffusion * MDZ_MECH_DIFFUSION | gbs * MDZ_MECH_GBS | gs * MDZ_MECH_GRAIN_SIZE |
+            (plastic != 0) * MDZ_MECH_PLASTIC | (elastic != 0) * MDZ_MECH_ELASTIC;
   o->d1 = mt->gs_ref[phase];                               /* :486 */
   if (elastic == 0) { G = 1e1; dil = 0.0; K = 1e10; }      /* :493 */
   if (T < ZEROC / m->scale_T) T = ZEROC / m->scale_T;      /* :496 */
@@ -466,6 +470,7 @@ static void orc_viscosity_concise(const mdz_model *m, const mdz_materials *mt, c
   else if (plastic == 1) { o->etaVE = eta_vep; o->div_pl = divp; eta_pl = Tii / gdot; }
   else if (plastic == 2) { o->etaVE = eta_vep; o->div_pl = divp; eta_pl = Tii / (2.0 * lam_dot * A_tau); }
   o->is_pl = is_pl;
+  if (is_pl) o->mech |= MDZ_MECH_YIELD;
   o->Txx = 2.0 * (o->etaVE) * Exx;                         /* :981-983 */
   o->Tzz = 2.0 * (o->etaVE) * Ezz;
   o->Txz = 2.0 * (o->etaVE) * Exz;
@@ -537,6 +542,9 @@ static void orc_viscosity_concise_aniso(const mdz_model *m, const mdz_materials 
   if (mt->linv[phase] != 0) diffusion = 1;
   if (mt->plast[phase] != 0) plastic = 1;
   if (m->step == 0) elastic = 0;
+  o->mech = constant * MDZ_MECH_CONSTANT | dislocation * MDZ_MECH_DISLOCATION | peierls * MDZ_MECH_PEIERLS |
+            diffusion * MDZ_MECH_DIFFUSION | (mt->gs[phase] != 0) * MDZ_MECH_GRAIN_SIZE |
+            plastic * MDZ_MECH_PLASTIC | (elastic != 0) * MDZ_MECH_ELASTIC;
   if (elastic == 0) { G = 1e1; dil = 0.0; }
   if (T < ZEROC / m->scale_T) T = ZEROC / m->scale_T;
 
@@ -678,6 +686,7 @@ static void orc_viscosity_concise_aniso(const mdz_model *m, const mdz_materials 
   if (eta_vep > max_eta) eta_vep = max_eta;
   o->etaVE = eta_vep;
   o->is_pl = is_pl;
+  if (is_pl) o->mech |= MDZ_MECH_YIELD;
   double eta = eta_vep;
   const double eta_pl = Tii / gdot, divp = gdot * sin(dil);
   if (in->post_process == 1) {                             /* :681-714 */
@@ -857,7 +866,7 @@ static int orc_sweep_impl(const mdz_model *m, const mdz_materials *mt, const mdz
       acc_error(&acc, r.status, c0);
       calls++; iters += (uint64_t)r.iters; plastic += (uint64_t)r.is_pl;
       if ((uint32_t)r.iters > maxit) maxit = (uint32_t)r.iters;
-      if (iters_n) iters_n[(int64_t)p * Nc + c0] = r.iters;
+      if (iters_n) iters_n[(int64_t)p * Nc + c0] = MDZ_ITEM_WORD(r.iters, r.mech);
       f->phase_eta_n[p][c0] = r.etaVE;
       switch (avg) {
         case 0: f->eta_n[c0] += perc * r.etaVE; f->eta_phys_n[c0] += perc * r.eta; break;
@@ -951,7 +960,7 @@ static int orc_sweep_impl(const mdz_model *m, const mdz_materials *mt, const mdz
       acc_error(&acc, r.status, (int64_t)Nc + c1);
       calls++; iters += (uint64_t)r.iters; plastic += (uint64_t)r.is_pl;
       if ((uint32_t)r.iters > maxit) maxit = (uint32_t)r.iters;
-      if (iters_s) iters_s[(int64_t)p * Nv + c1] = r.iters;
+      if (iters_s) iters_s[(int64_t)p * Nv + c1] = MDZ_ITEM_WORD(r.iters, r.mech);
       f->phase_eta_s[p][c1] = r.etaVE;
       switch (avg) {
         case 0: f->eta_s[c1] += perc * r.etaVE; f->eta_phys_s[c1] += perc * r.eta; break;
