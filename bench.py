@@ -38,6 +38,7 @@ import time
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "mdoodz7.0_gb300"))
 
+REP_SEED_HEADLINE = 1  # the headline grid's seed (rank 0)
 METRIC = "rheology point-updates/s on 1 GB300: plain FP64 vs NN warm-start at tol 1e-11"
 UNIT = "point-updates/s"
 
@@ -47,11 +48,16 @@ UNIT = "point-updates/s"
 # cells (527,365 nodes), per workload (profiles/k_sweep_plain_large_513.md,
 # profiles/k_sweep_aniso_513.md).  `roofline.achieved` = this x nodes / the CUDA-event
 # time of one sweep (events before the first launch and after the second).
-FP64_FLOPS_PER_POINT = {"plain_large": 1697.3, "aniso": 1143.8}
-# DRAM bytes (read + write) per point-update of the same captures (both launches), scaled
-# to a sweep by its node count; the write count of those small captures misses lines still
-# in L2 when each kernel ends.
-DRAM_BYTES_PER_POINT = {"plain_large": 199.2, "aniso": 200.0}
+FP64_FLOPS_PER_POINT = {"plain_large": 1560.2, "aniso": 1094.8}
+# FP64 work of the batched many-grid sweep per local solve (phase call), same convention:
+# the two k_sweep_batch launches of one sweep of an 8-grid batch of the many-grid
+# distribution (5,096,155 phase calls; profiles/k_sweep_batch_many_grids.md); the grids
+# have 2 to 5 phases, so the work is counted per phase call.
+FP64_FLOPS_PER_PHASE_CALL = {"many_grids": 312.0}
+# DRAM bytes (read + write) per point-update of one sweep's two launches at 1025 x 1025
+# cells (0.7 GB of fields, five times L2; profiles/k_sweep_plain_large_dram_1025.md),
+# scaled to a sweep by its node count; none measured for the anisotropic sweep.
+DRAM_BYTES_PER_POINT = {"plain_large": 315.4, "aniso": None}
 # FP64 work of k_marker_update per marker (inactive ones included), same convention:
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
@@ -70,6 +76,7 @@ def parse():
                     help="plain_large: the headline; aniso: ViscosityConciseAniso sweep; many_grids: "
                          "64 uneven grids in one launch and a 20-sweep CUDA graph")
     ap.add_argument("--phases", type=int, default=5)
+    ap.add_argument("--grids", type=int, default=64, help="grids of the many-grid workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm start")
@@ -78,6 +85,8 @@ def parse():
     ap.add_argument("--no-strain-rates", action="store_true", help="skip the StrainRateComponents timing")
     ap.add_argument("--no-prep", action="store_true", help="skip the Softening / ShearModCompExpGrid timing")
     ap.add_argument("--no-markers", action="store_true", help="skip the UpdateParticleStress timing")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the anisotropic 4097^2 and the 64-grid sections of the default line")
     args = ap.parse_args()
     if args.size is None:
         args.size = 4097 if args.workload == "aniso" else 2049
@@ -226,10 +235,12 @@ def marker_cpu_baseline(W, O, sample_cells=1025):
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU implementation of the path on the host cores.
-    The MDOODZ7.0 sources are compiled by oracle/Makefile where the tree exists (this
-    build host); elsewhere the C restatement of the same code (bit-identical, pinned by
-    the tests) stands in."""
+    """--impl reference: the reference's own NonNewtonianViscosityGrid, compiled from the
+    MDOODZ7.0 sources by oracle/Makefile with the reference's release flags (on a host
+    without the tree, from the preprocessed units the build wrote beside it), timed on
+    all host cores (OpenMP) on the same 2049 x 2049, 5-phase workload as our line.  Only
+    where neither exists does the C restatement of the same code (bit-identical, pinned
+    by the tests) stand in, and the line says so (kind "port")."""
     ws_, rank, _ = dist_env()
     if rank != 0:
         return
@@ -238,8 +249,8 @@ def run_reference(args):
     import mdz_workloads as W
     import oracle_lib as O
     O.build(ref=True)
-    sample = 1025
-    w = W.plain_large(seed=101, ncx=sample, nphases=args.phases)
+    sample = args.size
+    w = W.plain_large(seed=REP_SEED_HEADLINE, ncx=sample, nphases=args.phases)
     ref = O.reference()
     kind = "reference" if ref is not None else "port"
 
@@ -263,26 +274,26 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"plain_large {args.size}x{args.size} cells, {args.phases} phases; "
-                                   f"each step a {sample}x{sample}-cell sample of it",
-                       "nodes_per_step": w.nodes},
+            "config": {"workload": f"plain_large: {args.size}x{args.size} cells, {args.phases} phases (dislocation, "
+                                   "diffusion, Peierls, softened Drucker-Prager); the reference's own local Newton "
+                                   "to |r| < 1e-13 Eii from its own start",
+                       "nodes_per_step": w.nodes, "same_config": True,
+                       "what": ("NonNewtonianViscosityGrid of MDOODZ7.0 (RheologyDensity.c:1131), compiled from its "
+                                "sources with -O3 -ftree-vectorize -funroll-loops -fopenmp -D_OMP_")
+                               if ref is not None else "the C restatement of NonNewtonianViscosityGrid"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                             "sample": f"{sample}x{sample}-cell grid, {w.nodes} nodes per step"},
+                             "sample": f"the whole {sample}x{sample}-cell grid, {w.nodes} nodes per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 def run_many_grids(args):
-    """64 grids of uneven size (65-1025 cells per side, 2-5 phases, dt 1e10-1e12 s, each
-    with its own seed) on one GPU, device-resident.  Three forms of one Picard sweep over
-    all of them: 64 separate sweep calls, one batched launch, and a CUDA graph of 20
-    batched sweeps with the strain rates perturbed by +-5 % before each (the headline
-    `value`: point-updates/s over the graph)."""
+    """--workload many_grids: config 3 alone (many_grids_section), its graph of 20 batched
+    sweeps with the default start as the line's value."""
     import torch
 
     import mdz_replicas as REP
     import mdz_rheo as R
-    import mdz_workloads as W
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -290,23 +301,152 @@ def run_many_grids(args):
         REP.init("nccl")
     dev = local if ws > 1 else 0
     torch.cuda.set_device(dev)
-    t0 = time.perf_counter()
-    grids = W.many_grids(seed=REP.replica_seed(7, rank), n=64)
-    gen_s = time.perf_counter() - t0
-    devs = [{k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
-             for k, v in g.arrays.items()} for g in grids]
-    fss = [R.FieldSet(d) for d in devs]
-    nodes = sum(g.nodes for g in grids)
     ctx = R.Context(dev)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
+
+    with ClockSampler(dev) as clk:
+        mg, _ = many_grids_section(args, ctx, dev, ws, rank, stream, barrier)
+    if rank != 0:
+        REP.finalize()
+        return
+    g = mg["graph"]["default"]
+    line = {"metric": METRIC, "value": g["value"], "unit": UNIT, "n_gpus": ws, "steps": max(1, args.steps // 4),
+            "warmup": args.warmup, "ms_per_step": g["ms_per_graph"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": mg["workload"], "nodes_per_sweep": mg["nodes_per_sweep"],
+                       "sweeps_per_step": mg["sweeps_per_graph"], "l2": "inputs larger than L2, no flush"},
+            "forms_ms_per_sweep": mg["forms_ms_per_sweep"], "graph": mg["graph"],
+            "roofline": None, "cpu_baseline": None, "e2e": None, "clocks": clk.summary(),
+            "gpu_launches": max(1, args.steps // 4) * g["kernel_launches_per_graph"]}
+    print(json.dumps(line))
+    if ws > 1:
+        REP.finalize()
+
+
+def timed_sweeps(args, fn, w, fs, flags, stream, barrier, dev, reps=None):
+    """W warm-up sweeps, then `reps` (default K) timed between barriers, CUDA events on the
+    context's stream; returns (ms per sweep, max over ranks; the last sweep's statistics)."""
+    import torch
+
+    import mdz_replicas as REP
+    import mdz_rheo as R
+    reps = reps or args.steps
+    for _ in range(args.warmup):
+        fn(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    stats = []
+    for _ in range(reps):
+        _, st = fn(w.model, w.mat, fs, mem=R.MEM_DEVICE, flags=flags)
+        stats.append(st)
+    e1.record(stream)
+    barrier()
+    return REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps, stats
+
+
+def sweep_summary(ms, stats, nodes, ws):
+    import mdz_replicas as REP
+    calls = max(1, sum(int(x.phase_calls) for x in stats))
+    return {"value": REP.whole_job_rate(nodes, ws, ms), "unit": UNIT, "ms_per_step": ms,
+            "mean_newton_iters": sum(int(x.newton_iters) for x in stats) / calls,
+            "max_newton_iters": max(int(x.max_newton_iters) for x in stats),
+            "mean_fp32_steps": sum(int(x.fp32_steps) for x in stats) / calls,
+            "kernel_ms_per_sweep": statistics.mean(x.elapsed_ms for x in stats)}
+
+
+def aniso_section(args, ctx, dev, ws, rank, stream, barrier, no_warm):
+    """Config 4: ViscosityConciseAniso over 4097 x 4097 cells, 3 phases, on the device; the
+    default start, the reference's start and the learned warm start (a 12-input network
+    trained here on pairs the plain kernel produces from a fresh seed), and end to end
+    through the C ABI with page-locked host buffers."""
+    import torch
+
+    import mdz_replicas as REP
+    import mdz_rheo as R
+    import mdz_workloads as W
+    t0 = time.perf_counter()
+    w = W.aniso(seed=REP.replica_seed(4, rank), ncx=4097, nphases=3)
+    gen_s = time.perf_counter() - t0
+    d = {k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
+         for k, v in w.arrays.items()}
+    fs = R.FieldSet(d)
+    fn = ctx.sweep_aniso
+    tune = None
+    if not args.no_autotune:  # each start keeps its own choice (the reference's: 10 bisection steps, Newton)
+        tune = {"candidates": list(R.Context.AUTOTUNE_NAMES)}
+        for label, fl in (("default_start", 0), ("reference_start", R.SWEEP_REF_START)):
+            t_ms, t_best, t_shape = ctx.autotune(w.model, w.mat, fs, aniso=True, flags=fl, reps=1)
+            tune[label] = {"ms_per_sweep": [float(x) for x in t_ms], "chosen": int(t_best),
+                           "block": t_shape[0], "grid_cap": t_shape[1], "form": ctx.launch_form(True)}
+    ms, st = timed_sweeps(args, fn, w, fs, 0, stream, barrier, dev)
+    out = sweep_summary(ms, st, w.nodes, ws)
+    out["autotune"] = tune
+    out.update({"workload": "aniso: 4097x4097 cells, 3 phases (dislocation, softened Drucker-Prager), director "
+                            "angle U[0,pi), anisotropy factor log-U(1,10); FP64 local Newton to |r| < 1e-13 Eii",
+                "nodes": w.nodes, "generate_s": gen_s,
+                "algorithmic_bytes_per_sweep": algorithmic_bytes(w, True)})
+    ms_r, st_r = timed_sweeps(args, fn, w, fs, R.SWEEP_REF_START, stream, barrier, dev)
+    out["reference_start"] = sweep_summary(ms_r, st_r, w.nodes, ws)
+    if not no_warm:
+        import mdz_warmstart as WSt
+        src = W.aniso(seed=130 + 1000 * rank, ncx=1449, nphases=3)
+        Xs, Ys = WSt.collect(ctx, [src], aniso=True, max_pairs=8_000_000)
+        del src
+        wts, loss, train_s = WSt.train(ctx, Xs, Ys, WSt.FEAT_ANISO)
+        del Xs, Ys
+        ctx.set_warmstart(wts, R.DEFAULT_START)
+        ms_w, st_w = timed_sweeps(args, fn, w, fs, R.SWEEP_WARMSTART, stream, barrier, dev)
+        ctx.set_warmstart(None, R.DEFAULT_START)
+        out["warm_start"] = sweep_summary(ms_w, st_w, w.nodes, ws)
+        out["warm_start"].update({"train_s": train_s, "final_train_loss": float(loss[-1])})
+    if not args.no_e2e:
+        h = {k: ([torch.from_numpy(x).pin_memory() for x in v] if isinstance(v, list)
+                 else torch.from_numpy(v).pin_memory()) for k, v in w.arrays.items()}
+        fh = R.FieldSet(h)
+        for _ in range(max(1, args.warmup)):
+            fn(w.model, w.mat, fh, mem=R.MEM_HOST)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            _, est = fn(w.model, w.mat, fh, mem=R.MEM_HOST)
+        e1.record(stream)
+        barrier()
+        e2e_ms = REP.max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
+        out["e2e"] = {"value": REP.whole_job_rate(w.nodes, ws, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
+                      "h2d_bytes_per_step": int(est.h2d_bytes), "d2h_bytes_per_step": int(est.d2h_bytes)}
+        del h, fh
+    del d, fs, w
+    torch.cuda.empty_cache()
+    return out
+
+
+def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, wts=None):
+    """Config 3: 64 grids of uneven size (65-1025 cells per side, 2-5 phases, dt 1e10-1e12 s,
+    each with its own seed), device-resident.  Forms of one Picard sweep over all of them:
+    64 separate sweep calls, one batched sweep (two launches), and a CUDA graph of 20
+    batched sweeps with the strain rates perturbed by +-5 % in each (fused into the
+    sweep's load), with the default start and with the learned warm start (`wts`)."""
+    import torch
+
+    import mdz_replicas as REP
+    import mdz_rheo as R
+    import mdz_workloads as W
+    t0 = time.perf_counter()
+    grids = W.many_grids(seed=REP.replica_seed(7, rank), n=args.grids)
+    gen_s = time.perf_counter() - t0
+    devs = [{k: ([torch.from_numpy(x).to(dev) for x in v] if isinstance(v, list) else torch.from_numpy(v).to(dev))
+             for k, v in g.arrays.items()} for g in grids]
+    fss = [R.FieldSet(d) for d in devs]
+    nodes = sum(g.nodes for g in grids)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def timed(step, reps):
         for _ in range(args.warmup):
@@ -324,50 +464,69 @@ def run_many_grids(args):
             ctx.sweep(g.model, g.mat, fs, mem=R.MEM_DEVICE)
 
     ms_sep = timed(separate, args.steps)
-    batch = R.Batch(ctx, [g.model for g in grids], [g.mat for g in grids], fss)
-    calls = [0]
-
-    def batched():
-        _, st = batch.sweep()
-        calls[0] = st.phase_calls
-
-    ms_batch = timed(batched, args.steps)
     nsw, amp = 20, 0.05
-    batch.capture(nsw, amp=amp, seed=2026)
-    stats = []
+    forms = {"separate_calls": ms_sep}
+    graphs = {}
+    for label, flags in (("default", 0), ("warm", R.SWEEP_WARMSTART)):
+        if flags and wts is None:
+            continue
+        if flags:
+            ctx.set_warmstart(wts, R.DEFAULT_START)
+        batch = R.Batch(ctx, [g.model for g in grids], [g.mat for g in grids], fss, flags=flags)
+        calls = [0]
 
-    def graph():
-        _, st = batch.launch()
-        stats.append(st)
+        def batched():
+            _, st = batch.sweep()
+            calls[0] = st.phase_calls
 
-    with ClockSampler(dev) as clk:
-        ms_graph = timed(graph, args.steps)
-    st = stats[-1]
-    batch.close()
-    if rank != 0:
-        REP.finalize()
-        return
-    value = REP.whole_job_rate(nodes * nsw, ws, ms_graph)
+        forms[f"one_batched_launch_{label}"] = timed(batched, args.steps)
+        batch.capture(nsw, amp=amp, seed=2026)
+        stats = []
+
+        def graph():
+            _, st = batch.launch()
+            stats.append(st)
+
+        ms_graph = timed(graph, max(1, args.steps // 4))
+        forms[f"graph_{label}"] = ms_graph / nsw
+        st = stats[-1]
+        graphs[label] = {"value": REP.whole_job_rate(nodes * nsw, ws, ms_graph), "unit": UNIT,
+                         "ms_per_graph": ms_graph, "ms_per_sweep": ms_graph / nsw,
+                         "phase_calls_per_sweep": int(calls[0]),
+                         "mean_newton_iters": st.newton_iters / max(1, st.phase_calls),
+                         "max_newton_iters": int(st.max_newton_iters),
+                         "mean_fp32_steps": st.fp32_steps / max(1, st.phase_calls),
+                         "kernel_launches_per_graph": int(st.kernel_launches)}
+        batch.close()
+        if flags:
+            ctx.set_warmstart(None, R.DEFAULT_START)
     sides = sorted(g.model.Nx - 1 for g in grids)
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"many_grids: 64 grids, {sides[0]}-{sides[-1]} cells per side (log-uniform), "
-                                   "2-5 phases each, dt 1e10-1e12 s; one step = one CUDA graph of 20 batched "
-                                   "sweeps, strain rates x (1 + 0.05 U[-1,1)) before each",
-                       "nodes_per_sweep": nodes, "sweeps_per_step": nsw,
-                       "phase_calls_per_sweep": calls[0],
-                       "mean_newton_iters": st.newton_iters / max(1, st.phase_calls),
-                       "max_newton_iters": int(st.max_newton_iters), "generate_s": gen_s,
-                       "l2": "inputs larger than L2, no flush"},
-            "forms_ms_per_sweep": {"separate_calls": ms_sep, "one_batched_launch": ms_batch,
-                                   "graph": ms_graph / nsw},
-            "separate_vs_graph": ms_sep / (ms_graph / nsw),
-            "roofline": None, "cpu_baseline": None, "e2e": None, "clocks": clk.summary(),
-            "gpu_launches": args.steps * st.kernel_launches}
-    print(json.dumps(line))
-    if ws > 1:
-        REP.finalize()
+    out = {"workload": f"many_grids: {len(grids)} grids, {sides[0]}-{sides[-1]} cells per side (log-uniform), 2-5 phases "
+                       "each, dt 1e10-1e12 s; one CUDA graph of 20 batched sweeps, strain rates x (1 + 0.05 "
+                       "U[-1,1)) in each (fused into the sweep's load)",
+           "nodes_per_sweep": nodes, "sweeps_per_graph": nsw, "generate_s": gen_s,
+           "value": graphs["default"]["value"], "unit": UNIT, "ms_per_sweep": graphs["default"]["ms_per_sweep"],
+           "graph": graphs, "forms_ms_per_sweep": forms,
+           "separate_vs_graph": ms_sep / graphs["default"]["ms_per_sweep"]}
+    del devs, fss
+    torch.cuda.empty_cache()
+    return out, grids[:4]
+
+
+def many_grids_cpu_baseline(O, grids):
+    """The oracle (C restatement, OpenMP on the host cores) on a few grids of the same batch."""
+    import mdz_rheo as R
+    nodes = sum(g.nodes for g in grids)
+    for g in grids[:1]:
+        O.orc_sweep(g.model, g.mat, R.FieldSet(g.arrays))
+    t0 = time.perf_counter()
+    for g in grids:
+        O.orc_sweep(g.model, g.mat, R.FieldSet(g.arrays))
+    dt = time.perf_counter() - t0
+    sides = ", ".join(str(g.model.Nx - 1) for g in grids)
+    return {"value": nodes / dt, "unit": UNIT, "cores": O.oracle().orc_num_threads(), "kind": "port",
+            "sample": f"the batch's first {len(grids)} grids ({sides} cells per side, {nodes} nodes), one sweep "
+                      f"each, {dt:.2f} s"}
 
 
 def main():
@@ -406,11 +565,14 @@ def main():
     sweep = ctx.sweep_aniso if aniso else ctx.sweep
     tune = None
     if not args.no_autotune:  # launch shape for this grid, before any timed region
-        t_ms, t_best, t_shape = ctx.autotune(w.model, w.mat, fs, aniso=aniso, reps=2)
-        tune = {"candidates": [f"block {b}, " + (f"{v} waves" if v else "one thread per node")
-                               for b, v in R.Context.AUTOTUNE_CANDIDATES],
-                "ms_per_sweep": [float(x) for x in t_ms], "chosen": int(t_best),
-                "block": t_shape[0], "grid_cap": t_shape[1]}
+        # every candidate form, from the default start and from the reference's start (where
+        # the local Newton's iteration counts are most uneven: 1 to 8); each start keeps its
+        # own choice
+        tune = {"candidates": list(R.Context.AUTOTUNE_NAMES)}
+        for label, fl in (("default_start", 0), ("reference_start", R.SWEEP_REF_START)):
+            t_ms, t_best, t_shape = ctx.autotune(w.model, w.mat, fs, aniso=aniso, flags=fl, reps=2)
+            tune[label] = {"ms_per_sweep": [float(x) for x in t_ms], "chosen": int(t_best),
+                           "block": t_shape[0], "grid_cap": t_shape[1], "form": ctx.launch_form(aniso)}
 
     def barrier():
         if ws > 1:
@@ -509,6 +671,7 @@ def main():
     ctx.set_warmstart(None, R.DEFAULT_START)
     # ---- learned warm start ----
     warm = None
+    wts = None
     if not args.no_warm:
         import mdz_warmstart as WSt
         t0 = time.perf_counter()
@@ -691,6 +854,12 @@ def main():
                              "markers_per_s": REP.whole_job_rate(nmk, ws, ms)}
         del gd, md, mw, vals, node_n, node_s
 
+    # ---- configs 4 and 3: the anisotropic sweep at 4097^2 and 64 uneven grids in one launch ----
+    configs, mg_sample = None, None
+    if not args.no_configs and not aniso:
+        configs = {"aniso_4097": aniso_section(args, ctx, dev, ws, rank, stream, barrier, args.no_warm)}
+        configs["many_grids_64"], mg_sample = many_grids_section(args, ctx, dev, ws, rank, stream, barrier, wts)
+
     if rank != 0:
         REP.finalize()
         return
@@ -703,7 +872,8 @@ def main():
         achieved = FP64_FLOPS_PER_POINT[args.workload] * w.nodes / (launch_ms * 1e-3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": peak_fp64, "unit": "TFLOP/s",
                 "frac": achieved / peak_fp64, "peak_source": "measured (DFMA probe, mdz_rheo_measure_fp64_peak)",
-                "traffic": DRAM_BYTES_PER_POINT[args.workload] * w.nodes}
+                "traffic": (DRAM_BYTES_PER_POINT[args.workload] * w.nodes
+                            if DRAM_BYTES_PER_POINT[args.workload] else None)}
     else:
         roof = {"bound": "fp64", "achieved": None, "peak": peak_fp64, "unit": "TFLOP/s", "frac": None,
                 "peak_source": "measured (DFMA probe)", "traffic": None}
@@ -728,6 +898,23 @@ def main():
             v["fp64_achieved_tflops"] = FP64_FLOPS_PER_MARKER[name] * nmk / (v["kernel_ms_per_call"] * 1e-3) / 1e12
             v["fp64_frac"] = v["fp64_achieved_tflops"] / peak_fp64
 
+    if configs is not None:
+        a = configs["aniso_4097"]
+        fl = FP64_FLOPS_PER_POINT["aniso"] * a["nodes"] / (a["kernel_ms_per_sweep"] * 1e-3) / 1e12
+        a["roofline"] = {"bound": "fp64", "achieved": fl, "peak": peak_fp64, "unit": "TFLOP/s",
+                         "frac": fl / peak_fp64, "peak_source": "measured (DFMA probe)",
+                         "traffic": None,
+                         "hbm_achieved_gbs": a["algorithmic_bytes_per_sweep"] / (a["kernel_ms_per_sweep"] * 1e-3) / 1e9}
+        m = configs["many_grids_64"]
+        per_call = FP64_FLOPS_PER_PHASE_CALL["many_grids"]
+        g = m["graph"]["default"]
+        if per_call:
+            fl = per_call * g["phase_calls_per_sweep"] / (g["ms_per_sweep"] * 1e-3) / 1e12
+            m["roofline"] = {"bound": "fp64", "achieved": fl, "peak": peak_fp64, "unit": "TFLOP/s",
+                             "frac": fl / peak_fp64, "peak_source": "measured (DFMA probe)", "traffic": None}
+        else:
+            m["roofline"] = {"bound": "fp64", "achieved": None, "peak": peak_fp64, "unit": "TFLOP/s", "frac": None,
+                             "peak_source": "measured (DFMA probe)", "traffic": None}
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -737,6 +924,9 @@ def main():
             cpu = cpu_baseline(W, O, aniso=aniso)
             if markers is not None:
                 markers["cpu_baseline"] = marker_cpu_baseline(W, O)
+            if configs is not None:
+                configs["aniso_4097"]["cpu_baseline"] = cpu_baseline(W, O, aniso=True)
+                configs["many_grids_64"]["cpu_baseline"] = many_grids_cpu_baseline(O, mg_sample)
         except Exception as e:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {e}"}
 
@@ -761,7 +951,7 @@ def main():
             "sweep_kernels": "k_sweep over the centroids, then k_sweep over the vertices: 2 launches per sweep",
             "median_kernel_ms_per_sweep": statistics.median(kernel_ms),
             "reference_start": ref_r, "warm_start": warm, "autotune": tune, "newton_operator": newton_op,
-            "strain_rates": strain, "input_preparation": prep, "marker_stress": markers}
+            "strain_rates": strain, "input_preparation": prep, "marker_stress": markers, "configs": configs}
     print(json.dumps(line))
     if ws > 1:
         REP.finalize()

@@ -507,7 +507,10 @@ int mdz_rheo_points_static(const mdz_model *model, const mdz_materials *mat, con
  * centroids and one over every grid's vertices: each grid's centroids (vertices) are
  * cut into tiles of 128 nodes and one CTA takes one tile.  The grids'
  * arguments are folded and uploaded once, at creation; the field arrays must stay
- * valid until the batch is destroyed.  `flags` may hold MDZ_SWEEP_REF_START only.
+ * valid until the batch is destroyed.  `flags` may hold MDZ_SWEEP_REF_START or
+ * MDZ_SWEEP_WARMSTART (the learned warm start in every sweep of the batch, evaluated per
+ * warp on the tensor cores: the context's network and start descriptor at each sweep or
+ * capture; needs mdz_rheo_set_warmstart first).
  * stats->error_node counts nodes through the batch in order (grid 0's centroids, its
  * vertices, grid 1's centroids, ...). */
 typedef struct mdz_rheo_batch mdz_rheo_batch;
@@ -519,8 +522,9 @@ int mdz_rheo_batch_destroy(mdz_rheo_batch *batch);
  * context's stream, blocking. */
 int mdz_rheo_batch_sweep(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
 /* Capture `nsweeps` consecutive batch sweeps as one CUDA graph (replacing any earlier
- * capture).  With amp != 0 every sweep is preceded by a perturbation of the strain-rate
- * inputs IN PLACE (exxd, ezzd, exz_n at centroids; exxd_s, ezzd_s, exz at vertices):
+ * capture).  With amp != 0 every sweep first perturbs the strain-rate inputs IN PLACE
+ * (exxd, ezzd, exz_n at centroids; exxd_s, ezzd_s, exz at vertices), fused into the
+ * sweep kernels' load of them (two launches per sweep, no separate pass):
  * x <- x (1 + amp u), u uniform in [-1, 1) from SplitMix64 of
  * key = sm(sm(seed ^ sweep) ^ grid), then sm(key ^ (3 node + component)), with
  * u = (h >> 11) 2^-52 - 1 (all steps rounded, no fused multiply-add).  The statistics
@@ -530,20 +534,35 @@ int mdz_rheo_batch_capture(mdz_rheo_batch *batch, int nsweeps, double amp, uint6
 int mdz_rheo_batch_launch(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
 
 /* ---- launch-shape autotuner (no reference counterpart) -----------------
- * Times the sweep kernel on the caller's own device-resident grid (MDZ_MEM_DEVICE
- * fields; final_update 0) for every candidate launch shape and keeps the fastest for
- * later sweeps of that kind (aniso 0/1) on this context.  Candidates, in this order:
- * 128 then 64 threads per block; for each, one thread per node, then a persistent grid
- * of 1, 2, 4 or 8 waves of the CTAs resident per SM.  Each candidate runs one warm-up
- * and `reps` timed sweeps; ms_out (may be NULL) receives MDZ_AUTOTUNE_CANDIDATES mean
- * kernel times and best_out (may be NULL) the chosen index.  The shape changes no result
- * bit: every node is computed by one thread, independently of the others.  `flags` may
- * hold MDZ_SWEEP_REF_START only.  The tuned sweeps overwrite the grid's outputs with the
- * values one sweep produces. */
-#define MDZ_AUTOTUNE_CANDIDATES 10
+ * Times the sweep on the caller's own device-resident grid (MDZ_MEM_DEVICE fields;
+ * final_update 0) in every candidate form and keeps the fastest, for later sweeps on this
+ * context of the same kind: anisotropic or not, phase count, start (MDZ_SWEEP_REF_START or
+ * not) and, among tuned sizes, the nearest node count (a cache keyed by those; other
+ * sweeps use the last shape tuned for their kind, aniso 0/1).  Candidates, in this order:
+ *   0-4   128 threads per block, 3 CTAs per SM (168 registers): one thread per node, then a
+ *         grid-stride loop over 1, 2, 4 or 8 waves of the resident CTAs;
+ *   5-9   the same with 64 threads per block;
+ *   10    128 threads per block, one thread per node, 2 CTAs per SM (255 registers, no
+ *         spills);
+ *   11    persistent: one wave of resident CTAs whose warps pull 32-node chunks from a
+ *         work counter (one atomic per chunk, lanes past the end retired by a ballot).
+ * Each candidate runs one warm-up and `reps` timed sweeps; ms_out (may be NULL) receives
+ * MDZ_AUTOTUNE_CANDIDATES mean kernel times and best_out (may be NULL) the chosen index.
+ * No candidate changes a result bit: every node is computed by the same code, by one
+ * thread, independently of the others.  `flags` may hold MDZ_SWEEP_REF_START only.  The
+ * tuned sweeps overwrite the grid's outputs with the values one sweep produces.  Banded
+ * host-memory sweeps take the persistent candidate's block size as one thread per node. */
+#define MDZ_AUTOTUNE_CANDIDATES 12
 int mdz_rheo_autotune(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                       const mdz_grid_fields *f, int aniso, int flags, int reps, double *ms_out,
                       int *best_out);
+/* The kernel form of that shape: 0 one thread per node or grid-stride (168 registers),
+ * 1 the 255-register form, 2 the persistent work-counter form. */
+int mdz_rheo_get_launch_form(mdz_rheo_ctx *ctx, int aniso, int *form);
+/* Set the shape of sweeps of this kind by hand (block 64 or 128, grid cap as above, form
+ * 0/1/2; form 2 with grid_cap 0 takes one wave of resident CTAs), dropping the tuned
+ * cache.  No result bit depends on it. */
+int mdz_rheo_set_launch_shape(mdz_rheo_ctx *ctx, int aniso, int block, int grid_cap, int form);
 /* The launch shape sweeps of this kind use now: threads per block and the grid cap
  * (0: one thread per node). */
 int mdz_rheo_get_launch_shape(mdz_rheo_ctx *ctx, int aniso, int *block, int *grid_cap);

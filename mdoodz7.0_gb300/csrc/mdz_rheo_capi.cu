@@ -41,7 +41,15 @@ struct mdz_rheo_ctx {
   int last_np = 0, have_iters = 0, pending = 0;
   unsigned long long h2d = 0, d2h = 0;
   unsigned launches = 0;
-  int block[2] = {128, 128}, grid_cap[2] = {0, 0};  // launch shape of k_sweep, [iso, aniso]
+  LaunchShape shape[2] = {{128, 0, SHAPE_THREAD}, {128, 0, SHAPE_THREAD}};  // untuned shape, [iso, aniso]
+  // shapes the autotuner chose, keyed by (anisotropic, phases, reference start, nodes); a
+  // sweep takes the entry of its key with the nearest node count, else shape[aniso]
+  struct Tuned {
+    int aniso, np, ref;
+    long long nodes;
+    LaunchShape shape;
+  };
+  std::vector<Tuned> tuned;
   // host-memory sweeps in row bands: copies in, kernels and copies out overlap
   cudaStream_t copy_in = nullptr, copy_out = nullptr, compute2 = nullptr;
   cudaEvent_t band_ev[2 * 16 + 3] = {};
@@ -58,7 +66,7 @@ struct mdz_rheo_ctx {
 struct mdz_rheo_batch {
   mdz_rheo_ctx *ctx = nullptr;
   int n = 0;
-  bool aniso = false;
+  bool aniso = false, warm = false;  // warm: the learned warm start in every sweep of the batch
   SweepArgs *d_grids = nullptr;
   long long *d_tile_start = nullptr;
   long long tiles = 0, nodes = 0;
@@ -353,6 +361,17 @@ void band_rows(int Nz, int B, int *a) {
 // kernel is done.  The copies of one band thus overlap the kernels of the others.  A
 // vertex row l reads the centroid rows l - 1 and l, which bands up to b have uploaded by
 // then (copy_in runs in order), and every node writes only its own outputs.
+LaunchShape pick_shape(const mdz_rheo_ctx *ctx, bool aniso, int np, bool ref, long long nodes) {
+  const mdz_rheo_ctx::Tuned *best = nullptr;
+  double best_d = 1e300;
+  for (const auto &t : ctx->tuned) {
+    if (t.aniso != (int)aniso || t.np != np || t.ref != (int)ref) continue;
+    const double d = fabs(log((double)t.nodes / (double)(nodes > 0 ? nodes : 1)));
+    if (d < best_d) { best_d = d; best = &t; }
+  }
+  return best ? best->shape : ctx->shape[aniso ? 1 : 0];
+}
+
 int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &L, const mdz_grid_fields *f,
                  int B) {
   const int Nx = A.M.Nx, Nz = A.M.Nz, Ncx = A.M.Ncx, Ncz = A.M.Ncz, np = A.M.np;
@@ -421,7 +440,7 @@ int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &
     if (b == 0) CK(cudaEventRecord(ctx->ev0, ks));
     A.ranged = 1;
     A.c_lo = (long long)coff; A.c_n = (long long)cn; A.v_lo = (long long)voff; A.v_n = (long long)vn;
-    CK(launch_sweep(A, aniso, ks, ctx->block[aniso], ctx->grid_cap[aniso]));
+    CK(launch_sweep(A, aniso, ks, pick_shape(ctx, aniso, A.M.np, A.polish == 0, A.M.Nc + A.M.Nv)));
     ctx->launches += sweep_kernel_count(A);
     CK(cudaEventRecord(ev[1 + B + b], ks));
     CK(cudaStreamWaitEvent(ctx->copy_out, ev[1 + B + b], 0));
@@ -531,7 +550,8 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   }
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   if (mode < 0) {
-    CK(launch_sweep(A, aniso, ctx->stream, ctx->block[aniso], ctx->grid_cap[aniso]));
+    CK(launch_sweep(A, aniso, ctx->stream,
+                    pick_shape(ctx, aniso, A.M.np, A.polish == 0, A.M.Nc + A.M.Nv)));
   } else if (mode == MODE_WARM && !(flags & MDZ_SWEEP_WARM_TILES)) {
     MlpDevice w = ctx->warm;
     w.polish_iters = ctx->polish_iters;
@@ -938,10 +958,13 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
   const size_t nb = (size_t)n * sizeof(double);
   A.in = *in;
   A.in.phase = (const int32_t *)up(in->phase, (size_t)n * sizeof(int32_t));
+  // the inputs k_points reads (strain_acc, div and angle it never reads: not staged)
+  A.in.strain_acc = A.in.div = A.in.angle = nullptr;
   const double **pin[] = {&A.in.G, &A.in.T, &A.in.P, &A.in.d, &A.in.phi, &A.in.X0, &A.in.Exx, &A.in.Ezz,
-                          &A.in.Exz, &A.in.Txx0, &A.in.Tzz0, &A.in.Txz0, &A.in.strain_acc, &A.in.dil,
-                          &A.in.fric, &A.in.C, &A.in.P0, &A.in.T0, &A.in.beta, &A.in.div,
-                          &A.in.lxlz, &A.in.lx2, &A.in.angle, &A.in.ani_fac};
+                          &A.in.Exz, &A.in.Txx0, &A.in.Tzz0, &A.in.Txz0, &A.in.dil,
+                          &A.in.fric, &A.in.C, &A.in.P0, &A.in.T0, &A.in.beta,
+                          &A.in.lxlz, &A.in.lx2, &A.in.ani_fac};
+  if (!aniso) A.in.lxlz = A.in.lx2 = A.in.ani_fac = nullptr;
   for (auto pp : pin) *pp = (const double *)up(*pp, nb);
   // every input the kernel reads must be present
   const void *req[] = {A.in.phase, A.in.G, A.in.T, A.in.P, A.in.d, A.in.phi, A.in.X0, A.in.Exx, A.in.Ezz,
@@ -999,6 +1022,9 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
   if (!md || !m || !in || !out || n < 0) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
   const bool host = (mem == MDZ_MEM_HOST);
+  // host memory stages n int32 at least: a count above the array's capacity is rejected
+  // before any input is read or any byte count is formed (no size_t wrap-around for huge n)
+  if (host && (uint64_t)n > (uint64_t)(MDZ_STATIC_SCRATCH_BYTES / sizeof(int32_t))) return MDZ_ESCRATCH;
   // every input the kernel reads must be present
   const void *req[] = {in->phase, in->G, in->T, in->P, in->d, in->phi, in->X0, in->Exx, in->Ezz, in->Exz,
                        in->Txx0, in->Tzz0, in->Txz0, in->dil, in->fric, in->C, in->P0, in->T0, in->beta};
@@ -1019,10 +1045,13 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
   A.out = *out;
   // layout of the array: statistics, then (host memory) one 256-aligned slot per array
   const size_t nb = (size_t)n * sizeof(double), ni = (size_t)n * sizeof(int32_t);
+  // the inputs k_points reads (strain_acc, div and angle it never reads: not staged)
+  A.in.strain_acc = A.in.div = A.in.angle = nullptr;
   const double **pin[] = {&A.in.G, &A.in.T, &A.in.P, &A.in.d, &A.in.phi, &A.in.X0, &A.in.Exx, &A.in.Ezz,
-                          &A.in.Exz, &A.in.Txx0, &A.in.Tzz0, &A.in.Txz0, &A.in.strain_acc, &A.in.dil,
-                          &A.in.fric, &A.in.C, &A.in.P0, &A.in.T0, &A.in.beta, &A.in.div,
-                          &A.in.lxlz, &A.in.lx2, &A.in.angle, &A.in.ani_fac};
+                          &A.in.Exz, &A.in.Txx0, &A.in.Tzz0, &A.in.Txz0, &A.in.dil,
+                          &A.in.fric, &A.in.C, &A.in.P0, &A.in.T0, &A.in.beta,
+                          &A.in.lxlz, &A.in.lx2, &A.in.ani_fac};
+  if (!aniso) A.in.lxlz = A.in.lx2 = A.in.ani_fac = nullptr;
   double **pout[] = {&A.out.eta, &A.out.Txx, &A.out.Tzz, &A.out.Txz, &A.out.etaVE, &A.out.VEcoeff,
                      &A.out.Eii_el, &A.out.Eii_pl, &A.out.Eii_pwl, &A.out.Eii_exp, &A.out.Eii_lin,
                      &A.out.Eii_gbs, &A.out.Eii_cst, &A.out.d1, &A.out.X1, &A.out.OverS, &A.out.Pcorr,
@@ -1053,6 +1082,15 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
   char *base = (char *)g_static_addr[dev];
   DevStats *dstats = (DevStats *)base;
   A.stats = dstats;
+  // From the first enqueue on, every return waits for `stream` while the lock is still
+  // held (this guard is destroyed before the lock): no copy or kernel of this call can
+  // still touch the array when the next call takes it.
+  struct Drain {
+    cudaStream_t s;
+    bool on = false;
+    ~Drain() { if (on) cudaStreamSynchronize(s); }
+  } drain{s};
+  drain.on = true;
   CK(cudaMemsetAsync(dstats, 0, sizeof(DevStats), s));
   CK(cudaMemsetAsync(&dstats->err_key, 0xff, sizeof(dstats->err_key), s));
   if (n > 0) {
@@ -1086,6 +1124,7 @@ int mdz_rheo_points_static(const mdz_model *md, const mdz_materials *m, const md
   }
   DevStats h;
   CK(cudaMemcpyAsync(&h, dstats, sizeof(h), cudaMemcpyDeviceToHost, s));
+  drain.on = false;
   CK(cudaStreamSynchronize(s));
   int status = MDZ_OK;
   long long node = -1;
@@ -1107,7 +1146,10 @@ int mdz_rheo_batch_create(mdz_rheo_ctx *c, int n, const mdz_model *models, const
                           const mdz_grid_fields *fields, int aniso, int final_update, int flags,
                           mdz_rheo_batch **out) {
   if (!c || !models || !mats || !fields || !out || n < 1 || n > kBatchMaxGrids) return MDZ_EINVAL;
-  if (flags & ~MDZ_SWEEP_REF_START) return MDZ_EINVAL;
+  if (flags & ~(MDZ_SWEEP_REF_START | MDZ_SWEEP_WARMSTART)) return MDZ_EINVAL;
+  if ((flags & MDZ_SWEEP_REF_START) && (flags & MDZ_SWEEP_WARMSTART)) return MDZ_EINVAL;
+  if ((flags & MDZ_SWEEP_WARMSTART) && !c->warm_ready) return MDZ_ENOTREADY;
+  if ((flags & MDZ_SWEEP_WARMSTART) && c->warm.n_feat != (aniso ? kFeatAniso : kFeatIso)) return MDZ_EINVAL;
   *out = nullptr;
   CK(cudaSetDevice(c->device));
   std::vector<SweepArgs> h((size_t)n);
@@ -1153,6 +1195,7 @@ int mdz_rheo_batch_create(mdz_rheo_ctx *c, int n, const mdz_model *models, const
   b->ctx = c;
   b->n = n;
   b->aniso = aniso != 0;
+  b->warm = (flags & MDZ_SWEEP_WARMSTART) != 0;
   b->nodes = nodes;
   b->tiles = tile_start[n];
   if (cudaMalloc(&b->d_grids, sizeof(SweepArgs) * n) != cudaSuccess ||
@@ -1193,6 +1236,22 @@ int mdz_rheo_batch_destroy(mdz_rheo_batch *b) {
   return MDZ_OK;
 }
 
+// The per-launch options of a batch sweep: the context's network and start descriptor as
+// they are now (a warm batch), and the perturbation of sweep `sweep` (amp 0: none).
+BatchSweepArgs batch_launch_args(const mdz_rheo_batch *b, double amp, uint64_t seed, int sweep) {
+  BatchSweepArgs x;
+  memset(&x, 0, sizeof(x));
+  x.warm = b->warm ? 1 : 0;
+  if (b->warm) {
+    x.mlp = b->ctx->warm;
+    x.mlp.polish_iters = b->ctx->polish_iters;
+  }
+  x.amp = amp;
+  x.seed = (unsigned long long)seed;
+  x.sweep = sweep;
+  return x;
+}
+
 int mdz_rheo_batch_sweep(mdz_rheo_batch *b, mdz_sweep_stats *st) {
   if (!b) return MDZ_EINVAL;
   mdz_rheo_ctx *c = b->ctx;
@@ -1202,7 +1261,8 @@ int mdz_rheo_batch_sweep(mdz_rheo_batch *b, mdz_sweep_stats *st) {
   c->h2d = c->d2h = 0;
   c->launches = batch_kernel_count(b->args);
   CK(cudaEventRecord(c->ev0, c->stream));
-  CK(launch_sweep_batch(b->args, b->aniso, c->stream, b->grid));
+  if (b->warm && !c->warm_ready) return MDZ_ENOTREADY;
+  CK(launch_sweep_batch(b->args, batch_launch_args(b, 0.0, 0, 0), b->aniso, c->stream, b->grid));
   CK(cudaEventRecord(c->ev1, c->stream));
   return finish(c, st);
 }
@@ -1210,6 +1270,7 @@ int mdz_rheo_batch_sweep(mdz_rheo_batch *b, mdz_sweep_stats *st) {
 int mdz_rheo_batch_capture(mdz_rheo_batch *b, int nsweeps, double amp, uint64_t seed) {
   if (!b || nsweeps < 1 || nsweeps > 100000 || !(amp >= 0.0 && amp < 1.0)) return MDZ_EINVAL;
   mdz_rheo_ctx *c = b->ctx;
+  if (b->warm && !c->warm_ready) return MDZ_ENOTREADY;
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->stream));
   if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
@@ -1217,10 +1278,9 @@ int mdz_rheo_batch_capture(mdz_rheo_batch *b, int nsweeps, double amp, uint64_t 
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaMemsetAsync(c->d_stats, 0, sizeof(DevStats), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(&c->d_stats->err_key, 0xff, sizeof(c->d_stats->err_key), c->stream);
-  for (int s = 0; s < nsweeps && e == cudaSuccess; s++) {
-    if (amp != 0.0) e = launch_perturb_batch(b->args, amp, (unsigned long long)seed, s, c->stream, b->grid);
-    if (e == cudaSuccess) e = launch_sweep_batch(b->args, b->aniso, c->stream, b->grid);
-  }
+  // each sweep perturbs the strain rates as it loads them (fused: no separate pass)
+  for (int s = 0; s < nsweeps && e == cudaSuccess; s++)
+    e = launch_sweep_batch(b->args, batch_launch_args(b, amp, seed, s), b->aniso, c->stream, b->grid);
   cudaGraph_t g = nullptr;
   const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -1236,7 +1296,7 @@ int mdz_rheo_batch_capture(mdz_rheo_batch *b, int nsweeps, double amp, uint64_t 
     return MDZ_ECUDA;
   }
   b->graph_sweeps = nsweeps;
-  b->graph_launches = nsweeps * ((amp != 0.0 ? 1 : 0) + (int)batch_kernel_count(b->args));
+  b->graph_launches = nsweeps * (int)batch_kernel_count(b->args);
   return MDZ_OK;
 }
 
@@ -1259,49 +1319,81 @@ int mdz_rheo_autotune(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials 
   if (flags & (MDZ_SWEEP_ASYNC | MDZ_SWEEP_WARMSTART | MDZ_SWEEP_ITERS)) return MDZ_EINVAL;
   CK(cudaSetDevice(c->device));
   const int a = aniso ? 1 : 0;
-  const int blocks[2] = {128, 64};
+  // the candidates, in the order of MDZ_AUTOTUNE_CANDIDATES
+  std::vector<LaunchShape> cand;
   const int waves[5] = {0, 1, 2, 4, 8};  // 0: one thread per node
-  int regs = 0, smem = 0;
-  double best_ms = 1e300;
-  int best = 0, cand = 0;
-  const int keep_block = c->block[a], keep_cap = c->grid_cap[a];
-  for (int bi = 0; bi < 2; bi++) {
-    int occ = 0;
-    sweep_kernel_info(a, &regs, &smem, &occ, blocks[bi]);
-    for (int wi = 0; wi < 5; wi++, cand++) {
-      c->block[a] = blocks[bi];
-      c->grid_cap[a] = waves[wi] ? c->sms * (occ > 0 ? occ : 1) * waves[wi] : 0;
-      double sum = 0.0;
-      mdz_sweep_stats st;
-      for (int r = 0; r <= reps; r++) {  // the first is a warm-up
-        const int rc = sweep_impl(c, md, m, f, 0, MDZ_MEM_DEVICE, flags, &st, aniso != 0);
-        if (rc != MDZ_OK) {
-          c->block[a] = keep_block;
-          c->grid_cap[a] = keep_cap;
-          return rc;
-        }
-        if (r > 0) sum += st.elapsed_ms;
-      }
-      const double ms = sum / reps;
-      if (ms_out) ms_out[cand] = ms;
-      if (ms < best_ms) { best_ms = ms; best = cand; }
+  for (int block : {128, 64})
+    for (int w : waves) {
+      int occ = 0, regs = 0, smem = 0;
+      sweep_kernel_info(a, &regs, &smem, &occ, block, SHAPE_THREAD);
+      cand.push_back({block, w ? c->sms * (occ > 0 ? occ : 1) * w : 0, SHAPE_THREAD});
     }
-  }
+  cand.push_back({128, 0, SHAPE_REGS255});
   {
-    int occ = 0;
-    const int bi = best / 5, wi = best % 5;
-    sweep_kernel_info(a, &regs, &smem, &occ, blocks[bi]);
-    c->block[a] = blocks[bi];
-    c->grid_cap[a] = waves[wi] ? c->sms * (occ > 0 ? occ : 1) * waves[wi] : 0;
+    int occ = 0, regs = 0, smem = 0;
+    sweep_kernel_info(a, &regs, &smem, &occ, 128, SHAPE_QUEUE);
+    cand.push_back({128, c->sms * (occ > 0 ? occ : 1), SHAPE_QUEUE});
   }
+  static_assert(MDZ_AUTOTUNE_CANDIDATES == 12, "candidate list");
+  const LaunchShape keep = c->shape[a];
+  const auto keep_tuned = c->tuned;
+  c->tuned.clear();  // every candidate below runs as the context's shape
+  double best_ms = 1e300;
+  int best = 0;
+  for (int ci = 0; ci < (int)cand.size(); ci++) {
+    c->shape[a] = cand[ci];
+    double sum = 0.0;
+    mdz_sweep_stats st;
+    for (int r = 0; r <= reps; r++) {  // the first is a warm-up
+      const int rc = sweep_impl(c, md, m, f, 0, MDZ_MEM_DEVICE, flags, &st, aniso != 0);
+      if (rc != MDZ_OK) {
+        c->shape[a] = keep;
+        c->tuned = keep_tuned;
+        return rc;
+      }
+      if (r > 0) sum += st.elapsed_ms;
+    }
+    const double ms = sum / reps;
+    if (ms_out) ms_out[ci] = ms;
+    if (ms < best_ms) { best_ms = ms; best = ci; }
+  }
+  c->shape[a] = cand[best];
+  c->tuned = keep_tuned;
+  // cache the choice for sweeps of this kind: phases, start, size
+  const bool ref = (flags & MDZ_SWEEP_REF_START) != 0;
+  const long long nodes = (long long)(md->Nx - 1) * (md->Nz - 1) + (long long)md->Nx * md->Nz;
+  for (auto it = c->tuned.begin(); it != c->tuned.end();)
+    if (it->aniso == a && it->np == m->Nb_phases && it->ref == (int)ref && it->nodes == nodes) it = c->tuned.erase(it);
+    else ++it;
+  c->tuned.push_back({a, m->Nb_phases, (int)ref, nodes, cand[best]});
   if (best_out) *best_out = best;
+  return MDZ_OK;
+}
+
+int mdz_rheo_set_launch_shape(mdz_rheo_ctx *c, int aniso, int block, int grid_cap, int form) {
+  if (!c || (block != 64 && block != 128) || grid_cap < 0) return MDZ_EINVAL;
+  if (form != SHAPE_THREAD && form != SHAPE_REGS255 && form != SHAPE_QUEUE) return MDZ_EINVAL;
+  if (form == SHAPE_QUEUE && grid_cap == 0) {  // one wave of resident CTAs
+    int occ = 0, regs = 0, smem = 0;
+    CK(cudaSetDevice(c->device));
+    sweep_kernel_info(aniso ? 1 : 0, &regs, &smem, &occ, 128, SHAPE_QUEUE);
+    grid_cap = c->sms * (occ > 0 ? occ : 1);
+  }
+  c->shape[aniso ? 1 : 0] = {form == SHAPE_QUEUE ? 128 : block, grid_cap, form};
+  c->tuned.clear();
+  return MDZ_OK;
+}
+
+int mdz_rheo_get_launch_form(mdz_rheo_ctx *c, int aniso, int *form) {
+  if (!c || !form) return MDZ_EINVAL;
+  *form = c->shape[aniso ? 1 : 0].form;
   return MDZ_OK;
 }
 
 int mdz_rheo_get_launch_shape(mdz_rheo_ctx *c, int aniso, int *block, int *grid_cap) {
   if (!c || !block || !grid_cap) return MDZ_EINVAL;
-  *block = c->block[aniso ? 1 : 0];
-  *grid_cap = c->grid_cap[aniso ? 1 : 0];
+  *block = c->shape[aniso ? 1 : 0].block;
+  *grid_cap = c->shape[aniso ? 1 : 0].grid_cap;
   return MDZ_OK;
 }
 

@@ -35,6 +35,42 @@ struct Acc {
   unsigned long long f32;  // FP32 Newton steps of the starts
 };
 
+// Multiplicative perturbation of the strain-rate inputs of every grid of a batch:
+// x <- x (1 + amp u), u uniform in [-1, 1) from a counter hash (SplitMix64, Steele et
+// al. 2014) of (seed, sweep, grid, node, component).  Rounded steps without
+// contraction, so a host restatement reproduces the values exactly.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double perturb_factor(unsigned long long key, long long node, int comp, double amp) {
+  const unsigned long long h = splitmix64(key ^ (unsigned long long)(node * 3 + comp));
+  const double u = __dsub_rn(__dmul_rn((double)(h >> 11), 0x1.0p-52), 1.0);  // [-1, 1)
+  return __dadd_rn(1.0, __dmul_rn(amp, u));
+}
+
+// The perturbation of one grid in one sweep, fused into the sweep's load of the strain
+// rates: key = the hash of (seed, sweep, grid), amp > 0.
+struct PerturbKey {
+  unsigned long long key;
+  double amp;
+};
+
+__device__ __forceinline__ unsigned long long perturb_key(unsigned long long seed, int sweep, int grid) {
+  return splitmix64(splitmix64(seed ^ (unsigned long long)sweep) ^ (unsigned long long)grid);
+}
+
+// The node's three strain-rate inputs x[0..2] (exxd, ezzd, exz of a centroid or of a
+// vertex, node index i over [centroids | vertices]) multiplied by their factors and stored
+// back, as the separate perturbation kernel does.
+__device__ __forceinline__ void perturb_inputs(const PerturbKey &pk, long long i, double *const *x) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) *x[k] = __dmul_rn(*x[k], perturb_factor(pk.key, i, k, pk.amp));
+}
+
 // ---------------------------------------------------------------------------------
 // one node: load and prepare (RheologyDensity.c:1165-1204, :1324-1340;
 // AnisotropyRoutines.c:917-977, :1097-1131)
@@ -51,12 +87,27 @@ struct Node {
 
 // NODES: 0 either kind (index i decides), 1 centroids only, 2 vertices only; a kernel
 // specialised to one kind of node drops the other kind's code and registers
+// pk (may be null): the strain rates are perturbed first, at every node, air included.
 template <bool ANISO, int NODES = 0>
-__device__ __forceinline__ void node_prepare(const SweepArgs &A, long long i, Node &n) {
+__device__ __forceinline__ void node_prepare(const SweepArgs &A, long long i, Node &n,
+                                             const PerturbKey *pk = nullptr) {
   const ModelConst &M = A.M;
   n.centroid = NODES == 1 ? true : (NODES == 2 ? false : i < M.Nc);
   const double el = (M.elastic == 1) ? 1.0 : 0.0;
   double mu, exxd, ezzd, exz;
+  if (pk) {
+    double *x[3];
+    if (n.centroid) {
+      x[0] = const_cast<double *>(A.ci[CI_exxd]) + i;
+      x[1] = const_cast<double *>(A.ci[CI_ezzd]) + i;
+      x[2] = const_cast<double *>(A.ci[CI_exz]) + i;
+    } else {
+      x[0] = const_cast<double *>(A.vi[VI_exxd]) + (i - M.Nc);
+      x[1] = const_cast<double *>(A.vi[VI_ezzd]) + (i - M.Nc);
+      x[2] = const_cast<double *>(A.vi[VI_exz]) + (i - M.Nc);
+    }
+    perturb_inputs(*pk, i, x);
+  }
   if (n.centroid) {
     const long long c0 = i;
     n.idx = c0;
@@ -239,9 +290,10 @@ __device__ __forceinline__ void flush_acc(DevStats *st, Acc &acc) {
 // ---------------------------------------------------------------------------------
 // One node of one grid: prepare, every active phase's local solve, averaging, store.
 template <bool ANISO, int NODES = 0>
-__device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc &acc) {
+__device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc &acc,
+                                           const PerturbKey *pk = nullptr) {
   Node n;
-  node_prepare<ANISO, NODES>(A, i, n);
+  node_prepare<ANISO, NODES>(A, i, n, pk);
   double out[CO_COUNT];
 #pragma unroll
   for (int j = 0; j < CO_COUNT; j++) out[j] = 0.0;
@@ -268,14 +320,41 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
 // vertex kernel, 532 B for the centroid kernel).  Twelve warps per SM hide more of the FP64
 // pipe's latency than the spills cost: at 2049 x 2049 cells the default-start sweep takes
 // 22.47 ms against 23.12 ms with two CTAs per SM and no spills.
-template <bool ANISO, int NODES>
-__global__ void __launch_bounds__(128, 3) k_sweep(const __grid_constant__ SweepArgs A) {
+// MINB: CTAs of 128 per SM the register allocation is capped for (3: 168 registers, with
+// spills; 2: 255 registers); the autotuner times both.
+template <bool ANISO, int NODES, int MINB = 3>
+__global__ void __launch_bounds__(128, MINB) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0, 0};
   const long long total = NODES == 1 ? (A.ranged ? A.c_n : A.M.Nc) : (A.ranged ? A.v_n : A.M.Nv);
   const long long lo = NODES == 1 ? (A.ranged ? A.c_lo : 0) : A.M.Nc + (A.ranged ? A.v_lo : 0);
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride)
     sweep_node<ANISO, NODES>(A, lo + j, acc);
+  flush_acc(A.stats, acc);
+}
+
+// Persistent form: a grid of resident CTAs whose warps pull chunks of 32 consecutive
+// nodes from a work counter until none is left.  A warp takes its next chunk as soon as
+// its slowest lane is done, instead of a CTA waiting for all four of its warps and the
+// block scheduler refilling the SM; one lane fetches for the warp (one atomic per chunk),
+// the chunk start is broadcast by shuffle, and the lanes past the end are retired by a
+// ballot.  The node body is the plain sweep's, so the results are the same bits.
+template <bool ANISO, int NODES>
+__global__ void __launch_bounds__(128, 3) k_sweep_queue(const __grid_constant__ SweepArgs A) {
+  Acc acc = {0, 0, 0, 0, 0};
+  const long long total = NODES == 1 ? A.M.Nc : A.M.Nv;
+  const long long lo = NODES == 1 ? 0 : A.M.Nc;
+  unsigned long long *counter = &A.stats->queue[NODES - 1];
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const long long j = (long long)base + lane;
+    const unsigned live = __ballot_sync(0xffffffffu, j < total);
+    if (live == 0u) break;
+    if ((live >> lane) & 1u) sweep_node<ANISO, NODES>(A, lo + j, acc);
+  }
   flush_acc(A.stats, acc);
 }
 
@@ -293,6 +372,49 @@ __device__ __forceinline__ void warm_inputs(const MlpDevice &W, const float *f, 
 // One node per lane, the warp's 32 nodes consecutive, so every lane of a warp runs the
 // same number of node iterations and reaches the network at the same phase; lanes past
 // the end or at inactive (node, phase) items feed zeros and discard the output.
+// One node of the learned-warm-start sweep; every lane of the warp calls it together
+// (valid false: a lane without a node, which still takes part in the network).
+template <bool ANISO, int NODES>
+__device__ __forceinline__ void warm_node(const SweepArgs &A, MlpWarpShared &S, const MlpDevice &W, bool valid,
+                                          long long i, Acc &acc, const PerturbKey *pk = nullptr) {
+  const int nfeat = ANISO ? kFeatAniso : kFeatIso;
+  Node n;
+  n.solid = false;
+  n.centroid = NODES == 1;
+  if (valid) node_prepare<ANISO, NODES>(A, i, n, pk);
+  double out[CO_COUNT];
+#pragma unroll
+  for (int k = 0; k < CO_COUNT; k++) out[k] = 0.0;
+  int status = MDZ_OK;
+  for (int p = 0; p < A.M.np; p++) {  // uniform over the warp
+    const double perc = (valid && n.solid) ? node_perc(A, n, p) : 0.0;
+    const bool active = fp64_abs_gt(perc, 1e-13);
+    if (valid && n.solid && !active) node_iters(A, n, p, 0);
+    IsoState st;
+    PointOut o;
+    float f[kMlpIn], x[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; k++) f[k] = 0.0f;
+    if (active) {
+      if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
+      else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
+      warm_features(A.M, n.in, n.ctx, st, ANISO, f);
+    }
+    warm_inputs(W, f, nfeat, x);
+    __syncwarp();
+    const float y = mlp_warp_predict(S, x);
+    if (!active) continue;
+    const float s_start = warm_start_point(y, W.z_scale, W.z_shift);
+    if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, s_start, W.polish_iters, o);
+    else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, s_start, W.polish_iters, o);
+    node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
+  }
+  if (valid) node_store<ANISO>(A, n, out, status);
+}
+
+// One node per lane, the warp's 32 nodes consecutive, so every lane of a warp runs the
+// same number of node iterations and reaches the network at the same phase; lanes past
+// the end or at inactive (node, phase) items feed zeros and discard the output.
 template <bool ANISO, int NODES>
 __global__ void __launch_bounds__(128, 3) k_sweep_warm(const __grid_constant__ SweepArgs A,
                                                     const __grid_constant__ MlpDevice W) {
@@ -303,42 +425,10 @@ __global__ void __launch_bounds__(128, 3) k_sweep_warm(const __grid_constant__ S
   const long long total = NODES == 1 ? A.M.Nc : A.M.Nv;
   const long long lo = NODES == 1 ? 0 : A.M.Nc;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31, nfeat = ANISO ? kFeatAniso : kFeatIso;
+  const int lane = threadIdx.x & 31;
   for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
     const long long j = base + lane;
-    const bool valid = j < total;
-    Node n;
-    n.solid = false;
-    n.centroid = NODES == 1;
-    if (valid) node_prepare<ANISO, NODES>(A, lo + j, n);
-    double out[CO_COUNT];
-#pragma unroll
-    for (int k = 0; k < CO_COUNT; k++) out[k] = 0.0;
-    int status = MDZ_OK;
-    for (int p = 0; p < A.M.np; p++) {  // uniform over the warp
-      const double perc = (valid && n.solid) ? node_perc(A, n, p) : 0.0;
-      const bool active = fp64_abs_gt(perc, 1e-13);
-      if (valid && n.solid && !active) node_iters(A, n, p, 0);
-      IsoState st;
-      PointOut o;
-      float f[kMlpIn], x[kMlpIn];
-#pragma unroll
-      for (int k = 0; k < kMlpIn; k++) f[k] = 0.0f;
-      if (active) {
-        if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
-        else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
-        warm_features(A.M, n.in, n.ctx, st, ANISO, f);
-      }
-      warm_inputs(W, f, nfeat, x);
-      __syncwarp();
-      const float y = mlp_warp_predict(S, x);
-      if (!active) continue;
-      const float s_start = warm_start_point(y, W.z_scale, W.z_shift);
-      if (ANISO) aniso_finish(A.M, A.ph[p], n.in, n.ctx, n.an, st, s_start, W.polish_iters, o);
-      else iso_finish(A.M, A.ph[p], n.in, n.ctx, st, s_start, W.polish_iters, o);
-      node_accumulate<ANISO>(A, n, p, perc, o, out, acc, status);
-    }
-    if (valid) node_store<ANISO>(A, n, out, status);
+    warm_node<ANISO, NODES>(A, S, W, j < total, lo + j, acc);
   }
   flush_acc(A.stats, acc);
 }
@@ -360,60 +450,32 @@ __device__ __forceinline__ int batch_grid_of(const long long *tile_start, int n,
 
 // One kernel per kind of node, as for a single grid (and with the same node body, so a
 // grid swept here gives the single-grid results to the bit): the centroid tiles of every
-// grid (NODES 1), then the vertex tiles (NODES 2).
-template <bool ANISO, int NODES>
-__global__ void __launch_bounds__(kBatchTile, 3) k_sweep_batch(const __grid_constant__ BatchArgs B) {
+// grid (NODES 1), then the vertex tiles (NODES 2).  A tile of kBatchTile nodes is one CTA
+// and lies in one grid, so the phase loop is uniform over the CTA and the learned warm
+// start (WARM) is evaluated per warp as in k_sweep_warm.  PERTURB: the strain rates are
+// multiplied by the sweep's perturbation factors as they are loaded, in place (the
+// captured multi-sweep graph), instead of by a separate pass over them.
+template <bool ANISO, int NODES, bool WARM, bool PERTURB>
+__global__ void __launch_bounds__(kBatchTile, 3) k_sweep_batch(const __grid_constant__ BatchArgs B,
+                                                             const __grid_constant__ BatchSweepArgs X) {
+  extern __shared__ __align__(16) unsigned char smem_batch[];
+  MlpWarpShared &S = *reinterpret_cast<MlpWarpShared *>(smem_batch);
+  if (WARM) mlp_warp_load(S, X.mlp);
   Acc acc = {0, 0, 0, 0, 0};
   const long long *ts = NODES == 1 ? B.tile_start_n : B.tile_start_s;
   const long long tiles = NODES == 1 ? B.tiles_n : B.tiles_s;
-  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {
+  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {  // uniform over the CTA
     const int g = batch_grid_of(ts, B.n, t);
     const SweepArgs &A = B.grids[g];
     const long long j = (t - __ldg(&ts[g])) * kBatchTile + threadIdx.x;
-    if (j < (NODES == 1 ? A.M.Nc : A.M.Nv)) sweep_node<ANISO, NODES>(A, NODES == 1 ? j : A.M.Nc + j, acc);
+    const bool valid = j < (NODES == 1 ? A.M.Nc : A.M.Nv);
+    const long long i = NODES == 1 ? j : A.M.Nc + j;
+    PerturbKey pk;
+    if (PERTURB) { pk.key = perturb_key(X.seed, X.sweep, g); pk.amp = X.amp; }
+    if (WARM) warm_node<ANISO, NODES>(A, S, X.mlp, valid, i, acc, PERTURB ? &pk : nullptr);
+    else if (valid) sweep_node<ANISO, NODES>(A, i, acc, PERTURB ? &pk : nullptr);
   }
   flush_acc(B.stats, acc);
-}
-
-// Multiplicative perturbation of the strain-rate inputs of every grid of a batch:
-// x <- x (1 + amp u), u uniform in [-1, 1) from a counter hash (SplitMix64, Steele et
-// al. 2014) of (seed, sweep, grid, node, component).  Rounded steps without
-// contraction, so a host restatement reproduces the values exactly.
-__device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
-  z += 0x9e3779b97f4a7c15ull;
-  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-  return z ^ (z >> 31);
-}
-
-__device__ __forceinline__ double perturb_factor(unsigned long long key, long long node, int comp, double amp) {
-  const unsigned long long h = splitmix64(key ^ (unsigned long long)(node * 3 + comp));
-  const double u = __dsub_rn(__dmul_rn((double)(h >> 11), 0x1.0p-52), 1.0);  // [-1, 1)
-  return __dadd_rn(1.0, __dmul_rn(amp, u));
-}
-
-__global__ void __launch_bounds__(kBatchTile) k_perturb_batch(const __grid_constant__ BatchArgs B, double amp,
-                                                             unsigned long long seed, int sweep) {
-  for (long long t = blockIdx.x; t < B.tiles; t += gridDim.x) {
-    const int g = batch_grid_of(B.tile_start, B.n, t);
-    const SweepArgs &A = B.grids[g];
-    const long long i = (t - __ldg(&B.tile_start[g])) * kBatchTile + threadIdx.x;
-    const long long Nc = A.M.Nc;
-    if (i >= Nc + A.M.Nv) continue;
-    const unsigned long long key = splitmix64(splitmix64(seed ^ (unsigned long long)sweep) ^ (unsigned long long)g);
-    double *x[3];
-    if (i < Nc) {
-      x[0] = const_cast<double *>(A.ci[CI_exxd]) + i;
-      x[1] = const_cast<double *>(A.ci[CI_ezzd]) + i;
-      x[2] = const_cast<double *>(A.ci[CI_exz]) + i;
-    } else {
-      x[0] = const_cast<double *>(A.vi[VI_exxd]) + (i - Nc);
-      x[1] = const_cast<double *>(A.vi[VI_ezzd]) + (i - Nc);
-      x[2] = const_cast<double *>(A.vi[VI_exz]) + (i - Nc);
-    }
-#pragma unroll
-    for (int k = 0; k < 3; k++) *x[k] = __dmul_rn(*x[k], perturb_factor(key, i, k, amp));
-  }
 }
 
 // ---------------------------------------------------------------------------------
@@ -550,16 +612,30 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ PointArg
   flush_acc(A.stats, acc);
 }
 
-cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap) {
+template <bool ANISO, int NODES>
+static void launch_kind(const SweepArgs &a, const LaunchShape &sh, long long count, cudaStream_t s) {
+  if (sh.form == SHAPE_QUEUE) {
+    k_sweep_queue<ANISO, NODES><<<(unsigned)sh.grid_cap, 128, 0, s>>>(a);
+    return;
+  }
+  long long grid = (count + sh.block - 1) / sh.block;
+  if (sh.grid_cap > 0 && grid > sh.grid_cap) grid = sh.grid_cap;
+  if (sh.form == SHAPE_REGS255) k_sweep<ANISO, NODES, 2><<<(unsigned)grid, sh.block, 0, s>>>(a);
+  else k_sweep<ANISO, NODES, 3><<<(unsigned)grid, sh.block, 0, s>>>(a);
+}
+
+cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, const LaunchShape &shape) {
   const long long counts[2] = {a.ranged ? a.c_n : a.M.Nc, a.ranged ? a.v_n : a.M.Nv};
+  // the work counter of the persistent form covers a whole sweep, not a band of rows
+  LaunchShape sh = shape;
+  if (sh.form == SHAPE_QUEUE && (a.ranged || sh.grid_cap <= 0)) sh.form = SHAPE_THREAD;
+  if (sh.form == SHAPE_QUEUE) sh.block = 128;
   for (int kind = 0; kind < 2; kind++) {
     if (counts[kind] <= 0) continue;
-    long long grid = (counts[kind] + block - 1) / block;
-    if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
-    if (kind == 0 && aniso) k_sweep<true, 1><<<(unsigned)grid, block, 0, s>>>(a);
-    else if (kind == 0) k_sweep<false, 1><<<(unsigned)grid, block, 0, s>>>(a);
-    else if (aniso) k_sweep<true, 2><<<(unsigned)grid, block, 0, s>>>(a);
-    else k_sweep<false, 2><<<(unsigned)grid, block, 0, s>>>(a);
+    if (kind == 0 && aniso) launch_kind<true, 1>(a, sh, counts[kind], s);
+    else if (kind == 0) launch_kind<false, 1>(a, sh, counts[kind], s);
+    else if (aniso) launch_kind<true, 2>(a, sh, counts[kind], s);
+    else launch_kind<false, 2>(a, sh, counts[kind], s);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -649,25 +725,32 @@ int tiles_blocks_per_sm(bool aniso, int mode) {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_sweep_batch(const BatchArgs &b, bool aniso, cudaStream_t s, int grid) {
-  // one CTA per tile, up to `grid`, per kind
-  const long long gn = b.tiles_n < grid ? b.tiles_n : grid, gs = b.tiles_s < grid ? b.tiles_s : grid;
-  if (gn > 0) {
-    if (aniso) k_sweep_batch<true, 1><<<(unsigned)gn, kBatchTile, 0, s>>>(b);
-    else k_sweep_batch<false, 1><<<(unsigned)gn, kBatchTile, 0, s>>>(b);
-  }
-  if (gs > 0) {
-    if (aniso) k_sweep_batch<true, 2><<<(unsigned)gs, kBatchTile, 0, s>>>(b);
-    else k_sweep_batch<false, 2><<<(unsigned)gs, kBatchTile, 0, s>>>(b);
-  }
+template <bool ANISO, int NODES, bool WARM, bool PERTURB>
+static cudaError_t launch_batch_t(const BatchArgs &b, const BatchSweepArgs &x, cudaStream_t s, long long grid) {
+  auto fn = k_sweep_batch<ANISO, NODES, WARM, PERTURB>;
+  const size_t smem = WARM ? sizeof(MlpWarpShared) : 0;
+  if (WARM) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  fn<<<(unsigned)grid, kBatchTile, smem, s>>>(b, x);
   return cudaGetLastError();
 }
 
-cudaError_t launch_perturb_batch(const BatchArgs &b, double amp, unsigned long long seed, int sweep, cudaStream_t s,
-                                 int grid) {
-  if (grid < 1) grid = 1;
-  k_perturb_batch<<<grid, kBatchTile, 0, s>>>(b, amp, seed, sweep);
-  return cudaGetLastError();
+template <bool ANISO, int NODES>
+static cudaError_t launch_batch_kind(const BatchArgs &b, const BatchSweepArgs &x, cudaStream_t s, long long grid) {
+  const bool pert = x.amp != 0.0;
+  if (x.warm) return pert ? launch_batch_t<ANISO, NODES, true, true>(b, x, s, grid)
+                          : launch_batch_t<ANISO, NODES, true, false>(b, x, s, grid);
+  return pert ? launch_batch_t<ANISO, NODES, false, true>(b, x, s, grid)
+              : launch_batch_t<ANISO, NODES, false, false>(b, x, s, grid);
+}
+
+cudaError_t launch_sweep_batch(const BatchArgs &b, const BatchSweepArgs &x, bool aniso, cudaStream_t s, int grid) {
+  // one CTA per tile, up to `grid`, per kind
+  const long long gn = b.tiles_n < grid ? b.tiles_n : grid, gs = b.tiles_s < grid ? b.tiles_s : grid;
+  cudaError_t e = cudaSuccess;
+  if (gn > 0) e = aniso ? launch_batch_kind<true, 1>(b, x, s, gn) : launch_batch_kind<false, 1>(b, x, s, gn);
+  if (e != cudaSuccess) return e;
+  if (gs > 0) e = aniso ? launch_batch_kind<true, 2>(b, x, s, gs) : launch_batch_kind<false, 2>(b, x, s, gs);
+  return e;
 }
 
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s) {
@@ -677,10 +760,12 @@ cudaError_t launch_points(const PointArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block) {
+void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block, int form) {
   cudaFuncAttributes fa;
   // the centroid kernel: the larger of the two, it sets the launch shape
-  const void *fn = aniso ? (const void *)k_sweep<true, 1> : (const void *)k_sweep<false, 1>;
+  const void *fn = aniso ? (const void *)k_sweep<true, 1, 3> : (const void *)k_sweep<false, 1, 3>;
+  if (form == SHAPE_REGS255) fn = aniso ? (const void *)k_sweep<true, 1, 2> : (const void *)k_sweep<false, 1, 2>;
+  if (form == SHAPE_QUEUE) fn = aniso ? (const void *)k_sweep_queue<true, 1> : (const void *)k_sweep_queue<false, 1>;
   cudaFuncGetAttributes(&fa, fn);
   *regs = fa.numRegs;
   *smem = (int)fa.sharedSizeBytes;

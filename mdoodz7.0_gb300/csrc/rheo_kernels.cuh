@@ -26,6 +26,14 @@ struct DevStats {
   unsigned int maxit;
   unsigned int mma_fault;      // a tensor-core completion wait gave up (warm start)
   unsigned long long f32_steps;  // FP32 Newton steps taken by the starts of the local solves
+  unsigned long long queue[2];   // work counters of the persistent sweep (centroids, vertices)
+};
+
+// Launch shape of the plain sweep: threads per block, grid cap (0: one thread per node;
+// else a grid-stride loop over that many CTAs) and the kernel form.
+enum { SHAPE_THREAD = 0, SHAPE_REGS255 = 1, SHAPE_QUEUE = 2 };
+struct LaunchShape {
+  int block, grid_cap, form;
 };
 
 // modes of the tiled sweep
@@ -86,7 +94,7 @@ struct PointArgs {
   DevStats *stats;
 };
 
-cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, int block, int grid_cap);
+cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, const LaunchShape &shape);
 // kernels launch_sweep issues for these arguments: one per kind of node (centroids,
 // vertices) with nodes in range; launch_sweep_tiles issues the same over the whole grid
 inline unsigned sweep_kernel_count(const SweepArgs &a) {
@@ -96,14 +104,22 @@ inline unsigned sweep_kernel_count(const SweepArgs &a) {
 // kernels launch_sweep_batch issues: one per kind of node with tiles
 inline unsigned batch_kernel_count(const BatchArgs &b) { return (b.tiles_n > 0 ? 1u : 0u) + (b.tiles_s > 0 ? 1u : 0u); }
 cudaError_t launch_points(const PointArgs &a, cudaStream_t s);
-cudaError_t launch_sweep_batch(const BatchArgs &b, bool aniso, cudaStream_t s, int grid);
-cudaError_t launch_perturb_batch(const BatchArgs &b, double amp, unsigned long long seed, int sweep, cudaStream_t s,
-                                 int grid);
+// Per-launch options of a batched sweep: the learned warm start (warm, mlp), and the
+// strain-rate perturbation fused into the load (amp != 0: factors 1 + amp u, u uniform in
+// [-1, 1) from the counter hash of (seed, sweep, grid, node, component)).
+struct BatchSweepArgs {
+  MlpDevice mlp;
+  int warm;
+  double amp;
+  unsigned long long seed;
+  int sweep;
+};
+cudaError_t launch_sweep_batch(const BatchArgs &b, const BatchSweepArgs &x, bool aniso, cudaStream_t s, int grid);
 cudaError_t launch_sweep_tiles(const SweepArgs &a, const WarmArgs &w, bool aniso, int mode, cudaStream_t s,
                                int grid);
 // the learned warm start evaluated per warp (mlp_warp.cuh): one launch per kind of node
 cudaError_t launch_sweep_warm(const SweepArgs &a, const MlpDevice &w, bool aniso, cudaStream_t s);
 int tiles_blocks_per_sm(bool aniso, int mode);
-void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block);
+void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block, int form);
 
 }  // namespace mdz

@@ -431,6 +431,8 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_autotune.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                       C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_get_launch_shape.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.mdz_rheo_get_launch_form.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    lib.mdz_rheo_set_launch_shape.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.mdz_rheo_set_warmstart.argtypes = [C.c_void_p, C.POINTER(MlpWeights), C.c_int]
     lib.mdz_rheo_set_mma_poll_limit.argtypes = [C.c_void_p, C.c_int32]
     lib.mdz_rheo_collect.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
@@ -721,7 +723,12 @@ class Context:
         return rc, st
 
     # ---- launch-shape autotuner
-    AUTOTUNE_CANDIDATES = [(b, w) for b in (128, 64) for w in (0, 1, 2, 4, 8)]  # (threads per block, waves)
+    # (threads per block, waves of resident CTAs or 0 for one thread per node, form); forms:
+    # 0 the 168-register kernel, 1 the 255-register kernel, 2 persistent work counter
+    AUTOTUNE_CANDIDATES = [(b, w, 0) for b in (128, 64) for w in (0, 1, 2, 4, 8)] + [(128, 0, 1), (128, 1, 2)]
+    AUTOTUNE_NAMES = ([f"block {b}, " + (f"{w} waves" if w else "one thread per node") for b in (128, 64)
+                       for w in (0, 1, 2, 4, 8)] + ["block 128, one thread per node, 255 registers (2 CTAs/SM)",
+                                                    "block 128, persistent warps on a work counter"])
 
     def autotune(self, model, mat, fields, aniso=False, flags=0, reps=3):
         """Time every launch shape on this device-resident grid and keep the fastest.
@@ -733,6 +740,18 @@ class Context:
         if rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_autotune")
         return ms, best.value, self.launch_shape(aniso)
+
+    def launch_form(self, aniso=False):
+        f = C.c_int()
+        rc = self.lib.mdz_rheo_get_launch_form(self.handle, int(aniso), C.byref(f))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_get_launch_form")
+        return f.value
+
+    def set_launch_shape(self, aniso=False, block=128, grid_cap=0, form=0):
+        rc = self.lib.mdz_rheo_set_launch_shape(self.handle, int(aniso), block, grid_cap, form)
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_set_launch_shape")
 
     def launch_shape(self, aniso=False):
         b, g = C.c_int(), C.c_int()

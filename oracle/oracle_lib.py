@@ -33,12 +33,24 @@ SHIM_SO = os.path.join(HERE, "_ref", "libmdz_shimtest.so")
 REF_TREE = os.environ.get("MDZ_REFERENCE_TREE") or os.path.join(os.path.dirname(REPO), "reference")
 
 
+GPUSHIM_SO = os.path.join(HERE, "_ref", "libmdz_gpushim.so")
+PRE_DIR = os.path.join(HERE, "_ref", "pre")
+GPU_LIB = os.path.join(REPO, "mdoodz7.0_gb300", "build", "libmdz_rheo_gb300.so")
+
+
 def build(ref: bool = False, quiet: bool = True):
-    """Build the restatement (and, when asked and the reference tree exists, _ref)."""
-    targets = ["all"]
+    """Build the restatement and, when asked, the reference's own code (_ref): from the
+    MDOODZ7.0 tree where it exists (which also writes the preprocessed units), else from
+    the preprocessed units written there before."""
+    targets, tree = ["all"], ""
     if ref and os.path.isdir(os.path.join(REF_TREE, "MDLIB")):
+        targets += ["pre", "ref", "shim"]
+        tree = REF_TREE
+    elif ref and os.path.exists(os.path.join(PRE_DIR, "RheologyDensity.i")):
         targets += ["ref", "shim"]
-    out = subprocess.run(["make", "-C", HERE, f"REF={REF_TREE}", "-j8"] + targets,
+    if len(targets) > 1 and os.path.exists(GPU_LIB):
+        targets.append("gpushim")
+    out = subprocess.run(["make", "-C", HERE, f"REF={tree}", "-j8"] + targets,
                          capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
@@ -135,6 +147,39 @@ def shimtest():
             fn.restype = C.c_int
         _shim = lib
     return _shim
+
+
+_gpushim = None
+
+
+def gpushim():
+    """The drop-in over the GPU library beside the reference's own code, or None where it
+    was not built."""
+    global _gpushim
+    if _gpushim is None and os.path.exists(GPUSHIM_SO):
+        lib = C.CDLL(GPUSHIM_SO)
+        for name in ("shimtest_ref_sweep", "shimtest_shim_sweep"):
+            fn = getattr(lib, name)
+            fn.argtypes = [C.POINTER(R.Model), C.POINTER(R.Materials), C.POINTER(R.GridFields), C.c_int, C.c_int]
+            fn.restype = C.c_int
+        _gpushim = lib
+    return _gpushim
+
+
+def gpushim_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False, drop_in=True):
+    """NonNewtonianViscosityGrid(Aniso) on a harness-built `grid`: the drop-in over the GPU
+    library (drop_in=True) or the reference's own."""
+    lib = gpushim()
+    fn = lib.shimtest_shim_sweep if drop_in else lib.shimtest_ref_sweep
+    return fn(C.byref(model), C.byref(mat), C.byref(fs.struct), final_update, int(aniso))
+
+
+def gpushim_strain_rates(model, dx, dz, sr: dict, out_of_plane=0, compressible=0.0, drop_in=True):
+    """StrainRateComponents on a harness-built `grid`: the drop-in over the GPU library or
+    the reference's own."""
+    name = "shimtest_shim_strain_rates" if drop_in else "shimtest_ref_strain_rates"
+    return _strain_fn(gpushim(), name)(C.byref(model), dx, dz, out_of_plane, float(compressible),
+                                       C.byref(R.make_strain_rate_fields(sr)))
 
 
 def shim_sweep(model, mat, fs: "R.FieldSet", final_update=0, aniso=False, drop_in=True):

@@ -35,6 +35,7 @@ def test_autotune_keeps_results_and_picks_a_candidate(aniso):
         assert np.all(ms > 0) and ms[best] == ms.min()
         assert shape[0] == R.Context.AUTOTUNE_CANDIDATES[best][0]
         assert (shape[1] == 0) == (R.Context.AUTOTUNE_CANDIDATES[best][1] == 0)
+        assert ctx.launch_form(aniso) == R.Context.AUTOTUNE_CANDIDATES[best][2]
         again = to_device(clone(w.arrays))
         fn(w.model, w.mat, R.FieldSet(again), mem=R.MEM_DEVICE)   # runs with the tuned shape
         a, t, g = to_host(ref), to_host(tuned), to_host(again)
@@ -44,5 +45,31 @@ def test_autotune_keeps_results_and_picks_a_candidate(aniso):
                 assert np.array_equal(a[k], g[k], equal_nan=True), k
         # the other kind keeps its own shape
         assert ctx.launch_shape(not aniso) == (128, 0)
+    finally:
+        ctx.close()
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+@pytest.mark.parametrize("form", [1, 2])
+def test_every_form_gives_the_same_bits(aniso, form):
+    """The 255-register kernel and the persistent work-counter kernel against the default
+    one-thread-per-node kernel, bit for bit, from both starts."""
+    w = W.aniso(seed=9, ncx=80) if aniso else W.plain_large(seed=9, ncx=90)
+    ctx = R.Context(0)
+    try:
+        fn = ctx.sweep_aniso if aniso else ctx.sweep
+        for flags in (0, R.SWEEP_REF_START):
+            ctx.set_launch_shape(aniso, 128, 0, 0)
+            ref = to_device(clone(w.arrays))
+            fn(w.model, w.mat, R.FieldSet(ref), mem=R.MEM_DEVICE, flags=flags)
+            ctx.set_launch_shape(aniso, 128, 0, form)
+            assert ctx.launch_form(aniso) == form
+            got = to_device(clone(w.arrays))
+            _, st = fn(w.model, w.mat, R.FieldSet(got), mem=R.MEM_DEVICE, flags=flags)
+            a, g = to_host(ref), to_host(got)
+            for k in R.CEN_OUT + R.VER_OUT:
+                if a.get(k) is not None:
+                    assert np.array_equal(a[k], g[k], equal_nan=True), (flags, k)
+            assert st.phase_calls > 0
     finally:
         ctx.close()

@@ -2,9 +2,10 @@
 
 Each grid of a batch has its own size, phase table and time step; after a batched
 sweep every grid must match its own oracle sweep at the plain kernel's bar.  The
-graph test perturbs the strain rates before each captured sweep; the perturbed
-inputs must equal the host statement of the perturbation exactly, and the outputs
-of the last sweep must match the oracle run on those inputs.
+graph tests perturb the strain rates in each captured sweep (fused into the sweep's
+load); the perturbed inputs must equal the host statement of the perturbation exactly,
+and the outputs of the last sweep must match the oracle run on those inputs, with the
+default start and with the learned warm start.
 """
 import numpy as np
 import pytest
@@ -85,7 +86,7 @@ def test_captured_graph_with_perturbed_strain_rates(ctx):
     nsw, amp, seed = 3, 0.05, 11
     b.capture(nsw, amp=amp, seed=seed)
     rc, st = b.launch()
-    assert rc == R.MDZ_OK and st.kernel_launches == 3 * nsw  # perturbation, centroids, vertices
+    assert rc == R.MDZ_OK and st.kernel_launches == 2 * nsw  # centroids, vertices; perturbation fused
     total_calls = 0
     for gi, (w, d) in enumerate(zip(ws, devs)):
         h = to_host(d)
@@ -121,12 +122,79 @@ def test_aniso_batch(ctx):
     b.close()
 
 
+def expected_inputs(w, gi, nsw, amp, seed):
+    """The host statement of `nsw` perturbations of grid gi's strain rates."""
+    expect = clone(w.arrays)
+    for s in range(nsw):
+        for comp, (kc, kv) in enumerate((("exxd", "exxd_s"), ("ezzd", "ezzd_s"), ("exz_n", "exz"))):
+            expect[kc] = R.perturb_reference(expect[kc], amp, seed, s, gi, comp, 0)
+            expect[kv] = R.perturb_reference(expect[kv], amp, seed, s, gi, comp, w.Nc)
+    return expect
+
+
+@pytest.fixture(scope="module")
+def network(ctx):
+    import mdz_warmstart as WS
+    X, Y = WS.collect(ctx, [W.plain_large(seed=150, ncx=129), W.plain_small(seed=151, ncx=129)])
+    w, _, _ = WS.train(ctx, X, Y, WS.FEAT_ISO, WS.default_cfg(epochs=3, batch=4096))
+    return w
+
+
+def test_warm_batch_matches_warm_single_sweeps_bitwise(ctx, network):
+    ctx.set_warmstart(network, R.DEFAULT_START)
+    ws = small_batch(seed=8, n=4)
+    devs = [to_device(clone(w.arrays)) for w in ws]
+    b = R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in devs],
+                flags=R.SWEEP_WARMSTART)
+    rc, st = b.sweep()
+    assert rc == R.MDZ_OK and st.kernel_launches == 2
+    for w, d in zip(ws, devs):
+        one = to_device(clone(w.arrays))
+        ctx.sweep(w.model, w.mat, R.FieldSet(one), mem=R.MEM_DEVICE, flags=R.SWEEP_WARMSTART)
+        a, o = to_host(d), to_host(one)
+        for k in R.CEN_OUT + R.VER_OUT:
+            if a.get(k) is not None:
+                assert np.array_equal(a[k], o[k], equal_nan=True), k
+    b.close()
+
+
+def test_warm_graph_of_20_perturbed_sweeps(ctx, network):
+    """Config 3's form on a few grids: one batch of uneven grids with the learned warm start,
+    20 sweeps captured as one graph, strain rates perturbed by +-5 % in each."""
+    ctx.set_warmstart(network, R.DEFAULT_START)
+    ws = small_batch(seed=9, n=4)
+    devs = [to_device(clone(w.arrays)) for w in ws]
+    b = R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in devs],
+                flags=R.SWEEP_WARMSTART)
+    nsw, amp, seed = 20, 0.05, 2026
+    b.capture(nsw, amp=amp, seed=seed)
+    rc, st = b.launch()
+    assert rc == R.MDZ_OK and st.kernel_launches == 2 * nsw and st.mma_fault == 0
+    calls = 0
+    for gi, (w, d) in enumerate(zip(ws, devs)):
+        h = to_host(d)
+        expect = expected_inputs(w, gi, nsw, amp, seed)
+        for k in ("exxd", "ezzd", "exz_n", "exxd_s", "ezzd_s", "exz"):
+            assert np.array_equal(h[k], expect[k]), (gi, k)
+        rc2, st2 = O.orc_sweep(w.model, w.mat, R.FieldSet(expect))
+        assert rc2 == R.MDZ_OK
+        calls += st2.phase_calls
+        check(h, expect, W.Workload(w.name, w.model, w.mat, expect), f"warm graph grid {gi}")
+    assert st.phase_calls == nsw * calls
+    assert st.newton_iters <= 1.05 * st.phase_calls  # about one FP64 evaluation per local solve
+    b.close()
+
+
 def test_batch_argument_checks(ctx):
     ws = small_batch(seed=6, n=2)
     devs = [to_device(clone(w.arrays)) for w in ws]
-    with pytest.raises(R.RheoError):
+    ctx.set_warmstart(None)
+    with pytest.raises(R.RheoError):  # no network installed
         R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in devs],
                 flags=R.SWEEP_WARMSTART)
+    with pytest.raises(R.RheoError):
+        R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in devs],
+                flags=R.SWEEP_WARMSTART | R.SWEEP_REF_START)
     b = R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in devs])
     rc, _ = b.launch(check=False)
     assert rc == R.MDZ_ENOTREADY
