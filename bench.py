@@ -428,12 +428,27 @@ def aniso_section(args, ctx, dev, ws, rank, stream, barrier, no_warm):
     return out
 
 
-def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, wts=None):
+def many_grid_network(ctx, rank):
+    """The 10-input network for the many-grid workload, trained on pairs the plain kernel
+    produces on a separate batch of the same distribution (fresh seed): its time steps
+    (1e10-1e12 s) and phase counts are not the single grid's."""
+    import mdz_rheo as R
+    import mdz_warmstart as WSt
+    import mdz_workloads as W
+    src = W.many_grids(seed=700 + 1000 * rank, n=24)
+    Xs, Ys = WSt.collect(ctx, src, max_pairs=8_000_000)
+    del src
+    wts, loss, train_s = WSt.train(ctx, Xs, Ys, WSt.FEAT_ISO)
+    return wts, {"pairs": int(Xs.shape[0]), "train_s": train_s, "final_train_loss": float(loss[-1])}
+
+
+def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, warm=False):
     """Config 3: 64 grids of uneven size (65-1025 cells per side, 2-5 phases, dt 1e10-1e12 s,
     each with its own seed), device-resident.  Forms of one Picard sweep over all of them:
     64 separate sweep calls, one batched sweep (two launches), and a CUDA graph of 20
     batched sweeps with the strain rates perturbed by +-5 % in each (fused into the
-    sweep's load), with the default start and with the learned warm start (`wts`)."""
+    sweep's load), with the default start and (warm) with the learned warm start, its
+    network trained on a separate batch of the same distribution."""
     import torch
 
     import mdz_replicas as REP
@@ -467,6 +482,7 @@ def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, wts=None):
     nsw, amp = 20, 0.05
     forms = {"separate_calls": ms_sep}
     graphs = {}
+    wts, train = (many_grid_network(ctx, rank) if warm else (None, None))
     for label, flags in (("default", 0), ("warm", R.SWEEP_WARMSTART)):
         if flags and wts is None:
             continue
@@ -506,7 +522,7 @@ def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, wts=None):
                        "U[-1,1)) in each (fused into the sweep's load)",
            "nodes_per_sweep": nodes, "sweeps_per_graph": nsw, "generate_s": gen_s,
            "value": graphs["default"]["value"], "unit": UNIT, "ms_per_sweep": graphs["default"]["ms_per_sweep"],
-           "graph": graphs, "forms_ms_per_sweep": forms,
+           "graph": graphs, "forms_ms_per_sweep": forms, "warm_network": train,
            "separate_vs_graph": ms_sep / graphs["default"]["ms_per_sweep"]}
     del devs, fss
     torch.cuda.empty_cache()
@@ -858,7 +874,8 @@ def main():
     configs, mg_sample = None, None
     if not args.no_configs and not aniso:
         configs = {"aniso_4097": aniso_section(args, ctx, dev, ws, rank, stream, barrier, args.no_warm)}
-        configs["many_grids_64"], mg_sample = many_grids_section(args, ctx, dev, ws, rank, stream, barrier, wts)
+        configs["many_grids_64"], mg_sample = many_grids_section(args, ctx, dev, ws, rank, stream, barrier,
+                                                                 warm=not args.no_warm)
 
     if rank != 0:
         REP.finalize()

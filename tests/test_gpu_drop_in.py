@@ -7,8 +7,7 @@ links that translation unit, unchanged, with the real GPU library and with the
 reference's own sources (its functions renamed, so both sit side by side), and the
 reference's harness builds a real `grid` / `mat_prop` / `params` / `scale` from the
 test's arrays.  So this is a whole MDOODZ call on the GPU, compared with the same call
-of the reference itself: sweeps within the parity bar of the other GPU tests, strain
-rates bit for bit.  The library is built by `__graft_entry__.build()` from the
+of the reference itself, within the parity bar of the other GPU tests.  The library is built by `__graft_entry__.build()` from the
 reference's sources, or from their preprocessed units where the tree is absent.
 """
 import numpy as np
@@ -59,11 +58,18 @@ def test_drop_in_on_gpu_periodic_and_air():
     compare(gpu, ref, w, "drop-in periodic + air")
 
 
-def test_drop_in_strain_rates_on_gpu_bitwise():
+def test_drop_in_strain_rates_on_gpu():
+    """StrainRateComponents through the drop-in on the GPU against the reference's own,
+    within 1e-13 of each field's largest magnitude.  (The GPU kernel reproduces the
+    reference's x86-64 build bit for bit -- tests/test_gpu_strain_rates.py, on the golden
+    fixtures -- but where the reference is compiled on an aarch64 host, gcc contracts its
+    multiply-adds into fused ones by default, which moves its own last bits.)"""
     v = W.velocity_field(seed=12, ncx=70, ncz=50, air=0.2, periodic=1)
     ref = {k: a.copy() for k, a in v.arrays.items()}
     gpu = {k: a.copy() for k, a in v.arrays.items()}
     assert O.gpushim_strain_rates(v.model, v.info["dx"], v.info["dz"], ref, 1, 1.0, drop_in=False) == 0
     assert O.gpushim_strain_rates(v.model, v.info["dx"], v.info["dz"], gpu, 1, 1.0, drop_in=True) == 0
     for k in R.SR_N + R.SR_S:
-        assert np.array_equal(gpu[k].view(np.uint64), ref[k].view(np.uint64)), k
+        scale = max(float(np.max(np.abs(ref[k]))), 1e-300)
+        err = float(np.max(np.abs(gpu[k] - ref[k]))) / scale
+        assert err <= 1e-13, (k, err)
