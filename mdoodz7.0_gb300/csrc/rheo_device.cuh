@@ -363,22 +363,22 @@ __device__ __forceinline__ double ve_S(const VeCoef &q, const VeState &s) {
 
 // Newton on s from sv: s <- s (1 + step), step = r / (Aup s + S), i.e. s - r / r'(s)
 // with r' = -Aup - S/s (LocalIterationViscoElastic); returns eta = s eta_up in st.eta.
-// A start moved away from the reference's (sv != 1) that has not converged within the cap
-// is abandoned: the iteration runs again from the reference's start, with the reference's
-// cap, and the evaluations of both runs count.
-__device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s) {
+// A moved start (one the start stages chose) that has not converged within the cap is
+// abandoned: the iteration runs again from the upper bound eta_up (s_up), with the
+// reference's cap, and the evaluations of both runs count.
+__device__ __forceinline__ void ve_newton(const VeCoef &q, double sv, VeState &s, float s_up = 1.0f,
+                                          bool moved = false) {
   const int nitmax = 20;
   s.iters = 0;
-  bool moved = !fp64_eq_nonzero(sv, 1.0);
   double step = -1.0;  // no previous point yet
   for (int it = 0; it < nitmax; it++) {
     double r;
     ve_eval(q, sv, s, r, step);
     s.iters++;
     if (fp64_abs_lt(r, q.thr_conv)) break;
-    if (it == nitmax - 1 && moved) {  // back to the reference's start
+    if (it == nitmax - 1 && moved) {  // back to the upper bound
       moved = false;
-      sv = 1.0;
+      sv = f64_of_f32(s_up);
       step = -1.0;
       it = -1;
       continue;
@@ -425,8 +425,9 @@ __device__ __forceinline__ void start_coef(const VeCoef &q, StartCoef &sc) {
   for (int k = 0; k < K_COUNT; k++) sc.c[k] = (q.nl >> k & 1) ? fma(q.n[k], q.lp, q.nc[k]) : 0.0;
 }
 
+// s_hi: the upper bound the iteration falls back to
 __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef &sc, float s0, int iters,
-                                               int &taken) {
+                                               int &taken, float s_hi) {
   taken = 0;
   if (iters <= 0) return s0;
   const float a = f32_trunc(sc.a);
@@ -453,7 +454,7 @@ __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef 
     if (fabsf(r) < 1e-6f) break;
     const float sn = s + r * s / fmaf(a, s, S);
     taken = it + 1;
-    if (!(sn > 0.0f && sn <= 2.0f)) return 1.0f;  // the upper bound eta_up: right of the root
+    if (!(sn > 0.0f && sn <= 2.0f)) return s_hi;  // the upper bound eta_up: right of the root
     s = sn;
   }
   return s;
@@ -462,8 +463,8 @@ __device__ __forceinline__ float ve_polish_f32(const VeCoef &q, const StartCoef 
 // Stage 2 from the FP32 point s (see above).  Where s is not a positive normal number in
 // (0, 2], or the correction is not small (the polish did not settle), the FP64 Newton
 // starts at s itself if s lies above the root and at the upper bound s = 1 otherwise.
-__device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef &sc, float s) {
-  if (!(s >= 1.17549435e-38f && s <= 2.0f)) return 1.0;
+__device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef &sc, float s, float s_hi) {
+  if (!(s >= 1.17549435e-38f && s <= 2.0f)) return f64_of_f32(s_hi);
   const f2 a = dd_of_f64(sc.a);
   const f2 as = dd_mul_f(a, s);
   f2 E = {0.0f, 0.0f}, D = as;
@@ -486,7 +487,7 @@ __device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef 
   const float q1 = __fdividef(r.hi, D.hi);
   // an unsettled point: the FP64 Newton takes it from there if it lies above the root
   // (r <= 0, monotone descent), from the upper bound s = 1 otherwise
-  if (!(fabsf(q1) < 1e-3f)) return (r.hi > 0.0f) ? 1.0 : f64_of_f32(s);
+  if (!(fabsf(q1) < 1e-3f)) return f64_of_f32((r.hi > 0.0f) ? s_hi : s);
   const f2 rem = dd_add(r, dd_neg(dd_mul_f(D, q1)));
   const float q2 = __fdividef(rem.hi, D.hi);
   const float h = __fdividef(__fmul_rn(__fmul_rn(q1, q1), Q), 2.0f * D.hi);  // Halley's term d^2 Q / (2 D)
@@ -499,13 +500,14 @@ __device__ __forceinline__ double ve_halley_dd(const VeCoef &q, const StartCoef 
 
 // The start of the FP64 Newton: `fp32` FP32 Newton steps from s0, then, with `dd`, the
 // double-float Halley step.
-__device__ __forceinline__ double ve_start(const VeCoef &q, float s0, int fp32, bool dd, int &taken) {
+__device__ __forceinline__ double ve_start(const VeCoef &q, float s0, int fp32, bool dd, int &taken,
+                                           float s_hi = 1.0f) {
   taken = 0;
   if (fp32 <= 0 && !dd) return f64_of_f32(s0);
   StartCoef sc;
   start_coef(q, sc);
-  const float s = ve_polish_f32(q, sc, s0, fp32, taken);
-  return dd ? ve_halley_dd(q, sc, s) : f64_of_f32(s);
+  const float s = ve_polish_f32(q, sc, s0, fp32, taken, s_hi);
+  return dd ? ve_halley_dd(q, sc, s, s_hi) : f64_of_f32(s);
 }
 
 // The start descriptor carried by the kernels' `polish` argument: FP32 Newton steps in the
@@ -676,6 +678,11 @@ __device__ inline int plastic_popov(const ModelConst &M, const PhaseConst &ph, d
 struct IsoState {
   Laws L;
   double eta_up, ln_eta_up, eta_cst, Tyield, C, Ag, lnd;
+  // normalisation of the local Newton's unknown s = eta / eta_n: eta_n = eta_up where the
+  // start is the reference's (exact), else the power of two nearest eta_up; s_up = the
+  // start point eta_up in that unknown (1 when exact)
+  double eta_n, ln_eta_n;
+  float s_up;
 };
 
 // Start point of the local solve (RheologyDensity.c:582-592, AnisotropyRoutines.c:409-415):
@@ -696,6 +703,41 @@ __device__ __forceinline__ void start_viscosity(const ModelConst &M, double ln_i
   if (from_cst) ln_eta_up = fast_log(eta_cst);
 }
 
+// The start point and the normalisation of the local solve.  Exact (the reference's start,
+// and the grain-size and bisection solves, which need its bracket): eta_up as the
+// reference forms it, and eta_n = eta_up.  Otherwise eta_up is only the upper bound where
+// the start stages begin (s_up), and nothing needs its FP64 value: its logarithm is the
+// smallest of the candidates' logarithms (compared on the integer pipe; no exp), and the
+// unknown is normalised by eta_n = 2^k, k the nearest integer to log2(eta_up), built from
+// bits, with ln(eta_n) = k ln2; s_up = exp(ln eta_up - k ln2) in [0.7, 1.42] in FP32.
+__device__ __forceinline__ void start_point(const ModelConst &M, double ln_inv_max, bool constant, double eta_cst,
+                                            bool elastic, const NodeCtx &c, bool exact, IsoState &S) {
+  if (!exact) {
+    double ln = M.ln_eta_up0;
+    if (constant) {
+      const double lc = fast_log(eta_cst);
+      if (fp64_lt(lc, ln)) ln = lc;
+    }
+    if (fp64_gt(ln_inv_max, -kInf) && fp64_lt(-ln_inv_max, ln)) ln = -ln_inv_max;
+    if (elastic && fp64_lt(c.ln_eta_el, ln)) ln = c.ln_eta_el;
+    const float lf = f32_trunc(ln);
+    if (fabsf(lf) < 690.0f) {  // finite, and 2^k a normal double
+      const int k = __float2int_rn(lf * 1.44269504f);
+      S.ln_eta_up = ln;
+      S.eta_up = 0.0;  // not formed
+      S.eta_n = __hiloint2double((k + 1023) << 20, 0);
+      const double kd = __hiloint2double(0x43300000, k ^ (int)0x80000000) - 4503601774854144.0;  // (double)k
+      S.ln_eta_n = fma(kd, MDZ_LN2_HI, kd * MDZ_LN2_LO);
+      S.s_up = __expf(fmaf((float)-k, 0.693147182f, lf));
+      return;
+    }
+  }
+  start_viscosity(M, ln_inv_max, constant, eta_cst, elastic, c, S.eta_up, S.ln_eta_up);
+  S.eta_n = S.eta_up;
+  S.ln_eta_n = S.ln_eta_up;
+  S.s_up = 1.0f;
+}
+
 // Lower end of the reference's bracket: the largest of the lower bound, eta_cst, eta_el and
 // the isolated creep viscosities (needed by the grain-size solve and the bisection only).
 __device__ __forceinline__ double lower_viscosity(const ModelConst &M, const Laws &L, bool constant, double eta_cst,
@@ -710,8 +752,9 @@ __device__ __forceinline__ double lower_viscosity(const ModelConst &M, const Law
   return eta_lo;
 }
 
+// exact: the local solve starts where the reference's does (start descriptor 0)
 __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                 IsoState &S, PointOut &o) {
+                                 IsoState &S, PointOut &o, bool exact = true) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, diffusion = (fl & F_LIN) != 0, gs = (fl & F_GS) != 0;
   const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
@@ -765,7 +808,7 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   // bracket (:582-592): the smallest isolated viscosity is 1 / the largest reciprocal
   const double ln_inv_max =
       fp64_fmax(fp64_fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), fp64_fmax(L.ln_inv[K_LIN], L.ln_inv_gbs));
-  start_viscosity(M, ln_inv_max, constant, eta_cst, elastic == 1, c, S.eta_up, S.ln_eta_up);
+  start_point(M, ln_inv_max, constant, eta_cst, elastic == 1, c, exact || gs, S);
   S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
 
@@ -790,10 +833,11 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   double eta_ve, Tii, e_cst, e_pwl, e_exp, e_lin;
   if (!gs) {  // LocalIterationViscoElastic (:646)
     VeCoef q;
-    ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
+    ve_coef(L, c, eta_cst, S.eta_n, S.ln_eta_n, q);
     VeState s;
     s.status = MDZ_OK;
-    ve_newton(q, ve_start(q, s_start, start_fp32(polish), start_dd(polish), o.f32_steps), s);
+    ve_newton(q, ve_start(q, s_start * S.s_up, start_fp32(polish), start_dd(polish), o.f32_steps, S.s_up), s,
+              S.s_up, polish != 0);
     set_status(o.status, s.status);
     eta_ve = s.eta; Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
     o.iters = s.iters;
@@ -963,7 +1007,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
 __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
                                  int polish, PointOut &o) {
   IsoState S;
-  iso_setup(M, ph, in, c, S, o);
+  iso_setup(M, ph, in, c, S, o, polish == 0);
   iso_finish(M, ph, in, c, S, 1.0f, polish, o);
 }
 
@@ -1004,7 +1048,7 @@ __device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const Node
 }
 
 __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                   const AnisoNode &an, IsoState &S, PointOut &o) {
+                                   const AnisoNode &an, IsoState &S, PointOut &o, bool exact = true) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
   const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
@@ -1037,7 +1081,7 @@ __device__ inline void aniso_setup(const ModelConst &M, const PhaseConst &ph, co
   const double eta_cst = constant ? ph.eta0 : 0.0;
   // bracket (:409-415); its lower end is formed only where it is used
   const double ln_inv_max = fp64_fmax(fp64_fmax(L.ln_inv[K_PWL], L.ln_inv[K_EXP]), L.ln_inv[K_LIN]);
-  start_viscosity(M, ln_inv_max, constant, eta_cst, elastic != 0, c, S.eta_up, S.ln_eta_up);
+  start_point(M, ln_inv_max, constant, eta_cst, elastic != 0, c, exact || (fl & F_GS), S);
   S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = Coh; S.Ag = 0.0;
   S.lnd = c.lnd;
   (void)an; (void)T; (void)K; (void)dt; (void)min_eta; (void)max_eta; (void)dislocation; (void)eta_el;
@@ -1078,12 +1122,13 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   } else {  // :474-585: 10 log-space bisection steps on [min_eta 1e-3, 10 max(eta_lo, max_eta)], then Newton
     const double tol = 1e-11;
     VeCoef q;
-    ve_coef(L, c, eta_cst, eta_up, S.ln_eta_up, q);
+    ve_coef(L, c, eta_cst, S.eta_n, S.ln_eta_n, q);
     VeState s;
     s.status = MDZ_OK;
-    double r, sv;  // sv = eta_ve / eta_up
+    double r, sv;  // sv = eta_ve / eta_n (eta_n = eta_up from the bisection: that start is exact)
     if (s_start > 0.0f || polish > 0) {
-      sv = ve_start(q, (s_start > 0.0f) ? s_start : 1.0f, start_fp32(polish), start_dd(polish), o.f32_steps);
+      sv = ve_start(q, ((s_start > 0.0f) ? s_start : 1.0f) * S.s_up, start_fp32(polish), start_dd(polish),
+                    o.f32_steps, S.s_up);
     } else {
       const double inv_up = 1.0 / eta_up;
       const double eta_lo = lower_viscosity(M, L, constant, eta_cst, elastic != 0, eta_el, false);
@@ -1109,12 +1154,12 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
       const double d = newton_quotient(r, fma(q.Aup, sv, ve_S(q, s)));
       sv = fma(sv, d, sv);
       step = fp64_lt(fabs(d) * q.nmax, 1e-5) ? d : -1.0;
-      if (fp64_le(sv, 0.0)) { sv = min_eta / eta_up; step = -1.0; }
+      if (fp64_le(sv, 0.0)) { sv = min_eta / q.eta_up; step = -1.0; }
       const double ar = fabs(r);
       if (fp64_abs_lt(r, q.thr_conv)) break;
       if (it == 49 && moved && !(ar < 10.0 * tol * Eii)) {
         moved = false;
-        sv = 1.0;
+        sv = f64_of_f32(S.s_up);
         step = -1.0;
         it = -1;
         continue;
@@ -1122,7 +1167,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
       if (it == 49 && ar < 10.0 * tol * Eii) break;
       if (it == 49 && ar > q.thr_fail) { set_status(o.status, MDZ_EANISO_ITER); break; }
     }
-    eta_ve = sv * eta_up;
+    eta_ve = sv * q.eta_up;
     Tii = s.Tii; e_cst = s.e_cst; e_pwl = s.e_pwl; e_exp = s.e_exp; e_lin = s.e_lin;
   }
   if (fp64_lt(eta_ve, min_eta)) eta_ve = min_eta;  // :589-603
@@ -1193,7 +1238,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
 __device__ inline void point_aniso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
                                    const AnisoNode &an, int polish, PointOut &o) {
   IsoState S;
-  aniso_setup(M, ph, in, c, an, S, o);
+  aniso_setup(M, ph, in, c, an, S, o, polish == 0);
   aniso_finish(M, ph, in, c, an, S, 0.0f, polish, o);
 }
 

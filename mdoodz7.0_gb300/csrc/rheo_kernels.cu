@@ -396,8 +396,8 @@ __device__ __forceinline__ void warm_node(const SweepArgs &A, MlpWarpShared &S, 
 #pragma unroll
     for (int k = 0; k < kMlpIn; k++) f[k] = 0.0f;
     if (active) {
-      if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
-      else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
+      if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o, W.polish_iters == 0);
+      else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o, W.polish_iters == 0);
       warm_features(A.M, n.in, n.ctx, st, ANISO, f);
     }
     warm_inputs(W, f, nfeat, x);
@@ -518,8 +518,9 @@ __global__ void __launch_bounds__(128, 2) k_sweep_tiles(const __grid_constant__ 
       for (int j = 0; j < kMlpIn; j++) f[j] = 0.0f;
       float s_start = ANISO ? 0.0f : 1.0f;  // the reference's own start
       if (active) {
-        if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o);
-        else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o);
+        const bool exact = (MODE == MODE_COLLECT) || W.mlp.polish_iters == 0;  // the pairs' targets need eta_up
+        if (ANISO) aniso_setup(A.M, A.ph[p], n.in, n.ctx, n.an, st, o, exact);
+        else iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o, exact);
         warm_features(A.M, n.in, n.ctx, st, ANISO, f);
       }
       if (MODE == MODE_WARM) {
