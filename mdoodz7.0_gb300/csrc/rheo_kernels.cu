@@ -46,9 +46,14 @@ __device__ __forceinline__ unsigned long long splitmix64(unsigned long long z) {
   return z ^ (z >> 31);
 }
 
+// u = m 2^-52 - 1 for the top 53 bits m of the hash, in [-1, 1).  Every such value is a
+// double, so u is formed exactly without an integer-to-double conversion (an FP64-pipe
+// instruction on this GPU): the low 52 bits of m as the fraction of a number in [1, 2),
+// minus 1 where m >= 2^52 and minus 2 below (both subtractions exact).
 __device__ __forceinline__ double perturb_factor(unsigned long long key, long long node, int comp, double amp) {
-  const unsigned long long h = splitmix64(key ^ (unsigned long long)(node * 3 + comp));
-  const double u = __dsub_rn(__dmul_rn((double)(h >> 11), 0x1.0p-52), 1.0);  // [-1, 1)
+  const unsigned long long m = splitmix64(key ^ (unsigned long long)(node * 3 + comp)) >> 11;
+  const double f = __longlong_as_double((long long)(0x3ff0000000000000ull | (m & 0xfffffffffffffull)));
+  const double u = __dsub_rn(f, (m >> 52) ? 1.0 : 2.0);  // [-1, 1)
   return __dadd_rn(1.0, __dmul_rn(amp, u));
 }
 
@@ -65,7 +70,7 @@ __device__ __forceinline__ unsigned long long perturb_key(unsigned long long see
 
 // The node's three strain-rate inputs x[0..2] (exxd, ezzd, exz of a centroid or of a
 // vertex, node index i over [centroids | vertices]) multiplied by their factors and stored
-// back, as the separate perturbation kernel does.
+// back, so the next captured sweep starts from the perturbed rates.
 __device__ __forceinline__ void perturb_inputs(const PerturbKey &pk, long long i, double *const *x) {
 #pragma unroll
   for (int k = 0; k < 3; k++) *x[k] = __dmul_rn(*x[k], perturb_factor(pk.key, i, k, pk.amp));

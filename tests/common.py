@@ -6,7 +6,10 @@ The reference itself only resolves its local solve to |r/Eii| < 1e-13
 (MDLIB/RheologyDensity.c:154,172), so an output that is a small difference of
 larger quantities is only defined to that tolerance in the reference too:
 
-  * strain-rate partition (eII_*, div_u_pl): scale max(|ref|, Eii of the node);
+  * strain-rate partition (eII_*, div_u_pl): scale max(|ref|, Eii of the node), the
+    invariant the local solve normalises its residual by (for the anisotropic routine,
+    that of its own effective strain rate, whose elastic term goes through the inverse of
+    the anisotropic elastic matrix and can be tens of times the isotropic one);
   * dissipative viscosity eta_phys: scale |ref| * max(1, |ref| / eta_VE) (it is
     the reciprocal of the viscous + plastic part of Eii, ill-conditioned where
     deformation is mostly elastic);
@@ -41,16 +44,40 @@ def field(a, k):
     return np.concatenate(v) if isinstance(v, list) else v
 
 
-def node_Eii(a, model, where="n"):
-    """Effective strain-rate invariant of the centroids ("n") or vertices ("s")."""
+def node_strain_rates(a, model, where="n"):
+    """Effective strain rates (Exx, Ezz, Exz) of the centroids ("n") or vertices ("s"): the
+    strain rates plus the elastic stress memory, isotropic (RheologyDensity.c:1199-1204,
+    :1335-1340) or, where the workload carries the anisotropy fields, through the inverse of
+    the anisotropic elastic matrix (EffectiveStrainRate, RheologyDensity.c:116-146, called at
+    AnisotropyRoutines.c:976, :1123)."""
+    s = "_n" if where == "n" else "_s"
     if where == "n":
         exx, ezz, exz, sxx, szz, sxz, mu = (a["exxd"], a["ezzd"], a["exz_n"], a["sxxd0"], a["szzd0"],
                                             a["sxz0_n"], a["mu_n"])
     else:
         exx, ezz, exz, sxx, szz, sxz, mu = (a["exxd_s"], a["ezzd_s"], a["exz"], a["sxxd0_s"], a["szzd0_s"],
                                             a["sxz0"], a["mu_s"])
-    h = (0.5 / (model.dt * mu)) if model.elastic == 1 else 0.0
-    Exx, Ezz, Exz = exx + sxx * h, ezz + szz * h, exz + sxz * h
+    if model.elastic != 1:
+        return exx, ezz, exz
+    eta_e = model.dt * mu
+    if a.get("aniso_factor" + s) is None:
+        return exx + sxx / eta_e / 2.0, ezz + szz / eta_e / 2.0, exz + sxz / eta_e / 2.0
+    d1, d2, ani = a["d1" + s], a["d2" + s], 1.0 - 1.0 / a["aniso_factor" + s]
+    D11, D12, D13 = 2.0 - 2.0 * ani * d1, 2.0 * ani * d1, -2.0 * ani * d2
+    D22, D23, D33 = 2.0 - 2.0 * ani * d1, 2.0 * ani * d2, 1.0 + 2.0 * ani * (d1 - 0.5)
+    a11, a12, a13 = D33 * D22 - D23 ** 2, D13 * D23 - D33 * D12, D12 * D23 - D13 * D22
+    a22, a23, a33 = D33 * D11 - D13 ** 2, D12 * D13 - D11 * D23, D11 * D22 - D12 ** 2
+    det = D11 * a11 + D12 * a12 + D13 * a13
+    return (exx + (a11 / det * sxx + a12 / det * szz + a13 / det * sxz) / eta_e,
+            ezz + (a12 / det * sxx + a22 / det * szz + a23 / det * sxz) / eta_e,
+            exz + (a13 / det * sxx + a23 / det * szz + a33 / det * sxz) / eta_e / 2.0)
+
+
+def node_Eii(a, model, where="n"):
+    """Invariant of the effective strain rate of the centroids ("n") or vertices ("s"): the
+    Eii that the node's local solves normalise their residual by (the anisotropic routine's
+    rotation to the director frame leaves it unchanged)."""
+    Exx, Ezz, Exz = node_strain_rates(a, model, where)
     Eyy = -(Exx + Ezz)
     return np.sqrt(0.5 * (Exx ** 2 + Ezz ** 2 + Eyy ** 2) + Exz ** 2)
 
@@ -112,23 +139,25 @@ def eta_phys_phase_scale(w, ref, nodes, where="s", phases=False):
                "Txx0": a["sxxd0"], "Tzz0": a["szzd0"], "Txz0": a["sxz0_n"], "strain_acc": a["strain_n"],
                "dil": a["dil_n"], "fric": a["fric_n"], "C": a["C_n"], "P0": a["p0_n"], "T0": a["T0_n"],
                "beta": a["bet_n"], "div": a["div_u"]}
-        exx, ezz, exz = a["exxd"], a["ezzd"], a["exz_n"]
     else:
         src = {"G": a["mu_s"], "T": ref["T_s"], "P": ref["P_s"], "d": ref["d0_s"], "phi": ref["phi0_s"],
                "X0": a["X0_s"], "Txx0": a["sxxd0_s"], "Tzz0": a["szzd0_s"], "Txz0": a["sxz0"],
                "strain_acc": a["strain_s"], "dil": a["dil_s"], "fric": a["fric_s"], "C": a["C_s"], "P0": a["p0_s"],
                "T0": np.zeros_like(a["mu_s"]), "beta": a["bet_s"], "div": a["div_u_s"]}
-        exx, ezz, exz = a["exxd_s"], a["ezzd_s"], a["exz"]
     pin = {k: np.repeat(v[nodes], np_) for k, v in src.items()}
-    el = 1.0 if m.elastic == 1 else 0.0
-    eta_e = m.dt * pin["G"] if m.elastic == 1 else np.ones(npn * np_)
-    pin["Exx"] = np.repeat(exx[nodes], np_) + el * pin["Txx0"] / eta_e / 2.0
-    pin["Ezz"] = np.repeat(ezz[nodes], np_) + el * pin["Tzz0"] / eta_e / 2.0
-    pin["Exz"] = np.repeat(exz[nodes], np_) + el * pin["Txz0"] / eta_e / 2.0
+    E = node_strain_rates(a, m, where)
+    pin["Exx"], pin["Ezz"], pin["Exz"] = (np.repeat(x[nodes], np_) for x in E)
+    aniso = a.get("aniso_factor_n") is not None
+    if aniso:  # the director frame of NonNewtonianViscosityGridAniso (AnisotropyRoutines.c:959-961)
+        s = "_n" if cen else "_s"
+        angle = np.repeat(a["angle" + s][nodes], np_)
+        lay = angle - np.pi / 2.0
+        pin["lxlz"], pin["lx2"], pin["angle"] = np.cos(lay) * np.sin(lay), np.cos(lay) * np.cos(lay), angle
+        pin["ani_fac"] = np.repeat(a["aniso_factor" + s][nodes], np_)
     pin["phase"] = np.tile(np.arange(np_, dtype=np.int32), npn)
     out = {k: np.zeros(npn * np_) for k in R.PT_OUT}
     pi, po = R.make_points(pin, out, centroid=1 if cen else 0)
-    O.orc_points(m, mat, pi, po, npn * np_, 0)
+    O.orc_points(m, mat, pi, po, npn * np_, 1 if aniso else 0)
     eta = out["eta"].reshape(npn, np_)
     eve = out["etaVE"].reshape(npn, np_)
     perc = np.stack([a["phase_perc_n" if cen else "phase_perc_s"][p][nodes] for p in range(np_)], axis=1)

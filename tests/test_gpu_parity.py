@@ -202,8 +202,6 @@ def test_aniso_typical_scale_harmonic(ctx):
     check_close(g, c, "aniso-typical-harmonic", w)
 
 
-ANISO_SOLVE_TOL = 1e-11  # tol of ViscosityConciseAniso's local Newton (AnisotropyRoutines.c:507-583)
-
 FULL = {
     # the headline sweep: 2049 x 2049 cells, 5 phases, 8,400,901 nodes (host memory, in row bands)
     "plain_large_2049": (lambda: W.plain_large(seed=1, ncx=2049), False),
@@ -217,7 +215,12 @@ def test_full_size_sweep_matches_oracle(ctx, name):
     """The benchmark workloads at their full sizes, every node against the oracle (which
     runs with OpenMP on the host cores), with the same parity bar as the small cases; the
     few nodes whose eta_phys the node-average scale flags are measured with the per-phase
-    scale (common.eta_phys_phase_scale)."""
+    scale (common.eta_phys_phase_scale).  In the anisotropic sweep those nodes are phases
+    just past their yield stress where deformation is mostly elastic: the plastic strain
+    rate gdot = (Tii - Tyield) / (eta_ve + ...) (AnisotropyRoutines.c:625-648) is a small
+    difference, which the local solve's tolerance |r| < 1e-13 Eii (:563) leaves open in its
+    last bits, and its dissipative viscosity Tii / gdot dominates the phase's eta_phys; the
+    per-phase scale carries exactly that conditioning."""
     make, aniso = FULL[name]
     w = make()
     rc, st, g, rc2, st2, c = run_pair(ctx, w, aniso=aniso)
@@ -228,20 +231,13 @@ def test_full_size_sweep_matches_oracle(ctx, name):
     for k, v in errs.items():
         if v <= RTOL:
             continue
-        if aniso:
-            # ViscosityConciseAniso documents that its residual loses about 12 digits where
-            # deformation is mostly elastic and accepts an iterate at |r/Eii| < 10 tol
-            # (AnisotropyRoutines.c:568-583): the plastic part and the dissipative
-            # viscosity are only defined to its tolerance, 1e-11, there
-            assert k in ("eta_phys_n", "eta_phys_s", "eII_pl") and v <= ANISO_SOLVE_TOL, (k, v)
-            continue
         assert k in ("eta_phys_n", "eta_phys_s"), (k, v)
         where = k[-1]
         x, ref = g[k], c[k]
         e = scaled_error(x, ref, np.abs(ref) * np.maximum(1.0, np.abs(ref) / np.abs(c["eta_" + where])))
         flagged = np.flatnonzero(e > RTOL)
-        print(k, "nodes flagged by the node-average scale:", flagged.size)
-        assert flagged.size <= 1000
+        print(k, "nodes flagged by the node-average scale:", flagged.size, "of", x.size)
+        assert flagged.size <= max(1000, x.size // 10000)
         scale = eta_phys_phase_scale(w, c, flagged, where)
         pe = np.abs(x[flagged] - ref[flagged]) / scale
         print(k, "largest per-phase scaled error:", float(pe.max()))
