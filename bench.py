@@ -60,9 +60,9 @@ FP64_FLOPS_PER_POINT = {"plain_large": 1560.2, "aniso": 1094.8}
 # have 2 to 5 phases, so the work is counted per phase call.
 FP64_FLOPS_PER_PHASE_CALL = {"many_grids": 312.0}
 # DRAM bytes (read + write) per point-update of one sweep's two launches at 1025 x 1025
-# cells (0.7 GB of fields, five times L2; profiles/k_sweep_plain_large_dram_1025.md),
-# scaled to a sweep by its node count; none measured for the anisotropic sweep.
-DRAM_BYTES_PER_POINT = {"plain_large": 315.4, "aniso": None}
+# cells (0.7 GB of fields, five times L2; profiles/k_sweep_plain_large_dram_1025.md,
+# profiles/k_sweep_spills_and_dram_1025.md), scaled to a sweep by its node count.
+DRAM_BYTES_PER_POINT = {"plain_large": 315.4, "aniso": 308.4}
 # FP64 work of k_marker_update per marker (inactive ones included), same convention:
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
@@ -514,6 +514,10 @@ def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, warm=False):
             calls[0] = st.phase_calls
 
         forms[f"one_batched_launch_{label}"] = timed(batched, args.steps)
+        # the same launch as a persistent grid: 3 resident CTAs per SM striding over the tiles
+        batch.set_grid(3 * torch.cuda.get_device_properties(dev).multi_processor_count)
+        forms[f"one_batched_launch_{label}_persistent_grid"] = timed(batched, args.steps)
+        batch.set_grid(0)
         batch.capture(nsw, amp=amp, seed=2026)
         stats = []
 
@@ -941,7 +945,7 @@ def main():
         fl = FP64_FLOPS_PER_POINT["aniso"] * a["nodes"] / (a["kernel_ms_per_sweep"] * 1e-3) / 1e12
         a["roofline"] = {"bound": "fp64", "achieved": fl, "peak": peak_fp64, "unit": "TFLOP/s",
                          "frac": fl / peak_fp64, "peak_source": "measured (DFMA probe)",
-                         "traffic": None,
+                         "traffic": DRAM_BYTES_PER_POINT["aniso"] * a["nodes"],
                          "hbm_achieved_gbs": a["algorithmic_bytes_per_sweep"] / (a["kernel_ms_per_sweep"] * 1e-3) / 1e9}
         m = configs["many_grids_64"]
         per_call = FP64_FLOPS_PER_PHASE_CALL["many_grids"]

@@ -532,6 +532,11 @@ int mdz_rheo_batch_sweep(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
 int mdz_rheo_batch_capture(mdz_rheo_batch *batch, int nsweeps, double amp, uint64_t seed);
 /* Launch the captured graph on the context's stream and wait for it. */
 int mdz_rheo_batch_launch(mdz_rheo_batch *batch, mdz_sweep_stats *stats);
+/* CTAs per batch launch: 0 (the default) one CTA per tile; ctas > 0 a persistent grid of
+ * min(ctas, tiles) CTAs that stride over the tiles (SMs x resident CTAs per SM, e.g.
+ * 3 x 152, keeps every CTA resident for the whole launch).  The results are the same bits
+ * either way.  Drops a captured graph: capture again before the next launch. */
+int mdz_rheo_batch_set_grid(mdz_rheo_batch *batch, int ctas);
 
 /* ---- launch-shape autotuner (no reference counterpart) -----------------
  * Times the sweep on the caller's own device-resident grid (MDZ_MEM_DEVICE fields;

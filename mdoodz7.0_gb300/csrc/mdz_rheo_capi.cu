@@ -1300,6 +1300,17 @@ int mdz_rheo_batch_capture(mdz_rheo_batch *b, int nsweeps, double amp, uint64_t 
   return MDZ_OK;
 }
 
+int mdz_rheo_batch_set_grid(mdz_rheo_batch *b, int ctas) {
+  if (!b || ctas < 0) return MDZ_EINVAL;
+  CK(cudaSetDevice(b->ctx->device));
+  CK(cudaStreamSynchronize(b->ctx->stream));
+  if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+  if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+  b->graph_sweeps = b->graph_launches = 0;
+  b->grid = (int)std::min<long long>(ctas > 0 ? (long long)ctas : b->tiles, 0x7fffffffLL);
+  return MDZ_OK;
+}
+
 int mdz_rheo_batch_launch(mdz_rheo_batch *b, mdz_sweep_stats *st) {
   if (!b) return MDZ_EINVAL;
   if (!b->exec) return MDZ_ENOTREADY;

@@ -413,6 +413,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_batch_sweep.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
     lib.mdz_rheo_batch_capture.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_uint64]
     lib.mdz_rheo_batch_launch.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
+    lib.mdz_rheo_batch_set_grid.argtypes = [C.c_void_p, C.c_int]
     lib.mdz_rheo_operators.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
                                        C.POINTER(OperatorFields), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.POINTER(SweepStats)]
@@ -564,6 +565,13 @@ class Batch:
         if check and rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_batch_launch")
         return rc, st
+
+    def set_grid(self, ctas: int):
+        """0: one CTA per tile (default); ctas > 0: a persistent grid of that many CTAs
+        striding over the tiles.  Drops a captured graph."""
+        rc = self.lib.mdz_rheo_batch_set_grid(self.handle, int(ctas))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_batch_set_grid")
 
     def close(self):
         if getattr(self, "handle", None):

@@ -122,6 +122,34 @@ def test_aniso_batch(ctx):
     b.close()
 
 
+@pytest.mark.parametrize("ctas", [1, 7, 456])
+def test_persistent_grid_gives_the_same_bits(ctx, ctas):
+    """A persistent grid (CTAs striding over the tiles) against one CTA per tile: the same
+    node body, so the same bits; a captured graph is dropped by the change."""
+    ws = small_batch(seed=12, n=5)
+    ref = [to_device(clone(w.arrays)) for w in ws]
+    b = R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in ref])
+    _, st_ref = b.sweep()
+    b.close()
+    devs = [to_device(clone(w.arrays)) for w in ws]
+    b = R.Batch(ctx, [w.model for w in ws], [w.mat for w in ws], [R.FieldSet(d) for d in devs])
+    b.capture(2)
+    b.set_grid(ctas)
+    rc, _ = b.launch(check=False)
+    assert rc == R.MDZ_ENOTREADY
+    rc, st = b.sweep()
+    assert rc == R.MDZ_OK and st.kernel_launches == 2
+    assert (st.phase_calls, st.newton_iters, st.plastic_calls) == (st_ref.phase_calls, st_ref.newton_iters,
+                                                                   st_ref.plastic_calls)
+    for d, r in zip(devs, ref):
+        a, o = to_host(d), to_host(r)
+        for k in R.CEN_OUT + R.VER_OUT:
+            if a.get(k) is not None:
+                assert np.array_equal(a[k], o[k], equal_nan=True), k
+    b.set_grid(0)
+    b.close()
+
+
 def expected_inputs(w, gi, nsw, amp, seed):
     """The host statement of `nsw` perturbations of grid gi's strain rates."""
     expect = clone(w.arrays)
