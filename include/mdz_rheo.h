@@ -630,6 +630,11 @@ int mdz_rheo_math_selftest(int device, const double *x, int64_t n, double *fast_
  * counterpart. */
 int mdz_rheo_div_selftest(int device, const double *a, int64_t n, double b, double *fast_out,
                           double *cuda_out);
+/* Self-check of the quotient the local solve uses for its outputs (1/eta, 2/Tii, the
+ * node's reciprocals): out[i] = r[i] / den[i] from two Newton steps on the hardware
+ * reciprocal estimate (within 2 ulp of the IEEE quotient; den outside [2^-1000, 2^1000]
+ * takes the IEEE division), for n host pairs.  No reference counterpart. */
+int mdz_rheo_quotient_selftest(int device, const double *r, const double *den, int64_t n, double *out);
 /* Self-check of the cell-index ceil used by mdz_rheo_marker_stress: ceil(q[i]) from the
  * bits of q (saturated to +-2^30 beyond that range and for NaN) and CUDA's ceil, for n
  * host arguments.  No reference counterpart. */

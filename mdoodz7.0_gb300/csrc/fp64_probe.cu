@@ -8,6 +8,8 @@
 // exp/log on the same arguments, for the accuracy tests.
 // mdz_rheo_div_selftest: the division by a known divisor of fp64_div.cuh next to CUDA's
 // division, for the bit-for-bit test.
+// mdz_rheo_quotient_selftest: the output quotient of fp64_div.cuh (two Newton steps on the
+// reciprocal estimate), for the accuracy test against IEEE division.
 // mdz_rheo_ceil_selftest: the integer-pipe ceil of fp64_bits.cuh next to CUDA's ceil.
 // mdz_rheo_dd_selftest: the double-float conversion, exp and log of dd_math.cuh, for the
 // accuracy tests.
@@ -53,6 +55,12 @@ __global__ void k_div(const double *a, long long n, mdz::Divisor d, double *fast
   plain[i] = a[i] / d.b;
 }
 
+__global__ void k_quotient(const double *r, const double *den, long long n, double *out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = mdz::quotient(r[i], den[i]);
+}
+
 __global__ void k_ceil(const double *q, long long n, int *fast, double *plain) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -91,6 +99,26 @@ extern "C" int mdz_rheo_dd_selftest(int device, const double *x, int64_t n, floa
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = MDZ_ECUDA;
   }
   if (rc == MDZ_OK && cudaMemcpy(out, dout, bo, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
+  cudaFree(d);
+  return rc;
+}
+
+extern "C" int mdz_rheo_quotient_selftest(int device, const double *r, const double *den, int64_t n,
+                                          double *out) {
+  if (!r || !den || n < 0 || !out) return MDZ_EINVAL;
+  if (n == 0) return MDZ_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return MDZ_ECUDA;
+  const size_t bytes = (size_t)n * sizeof(double);
+  double *d = nullptr;
+  if (cudaMalloc(&d, 3 * bytes) != cudaSuccess) return MDZ_ENOMEM;
+  int rc = MDZ_OK;
+  if (cudaMemcpy(d, r, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK && cudaMemcpy(d + n, den, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = MDZ_ECUDA;
+  if (rc == MDZ_OK) {
+    k_quotient<<<(unsigned)((n + 255) / 256), 256>>>(d, d + n, n, d + 2 * n);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = MDZ_ECUDA;
+  }
+  if (rc == MDZ_OK && cudaMemcpy(out, d + 2 * n, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = MDZ_ECUDA;
   cudaFree(d);
   return rc;
 }

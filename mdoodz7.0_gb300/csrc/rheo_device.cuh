@@ -133,7 +133,7 @@ __device__ __forceinline__ void node_common(const ModelConst &M, const NodeIn &i
   node_strain_update(c);
   c.Traw = in.T;
   c.T = fp64_lt(in.T, M.Tmin) ? M.Tmin : in.T;
-  c.invT = 1.0 / c.T;
+  c.invT = quotient(1.0, c.T);
   c.lnd = need_lnd ? fast_log(in.d) : 0.0;
   c.inv_d = 0.0;
   sincos(in.fric, &c.sin_fric, &c.cos_fric);
@@ -151,7 +151,7 @@ __device__ __forceinline__ void node_strain_iso(const ModelConst &M, const NodeI
 
 __device__ __forceinline__ void node_strain_update(NodeCtx &c) {
   c.lnEii = fast_log(c.Eii);
-  c.inv2Eii = 0.5 / c.Eii;
+  c.inv2Eii = quotient(0.5, c.Eii);
 }
 
 __device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn &in, bool need_lnd,
@@ -159,14 +159,14 @@ __device__ __forceinline__ void node_setup_iso(const ModelConst &M, const NodeIn
   node_strain_iso(M, in, c);
   c.elastic = (M.step == 0) ? 0 : M.elastic;
   c.plastic_on = (M.step != 0);
-  c.K = 1.0 / in.beta;
+  c.K = quotient(1.0, in.beta);
   c.G = in.G;
   c.dil = in.dil;
   if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; c.K = 1e10; }
   c.eta_el = c.G * M.dt;
-  c.inv_eta_el = 1.0 / c.eta_el;
+  c.inv_eta_el = quotient(1.0, c.eta_el);
   c.ln_eta_el = c.elastic ? fast_log(c.eta_el) : 0.0;
-  c.inv_Kdt = 1.0 / (c.K * M.dt);
+  c.inv_Kdt = quotient(1.0, c.K * M.dt);
   node_common(M, in, need_lnd, c);
 }
 
@@ -239,7 +239,7 @@ __device__ __forceinline__ void creep_laws(const ModelConst &M, const PhaseConst
     const double nE = L.ST + ph.exp_n;
     L.n[K_EXP] = nE;
     L.lnA_exp = ph.exp_lnA0 - ph.exp_EaR * ph.exp_om2 * c.invT;
-    L.ln_inv[K_EXP] = (kLn2 + ph.exp_ln_s3gS + lnEii) - (lnEii - L.lnA_exp) / nE;
+    L.ln_inv[K_EXP] = (kLn2 + ph.exp_ln_s3gS + lnEii) - quotient(lnEii - L.lnA_exp, nE);
   }
   if (fl & F_GBS) {
     double lnB = ph.gbs_lnK + (ph.gbs_Q + P * ph.gbs_V) * ph.gbs_invRn * c.invT - ph.gbs_an * phi;
@@ -880,7 +880,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
       double Tiic = 0.0;
       is_pl = 1;
       eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
-      gdot = F / (eta_ve + eta_vp + ksd);
+      gdot = quotient(F, eta_ve + eta_vp + ksd);
       const double F0 = F, tolF0 = tol * F0;
       // with n_vp == 1, eta_vp / n_vp is eta_vp exactly and the derivative is a constant
       const double dF1 = __dsub_rn(__dsub_rn(-eta_ve, eta_vp0), ksd);
@@ -937,14 +937,14 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
 
   double inv_eta_pl = 0.0;
   if (is_pl == 0) o.etaVE = eta_ve;
-  else if (plastic == 1) { o.etaVE = eta_vep; inv_eta_pl = gdot / Tii; }
+  else if (plastic == 1) { o.etaVE = eta_vep; inv_eta_pl = quotient(gdot, Tii); }
   else { o.etaVE = eta_vep; inv_eta_pl = 2.0 * lam_dot * A_tau / Tii; }
   o.is_pl = is_pl;
   if (is_pl) o.mech |= MDZ_MECH_YIELD;
   o.Eii_cst = e_cst; o.Eii_pwl = e_pwl; o.Eii_exp = e_exp; o.Eii_lin = e_lin;
   // the dissipative viscosity: 1 / eta = sum_k 2 Eii_k / Tii (+ 1/eta_cst, 1/eta_pl)
   const auto dissipative = [&](double &inv_half_T) {
-    inv_half_T = 2.0 / Tii_ve;  // 1/eta_k = 2 Eii_k / Tii
+    inv_half_T = quotient(2.0, Tii_ve);  // 1/eta_k = 2 Eii_k / Tii
     double inv = 0.0;
     if (peierls) inv = __fma_rn(e_exp, inv_half_T, inv);
     if (dislocation) inv = __fma_rn(e_pwl, inv_half_T, inv);
@@ -962,7 +962,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   double eta = 0.0;
   if (in.post_process == 2) {  // a vertex of the sweep: only etaVE, eta and X are kept
     double inv_half_T;
-    eta = 1.0 / dissipative(inv_half_T);
+    eta = quotient(1.0, dissipative(inv_half_T));
   } else {
     o.Txx = 2.0 * o.etaVE * in.Exx;
     o.Tzz = 2.0 * o.etaVE * in.Ezz;
@@ -970,7 +970,7 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     if (in.post_process == 1) {  // :986-1053
       double inv_half_T;
       const double inv = dissipative(inv_half_T);
-      eta = 1.0 / inv;
+      eta = quotient(1.0, inv);
       if (elastic) {
         const double h = 0.5 * c.inv_eta_el;
         const double Tyy = -(o.Txx + o.Tzz), Tyy0 = -(in.Txx0 + in.Tzz0);
@@ -1035,14 +1035,14 @@ __device__ __forceinline__ void node_setup_aniso(const ModelConst &M, const Node
   node_strain_aniso(in, c, a);
   c.elastic = (M.step == 0) ? 0 : M.elastic;
   c.plastic_on = 1;
-  c.K = 1.0 / in.beta;
+  c.K = quotient(1.0, in.beta);
   c.G = in.G;
   c.dil = in.dil;
   if (c.elastic == 0) { c.G = 1e1; c.dil = 0.0; }
   c.eta_el = c.elastic ? c.G * M.dt_model : 1e20;
-  c.inv_eta_el = 1.0 / c.eta_el;
+  c.inv_eta_el = quotient(1.0, c.eta_el);
   c.ln_eta_el = c.elastic ? fast_log(c.eta_el) : 0.0;
-  c.inv_Kdt = 1.0 / (c.K * M.dt_model);
+  c.inv_Kdt = quotient(1.0, c.K * M.dt_model);
   node_common(M, in, need_lnd, c);
   c.inv_d = 1.0 / in.d;
 }
@@ -1182,7 +1182,7 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
     is_pl = 1;
     // rounded one by one, as in the isotropic return
     const double Kdt_sd = __dmul_rn(__dmul_rn(K, dt), c.sin_dil);
-    gdot = Ft / __dadd_rn(__dadd_rn(eta_ve, ph.eta_vp), __dmul_rn(Kdt_sd, c.sin_fric));
+    gdot = quotient(Ft, __dadd_rn(__dadd_rn(eta_ve, ph.eta_vp), __dmul_rn(Kdt_sd, c.sin_fric)));
     const double Tiic = __dsub_rn(Tii, __dmul_rn(gdot, eta_ve));
     Pc = __dadd_rn(P, __dmul_rn(Kdt_sd, gdot));
     eta_vep = Tiic * c.inv2Eii;
@@ -1209,13 +1209,13 @@ __device__ inline void aniso_finish(const ModelConst &M, const PhaseConst &ph, c
   double eta = eta_vep;
   double inv = 0.0;
   if (in.post_process != 0) {  // :681-714 (eta_lin uses *d, the same d as the Newton: no correction)
-    const double inv_half_T = 2.0 / Tii_ve;
+    const double inv_half_T = quotient(2.0, Tii_ve);
     if (diffusion) inv += e_lin * inv_half_T;
     if (peierls) inv += e_exp * inv_half_T;
     if (dislocation) inv += e_pwl * inv_half_T;
     if (constant) inv += 1.0 / eta_cst;
-    if (is_pl) inv += gdot / Tii;
-    eta = 1.0 / inv;
+    if (is_pl) inv += quotient(gdot, Tii);
+    eta = quotient(1.0, inv);
   }
   if (in.post_process == 1) {
     if (elastic) o.Eii_el = Tii * Tii * (0.25 * c.inv_eta_el * c.inv_eta_el);

@@ -403,6 +403,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_div_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_ceil_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
     lib.mdz_rheo_dd_selftest.argtypes = [C.c_int, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.mdz_rheo_quotient_selftest.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     lib.mdz_rheo_points_static.argtypes = [C.POINTER(Model), C.POINTER(Materials), C.POINTER(PointInputs),
                                            C.POINTER(PointOutputs), C.c_int64, C.c_int, C.c_int, C.c_void_p,
                                            C.POINTER(SweepStats)]
@@ -500,6 +501,19 @@ def div_selftest(a: np.ndarray, b: float, device: int = 0):
     if rc != MDZ_OK:
         raise RheoError(rc, "mdz_rheo_div_selftest")
     return fast, plain
+
+
+def quotient_selftest(r: np.ndarray, den: np.ndarray, device: int = 0):
+    """r / den by the local solve's output quotient (two Newton steps on the reciprocal
+    estimate) on the GPU, for float64 arrays of one shape."""
+    r = np.ascontiguousarray(r, np.float64)
+    den = np.ascontiguousarray(den, np.float64)
+    assert r.shape == den.shape
+    out = np.empty_like(r)
+    rc = load_library().mdz_rheo_quotient_selftest(device, r.ctypes.data, den.ctypes.data, r.size, out.ctypes.data)
+    if rc != MDZ_OK:
+        raise RheoError(rc, "mdz_rheo_quotient_selftest")
+    return out
 
 
 def ceil_selftest(q: np.ndarray, device: int = 0):

@@ -106,3 +106,34 @@ def test_integer_pipe_ceil_matches_cuda():
     big = ~small & ~np.isnan(q)
     assert np.array_equal(fast[big], np.where(q[big] < 0, -(2 ** 30), 2 ** 30))
     assert (fast[np.isnan(q)] == 2 ** 30).all()
+
+
+def test_output_quotient_within_two_ulp():
+    """The quotient of the local solve's outputs (csrc/fp64_div.cuh `quotient`: two Newton
+    steps on the hardware reciprocal estimate, then one product) against IEEE division:
+    within 2 ulp of the correctly rounded quotient for operands of every scale and sign,
+    and equal to it where the divisor lies outside [2^-1000, 2^1000] (zero, subnormal,
+    huge, Inf, NaN: the IEEE division itself)."""
+    rng = np.random.default_rng(17)
+    n = 2_000_000
+    r = rng.standard_normal(n) * 10.0 ** rng.uniform(-150, 150, n)
+    den = rng.standard_normal(n) * 10.0 ** rng.uniform(-290, 290, n)
+    # mantissas near 1 and near 2, and exact powers of two
+    den[:1000] = 2.0 ** rng.integers(-900, 900, 1000)
+    den[1000:2000] = np.nextafter(2.0, 0.0) * 2.0 ** rng.integers(-900, 900, 1000)
+    den[2000:3000] = np.nextafter(1.0, 2.0) * 2.0 ** rng.integers(-900, 900, 1000)
+    r[:3000] = 1.0
+    with np.errstate(all="ignore"):
+        exact = r / den
+    got = R.quotient_selftest(r, den)
+    ok = np.isfinite(exact) & (exact != 0) & (np.abs(exact) > 1e-290) & (np.abs(exact) < 1e290)
+    ulps = np.abs(got[ok] - exact[ok]) / np.spacing(np.abs(exact[ok]))
+    print("output quotient: worst", float(ulps.max()), "ulp; mean", float(ulps.mean()))
+    assert ulps.max() <= 2.0
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 2.0 ** -1001, 2.0 ** 1001, 1.7976931348623157e308,
+                        np.inf, -np.inf, np.nan])
+    rs = np.full(special.size, 3.0)
+    with np.errstate(all="ignore"):
+        want = rs / special
+    got = R.quotient_selftest(rs, special)
+    assert np.array_equal(got, want, equal_nan=True)
