@@ -544,7 +544,7 @@ int mdz_rheo_batch_set_grid(mdz_rheo_batch *batch, int ctas);
  * context of the same kind: anisotropic or not, phase count, start (MDZ_SWEEP_REF_START or
  * not) and, among tuned sizes, the nearest node count (a cache keyed by those; other
  * sweeps use the last shape tuned for their kind, aniso 0/1).  Candidates, in this order:
- *   0-4   128 threads per block, 3 CTAs per SM (168 registers): one thread per node, then a
+ *   0-4   128 threads per block, 4 CTAs per SM (128 registers): one thread per node, then a
  *         grid-stride loop over 1, 2, 4 or 8 waves of the resident CTAs;
  *   5-9   the same with 64 threads per block;
  *   10    128 threads per block, one thread per node, 2 CTAs per SM (255 registers, no
@@ -561,7 +561,7 @@ int mdz_rheo_batch_set_grid(mdz_rheo_batch *batch, int ctas);
 int mdz_rheo_autotune(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                       const mdz_grid_fields *f, int aniso, int flags, int reps, double *ms_out,
                       int *best_out);
-/* The kernel form of that shape: 0 one thread per node or grid-stride (168 registers),
+/* The kernel form of that shape: 0 one thread per node or grid-stride (128 registers),
  * 1 the 255-register form, 2 the persistent work-counter form. */
 int mdz_rheo_get_launch_form(mdz_rheo_ctx *ctx, int aniso, int *form);
 /* Set the shape of sweeps of this kind by hand (block 64 or 128, grid cap as above, form

@@ -321,13 +321,16 @@ __device__ __forceinline__ void sweep_node(const SweepArgs &A, long long i, Acc 
 
 // One sweep is two launches: the centroids (NODES 1), then the vertices (NODES 2), each
 // over its whole range or over the band of rows a banded sweep gives it.
-// Three CTAs of 128 per SM (168 registers, and a few hundred bytes of spills: 336 B for the
-// vertex kernel, 532 B for the centroid kernel).  Twelve warps per SM hide more of the FP64
-// pipe's latency than the spills cost: at 2049 x 2049 cells the default-start sweep takes
-// 22.47 ms against 23.12 ms with two CTAs per SM and no spills.
-// MINB: CTAs of 128 per SM the register allocation is capped for (3: 168 registers, with
-// spills; 2: 255 registers); the autotuner times both.
-template <bool ANISO, int NODES, int MINB = 3>
+// Four CTAs of 128 per SM (128 registers, with spills: about 0.7 kB per vertex thread and
+// 0.9 kB per centroid thread, which stay in L1 and L2).  Sixteen warps per SM hide more of
+// the FP64 pipe's latency than the spills cost: at 2049 x 2049 cells the default-start
+// sweep takes 19.1 ms against 19.5 ms at three CTAs per SM (168 registers) and 20.6 ms at
+// two (255 registers, no spills); five CTAs gain another 0.4 % there but lose 1.6 % on the
+// many-grid batch.
+// MINB: CTAs of 128 per SM the register allocation is capped for (4: 128 registers; 2: 255
+// registers, which wins where local solves take many Newton evaluations); the autotuner
+// times both.
+template <bool ANISO, int NODES, int MINB = 4>
 __global__ void __launch_bounds__(128, MINB) k_sweep(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0, 0};
   const long long total = NODES == 1 ? (A.ranged ? A.c_n : A.M.Nc) : (A.ranged ? A.v_n : A.M.Nv);
@@ -345,7 +348,7 @@ __global__ void __launch_bounds__(128, MINB) k_sweep(const __grid_constant__ Swe
 // the chunk start is broadcast by shuffle, and the lanes past the end are retired by a
 // ballot.  The node body is the plain sweep's, so the results are the same bits.
 template <bool ANISO, int NODES>
-__global__ void __launch_bounds__(128, 3) k_sweep_queue(const __grid_constant__ SweepArgs A) {
+__global__ void __launch_bounds__(128, 4) k_sweep_queue(const __grid_constant__ SweepArgs A) {
   Acc acc = {0, 0, 0, 0, 0};
   const long long total = NODES == 1 ? A.M.Nc : A.M.Nv;
   const long long lo = NODES == 1 ? 0 : A.M.Nc;
@@ -421,7 +424,7 @@ __device__ __forceinline__ void warm_node(const SweepArgs &A, MlpWarpShared &S, 
 // same number of node iterations and reaches the network at the same phase; lanes past
 // the end or at inactive (node, phase) items feed zeros and discard the output.
 template <bool ANISO, int NODES>
-__global__ void __launch_bounds__(128, 3) k_sweep_warm(const __grid_constant__ SweepArgs A,
+__global__ void __launch_bounds__(128, 4) k_sweep_warm(const __grid_constant__ SweepArgs A,
                                                     const __grid_constant__ MlpDevice W) {
   extern __shared__ __align__(16) unsigned char smem_warm[];
   MlpWarpShared &S = *reinterpret_cast<MlpWarpShared *>(smem_warm);
@@ -461,7 +464,7 @@ __device__ __forceinline__ int batch_grid_of(const long long *tile_start, int n,
 // multiplied by the sweep's perturbation factors as they are loaded, in place (the
 // captured multi-sweep graph), instead of by a separate pass over them.
 template <bool ANISO, int NODES, bool WARM, bool PERTURB>
-__global__ void __launch_bounds__(kBatchTile, 3) k_sweep_batch(const __grid_constant__ BatchArgs B,
+__global__ void __launch_bounds__(kBatchTile, 4) k_sweep_batch(const __grid_constant__ BatchArgs B,
                                                              const __grid_constant__ BatchSweepArgs X) {
   extern __shared__ __align__(16) unsigned char smem_batch[];
   MlpWarpShared &S = *reinterpret_cast<MlpWarpShared *>(smem_batch);
@@ -627,7 +630,7 @@ static void launch_kind(const SweepArgs &a, const LaunchShape &sh, long long cou
   long long grid = (count + sh.block - 1) / sh.block;
   if (sh.grid_cap > 0 && grid > sh.grid_cap) grid = sh.grid_cap;
   if (sh.form == SHAPE_REGS255) k_sweep<ANISO, NODES, 2><<<(unsigned)grid, sh.block, 0, s>>>(a);
-  else k_sweep<ANISO, NODES, 3><<<(unsigned)grid, sh.block, 0, s>>>(a);
+  else k_sweep<ANISO, NODES, 4><<<(unsigned)grid, sh.block, 0, s>>>(a);
 }
 
 cudaError_t launch_sweep(const SweepArgs &a, bool aniso, cudaStream_t s, const LaunchShape &shape) {
@@ -769,7 +772,7 @@ cudaError_t launch_points(const PointArgs &a, cudaStream_t s) {
 void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, int block, int form) {
   cudaFuncAttributes fa;
   // the centroid kernel: the larger of the two, it sets the launch shape
-  const void *fn = aniso ? (const void *)k_sweep<true, 1, 3> : (const void *)k_sweep<false, 1, 3>;
+  const void *fn = aniso ? (const void *)k_sweep<true, 1, 4> : (const void *)k_sweep<false, 1, 4>;
   if (form == SHAPE_REGS255) fn = aniso ? (const void *)k_sweep<true, 1, 2> : (const void *)k_sweep<false, 1, 2>;
   if (form == SHAPE_QUEUE) fn = aniso ? (const void *)k_sweep_queue<true, 1> : (const void *)k_sweep_queue<false, 1>;
   cudaFuncGetAttributes(&fa, fn);
