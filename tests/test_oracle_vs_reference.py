@@ -20,6 +20,13 @@ GRIDS = {
     "plain_large_geometric": (lambda: W.plain_large(seed=4, ncx=50, ncz=30, eta_average=2), False, 0),
     "aniso_64": (lambda: W.aniso(seed=5, ncx=64), True, 0),
     "aniso_typical": (lambda: W.aniso(seed=6, ncx=40, sc=W.TYPICAL), True, 1),
+    # edges: one cell, one column, one row, ragged, one phase
+    "one_cell": (lambda: W.plain_large(seed=21, ncx=1, ncz=1), False, 0),
+    "one_column": (lambda: W.plain_large(seed=22, ncx=1, ncz=9), False, 0),
+    "one_row": (lambda: W.plain_large(seed=23, ncx=9, ncz=1), False, 0),
+    "ragged_3x300": (lambda: W.plain_large(seed=24, ncx=3, ncz=300), False, 0),
+    "one_phase": (lambda: W.plain_large(seed=25, ncx=12, ncz=10, nphases=1), False, 0),
+    "aniso_one_row": (lambda: W.aniso(seed=26, ncx=7, ncz=1), True, 0),
 }
 
 
