@@ -60,9 +60,9 @@ FP64_FLOPS_PER_POINT = {"plain_large": 1560.2, "aniso": 1094.8}
 # have 2 to 5 phases, so the work is counted per phase call.
 FP64_FLOPS_PER_PHASE_CALL = {"many_grids": 312.0}
 # DRAM bytes (read + write) per point-update of one sweep's two launches at 1025 x 1025
-# cells (0.7 GB of fields, five times L2; profiles/k_sweep_plain_large_dram_1025.md,
-# profiles/k_sweep_spills_and_dram_1025.md), scaled to a sweep by its node count.
-DRAM_BYTES_PER_POINT = {"plain_large": 315.4, "aniso": 308.4}
+# cells (0.7 GB of fields, five times L2; profiles/k_sweep_spills_and_dram_1025.md, the
+# 4-CTA kernels whose spills reach DRAM in part), scaled to a sweep by its node count.
+DRAM_BYTES_PER_POINT = {"plain_large": 381.0, "aniso": 364.2}
 # FP64 work of k_marker_update per marker (inactive ones included), same convention:
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).

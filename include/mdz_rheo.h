@@ -484,11 +484,13 @@ int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_marke
  *   output), n * element size rounded up to 256; for MDZ_MEM_DEVICE only the 256.
  *   strain_acc, div and angle are not read and not staged.
  * A request above the array returns MDZ_ESCRATCH before anything is enqueued (about
- * 10,000 points with every input and output present, host memory).
+ * 12,000 isotropic or 11,000 anisotropic points with every input and output present,
+ * host memory).
  * Nothing in the array has to start at zero: the call itself resets the statistics
  * block (counters 0, error key all ones) on `stream` before its kernel.  Stream 0 / NULL
  * is the legacy default stream.  The call is blocking: it returns after `stream` has
- * drained, with outputs (and `stats`, may be NULL) in place.  Two calls that overlapped
+ * drained, with outputs (and `stats`, may be NULL) in place, so it cannot be recorded
+ * into a CUDA graph.  Two calls that overlapped
  * on one device would race on the one array; calls are therefore serialised per
  * process by a lock held until the stream has drained.
  * The first call on each device looks up the array's address with

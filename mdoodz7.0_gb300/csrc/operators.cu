@@ -97,8 +97,12 @@ __device__ __forceinline__ void fd_derivatives(const OpArgs &A, const OpNode &nd
     for (int k = 0; k < 4; k++) d[k] *= nd.eta;
 }
 
+// Registers capped for 4 CTAs of 128 per SM (3 for the anisotropic form): the extra
+// resident warps hide more of the FP64 pipe's latency than the spills cost.  At 2049 x
+// 2049 cells the Newton operator took 131.4 ms uncapped (232 registers, 2 CTAs per SM),
+// 123.7 ms at 3 and 120.4 ms at 4 CTAs per SM; the anisotropic one 73.5, 65.3 and 66.6 ms.
 template <bool ANISO, bool JAC>
-__global__ void __launch_bounds__(128) k_operators(const __grid_constant__ OpArgs A) {
+__global__ void __launch_bounds__(128, ANISO ? 3 : 4) k_operators(const __grid_constant__ OpArgs A) {
   const ModelConst &M = A.M;
   const long long total = M.Nc + M.Nv;
   unsigned long long calls = 0;
