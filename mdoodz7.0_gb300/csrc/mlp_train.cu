@@ -60,23 +60,33 @@ __device__ __forceinline__ void sync_mma() {
   umma::fence_after_sync();
 }
 
-// D[tcol] = A * B^T, A = M x K tile, B = N x K tile (both K-major), then wait.
-__device__ __forceinline__ void gemm(TrainShared &S, int M, int N, int K, uint32_t tcol, const unsigned char *At,
-                                     const unsigned char *Bt, uint32_t &phase) {
+// Issue D[tcol] = A * B^T, A = M x K tile, B = N x K tile (both K-major), from thread 0.
+__device__ __forceinline__ void issue(TrainShared &S, int M, int N, int K, uint32_t tcol, const unsigned char *At,
+                                      const unsigned char *Bt) {
   if (threadIdx.x == 0 && !S.fault) {
     const uint32_t idesc = umma::idesc_bf16_f32(M, N);
     const uint32_t a0 = umma::smem_u32(At), b0 = umma::smem_u32(Bt);
     for (int kk = 0; kk < K / 16; kk++)
       umma::mma_bf16(S.tmem + tcol, umma::smem_desc(a0 + kk * 256, 128, 16 * K),
                      umma::smem_desc(b0 + kk * 256, 128, 16 * K), idesc, kk > 0);
-    umma::commit(&S.mbar);
   }
+}
+
+// One commit for every MMA issued since the last, then the CTA waits for them.
+__device__ __forceinline__ void complete(TrainShared &S, uint32_t &phase) {
+  if (threadIdx.x == 0 && !S.fault) umma::commit(&S.mbar);
   if (!S.fault && !umma::mbar_wait(&S.mbar, phase)) {  // every writer stores the same values
     S.fault_parity = phase;
     S.fault = 1;
   }
   phase ^= 1;
   umma::fence_after_sync();
+}
+
+__device__ __forceinline__ void gemm(TrainShared &S, int M, int N, int K, uint32_t tcol, const unsigned char *At,
+                                     const unsigned char *Bt, uint32_t &phase) {
+  issue(S, M, N, K, tcol, At, Bt);
+  complete(S, phase);
 }
 
 __device__ __forceinline__ void put_bf16(unsigned char *tile, int r, int k, int K, float v) {
@@ -187,8 +197,11 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
     if (t < 2) atomicAdd(&W.gb3[t], gb);
   }
   sync_mma();
-  // ---- backward through layer 3: dH2 = dY W3, dZ2 = dH2 * (A2 > 0)
-  gemm(S, T, kMlpHid, kMlpOut, C_DH2, S.dY, S.W3t, phase);
+  // ---- backward through layer 3: dH2 = dY W3, dZ2 = dH2 * (A2 > 0); with it, in the same
+  // commit group, layer 3's weight gradient (its operands are ready: A2 and dY)
+  issue(S, T, kMlpHid, kMlpOut, C_DH2, S.dY, S.W3t);
+  issue(S, 64, kMlpOut, T, C_GW3, S.A2t, S.dYt);   // gW3^T[h][o]
+  complete(S, phase);
   float gsum[kMlpHid];
   for (int c = 0; c < kMlpHid; c += 16) {
     float v[16];
@@ -209,8 +222,11 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
     if (t < kMlpHid) atomicAdd(&W.gb2[t], gb);
   }
   sync_mma();
-  // ---- backward through layer 2: dH1 = dZ2 W2, dZ1 = dH1 * (A1 > 0)
-  gemm(S, T, kMlpHid, kMlpHid, C_DH1, S.dZ2, S.W2t, phase);
+  // ---- backward through layer 2: dH1 = dZ2 W2, dZ1 = dH1 * (A1 > 0); with it layer 2's
+  // weight gradient (dZ2 and A1 are ready)
+  issue(S, T, kMlpHid, kMlpHid, C_DH1, S.dZ2, S.W2t);
+  issue(S, 64, kMlpHid, T, C_GW2, S.dZ2t, S.A1t);  // gW2[o][i]
+  complete(S, phase);
   for (int c = 0; c < kMlpHid; c += 16) {
     float v[16];
     umma::tmem_ld16(umma::tmem_addr(S.tmem, w, C_DH1 + c), v);
@@ -228,9 +244,9 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
     if (t < kMlpHid) atomicAdd(&W.gb1[t], gb);
   }
   sync_mma();
-  // ---- weight gradients, reduction over the 128 samples (M = 64 tiles, K = samples)
-  gemm(S, 64, kMlpOut, T, C_GW3, S.A2t, S.dYt, phase);   // gW3^T[h][o]
-  gemm(S, 64, kMlpHid, T, C_GW2, S.dZ2t, S.A1t, phase);  // gW2[o][i]
+  // ---- weight gradients, reduction over the 128 samples (M = 64 tiles, K = samples);
+  // layers 3 and 2 were issued with the backward GEMMs above, in the TMEM columns that
+  // no later GEMM writes
   gemm(S, 64, kMlpIn, T, C_GW1, S.dZ1t, S.Xt, phase);    // gW1[h][f]
   const int row = m64_row_of_thread(t);
   {

@@ -6,14 +6,16 @@
 // thread per node over the index space [centroids | vertices], launched once over the
 // centroids (NODES 1) and once over the vertices (NODES 2) so that each kernel carries only
 // its own kind's work (vertices skip the per-phase outputs only centroids keep), per-phase
-// tables in the
-// kernel's constant parameter bank (uniform across a warp, so every lookup is a
-// broadcast), SoA loads and stores coalesced along the node index.
+// tables in the kernel's constant parameter bank (uniform across a warp, so every lookup
+// is a broadcast), SoA loads and stores coalesced along the node index.  k_sweep_queue is
+// the same sweep as a persistent grid on a work counter; k_sweep_warm puts the learned
+// warm start (evaluated per warp on the tensor cores) before each local solve;
+// k_sweep_batch sweeps many grids in one launch per kind of node.
 //
 // k_sweep_tiles<ANISO, MODE, NODES> walks the same index space in tiles of 128 nodes, one tile
 // per CTA at a time, with the phase loop uniform over the CTA so that a block-wide stage
 // can sit between each phase's set-up and its local solve: the learned warm start
-// (MODE_WARM: tcgen05 MLP guess, then the FP32 polish) or the training-data dump
+// (MODE_WARM: the tcgen05 network's guess, then the start stages) or the training-data dump
 // (MODE_COLLECT, from the reference's own start).
 #include <cuda_runtime.h>
 
