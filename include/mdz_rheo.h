@@ -552,19 +552,24 @@ int mdz_rheo_batch_set_grid(mdz_rheo_batch *batch, int ctas);
  *   10    128 threads per block, one thread per node, 2 CTAs per SM (255 registers, no
  *         spills);
  *   11    persistent: one wave of resident CTAs whose warps pull 32-node chunks from a
- *         work counter (one atomic per chunk, lanes past the end retired by a ballot).
+ *         work counter (one atomic per chunk, lanes past the end retired by a ballot);
+ *   12    compacting (isotropic): the CTA's threads walk their nodes' phases in step and,
+ *         after each phase's visco-elastic solve, run the Drucker-Prager returns of the
+ *         yielding items packed into the first threads (gathered by ballot into shared
+ *         memory); the anisotropic sweep runs this candidate as one thread per node.
  * Each candidate runs one warm-up and `reps` timed sweeps; ms_out (may be NULL) receives
  * MDZ_AUTOTUNE_CANDIDATES mean kernel times and best_out (may be NULL) the chosen index.
  * No candidate changes a result bit: every node is computed by the same code, by one
  * thread, independently of the others.  `flags` may hold MDZ_SWEEP_REF_START only.  The
  * tuned sweeps overwrite the grid's outputs with the values one sweep produces.  Banded
  * host-memory sweeps take the persistent candidate's block size as one thread per node. */
-#define MDZ_AUTOTUNE_CANDIDATES 12
+#define MDZ_AUTOTUNE_CANDIDATES 13
 int mdz_rheo_autotune(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                       const mdz_grid_fields *f, int aniso, int flags, int reps, double *ms_out,
                       int *best_out);
 /* The kernel form of that shape: 0 one thread per node or grid-stride (128 registers),
- * 1 the 255-register form, 2 the persistent work-counter form. */
+ * 1 the 255-register form, 2 the persistent work-counter form, 3 the compacting form
+ * (isotropic, block 128). */
 int mdz_rheo_get_launch_form(mdz_rheo_ctx *ctx, int aniso, int *form);
 /* Set the shape of sweeps of this kind by hand (block 64 or 128, grid cap as above, form
  * 0/1/2; form 2 with grid_cap 0 takes one wave of resident CTAs), dropping the tuned

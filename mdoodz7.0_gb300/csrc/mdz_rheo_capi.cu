@@ -41,7 +41,8 @@ struct mdz_rheo_ctx {
   int last_np = 0, have_iters = 0, pending = 0;
   unsigned long long h2d = 0, d2h = 0;
   unsigned launches = 0;
-  LaunchShape shape[2] = {{128, 0, SHAPE_THREAD}, {128, 0, SHAPE_THREAD}};  // untuned shape, [iso, aniso]
+  // untuned shape, [iso, aniso]: the isotropic sweep compacts its plastic returns per CTA
+  LaunchShape shape[2] = {{128, 0, SHAPE_COMPACT}, {128, 0, SHAPE_THREAD}};
   // shapes the autotuner chose, keyed by (anisotropic, phases, reference start, nodes); a
   // sweep takes the entry of its key with the nearest node count, else shape[aniso]
   struct Tuned {
@@ -1345,7 +1346,10 @@ int mdz_rheo_autotune(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials 
     sweep_kernel_info(a, &regs, &smem, &occ, 128, SHAPE_QUEUE);
     cand.push_back({128, c->sms * (occ > 0 ? occ : 1), SHAPE_QUEUE});
   }
-  static_assert(MDZ_AUTOTUNE_CANDIDATES == 12, "candidate list");
+  // the compacting form; the anisotropic sweep, which has no iterated plastic return, runs
+  // it as one thread per node
+  cand.push_back({128, 0, aniso ? SHAPE_THREAD : SHAPE_COMPACT});
+  static_assert(MDZ_AUTOTUNE_CANDIDATES == 13, "candidate list");
   const LaunchShape keep = c->shape[a];
   const auto keep_tuned = c->tuned;
   c->tuned.clear();  // every candidate below runs as the context's shape
@@ -1383,7 +1387,9 @@ int mdz_rheo_autotune(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials 
 
 int mdz_rheo_set_launch_shape(mdz_rheo_ctx *c, int aniso, int block, int grid_cap, int form) {
   if (!c || (block != 64 && block != 128) || grid_cap < 0) return MDZ_EINVAL;
-  if (form != SHAPE_THREAD && form != SHAPE_REGS255 && form != SHAPE_QUEUE) return MDZ_EINVAL;
+  if (form != SHAPE_THREAD && form != SHAPE_REGS255 && form != SHAPE_QUEUE && form != SHAPE_COMPACT)
+    return MDZ_EINVAL;
+  if (form == SHAPE_COMPACT && (aniso || block != 128)) return MDZ_EINVAL;
   if (form == SHAPE_QUEUE && grid_cap == 0) {  // one wave of resident CTAs
     int occ = 0, regs = 0, smem = 0;
     CK(cudaSetDevice(c->device));

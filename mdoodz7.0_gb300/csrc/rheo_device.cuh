@@ -812,24 +812,108 @@ __device__ inline void iso_setup(const ModelConst &M, const PhaseConst &ph, cons
   S.eta_cst = eta_cst; S.Tyield = Tyield; S.C = C; S.Ag = Ag; S.lnd = lnd;
 }
 
+// The state of one (node, phase) between its visco-elastic solve and its post-processing.
+struct IsoMid {
+  double eta_ve, Tii, Tii_ve, Tyield, e_cst, e_pwl, e_exp, e_lin;
+  double gdot, divp, Pc, eta_vep, lam_dot, A_tau, A_P, eta_vp;
+  int is_pl;
+};
+
+// Inputs and results of the Drucker-Prager return of one (node, phase) (plastic == 1,
+// RheologyDensity.c:655-707).  It depends only on these and on the phase's constants, so a
+// CTA can run the returns of all its yielding items together, one per thread
+// (k_sweep_compact), with the bits of the inline return.
+struct DpItem {
+  double Tii, Tyield, eta_ve, P, K, sin_fric, sin_dil, Eii, inv2Eii;  // in; Tii, Tyield out
+  double gdot, divp, Pc, eta_vp, eta_vep;                              // out
+};
+
+__device__ __forceinline__ bool iso_yields_dp(const ModelConst &M, const PhaseConst &ph, const NodeCtx &c,
+                                              const IsoMid &m) {
+  const int plastic = c.plastic_on ? ((ph.flags & F_PL1) ? 1 : ((ph.flags & F_PL2) ? 2 : 0)) : 0;
+  return plastic == 1 && fp64_gt(m.Tii - m.Tyield, 1e-17);
+}
+
+__device__ __forceinline__ void dp_load(DpItem &d, const IsoMid &m, const NodeIn &in, const NodeCtx &c) {
+  d.Tii = m.Tii; d.Tyield = m.Tyield; d.eta_ve = m.eta_ve; d.P = in.P; d.K = c.K;
+  d.sin_fric = c.sin_fric; d.sin_dil = c.sin_dil; d.Eii = c.Eii; d.inv2Eii = c.inv2Eii;
+}
+
+__device__ __forceinline__ void dp_store(IsoMid &m, const DpItem &d) {
+  m.is_pl = 1;
+  m.Tii = d.Tii; m.Tyield = d.Tyield; m.gdot = d.gdot; m.divp = d.divp; m.Pc = d.Pc; m.eta_vp = d.eta_vp;
+  m.eta_vep = d.eta_vep;
+}
+
+// The Drucker-Prager return (:655-707) of an item that yields (Tii - Tyield > 1e-17).
+__device__ inline void dp_return(const ModelConst &M, const PhaseConst &ph, DpItem &d) {
+  const int fl = ph.flags;
+  const double Tii = d.Tii, eta_ve = d.eta_ve, P = d.P, dt = M.dt;
+  double Tyield = d.Tyield;
+  double F = Tii - Tyield;
+  const double tol = M.eta_tol, eta_vp0 = ph.eta_vp, n_vp = ph.n_vp;
+  const bool vp1 = (fl & F_VP1) != 0;
+  // The products and sums of this return are rounded one by one (explicit intrinsics, which
+  // the compiler never fuses), as the reference's unfused arithmetic does: left to the
+  // compiler, whether a product fused into the following sum depended on the kernel the
+  // function was inlined into, and the iteration magnified that last bit.
+  const double Kdt = __dmul_rn(d.K, dt);
+  const double ksd = __dmul_rn(__dmul_rn(Kdt, d.sin_fric), d.sin_dil);
+  double Tiic = 0.0, divp = 0.0, Pc = P;
+  double eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(d.Eii, 1.0 / n_vp - 1);
+  double gdot = quotient(F, eta_ve + eta_vp + ksd);
+  const double F0 = F, tolF0 = tol * F0;
+  // with n_vp == 1, eta_vp / n_vp is eta_vp exactly and the derivative is a constant
+  const double dF1 = __dsub_rn(__dsub_rn(-eta_ve, eta_vp0), ksd);
+  // The return is a fixed map of the state (gdot, Tyield) entering each iteration.  When
+  // the state that the update produces equals one already entered -- the previous
+  // iteration's (the Newton step rounds away) or the one before (two states alternate
+  // in the last bit) -- every later iteration repeats one already done, and the values
+  // the loop ends with at its cap of 20 are known now: stop there instead of running
+  // the repeats.  The results are those of the full loop, bit for bit.
+  unsigned long long g1 = ~0ull, y1 = ~0ull;  // state entering the previous iteration
+  int last = 19;
+  for (int it = 0; it <= last; it++) {
+    const unsigned long long g0 = fp64_bits(gdot), y0 = fp64_bits(Tyield);
+    divp = __dmul_rn(gdot, d.sin_dil);
+    Pc = __dadd_rn(P, __dmul_rn(Kdt, divp));
+    eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+    Tyield = __dadd_rn(Tyield, __dmul_rn(gdot, eta_vp));
+    Tiic = __dsub_rn(Tii, __dmul_rn(eta_ve, gdot));
+    F = Tiic - Tyield;
+    if (fp64_abs_lt(F, tol) || fp64_abs_lt(F, tolF0)) break;
+    gdot -= F / (vp1 ? dF1 : (-eta_ve - eta_vp / n_vp - ksd));
+    if (it == last) break;
+    const unsigned long long gn = fp64_bits(gdot), yn = fp64_bits(Tyield);
+    if (gn == g0 && yn == y0) break;  // period 1: iteration 19 would be this one
+    if (gn == g1 && yn == y1) {       // period 2: iteration 19 repeats this one or the next
+      if (((19 - it) & 1) == 0) break;
+      last = it + 1;
+    }
+    g1 = g0; y1 = y0;
+  }
+  if (fp64_lt(Tiic, 0.0)) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }  // :697-704
+  d.gdot = gdot; d.divp = divp; d.Pc = Pc; d.eta_vp = eta_vp; d.Tyield = Tyield;
+  d.eta_vep = Tiic * d.inv2Eii;
+  d.Tii = Tiic;
+}
+
 // Local solve (from s_start * eta_up, moved by the start stages that the descriptor
-// `polish` names (ve_start); s_start = 1 and polish = 0 is the reference's start), plastic corrections and post-processing of
-// one (node, phase).  eta_conv (may be null) receives the converged visco-elastic
-// viscosity, before plasticity.
-__device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
-                                  IsoState &S, float s_start, int polish, PointOut &o,
-                                  double *eta_conv = nullptr) {
+// `polish` names (ve_start); s_start = 1 and polish = 0 is the reference's start) of one
+// (node, phase), up to its plastic corrections.  eta_conv (may be null) receives the
+// converged visco-elastic viscosity, before plasticity.
+__device__ inline void iso_ve(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                              IsoState &S, float s_start, int polish, PointOut &o, IsoMid &m,
+                              double *eta_conv = nullptr) {
   const int fl = ph.flags;
   const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
   const int gbs = (fl & F_GBS) != 0, gs = (fl & F_GS) != 0;
   const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
-  const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
   const int elastic = c.elastic;
-  const double T = c.T, P = in.P, Eii = c.Eii, eta_el = c.eta_el, K = c.K, dt = M.dt;
+  const double P = in.P, Eii = c.Eii, eta_el = c.eta_el;
   Laws &L = S.L;
-  const double eta_up = S.eta_up, eta_cst = S.eta_cst, C = S.C, Ag = S.Ag, lnd = S.lnd;
-  double Tyield = S.Tyield;
-  (void)T;
+  const double eta_up = S.eta_up, eta_cst = S.eta_cst, Ag = S.Ag;
+  const double Tyield = S.Tyield;
   double eta_ve, Tii, e_cst, e_pwl, e_exp, e_lin;
   if (!gs) {  // LocalIterationViscoElastic (:646)
     VeCoef q;
@@ -860,63 +944,34 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
     o.d1 = dd;
     o.inv_d1 = 1.0 / dd;
   }
-  const double Tii_ve = Tii;
   if (eta_conv) *eta_conv = eta_ve;
+  m.eta_ve = eta_ve; m.Tii = Tii; m.Tii_ve = Tii; m.Tyield = Tyield;
+  m.e_cst = e_cst; m.e_pwl = e_pwl; m.e_exp = e_exp; m.e_lin = e_lin;
+  m.gdot = 0.0; m.divp = 0.0; m.Pc = P; m.eta_vep = 0.0; m.lam_dot = 0.0; m.A_tau = 1.0; m.A_P = 0.0;
+  m.eta_vp = ph.eta_vp;
+  m.is_pl = 0;
+}
 
-  // plastic corrections (:655-930)
-  int is_pl = 0;
-  double gdot = 0.0, divp = 0.0, Pc = P, eta_vep = 0.0, lam_dot = 0.0, A_tau = 1.0, eta_vp = ph.eta_vp;
-  if (plastic == 1) {
-    double F = Tii - Tyield;
-    if (fp64_gt(F, 1e-17)) {
-      const double tol = M.eta_tol, eta_vp0 = ph.eta_vp, n_vp = ph.n_vp;
-      const bool vp1 = (fl & F_VP1) != 0;
-      // The products and sums of this return are rounded one by one (explicit intrinsics, which
-      // the compiler never fuses), as the reference's unfused arithmetic does: left to the
-      // compiler, whether a product fused into the following sum depended on the kernel the
-      // function was inlined into, and the iteration magnified that last bit.
-      const double Kdt = __dmul_rn(K, dt);
-      const double ksd = __dmul_rn(__dmul_rn(Kdt, c.sin_fric), c.sin_dil);
-      double Tiic = 0.0;
-      is_pl = 1;
-      eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
-      gdot = quotient(F, eta_ve + eta_vp + ksd);
-      const double F0 = F, tolF0 = tol * F0;
-      // with n_vp == 1, eta_vp / n_vp is eta_vp exactly and the derivative is a constant
-      const double dF1 = __dsub_rn(__dsub_rn(-eta_ve, eta_vp0), ksd);
-      // The return is a fixed map of the state (gdot, Tyield) entering each iteration.  When
-      // the state that the update produces equals one already entered -- the previous
-      // iteration's (the Newton step rounds away) or the one before (two states alternate
-      // in the last bit) -- every later iteration repeats one already done, and the values
-      // the loop ends with at its cap of 20 are known now: stop there instead of running
-      // the repeats.  The results are those of the full loop, bit for bit.
-      unsigned long long g1 = ~0ull, y1 = ~0ull;  // state entering the previous iteration
-      int last = 19;
-      for (int it = 0; it <= last; it++) {
-        const unsigned long long g0 = fp64_bits(gdot), y0 = fp64_bits(Tyield);
-        divp = __dmul_rn(gdot, c.sin_dil);
-        Pc = __dadd_rn(P, __dmul_rn(Kdt, divp));
-        eta_vp = vp1 ? eta_vp0 : eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
-        Tyield = __dadd_rn(Tyield, __dmul_rn(gdot, eta_vp));
-        Tiic = __dsub_rn(Tii, __dmul_rn(eta_ve, gdot));
-        F = Tiic - Tyield;
-        if (fp64_abs_lt(F, tol) || fp64_abs_lt(F, tolF0)) break;
-        gdot -= F / (vp1 ? dF1 : (-eta_ve - eta_vp / n_vp - ksd));
-        if (it == last) break;
-        const unsigned long long gn = fp64_bits(gdot), yn = fp64_bits(Tyield);
-        if (gn == g0 && yn == y0) break;  // period 1: iteration 19 would be this one
-        if (gn == g1 && yn == y1) {       // period 2: iteration 19 repeats this one or the next
-          if (((19 - it) & 1) == 0) break;
-          last = it + 1;
-        }
-        g1 = g0; y1 = y0;
-      }
-      if (fp64_lt(Tiic, 0.0)) { gdot = (Tii - M.Tiimin) / (eta_ve); Tiic = M.Tiimin; Pc = P; }  // :697-704
-      o.Pcorr = Pc;
-      eta_vep = Tiic * c.inv2Eii;
-      Tii = Tiic;
-    }
-  }
+// Plastic corrections but the Drucker-Prager return (which dp_return does), and the
+// post-processing of one (node, phase) after its visco-elastic solve (:655-1073).
+__device__ inline void iso_post(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                IsoState &S, PointOut &o, IsoMid &m) {
+  const int fl = ph.flags;
+  const int constant = (fl & F_CST) != 0, dislocation = (fl & F_PWL) != 0, diffusion = (fl & F_LIN) != 0;
+  const int gs = (fl & F_GS) != 0;
+  const int peierls = ((fl & F_EXPV) != 0) && fp64_lt(c.Traw, M.TmaxPeierls);
+  const int plastic = c.plastic_on ? ((fl & F_PL1) ? 1 : ((fl & F_PL2) ? 2 : 0)) : 0;
+  const int elastic = c.elastic;
+  const double T = c.T, P = in.P, Eii = c.Eii, K = c.K;
+  const double eta_cst = S.eta_cst, C = S.C, lnd = S.lnd;
+  (void)T;
+  const double eta_ve = m.eta_ve, Tii_ve = m.Tii_ve;
+  const double e_cst = m.e_cst, e_pwl = m.e_pwl, e_exp = m.e_exp, e_lin = m.e_lin;
+  double Tii = m.Tii;
+  int is_pl = m.is_pl;
+  double gdot = m.gdot, divp = m.divp, Pc = m.Pc, eta_vep = m.eta_vep, lam_dot = m.lam_dot, A_tau = m.A_tau;
+  double eta_vp = m.eta_vp;
+  if (is_pl && plastic == 1) o.Pcorr = Pc;
   double A_P = 0.0;
   if (plastic == 2) {
     int st = MDZ_OK;
@@ -1002,6 +1057,22 @@ __device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, con
   if (fp64_gt(eta, M.max_eta)) eta = M.max_eta;
   if (fp64_lt(eta, M.min_eta)) eta = M.min_eta;
   o.eta = eta;
+}
+
+// Local solve, plastic corrections and post-processing of one (node, phase): iso_ve, the
+// Drucker-Prager return where the item yields, iso_post.
+__device__ inline void iso_finish(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,
+                                  IsoState &S, float s_start, int polish, PointOut &o,
+                                  double *eta_conv = nullptr) {
+  IsoMid m;
+  iso_ve(M, ph, in, c, S, s_start, polish, o, m, eta_conv);
+  if (iso_yields_dp(M, ph, c, m)) {
+    DpItem d;
+    dp_load(d, m, in, c);
+    dp_return(M, ph, d);
+    dp_store(m, d);
+  }
+  iso_post(M, ph, in, c, S, o, m);
 }
 
 __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, const NodeIn &in, const NodeCtx &c,

@@ -368,6 +368,114 @@ __global__ void __launch_bounds__(128, 4) k_sweep_queue(const __grid_constant__ 
   flush_acc(A.stats, acc);
 }
 
+// Compacting form of the isotropic sweep.  The Drucker-Prager return of an item that yields
+// takes a few iterations with a division each, and about one item in eleven yields: inline,
+// nearly every warp carries one or two yielding lanes through the return while the other
+// lanes wait.  Here the CTA's 128 threads walk their nodes' phases in step (the node and
+// phase loops are uniform over the CTA); after each phase's visco-elastic solve the yielding
+// items are gathered by ballot into a queue in shared memory, the first threads of the
+// CTA run one return each, packed into as few warps as the queue needs, and every owner
+// takes its result back for the post-processing.  Same functions, so the same bits as
+// k_sweep.
+struct CompactQueue {
+  DpItem item[128];
+  int count[2];  // per phase parity: the counter of the phase in flight and of the next
+};
+
+__device__ __forceinline__ void compact_init(CompactQueue &Q) {
+  if (threadIdx.x < 2) Q.count[threadIdx.x] = 0;
+  __syncthreads();
+}
+
+// The warm-start declarations (used below with WARM)
+__device__ __forceinline__ void warm_inputs(const MlpDevice &W, const float *f, int nfeat, float *x);
+
+// One isotropic node per thread; every thread of the CTA calls it together (valid false: a
+// thread without a node, which still takes part in the CTA's barriers and, WARM, in its
+// warp's network).  WARM: the learned start, evaluated per warp, before each local solve.
+template <int NODES, bool WARM>
+__device__ __forceinline__ void compact_node(const SweepArgs &A, bool valid, long long i, Acc &acc,
+                                             CompactQueue &Q, int &par, MlpWarpShared *S = nullptr,
+                                             const MlpDevice *W = nullptr, const PerturbKey *pk = nullptr) {
+  const int t = threadIdx.x, lane = t & 31;
+  Node n;
+  n.solid = false;
+  n.centroid = NODES == 1;
+  if (valid) node_prepare<false, NODES>(A, i, n, pk);
+  double out[CO_COUNT];
+#pragma unroll
+  for (int k = 0; k < CO_COUNT; k++) out[k] = 0.0;
+  int status = MDZ_OK;
+  const int polish = WARM ? W->polish_iters : A.polish;
+  for (int p = 0; p < A.M.np; p++) {  // uniform over the CTA
+    const double perc = (valid && n.solid) ? node_perc(A, n, p) : 0.0;
+    const bool active = fp64_abs_gt(perc, 1e-13);  // :1210-1212
+    if (valid && n.solid && !active) node_iters(A, n, p, 0);
+    IsoState st;
+    PointOut o;
+    IsoMid m;
+    float s_start = 1.0f;
+    if (WARM) {
+      float f[kMlpIn], x[kMlpIn];
+#pragma unroll
+      for (int k = 0; k < kMlpIn; k++) f[k] = 0.0f;
+      if (active) {
+        iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o, polish == 0);
+        warm_features(A.M, n.in, n.ctx, st, false, f);
+      }
+      warm_inputs(*W, f, kFeatIso, x);
+      __syncwarp();
+      const float y = mlp_warp_predict(*S, x);
+      s_start = warm_start_point(y, W->z_scale, W->z_shift);
+    } else if (active) {
+      iso_setup(A.M, A.ph[p], n.in, n.ctx, st, o, polish == 0);
+    }
+    bool yields = false;
+    if (active) {
+      iso_ve(A.M, A.ph[p], n.in, n.ctx, st, s_start, polish, o, m);
+      yields = iso_yields_dp(A.M, A.ph[p], n.ctx, m);
+    }
+    // the warp's yielding lanes take consecutive slots: one shared atomic per warp
+    const unsigned ball = __ballot_sync(0xffffffffu, yields);
+    int slot = 0;
+    if (lane == 0 && ball) slot = atomicAdd(&Q.count[par], __popc(ball));
+    slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(ball & ((1u << lane) - 1u));
+    if (yields) dp_load(Q.item[slot], m, n.in, n.ctx);
+    __syncthreads();
+    const int q = Q.count[par];
+    if (t == 0) Q.count[par ^ 1] = 0;  // the next phase's counter, idle until after the next barrier
+    if (t < q) {
+      DpItem d = Q.item[t];
+      dp_return(A.M, A.ph[p], d);
+      Q.item[t] = d;
+    }
+    __syncthreads();
+    if (yields) dp_store(m, Q.item[slot]);
+    if (active) {
+      iso_post(A.M, A.ph[p], n.in, n.ctx, st, o, m);
+      node_accumulate<false>(A, n, p, perc, o, out, acc, status);
+    }
+    par ^= 1;
+  }
+  if (valid) node_store<false>(A, n, out, status);
+}
+
+template <int NODES>
+__global__ void __launch_bounds__(128, 4) k_sweep_compact(const __grid_constant__ SweepArgs A) {
+  __shared__ CompactQueue Q;
+  compact_init(Q);
+  Acc acc = {0, 0, 0, 0, 0};
+  const long long total = NODES == 1 ? (A.ranged ? A.c_n : A.M.Nc) : (A.ranged ? A.v_n : A.M.Nv);
+  const long long lo = NODES == 1 ? (A.ranged ? A.c_lo : 0) : A.M.Nc + (A.ranged ? A.v_lo : 0);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  int par = 0;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < total; base += stride) {  // uniform
+    const long long j = base + threadIdx.x;
+    compact_node<NODES, false>(A, j < total, lo + j, acc, Q, par);
+  }
+  flush_acc(A.stats, acc);
+}
+
 // ---------------------------------------------------------------------------------
 // learned warm start, per warp: the plain sweep with the network between each phase's
 // set-up and its local solve, evaluated by the warp's 32 lanes on the tensor cores
@@ -435,10 +543,20 @@ __global__ void __launch_bounds__(128, 4) k_sweep_warm(const __grid_constant__ S
   const long long total = NODES == 1 ? A.M.Nc : A.M.Nv;
   const long long lo = NODES == 1 ? 0 : A.M.Nc;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
-    const long long j = base + lane;
-    warm_node<ANISO, NODES>(A, S, W, j < total, lo + j, acc);
+  if constexpr (ANISO) {
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < total; base += stride) {
+      const long long j = base + lane;
+      warm_node<ANISO, NODES>(A, S, W, j < total, lo + j, acc);
+    }
+  } else {  // the isotropic sweep compacts its plastic returns per CTA (k_sweep_compact)
+    __shared__ CompactQueue Q;
+    compact_init(Q);
+    int par = 0;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < total; base += stride) {  // uniform
+      const long long j = base + threadIdx.x;
+      compact_node<NODES, true>(A, j < total, lo + j, acc, Q, par, &S, &W);
+    }
   }
   flush_acc(A.stats, acc);
 }
@@ -474,16 +592,32 @@ __global__ void __launch_bounds__(kBatchTile, 4) k_sweep_batch(const __grid_cons
   Acc acc = {0, 0, 0, 0, 0};
   const long long *ts = NODES == 1 ? B.tile_start_n : B.tile_start_s;
   const long long tiles = NODES == 1 ? B.tiles_n : B.tiles_s;
-  for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {  // uniform over the CTA
-    const int g = batch_grid_of(ts, B.n, t);
-    const SweepArgs &A = B.grids[g];
-    const long long j = (t - __ldg(&ts[g])) * kBatchTile + threadIdx.x;
-    const bool valid = j < (NODES == 1 ? A.M.Nc : A.M.Nv);
-    const long long i = NODES == 1 ? j : A.M.Nc + j;
-    PerturbKey pk;
-    if (PERTURB) { pk.key = perturb_key(X.seed, X.sweep, g); pk.amp = X.amp; }
-    if (WARM) warm_node<ANISO, NODES>(A, S, X.mlp, valid, i, acc, PERTURB ? &pk : nullptr);
-    else if (valid) sweep_node<ANISO, NODES>(A, i, acc, PERTURB ? &pk : nullptr);
+  [[maybe_unused]] int par = 0;
+  if constexpr (!ANISO) {
+    __shared__ CompactQueue Q;
+    compact_init(Q);
+    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {  // uniform over the CTA
+      const int g = batch_grid_of(ts, B.n, t);
+      const SweepArgs &A = B.grids[g];
+      const long long j = (t - __ldg(&ts[g])) * kBatchTile + threadIdx.x;
+      const bool valid = j < (NODES == 1 ? A.M.Nc : A.M.Nv);
+      const long long i = NODES == 1 ? j : A.M.Nc + j;
+      PerturbKey pk;
+      if (PERTURB) { pk.key = perturb_key(X.seed, X.sweep, g); pk.amp = X.amp; }
+      compact_node<NODES, WARM>(A, valid, i, acc, Q, par, &S, &X.mlp, PERTURB ? &pk : nullptr);
+    }
+  } else {
+    for (long long t = blockIdx.x; t < tiles; t += gridDim.x) {  // uniform over the CTA
+      const int g = batch_grid_of(ts, B.n, t);
+      const SweepArgs &A = B.grids[g];
+      const long long j = (t - __ldg(&ts[g])) * kBatchTile + threadIdx.x;
+      const bool valid = j < (NODES == 1 ? A.M.Nc : A.M.Nv);
+      const long long i = NODES == 1 ? j : A.M.Nc + j;
+      PerturbKey pk;
+      if (PERTURB) { pk.key = perturb_key(X.seed, X.sweep, g); pk.amp = X.amp; }
+      if (WARM) warm_node<ANISO, NODES>(A, S, X.mlp, valid, i, acc, PERTURB ? &pk : nullptr);
+      else if (valid) sweep_node<ANISO, NODES>(A, i, acc, PERTURB ? &pk : nullptr);
+    }
   }
   flush_acc(B.stats, acc);
 }
@@ -627,6 +761,12 @@ template <bool ANISO, int NODES>
 static void launch_kind(const SweepArgs &a, const LaunchShape &sh, long long count, cudaStream_t s) {
   if (sh.form == SHAPE_QUEUE) {
     k_sweep_queue<ANISO, NODES><<<(unsigned)sh.grid_cap, 128, 0, s>>>(a);
+    return;
+  }
+  if (!ANISO && sh.form == SHAPE_COMPACT) {  // the isotropic sweep only
+    long long grid = (count + 127) / 128;
+    if (sh.grid_cap > 0 && grid > sh.grid_cap) grid = sh.grid_cap;
+    k_sweep_compact<NODES><<<(unsigned)grid, 128, 0, s>>>(a);
     return;
   }
   long long grid = (count + sh.block - 1) / sh.block;
@@ -777,6 +917,7 @@ void sweep_kernel_info(int aniso, int *regs, int *smem, int *max_blocks_per_sm, 
   const void *fn = aniso ? (const void *)k_sweep<true, 1, 4> : (const void *)k_sweep<false, 1, 4>;
   if (form == SHAPE_REGS255) fn = aniso ? (const void *)k_sweep<true, 1, 2> : (const void *)k_sweep<false, 1, 2>;
   if (form == SHAPE_QUEUE) fn = aniso ? (const void *)k_sweep_queue<true, 1> : (const void *)k_sweep_queue<false, 1>;
+  if (form == SHAPE_COMPACT && !aniso) fn = (const void *)k_sweep_compact<1>;
   cudaFuncGetAttributes(&fa, fn);
   *regs = fa.numRegs;
   *smem = (int)fa.sharedSizeBytes;

@@ -31,7 +31,7 @@ struct DevStats {
 
 // Launch shape of the plain sweep: threads per block, grid cap (0: one thread per node;
 // else a grid-stride loop over that many CTAs) and the kernel form.
-enum { SHAPE_THREAD = 0, SHAPE_REGS255 = 1, SHAPE_QUEUE = 2 };
+enum { SHAPE_THREAD = 0, SHAPE_REGS255 = 1, SHAPE_QUEUE = 2, SHAPE_COMPACT = 3 };
 struct LaunchShape {
   int block, grid_cap, form;
 };

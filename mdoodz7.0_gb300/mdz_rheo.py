@@ -746,11 +746,14 @@ class Context:
 
     # ---- launch-shape autotuner
     # (threads per block, waves of resident CTAs or 0 for one thread per node, form); forms:
-    # 0 the 128-register kernel, 1 the 255-register kernel, 2 persistent work counter
-    AUTOTUNE_CANDIDATES = [(b, w, 0) for b in (128, 64) for w in (0, 1, 2, 4, 8)] + [(128, 0, 1), (128, 1, 2)]
+    # 0 the 128-register kernel, 1 the 255-register kernel, 2 persistent work counter,
+    # 3 the compacting kernel (isotropic; one thread per node for the anisotropic sweep)
+    AUTOTUNE_CANDIDATES = ([(b, w, 0) for b in (128, 64) for w in (0, 1, 2, 4, 8)]
+                           + [(128, 0, 1), (128, 1, 2), (128, 0, 3)])
     AUTOTUNE_NAMES = ([f"block {b}, " + (f"{w} waves" if w else "one thread per node") for b in (128, 64)
                        for w in (0, 1, 2, 4, 8)] + ["block 128, one thread per node, 255 registers (2 CTAs/SM)",
-                                                    "block 128, persistent warps on a work counter"])
+                                                    "block 128, persistent warps on a work counter",
+                                                    "block 128, yielding items compacted per CTA"])
 
     def autotune(self, model, mat, fields, aniso=False, flags=0, reps=3):
         """Time every launch shape on this device-resident grid and keep the fastest.

@@ -35,7 +35,9 @@ def test_autotune_keeps_results_and_picks_a_candidate(aniso):
         assert np.all(ms > 0) and ms[best] == ms.min()
         assert shape[0] == R.Context.AUTOTUNE_CANDIDATES[best][0]
         assert (shape[1] == 0) == (R.Context.AUTOTUNE_CANDIDATES[best][1] == 0)
-        assert ctx.launch_form(aniso) == R.Context.AUTOTUNE_CANDIDATES[best][2]
+        # the compacting candidate runs the anisotropic sweep as one thread per node
+        want = R.Context.AUTOTUNE_CANDIDATES[best][2]
+        assert ctx.launch_form(aniso) == (0 if (aniso and want == 3) else want)
         again = to_device(clone(w.arrays))
         fn(w.model, w.mat, R.FieldSet(again), mem=R.MEM_DEVICE)   # runs with the tuned shape
         a, t, g = to_host(ref), to_host(tuned), to_host(again)
@@ -49,11 +51,11 @@ def test_autotune_keeps_results_and_picks_a_candidate(aniso):
         ctx.close()
 
 
-@pytest.mark.parametrize("aniso", [False, True])
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("aniso,form", [(False, 1), (True, 1), (False, 2), (True, 2), (False, 3)])
 def test_every_form_gives_the_same_bits(aniso, form):
-    """The 255-register kernel and the persistent work-counter kernel against the default
-    one-thread-per-node kernel, bit for bit, from both starts."""
+    """The 255-register kernel, the persistent work-counter kernel and the compacting kernel
+    against the default one-thread-per-node kernel, bit for bit, from both starts (the
+    compacting kernel runs the yielding items' plastic returns in other threads)."""
     w = W.aniso(seed=9, ncx=80) if aniso else W.plain_large(seed=9, ncx=90)
     ctx = R.Context(0)
     try:
@@ -71,5 +73,41 @@ def test_every_form_gives_the_same_bits(aniso, form):
                 if a.get(k) is not None:
                     assert np.array_equal(a[k], g[k], equal_nan=True), (flags, k)
             assert st.phase_calls > 0
+    finally:
+        ctx.close()
+
+
+def test_compacting_form_rejects_what_it_does_not_run():
+    ctx = R.Context(0)
+    try:
+        assert ctx.lib.mdz_rheo_set_launch_shape(ctx.handle, 1, 128, 0, 3) == R.MDZ_EINVAL  # anisotropic
+        assert ctx.lib.mdz_rheo_set_launch_shape(ctx.handle, 0, 64, 0, 3) == R.MDZ_EINVAL   # block 64
+    finally:
+        ctx.close()
+
+
+def test_compacting_form_in_banded_host_sweeps_and_with_iterations():
+    """Host-memory sweeps in row bands (each band a ranged launch) and the per-item words
+    with the compacting form: the same bits as the one-thread-per-node form."""
+    w = W.plain_large(seed=10, ncx=120, ncz=300)
+    ctx = R.Context(0)
+    try:
+        out = []
+        for form in (0, 3):
+            ctx.set_launch_shape(False, 128, 0, form)
+            ctx.set_host_bands(7)
+            h = clone(w.arrays)
+            ctx.sweep(w.model, w.mat, R.FieldSet(h))
+            it = clone(w.arrays)
+            ctx.sweep(w.model, w.mat, R.FieldSet(it), flags=R.SWEEP_ITERS)
+            n = np.zeros(w.mat.Nb_phases * w.Nc, np.int32)
+            s = np.zeros(w.mat.Nb_phases * w.Nv, np.int32)
+            ctx.get_iterations(n, s)
+            out.append((h, n, s))
+        (h0, n0, s0), (h3, n3, s3) = out
+        for k in R.CEN_OUT + R.VER_OUT:
+            if h0.get(k) is not None:
+                assert np.array_equal(h0[k], h3[k], equal_nan=True), k
+        assert np.array_equal(n0, n3) and np.array_equal(s0, s3)
     finally:
         ctx.close()
