@@ -81,6 +81,8 @@ extern "C" {
 #define MDZ_SWEEP_REF_START  0x8  /* start each local Newton where the reference does (see below) */
 #define MDZ_SWEEP_WARM_TILES 0x10 /* with MDZ_SWEEP_WARMSTART: evaluate the network CTA-wide on tcgen05
                                      (128-node tiles, CTA barriers per phase) instead of per warp */
+#define MDZ_SWEEP_STAGED     0x20 /* MDZ_MEM_HOST: stage every array through device copies in row
+                                     bands even where the GPU can address the host arrays directly */
 #define MDZ_DEFAULT_POLISH   4    /* FP32 Newton steps before each FP64 local solve, by default */
 /* Start descriptor of the local solves (mdz_rheo_set_warmstart): FP32 Newton steps in the
  * low byte, plus MDZ_START_DD for one Halley step evaluated in double-float (FP32 pairs)

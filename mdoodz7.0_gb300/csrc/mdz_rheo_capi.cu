@@ -461,6 +461,48 @@ int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &
   return MDZ_OK;
 }
 
+// Host arrays the kernels can address directly: page-locked memory mapped into the device's
+// address space at the same address (cudaHostAlloc, cudaMallocHost, or cudaHostRegister of
+// the whole array), checked at the array's first and last byte.  On a Grace-Blackwell
+// system the host link (NVLink-C2C) is coherent and fast enough that the sweep reads its
+// inputs and writes its outputs there during the kernels at nearly the speed of device
+// memory (the kernels are bound by the FP64 pipe), with no staging copies.
+bool host_mapped(const void *p, size_t bytes) {
+  if (!p || !bytes) return true;
+  const void *ends[2] = {p, (const char *)p + (bytes - 1)};
+  for (const void *q : ends) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, q) != cudaSuccess || a.type != cudaMemoryTypeHost || a.devicePointer != q) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  return true;
+}
+
+// Every array of a host-memory sweep addressable by the kernels (host_mapped); the bytes
+// the kernels then read from and write to host memory go into the context's counters.
+bool sweep_arrays_mapped(mdz_rheo_ctx *ctx, const FieldLists &L, const mdz_grid_fields *f, int np, size_t Nc,
+                         size_t Nv) {
+  size_t in = 0, out = 0;
+  for (int i = 0; i < L.nci; i++) { if (!host_mapped(L.cin[i], Nc * 8)) return false; in += L.cin[i] ? Nc * 8 : 0; }
+  for (int i = 0; i < L.nvi; i++) { if (!host_mapped(L.vin[i], Nv * 8)) return false; in += L.vin[i] ? Nv * 8 : 0; }
+  for (int i = 0; i < CO_COUNT; i++) { if (!host_mapped(L.cout[i], Nc * 8)) return false; out += L.cout[i] ? Nc * 8 : 0; }
+  for (int i = 0; i < VO_COUNT; i++) { if (!host_mapped(L.vout[i], Nv * 8)) return false; out += L.vout[i] ? Nv * 8 : 0; }
+  for (int p = 0; p < np; p++) {
+    if (!host_mapped(f->phase_perc_n[p], Nc * 8) || !host_mapped(f->phase_perc_s[p], Nv * 8) ||
+        !host_mapped(f->phase_eta_n[p], Nc * 8) || !host_mapped(f->phase_eta_s[p], Nv * 8))
+      return false;
+    in += 2 * (Nc + Nv) * 8;  // fractions, and the previous phase viscosities that inactive phases keep
+    out += (Nc + Nv) * 8;
+  }
+  if (!host_mapped(f->BCp_type, Nc) || !host_mapped(f->BCg_type, Nv)) return false;
+  in += Nc + Nv;
+  ctx->h2d += in;
+  ctx->d2h += out;
+  return true;
+}
+
 int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat, const mdz_grid_fields *f,
                int final_update, int mem, int flags, mdz_sweep_stats *st, bool aniso, float *X = nullptr,
                float *Y = nullptr) {
@@ -485,7 +527,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   A.polish = (flags & MDZ_SWEEP_REF_START) ? 0 : ctx->polish_iters;
   const size_t Nc = (size_t)A.M.Nc, Nv = (size_t)A.M.Nv;
   const int np = A.M.np;
-  const bool host = (mem == MDZ_MEM_HOST);
+  const bool host_mem = (mem == MDZ_MEM_HOST);
   FieldLists L;
   if ((rc = field_lists(md, f, aniso, L)) != MDZ_OK) return rc;
   const double *const *cin = L.cin, *const *vin = L.vin;
@@ -494,6 +536,9 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
 
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
+  // host arrays the kernels can address in place need no staging copies
+  const bool direct = host_mem && !(flags & MDZ_SWEEP_STAGED) && sweep_arrays_mapped(ctx, L, f, np, Nc, Nv);
+  const bool host = host_mem && !direct;  // staged through device mirrors
   const int bands = (host && mode < 0 && !(flags & MDZ_SWEEP_ITERS)) ? host_bands(ctx, md->Nz) : 1;
   if (bands > 1) {
     A.stats = ctx->d_stats;
@@ -543,7 +588,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
     DevBuf b;
     ~Scratch() { if (b.p) cudaFree(b.p); }
   } tmpX, tmpY;
-  if (collect && host) {
+  if (collect && host_mem) {
     if (ensure(tmpX.b, items * kMlpIn * sizeof(float)) != MDZ_OK || ensure(tmpY.b, items * 2 * sizeof(float)) != MDZ_OK)
       return MDZ_ENOMEM;
     dX = (float *)tmpX.b.p;
@@ -570,7 +615,7 @@ int sweep_impl(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materials *mat,
   }
   ctx->launches += sweep_kernel_count(A);
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
-  if (collect && host) {
+  if (collect && host_mem) {
     CK(cudaMemcpyAsync(X, dX, items * kMlpIn * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(Y, dY, items * 2 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

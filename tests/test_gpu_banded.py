@@ -92,3 +92,56 @@ def test_host_bands_argument_checked(ctx):
         ctx.set_host_bands(17)
     with pytest.raises(R.RheoError):
         ctx.set_host_bands(-1)
+
+
+def pinned(arrays):
+    return {k: ([torch.from_numpy(x.copy()).pin_memory() for x in v] if isinstance(v, list)
+                else torch.from_numpy(v.copy()).pin_memory()) for k, v in arrays.items()}
+
+
+def host_view(d):
+    return {k: ([x.numpy() for x in v] if isinstance(v, list) else v.numpy()) for k, v in d.items()}
+
+
+@pytest.mark.parametrize("aniso", [False, True])
+def test_direct_sweep_of_page_locked_host_arrays(ctx, aniso):
+    """Page-locked host arrays are read and written by the kernels in place (no staging
+    copies: two launches, no bands), with the same bits and the same host<->device byte
+    counts as the staged sweep in row bands (MDZ_SWEEP_STAGED) and as the sweep of
+    device-resident copies."""
+    w = W.aniso(seed=41, ncx=300, ncz=280) if aniso else with_air_and_periodic(W.plain_large(seed=41, ncx=300, ncz=280))
+    fn = ctx.sweep_aniso if aniso else ctx.sweep
+    ctx.set_host_bands(0)
+    direct = pinned(clone(w.arrays))
+    rc, st_d = fn(w.model, w.mat, R.FieldSet(direct))
+    assert rc == R.MDZ_OK and st_d.kernel_launches == 2
+    staged = pinned(clone(w.arrays))
+    rc, st_s = fn(w.model, w.mat, R.FieldSet(staged), flags=R.SWEEP_STAGED)
+    assert rc == R.MDZ_OK and st_s.kernel_launches > 2  # row bands
+    dev = {k: ([torch.from_numpy(x.copy()).cuda() for x in v] if isinstance(v, list)
+               else torch.from_numpy(v.copy()).cuda()) for k, v in w.arrays.items()}
+    fn(w.model, w.mat, R.FieldSet(dev), mem=R.MEM_DEVICE)
+    torch.cuda.synchronize()
+    a, b = host_view(direct), host_view(staged)
+    c = {k: ([x.cpu().numpy() for x in v] if isinstance(v, list) else v.cpu().numpy()) for k, v in dev.items()}
+    for k in R.VER_INTERP + R.CEN_OUT + R.VER_OUT + ["phase_eta_n", "phase_eta_s"]:
+        if a.get(k) is None:
+            continue
+        x, y, z = (np.concatenate(v) if isinstance(v, list) else v for v in (a[k], b[k], c[k]))
+        assert np.array_equal(x, y, equal_nan=True) and np.array_equal(x, z, equal_nan=True), k
+    assert (st_d.h2d_bytes, st_d.d2h_bytes) == (st_s.h2d_bytes, st_s.d2h_bytes)
+    assert st_d.phase_calls == st_s.phase_calls
+
+
+def test_partly_page_locked_arrays_are_staged(ctx):
+    """One pageable array among page-locked ones: the sweep stages everything (bands)."""
+    w = W.plain_large(seed=42, ncx=200, ncz=260)
+    arrays = pinned(clone(w.arrays))
+    arrays["T"] = torch.from_numpy(w.arrays["T"].copy())  # pageable
+    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(arrays))
+    assert rc == R.MDZ_OK and st.kernel_launches > 2
+    ref = clone(w.arrays)
+    ctx.sweep(w.model, w.mat, R.FieldSet(ref))
+    for k in R.CEN_OUT + R.VER_OUT:
+        if ref.get(k) is not None:
+            assert np.array_equal(arrays[k].numpy(), ref[k], equal_nan=True), k
