@@ -25,8 +25,10 @@ UpdateParticleStress.
 
 `value` is timed with CUDA events on the launching stream with inputs resident in
 HBM (3.3 GB of fields, larger than the 129 MB L2, so no flush between steps);
-`e2e` is the same sweep through the C ABI with pinned host buffers, host<->device
-copies inside the timed region.  Under torchrun each rank sweeps its own grid
+`e2e` is the same sweep through the C ABI on page-locked host arrays, which the kernels
+read and write over the coherent host link inside the timed region (no staging copies);
+the line also carries the staged forms (host<->device copies in row bands, and in one
+piece).  Under torchrun each rank sweeps its own grid
 (independent instances, weak scaling; the path has no exchange step).
 """
 from __future__ import annotations
@@ -775,10 +777,20 @@ def main():
         barrier()
         ms_op = REP.max_over_ranks(e0.elapsed_time(e1), dev) / args.steps
         newton_op = {"what": "RheologicalOperators(Jacobian=1): D tensors with finite-difference derivatives, "
-                             "8 perturbed local solves per node and active phase",
+                             "8 perturbed local solves per node and active phase"
+                             + ("" if aniso else "; plastic returns compacted per CTA"),
                      "ms_per_launch": ms_op, "node_updates_per_s": REP.whole_job_rate(w.nodes, ws, ms_op),
                      "local_solves_per_launch": int(op_calls),
                      "local_solves_per_s": op_calls * ws / (ms_op * 1e-3)}
+        if not aniso:  # the same operator one thread per node, for comparison
+            ctx.operators(w.model, w.mat, fs, ops, jacobian=1, mem=R.MEM_DEVICE, flags=R.OPS_PER_NODE)
+            barrier()
+            e0.record(stream)
+            for _ in range(args.steps):
+                ctx.operators(w.model, w.mat, fs, ops, jacobian=1, mem=R.MEM_DEVICE, flags=R.OPS_PER_NODE)
+            e1.record(stream)
+            barrier()
+            newton_op["one_thread_per_node_ms_per_launch"] = REP.max_over_ranks(e0.elapsed_time(e1), dev) / args.steps
         del ops
 
     # ---- StrainRateComponents on the same grid: the step before the sweep ----

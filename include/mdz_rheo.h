@@ -83,6 +83,9 @@ extern "C" {
                                      (128-node tiles, CTA barriers per phase) instead of per warp */
 #define MDZ_SWEEP_STAGED     0x20 /* MDZ_MEM_HOST: stage every array through device copies in row
                                      bands even where the GPU can address the host arrays directly */
+#define MDZ_OPS_PER_NODE     0x40 /* mdz_rheo_operators: run the isotropic Newton operator one thread
+                                     per node instead of compacting its plastic returns per CTA
+                                     (the same bits; for comparison) */
 #define MDZ_DEFAULT_POLISH   4    /* FP32 Newton steps before each FP64 local solve, by default */
 /* Start descriptor of the local solves (mdz_rheo_set_warmstart): FP32 Newton steps in the
  * low byte, plus MDZ_START_DD for one Halley step evaluated in double-float (FP32 pairs)
@@ -311,8 +314,11 @@ int mdz_rheo_points(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materia
  *     per node and active phase (DerivativesOnTheFly_n / _s and PhaseRheologyLoop_v1,
  *     MDLIB/FD_Jacobian.c:48-323), all solved on the GPU in one launch.
  * `compressible` is params.compressible; `flags` may hold MDZ_SWEEP_REF_START, which
- * starts the perturbed solves where the reference does.  `mem` and `stats` as for the
- * sweep (stats count the perturbed local solves). */
+ * starts the perturbed solves where the reference does, and MDZ_OPS_PER_NODE.  The
+ * isotropic Newton operator walks the 8 perturbations and the phases of a CTA's 128 nodes
+ * in step and runs the Drucker-Prager returns of each phase's yielding items packed into
+ * the CTA's first warps; MDZ_OPS_PER_NODE runs one thread per node instead, with the same
+ * bits.  `mem` and `stats` as for the sweep (stats count the perturbed local solves). */
 int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *model, const mdz_materials *mat,
                        const mdz_grid_fields *f, mdz_operator_fields *ops, int jacobian, int compressible,
                        int aniso, int mem, int flags, mdz_sweep_stats *stats);

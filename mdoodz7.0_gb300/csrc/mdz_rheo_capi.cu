@@ -1464,7 +1464,7 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materia
                        mdz_sweep_stats *st) {
   if (!ctx || !md || !mat || !f || !ops) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
-  if (flags & ~MDZ_SWEEP_REF_START) return MDZ_EINVAL;
+  if (flags & ~(MDZ_SWEEP_REF_START | MDZ_OPS_PER_NODE)) return MDZ_EINVAL;
   if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
   CK(cudaSetDevice(ctx->device));
   static thread_local OpArgs A;
@@ -1519,7 +1519,7 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materia
   A.stats = ctx->d_stats;
   if ((rc = reset_stats(ctx)) != MDZ_OK) return rc;
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  CK(launch_operators(A, anis, jac, ctx->stream));
+  CK(launch_operators(A, anis, jac, !(flags & MDZ_OPS_PER_NODE), ctx->stream));
   ctx->launches = 1;
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
   for (int i = 0; i < OP_COUNT; i++) mi.back(dout[i], S_OP + i, i < OP_D31 ? Nc : Nv, host);

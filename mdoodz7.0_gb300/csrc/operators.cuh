@@ -25,6 +25,8 @@ struct OpArgs {
   int compressible, need_lnd, polish;
 };
 
-cudaError_t launch_operators(const OpArgs &a, bool aniso, bool jacobian, cudaStream_t s);
+// compact: the isotropic Newton operator with its plastic returns compacted per CTA (the
+// same bits as one thread per node); ignored elsewhere.
+cudaError_t launch_operators(const OpArgs &a, bool aniso, bool jacobian, bool compact, cudaStream_t s);
 
 }  // namespace mdz

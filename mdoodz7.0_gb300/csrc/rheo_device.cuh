@@ -1082,6 +1082,48 @@ __device__ inline void point_iso(const ModelConst &M, const PhaseConst &ph, cons
   iso_finish(M, ph, in, c, S, 1.0f, polish, o);
 }
 
+// CTA-level compaction of the Drucker-Prager returns.  The return of an item that yields
+// takes a few iterations with a division each, and about one item in eleven yields: inline,
+// nearly every warp carries one or two yielding lanes through the return while the other
+// lanes wait.  A kernel whose CTA (at most 128 threads) walks its items' phases in step
+// calls dp_compact with every thread once per phase, after iso_ve: the yielding items are
+// gathered by ballot into a queue in shared memory (one shared atomic per warp, slots by
+// popcount), the first threads of the CTA run one return each, packed into as few warps as
+// the queue needs, and every owner takes its result back for iso_post.  The same
+// functions as iso_finish, so the same bits.
+struct CompactQueue {
+  DpItem item[128];
+  int count[2];  // per phase parity: the counter of the phase in flight and of the next
+};
+
+__device__ __forceinline__ void compact_init(CompactQueue &Q) {
+  if (threadIdx.x < 2) Q.count[threadIdx.x] = 0;
+  __syncthreads();
+}
+
+// par: the phase parity, flipped here.  count[par ^ 1] is cleared between the two
+// barriers, where no thread touches it; count[par] is read only between them.
+__device__ __forceinline__ void dp_compact(const ModelConst &M, const PhaseConst &ph, CompactQueue &Q, int &par,
+                                           bool yields, IsoMid &m, const NodeIn &in, const NodeCtx &c) {
+  const int t = threadIdx.x, lane = t & 31;
+  const unsigned ball = __ballot_sync(0xffffffffu, yields);
+  int slot = 0;
+  if (lane == 0 && ball) slot = atomicAdd(&Q.count[par], __popc(ball));
+  slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(ball & ((1u << lane) - 1u));
+  if (yields) dp_load(Q.item[slot], m, in, c);
+  __syncthreads();
+  const int q = Q.count[par];
+  if (t == 0) Q.count[par ^ 1] = 0;
+  if (t < q) {
+    DpItem d = Q.item[t];
+    dp_return(M, ph, d);
+    Q.item[t] = d;
+  }
+  __syncthreads();
+  if (yields) dp_store(m, Q.item[slot]);
+  par ^= 1;
+}
+
 // ---------------------------------------------------------------------------------------
 // ViscosityConciseAniso (AnisotropyRoutines.c:282-727).  The node context carries the
 // rotated-frame invariant; Er_* are the rotated strain-rate components.

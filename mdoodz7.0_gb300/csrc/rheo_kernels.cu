@@ -368,24 +368,10 @@ __global__ void __launch_bounds__(128, 4) k_sweep_queue(const __grid_constant__ 
   flush_acc(A.stats, acc);
 }
 
-// Compacting form of the isotropic sweep.  The Drucker-Prager return of an item that yields
-// takes a few iterations with a division each, and about one item in eleven yields: inline,
-// nearly every warp carries one or two yielding lanes through the return while the other
-// lanes wait.  Here the CTA's 128 threads walk their nodes' phases in step (the node and
-// phase loops are uniform over the CTA); after each phase's visco-elastic solve the yielding
-// items are gathered by ballot into a queue in shared memory, the first threads of the
-// CTA run one return each, packed into as few warps as the queue needs, and every owner
-// takes its result back for the post-processing.  Same functions, so the same bits as
-// k_sweep.
-struct CompactQueue {
-  DpItem item[128];
-  int count[2];  // per phase parity: the counter of the phase in flight and of the next
-};
-
-__device__ __forceinline__ void compact_init(CompactQueue &Q) {
-  if (threadIdx.x < 2) Q.count[threadIdx.x] = 0;
-  __syncthreads();
-}
+// Compacting form of the isotropic sweep: the CTA's 128 threads walk their nodes' phases
+// in step (the node and phase loops are uniform over the CTA), and the Drucker-Prager
+// returns of each phase's yielding items run packed into the first warps (dp_compact).
+// Same functions, so the same bits as k_sweep.
 
 // The warm-start declarations (used below with WARM)
 __device__ __forceinline__ void warm_inputs(const MlpDevice &W, const float *f, int nfeat, float *x);
@@ -397,7 +383,6 @@ template <int NODES, bool WARM>
 __device__ __forceinline__ void compact_node(const SweepArgs &A, bool valid, long long i, Acc &acc,
                                              CompactQueue &Q, int &par, MlpWarpShared *S = nullptr,
                                              const MlpDevice *W = nullptr, const PerturbKey *pk = nullptr) {
-  const int t = threadIdx.x, lane = t & 31;
   Node n;
   n.solid = false;
   n.centroid = NODES == 1;
@@ -435,27 +420,11 @@ __device__ __forceinline__ void compact_node(const SweepArgs &A, bool valid, lon
       iso_ve(A.M, A.ph[p], n.in, n.ctx, st, s_start, polish, o, m);
       yields = iso_yields_dp(A.M, A.ph[p], n.ctx, m);
     }
-    // the warp's yielding lanes take consecutive slots: one shared atomic per warp
-    const unsigned ball = __ballot_sync(0xffffffffu, yields);
-    int slot = 0;
-    if (lane == 0 && ball) slot = atomicAdd(&Q.count[par], __popc(ball));
-    slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(ball & ((1u << lane) - 1u));
-    if (yields) dp_load(Q.item[slot], m, n.in, n.ctx);
-    __syncthreads();
-    const int q = Q.count[par];
-    if (t == 0) Q.count[par ^ 1] = 0;  // the next phase's counter, idle until after the next barrier
-    if (t < q) {
-      DpItem d = Q.item[t];
-      dp_return(A.M, A.ph[p], d);
-      Q.item[t] = d;
-    }
-    __syncthreads();
-    if (yields) dp_store(m, Q.item[slot]);
+    dp_compact(A.M, A.ph[p], Q, par, yields, m, n.in, n.ctx);
     if (active) {
       iso_post(A.M, A.ph[p], n.in, n.ctx, st, o, m);
       node_accumulate<false>(A, n, p, perc, o, out, acc, status);
     }
-    par ^= 1;
   }
   if (valid) node_store<false>(A, n, out, status);
 }

@@ -54,6 +54,7 @@ SWEEP_ITERS = 0x4
 SWEEP_REF_START = 0x8
 SWEEP_WARM_TILES = 0x10
 SWEEP_STAGED = 0x20  # host memory: stage through device copies even where the GPU can address the arrays
+OPS_PER_NODE = 0x40  # operators: the isotropic Newton operator one thread per node (same bits)
 # per-(node, phase) item words of SWEEP_ITERS: iterations in bits 0-7, then mechanism bits
 MECH_CONSTANT, MECH_DISLOCATION, MECH_PEIERLS, MECH_DIFFUSION = 1 << 8, 1 << 9, 1 << 10, 1 << 11
 MECH_GBS, MECH_GRAIN_SIZE, MECH_PLASTIC, MECH_ELASTIC, MECH_YIELD = 1 << 12, 1 << 13, 1 << 14, 1 << 15, 1 << 16

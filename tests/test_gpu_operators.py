@@ -119,3 +119,41 @@ def test_gpu_picard_matches_oracle_exactly(ctx):
     O.orc_operators(w.model, w.mat, R.FieldSet(clone(w.arrays)), b, 0, 0, False)
     for k in R.OPS_N + R.OPS_S:
         assert np.array_equal(a[k], b[k]), k
+
+
+def _newton_both_forms(ctx, w, aniso=False, comp=0, flags=0):
+    out = []
+    for form in (0, R.OPS_PER_NODE):  # plastic returns compacted per CTA (the default), one thread per node
+        ops = R.alloc_operator_fields(w.Nc, w.Nv)
+        for k in ops:  # the Newton operator leaves drhodp_n at air cells untouched
+            ops[k][:] = 7.0
+        rc, st = ctx.operators(w.model, w.mat, R.FieldSet(clone(w.arrays)), ops, jacobian=1, compressible=comp,
+                               aniso=aniso, flags=flags | form)
+        assert rc == R.MDZ_OK
+        out.append((ops, st.phase_calls))
+    return out
+
+
+@pytest.mark.parametrize("flags", [0, R.SWEEP_REF_START])
+@pytest.mark.parametrize("name", [n for n, c in cases.OPERATOR_CASES.items() if c[1] == 1])
+def test_gpu_compacting_newton_operator_is_bitwise_one_thread_per_node(ctx, name, flags):
+    """The isotropic Newton operator runs its Drucker-Prager returns packed into the first
+    warps of each CTA; the result must be the one-thread-per-node operator's, bit for bit
+    (the anisotropic operator keeps one thread per node in both forms)."""
+    grid_case, _, comp = cases.OPERATOR_CASES[name]
+    w, aniso = swept_grid(grid_case)
+    (a, ca), (b, cb) = _newton_both_forms(ctx, w, aniso, comp, flags)
+    assert ca == cb > 0
+    for k in a:
+        assert np.array_equal(a[k], b[k], equal_nan=True), (name, k)
+
+
+def test_gpu_compacting_newton_operator_ragged_grid(ctx):
+    """A grid whose node count leaves the last CTA partly empty, with many yielding items."""
+    w = W.plain_large(seed=23, ncx=97, ncz=75)
+    ctx.sweep(w.model, w.mat, R.FieldSet(w.arrays))
+    assert (w.Nc + w.Nv) % 128 != 0
+    (a, ca), (b, cb) = _newton_both_forms(ctx, w)
+    assert ca == cb > 0
+    for k in a:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
