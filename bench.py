@@ -50,25 +50,40 @@ METRIC = "rheology point-updates/s on 1 GB300: plain FP64 vs NN warm-start at to
 UNIT = "point-updates/s"
 
 # FP64 work of the sweep per point-update, in flops (DFMA = 2, DADD/DMUL = 1): ncu's
-# thread-level FP64 instruction counters of one sweep's two k_sweep launches (centroids,
-# then vertices; default start), summed, on the same field distributions at 513 x 513
-# cells (527,365 nodes), per workload (profiles/k_sweep_plain_large_513.md,
+# thread-level FP64 instruction counters of one sweep's two launches (centroids, then
+# vertices; default start, default form: k_sweep_compact for the isotropic sweep, k_sweep
+# for the anisotropic one), summed, on the same field distributions at 513 x 513 cells
+# (527,365 nodes), per workload (profiles/k_sweep_plain_large_513.md,
 # profiles/k_sweep_aniso_513.md).  `roofline.achieved` = this x nodes / the CUDA-event
 # time of one sweep (events before the first launch and after the second).
-FP64_FLOPS_PER_POINT = {"plain_large": 1560.2, "aniso": 1094.8}
+FP64_FLOPS_PER_POINT = {"plain_large": 1448.7, "aniso": 1038.4}
 # FP64 work of the batched many-grid sweep per local solve (phase call), same convention:
 # the two k_sweep_batch launches of one sweep of an 8-grid batch of the many-grid
 # distribution (5,096,155 phase calls; profiles/k_sweep_batch_many_grids.md); the grids
 # have 2 to 5 phases, so the work is counted per phase call.
-FP64_FLOPS_PER_PHASE_CALL = {"many_grids": 312.0}
+FP64_FLOPS_PER_PHASE_CALL = {"many_grids": 288.8}
 # DRAM bytes (read + write) per point-update of one sweep's two launches at 1025 x 1025
-# cells (0.7 GB of fields, five times L2; profiles/k_sweep_spills_and_dram_1025.md, the
-# 4-CTA kernels whose spills reach DRAM in part), scaled to a sweep by its node count.
-DRAM_BYTES_PER_POINT = {"plain_large": 381.0, "aniso": 364.2}
+# cells (0.7 GB of fields, five times L2; profiles/k_sweep_spills_and_dram_1025.md: the
+# default forms at 4 CTAs per SM, whose register spills reach DRAM in part), scaled to a
+# sweep by its node count.
+DRAM_BYTES_PER_POINT = {"plain_large": 414.6, "aniso": 364.2}
 # FP64 work of k_marker_update per marker (inactive ones included), same convention:
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
-FP64_FLOPS_PER_MARKER = {"jaumann_stencil1": 98.34, "analytical_director_stencil9": 226.16}
+FP64_FLOPS_PER_MARKER = {"jaumann_stencil1": 90.48, "analytical_director_stencil9": 218.31}
+# FP64-pipe thread instructions (DFMA, DADD, DMUL and the few conversions; each takes a
+# pipe slot whether it carries two flops or one) per unit, from the same captures:
+# `fp64_issue_frac` = this x units / time / (measured DFMA rate / 2) is how busy the FP64
+# pipe is with useful lanes, the figure the flop fraction understates by the DADD/DMUL share.
+FP64_THREAD_INSTS = {"plain_large": 954.4, "aniso": 671.0, "many_grids": 190.0,
+                     "jaumann_stencil1": 77.23, "analytical_director_stencil9": 183.50}
+
+
+def issue_frac(insts_per_unit, units, ms, peak_tflops):
+    """FP64-pipe thread instructions per second over the DFMA lane rate (peak flops / 2)."""
+    if not insts_per_unit or not ms:
+        return None
+    return insts_per_unit * units / (ms * 1e-3) / (peak_tflops * 1e12 / 2.0)
 
 
 def parse():
@@ -932,7 +947,8 @@ def main():
         roof = {"bound": "fp64", "achieved": achieved, "peak": peak_fp64, "unit": "TFLOP/s",
                 "frac": achieved / peak_fp64, "peak_source": "measured (DFMA probe, mdz_rheo_measure_fp64_peak)",
                 "traffic": (DRAM_BYTES_PER_POINT[args.workload] * w.nodes
-                            if DRAM_BYTES_PER_POINT[args.workload] else None)}
+                            if DRAM_BYTES_PER_POINT[args.workload] else None),
+                "fp64_issue_frac": issue_frac(FP64_THREAD_INSTS[args.workload], w.nodes, launch_ms, peak_fp64)}
     else:
         roof = {"bound": "fp64", "achieved": None, "peak": peak_fp64, "unit": "TFLOP/s", "frac": None,
                 "peak_source": "measured (DFMA probe)", "traffic": None}
@@ -956,6 +972,7 @@ def main():
             v["fp64_flops_per_marker"] = FP64_FLOPS_PER_MARKER[name]
             v["fp64_achieved_tflops"] = FP64_FLOPS_PER_MARKER[name] * nmk / (v["kernel_ms_per_call"] * 1e-3) / 1e12
             v["fp64_frac"] = v["fp64_achieved_tflops"] / peak_fp64
+            v["fp64_issue_frac"] = issue_frac(FP64_THREAD_INSTS.get(name), nmk, v["kernel_ms_per_call"], peak_fp64)
 
     if configs is not None:
         a = configs["aniso_4097"]
@@ -963,14 +980,18 @@ def main():
         a["roofline"] = {"bound": "fp64", "achieved": fl, "peak": peak_fp64, "unit": "TFLOP/s",
                          "frac": fl / peak_fp64, "peak_source": "measured (DFMA probe)",
                          "traffic": DRAM_BYTES_PER_POINT["aniso"] * a["nodes"],
-                         "hbm_achieved_gbs": a["algorithmic_bytes_per_sweep"] / (a["kernel_ms_per_sweep"] * 1e-3) / 1e9}
+                         "hbm_achieved_gbs": a["algorithmic_bytes_per_sweep"] / (a["kernel_ms_per_sweep"] * 1e-3) / 1e9,
+                         "fp64_issue_frac": issue_frac(FP64_THREAD_INSTS["aniso"], a["nodes"],
+                                                       a["kernel_ms_per_sweep"], peak_fp64)}
         m = configs["many_grids_64"]
         per_call = FP64_FLOPS_PER_PHASE_CALL["many_grids"]
         g = m["graph"]["default"]
         if per_call:
             fl = per_call * g["phase_calls_per_sweep"] / (g["ms_per_sweep"] * 1e-3) / 1e12
             m["roofline"] = {"bound": "fp64", "achieved": fl, "peak": peak_fp64, "unit": "TFLOP/s",
-                             "frac": fl / peak_fp64, "peak_source": "measured (DFMA probe)", "traffic": None}
+                             "frac": fl / peak_fp64, "peak_source": "measured (DFMA probe)", "traffic": None,
+                             "fp64_issue_frac": issue_frac(FP64_THREAD_INSTS["many_grids"],
+                                                           g["phase_calls_per_sweep"], g["ms_per_sweep"], peak_fp64)}
         else:
             m["roofline"] = {"bound": "fp64", "achieved": None, "peak": peak_fp64, "unit": "TFLOP/s", "frac": None,
                              "peak_source": "measured (DFMA probe)", "traffic": None}
