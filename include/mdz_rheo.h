@@ -71,7 +71,11 @@ extern "C" {
 #define MDZ_EMARKER_OUT     -22  /* marker beyond the vertex grid in x (ParticleRoutines.c:1258-1266, exit 89) */
 
 /* memory space of the field pointers handed to a sweep */
-#define MDZ_MEM_HOST   0  /* host memory: the library copies in and out (drop-in mode) */
+#define MDZ_MEM_HOST   0  /* host memory (drop-in mode): the library copies in and out, except
+                             that page-locked arrays the device addresses at the same pointer
+                             are read and written in place over the host link by the sweeps,
+                             the operators, the strain rates and the input preparation (the
+                             marker calls always copy); MDZ_SWEEP_STAGED forces the copies */
 #define MDZ_MEM_DEVICE 1  /* device memory of the context's GPU: no copies */
 
 /* sweep flags */
@@ -209,8 +213,9 @@ typedef struct mdz_sweep_stats {
   int32_t  status;           /* MDZ_OK or the first error code met */
   int64_t  error_node;       /* node of that error: centroid c0, or Nc + c1 for a vertex; -1 if none */
   double   elapsed_ms;       /* device time of the sweep kernels (CUDA events) */
-  uint64_t h2d_bytes;        /* bytes copied host->device by this call (MDZ_MEM_HOST) */
-  uint64_t d2h_bytes;        /* bytes copied device->host by this call (MDZ_MEM_HOST) */
+  uint64_t h2d_bytes;        /* bytes moved host->device by this call (MDZ_MEM_HOST): copied, or
+                                read in place from page-locked arrays */
+  uint64_t d2h_bytes;        /* bytes moved device->host by this call (MDZ_MEM_HOST) */
   uint32_t kernel_launches;  /* kernels this call launched */
   uint32_t mma_fault;        /* warm start: a tensor-core wait gave up; those items used the plain start */
   uint64_t fp32_steps;       /* FP32 Newton steps taken by the starts of the local solves */

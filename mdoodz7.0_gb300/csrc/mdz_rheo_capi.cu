@@ -256,14 +256,26 @@ enum { S_CI = 0, S_VI = S_CI + CI_COUNT, S_CO = S_VI + VI_COUNT, S_VO = S_CO + C
        S_ES = S_EN + MDZ_MAX_PHASES, S_BCP = S_ES + MDZ_MAX_PHASES, S_BCG, S_OP, S_SR = S_OP + OP_COUNT,
        S_SRU = S_SR + SR_COUNT, S_SRV, S_PREP, S_MK = S_PREP + 16, S_P2M = S_MK + 33, S_COUNT = S_P2M + 12 };
 
+bool host_mapped(const void *p, size_t bytes);
+
+// Device copies of host arrays, one slot per array.  With `direct`, a page-locked host
+// array that the device addresses at the same pointer (host_mapped) is used in place: the
+// kernels read and write it over the host link, and its bytes count as crossing it.
 struct Mirror {
   mdz_rheo_ctx *ctx;
+  bool direct = false;
   int err = MDZ_OK;
-  // upload (if host) a read-only array of n elements of `es` bytes into slot s
+  template <class T>
+  bool mapped(const T *h, size_t n) const { return direct && host_mapped(h, n * sizeof(T)); }
+  // upload (if host) a read-only array of n elements into slot s
   template <class T>
   T *in(const T *h, int slot, size_t n, bool host) {
     if (!h || err) return const_cast<T *>(h);
     if (!host) return const_cast<T *>(h);
+    if (mapped(h, n)) {
+      ctx->h2d += n * sizeof(T);
+      return const_cast<T *>(h);
+    }
     if ((err = ensure(ctx->bufs[slot], n * sizeof(T))) != MDZ_OK) return nullptr;
     if (cudaMemcpyAsync(ctx->bufs[slot].p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
       err = MDZ_ECUDA;
@@ -273,13 +285,18 @@ struct Mirror {
   template <class T>
   T *out(T *h, int slot, size_t n, bool host) {
     if (!h || err) return h;
-    if (!host) return h;
+    if (!host || mapped(h, n)) return h;
     if ((err = ensure(ctx->bufs[slot], n * sizeof(T))) != MDZ_OK) return nullptr;
     return (T *)ctx->bufs[slot].p;
   }
+  // an array that was `in` or `out`: copy it back unless the kernels wrote it in place
   template <class T>
   void back(T *h, int slot, size_t n, bool host) {
     if (!h || err || !host) return;
+    if (mapped(h, n)) {
+      ctx->d2h += n * sizeof(T);
+      return;
+    }
     if (cudaMemcpyAsync(h, ctx->bufs[slot].p, n * sizeof(T), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess)
       err = MDZ_ECUDA;
     ctx->d2h += n * sizeof(T);
@@ -669,7 +686,7 @@ void fold_soft(const mdz_prep_materials *m, int p, SoftPhase &P) {
 bool prep_common(const mdz_model *md, const mdz_prep_materials *mat, const mdz_prep_fields *f, int mem, int flags) {
   if (!md || !mat || !f) return false;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return false;
-  if (flags & ~MDZ_SWEEP_ASYNC) return false;
+  if (flags & ~(MDZ_SWEEP_ASYNC | MDZ_SWEEP_STAGED)) return false;
   if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return false;
   if (md->Nx < 2 || md->Nz < 2 || md->Nb_phases < 1 || md->Nb_phases > MDZ_MAX_PHASES) return false;
   if (!f->phase_perc_n || !f->phase_perc_s || !f->BCp_type || !f->BCg_type) return false;
@@ -1464,7 +1481,7 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materia
                        mdz_sweep_stats *st) {
   if (!ctx || !md || !mat || !f || !ops) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
-  if (flags & ~(MDZ_SWEEP_REF_START | MDZ_OPS_PER_NODE)) return MDZ_EINVAL;
+  if (flags & ~(MDZ_SWEEP_REF_START | MDZ_OPS_PER_NODE | MDZ_SWEEP_STAGED)) return MDZ_EINVAL;
   if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
   CK(cudaSetDevice(ctx->device));
   static thread_local OpArgs A;
@@ -1492,7 +1509,7 @@ int mdz_rheo_operators(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_materia
   for (int i = 0; i < OP_COUNT; i++) if (i != OP_DRHODP && !dout[i]) return MDZ_EINVAL;
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};
+  Mirror mi{ctx, !(flags & MDZ_SWEEP_STAGED)};
   for (int i = 0; i < L.nci; i++) A.ci[i] = mi.in(L.cin[i], S_CI + i, Nc, host);
   for (int i = 0; i < L.nvi; i++) A.vi[i] = mi.in(L.vin[i], S_VI + i, Nv, host);
   for (int p = 0; p < A.M.np; p++) {
@@ -1531,7 +1548,7 @@ int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *md, double dx, dou
                           double compressible, mdz_strain_rate_fields *sr, int mem, int flags, mdz_sweep_stats *st) {
   if (!ctx || !md || !sr) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
-  if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
+  if (flags & ~(MDZ_SWEEP_ASYNC | MDZ_SWEEP_STAGED)) return MDZ_EINVAL;
   if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
   if (md->Nx < 2 || md->Nz < 2) return MDZ_EINVAL;
   double *out[SR_COUNT] = {sr->div_u, sr->exxd, sr->ezzd, sr->exz_n, sr->wxz_n,
@@ -1551,7 +1568,7 @@ int mdz_rheo_strain_rates(mdz_rheo_ctx *ctx, const mdz_model *md, double dx, dou
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};
+  Mirror mi{ctx, !(flags & MDZ_SWEEP_STAGED)};
   A.u = mi.in(sr->u_in, S_SRU, Nx * (Nz + 1), host);
   A.v = mi.in(sr->v_in, S_SRV, (Nx + 1) * Nz, host);
   A.bcp = mi.in(sr->BCp_type, S_BCP, Nc, host);
@@ -1618,7 +1635,7 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};
+  Mirror mi{ctx};  // marker arrays are always staged
   A.xg = mi.in(g->xg_coord, S_MK + 8, Nx, host);
   A.zg = mi.in(g->zg_coord, S_MK + 9, Nz, host);
   A.xvz = mi.in(g->xvz_coord, S_MK + 10, Nx + 1, host);
@@ -1749,7 +1766,7 @@ int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_marker_g
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};
+  Mirror mi{ctx};  // marker arrays are always staged
   A.x = mi.in(mk->x, S_P2M + 0, n, host);
   A.z = mi.in(mk->z, S_P2M + 1, n, host);
   A.phase = mi.in((const int *)mk->phase, S_P2M + 2, n, host);
@@ -1812,7 +1829,7 @@ int mdz_rheo_softening(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_prep_ma
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};
+  Mirror mi{ctx, !(flags & MDZ_SWEEP_STAGED)};
   for (int p = 0; p < A.np; p++) {
     A.perc_n[p] = mi.in(f->phase_perc_n[p], S_PN + p, Nc, host);
     A.perc_s[p] = mi.in(f->phase_perc_s[p], S_PS + p, Nv, host);
@@ -1865,7 +1882,7 @@ int mdz_rheo_shear_modulus(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_pre
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};
+  Mirror mi{ctx, !(flags & MDZ_SWEEP_STAGED)};
   for (int p = 0; p < A.np; p++) {
     A.perc_n[p] = mi.in(f->phase_perc_n[p], S_PN + p, Nc, host);
     A.perc_s[p] = mi.in(f->phase_perc_s[p], S_PS + p, Nv, host);

@@ -24,6 +24,7 @@
  * environment variable MDZ_RHEO_DEVICE (default 0).  Like the reference, the calls
  * are blocking and are made from one host thread.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -186,7 +187,12 @@ void RheologicalOperators(grid *mesh, params *model, mat_prop *materials, scale 
   memset(&st, 0, sizeof(st));
   const int rc = mdz_rheo_operators(mdz_context(), &md, &mt, &f, &ops, Jacobian, (int)model->compressible,
                                     anisotropy, MDZ_MEM_HOST, 0, &st);
-  if (rc == MDZ_ENONFINITE) { fprintf(stderr, "EXIT: D34 is NAN!\n"); exit(1); } /* :384-385 */
+  if (rc == MDZ_ENONFINITE) { /* :375-376, by the value at the first such vertex */
+    const int64_t v = st.error_node - (int64_t)(mesh->Nx - 1) * (mesh->Nz - 1);
+    const int inf = v >= 0 && v < (int64_t)mesh->Nx * mesh->Nz && isinf(mesh->D34_s[v]);
+    fprintf(stderr, inf ? "EXIT: D34 is INF!\n" : "EXIT: D34 is NAN!\n");
+    exit(1);
+  }
   if (rc != MDZ_OK) mdz_fail(rc, &st);
 }
 

@@ -1,0 +1,108 @@
+"""Page-locked host arrays used in place by the grid entry points other than the sweep.
+
+RheologicalOperators, StrainRateComponents and the input preparation (softening, shear
+modulus) read and write page-locked host arrays that the device addresses at the same
+pointer directly, without device copies; any other array, or MDZ_SWEEP_STAGED, goes through
+the context's device mirrors.  Each case checks that the three forms (in place, staged by
+the flag, pageable) give the same bits and the same byte counts, and that the in-place call
+allocates no mirrors (free device memory of a fresh context) while the staged one does.
+"""
+import numpy as np
+import pytest
+
+import mdz_rheo as R
+import mdz_workloads as W
+from common import clone
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+MiB = 1 << 20
+
+
+def pinned(d):
+    return {k: (None if v is None else [torch.from_numpy(np.array(x, copy=True)).pin_memory() for x in v]
+                if isinstance(v, list) else torch.from_numpy(np.array(v, copy=True)).pin_memory())
+            for k, v in d.items()}
+
+
+def as_numpy(d):
+    return {k: (None if v is None else [x.numpy() if hasattr(x, "numpy") else x for x in v]
+                if isinstance(v, list) else (v.numpy() if hasattr(v, "numpy") else v)) for k, v in d.items()}
+
+
+def free_bytes():
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info(0)[0]
+
+
+def three_ways(call, arrays):
+    """(in place, staged by the flag, pageable): outputs, statistics, device bytes the
+    call took in a fresh context."""
+    out = []
+    for form in ("in_place", "flag", "pageable"):
+        a = pinned(arrays) if form != "pageable" else clone(arrays)
+        ctx = R.Context(0)
+        f0 = free_bytes()
+        rc, st = call(ctx, a, R.SWEEP_STAGED if form == "flag" else 0)
+        used = f0 - free_bytes()
+        ctx.close()
+        assert rc == R.MDZ_OK, form
+        out.append((as_numpy(a), st, used))
+    return out
+
+
+def check_same(res, keys):
+    (a, sa, ua), (b, sb, ub), (c, sc, uc) = res
+    for k in keys:
+        if a.get(k) is None:
+            continue
+        x, y, z = (np.concatenate(v) if isinstance(v, list) else v for v in (a[k], b[k], c[k]))
+        assert np.array_equal(x, y, equal_nan=True) and np.array_equal(x, z, equal_nan=True), k
+    assert (sa.h2d_bytes, sa.d2h_bytes) == (sb.h2d_bytes, sb.d2h_bytes) == (sc.h2d_bytes, sc.d2h_bytes)
+    assert sa.h2d_bytes > 0 and sa.d2h_bytes > 0
+    # in place: no mirrors; staged: one per array (tens of MiB here)
+    assert ua <= 8 * MiB, ua
+    assert ub >= 32 * MiB and uc >= 32 * MiB, (ub, uc)
+
+
+@pytest.mark.parametrize("jac", [0, 1])
+def test_operators_in_place(jac):
+    big = W.plain_large(seed=5, ncx=400, ncz=360)
+    c = R.Context(0)
+    c.sweep(big.model, big.mat, R.FieldSet(big.arrays))  # the state the operator linearises
+    c.close()
+    arrays = dict(big.arrays)
+    ops = R.alloc_operator_fields(big.Nc, big.Nv)
+    for k in ops:
+        ops[k][:] = 3.0
+    arrays.update({"op_" + k: v for k, v in ops.items()})
+
+    def call(ctx, a, flags):
+        fields = {k: v for k, v in a.items() if not k.startswith("op_")}
+        o = {k[3:]: v for k, v in a.items() if k.startswith("op_")}
+        return ctx.operators(big.model, big.mat, R.FieldSet(fields), o, jacobian=jac, flags=flags)
+
+    res = three_ways(call, arrays)
+    check_same(res, ["op_" + k for k in R.OPS_N + R.OPS_S])
+
+
+def test_strain_rates_in_place():
+    w = W.velocity_field(seed=8, ncx=700, ncz=650, air=0.2, periodic=1)
+    res = three_ways(lambda ctx, a, flags: ctx.strain_rates(w.model, w.info["dx"], w.info["dz"], a,
+                                                             out_of_plane=1, compressible=1.0, flags=flags),
+                     w.arrays)
+    check_same(res, R.SR_N + R.SR_S)
+
+
+@pytest.mark.parametrize("step", ["softening", "shear_modulus"])
+def test_input_preparation_in_place(step):
+    w = W.prep_workload(seed=9, ncx=700, ncz=650, nphases=4, air=0.1, periodic=1)
+
+    def call(ctx, a, flags):
+        if step == "softening":
+            return ctx.softening(w.model, w.mat, R.PrepFieldSet(a), 1, 0, 1, flags=flags)
+        return ctx.shear_modulus(w.model, w.mat, R.PrepFieldSet(a), flags=flags)
+
+    res = three_ways(call, w.arrays)
+    check_same(res, [k for k in w.arrays if k not in ("phase_perc_n", "phase_perc_s", "BCp_type", "BCg_type")])
