@@ -28,7 +28,8 @@ HBM (3.3 GB of fields, larger than the 129 MB L2, so no flush between steps);
 `e2e` is the same sweep through the C ABI on page-locked host arrays, which the kernels
 read and write over the coherent host link inside the timed region (no staging copies);
 the line also carries the staged forms (host<->device copies in row bands, and in one
-piece).  Under torchrun each rank sweeps its own grid
+piece) and the same calls on ordinary pageable arrays (read in place where the GPU reads
+pageable memory through the host page tables).  Under torchrun each rank sweeps its own grid
 (independent instances, weak scaling; the path has no exchange step).
 """
 from __future__ import annotations
@@ -725,6 +726,21 @@ def main():
                "staged_row_bands": staged(0),
                "staged_one_band": staged(1)}
         del h, fh
+        # the same calls on ordinary pageable host arrays, as a simulation code allocates them
+        pg = {k: ([x.copy() for x in v] if isinstance(v, list) else v.copy()) for k, v in w.arrays.items()}
+        fpg = R.FieldSet(pg)
+        sweep(w.model, w.mat, fpg, mem=R.MEM_HOST)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            _, pst = sweep(w.model, w.mat, fpg, mem=R.MEM_HOST)
+        e1.record(stream)
+        barrier()
+        pg_ms = REP.max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
+        e2e["pageable_arrays"] = {"value": REP.whole_job_rate(w.nodes, ws, pg_ms), "ms_per_step": pg_ms,
+                                  "in_place": bool(ctx.pageable_in_place()),
+                                  "kernel_launches_per_step": int(pst.kernel_launches)}
+        del pg, fpg
 
     # ---- the reference's own start point (same kernel, same tolerance) ----
     ref_r = summary(timed(R.SWEEP_REF_START))

@@ -72,10 +72,13 @@ extern "C" {
 
 /* memory space of the field pointers handed to a sweep */
 #define MDZ_MEM_HOST   0  /* host memory (drop-in mode): the library copies in and out, except
-                             that page-locked arrays the device addresses at the same pointer
-                             are read and written in place over the host link by the sweeps,
-                             the operators, the strain rates and the input preparation (the
-                             marker calls always copy); MDZ_SWEEP_STAGED forces the copies */
+                             that arrays the device can address -- page-locked arrays mapped at
+                             the same pointer, and any pageable array where the GPU reads
+                             pageable memory through the host page tables (Grace-Blackwell;
+                             mdz_rheo_host_access) -- are read and written in place over the
+                             host link by the sweeps, the operators, the strain rates and the
+                             input preparation (the marker calls always copy);
+                             MDZ_SWEEP_STAGED forces the copies */
 #define MDZ_MEM_DEVICE 1  /* device memory of the context's GPU: no copies */
 
 /* sweep flags */
@@ -285,6 +288,12 @@ int mdz_rheo_sync(mdz_rheo_ctx *ctx, mdz_sweep_stats *stats);
  * one band overlap the kernels of the others (with page-locked host arrays).  bands = 0
  * picks rows / 128, at most 16; 1 to 16 fixes the count.  Results do not depend on it. */
 int mdz_rheo_set_host_bands(mdz_rheo_ctx *ctx, int bands);
+/* *pageable = 1 where the context's GPU reads and writes pageable host memory (malloc,
+ * new, mmap) in place through the host's page tables (the attribute
+ * cudaDevAttrPageableMemoryAccessUsesHostPageTables, as on Grace-Blackwell), so that
+ * MDZ_MEM_HOST calls use ordinary host arrays without copies; 0 where only page-locked
+ * arrays are used in place. */
+int mdz_rheo_host_access(mdz_rheo_ctx *ctx, int *pageable);
 
 /* ---- the hot path --------------------------------------------------- */
 /* NonNewtonianViscosityGrid: vertex interpolation of T, p_in, d0, phi0, then

@@ -478,21 +478,51 @@ int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &
   return MDZ_OK;
 }
 
-// Host arrays the kernels can address directly: page-locked memory mapped into the device's
-// address space at the same address (cudaHostAlloc, cudaMallocHost, or cudaHostRegister of
-// the whole array), checked at the array's first and last byte.  On a Grace-Blackwell
-// system the host link (NVLink-C2C) is coherent and fast enough that the sweep reads its
-// inputs and writes its outputs there during the kernels at nearly the speed of device
+// Whether the current device reads and writes pageable host memory (malloc, new, mmap)
+// through the host's page tables, as the GPU of a Grace-Blackwell system does over its
+// coherent NVLink-C2C link (cudaDevAttrPageableMemoryAccessUsesHostPageTables); cached per
+// device.
+bool pageable_in_place() {
+  static int cached[64];
+  static bool init = false;
+  if (!init) {
+    for (int &c : cached) c = -1;
+    init = true;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return false;
+  }
+  if (cached[dev] < 0) {
+    int a = 0, b = 0;
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) a = 0;
+    if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) b = 0;
+    cudaGetLastError();
+    cached[dev] = (a == 1 && b == 1) ? 1 : 0;
+  }
+  return cached[dev] == 1;
+}
+
+// Host arrays the kernels can address directly, checked at the array's first and last
+// byte: page-locked memory mapped into the device's address space at the same address
+// (cudaHostAlloc, cudaMallocHost, or cudaHostRegister of the whole array), and, where the
+// device reads pageable memory through the host page tables, ordinary pageable memory.  On
+// a Grace-Blackwell system the host link is coherent and fast enough that the sweep reads
+// its inputs and writes its outputs there during the kernels at nearly the speed of device
 // memory (the kernels are bound by the FP64 pipe), with no staging copies.
 bool host_mapped(const void *p, size_t bytes) {
   if (!p || !bytes) return true;
   const void *ends[2] = {p, (const char *)p + (bytes - 1)};
   for (const void *q : ends) {
     cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, q) != cudaSuccess || a.type != cudaMemoryTypeHost || a.devicePointer != q) {
+    if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
       cudaGetLastError();
       return false;
     }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer == q) continue;
+    if (a.type == cudaMemoryTypeUnregistered && pageable_in_place()) continue;
+    return false;
   }
   return true;
 }
@@ -966,6 +996,13 @@ int mdz_rheo_destroy(mdz_rheo_ctx *c) {
 int mdz_rheo_set_host_bands(mdz_rheo_ctx *c, int bands) {
   if (!c || bands < 0 || bands > kMaxBands) return MDZ_EINVAL;
   c->bands = bands;
+  return MDZ_OK;
+}
+
+int mdz_rheo_host_access(mdz_rheo_ctx *c, int *pageable) {
+  if (!c || !pageable) return MDZ_EINVAL;
+  CK(cudaSetDevice(c->device));
+  *pageable = pageable_in_place() ? 1 : 0;
   return MDZ_OK;
 }
 

@@ -391,6 +391,7 @@ def load_library(path: str = LIB_PATH):
     lib.mdz_rheo_destroy.argtypes = [C.c_void_p]
     lib.mdz_rheo_set_stream.argtypes = [C.c_void_p, C.c_void_p]
     lib.mdz_rheo_set_host_bands.argtypes = [C.c_void_p, C.c_int]
+    lib.mdz_rheo_host_access.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     lib.mdz_rheo_sync.argtypes = [C.c_void_p, C.POINTER(SweepStats)]
     for fn in (lib.mdz_rheo_sweep, lib.mdz_rheo_sweep_aniso):
         fn.argtypes = [C.c_void_p, C.POINTER(Model), C.POINTER(Materials), C.POINTER(GridFields),
@@ -647,6 +648,14 @@ class Context:
         rc = self.lib.mdz_rheo_set_stream(self.handle, stream_ptr)
         if rc != MDZ_OK:
             raise RheoError(rc, "mdz_rheo_set_stream")
+
+    def pageable_in_place(self) -> bool:
+        """Whether MDZ_MEM_HOST calls use ordinary pageable host arrays in place."""
+        v = C.c_int()
+        rc = self.lib.mdz_rheo_host_access(self.handle, C.byref(v))
+        if rc != MDZ_OK:
+            raise RheoError(rc, "mdz_rheo_host_access")
+        return bool(v.value)
 
     def set_host_bands(self, bands: int = 0):
         """Row bands of host-memory sweeps (0: automatic)."""

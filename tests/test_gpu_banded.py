@@ -1,6 +1,8 @@
-"""Sweeps of host arrays in row bands (copies overlapping the kernels) against the
+"""Sweeps of host arrays staged in row bands (copies overlapping the kernels) against the
 one-shot host sweep and the device-resident sweep: every output bit for bit, for any
-band count, with periodic x, air rows and uneven band edges."""
+band count, with periodic x, air rows and uneven band edges; and host arrays that the
+kernels read and write in place.  MDZ_SWEEP_STAGED makes the banded path run where the GPU
+could address the arrays directly."""
 import numpy as np
 import pytest
 
@@ -53,7 +55,7 @@ def test_banded_host_sweep_is_the_one_shot_sweep(ctx, name):
     fn = ctx.sweep_aniso if aniso else ctx.sweep
     ctx.set_host_bands(1)
     one = clone(w.arrays)
-    _, st1 = fn(w.model, w.mat, R.FieldSet(one))
+    _, st1 = fn(w.model, w.mat, R.FieldSet(one), flags=R.SWEEP_STAGED)
     assert st1.kernel_launches == 2  # the centroid kernel and the vertex kernel
     # the device-resident sweep on the same inputs
     dev = {k: ([torch.from_numpy(x.copy()).cuda() for x in v] if isinstance(v, list) else
@@ -63,7 +65,7 @@ def test_banded_host_sweep_is_the_one_shot_sweep(ctx, name):
     for bands in (2, 3, 7, 16):
         ctx.set_host_bands(bands)
         got = clone(w.arrays)
-        _, st = fn(w.model, w.mat, R.FieldSet(got))
+        _, st = fn(w.model, w.mat, R.FieldSet(got), flags=R.SWEEP_STAGED)
         # a vertex kernel per band and a centroid kernel per band with centroid rows (all but
         # a last band holding only the last vertex row)
         assert 2 * min(bands, w.model.Nz) - 1 <= st.kernel_launches <= 2 * min(bands, w.model.Nz)
@@ -80,9 +82,9 @@ def test_banded_sweep_reports_the_failing_node(ctx):
     c1 = w.model.Nx * 150 + 7  # a vertex in the fourth of five bands
     w.arrays["exz"][c1] = np.nan
     ctx.set_host_bands(1)
-    rc1, st1 = ctx.sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), check=False)
+    rc1, st1 = ctx.sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), flags=R.SWEEP_STAGED, check=False)
     ctx.set_host_bands(5)
-    rc5, st5 = ctx.sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), check=False)
+    rc5, st5 = ctx.sweep(w.model, w.mat, R.FieldSet(clone(w.arrays)), flags=R.SWEEP_STAGED, check=False)
     ctx.set_host_bands(0)
     assert rc1 == rc5 and st1.status == st5.status and st1.error_node == st5.error_node
 
@@ -133,15 +135,26 @@ def test_direct_sweep_of_page_locked_host_arrays(ctx, aniso):
     assert st_d.phase_calls == st_s.phase_calls
 
 
-def test_partly_page_locked_arrays_are_staged(ctx):
-    """One pageable array among page-locked ones: the sweep stages everything (bands)."""
+def test_pageable_arrays(ctx):
+    """One pageable array among page-locked ones, and all arrays pageable: in place where the
+    GPU reads pageable memory through the host page tables (two launches), else the sweep
+    stages everything (bands); the same bits as the staged sweep either way."""
     w = W.plain_large(seed=42, ncx=200, ncz=260)
-    arrays = pinned(clone(w.arrays))
-    arrays["T"] = torch.from_numpy(w.arrays["T"].copy())  # pageable
-    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(arrays))
-    assert rc == R.MDZ_OK and st.kernel_launches > 2
+    ctx.set_host_bands(0)
+    in_place = ctx.pageable_in_place()
     ref = clone(w.arrays)
-    ctx.sweep(w.model, w.mat, R.FieldSet(ref))
-    for k in R.CEN_OUT + R.VER_OUT:
-        if ref.get(k) is not None:
-            assert np.array_equal(arrays[k].numpy(), ref[k], equal_nan=True), k
+    rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(ref), flags=R.SWEEP_STAGED)
+    assert rc == R.MDZ_OK and st.kernel_launches > 2
+    mixed = pinned(clone(w.arrays))
+    mixed["T"] = torch.from_numpy(w.arrays["T"].copy())  # pageable
+    plain = clone(w.arrays)  # numpy: pageable
+    for arrays in (mixed, plain):
+        rc, st = ctx.sweep(w.model, w.mat, R.FieldSet(arrays))
+        assert rc == R.MDZ_OK
+        assert (st.kernel_launches == 2) if in_place else (st.kernel_launches > 2)
+        got = host_view(arrays) if arrays is mixed else arrays
+        for k in R.VER_INTERP + R.CEN_OUT + R.VER_OUT + ["phase_eta_n", "phase_eta_s"]:
+            if ref.get(k) is None:
+                continue
+            x, y = (np.concatenate(v) if isinstance(v, list) else v for v in (got[k], ref[k]))
+            assert np.array_equal(x, y, equal_nan=True), k
