@@ -918,6 +918,30 @@ def main():
                              "markers_per_s": REP.whole_job_rate(nmk, ws, ms),
                              "algorithmic_bytes_per_call": nbytes,
                              "hbm_achieved_gbs": nbytes / (statistics.mean(k_ms) * 1e-3) / 1e9}
+        # the default options end to end on ordinary pageable host arrays, as the drop-in
+        # passes them: read and written in place where the GPU reads pageable memory through
+        # the host page tables, and staged through device copies (MDZ_SWEEP_STAGED)
+        opts = R.MarkerOpts()
+        (opts.elastic, opts.stress_rotation, opts.anisotropy, opts.advection, opts.interp_stencil,
+         opts.subgrid_diffusion) = variants["jaumann_stencil1"]
+        opts.set_G(mw.info["G"])
+        gh = {k: v.copy() for k, v in mw.arrays.items()}
+        mh = {k: v.copy() for k, v in mw.info["markers"].items()}
+        for label, fl in (("e2e_pageable", 0), ("e2e_pageable_staged", R.SWEEP_STAGED)):
+            ctx.marker_stress(mw.model, opts, gh, mh, mw.info["dx"], mw.info["dz"], flags=fl)
+            barrier()
+            reps = max(2, args.steps // 2)
+            e0.record(stream)
+            for _ in range(reps):
+                _, hst = ctx.marker_stress(mw.model, opts, gh, mh, mw.info["dx"], mw.info["dz"], flags=fl)
+            e1.record(stream)
+            barrier()
+            ms = REP.max_over_ranks(e0.elapsed_time(e1), dev) / reps
+            markers["jaumann_stencil1"][label] = {
+                "ms_per_call": ms, "markers_per_s": REP.whole_job_rate(nmk, ws, ms),
+                "in_place": bool(fl == 0 and ctx.pageable_in_place()),
+                "h2d_bytes_per_call": int(hst.h2d_bytes), "d2h_bytes_per_call": int(hst.d2h_bytes)}
+        del gh, mh
         # P2Mastah of a marker array onto the centroids and the vertices (the plastic strain
         # of CohesionFrictionDilationGrid), device-resident
         vals = torch.rand(nmk, dtype=torch.float64, device=dev)

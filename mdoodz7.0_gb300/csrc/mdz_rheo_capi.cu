@@ -1636,7 +1636,7 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
                            mdz_markers *mk, int mem, int flags, mdz_sweep_stats *st) {
   if (!ctx || !md || !o || !g || !mk) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
-  if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
+  if (flags & ~(MDZ_SWEEP_ASYNC | MDZ_SWEEP_STAGED)) return MDZ_EINVAL;
   if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
   if (md->Nx < 2 || md->Nz < 2 || mk->n < 0 || mk->n > 0x7fffffffLL) return MDZ_EINVAL;
   if (o->interp_stencil != 1 && o->interp_stencil != 9) return MDZ_EINVAL;
@@ -1672,7 +1672,7 @@ int mdz_rheo_marker_stress(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_mar
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};  // marker arrays are always staged
+  Mirror mi{ctx, !(flags & MDZ_SWEEP_STAGED)};
   A.xg = mi.in(g->xg_coord, S_MK + 8, Nx, host);
   A.zg = mi.in(g->zg_coord, S_MK + 9, Nz, host);
   A.xvz = mi.in(g->xvz_coord, S_MK + 10, Nx + 1, host);
@@ -1782,7 +1782,7 @@ int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_marker_g
                       int flags, mdz_sweep_stats *st) {
   if (!ctx || !md || !g || !mk || !values || (!node_n && !node_s)) return MDZ_EINVAL;
   if (mem != MDZ_MEM_HOST && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
-  if (flags & ~MDZ_SWEEP_ASYNC) return MDZ_EINVAL;
+  if (flags & ~(MDZ_SWEEP_ASYNC | MDZ_SWEEP_STAGED)) return MDZ_EINVAL;
   if ((flags & MDZ_SWEEP_ASYNC) && mem != MDZ_MEM_DEVICE) return MDZ_EINVAL;
   if (md->Nx < 2 || md->Nz < 2 || md->Nb_phases < 1 || mk->n < 0 || mk->n > 0x7fffffffLL) return MDZ_EINVAL;
   if (avg < 0 || avg > 2 || (interp_stencil != 1 && interp_stencil != 9)) return MDZ_EINVAL;
@@ -1803,7 +1803,7 @@ int mdz_rheo_p2mastah(mdz_rheo_ctx *ctx, const mdz_model *md, const mdz_marker_g
   const bool host = (mem == MDZ_MEM_HOST);
   ctx->h2d = ctx->d2h = 0;
   ctx->launches = 0;
-  Mirror mi{ctx};  // marker arrays are always staged
+  Mirror mi{ctx, !(flags & MDZ_SWEEP_STAGED)};
   A.x = mi.in(mk->x, S_P2M + 0, n, host);
   A.z = mi.in(mk->z, S_P2M + 1, n, host);
   A.phase = mi.in((const int *)mk->phase, S_P2M + 2, n, host);
