@@ -76,8 +76,9 @@ extern "C" {
                              the same pointer, and any pageable array where the GPU reads
                              pageable memory through the host page tables (Grace-Blackwell;
                              mdz_rheo_host_access) -- are read and written in place over the
-                             host link by every grid and marker call; MDZ_SWEEP_STAGED forces
-                             the copies */
+                             host link by every call but mdz_rheo_points_static, which stages
+                             through its static array; MDZ_SWEEP_STAGED forces the copies where
+                             a call takes flags */
 #define MDZ_MEM_DEVICE 1  /* device memory of the context's GPU: no copies */
 
 /* sweep flags */

@@ -1045,10 +1045,14 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
   A.stats = c->d_stats;
   if (n == 0) return MDZ_OK;
   const bool host = (mem == MDZ_MEM_HOST);
+  c->h2d = c->d2h = 0;
   std::vector<void *> tmp;
+  // host arrays the device can address (host_mapped) are used in place; others are copied
   auto up = [&](const void *h, size_t bytes) -> void * {
     if (!h) return nullptr;
     if (!host) return const_cast<void *>(h);
+    c->h2d += bytes;
+    if (host_mapped(h, bytes)) return const_cast<void *>(h);
     void *d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
     tmp.push_back(d);
@@ -1083,6 +1087,8 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
   auto dn = [&](void *h, size_t bytes) -> void * {
     if (!h) return nullptr;
     if (!host) return h;
+    c->d2h += bytes;
+    if (host_mapped(h, bytes)) return h;
     void *d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
     tmp.push_back(d);
@@ -1102,7 +1108,6 @@ int mdz_rheo_points(mdz_rheo_ctx *c, const mdz_model *md, const mdz_materials *m
     return MDZ_EINVAL;
   }
   if ((rc = reset_stats(c)) != MDZ_OK) return rc;
-  c->h2d = c->d2h = 0;
   c->launches = 1;
   CK(cudaEventRecord(c->ev0, c->stream));
   CK(launch_points(A, c->stream));
