@@ -6,6 +6,7 @@
 // table the kernels read from their constant parameter bank.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -483,25 +484,22 @@ int banded_sweep(mdz_rheo_ctx *ctx, SweepArgs &A, bool aniso, const FieldLists &
 // coherent NVLink-C2C link (cudaDevAttrPageableMemoryAccessUsesHostPageTables); cached per
 // device.
 bool pageable_in_place() {
-  static int cached[64];
-  static bool init = false;
-  if (!init) {
-    for (int &c : cached) c = -1;
-    init = true;
-  }
+  static std::atomic<int> cached[64];  // 0: not asked yet, 1: no, 2: yes
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
     cudaGetLastError();
     return false;
   }
-  if (cached[dev] < 0) {
+  int v = cached[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
     int a = 0, b = 0;
     if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) a = 0;
     if (cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) b = 0;
     cudaGetLastError();
-    cached[dev] = (a == 1 && b == 1) ? 1 : 0;
+    v = (a == 1 && b == 1) ? 2 : 1;
+    cached[dev].store(v, std::memory_order_relaxed);
   }
-  return cached[dev] == 1;
+  return v == 2;
 }
 
 // Host arrays the kernels can address directly, checked at the array's first and last
