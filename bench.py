@@ -311,8 +311,8 @@ def run_reference(args):
 
 
 def run_many_grids(args):
-    """--workload many_grids: config 3 alone (many_grids_section), its graph of 20 batched
-    sweeps with the default start as the line's value."""
+    """--workload many_grids: the 64-grid workload alone (many_grids_section), its graph of
+    20 batched sweeps with the default start as the line's value."""
     import torch
 
     import mdz_replicas as REP
@@ -385,10 +385,10 @@ def sweep_summary(ms, stats, nodes, ws):
 
 
 def aniso_section(args, ctx, dev, ws, rank, stream, barrier, no_warm):
-    """Config 4: ViscosityConciseAniso over 4097 x 4097 cells, 3 phases, on the device; the
-    default start, the reference's start and the learned warm start (a 12-input network
-    trained here on pairs the plain kernel produces from a fresh seed), and end to end
-    through the C ABI with page-locked host buffers."""
+    """The anisotropic workload: ViscosityConciseAniso over 4097 x 4097 cells, 3 phases,
+    on the device; the default start, the reference's start and the learned warm start (a
+    12-input network trained here on pairs the plain kernel produces from a fresh seed),
+    and end to end through the C ABI with page-locked host buffers."""
     import torch
 
     import mdz_replicas as REP
@@ -466,8 +466,9 @@ def many_grid_network(ctx, rank):
 
 
 def many_grids_section(args, ctx, dev, ws, rank, stream, barrier, warm=False):
-    """Config 3: 64 grids of uneven size (65-1025 cells per side, 2-5 phases, dt 1e10-1e12 s,
-    each with its own seed), device-resident.  Forms of one Picard sweep over all of them:
+    """The many-grid workload: 64 grids of uneven size (65-1025 cells per side, 2-5 phases,
+    dt 1e10-1e12 s, each with its own seed), device-resident.  Forms of one Picard sweep
+    over all of them:
     64 separate sweep calls, one batched sweep (two launches), and a CUDA graph of 20
     batched sweeps with the strain rates perturbed by +-5 % in each (fused into the
     sweep's load), with the default start and (warm) with the learned warm start, its
@@ -967,7 +968,7 @@ def main():
                              "markers_per_s": REP.whole_job_rate(nmk, ws, ms)}
         del gd, md, mw, vals, node_n, node_s
 
-    # ---- configs 4 and 3: the anisotropic sweep at 4097^2 and 64 uneven grids in one launch ----
+    # ---- the anisotropic sweep at 4097^2 and 64 uneven grids in one launch ----
     configs, mg_sample = None, None
     if not args.no_configs and not aniso:
         configs = {"aniso_4097": aniso_section(args, ctx, dev, ws, rank, stream, barrier, args.no_warm)}

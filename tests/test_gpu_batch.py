@@ -187,7 +187,7 @@ def test_warm_batch_matches_warm_single_sweeps_bitwise(ctx, network):
 
 
 def test_warm_graph_of_20_perturbed_sweeps(ctx, network):
-    """Config 3's form on a few grids: one batch of uneven grids with the learned warm start,
+    """The many-grid form on a few grids: one batch of uneven grids with the learned warm start,
     20 sweeps captured as one graph, strain rates perturbed by +-5 % in each."""
     ctx.set_warmstart(network, R.DEFAULT_START)
     ws = small_batch(seed=9, n=4)
