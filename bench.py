@@ -72,12 +72,17 @@ DRAM_BYTES_PER_POINT = {"plain_large": 414.6, "aniso": 364.2}
 # thread-level counters of one launch at 513 x 513 cells with 16 markers per cell
 # (4,210,704 markers) per option set (profiles/k_marker_update_513.md).
 FP64_FLOPS_PER_MARKER = {"jaumann_stencil1": 90.48, "analytical_director_stencil9": 218.31}
+# FP64 work of the Newton operator per perturbed local solve, same convention: one launch of
+# k_operators_compact at 513 x 513 cells (21,094,600 perturbed solves;
+# profiles/k_operators_newton_257.md).
+FP64_FLOPS_PER_OPERATOR_SOLVE = 224.7
 # FP64-pipe thread instructions (DFMA, DADD, DMUL and the few conversions; each takes a
 # pipe slot whether it carries two flops or one) per unit, from the same captures:
 # `fp64_issue_frac` = this x units / time / (measured DFMA rate / 2) is how busy the FP64
 # pipe is with useful lanes, the figure the flop fraction understates by the DADD/DMUL share.
 FP64_THREAD_INSTS = {"plain_large": 954.4, "aniso": 671.0, "many_grids": 190.0,
-                     "jaumann_stencil1": 77.23, "analytical_director_stencil9": 183.50}
+                     "jaumann_stencil1": 77.23, "analytical_director_stencil9": 183.50,
+                     "newton_operator": 148.7}
 
 
 def issue_frac(insts_per_unit, units, ms, peak_tflops):
@@ -1007,6 +1012,14 @@ def main():
     for v in list((prep or {}).values()) + list((markers or {}).values()):
         if isinstance(v, dict) and "hbm_achieved_gbs" in v:
             v["hbm_frac"] = v["hbm_achieved_gbs"] / hbm if hbm else None
+    if newton_op is not None and not aniso:  # per perturbed local solve, isotropic operator
+        solves, ms_op = newton_op["local_solves_per_launch"], newton_op["ms_per_launch"]
+        fl_op = FP64_FLOPS_PER_OPERATOR_SOLVE * solves / (ms_op * 1e-3) / 1e12
+        newton_op["roofline"] = {"bound": "fp64", "achieved": fl_op, "peak": peak_fp64, "unit": "TFLOP/s",
+                                 "frac": fl_op / peak_fp64, "peak_source": "measured (DFMA probe)",
+                                 "fp64_flops_per_solve": FP64_FLOPS_PER_OPERATOR_SOLVE,
+                                 "fp64_issue_frac": issue_frac(FP64_THREAD_INSTS["newton_operator"], solves, ms_op,
+                                                               peak_fp64)}
     for name, v in (markers or {}).items():
         if name in FP64_FLOPS_PER_MARKER:
             nmk = v["markers_per_call"]
