@@ -2010,14 +2010,23 @@ int mdz_rheo_train_mlp(mdz_rheo_ctx *c, const float *X, const float *Y, int64_t 
   if ((rc = put_weights(B, w)) != MDZ_OK) return rc;
   void *dXY = nullptr;
   int *dperm = nullptr;
+  float *dpart = nullptr;
   const size_t xb = (size_t)n * kMlpIn * sizeof(float), yb = (size_t)n * 2 * sizeof(float);
+  const size_t pb = (size_t)(cfg->batch / kMlpTile) * kGradCount * sizeof(float);  // one block per CTA of a step
   CK(cudaMalloc(&dXY, xb + yb));
   if (cudaMalloc(&dperm, keep.size() * sizeof(int)) != cudaSuccess) { cudaFree(dXY); return MDZ_ENOMEM; }
+  if (cudaMalloc(&dpart, pb) != cudaSuccess || cudaMemset(dpart, 0, pb) != cudaSuccess) {
+    cudaFree(dXY);
+    cudaFree(dperm);
+    cudaFree(dpart);
+    return MDZ_ENOMEM;
+  }
   CK(cudaMemcpy(dXY, pX, xb, cudaMemcpyHostToDevice));
   CK(cudaMemcpy((char *)dXY + xb, pY, yb, cudaMemcpyHostToDevice));
   MlpTrainArgs a;
   memset(&a, 0, sizeof(a));
   a.W = B.S;
+  a.part = dpart;
   a.X = (const float *)dXY;
   a.Y = (const float *)((char *)dXY + xb);
   a.perm = dperm;
@@ -2042,7 +2051,9 @@ int mdz_rheo_train_mlp(mdz_rheo_ctx *c, const float *X, const float *Y, int64_t 
       a.offset = off;
       a.n = off + nb;
       a.inv_batch = 1.0f / (float)nb;
-      k_mlp_step<<<(unsigned)((nb + kMlpTile - 1) / kMlpTile), kMlpTile, smem, c->stream>>>(a);
+      const int ctas = (int)((nb + kMlpTile - 1) / kMlpTile);
+      k_mlp_step<<<(unsigned)ctas, kMlpTile, smem, c->stream>>>(a);
+      k_mlp_reduce<<<(kGradCount + 255) / 256, 256, 0, c->stream>>>(a, ctas);
       MlpAdam o;
       const double frac = (double)step / (double)std::max<long long>(1, total_steps - 1);
       o.lr = (float)(cfg->lr_final + 0.5 * (cfg->lr - cfg->lr_final) * (1.0 + cos(3.14159265358979323846 * frac)));
@@ -2061,6 +2072,7 @@ int mdz_rheo_train_mlp(mdz_rheo_ctx *c, const float *X, const float *Y, int64_t 
   cudaMemcpy(&fault, B.S.fault, sizeof(int), cudaMemcpyDeviceToHost);
   cudaFree(dXY);
   cudaFree(dperm);
+  cudaFree(dpart);
   if (rc != MDZ_OK) return rc;
   if (fault) return MDZ_ECUDA;
   return get_weights(B, w);
@@ -2125,9 +2137,18 @@ int mdz_rheo_mlp_gradient(mdz_rheo_ctx *c, const mdz_mlp_weights *w, const float
     dX = (const float *)tmp;
     dY = (const float *)((char *)tmp + xb);
   }
+  const long long ctas = (n + kMlpTile - 1) / kMlpTile;
+  const size_t pb = (size_t)ctas * kGradCount * sizeof(float);
+  float *dpart = nullptr;
+  if (ctas > 0x7fffffffLL || cudaMalloc(&dpart, pb) != cudaSuccess || cudaMemset(dpart, 0, pb) != cudaSuccess) {
+    cudaFree(dpart);
+    if (tmp) cudaFree(tmp);
+    return MDZ_ENOMEM;
+  }
   MlpTrainArgs a;
   memset(&a, 0, sizeof(a));
   a.W = B.S;
+  a.part = dpart;
   a.X = dX;
   a.Y = dY;
   a.n = n;
@@ -2137,8 +2158,10 @@ int mdz_rheo_mlp_gradient(mdz_rheo_ctx *c, const mdz_mlp_weights *w, const float
   k_mlp_pack<<<(kP2 + 255) / 256, 256, 0, c->stream>>>(a);
   const size_t smem = mlp_step_smem();
   cudaFuncSetAttribute(k_mlp_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_mlp_step<<<(unsigned)((n + kMlpTile - 1) / kMlpTile), kMlpTile, smem, c->stream>>>(a);
+  k_mlp_step<<<(unsigned)ctas, kMlpTile, smem, c->stream>>>(a);
+  k_mlp_reduce<<<(kGradCount + 255) / 256, 256, 0, c->stream>>>(a, (int)ctas);
   rc = (cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(c->stream) == cudaSuccess) ? MDZ_OK : MDZ_ECUDA;
+  cudaFree(dpart);
   if (tmp) cudaFree(tmp);
   if (rc != MDZ_OK) return rc;
   int fault = 0;

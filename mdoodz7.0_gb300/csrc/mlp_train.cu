@@ -125,12 +125,14 @@ __device__ __forceinline__ float block_colsum(TrainShared &S, const float *v, in
 
 }  // namespace
 
-// Forward + backward of one tile per CTA; gradients accumulate into W.g*.
+// Forward + backward of one tile per CTA; the CTA's gradient sums go to its block of
+// a.part (k_mlp_reduce adds the blocks up).
 __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTrainArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TrainShared &S = *reinterpret_cast<TrainShared *>(smem_raw);
   const int t = threadIdx.x, w = t >> 5;
   const MlpTrainState &W = a.W;
+  float *gp = a.part + (size_t)blockIdx.x * kGradCount;
   load_weights(S, W);
   if (t == 0) { umma::mbar_init(&S.mbar, 1); S.fault = 0; S.fault_parity = 0; }
   if (w == 0) umma::tmem_alloc(&S.tmem, kTrainCols);
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
   for (int j = 0; j < kMlpOut; j++) put_bf16(S.dYt, j, t, T, dy[j]);
   {
     const float gb = block_colsum(S, dy, 2, t);
-    if (t < 2) atomicAdd(&W.gb3[t], gb);
+    if (t < 2) gp[kGradB3 + t] = gb;
   }
   sync_mma();
   // ---- backward through layer 3: dH2 = dY W3, dZ2 = dH2 * (A2 > 0); with it, in the same
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
   }
   {
     const float gb = block_colsum(S, gsum, kMlpHid, t);
-    if (t < kMlpHid) atomicAdd(&W.gb2[t], gb);
+    if (t < kMlpHid) gp[kGradB2 + t] = gb;
   }
   sync_mma();
   // ---- backward through layer 2: dH1 = dZ2 W2, dZ1 = dH1 * (A1 > 0); with it layer 2's
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
   }
   {
     const float gb = block_colsum(S, gsum, kMlpHid, t);
-    if (t < kMlpHid) atomicAdd(&W.gb1[t], gb);
+    if (t < kMlpHid) gp[kGradB1 + t] = gb;
   }
   sync_mma();
   // ---- weight gradients, reduction over the 128 samples (M = 64 tiles, K = samples);
@@ -252,15 +254,15 @@ __global__ void __launch_bounds__(128) k_mlp_step(const __grid_constant__ MlpTra
   {
     float v[16];
     umma::tmem_ld16(umma::tmem_addr(S.tmem, w, C_GW3), v);
-    if (row >= 0) { atomicAdd(&W.gW3[0 * kMlpHid + row], v[0]); atomicAdd(&W.gW3[1 * kMlpHid + row], v[1]); }
+    if (row >= 0) { gp[kGradW3 + 0 * kMlpHid + row] = v[0]; gp[kGradW3 + 1 * kMlpHid + row] = v[1]; }
     for (int c = 0; c < kMlpHid; c += 16) {
       umma::tmem_ld16(umma::tmem_addr(S.tmem, w, C_GW2 + c), v);
       if (row >= 0)
-        for (int i = 0; i < 16; i++) atomicAdd(&W.gW2[row * kMlpHid + c + i], v[i]);
+        for (int i = 0; i < 16; i++) gp[kGradW2 + row * kMlpHid + c + i] = v[i];
     }
     umma::tmem_ld16(umma::tmem_addr(S.tmem, w, C_GW1), v);
     if (row >= 0)
-      for (int i = 0; i < a.n_feat; i++) atomicAdd(&W.gW1[row * kMlpIn + i], v[i]);
+      for (int i = 0; i < a.n_feat; i++) gp[kGradW1 + row * kMlpIn + i] = v[i];
   }
   umma::fence_before_sync();
   __syncthreads();
@@ -288,6 +290,21 @@ __device__ __forceinline__ void put_tile(uint4 *tile, int r, int k, int K, float
 }
 
 }  // namespace
+
+// The step's gradient: the CTAs' blocks of a.part added in CTA order (deterministic).
+__global__ void k_mlp_reduce(const __grid_constant__ MlpTrainArgs a, int ctas) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kGradCount) return;
+  float s = 0.0f;
+  for (int c = 0; c < ctas; c++) s += a.part[(size_t)c * kGradCount + i];
+  const MlpTrainState &W = a.W;
+  if (i < kGradW2) W.gW1[i - kGradW1] = s;
+  else if (i < kGradW3) W.gW2[i - kGradW2] = s;
+  else if (i < kGradB1) W.gW3[i - kGradW3] = s;
+  else if (i < kGradB2) W.gb1[i - kGradB1] = s;
+  else if (i < kGradB3) W.gb2[i - kGradB2] = s;
+  else W.gb3[i - kGradB3] = s;
+}
 
 // One Adam step over every parameter, then the BF16 tiles; zeroes the gradients.
 __global__ void k_mlp_adam(const __grid_constant__ MlpTrainArgs a, const __grid_constant__ MlpAdam o) {

@@ -19,8 +19,17 @@ struct MlpTrainState {
   float z_shift, z_scale;
 };
 
+// One CTA's gradient sums, in this order: gW1 [64][16], gW2 [64][64], gW3 [2][64], gb1,
+// gb2, gb3 [16].  Each CTA of a step writes its own block; k_mlp_reduce adds the blocks in
+// CTA order into the gradient accumulators, so a step's gradient does not depend on the
+// order in which its CTAs finish.
+constexpr int kGradW1 = 0, kGradW2 = kGradW1 + kMlpHid * kMlpIn, kGradW3 = kGradW2 + kMlpHid * kMlpHid,
+              kGradB1 = kGradW3 + 2 * kMlpHid, kGradB2 = kGradB1 + kMlpHid, kGradB3 = kGradB2 + kMlpHid,
+              kGradCount = kGradB3 + 16;
+
 struct MlpTrainArgs {
   MlpTrainState W;
+  float *part;      // [CTAs of the step][kGradCount], zeroed once (entries no CTA writes stay 0)
   const float *X;   // [n][kMlpIn] raw features
   const float *Y;   // [n][2] raw targets
   const int *perm;  // sample order (may be null)
@@ -34,6 +43,7 @@ struct MlpAdam {
 };
 
 __global__ void k_mlp_step(const __grid_constant__ MlpTrainArgs a);
+__global__ void k_mlp_reduce(const __grid_constant__ MlpTrainArgs a, int ctas);
 __global__ void k_mlp_adam(const __grid_constant__ MlpTrainArgs a, const __grid_constant__ MlpAdam o);
 __global__ void k_mlp_pack(const __grid_constant__ MlpTrainArgs a);
 __global__ void k_mlp_predict(const __grid_constant__ MlpTrainArgs a, float *Yp);
